@@ -1,0 +1,274 @@
+/*
+ * trekis_gb300.h -- C ABI of the GB300 (sm_103a) Monte Carlo track loop.
+ *
+ * The reference program (TREKIS-3, Fortran-90) runs one swift-heavy-ion (SHI)
+ * passage per Monte Carlo iteration through `do_Monte_Carlo`
+ * (Source_files/Monte_Carlo.f90:39-44), after building its FP64 cross-section
+ * tables in `Analytical_ion_dEdx` / `Analytical_electron_dEdx`
+ * (Source_files/Analytical_IMFPs.f90:2242, :100) and the SHI transfer table in
+ * Universal_MC_for_SHI_MAIN.f90:231-238.  This header is the drop-in boundary
+ * for exactly that path: plain C structs, plain pointers and sizes, no
+ * Fortran derived types and no torch types.
+ *
+ * Conventions
+ *  - Units follow the reference: energies eV, lengths Angstrom, times fs,
+ *    masses of atoms/ions in proton masses, hole mass in electron masses.
+ *  - Shell/atom indices are 0-based here (the reference is 1-based).
+ *  - Tally arrays are column-major with the time index fastest, exactly as
+ *    the Fortran arrays `Out_ne(i_t, j_R)` etc. (Sorting_output_data.f90:1144).
+ *  - The callee ACCUMULATES (+=) un-normalised sums into caller-owned tally
+ *    arrays; the caller divides by NMC (Universal_MC_for_SHI_MAIN.f90:281-314).
+ *  - Every entry point returns 0 on success or a negative TREKIS_E* code; a
+ *    `trekis_status` (may be NULL) receives error bits and counters.
+ *  - The library has no CPU fallback: without a usable sm_103a device every
+ *    compute entry point returns TREKIS_ENODEVICE.
+ */
+#ifndef TREKIS_GB300_H
+#define TREKIS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TREKIS_ABI_VERSION 1
+
+#define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
+#define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
+#define TREKIS_MAX_OSC     16  /* Ritchie-Howie oscillators per shell          */
+#define TREKIS_MAX_PH_OSC  8   /* oscillators of the phonon loss function      */
+
+/* return codes */
+#define TREKIS_OK            0
+#define TREKIS_EINVAL       -1  /* bad argument / inconsistent sizes          */
+#define TREKIS_ENODEVICE    -2  /* no CUDA device or not sm_103a               */
+#define TREKIS_ECUDA        -3  /* a CUDA call failed                          */
+#define TREKIS_ENOMEM       -4  /* device allocation failed                    */
+#define TREKIS_EOVERFLOW    -5  /* particle queue capacity exceeded            */
+#define TREKIS_ETIMEOUT     -6  /* a bounded device wait ran out               */
+#define TREKIS_EUNSUPPORTED -7  /* option not implemented on this path         */
+
+/* error bits in trekis_status.error_bits (reference error numbers in brackets) */
+#define TREKIS_ERR_NEG_ENERGY_E   (1u << 0)  /* electron got negative energy [20-23,40,50] */
+#define TREKIS_ERR_NEG_ENERGY_H   (1u << 1)  /* hole got negative energy [20,41,51]         */
+#define TREKIS_ERR_HOLE_IN_GAP    (1u << 2)  /* hole energy inside the gap [41,52]          */
+#define TREKIS_ERR_AUGER          (1u << 3)  /* impossible Auger decay [25]                 */
+#define TREKIS_ERR_NEG_TRANSFER   (1u << 4)  /* transferred energy below ionisation [10]   */
+#define TREKIS_ERR_NAN            (1u << 5)  /* NaN met in kinematics                       */
+#define TREKIS_ERR_QUEUE_FULL     (1u << 6)  /* particle queue overflow (run aborted)       */
+#define TREKIS_ERR_PHOTON_ENERGY  (1u << 7)  /* photon got negative energy [30]             */
+
+/* One kind of atom: mirrors `type(Atom)` (Source_files/Objects.f90:257-275). */
+typedef struct {
+    int32_t Zat;                      /* atomic number                              */
+    int32_t N_shl;                    /* number of shells                           */
+    double  Mass;                     /* [proton masses]                            */
+    double  Pers;                     /* atoms of this kind per formula unit        */
+    int32_t Shl_num[TREKIS_MAX_SHELLS];   /* EADL designator (>=63: valence band)   */
+    int32_t KOCS[TREKIS_MAX_SHELLS];      /* electron CS kind: 1 = CDF              */
+    int32_t KOCS_SHI[TREKIS_MAX_SHELLS];  /* SHI/photon CS kind: 1 = CDF            */
+    int32_t N_osc[TREKIS_MAX_SHELLS];     /* Ritchie-Howie oscillators per shell    */
+    double  Nel[TREKIS_MAX_SHELLS];       /* electrons in the shell                 */
+    double  Ip[TREKIS_MAX_SHELLS];        /* [eV] ionisation potential              */
+    double  Auger[TREKIS_MAX_SHELLS];     /* [fs] Auger decay time                  */
+    double  Radiat[TREKIS_MAX_SHELLS];    /* [fs] radiative decay time              */
+    double  E0[TREKIS_MAX_SHELLS][TREKIS_MAX_OSC];    /* [eV] oscillator energy    */
+    double  A[TREKIS_MAX_SHELLS][TREKIS_MAX_OSC];     /* oscillator amplitude      */
+    double  Gamma[TREKIS_MAX_SHELLS][TREKIS_MAX_OSC]; /* [eV] oscillator width     */
+} trekis_atom;
+
+/* Target: mirrors `type(Solid)`, `type(Density_of_states)`, the phonon
+ * `type(CDF)` and the flags of `type(Flag)` used on the path
+ * (Source_files/Objects.f90:86-167). */
+typedef struct {
+    int32_t     N_atoms;
+    trekis_atom atoms[TREKIS_MAX_ATOMS];  /* the valence band is the last shell of atoms[0] */
+    double Dens;          /* [g/cm^3]                                     */
+    double At_Dens;       /* [1/cm^3] atomic density                      */
+    double Vsound;        /* [m/s]                                        */
+    double E_F;           /* [eV]                                         */
+    double Egap;          /* [eV]                                         */
+    double Layer;         /* [A] thickness of the analysed layer          */
+    double N_VB_el;       /* valence electrons per formula unit           */
+    double work_function; /* [eV] (<=0: no emission)                      */
+    double bar_length;    /* [A]                                          */
+    double bar_height;    /* [eV]                                         */
+    double hole_mass;     /* [me] valence-hole mass (>=1e3: immobile; <0: from DOS) */
+    double El_eff_mass;   /* [me] electron mass in the dispersion (0: from DOS) */
+    double cut_off;       /* [eV] electron/VB-hole cut-off                */
+    double temp;          /* [K] target temperature                       */
+    double v_f;           /* Fermi velocity as the reference defines it   */
+    /* phonon loss function (elastic kind 1) */
+    int32_t N_ph_osc;
+    double  ph_E0[TREKIS_MAX_PH_OSC];
+    double  ph_A[TREKIS_MAX_PH_OSC];
+    double  ph_Gamma[TREKIS_MAX_PH_OSC];
+    /* valence-band DOS on its 0.1 eV grid (Reading_files_and_parameters.f90:2317-2454);
+     * N_dos == 0 treats the valence band as an atomic level */
+    int32_t       N_dos;
+    const double* dos_E;      /* [eV] increasing, from the top of the band  */
+    const double* dos_DOS;    /* [1/eV]                                     */
+    const double* dos_int;    /* integrated DOS                             */
+    const double* dos_k;      /* [1/m]                                      */
+    const double* dos_Eff_m;  /* [me]                                       */
+    /* flags */
+    int32_t kind_of_EMFP;     /* 0 = Mott atomic elastic, 1 = phonon CDF      */
+    int32_t CDF_elast_Zeff;   /* target effective charge in the phonon CS     */
+    int32_t kind_of_DR;       /* 1 free electron, 2 plasmon pole, 3 Ritchie   */
+    int32_t plasmon_Emax;     /* 1: plasmon energy as upper limit            */
+    int32_t include_photons;  /* 1: radiative decay and photon transport     */
+} trekis_material;
+
+/* The projectile: mirrors `type(Ion)` (Source_files/Objects.f90:44-53). */
+typedef struct {
+    int32_t Zat;
+    int32_t Kind_Zeff;    /* 0 Barkas, 1 Bohr, 2 Nikolaev-Dmitriev, 3 Schiwietz-Grande, 4 fixed */
+    int32_t Kind_ion;     /* 0 point charge (1 Brandt-Kitagawa: unsupported) */
+    int32_t pad_;
+    double  Mass;         /* [proton masses]                              */
+    double  E;            /* [eV] initial kinetic energy                  */
+    double  fixed_Zeff;
+} trekis_ion;
+
+/* Table build options. */
+typedef struct {
+    int32_t build_shi;          /* 1: SHI per-shell tables + transfer rows    */
+    int32_t build_photon;       /* 1: photon absorption tables                */
+    double  shi_E_window_lo;    /* [eV] SHI grid rows below this are skipped (<=0: all) */
+    double  shi_E_window_hi;    /* [eV] SHI grid rows above this are skipped (<=0: all) */
+} trekis_table_cfg;
+
+/* Opaque table set (device-resident FP64 + FP32 copies, host FP64 mirror). */
+typedef struct trekis_tables trekis_tables;
+
+/* Run configuration of one do_Monte_Carlo call. */
+typedef struct {
+    int32_t NMC;                /* MC iterations                                 */
+    int32_t dt_flag;            /* 0 linear time grid, 1 logarithmic             */
+    double  Tim;                /* [fs] total time                               */
+    double  dt;                 /* [fs] time step (log grid: ratio)              */
+    int32_t N_R;                /* radial bins                                   */
+    int32_t precision;          /* 0: FP32 kinematics (default), 1: FP64         */
+    const double* Out_R;        /* [A] N_R outer radii of the cylindrical bins   */
+    uint64_t seed;              /* Philox key                                    */
+    int64_t  iteration_offset;  /* global index of the first iteration (shards)  */
+    /* scheduler knobs; 0 selects the tuned default */
+    int32_t  block_size;
+    int32_t  events_per_step;   /* events a thread runs before re-queueing       */
+    int64_t  queue_capacity;    /* particles per queue buffer                    */
+    int32_t  iterations_per_batch;
+    int32_t  use_graph;         /* capture the wavefront loop in a CUDA graph    */
+} trekis_run_cfg;
+
+/* Caller-owned tally arrays (un-normalised, accumulated with +=).  Any
+ * pointer may be NULL to skip that output.  Nt is the number of time-grid
+ * points (ceil(Tim/dt) for the linear grid), N_R the radial bins, Nat the
+ * kinds of atoms and Nshl the largest shell count. */
+typedef struct {
+    int32_t Nt, N_R, Nat, Nshl;
+    double* Out_ne;        /* [Nt*N_R] electron density       1/A^3 */
+    double* Out_Ee;        /* [Nt*N_R] electron energy density eV/A^3 */
+    double* Out_nphot;     /* [Nt*N_R]                                 */
+    double* Out_Ephot;     /* [Nt*N_R]                                 */
+    double* Out_Elat;      /* [Nt*N_R] lattice energy deposited in the interval */
+    double* Out_nh;        /* [Nt*N_R*Nat*Nshl]                        */
+    double* Out_Eh;        /* [Nt*N_R*Nat*Nshl]                        */
+    double* Out_Ehkin;     /* [Nt*N_R*Nat*Nshl]                        */
+    double* Out_tot_Ne;    /* [Nt]                                     */
+    double* Out_tot_Nphot; /* [Nt]                                     */
+    double* Out_tot_E;     /* [Nt]                                     */
+    double* Out_E_e;       /* [Nt]                                     */
+    double* Out_E_phot;    /* [Nt]                                     */
+    double* Out_E_at;      /* [Nt]                                     */
+    double* Out_E_h;       /* [Nt*Nat*Nshl]                            */
+} trekis_tallies;
+
+/* Counters and error record. */
+typedef struct {
+    int32_t  code;             /* last return code                              */
+    uint32_t error_bits;       /* TREKIS_ERR_* bits seen                        */
+    int64_t  first_offender;   /* iteration of the first error, -1 if none      */
+    uint64_t n_events;         /* collision events (all kinds)                  */
+    uint64_t n_shi;            /* SHI collisions                                */
+    uint64_t n_el_inelastic;   /* electron impact ionisations                   */
+    uint64_t n_el_elastic;     /* electron elastic collisions                   */
+    uint64_t n_hole_events;    /* VB-hole collisions                            */
+    uint64_t n_auger;          /* Auger decays                                  */
+    uint64_t n_radiative;      /* radiative decays                              */
+    uint64_t n_photon_abs;     /* photo-absorptions                             */
+    uint64_t n_particles;      /* electrons + holes + photons created           */
+    uint64_t n_steps;          /* wavefront steps                               */
+    double   device_ms;        /* device time of the MC (CUDA events)           */
+    uint64_t n_kernel_launches;/* kernels launched by the call                  */
+} trekis_status;
+
+/* ---- entry points ------------------------------------------------------ */
+
+int32_t trekis_abi_version(void);
+
+/* Is an sm_103a device usable?  Returns 1 if yes, 0 if not. */
+int32_t trekis_device_ok(void);
+
+/* Build every FP64 table the MC reads, on the GPU.  Replaces
+ * Analytical_ion_dEdx (Analytical_IMFPs.f90:2242), Analytical_electron_dEdx
+ * for electrons, holes and photons (Analytical_IMFPs.f90:100, called from
+ * Universal_MC_for_SHI_MAIN.f90:184-198) and the SHI transfer table
+ * SHI_TotIMFP(..., dSedE) (Universal_MC_for_SHI_MAIN.f90:231-238). */
+int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion,
+                            const trekis_table_cfg* cfg, trekis_tables** out,
+                            trekis_status* st);
+
+void trekis_tables_free(trekis_tables* t);
+
+/* Table kinds for the export functions. */
+#define TREKIS_TAB_EL_INEL   0  /* electron IMFP per shell   (Total_el_MFPs)    */
+#define TREKIS_TAB_EL_ELAST  1  /* electron EMFP             (Elastic_MFP%Total)*/
+#define TREKIS_TAB_H_INEL    2  /* hole IMFP per shell       (Total_Hole_MFPs)  */
+#define TREKIS_TAB_H_ELAST   3  /* hole EMFP                 (Elastic_Hole_MFP) */
+#define TREKIS_TAB_PHOT      4  /* photon IMFP per shell     (Total_Photon_MFPs)*/
+#define TREKIS_TAB_SHI       5  /* SHI IMFP per shell        (SHI_MFP)          */
+#define TREKIS_TAB_SHI_DSDE  6  /* SHI transfer row per shell (diff_SHI_MFP)    */
+
+/* Size of a table: number of energy nodes (TAB_*), or of row entries. */
+int32_t trekis_tables_size(const trekis_tables* t, int32_t kind, int32_t atom,
+                           int32_t shell, int64_t* n);
+
+/* Copy one table out: E[n], L[n] (mean free path), dEdx[n] (any may be NULL). */
+int32_t trekis_tables_export(const trekis_tables* t, int32_t kind, int32_t atom,
+                             int32_t shell, double* E, double* L, double* dEdx,
+                             int64_t cap);
+
+/* Row kinds of integrated differential cross sections (`type(All_diff_CS)`,
+ * Objects.f90:246-251). */
+#define TREKIS_ROW_EL_INEL 0   /* aidCS%EIdCS(atom)%Int_diff_CS(shell) */
+#define TREKIS_ROW_H_INEL  1   /* aidCS%HIdCS (valence band)          */
+#define TREKIS_ROW_EL_ELAST 2  /* aidCS%EEdCS (phonon elastic)        */
+
+/* Copy the cumulative row at energy node iE: hw[n] and the MFP column dsdhw[n]. */
+int32_t trekis_tables_row(const trekis_tables* t, int32_t kind, int32_t atom,
+                          int32_t shell, int32_t iE, double* hw, double* dsdhw,
+                          int64_t cap, int64_t* n);
+
+/* One call of the track loop: NMC iterations of SHI passage + cascade,
+ * tallies accumulated into `out`.  Replaces do_Monte_Carlo
+ * (Monte_Carlo.f90:39-419); each iteration is Monte_Carlo_modelling
+ * (Monte_Carlo.f90:427-679). */
+int32_t trekis_mc_run(const trekis_tables* t, const trekis_material* mat,
+                      const trekis_ion* ion, const trekis_run_cfg* cfg,
+                      trekis_tallies* out, trekis_status* st);
+
+/* Same as trekis_mc_run with host tally arrays already on the device:
+ * `dev_out` members are device pointers (accumulated with +=).  Used to time
+ * the track loop with resident data. */
+int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
+                             const trekis_ion* ion, const trekis_run_cfg* cfg,
+                             trekis_tallies* dev_out, trekis_status* st);
+
+/* Human-readable text of the last error on this thread. */
+const char* trekis_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TREKIS_GB300_H */
