@@ -375,6 +375,8 @@ void shi_event(Ctx& c, int i) {
         const int N = (int)D.L.size();
         double RN = s.next();
         double Ecur = m.atoms[A].Ip[S];
+        if (N < 1) { dE = Ecur; goto transferred; }  // shell beyond the SHI's maximum transfer
+        {
         int Mt = find_monoton(D.E.data(), N, m.atoms[A].Ip[S]);
         double dL;
         if (Mt > 1) dL = (D.L[Mt - 2] > 1.0e-10) ? interp(5, D.E[Mt - 2], D.E[Mt - 1], D.L[Mt - 2], D.L[Mt - 1], Ecur)
@@ -386,7 +388,9 @@ void shi_event(Ctx& c, int i) {
         else nt = Mt;
         if (nt > Mt) dE = interp(5, 1.0 / D.L[nt - 2], 1.0 / D.L[nt - 1], D.E[nt - 2], D.E[nt - 1], Tot);
         else dE = m.atoms[A].Ip[S];
+        }
     }
+transferred:
     double L_new = next_free_path_2d(c.T->SHI_path, c.shi.E);
     double RN = s.next();
     L_new = -L_new * std::log(RN);

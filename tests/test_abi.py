@@ -1,0 +1,81 @@
+"""CPU tests of the C-ABI boundary: the library builds for sm_103a, loads,
+exports every symbol the header declares, the ctypes mirrors have the C
+layout, and compute entry points refuse to run without a GPU (no fallback)."""
+import ctypes as C
+import pathlib
+import re
+import subprocess
+
+import pytest
+
+from trekis import abi, build
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+HDR = ROOT / "include" / "trekis_gb300.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build_library()
+    return C.CDLL(str(build.LIB))
+
+
+def declared_symbols():
+    txt = HDR.read_text()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(trekis_\w+)\s*\(", txt, re.M)))
+
+
+def test_header_declares_the_path():
+    syms = declared_symbols()
+    for s in ("trekis_tables_build", "trekis_mc_run", "trekis_mc_run_device", "trekis_tables_export",
+              "trekis_tables_row", "trekis_device_ok"):
+        assert s in syms
+
+
+def test_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(build.LIB)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT\s+(trekis_\w+)", out))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    assert set(declared_symbols()) <= set(abi.SIGNATURES)
+
+
+def test_struct_layout_matches_c(tmp_path):
+    src = tmp_path / "sz.c"
+    names = {"trekis_atom": abi.Atom, "trekis_material": abi.Material, "trekis_ion": abi.Ion,
+             "trekis_table_cfg": abi.TableCfg, "trekis_run_cfg": abi.RunCfg, "trekis_tallies": abi.Tallies,
+             "trekis_status": abi.Status}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HDR}"', "int main(void){"]
+    for cn in names:
+        lines.append(f'printf("{cn} %zu\\n", sizeof({cn}));')
+    lines.append('printf("off_N_dos %zu\\n", offsetof(trekis_material, N_dos));')
+    lines.append('printf("off_include_photons %zu\\n", offsetof(trekis_material, include_photons));')
+    lines.append('printf("off_seed %zu\\n", offsetof(trekis_run_cfg, seed));')
+    lines.append("return 0;}")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sz"
+    subprocess.run(["gcc", "-o", str(exe), str(src)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
+    for cn, py in names.items():
+        assert int(got[cn]) == C.sizeof(py), cn
+    assert int(got["off_N_dos"]) == abi.Material.N_dos.offset
+    assert int(got["off_include_photons"]) == abi.Material.include_photons.offset
+    assert int(got["off_seed"]) == abi.RunCfg.seed.offset
+
+
+def test_no_cpu_fallback(lib):
+    """Without a usable sm_103a device the compute entry points fail loudly."""
+    l = abi.load()
+    if l.trekis_device_ok():
+        pytest.skip("a GPU is present; this checks the GPU-less path")
+    from trekis import configs
+    w = configs.small(configs.cfg0)
+    h = w.material.to_c()
+    from trekis import api
+    ion = api.ion_struct(w)
+    tc = abi.TableCfg(build_shi=1)
+    out = C.c_void_p()
+    st = abi.Status.fresh()
+    rc = l.trekis_tables_build(h.ref(), C.byref(ion), C.byref(tc), C.byref(out), C.byref(st))
+    assert rc == -2 and st.code == -2
+    assert b"sm_103a" in l.trekis_last_error()

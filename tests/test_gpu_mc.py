@@ -1,0 +1,177 @@
+"""GPU track loop against the oracle.
+
+* FP64 mode on identical tables and identical Philox streams: every tally
+  equals the oracle's chronological loop to the fixed-point resolution
+  (2^-24 eV per particle energy, 2^-40 eV per lattice deposit).
+* FP32 mode: radial electron density and energy density agree with the FP64
+  oracle within 3 combined standard errors in >= 97 % of the populated
+  (time, radius) bins (batch-means errors over independent seeds).
+* Scheduling knobs (events per step, block size) do not change a single bit;
+  batch sizes only change the order of the FP64 batch sums.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import copy_tables
+from trekis import abi, api, configs
+
+
+def _oracle_on(t, w):
+    import oracle_py
+    tc = abi.TableCfg(build_shi=1, build_photon=w.material.include_photons,
+                      shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+    o = oracle_py.OracleTables(t.mat, t.ion, tc)
+    copy_tables(t, o, w)
+    return o
+
+
+def _oracle_run(o, w, opt, NMC=None):
+    tal = api.new_tallies(w)
+    cfg, _R = api.run_cfg(w, opt, NMC)
+    st = abi.Status.fresh()
+    o.mc_run(cfg, tal, st)
+    return tal, st
+
+
+@pytest.fixture(scope="module")
+def small0(gpu_lib):
+    w = configs.small(configs.cfg0, NMC=6)
+    t = api.Tables(w, lib=gpu_lib)
+    return w, t, _oracle_on(t, w)
+
+
+@pytest.fixture(scope="module")
+def small1(gpu_lib):
+    # mobile valence holes, radiative decay and photon transport
+    w = configs.small(configs.cfg1, NMC=6, Tim=30.0)
+    for atom in w.material.atoms:        # shorten radiative times so photons appear in a short run
+        for sh in atom.shells:
+            if sh.designator < 63:
+                sh.Radiat = sh.Auger * 2.0
+    t = api.Tables(w, lib=gpu_lib)
+    return w, t, _oracle_on(t, w)
+
+
+def _assert_tallies_equal(g, r, what):
+    for k in g.a:
+        a, b = g[k], r[k]
+        tol = 1e-6 * np.abs(b) + 1e-9 * (np.max(np.abs(b)) + 1e-300)
+        bad = np.abs(a - b) > tol
+        assert not np.any(bad), f"{what} {k}: {np.sum(bad)} cells differ, max {np.max(np.abs(a - b)):.3e}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["small0", "small1"])
+def test_fp64_matches_oracle(case, request):
+    w, t, o = request.getfixturevalue(case)
+    opt = api.RunOptions(precision=1, seed=11)
+    g, sg = api.mc_run(t, opt)
+    r, sr = _oracle_run(o, w, opt)
+    assert sg.n_events == sr.n_events > 0
+    for f in ("n_shi", "n_el_inelastic", "n_el_elastic", "n_hole_events", "n_auger", "n_radiative", "n_photon_abs"):
+        assert getattr(sg, f) == getattr(sr, f), f
+    assert sg.error_bits == sr.error_bits
+    _assert_tallies_equal(g, r, case)
+    if case == "small1":
+        assert sg.n_hole_events > 0 and sg.n_radiative > 0 and sg.n_photon_abs > 0
+
+
+@pytest.mark.gpu
+def test_scheduling_invariance_bit_exact(small1):
+    w, t, _o = small1
+    ref, _ = api.mc_run(t, api.RunOptions(seed=5, iterations_per_batch=3))
+    for K, bs in ((1, 64), (7, 128), (200, 256)):
+        g, st = api.mc_run(t, api.RunOptions(seed=5, iterations_per_batch=3, events_per_step=K, block_size=bs))
+        for k in g.a:
+            assert np.array_equal(g[k], ref[k]), (K, bs, k)
+    # another batching: same int64 sums, FP64 batch-sum order differs
+    g, _ = api.mc_run(t, api.RunOptions(seed=5, iterations_per_batch=1))
+    for k in g.a:
+        assert np.allclose(g[k], ref[k], rtol=1e-12, atol=0), k
+
+
+@pytest.mark.gpu
+def test_run_to_run_determinism(small0):
+    w, t, _o = small0
+    a, _ = api.mc_run(t, api.RunOptions(seed=9))
+    b, _ = api.mc_run(t, api.RunOptions(seed=9))
+    for k in a.a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.gpu
+def test_energy_conservation_fp32(small1):
+    w, t, _o = small1
+    g, st = api.mc_run(t, api.RunOptions(seed=2))
+    tot = g["Out_tot_E"]
+    assert tot[0] > 0
+    assert np.max(np.abs(tot - tot[0])) / tot[0] < 1e-6
+
+
+@pytest.mark.gpu
+def test_shards_sum(small0):
+    w, t, _o = small0
+    full, _ = api.mc_run(t, api.RunOptions(seed=4), NMC=6)
+    a, _ = api.mc_run(t, api.RunOptions(seed=4, iteration_offset=0), NMC=2)
+    b, _ = api.mc_run(t, api.RunOptions(seed=4, iteration_offset=2), NMC=4)
+    for k in full.a:
+        assert np.allclose(full[k], a[k] + b[k], rtol=1e-12, atol=0), k
+
+
+@pytest.mark.gpu
+def test_fp32_statistically_equal_to_oracle(gpu_lib):
+    """3-sigma agreement of Out_ne / Out_Ee between FP32 GPU and FP64 oracle,
+    independent seeds, batch-means standard errors."""
+    w = configs.small(configs.cfg0, NMC=4, layer=10.0, Tim=20.0)
+    t = api.Tables(w, lib=gpu_lib)
+    o = _oracle_on(t, w)
+    nb = 16
+    G = {k: [] for k in ("Out_ne", "Out_Ee")}
+    R = {k: [] for k in ("Out_ne", "Out_Ee")}
+    for b in range(nb):
+        g, _ = api.mc_run(t, api.RunOptions(seed=1000 + b))
+        r, _ = _oracle_run(o, w, api.RunOptions(precision=1, seed=5000 + b))
+        for k in G:
+            G[k].append(g[k] / w.NMC)
+            R[k].append(r[k] / w.NMC)
+    for k in G:
+        g, r = np.array(G[k]), np.array(R[k])
+        mg, mr = g.mean(0), r.mean(0)
+        se = np.sqrt(g.var(0, ddof=1) / nb + r.var(0, ddof=1) / nb)
+        live = se > 1e-12 * np.max(np.abs(mr))
+        frac = np.mean(np.abs(mg[live] - mr[live]) <= 3 * se[live])
+        assert live.sum() > 100
+        assert frac >= 0.97, (k, frac)
+
+
+@pytest.mark.gpu
+def test_queue_overflow_recovers(small0):
+    w, t, _o = small0
+    ref, _ = api.mc_run(t, api.RunOptions(seed=6, iterations_per_batch=1))
+    # capacity below one batch: the driver shrinks the batch and retries
+    g, st = api.mc_run(t, api.RunOptions(seed=6, iterations_per_batch=6, queue_capacity=4000))
+    for k in g.a:
+        assert np.allclose(g[k], ref[k], rtol=1e-12, atol=0), k
+    # capacity below one iteration: a clean error, and the device stays usable
+    with pytest.raises(RuntimeError, match="overflow"):
+        api.mc_run(t, api.RunOptions(seed=6, queue_capacity=64))
+    again, _ = api.mc_run(t, api.RunOptions(seed=6, iterations_per_batch=1))
+    for k in again.a:
+        assert np.array_equal(again[k], ref[k])
+
+
+@pytest.mark.gpu
+def test_invalid_arguments(small0, gpu_lib):
+    w, t, _o = small0
+    tal = api.new_tallies(w)
+    cfg, R = api.run_cfg(w, api.RunOptions())
+    cfg.N_R = 0
+    st = abi.Status.fresh()
+    rc = gpu_lib.trekis_mc_run(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(tal.c()), C.byref(st))
+    assert rc == -1
+    bad = api.TallySet(tal.Nt + 1, tal.NR, tal.Nat, tal.Nshl)
+    cfg, R = api.run_cfg(w, api.RunOptions())
+    rc = gpu_lib.trekis_mc_run(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(bad.c()), C.byref(st))
+    assert rc == -1

@@ -1,0 +1,93 @@
+"""GPU FP64 table build against the oracle's FP64 restatement (tolerance 1e-6
+relative, the bound the track-loop specification sets for tables)."""
+import numpy as np
+import pytest
+
+from trekis import abi, api, configs
+
+RTOL = 1e-6
+
+
+def _close(a, b, rtol=RTOL):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    return np.all(np.abs(a - b) <= rtol * np.abs(b) + 1e-300)
+
+
+@pytest.fixture(scope="module", params=["cfg0", "cfg1"])
+def pair(request, gpu_lib):
+    import oracle_py
+    w = configs.cfg0() if request.param == "cfg0" else configs.cfg1(NMC=1)
+    t = api.Tables(w, lib=gpu_lib)
+    tc = abi.TableCfg(build_shi=1, build_photon=w.material.include_photons,
+                      shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+    o = oracle_py.OracleTables(t.mat, t.ion, tc)
+    return w, t, o
+
+
+@pytest.mark.gpu
+def test_inelastic_mfp_and_stopping(pair):
+    w, t, o = pair
+    for a, atom in enumerate(w.material.atoms):
+        for s in range(len(atom.shells)):
+            for kind in (abi.TAB_EL_INEL, abi.TAB_H_INEL):
+                E1, L1, D1 = t.export(kind, a, s)
+                E2, L2, D2 = o.export(kind, a, s)
+                assert np.array_equal(E1, E2)
+                assert _close(L1, L2), (kind, a, s)
+                assert _close(D1, D2), (kind, a, s)
+
+
+@pytest.mark.gpu
+def test_cumulative_rows(pair):
+    w, t, o = pair
+    for a, atom in enumerate(w.material.atoms):
+        for s in range(len(atom.shells)):
+            E, _L, _D = t.export(abi.TAB_EL_INEL, a, s)
+            for i in range(0, len(E), 3):
+                hw1, L1 = t.row(abi.ROW_EL_INEL, a, s, i)
+                hw2, L2 = o.row(abi.ROW_EL_INEL, a, s, i)
+                assert len(hw1) == len(hw2) >= 10
+                assert _close(hw1, hw2, 1e-12) and _close(L1, L2), (a, s, i)
+                if len(L1) > 1:
+                    body = L1[hw1 > 0]
+                    assert np.all(np.diff(body) <= 0)   # cumulative MFP decreases (CS:1021-1037)
+    E, _L, _D = t.export(abi.TAB_H_INEL, 0, 0)
+    for i in range(len(E)):
+        hw1, L1 = t.row(abi.ROW_H_INEL, 0, 0, i)
+        hw2, L2 = o.row(abi.ROW_H_INEL, 0, 0, i)
+        assert _close(hw1, hw2, 1e-12) and _close(L1, L2)
+
+
+@pytest.mark.gpu
+def test_elastic_photon_and_ion_tables(pair):
+    w, t, o = pair
+    for kind in (abi.TAB_EL_ELAST, abi.TAB_H_ELAST):
+        E1, L1, _ = t.export(kind)
+        E2, L2, _ = o.export(kind)
+        assert np.array_equal(E1, E2) and _close(L1, L2)
+    for a, atom in enumerate(w.material.atoms):
+        for s in range(len(atom.shells)):
+            E1, L1, D1 = t.export(abi.TAB_SHI, a, s)
+            E2, L2, D2 = o.export(abi.TAB_SHI, a, s)
+            assert np.array_equal(E1, E2) and _close(L1, L2) and _close(D1, D2)
+            E1, L1, D1 = t.export(abi.TAB_SHI_DSDE, a, s)
+            E2, L2, D2 = o.export(abi.TAB_SHI_DSDE, a, s)
+            assert _close(E1, E2, 1e-12) and _close(L1, L2) and _close(D1, D2)
+            if w.material.include_photons:
+                E1, L1, _ = t.export(abi.TAB_PHOT, a, s)
+                E2, L2, _ = o.export(abi.TAB_PHOT, a, s)
+                assert np.array_equal(E1, E2) and _close(L1, L2)
+
+
+@pytest.mark.gpu
+def test_mfp_physical(pair):
+    """Positive, finite IMFPs above threshold; infinite below (TotIMFP CS:1010)."""
+    w, t, _o = pair
+    for a, atom in enumerate(w.material.atoms):
+        for s, sh in enumerate(atom.shells):
+            E, L, _ = t.export(abi.TAB_EL_INEL, a, s)
+            assert np.all(L > 0)
+            assert np.all(L[E < sh.Ip] >= 1e20)
+            above = E > 2 * sh.Ip + 1
+            assert np.all(L[above] < 1e20)

@@ -1,0 +1,190 @@
+"""CPU tests of the FP64 oracle: known answers, invariants of the reference's
+algorithm (energy conservation, order independence) and edge cases."""
+import ctypes as C
+
+import numpy as np
+import pytest
+from scipy import integrate
+
+from trekis import abi, api, configs, material
+
+
+def _philox(lib, ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib.oracle_philox(c, k, o)
+    return list(o)
+
+
+def test_philox_known_answers(oracle_lib):
+    # Random123 philox4x32-10 known-answer vectors (Salmon et al., SC'11)
+    assert _philox(oracle_lib, [0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert _philox(oracle_lib, [0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert _philox(oracle_lib, [0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_child_ids_distinct(oracle_lib):
+    ids = {oracle_lib.oracle_child_pid(oracle_lib.oracle_shi_pid(it), o, s)
+           for it in range(4) for o in range(200) for s in range(3)}
+    assert len(ids) == 4 * 200 * 3
+
+
+def _grid(lib, mat, lo, hi):
+    h = mat.to_c()
+    out = np.zeros(20000)
+    n = C.c_int64()
+    assert lib.oracle_grid(C.addressof(h.struct), lo, hi, out.ctypes.data_as(C.POINTER(C.c_double)), 20000, C.byref(n)) == 0
+    return out[:n.value]
+
+
+def test_energy_grid_shape(oracle_lib):
+    w = configs.cfg0()
+    g = _grid(oracle_lib, w.material, 0.1, 175.6e6 * 2.0 / 1836.0)
+    assert np.all(np.diff(g) > 0)
+    assert abs(g[0] - 0.1) < 1e-12
+    # every ionisation potential is bracketed by +-1e-3 eV points (go_thru_grid, Analytical_IMFPs.f90:2911-2939)
+    for ip in (6.7, 73.0, 118.0, 543.0):
+        assert np.any(np.abs(g - (ip - 1e-3)) < 1e-9) and np.any(np.abs(g - (ip + 1e-3)) < 1e-9)
+    assert 400 < len(g) < 600
+
+
+def test_time_grid(oracle_lib):
+    out = np.zeros(4000)
+    n = C.c_int64()
+    oracle_lib.oracle_time_grid(100.0, 1.0, 0, out.ctypes.data_as(C.POINTER(C.c_double)), 4000, C.byref(n))
+    assert n.value == 100 and out[0] == 1.0 and out[n.value - 1] == 100.0
+    assert api.n_time_points(100.0, 1.0) == list(out[:n.value])
+    oracle_lib.oracle_time_grid(1000.0, 2.0, 1, out.ctypes.data_as(C.POINTER(C.c_double)), 4000, C.byref(n))
+    assert api.n_time_points(1000.0, 2.0, 1) == list(out[:n.value])
+
+
+def test_sumrule_closed_form_against_quadrature(oracle_lib):
+    """The k-sum closed form (Int_Ritchi_x, Cross_sections.f90:763) equals the
+    numerical integral of hw * Im(-1/eps) from Ip to infinity."""
+    w = configs.cfg0()
+    h = w.material.to_c()
+    for (A, E0, G, xmin) in [(500.0, 25.0, 12.0, 6.7), (80.0, 40.0, 5.0, 6.7), (1.0, 128.0, 128.0, 118.0)]:
+        f = lambda x: x * oracle_lib.oracle_loss_func(C.addressof(h.struct), A, E0, G, x, 0.0, 1)
+        num, _ = integrate.quad(f, xmin, np.inf, limit=400, epsabs=0, epsrel=1e-10)
+        ks, fs = C.c_double(), C.c_double()
+        arr = lambda v: (C.c_double * 1)(v)
+        # Omega chosen so that ksum = 2 e^2/(pi Omega hbar^2) * ne  ->  ne itself
+        om = 2.0 * material.G_E ** 2 / (np.pi * material.G_H ** 2)
+        oracle_lib.oracle_sumrules(arr(A), arr(E0), arr(G), 1, xmin, om, C.byref(ks), C.byref(fs))
+        assert abs(ks.value - num) / num < 1e-7
+        k2, _ = material.sumrules([A], [E0], [G], xmin, om)
+        assert abs(k2 - ks.value) / ks.value < 1e-12
+
+
+def test_vb_normalised_to_24_electrons():
+    w = configs.cfg0()
+    m = w.material
+    vb = m.atoms[0].shells[-1]
+    n_at_mol = sum(a.Pers for a in m.atoms)
+    ks, _ = material.sumrules(vb.A, vb.E0, vb.Gamma, vb.Ip, material.w_plasma(1e6 * m.At_Dens / n_at_mol))
+    assert abs(ks - 24.0) < 1e-9
+
+
+def test_dos_resampling():
+    w = configs.cfg0()
+    d = w.material.dos
+    assert len(d.E) == 200 and d.E[0] == 0.0 and np.all(np.diff(d.E) > 0)
+    assert abs(d.int_DOS[-1] - 24.0) < 1e-9
+    assert np.all(d.DOS >= 0) and np.all(np.isfinite(d.k))
+
+
+def test_mott_sampler_distribution():
+    """mu = (u(2nu+1)-nu)/(u+nu) (Mott_sample_mu, Cross_sections.f90:3573) inverts
+    the screened-Rutherford CDF of dsigma/dmu ~ 1/(1-mu+2nu)^2."""
+    nu = 0.37
+    u = np.linspace(0.01, 0.99, 9)
+    mu = (u * (2 * nu + 1) - nu) / (u + nu)
+    pdf = lambda m: 1.0 / (1.0 - m + 2 * nu) ** 2
+    tot, _ = integrate.quad(pdf, -1, 1)
+    cdf = np.array([integrate.quad(pdf, -1, m)[0] / tot for m in mu])
+    assert np.allclose(cdf, u, atol=1e-12)
+
+
+def _oracle_run(w, opt, nthreads=2, sched=1, NMC=None, table_cfg=None):
+    import oracle_py
+    h = w.material.to_c()
+    ion = api.ion_struct(w)
+    tc = table_cfg or abi.TableCfg(build_shi=1, build_photon=w.material.include_photons,
+                                   shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+    o = oracle_py.OracleTables(h, ion, tc, nthreads=nthreads)
+    tal = api.new_tallies(w)
+    cfg, _R = api.run_cfg(w, opt, NMC)
+    st = abi.Status.fresh()
+    o.mc_run(cfg, tal, st, nthreads=nthreads, sched=sched)
+    return tal, st
+
+
+@pytest.fixture(scope="module")
+def small_runs():
+    w = configs.small(configs.cfg0, NMC=4)
+    a, sa = _oracle_run(w, api.RunOptions(seed=3), sched=0, nthreads=1)
+    b, sb = _oracle_run(w, api.RunOptions(seed=3), sched=1, nthreads=3)
+    return w, a, sa, b, sb
+
+
+def test_order_independence(small_runs):
+    """The literal earliest-event scan and a heap give the same tallies: with
+    per-particle keyed streams the history does not depend on event order."""
+    w, a, sa, b, sb = small_runs
+    assert sa.n_events == sb.n_events > 0
+    for k in a.a:
+        assert np.allclose(a[k], b[k], rtol=1e-12, atol=1e-12 * (np.max(np.abs(a[k])) + 1e-300)), k
+
+
+def test_energy_conservation(small_runs):
+    """Out_tot_E is flat in time once the ion has left the layer (manual VI.5,
+    Monte_Carlo.f90:943-955): electrons + holes + lattice = deposited energy."""
+    w, a, sa, _b, _sb = small_runs
+    tot = a["Out_tot_E"]
+    assert tot[0] > 0
+    assert np.max(np.abs(tot - tot[0])) / tot[0] < 1e-12
+    parts = a["Out_E_e"] + a["Out_E_h"].reshape(-1, a.Nt).sum(0) + a["Out_E_at"]
+    assert np.allclose(parts, tot, rtol=1e-12)
+
+
+def test_counts_match_tallies(small_runs):
+    """Every electron is in exactly one radial bin at every grid time."""
+    w, a, _sa, _b, _sb = small_runs
+    V = 1.0 / (np.pi * w.material.Layer * np.diff(np.concatenate([[0.0], w.R_edges]) ** 2))
+    counts = (a.view("Out_ne") / V[None, :]).sum(1)
+    assert np.allclose(counts, a["Out_tot_Ne"], rtol=1e-9)
+
+
+def test_seed_changes_result():
+    w = configs.small(configs.cfg0, NMC=2)
+    a, _ = _oracle_run(w, api.RunOptions(seed=1))
+    b, _ = _oracle_run(w, api.RunOptions(seed=2))
+    assert not np.allclose(a["Out_ne"], b["Out_ne"])
+
+
+def test_iteration_shards_sum(oracle_lib):
+    """Iterations are keyed by their global index: two shards (offsets 0 and 2)
+    sum to the single run (the multi-GPU partition of the reference's MPI loop,
+    Monte_Carlo.f90:111-129)."""
+    w = configs.small(configs.cfg0, NMC=4)
+    full, _ = _oracle_run(w, api.RunOptions(seed=5), NMC=4)
+    p1, _ = _oracle_run(w, api.RunOptions(seed=5, iteration_offset=0), NMC=2)
+    p2, _ = _oracle_run(w, api.RunOptions(seed=5, iteration_offset=2), NMC=2)
+    for k in full.a:
+        assert np.allclose(full[k], p1[k] + p2[k], rtol=1e-12, atol=1e-300), k
+
+
+def test_edge_cases():
+    w = configs.small(configs.cfg0, NMC=0)
+    t, st = _oracle_run(w, api.RunOptions(seed=1), NMC=0)
+    assert st.n_events == 0 and all(np.all(v == 0) for v in t.a.values())
+    # a layer thinner than any SHI flight: the ion may leave without a collision
+    w = configs.small(configs.cfg0, NMC=3, layer=1e-6)
+    t, st = _oracle_run(w, api.RunOptions(seed=1))
+    assert st.n_shi <= 3
+    # one radial bin collects everything
+    w = configs.small(configs.cfg0, NMC=2, n_R=1)
+    t, st = _oracle_run(w, api.RunOptions(seed=1))
+    assert np.allclose(t["Out_ne"] * np.pi * w.material.Layer * w.R_edges[0] ** 2, t["Out_tot_Ne"])

@@ -1,0 +1,101 @@
+// impl.h -- host-side structures of the library (not part of the C ABI).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "../../include/trekis_gb300.h"
+
+namespace tk {
+
+constexpr int MAXSH = 32;   // compact shells over all atoms
+constexpr int MAXOSC = TREKIS_MAX_OSC;
+
+struct HTab { std::vector<double> E, L, dEdx; };
+struct HRow { std::vector<double> hw, L; };
+struct HRowSet { std::vector<double> E; std::vector<HRow> rows; };
+
+// Per-material constants the table kernels read (device copy lives in a buffer).
+struct BuildMat {
+    int nsh;
+    int kind_of_DR;
+    int dos_mass;          // 1: electron mass of the dispersion from the DOS
+    int N_dos;
+    double El_eff_mass, v_f, temp;
+    int nosc[MAXSH];
+    double Ip[MAXSH];
+    double E0[MAXSH * MAXOSC], A[MAXSH * MAXOSC], G[MAXSH * MAXOSC];
+    const double* dos_k;   // device
+    const double* dos_Eff_m;
+};
+
+// Device copies of a table set, one per precision.
+template <class T>
+struct DevTabs {
+    // electron grid shared by the per-shell IMFPs and the cumulative rows
+    const T* elE; int nE;
+    const T* elL;          // [nsh][nE] per-shell IMFP
+    const T* elIMFP;       // [nE] total
+    const T* elastE; const T* elastL; int nEl;
+    const int* row_off;    // [nsh*nE + 1]
+    const T* row_hw; const T* row_L;
+    // holes
+    const T* hE; int nH;
+    const T* hL;           // [nsh][nH]
+    const T* hIMFP;        // [nH]
+    const T* hElastE; const T* hElastL; int nHel;
+    const int* hrow_off;   // [nH + 1]
+    const T* hrow_hw; const T* hrow_L;
+    // photons
+    const T* pE; int nP;
+    const T* pL;           // [nsh][nP]
+    const T* pIMFP;
+    // DOS
+    const T* dosE; const T* dosD; const T* dosI; const T* dosM; int nD;
+};
+
+// SHI tables are always FP64 (the ion energy is ~1e8 eV).
+struct DevShi {
+    const double* sE; int nS;
+    const double* sL;      // [nsh][nS]
+    const double* path;    // [nS] total
+    const int* d_off;      // [nsh+1] transfer rows at the initial energy
+    const double* dE;      // lower edges
+    const double* dL;      // cumulative MFP
+    const double* dInvL;   // 1/L
+};
+
+struct Buffers {          // device allocations owned by a table set
+    std::vector<void*> ptrs;
+    void* alloc(size_t bytes);
+    ~Buffers();
+};
+
+}  // namespace tk
+
+struct trekis_tables {
+    trekis_material mat;                 // copy (DOS pointers refer to owned copies below)
+    trekis_ion ion;
+    std::vector<double> dos_E, dos_D, dos_I, dos_k, dos_M;
+    int nsh = 0;
+    int atom_of[tk::MAXSH], shell_of[tk::MAXSH];
+    int shell_index[TREKIS_MAX_ATOMS][TREKIS_MAX_SHELLS];
+    // host FP64 mirror
+    std::vector<tk::HTab> el, hole, phot, shi, dsde;  // per compact shell
+    tk::HTab el_elast, hole_elast, El_IMFP, Hole_IMFP, Phot_IMFP, SHI_path;
+    std::vector<tk::HRowSet> el_rows;   // per compact shell
+    tk::HRowSet hole_rows;
+    bool has_shi = false, has_phot = false;
+    // device
+    tk::Buffers buf;
+    tk::DevTabs<float> d32;
+    tk::DevTabs<double> d64;
+    tk::DevShi dshi;
+    double build_ms = 0.0;
+    uint64_t build_points = 0;
+};
+
+namespace tk {
+void set_error(const std::string& s);
+int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st);
+std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax);
+}  // namespace tk

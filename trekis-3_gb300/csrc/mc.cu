@@ -1,0 +1,965 @@
+// mc.cu -- the Monte Carlo track loop as an event-based wavefront on sm_103a.
+//
+// The reference advances one global clock and always processes the earliest
+// event of all particles (Find_min_time_particle, Monte_Carlo.f90:2060-2092),
+// tallying every particle at each grid time (Calculated_statistics,
+// Monte_Carlo.f90:881-1110).  Particles do not interact, so here:
+//   * every particle owns Philox streams keyed by (seed; id, event ordinal),
+//     which makes each history independent of the processing order;
+//   * the SHI track of an iteration is one thread (k_shi, FP64), emitting
+//     the primary electron-hole pairs into SoA queues;
+//   * k_step runs up to K events per live particle per launch, appending
+//     secondaries and survivors to the next queues with warp-aggregated
+//     atomics (one atomic per warp per append site);
+//   * each free-flight segment [t0, tn) is tallied once, when it starts, into
+//     int64 difference arrays over the time grid (run-length over the radial
+//     bin), which makes the tallies bit-exact and order-independent.
+// The event bodies follow, draw for draw, SHI_Monte_Carlo (MC:2153-2249),
+// Electron_Monte_Carlo (MC:2253-2474), Hole_Monte_Carlo (MC:2517-2869) and
+// Photon_Monte_Carlo (MC:2873-2965).
+#include <cooperative_groups.h>
+#include "mc.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace tk {
+
+template <class T>
+struct P {  // one particle in registers
+    T E, t0, tn, X, Y, Z, L, th, ph, Ek, M;
+    uint64_t pid;
+    uint32_t ord;
+    int sh;
+};
+
+// warp-aggregated append; returns -1 (and raises the overflow flag) when full
+__device__ __forceinline__ int64_t agg_append(int* ctr, int64_t cap, int* overflow) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(ctr, (int)g.size());
+    base = g.shfl(base, 0);
+    int64_t idx = (int64_t)base + g.thread_rank();
+    if (idx >= cap) { atomicExch(overflow, 1); return -1; }
+    return idx;
+}
+
+template <class T>
+__device__ __forceinline__ void store(const PQ<T>& q, int64_t i, const P<T>& p) {
+    q.E[i] = p.E; q.t0[i] = p.t0; q.tn[i] = p.tn; q.X[i] = p.X; q.Y[i] = p.Y; q.Z[i] = p.Z;
+    q.L[i] = p.L; q.th[i] = p.th; q.ph[i] = p.ph; q.pid[i] = p.pid; q.ord[i] = p.ord;
+    if (q.Ek) { q.Ek[i] = p.Ek; q.M[i] = p.M; q.sh[i] = (uint16_t)p.sh; }
+}
+template <class T>
+__device__ __forceinline__ void load(const PQ<T>& q, int64_t i, P<T>& p) {
+    p.E = q.E[i]; p.t0 = q.t0[i]; p.tn = q.tn[i]; p.X = q.X[i]; p.Y = q.Y[i]; p.Z = q.Z[i];
+    p.L = q.L[i]; p.th = q.th[i]; p.ph = q.ph[i]; p.pid = q.pid[i]; p.ord = q.ord[i];
+    if (q.Ek) { p.Ek = q.Ek[i]; p.M = q.M[i]; p.sh = q.sh[i]; } else { p.Ek = T(0); p.M = T(0); p.sh = 0; }
+}
+
+// mixed-precision event stream: draws for the FP64 SHI state use next_d()
+template <class T>
+struct EvStream {
+    uint32_t k0, k1, c0, c1, c2, c3, buf[4];
+    int used;
+    __device__ EvStream(uint64_t seed, uint64_t pid, uint32_t ordinal)
+        : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), c0((uint32_t)pid), c1((uint32_t)(pid >> 32)),
+          c2(ordinal), c3(0), used(4) {}
+    __device__ __forceinline__ uint32_t word() {
+        if (used == 4) { philox4x32(c0, c1, c2, c3, k0, k1, buf); ++c3; used = 0; }
+        return buf[used++];
+    }
+    __device__ __forceinline__ T next() { return Uni<T>::of(word()); }
+    __device__ __forceinline__ double next_d() { return Uni<double>::of(word()); }
+};
+
+template <class T> __device__ __forceinline__ T pi_() { return T(kPi); }
+
+// ---- tallies ------------------------------------------------------------------------
+__device__ __forceinline__ void add64(unsigned long long* p, long long v) { atomicAdd(p, (unsigned long long)v); }
+
+template <class T>
+__device__ __forceinline__ long long fixE(T E) { return __double2ll_rn((double)E * kEScale); }
+
+template <class T>
+__device__ __forceinline__ int rbin(const McConst<T>& C, T R) { return find_monoton(C.Rg, C.NR, R); }
+
+// one run of equal radial bin over rows [r0, r1] (1-based)
+template <class T>
+__device__ void flush_run(const McConst<T>& C, const Tal& tal, int kind, int sh, int j, int r0, int r1,
+                          long long qE, long long qK) {
+    const int NR = C.NR;
+    if (kind == 0 || kind == 2) {
+        unsigned long long* cnt = kind == 0 ? tal.e_cnt : tal.p_cnt;
+        unsigned long long* en = kind == 0 ? tal.e_E : tal.p_E;
+        add64(cnt + (size_t)r0 * NR + (j - 1), 1);
+        add64(en + (size_t)r0 * NR + (j - 1), qE);
+        if (r1 < C.Nt) {
+            add64(cnt + (size_t)(r1 + 1) * NR + (j - 1), -1);
+            add64(en + (size_t)(r1 + 1) * NR + (j - 1), -qE);
+        }
+    } else {
+        const size_t a = ((size_t)r0 * C.nsh + sh) * NR + (j - 1);
+        add64(tal.h_cnt + a, 1); add64(tal.h_E + a, qE); add64(tal.h_Ek + a, qK);
+        if (r1 < C.Nt) {
+            const size_t b = ((size_t)(r1 + 1) * C.nsh + sh) * NR + (j - 1);
+            add64(tal.h_cnt + b, -1); add64(tal.h_E + b, -qE); add64(tal.h_Ek + b, -qK);
+        }
+    }
+}
+
+// Tally the free-flight segment [t0, tn) at every grid time t_i with
+// t0 < t_i <= min(tn, Tim), exactly as Calculated_statistics sees it:
+// position X + V (t_i - t0) 1e-5 along (th, ph) for moving particles.
+template <class T>
+__device__ void emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn, T X, T Y,
+                         T th, T ph, T V /* m/s, 0: static */) {
+    const int Nt = C.Nt;
+    if (!(t0 < C.tg[Nt - 1])) return;
+    const int ia = find_monoton(C.tg, Nt, t0);
+    const T tend = tn < C.Tim ? tn : C.Tim;
+    const int ib = (tend >= C.tg[Nt - 1]) ? Nt : find_monoton(C.tg, Nt, tend) - 1;
+    if (ib < ia) return;
+    const long long qE = fixE(E), qK = fixE(Ek);
+    if (V == T(0)) {
+        flush_run(C, tal, kind, sh, rbin(C, m_sqrt(X * X + Y * Y)), ia, ib, qE, qK);
+        return;
+    }
+    const T s_t = m_sin(th), s_p = m_sin(ph), c_p = m_cos(ph);
+    int cur = -1, start = ia;
+    for (int i = ia; i <= ib; ++i) {
+        T L0 = V * (C.tg[i - 1] - t0) * T(1.0e-5);
+        if (L0 < T(0)) L0 = T(0);
+        T x = X + L0 * s_t * s_p;
+        T y = Y + L0 * s_t * c_p;
+        int j = rbin(C, m_sqrt(x * x + y * y));
+        if (j != cur) {
+            if (cur > 0) flush_run(C, tal, kind, sh, cur, start, i - 1, qE, qK);
+            cur = j; start = i;
+        }
+    }
+    flush_run(C, tal, kind, sh, cur, start, ib, qE, qK);
+}
+
+template <class T> __device__ __forceinline__ T v_el(T E) { return m_sqrt(T(2.0) * E * T(kE) / T(kMe)); }
+template <class T>
+__device__ __forceinline__ T v_hole(T Ek, T M) {  // Get_velosity for holes (MC:860-874)
+    if (M < T(1.0e6)) {
+        if (Ek < T(-1.0e-6) || M < T(1.0e-10)) return T(0);
+        if (m_abs(Ek) < T(1.0e-6)) return T(0);
+        return m_sqrt(T(2.0) * Ek * T(kE) / (M * T(kMe)));
+    }
+    return T(0);
+}
+template <class T> __device__ __forceinline__ T tn_of(T t0, T L, T V) {
+    return (V > T(1.0e-10)) ? t0 + L / V * T(1e5) : T(1.0e25);
+}
+
+template <class T>
+__device__ __forceinline__ void emit_electron(const McConst<T>& C, const Tal& tal, const P<T>& p) {
+    const T co = C.cut_off > T(0) ? C.cut_off : T(0);
+    const bool mv = p.E > co;
+    emit_seg(C, tal, 0, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0), mv ? v_el(p.E) : T(0));
+}
+template <class T>
+__device__ __forceinline__ void emit_hole(const McConst<T>& C, const Tal& tal, const P<T>& p) {
+    const T co = C.cut_off > T(0) ? C.cut_off : T(0);
+    const bool mv = (p.M < T(1.0e3)) && (p.Ek > co);
+    emit_seg(C, tal, 1, p.sh, p.E, p.Ek, p.t0, p.tn, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0));
+}
+template <class T>
+__device__ __forceinline__ void emit_photon(const McConst<T>& C, const Tal& tal, const P<T>& p) {
+    if (p.E > T(0)) emit_seg(C, tal, 2, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, p.th, p.ph, T(kC));
+}
+
+// per-thread accumulator of the lattice energy (one atomic per change of
+// cell); each deposit is rounded to fixed point on its own, so the sum does
+// not depend on how events are grouped into threads and launches
+struct LatAcc {
+    int cell = -1;
+    long long sum = 0;
+    __device__ __forceinline__ void add(const Tal& tal, int c, double v) {
+        if (c != cell) { flush(tal); cell = c; }
+        sum += __double2ll_rn(v * kLatScale);
+    }
+    __device__ __forceinline__ void flush(const Tal& tal) {
+        if (cell >= 0 && sum != 0) add64(tal.lat + cell, sum);
+        sum = 0;
+    }
+};
+
+// ---- samplers ----------------------------------------------------------------------
+
+// Which_shell (MC:1786-1832) over per-shell tables sharing one grid
+template <class T>
+__device__ int which_shell(const McConst<T>& C, const T* Eg, const T* Lbase, int n, T E, T RN) {
+    T inv[MAXSH];
+    T tot = T(0);
+    int nb = find_monoton(Eg, n, E);
+    for (int k = 0; k < C.nsh; ++k) {
+        const T* L = Lbase + (size_t)k * n;
+        T M;
+        if (nb == 1) M = T(1.0e20);
+        else if (L[nb - 2] == L[nb - 1] || L[nb - 2] > T(1e20)) M = L[nb - 2];
+        else M = interp<T>(5, Eg[nb - 2], Eg[nb - 1], L[nb - 2], L[nb - 1], E);
+        inv[k] = T(1) / M;
+        tot += inv[k];
+    }
+    tot = RN * tot;
+    T sum = T(0);
+    for (int k = 0; k < C.nsh; ++k) {
+        sum += inv[k];
+        if (sum >= tot) return k;
+    }
+    return C.nsh - 1;
+}
+
+// From_where_in_VB (MC:1522-1573)
+template <class T, class S>
+__device__ T from_where_in_vb(const DevTabs<T>& tb, S& s, bool hasE, T E) {
+    const int N = tb.nD;
+    if (N == 0) return T(0);
+    T sum;
+    if (!hasE) sum = tb.dosI[N - 1];
+    else {
+        int Mt = (E < tb.dosE[N - 1]) ? find_monoton(tb.dosE, N, E) : N + 1;
+        if (Mt <= 1) return T(0);
+        sum = tb.dosI[Mt - 2];
+    }
+    T Tot = s.next() * sum;
+    int n = find_monoton(tb.dosI, N, Tot);
+    if (n > 1)
+        return tb.dosE[n - 2] + (tb.dosE[n - 1] - tb.dosE[n - 2]) * (Tot - tb.dosI[n - 2]) / (tb.dosI[n - 1] - tb.dosI[n - 2]);
+    return tb.dosE[n - 1];
+}
+
+// Electron_recieves_E (MC:1653-1716)
+template <class T, class S>
+__device__ T electron_receives(const McConst<T>& C, const DevTabs<T>& tb, T dE, int k, S& s, unsigned& err) {
+    T E = dE - C.Ip[k];
+    T out = E;
+    if (k == C.vb && tb.nD > 0 && dE > C.Ip[k]) {
+        const int N = tb.nD;
+        int Mt = (E < tb.dosE[N - 1]) ? find_monoton(tb.dosE, N, E) : N + 1;
+        if (Mt > 1) {
+            T sum = tb.dosI[Mt - 2];
+            T Tot = s.next() * sum;
+            int n = find_monoton(tb.dosI, N, Tot);
+            T Ed = (n > 1) ? tb.dosE[n - 2] + (tb.dosE[n - 1] - tb.dosE[n - 2]) * (Tot - tb.dosI[n - 2]) /
+                                 (tb.dosI[n - 1] - tb.dosI[n - 2])
+                           : tb.dosE[n - 1];
+            out = E - Ed;
+        }
+    }
+    if (out < T(0)) err |= TREKIS_ERR_NEG_TRANSFER;
+    return out;
+}
+
+// Hole_parameters + Assign_holes_mass (MC:724-792); p.sh, p.t0 set by the caller
+template <class T, class S>
+__device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>& h, T Eh, S& s) {
+    if (h.sh == C.vb) {
+        T Etemp = h.Ek;
+        h.Ek = Eh - C.Egap;
+        h.E = C.Egap;
+        if (C.hole_mass > T(0)) h.M = C.hole_mass;
+        else h.M = tb.dosM[find_monoton(tb.dosE, tb.nD, h.Ek) - 1];
+        if (h.M < T(1.0e3)) {
+            T HI = nfp2(Tab<T>{tb.hE, tb.hIMFP, tb.nH}, h.Ek);
+            T HE = (Etemp == Eh - C.Egap) ? T(1.0e30) : nfp2(Tab<T>{tb.hElastE, tb.hElastL, tb.nHel}, h.Ek);
+            T RN = s.next();
+            T Mt = -m_log(RN) / (T(1) / HI + T(1) / HE);
+            h.tn = tn_of(h.t0, Mt, v_hole(h.Ek, h.M));
+            h.L = Mt;
+        } else { h.L = T(1.0e30); h.tn = T(1.0e30); }
+    } else {
+        h.M = T(1.0e29);
+        T RN = s.next();
+        T nu = T(1) / C.Auger[h.sh] + T(1) / C.Radiat[h.sh];
+        h.tn = h.t0 - m_log(RN) / nu;
+        h.L = T(1.0e30);
+        h.E = Eh;
+        h.Ek = T(0);
+    }
+}
+
+template <class T>
+__device__ __forceinline__ void cut_e(const McConst<T>& C, P<T>& p) { if (p.E < C.cut_off) p.tn = T(1.0e20); }
+template <class T>
+__device__ __forceinline__ void cut_h(const McConst<T>& C, P<T>& p) {
+    if (p.M < T(1e15) && p.Ek < C.cut_off) p.tn = T(1.0e20);
+}
+
+// New_Angles_both (MC:1328-1360)
+template <class T>
+__device__ __forceinline__ void new_angles(T phi0, T theta0, T theta, T psi, T& phi1, T& theta1) {
+    const T twoPi = T(2.0) * pi_<T>();
+    phi1 = phi0 + theta * m_cos(theta0) * m_sin(psi);
+    theta1 = theta0 + theta * m_cos(psi);
+    for (int g = 0; g < 64 && theta1 < T(0); ++g) { theta1 = m_abs(theta1); phi1 = phi1 + pi_<T>(); }
+    for (int g = 0; g < 64 && theta1 > pi_<T>(); ++g) { theta1 = twoPi - theta1; phi1 = phi1 - pi_<T>(); }
+    if (phi1 > twoPi) phi1 = phi1 - m_floor(phi1 / twoPi) * twoPi;
+    if (phi1 < T(0)) phi1 = phi1 + m_ceil(m_abs(phi1) / twoPi) * twoPi;
+}
+
+template <class T, class S>
+__device__ __forceinline__ void electron_flight(const DevTabs<T>& tb, P<T>& p, S& s) {
+    T I = nfp2(Tab<T>{tb.elE, tb.elIMFP, tb.nE}, p.E);
+    T Em = nfp2(Tab<T>{tb.elastE, tb.elastL, tb.nEl}, p.E);
+    T RN = s.next();
+    p.L = -m_log(RN) / (T(1) / I + T(1) / Em);
+    p.tn = tn_of(p.t0, p.L, v_el(p.E));
+}
+
+// Mott energy transfer, Pers-weighted average over species (MC:2394-2407, CS:3517-3613).
+// FP64 keeps the reference's expressions; FP32 uses algebraically identical
+// forms without cancellation: beta^2 = tau(tau+2)/(tau+1)^2, and with
+// mu = (u(2nu+1)-nu)/(u+nu) the exact 1-mu = 2nu(1-u)/(u+nu).
+template <class T, class S>
+__device__ T mott_transfer(const McConst<T>& C, T Ee, T M_eff, S& s) {
+    T dE = T(0);
+    const T Erest = C.mec2;
+    const T tau = Ee / Erest;
+    T beta2, v;
+    if constexpr (sizeof(T) == 8) {
+        const T fact = Ee / Erest + T(1);
+        v = T(kC) * m_sqrt(T(1) - T(1) / (fact * fact));
+        const T beta = v / T(kC);
+        beta2 = beta * beta;
+    } else {
+        beta2 = tau * (tau + T(2)) / ((tau + T(1)) * (tau + T(1)));
+        v = T(kC) * m_sqrt(beta2);
+    }
+    const T sq = m_sqrt(tau / (T(1) + tau));
+    const T mc2 = M_eff * C.mec2;
+    for (int a = 0; a < C.nat; ++a) {
+        const T Z = T(C.Zat[a]);
+        const T RN = s.next();
+        const T Mct2 = C.Mass_kg[a] * T(kC) * T(kC) / T(kE);
+        T W1, ct2;
+        if constexpr (sizeof(T) == 8) {
+            T ct;
+            if (v < T(1.0e-6)) ct = T(1);
+            else {
+                T nu = T(1.7e-5) * C.Z23[a] * (T(1) - beta2) / beta2 * (T(1.13) + T(3.76) * C.alpha * C.alpha / beta2 * Z * Z * sq);
+                T mu = (RN * (T(2) * nu + T(1)) - nu) / (RN + nu);
+                ct = m_cos(m_acos(mu));
+            }
+            ct2 = ct * ct;
+            const T st2 = T(1) - ct2;
+            W1 = (Ee + mc2) * st2 + Mct2 - ct * m_sqrt(Mct2 * Mct2 - mc2 * mc2 * st2);
+        } else {
+            T omc = T(0);
+            if (!(v < T(1.0e-6))) {
+                T nu = T(1.7e-5) * C.Z23[a] * (T(1) - beta2) / beta2 * (T(1.13) + T(3.76) * C.alpha * C.alpha / beta2 * Z * Z * sq);
+                omc = T(2) * nu * (T(1) - RN) / (RN + nu);
+            }
+            const T ct = T(1) - omc, st2 = omc * (T(2) - omc);
+            ct2 = ct * ct;
+            const T r = m_sqrt(Mct2 * Mct2 - mc2 * mc2 * st2);
+            W1 = (Ee + mc2) * st2 + Mct2 * omc + ct * (mc2 * mc2 * st2) / (Mct2 + r);
+        }
+        const T E2mc = Ee + T(2) * mc2, EmcMc = Ee + mc2 + Mct2;
+        const T W2 = Ee * E2mc / (EmcMc * EmcMc - Ee * E2mc * ct2);
+        dE += W1 * W2 * C.Pers[a];
+    }
+    return dE / C.Psum;
+}
+
+// Update_particle_angles_lat (MC:1252-1299)
+template <class T, class S>
+__device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& theta, T& phi) {
+    T Ein = M_eff * C.mec2, Et = C.Mtarget * T(kC) * T(kC) / T(kE);
+    T E2mc = E + T(2) * Ein, EmW = E - W;
+    T W1 = E * E2mc - W * (E + Ein + Et), W2 = E * E2mc * EmW * (E2mc - W);
+    T mu = (W2 > T(0)) ? W1 / m_sqrt(W2) : T(0);
+    if (m_abs(mu) > T(1)) { T RN = s.next(); mu = m_cos(pi_<T>() * RN); }
+    theta = m_acos(mu);
+    phi = T(2) * pi_<T>() * s.next();
+}
+
+// interpolate_transferred_energy (CS:1968-2045) over one table of cumulative rows
+template <class T>
+__device__ T interp_transfer(const T* Eg, int nE, const int* roff, const T* rhw, const T* rL, T Ele, T L_need) {
+    int iE = find_monoton(Eg, nE, Ele);
+    if (iE > 1 && m_abs(Eg[iE - 2] - Ele) < T(1.0e-6)) iE -= 1;
+    auto one = [&](int ie) -> T {
+        const int o = roff[ie - 1], len = roff[ie] - o;
+        const T* hw = rhw + o;
+        const T* L = rL + o;
+        int ih = find_decreasing(L, len, L_need);
+        if (ih == 1 || ih == len) return hw[ih - 1];
+        return interp<T>(5, L[ih - 1], L[ih], hw[ih - 1], hw[ih], L_need);
+    };
+    T hw1 = one(iE);
+    T out = hw1;
+    if (iE > 1) {
+        iE -= 1;
+        T hw2 = one(iE);
+        if (hw1 < T(1.0e-10) || hw2 < T(1.0e-10)) out = interp<T>(1, Eg[iE - 1], Eg[iE], hw1, hw2, Ele);
+        else out = interp<T>(5, Eg[iE - 1], Eg[iE], hw1, hw2, Ele);
+    }
+    return out;
+}
+
+// Electron_energy_transfer_inelastic (CS:1793-1871), tabulated rows (CS_method = 1)
+template <class T>
+__device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hole, int k, T Ele, T L_tot, T RN,
+                             unsigned& err) {
+    T L_need = L_tot / RN;
+    T Emin = C.Ip[k];
+    if (Emin <= T(1.0e-3)) Emin = T(1.0e-3);
+    T Emax, Mass;
+    if (hole) {
+        Mass = (C.hole_mass >= T(0)) ? C.hole_mass : tb.dosM[find_monoton(tb.dosE, tb.nD, Ele) - 1];
+        Emax = T(4) * Ele * Mass / ((Mass + T(1)) * (Mass + T(1)));
+    } else Emax = (Ele + Emin) / T(2);
+    T E = hole ? interp_transfer(tb.hE, tb.nH, tb.hrow_off, tb.hrow_hw, tb.hrow_L, Ele, L_need)
+               : interp_transfer(tb.elE, tb.nE, tb.row_off + (size_t)k * tb.nE, tb.row_hw, tb.row_L, Ele, L_need);
+    if (E < Emin) E = Emin;
+    if (E > Emax) E = Emax;
+    if (E < C.Egap) err |= TREKIS_ERR_NEG_TRANSFER;
+    if (m_isnan(E)) E = Emin;
+    return E;
+}
+
+// a hole created at (X,Y,Z) with random angles (Update_holes_angles_SHI, MC:1132-1140)
+template <class T, class S>
+__device__ void make_hole(const McConst<T>& C, const DevTabs<T>& tb, P<T>& hh, T t0, T X, T Y, T Z, int k, T Eh,
+                          S& s, unsigned& err) {
+    hh.th = pi_<T>() * s.next();
+    hh.ph = T(2) * pi_<T>() * s.next();
+    hh.t0 = t0; hh.X = X; hh.Y = Y; hh.Z = Z; hh.sh = k; hh.Ek = T(0); hh.E = T(0); hh.M = T(1.0e30);
+    hole_parameters(C, tb, hh, Eh, s);
+    cut_h(C, hh);
+    if (hh.Ek < T(-1.0e-9) || m_isnan(hh.Ek)) err |= TREKIS_ERR_NEG_ENERGY_H;
+}
+
+template <class T>
+struct Out {  // where a thread puts new particles
+    PQ<T> e, h, p;
+    Ctrs* ctr;
+};
+
+template <class T>
+__device__ __forceinline__ void push(const McConst<T>& C, const Tal& tal, const Out<T>& o, int kind, const P<T>& p) {
+    const PQ<T>& q = kind == 0 ? o.e : kind == 1 ? o.h : o.p;
+    int64_t i = agg_append(&o.ctr->n_out[kind], q.cap, &o.ctr->overflow);
+    if (i >= 0) store(q, i, p);
+}
+
+// ---- SHI track: one thread per iteration (FP64 ion) -----------------------------------
+template <class T>
+__global__ void __launch_bounds__(128) k_shi(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, DevShi sh, PQ<T> qe,
+                                             PQ<T> qh, Tal tal, Ctrs* ctr, int nit) {
+    const int it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= nit) return;
+    const McConst<T>& C = *Cp;
+    unsigned err = 0;
+    unsigned long long nev = 0;
+    const uint64_t pid = shi_pid(C.it0 + it);
+    double E = C.ion_E0, t0 = 0.0, tn = 0.0, X = 0.0, Y = 0.0, Z = 0.0, L;
+    const double MSHI = C.MSHI;
+    const Tab<double> path{sh.sE, sh.path, sh.nS};
+    {
+        EvStream<T> s(C.seed, pid, 0xFFFFFFFFu);
+        L = nfp2(path, E);
+        L = -L * log(s.next_d());
+        double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
+        tn = (V > 1.0e-10) ? t0 + L / V * 1e5 : 1.0e25;
+    }
+    Out<T> o{qe, qh, qe, ctr};
+    uint32_t ord = 0;
+    while (tn < (double)C.Tim) {
+        if (ord >= (1u << 26)) { err |= TREKIS_ERR_NAN; break; }   // no SHI track has this many collisions
+        EvStream<T> s(C.seed, pid, ord);
+        // Which_shell over the SHI tables
+        int k;
+        {
+            double inv[MAXSH], tot = 0.0;
+            int nb = find_monoton(sh.sE, sh.nS, E);
+            for (int q = 0; q < C.nsh; ++q) {
+                const double* Lq = sh.sL + (size_t)q * sh.nS;
+                double M;
+                if (nb == 1) M = 1.0e20;
+                else if (Lq[nb - 2] == Lq[nb - 1] || Lq[nb - 2] > 1e20) M = Lq[nb - 2];
+                else M = interp<double>(5, sh.sE[nb - 2], sh.sE[nb - 1], Lq[nb - 2], Lq[nb - 1], E);
+                inv[q] = 1.0 / M;
+                tot += inv[q];
+            }
+            tot = s.next_d() * tot;
+            double sum = 0.0;
+            k = C.nsh - 1;
+            for (int q = 0; q < C.nsh; ++q) { sum += inv[q]; if (sum >= tot) { k = q; break; } }
+        }
+        // SHI_energy_transfer (MC:1719-1780), CDF branch
+        double dE;
+        {
+            const int o0 = sh.d_off[k], N = sh.d_off[k + 1] - o0;
+            const double* DE = sh.dE + o0;
+            const double* DL = sh.dL + o0;
+            const double* DI = sh.dInvL + o0;
+            double RN = s.next_d();
+            const double Ip = C.Ipd[k];
+            if (N < 1) { dE = Ip; goto transferred; }   // shell beyond the SHI's maximum transfer
+            {
+            int Mt = find_monoton(DE, N, Ip);
+            double dL;
+            if (Mt > 1) dL = (DL[Mt - 2] > 1.0e-10) ? interp<double>(5, DE[Mt - 2], DE[Mt - 1], DL[Mt - 2], DL[Mt - 1], Ip)
+                                                    : interp<double>(1, DE[Mt - 2], DE[Mt - 1], DL[Mt - 2], DL[Mt - 1], Ip);
+            else dL = DL[0];
+            double Tot = (dL > 0.0 && DL[N - 1] > 0.0) ? 1.0 / dL + RN * (1.0 / DL[N - 1] - 1.0 / dL) : 1.5e21;
+            int nt;
+            if (Tot < 1e20) {  // first index with 1/L >= Tot (Find_in_1D_array, RF:3348), by bisection
+                int lo = 0, hi = N - 1;
+                while (lo < hi) { int mid = (lo + hi) >> 1; if (DI[mid] < Tot) lo = mid + 1; else hi = mid; }
+                nt = lo + 1;
+            } else nt = Mt;
+            dE = (nt > Mt) ? interp<double>(5, DI[nt - 2], DI[nt - 1], DE[nt - 2], DE[nt - 1], Tot) : Ip;
+            }
+        }
+    transferred:
+        double Lnew = nfp2(path, E);
+        Lnew = -Lnew * log(s.next_d());
+        const double Znew = Z + L;
+        E -= dE; t0 = tn; Z = Znew; L = Lnew;
+        {
+            double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
+            tn = (V > 1.0e-10) ? t0 + L / V * 1e5 : 1.0e25;
+        }
+        // Equilibrium_charge_SHI (CS:2641-2680)
+        double Zeff;
+        {
+            double vp = E > 0.0 ? sqrt(2.0 * E * kE / (C.ion_mass_p * kMp)) : 0.0;
+            double Zp = C.ion_Z, v0 = sqrt(2.0 * kRy * kE / kMe);
+            switch (C.ion_kind_zeff) {
+            case 1: Zeff = Zp * (1.0 - exp(-(vp / v0 / pow(Zp, 0.66666666)))); break;
+            case 2: Zeff = Zp * pow(1.0 + pow(vp / (pow(Zp, 0.45) * v0 * 4.0 / 3.0), -1.0 / 0.6), -0.6); break;
+            case 3: {
+                double Zt = C.Zt, c1 = 1.0 - 0.26 * exp(-Zt / 11.0 - (Zt - Zp) * (Zt - Zp) / 9.0);
+                double vpvo = pow(Zp, -0.543) * vp / v0, c2 = 1.0 + 0.03 * vpvo * log(Zt);
+                double x = c1 * pow(vpvo / c2 / 1.54, 1.0 + 1.83 / Zp), x2 = x * x, x4 = x2 * x2;
+                Zeff = Zp * (8.29 * x + x4) / (0.06 / x + 4.0 + 7.4 * x + x4);
+            } break;
+            case 4: Zeff = C.ion_fixed_zeff; break;
+            default: Zeff = Zp * (1.0 - exp(-(vp * 125.0 / kC / pow(Zp, 0.66666666))));
+            }
+        }
+        // the electron-hole pair
+        P<T> el;
+        el.pid = child_pid(pid, ord, 0); el.ord = 0; el.sh = 0; el.Ek = T(0); el.M = T(0);
+        T dEc = electron_receives(C, tb, (T)dE, k, s, err);
+        T theta = (E <= 0.0) ? pi_<T>() / T(2)
+            : (T)acos(sqrt((MSHI + kMe) * (MSHI + kMe) / (4.0 * MSHI * kMe) * dE / E));
+        T phi = T(2) * pi_<T>() * s.next();
+        el.E = dEc; el.t0 = (T)t0;
+        electron_flight(tb, el, s);
+        double Aa = 1.0 + MSHI / kMe;
+        double b = kA0 * Zeff * kRy / E * sqrt(4.0 * E / dE * MSHI / kMe - Aa * Aa);
+        el.X = (T)(X + b * sin((double)phi)); el.Y = (T)(Y + b * cos((double)phi)); el.Z = (T)Z;
+        el.th = theta; el.ph = phi;
+        cut_e(C, el);
+        if (el.E < T(-1.0e-9) || m_isnan(el.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
+        emit_electron(C, tal, el);
+        push(C, tal, o, 0, el);
+        P<T> hh;
+        hh.pid = child_pid(pid, ord, 1); hh.ord = 0;
+        make_hole(C, tb, hh, (T)t0, el.X, el.Y, el.Z, k, (T)dE - dEc, s, err);
+        emit_hole(C, tal, hh);
+        push(C, tal, o, 1, hh);
+        ++ord; ++nev;
+        if (Z >= C.Layer) tn = 1.0e16;
+    }
+    atomicAdd(&ctr->ev[0], nev);
+    atomicAdd(&ctr->ev[7], 2ull * nev);
+    if (err) atomicOr(&ctr->err_bits, err);
+}
+
+// ---- cascade events ------------------------------------------------------------------------
+template <class T>
+__device__ void electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
+                               P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev) {
+    const uint32_t ord = p.ord++;
+    EvStream<T> s(C.seed, p.pid, ord);
+    const T Eel = p.E;
+    const T I = nfp2(Tab<T>{tb.elE, tb.elIMFP, tb.nE}, Eel);
+    const T Em = nfp2(Tab<T>{tb.elastE, tb.elastL, tb.nEl}, Eel);
+    const T RN = s.next();
+    const T th0 = p.th, ph0 = p.ph, tev = p.tn;
+    const T X = p.X + p.L * m_sin(th0) * m_sin(ph0);
+    const T Y = p.Y + p.L * m_sin(th0) * m_cos(ph0);
+    const T Z = p.Z + p.L * m_cos(th0);
+    T dE, theta, phi;
+    if (RN * (T(1) / I + T(1) / Em) < T(1) / I) {  // impact ionisation
+        const int k = which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next());
+        const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
+        dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err);
+        theta = m_acos((Eel - dE) / m_sqrt(Eel * (Eel - dE)));
+        if (m_isnan(theta)) theta = s.next() * pi_<T>();
+        phi = T(2) * pi_<T>() * s.next();
+        const T dEc = electron_receives(C, tb, dE, k, s, err);
+        P<T> ne;
+        ne.pid = child_pid(p.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+        ne.E = dEc; ne.t0 = tev;
+        electron_flight(tb, ne, s);
+        T ph1, th1;
+        new_angles(ph0, th0, pi_<T>() / T(2) - theta, phi + pi_<T>(), ph1, th1);
+        ne.X = X; ne.Y = Y; ne.Z = Z; ne.th = th1; ne.ph = ph1;
+        cut_e(C, ne);
+        if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
+        P<T> hh;
+        hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0;
+        make_hole(C, tb, hh, tev, X, Y, Z, k, dE - dEc, s, err);
+        emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
+        emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
+        nev[1]++; nev[7] += 2;
+    } else {  // elastic (Mott)
+        dE = mott_transfer(C, Eel, T(1), s);
+        angles_lat(C, Eel, dE, T(1), s, theta, phi);
+        const int i = find_monoton(C.tg, C.Nt, tev);  // the interval t_{i-1} <= t < t_i
+        const int j = rbin(C, m_sqrt(X * X + Y * Y));
+        lat.add(tal, (i - 1) * C.NR + (j - 1), (double)dE);
+        nev[2]++;
+    }
+    p.E = Eel - dE;
+    p.t0 = tev;
+    electron_flight(tb, p, s);
+    T ph1, th1;
+    new_angles(ph0, th0, theta, phi, ph1, th1);
+    p.X = X; p.Y = Y; p.Z = Z; p.th = th1; p.ph = ph1;
+    cut_e(C, p);
+    if (p.E < T(-1.0e-9) || m_isnan(p.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
+    emit_electron(C, tal, p);
+}
+
+// check_hole_parameters (MC:682-721); the downward search stops at the first DOS node
+template <class T>
+__device__ T check_hole(const DevTabs<T>& tb, T Eel, T& dE, P<T>* el) {
+    T Eh = Eel - dE;
+    int mh = find_monoton(tb.dosE, tb.nD, Eh);
+    if (tb.dosD[mh - 1] < T(1.0e-4)) {
+        if (el) {
+            while (mh > 1 && tb.dosD[mh - 1] < T(1.0e-4)) --mh;
+            T Eloc = tb.dosE[mh - 1];
+            el->E = el->E + (Eh - Eloc);
+            Eh = Eloc;
+        } else {
+            while (mh < tb.nD && tb.dosD[mh - 1] < T(1.0e-4)) ++mh;
+            T Eloc = tb.dosE[mh - 1];
+            dE = dE + (Eh - Eloc);
+            Eh = Eloc;
+        }
+    }
+    return Eh;
+}
+
+template <class T>
+__device__ void hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& h,
+                           unsigned& err, LatAcc& lat, unsigned long long* nev) {
+    const uint32_t ord = h.ord++;
+    EvStream<T> s(C.seed, h.pid, ord);
+    if (h.sh == C.vb) {
+        const T Eel = h.Ek;
+        const T HI = nfp2(Tab<T>{tb.hE, tb.hIMFP, tb.nH}, Eel);
+        const T HE = nfp2(Tab<T>{tb.hElastE, tb.hElastL, tb.nHel}, Eel);
+        const T RN = s.next();
+        const T th0 = h.th, ph0 = h.ph, tev = h.tn, hm = h.M;
+        const T X = h.X + h.L * m_sin(th0) * m_sin(ph0);
+        const T Y = h.Y + h.L * m_sin(th0) * m_cos(ph0);
+        const T Z = h.Z + h.L * m_cos(th0);
+        T dE, th1, ph1, Eh;
+        if (RN * (T(1) / HI + T(1) / HE) < T(1) / HI && HI < T(1e15)) {
+            const int k = which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
+            const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
+            dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err);
+            // Update_holes_angles_el (MC:1142-1168)
+            // masses in kg as the reference writes them (FP64); in electron
+            // masses for FP32, where (Mh+me)^2 would underflow
+            const T E11 = Eel - dE;
+            const T Mh = (sizeof(T) == 8) ? hm * T(kMe) : hm;
+            const T me_ = (sizeof(T) == 8) ? T(kMe) : T(1);
+            T ht = m_acos(m_sqrt((Mh + me_) * (Mh + me_) / (T(4) * Mh * me_) * dE / Eel));
+            const T hp = T(2) * pi_<T>() * s.next();
+            if (m_isnan(ht)) ht = pi_<T>() * s.next();
+            th1 = m_acos((Eel * (Mh - me_) + E11 * (Mh + me_)) / (T(2) * Mh * m_sqrt(Eel * E11)));
+            ph1 = hp + pi_<T>();
+            if (m_isnan(th1)) th1 = pi_<T>() * s.next();
+            const T dEc = electron_receives(C, tb, dE, k, s, err);
+            P<T> ne;
+            ne.pid = child_pid(h.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+            ne.E = dEc; ne.t0 = tev;
+            electron_flight(tb, ne, s);
+            (void)s.next();  // the reference draws one unused number here (MC:2611)
+            T phe, the;
+            new_angles(ph0, th0, ht, hp, phe, the);
+            ne.X = X; ne.Y = Y; ne.Z = Z; ne.th = the; ne.ph = phe;
+            cut_e(C, ne);
+            if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
+            P<T> hh;
+            hh.pid = child_pid(h.pid, ord, 1); hh.ord = 0;
+            make_hole(C, tb, hh, tev, X, Y, Z, k, dE - dEc, s, err);
+            if (hh.E + hh.Ek < C.Egap - T(1.0e-12)) err |= TREKIS_ERR_HOLE_IN_GAP;
+            Eh = check_hole(tb, Eel, dE, &ne);
+            emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
+            emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
+            nev[3]++; nev[7] += 2;
+        } else {
+            dE = mott_transfer(C, Eel, hm, s);
+            angles_lat(C, Eel, dE, hm, s, th1, ph1);
+            Eh = check_hole(tb, Eel, dE, (P<T>*)nullptr);
+            const int i = find_monoton(C.tg, C.Nt, tev);
+            const int j = rbin(C, m_sqrt(X * X + Y * Y));
+            lat.add(tal, (i - 1) * C.NR + (j - 1), (double)dE);
+            nev[3]++;
+        }
+        T hp2, ht2;
+        new_angles(ph0, th0, th1, ph1, hp2, ht2);
+        h.t0 = tev; h.X = X; h.Y = Y; h.Z = Z; h.th = ht2; h.ph = hp2;
+        hole_parameters(C, tb, h, Eh + C.Egap, s);
+        cut_h(C, h);
+        if (h.Ek < T(-1.0e-9) || m_isnan(h.Ek)) err |= TREKIS_ERR_NEG_ENERGY_H;
+        emit_hole(C, tal, h);
+        return;
+    }
+    // deep hole: Auger vs radiative decay (MC:2739-2868)
+    const int KS = h.sh;
+    const T IpK = C.Ip[KS];
+    const T RN = s.next();
+    const T tA = C.Auger[KS], tR = C.Radiat[KS];
+    auto count_sh = [&](T NRG, bool second) {  // count_for_Auger_shells (MC:1576-1608)
+        T coun = T(0);
+        for (int q = 0; q < C.nsh; ++q) {
+            T Ed = second ? T(1.0e10) : NRG - C.Ip[q];
+            if (NRG > C.Ip[q] + T(1.0e-3) && Ed >= C.Egap) coun += C.Nel[q];
+        }
+        return coun;
+    };
+    auto choose_sh = [&](T NRG, T Shel, bool second, int def) {  // Choose_for_Auger_shell (MC:1610-1647)
+        T cs = T(0);
+        for (int q = 0; q < C.nsh; ++q) {
+            T Ed = second ? T(1.0e10) : NRG - C.Ip[q];
+            if (NRG > C.Ip[q] + T(1.0e-3) && Ed >= C.Egap) {
+                cs += C.Nel[q];
+                if (cs >= Shel) return q;
+            }
+        }
+        return def;
+    };
+    if (RN * (T(1) / tA + T(1) / tR) < T(1) / tA) {  // Auger_decay (MC:1366-1443)
+        T coun = count_sh(IpK, false);
+        T Shel = s.next() * coun;
+        const int K1 = choose_sh(IpK, Shel, false, KS);
+        T dEc = (K1 == C.vb) ? from_where_in_vb(tb, s, false, T(0)) : T(0);
+        const T En1 = dEc + C.Ip[K1];
+        const T Ed = IpK - En1;
+        coun = count_sh(Ed, true);
+        int K2 = -1;
+        T En2 = T(0), Ee = T(-1.0e-10);
+        if (coun > T(0)) {
+            Shel = s.next() * coun;
+            K2 = choose_sh(Ed, Shel, true, -1);
+            if (K2 >= 0) {
+                dEc = (K2 == C.vb) ? from_where_in_vb(tb, s, true, Ed - C.Ip[K2]) : T(0);
+                En2 = dEc + C.Ip[K2];
+                Ee = Ed - En2;
+            }
+        }
+        if (Ee < T(0) || En1 < T(0) || En2 < T(0)) err |= TREKIS_ERR_AUGER;
+        if (K2 >= 0) {
+            h.th = pi_<T>() * s.next();
+            h.ph = T(2) * pi_<T>() * s.next();
+            h.t0 = h.tn; h.sh = K1;
+            hole_parameters(C, tb, h, En1, s);
+            cut_h(C, h);
+            P<T> hh;
+            hh.pid = child_pid(h.pid, ord, 1); hh.ord = 0;
+            make_hole(C, tb, hh, h.t0, h.X, h.Y, h.Z, K2, En2, s, err);
+            P<T> ne;
+            ne.pid = child_pid(h.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+            ne.E = Ee; ne.t0 = h.t0;
+            electron_flight(tb, ne, s);
+            ne.ph = T(2) * pi_<T>() * s.next();
+            ne.th = pi_<T>() * s.next();
+            ne.X = h.X; ne.Y = h.Y; ne.Z = h.Z;
+            cut_e(C, ne);
+            if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
+            emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
+            emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
+            nev[7] += 2;
+        } else {
+            h.t0 = h.tn; h.tn = T(1.0e21);
+        }
+        emit_hole(C, tal, h);
+        nev[4]++;
+    } else {  // Radiative_decay (MC:2969-2997)
+        T coun = count_sh(IpK, true);
+        T Shel = s.next() * coun;
+        const int K1 = choose_sh(IpK, Shel, true, KS);
+        T dEc = (K1 == C.vb) ? from_where_in_vb(tb, s, false, T(0)) : T(0);
+        const T En1 = dEc + C.Ip[K1];
+        const T dE = IpK - En1;
+        h.th = pi_<T>() * s.next();
+        h.ph = T(2) * pi_<T>() * s.next();
+        h.t0 = h.tn; h.sh = K1;
+        hole_parameters(C, tb, h, En1, s);
+        cut_h(C, h);
+        P<T> pp;
+        pp.pid = child_pid(h.pid, ord, 2); pp.ord = 0; pp.sh = 0; pp.Ek = T(0); pp.M = T(0);
+        const T Ip_ = nfp2(Tab<T>{tb.pE, tb.pIMFP, tb.nP}, dE);
+        const T RN2 = s.next();
+        const T Mt = -m_log(RN2) * Ip_;
+        pp.ph = T(2) * pi_<T>() * s.next();
+        pp.th = pi_<T>() * s.next();
+        pp.E = dE; pp.t0 = h.t0; pp.X = h.X; pp.Y = h.Y; pp.Z = h.Z; pp.L = Mt;
+        pp.tn = tn_of(pp.t0, Mt, T(kC));
+        if (pp.E < T(-1.0e-9) || m_isnan(pp.E)) err |= TREKIS_ERR_PHOTON_ENERGY;
+        emit_hole(C, tal, h);
+        emit_photon(C, tal, pp); push(C, tal, o, 2, pp);
+        nev[5]++; nev[7] += 1;
+    }
+}
+
+template <class T>
+__device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& p,
+                             unsigned& err, unsigned long long* nev) {
+    const uint32_t ord = p.ord++;
+    EvStream<T> s(C.seed, p.pid, ord);
+    const T Eel = p.E;
+    const T X = p.X + p.L * m_sin(p.th) * m_sin(p.ph);
+    const T Y = p.Y + p.L * m_sin(p.th) * m_cos(p.ph);
+    const T Z = p.Z + p.L * m_cos(p.th);
+    const int k = which_shell(C, tb.pE, tb.pL, tb.nP, Eel, s.next());
+    const T dEc = electron_receives(C, tb, Eel, k, s, err);
+    P<T> ne;
+    ne.pid = child_pid(p.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+    ne.E = dEc; ne.t0 = p.tn;
+    electron_flight(tb, ne, s);
+    T ph1, th1;
+    new_angles(p.ph, p.th, pi_<T>() / T(2), T(0), ph1, th1);
+    ne.X = X; ne.Y = Y; ne.Z = Z; ne.th = th1; ne.ph = ph1;
+    cut_e(C, ne);
+    if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
+    P<T> hh;
+    hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0;
+    make_hole(C, tb, hh, p.tn, X, Y, Z, k, Eel - dEc, s, err);
+    if (hh.E + hh.Ek < C.Egap) err |= TREKIS_ERR_HOLE_IN_GAP;
+    emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
+    emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
+    // absorbed: the photon leaves the queues (its slot is not reused, unlike MC:2963)
+    p.E = T(0); p.tn = T(1.0e27);
+    nev[6]++; nev[7] += 2;
+}
+
+// One wavefront step: each thread runs up to K events of one particle.
+template <class T>
+__global__ void __launch_bounds__(256) k_step(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> ie, int ne,
+                                              PQ<T> ih, int nh, PQ<T> ip, int np, Out<T> o, Tal tal, int K,
+                                              int blocks_e, int blocks_h) {
+    const McConst<T>& C = *Cp;
+    int kind, idx;
+    if ((int)blockIdx.x < blocks_e) { kind = 0; idx = blockIdx.x * blockDim.x + threadIdx.x; if (idx >= ne) return; }
+    else if ((int)blockIdx.x < blocks_e + blocks_h) { kind = 1; idx = (blockIdx.x - blocks_e) * blockDim.x + threadIdx.x; if (idx >= nh) return; }
+    else { kind = 2; idx = (blockIdx.x - blocks_e - blocks_h) * blockDim.x + threadIdx.x; if (idx >= np) return; }
+    const PQ<T>& in = kind == 0 ? ie : kind == 1 ? ih : ip;
+    P<T> p;
+    load(in, idx, p);
+    unsigned err = 0;
+    unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    LatAcc lat;
+    for (int e = 0; e < K && p.tn < C.Tim; ++e) {
+        if (kind == 0) electron_event(C, tb, tal, o, p, err, lat, nev);
+        else if (kind == 1) hole_event(C, tb, tal, o, p, err, lat, nev);
+        else photon_event(C, tb, tal, o, p, err, nev);
+    }
+    lat.flush(tal);
+    if (p.tn < C.Tim) push(C, tal, o, kind, p);
+    for (int q = 1; q < 8; ++q)
+        if (nev[q]) atomicAdd(&o.ctr->ev[q], nev[q]);
+    if (err) atomicOr(&o.ctr->err_bits, err);
+}
+
+template <class T>
+void launch_shi(const McConst<T>* C, const DevTabs<T>& tb, const DevShi& sh, PQ<T> qe, PQ<T> qh, Tal tal, Ctrs* ctr,
+                int nit, int bs, cudaStream_t s) {
+    bs = bs > 128 ? 128 : bs;
+    k_shi<T><<<(nit + bs - 1) / bs, bs, 0, s>>>(C, tb, sh, qe, qh, tal, ctr, nit);
+}
+
+template <class T>
+void launch_step(const McConst<T>* C, const DevTabs<T>& tb, PQ<T> ie, int ne, PQ<T> ih, int nh, PQ<T> ip, int np,
+                 PQ<T> oe, PQ<T> oh, PQ<T> op, Tal tal, Ctrs* ctr, int K, int bs, cudaStream_t s) {
+    int be = (ne + bs - 1) / bs, bh = (nh + bs - 1) / bs, bp = (np + bs - 1) / bs;
+    if (be + bh + bp == 0) return;
+    Out<T> o{oe, oh, op, ctr};
+    k_step<T><<<be + bh + bp, bs, 0, s>>>(C, tb, ie, ne, ih, nh, ip, np, o, tal, K, be, bh);
+}
+
+template void launch_shi<float>(const McConst<float>*, const DevTabs<float>&, const DevShi&, PQ<float>, PQ<float>, Tal,
+                                Ctrs*, int, int, cudaStream_t);
+template void launch_shi<double>(const McConst<double>*, const DevTabs<double>&, const DevShi&, PQ<double>, PQ<double>,
+                                 Tal, Ctrs*, int, int, cudaStream_t);
+template void launch_step<float>(const McConst<float>*, const DevTabs<float>&, PQ<float>, int, PQ<float>, int,
+                                 PQ<float>, int, PQ<float>, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, cudaStream_t);
+template void launch_step<double>(const McConst<double>*, const DevTabs<double>&, PQ<double>, int, PQ<double>, int,
+                                  PQ<double>, int, PQ<double>, PQ<double>, PQ<double>, Tal, Ctrs*, int, int,
+                                  cudaStream_t);
+
+// ---- finalize: difference arrays -> FP64 tallies -----------------------------------------
+// One thread per (slice, bin): prefix over time rows, in place (exact int64).
+__global__ void k_prefix(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR,
+                         int ns) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns * NR) return;
+    const int s = t / NR, j = t % NR;
+    long long c = 0, e = 0, k = 0;
+    for (int r = 1; r <= Nt; ++r) {
+        size_t a = ((size_t)r * ns + s) * NR + j;
+        c += (long long)cnt[a]; cnt[a] = (unsigned long long)c;
+        e += (long long)en[a]; en[a] = (unsigned long long)e;
+        if (ek) { k += (long long)ek[a]; ek[a] = (unsigned long long)k; }
+    }
+}
+// One thread per (slice, row): weighted bins and per-time totals.
+__global__ void k_fin(const unsigned long long* cnt, const unsigned long long* en, const unsigned long long* ek,
+                      int Nt, int NR, int ns, const double* V, double* on, double* oE, double* oK, double* tn_,
+                      double* tE) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns * Nt) return;
+    const int s = t / Nt, i = t % Nt;
+    long long sc = 0, se = 0;
+    for (int j = 0; j < NR; ++j) {
+        size_t a = ((size_t)(i + 1) * ns + s) * NR + j;
+        long long c = (long long)cnt[a], e = (long long)en[a];
+        size_t o = (size_t)i + (size_t)Nt * (j + (size_t)NR * s);
+        on[o] += (double)c * V[j];
+        oE[o] += (double)e / kEScale * V[j];
+        sc += c; se += e;
+        if (ek) { long long k = (long long)ek[a]; oK[o] += (double)k / kEScale * V[j]; se += k; }
+    }
+    if (tn_) tn_[i + (size_t)Nt * s] += (double)sc;
+    if (tE) tE[i + (size_t)Nt * s] += (double)se / kEScale;
+}
+__global__ void k_fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t != 0) return;
+    long long cum = 0;
+    for (int i = 0; i < Nt; ++i) {
+        for (int j = 0; j < NR; ++j) {
+            long long v = (long long)lat[(size_t)i * NR + j];
+            oL[(size_t)i + (size_t)Nt * j] += (double)v / kLatScale * V[j];
+            cum += v;
+        }
+        Eat[i] += (double)cum / kLatScale;
+    }
+}
+
+void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
+               const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s) {
+    int n1 = ns * NR;
+    k_prefix<<<(n1 + 127) / 128, 128, 0, s>>>(cnt, en, ek, Nt, NR, ns);
+    int n2 = ns * Nt;
+    k_fin<<<(n2 + 127) / 128, 128, 0, s>>>(cnt, en, ek, Nt, NR, ns, V, on, oE, oK, tn_, tE);
+}
+void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat, cudaStream_t s) {
+    k_fin_lat<<<1, 32, 0, s>>>(lat, Nt, NR, V, oL, Eat);
+}
+}  // namespace tk

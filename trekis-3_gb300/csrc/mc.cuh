@@ -1,0 +1,71 @@
+// mc.cuh -- data layout of the event-based wavefront (shared by mc.cu and capi.cu).
+#pragma once
+#include <cstdint>
+#include "common.cuh"
+#include "impl.h"
+
+namespace tk {
+
+// Run constants, in the precision T of the kinematics (SHI quantities stay FP64).
+template <class T>
+struct McConst {
+    int nsh, nat, vb, include_photons;
+    int atom_of[MAXSH];
+    T Ip[MAXSH], Nel[MAXSH], Auger[MAXSH], Radiat[MAXSH];
+    int Zat[TREKIS_MAX_ATOMS];
+    T Mass_kg[TREKIS_MAX_ATOMS], Pers[TREKIS_MAX_ATOMS], Z23[TREKIS_MAX_ATOMS];
+    T Psum, Mtarget, Egap, cut_off, hole_mass;
+    double Layer;
+    // ion (FP64)
+    int ion_Z, ion_kind_zeff;
+    double ion_mass_p, MSHI, ion_E0, ion_fixed_zeff, Zt, Ipd[MAXSH];
+    // time / radial grids
+    T Tim;
+    int Nt, NR;
+    const T* tg;        // [Nt] tallied times
+    const T* Rg;        // [NR] outer radii
+    uint64_t seed;
+    int64_t it0;        // global index of iteration 0 of the batch
+    int mobile_holes;   // hole_mass < 1e3
+    T mec2, alpha;      // electron rest energy [eV], fine-structure constant
+};
+
+// Structure-of-arrays particle queue.
+template <class T>
+struct PQ {
+    T *E, *t0, *tn, *X, *Y, *Z, *L, *th, *ph, *Ek, *M;
+    uint64_t* pid;
+    uint32_t* ord;
+    uint16_t* sh;
+    int64_t cap;
+};
+
+// int64 fixed-point tallies of one batch.  *_cnt/_E/_Ek are difference
+// arrays over the time index (rows 0..Nt+1); lat is per interval.
+struct Tal {
+    unsigned long long *e_cnt, *e_E, *p_cnt, *p_E, *h_cnt, *h_E, *h_Ek, *lat;
+};
+
+constexpr double kEScale = 16777216.0;      // 2^24 per eV for particle energies
+constexpr double kLatScale = 1099511627776.0;  // 2^40 per eV for lattice energy
+
+// Counters written by the kernels.
+struct Ctrs {
+    int n_out[3];                 // appended electrons, holes, photons
+    int overflow;
+    unsigned int err_bits;
+    int first_bad_it;
+    unsigned long long ev[8];     // shi, el inel, el elastic, hole, auger, radiative, photon abs, particles
+};
+
+template <class T>
+void launch_shi(const McConst<T>* C, const DevTabs<T>& tb, const DevShi& sh, PQ<T> qe, PQ<T> qh, Tal tal,
+                Ctrs* ctr, int nit, int bs, cudaStream_t s);
+template <class T>
+void launch_step(const McConst<T>* C, const DevTabs<T>& tb, PQ<T> ie, int ne, PQ<T> ih, int nh, PQ<T> ip, int np,
+                 PQ<T> oe, PQ<T> oh, PQ<T> op, Tal tal, Ctrs* ctr, int K, int bs, cudaStream_t s);
+void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
+               const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s);
+void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat, cudaStream_t s);
+
+}  // namespace tk

@@ -1,0 +1,535 @@
+// tables.cu -- FP64 cross-section table build on the GPU.
+//
+// Restates, as data-parallel kernels, the reference's table build:
+//   TotIMFP                 Cross_sections.f90:881-1050   (electron/hole IMFP + cumulative rows)
+//   Diff_cross_section      Cross_sections.f90:2217-2282  (q-integral of Im(-1/eps)/q)
+//   SHI_TotIMFP             Cross_sections.f90:2452-2597  (SHI IMFP, dE/dx, transfer rows)
+//   SHI_Diff_cross_section  Cross_sections.f90:2683-2744
+//   Loss_func / Imewq       Cross_sections.f90:346-486
+//   define_dE               Cross_sections.f90:1374-1412
+// Work decomposition: one "job" is one (shell, energy node) integral.  The
+// omega steps of a job are counted (k_count), their abscissae laid out
+// (k_points), every q-integral is evaluated by its own thread (k_diff, the
+// FP64-heavy kernel) and each job's Simpson sum is accumulated in order
+// (k_accum), which keeps the summation order of the reference.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include "common.cuh"
+#include "impl.h"
+
+namespace tk {
+
+struct Job {
+    double Ele, Emin, Emax, Mass, E_low, E_high, Zeff;
+    int sh, kind, n, store;     // kind 0: electron/hole, 1: SHI
+    int n_steps, nsiz;
+    int64_t pt_off, row_off;
+    int row_len;
+};
+
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { set_error(std::string(#x) + ": " + cudaGetErrorString(e_)); return TREKIS_ECUDA; } } while (0)
+
+__device__ __forceinline__ double d_define_dE(int n, double E, double lo, double hi, double dmin) {
+    double dE = (E > lo && E < hi) ? (hi - lo) / (double)n : E / (double)n;
+    return dE > dmin ? dE : dmin;
+}
+
+// Loss_func + Extend_E0_to_finite_q (Cross_sections.f90:346-486), summed over oscillators (Imewq)
+__device__ double d_imewq(const BuildMat* __restrict__ bm, int sh, double hw, double hq) {
+    double Mass;
+    if (bm->dos_mass) {
+        double qlim = fabs(hq) * sqrt(kE);
+        if (qlim <= bm->dos_k[bm->N_dos - 1]) Mass = bm->dos_Eff_m[find_monoton(bm->dos_k, bm->N_dos, qlim) - 1];
+        else Mass = 1.0;
+    } else Mass = bm->El_eff_mass > 0 ? bm->El_eff_mass : 1.0;
+    const double hq2 = kH * kH * hq * hq;
+    const double sqq = hq2 / (2.0 * Mass * kMe);
+    const double dE2 = hw * hw;
+    double sum = 0.0;
+    const int no = bm->nosc[sh];
+    for (int i = 0; i < no; ++i) {
+        double E = bm->E0[sh * MAXOSC + i], G = bm->G[sh * MAXOSC + i], A = bm->A[sh * MAXOSC + i];
+        double E0, G1;
+        if (bm->kind_of_DR == 2) { E0 = sqrt(E * E + bm->v_f * bm->v_f * hq2 * 0.3333333333333 + sqq * sqq); G1 = G; }
+        else if (bm->kind_of_DR == 3) { E0 = pow(pow(E, 0.666666666666) + pow(sqq, 0.666666666666), 1.5); G1 = sqrt(G * G + sqq * sqq); }
+        else { E0 = E + sqq; G1 = G; }
+        double E02 = E0 * E0;
+        sum += A * G1 * hw / ((dE2 - E02) * (dE2 - E02) + G1 * G1 * dE2);
+    }
+    return sum;
+}
+
+// Diff_cross_section (Cross_sections.f90:2217-2282)
+__device__ double d_diff_cs(const BuildMat* __restrict__ bm, int sh, double Ele, double hw, double Mass) {
+    const double pre = sqrt(2.0 * Mass * kMe) / kH;
+    double qmin, qmax;
+    if (hw > Ele) { qmin = pre * sqrt(Ele); qmax = qmin; }
+    else { qmin = pre * (sqrt(Ele) - sqrt(Ele - hw)); qmax = pre * (sqrt(Ele) + sqrt(Ele - hw)); }
+    double dLs = 0.0, hq = qmin, dLs0 = 0.0;
+    while (hq < qmax) {
+        double dq = hq / 100.0;
+        double t1 = d_imewq(bm, sh, hw, hq + dq / 2.0);
+        double dL = d_imewq(bm, sh, hw, hq + dq);
+        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) / hq;
+        dLs0 = dL;
+        hq = hq + dq;
+    }
+    double T = (bm->temp > 0.0) ? 1.0 / (1.0 - exp(-hw / bm->temp * kKb)) : 1.0;
+    return 1.0 / (kPi * kA0 * Ele) * dLs * T;
+}
+
+// SHI_Diff_cross_section (Cross_sections.f90:2683-2744)
+__device__ double d_shi_diff(const BuildMat* __restrict__ bm, int sh, double Ele, double MSHI, double Emax, double hw) {
+    double qmin = (Ele > 0.0) ? hw / kH / sqrt(2.0 * Ele / MSHI) : 0.0;
+    if (!(Emax > 0.0)) return 0.0;
+    double qmax = sqrt(2.0 * kMe) / kH * sqrt(Emax);
+    double dLs = 0.0, hq = qmin, dLs0 = 0.0;
+    while (hq < qmax) {
+        double dq = hq / 100.0;
+        double t1 = d_imewq(bm, sh, hw, hq + dq / 2.0);
+        double dL = d_imewq(bm, sh, hw, hq + dq);
+        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) / hq;
+        dLs0 = dL;
+        hq = hq + dq;
+    }
+    double T = (bm->temp > 0.0) ? 1.0 / (1.0 - exp(-hw / bm->temp * kKb)) : 1.0;
+    return dLs * T;
+}
+
+__global__ void k_count(Job* jobs, int nj) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nj) return;
+    Job& J = jobs[j];
+    int c = 0;
+    for (double E = J.Emin; E <= J.Emax;) { ++c; E = E + d_define_dE(J.n, E, J.E_low, J.E_high, 0.001); }
+    int s = 0;   // get_diff_CS_grid_size (Cross_sections.f90:1278): steps counted from E_low
+    for (double E = J.E_low; E <= J.Emax;) { ++s; E = E + d_define_dE(J.n, E, J.E_low, J.E_high, 0.001); }
+    J.n_steps = c;
+    J.nsiz = s > 10 ? s : 10;
+}
+
+__global__ void k_points(const Job* __restrict__ jobs, int nj, double* __restrict__ pts, int* __restrict__ pjob) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nj) return;
+    const Job J = jobs[j];
+    int64_t p = J.pt_off;
+    pts[p] = J.Emin; pjob[p] = j; ++p;
+    double E = J.Emin;
+    for (int i = 0; i < J.n_steps; ++i) {
+        double dE = d_define_dE(J.n, E, J.E_low, J.E_high, 0.001);
+        pts[p] = E + dE / 2.0; pjob[p] = j; ++p;
+        pts[p] = E + dE; pjob[p] = j; ++p;
+        E = E + dE;
+    }
+}
+
+__global__ void k_diff(const BuildMat* __restrict__ bm, const Job* __restrict__ jobs, const double* __restrict__ pts,
+                       const int* __restrict__ pjob, double* __restrict__ val, int64_t np) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const Job& J = jobs[pjob[p]];
+    val[p] = (J.kind == 0) ? d_diff_cs(bm, J.sh, J.Ele, pts[p], J.Mass)
+                           : d_shi_diff(bm, J.sh, J.Ele, J.Mass, J.Emax, pts[p]);
+}
+
+// Simpson accumulation in the reference's order; writes (Sigma, dEdx) and rows
+__global__ void k_accum(const Job* __restrict__ jobs, int nj, const double* __restrict__ val,
+                        double* __restrict__ sig, double* __restrict__ dedx,
+                        double* __restrict__ rhw, double* __restrict__ rL, double* __restrict__ rX) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nj) return;
+    const Job J = jobs[j];
+    const double* v = val + J.pt_off;
+    double Ltot0 = v[0], Ltot1 = 0.0, dd = 0.0, E = J.Emin;
+    const double pref = kPi * kA0 * J.Ele * kMe / (J.Mass * J.Zeff * J.Zeff);
+    for (int i = 0; i < J.n_steps; ++i) {
+        double dE = d_define_dE(J.n, E, J.E_low, J.E_high, 0.001);
+        double t1 = v[1 + 2 * i], dL = v[2 + 2 * i];
+        double t2 = dE / 6.0 * (Ltot0 + 4.0 * t1 + dL);
+        Ltot1 += t2;
+        if (J.kind == 0) dd += E * t2;
+        else dd += dE / 6.0 * (E * Ltot0 + (E + dE / 2.0) * 4.0 * t1 + (E + dE) * dL);
+        Ltot0 = dL;
+        if (J.store == 1) { rhw[J.row_off + i] = E + dE; rL[J.row_off + i] = Ltot1; }
+        if (J.store == 2) { rhw[J.row_off + i] = E; rL[J.row_off + i] = pref / Ltot1; rX[J.row_off + i] = pref / dd; }
+        E = E + dE;
+    }
+    if (J.kind == 0) {
+        if (Ltot1 < 1.0e-15) { sig[j] = 1.0e20; dedx[j] = 0.0; }
+        else { sig[j] = 1.0 / (J.Mass * Ltot1); dedx[j] = J.Mass * dd; }
+        if (J.store == 1) {
+            for (int i = J.n_steps; i < J.row_len; ++i) { rhw[J.row_off + i] = 0.0; rL[J.row_off + i] = 0.0; }
+            for (int i = 0; i < J.row_len; ++i) {
+                double c = rL[J.row_off + i];
+                rL[J.row_off + i] = (c < 1.0e-15) ? 1.0e15 : 1.0 / (J.Mass * c);
+            }
+        }
+    } else {
+        double inv = 1.0 / (kPi * kA0 * J.Ele) * J.Mass / kMe * J.Zeff * J.Zeff * Ltot1;
+        sig[j] = inv > 1e30 ? 1e30 : inv;
+        dedx[j] = 1.0 / (kPi * kA0 * J.Ele) * J.Mass / kMe * J.Zeff * J.Zeff * dd;
+    }
+}
+
+// ---- host side -------------------------------------------------------------------
+
+static int order_of_number(double num) {  // find_order_of_number_real (Analytical_IMFPs.f90:3065)
+    char buf[64];
+    if (num > 1e9) {
+        snprintf(buf, sizeof buf, "%lld", (long long)std::ceil(num / 1.0e8));
+        return 8 + (int)strlen(buf);
+    }
+    snprintf(buf, sizeof buf, "%lld", (long long)std::ceil(num));
+    return (int)strlen(buf);
+}
+
+// get_grid_4CS / go_thru_grid (Analytical_IMFPs.f90:2815-2949)
+std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax) {
+    std::vector<double> sp;
+    for (int a = 0; a < m.N_atoms; ++a)
+        for (int s = 0; s < m.atoms[a].N_shl; ++s) sp.push_back(m.atoms[a].Ip[s]);
+    std::sort(sp.begin(), sp.end());
+    std::vector<double> uniq;   // exclude_doubles: keep the last of equal values
+    for (size_t i = 0; i < sp.size(); ++i) {
+        bool later = false;
+        for (size_t k = i + 1; k < sp.size(); ++k) later |= (sp[k] == sp[i]);
+        if (!later) uniq.push_back(sp[i]);
+    }
+    const double dmin = 0.01, eps = 1.0e-3;
+    std::vector<double> g;
+    size_t c = 0;
+    double E = Emin - dmin;
+    while (E < Emax) {
+        double dE = (E < 0.1 - dmin * 0.5) ? dmin
+                  : (E < 10.0 - dmin * 0.5) ? dmin * 10.0
+                  : (E < 100.0 - dmin * 0.5) ? dmin * 100.0
+                  : std::pow(10.0, order_of_number(E) - 2);
+        E = E + dE;
+        g.push_back(E);
+        if (c < uniq.size() && E >= uniq[c] && (E - dE) < uniq[c]) {
+            ++c;
+            g.push_back(uniq[c - 1] - eps);
+            g.push_back(uniq[c - 1] + eps);
+        }
+    }
+    std::stable_sort(g.begin(), g.end());
+    return g;
+}
+
+static double zeff_of(const trekis_ion& ion, const trekis_material& m, double E) {  // CS:2641-2680
+    double vp = E > 0 ? std::sqrt(2.0 * E * kE / (ion.Mass * kMp)) : 0.0;
+    double zs = 0, ps = 0;
+    for (int a = 0; a < m.N_atoms; ++a) { zs += m.atoms[a].Zat * m.atoms[a].Pers; ps += m.atoms[a].Pers; }
+    double Zt = zs / ps, Zp = ion.Zat, v0 = std::sqrt(2.0 * kRy * kE / kMe);
+    switch (ion.Kind_Zeff) {
+    case 1: return Zp * (1.0 - std::exp(-(vp / v0 / std::pow(Zp, 0.66666666))));
+    case 2: return Zp * std::pow(1.0 + std::pow(vp / (std::pow(Zp, 0.45) * v0 * 4.0 / 3.0), -1.0 / 0.6), -0.6);
+    case 3: {
+        double c1 = 1.0 - 0.26 * std::exp(-Zt / 11.0 - (Zt - Zp) * (Zt - Zp) / 9.0);
+        double vpvo = std::pow(Zp, -0.543) * vp / v0, c2 = 1.0 + 0.03 * vpvo * std::log(Zt);
+        double x = c1 * std::pow(vpvo / c2 / 1.54, 1.0 + 1.83 / Zp), x2 = x * x, x4 = x2 * x2;
+        return Zp * (8.29 * x + x4) / (0.06 / x + 4.0 + 7.4 * x + x4);
+    }
+    case 4: return ion.fixed_Zeff;
+    default: return Zp * (1.0 - std::exp(-(vp * 125.0 / kC / std::pow(Zp, 0.66666666))));
+    }
+}
+
+static int find_mono_h(const double* A, int N, double V) {
+    if (V < A[0]) return 1;
+    if (V >= A[N - 1]) return N;
+    int i1 = 1, i2 = N;
+    while (i1 != i2 - 1) { int ic = (i1 + i2) / 2; if (A[ic - 1] <= V) i1 = ic; else i2 = ic; }
+    return i1 + 1;
+}
+
+// integration limits of TotIMFP / Electron_energy_transfer_inelastic (CS:903-948)
+static void limits_eh(const trekis_tables* T, int a, int s, double Ele, bool hole, Job& J) {
+    const trekis_material& m = T->mat;
+    double Emin = m.atoms[a].Ip[s], Egap = m.atoms[0].Ip[m.atoms[0].N_shl - 1];
+    if (Emin <= 1.0e-3) Emin = 1.0e-3;
+    double Emax, Mass;
+    if (hole) {
+        Mass = (m.hole_mass >= 0) ? m.hole_mass : T->dos_M[find_mono_h(T->dos_E.data(), (int)T->dos_E.size(), Ele) - 1];
+        Emax = 4.0 * Ele * Mass / ((Mass + 1.0) * (Mass + 1.0));
+    } else { Emax = (Ele + Emin) / 2.0; Mass = 1.0; }
+    if (m.plasmon_Emax && Emin == Egap) {
+        double Ep = std::sqrt(m.N_VB_el * m.At_Dens * 1e6 * kH * kH / (kMe * kE0) + Egap * Egap);
+        if (Ep >= Emax) Emax = Ep;
+        if (Ele < Emax) Emax = Ele;
+    }
+    double mn = 1e300, mx = -1e300;
+    for (int i = 0; i < m.atoms[a].N_osc[s]; ++i) {
+        mn = std::min(mn, m.atoms[a].E0[s][i] - 5.0 * m.atoms[a].Gamma[s][i]);
+        mx = std::max(mx, m.atoms[a].E0[s][i] + 5.0 * m.atoms[a].Gamma[s][i]);
+    }
+    J.Ele = Ele; J.Emin = Emin; J.Emax = Emax; J.Mass = Mass;
+    J.E_low = std::max(mn, Emin); J.E_high = std::min(mx, Emax);
+    J.kind = 0; J.n = 100; J.Zeff = 1.0;
+}
+
+static void limits_shi(const trekis_tables* T, int a, int s, double Ele, Job& J) {
+    const trekis_material& m = T->mat;
+    double MSHI = kMp * T->ion.Mass, Egap = m.atoms[0].Ip[m.atoms[0].N_shl - 1];
+    double Emin = m.atoms[a].Ip[s];
+    if (Emin <= 1.0e-3) Emin = 1.0e-3;
+    double Emax = 4.0 * Ele * kMe * MSHI / ((MSHI + kMe) * (MSHI + kMe));
+    if (m.plasmon_Emax && Emin == Egap) {
+        double Ep = std::sqrt(m.N_VB_el * m.At_Dens * 1e6 * kH * kH / (kMe * kE0) + Egap * Egap);
+        if (Ep >= Emax) Emax = Ep;
+    }
+    double mn = 1e300, mx = -1e300;
+    for (int i = 0; i < m.atoms[a].N_osc[s]; ++i) {
+        mn = std::min(mn, m.atoms[a].E0[s][i] - 5.0 * m.atoms[a].Gamma[s][i]);
+        mx = std::max(mx, m.atoms[a].E0[s][i] + 5.0 * m.atoms[a].Gamma[s][i]);
+    }
+    J.Ele = Ele; J.Emin = Emin; J.Emax = Emax; J.Mass = MSHI;
+    J.E_low = std::max(mn, Emin); J.E_high = std::min(mx, Emax);
+    J.kind = 1; J.n = 1000; J.Zeff = zeff_of(T->ion, m, Ele);
+}
+
+// Mott atomic elastic cross section [cm^2] (Cross_sections.f90:3495-3514)
+static double mott_sigma(int Zi, double Ee) {
+    double Z = Zi, mec2e = kMe * kC * kC / kE, Z137 = Z / 137.0, RyEe = kRy / Ee, b2 = 2.0 * Ee / mec2e;
+    double pc = 1.7e-5 * std::pow(Z, 2.0 / 3.0) * (1.0 - b2) / b2;
+    double nc = pc * (1.13 + 3.76 * (Z137 * Z137) / b2 * std::sqrt(Ee / (Ee + mec2e)));
+    return kPi * kA0 * kA0 * Z * (Z + 1.0) / (nc * (nc + 1.0)) * RyEe * RyEe * 1e-16;
+}
+
+int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st) {
+    const trekis_material& m = T->mat;
+    cudaEvent_t ev0, ev1;
+    CK(cudaEventCreate(&ev0)); CK(cudaEventCreate(&ev1));
+    CK(cudaEventRecord(ev0));
+    // compact shells
+    T->nsh = 0;
+    for (int a = 0; a < m.N_atoms; ++a)
+        for (int s = 0; s < m.atoms[a].N_shl; ++s) {
+            if (T->nsh >= MAXSH) { set_error("too many shells"); return TREKIS_EINVAL; }
+            T->atom_of[T->nsh] = a; T->shell_of[T->nsh] = s; T->shell_index[a][s] = T->nsh; ++T->nsh;
+        }
+    const int nsh = T->nsh;
+    BuildMat bm;
+    std::memset(&bm, 0, sizeof bm);
+    bm.nsh = nsh; bm.kind_of_DR = m.kind_of_DR; bm.El_eff_mass = m.El_eff_mass; bm.v_f = m.v_f; bm.temp = m.temp;
+    const bool metal = m.atoms[0].Ip[m.atoms[0].N_shl - 1] < 0.2;
+    bm.dos_mass = (m.El_eff_mass == 0.0 && m.N_dos > 0 && !metal) ? 1 : 0;
+    bm.N_dos = m.N_dos;
+    for (int k = 0; k < nsh; ++k) {
+        const trekis_atom& at = m.atoms[T->atom_of[k]];
+        int s = T->shell_of[k];
+        bm.nosc[k] = at.N_osc[s]; bm.Ip[k] = at.Ip[s];
+        for (int i = 0; i < at.N_osc[s]; ++i) {
+            bm.E0[k * MAXOSC + i] = at.E0[s][i]; bm.A[k * MAXOSC + i] = at.A[s][i]; bm.G[k * MAXOSC + i] = at.Gamma[s][i];
+        }
+    }
+    if (m.N_dos > 0) {
+        double* dk = (double*)T->buf.alloc(8 * m.N_dos);
+        double* dm = (double*)T->buf.alloc(8 * m.N_dos);
+        if (!dk || !dm) return TREKIS_ENOMEM;
+        CK(cudaMemcpy(dk, T->dos_k.data(), 8 * m.N_dos, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(dm, T->dos_M.data(), 8 * m.N_dos, cudaMemcpyHostToDevice));
+        bm.dos_k = dk; bm.dos_Eff_m = dm;
+    }
+    BuildMat* d_bm = (BuildMat*)T->buf.alloc(sizeof(BuildMat));
+    if (!d_bm) return TREKIS_ENOMEM;
+    CK(cudaMemcpy(d_bm, &bm, sizeof bm, cudaMemcpyHostToDevice));
+
+    // grids (Analytical_IMFPs.f90:144-158, 206-210, 2269-2273)
+    const double Emax_e = 175.6e6 * 2.0 / 1836.0;
+    std::vector<double> gE = grid_4CS(m, 0.1, Emax_e);
+    double dosmax = 0.0;
+    for (double x : T->dos_E) dosmax = std::max(dosmax, x);
+    std::vector<double> gH = grid_4CS(m, 0.1, dosmax + 1.0);
+    std::vector<double> gS;
+    const double Egap = m.atoms[0].Ip[m.atoms[0].N_shl - 1];
+    if (cfg.build_shi) {
+        double MK = T->ion.Mass * kMp;
+        gS = grid_4CS(m, std::ceil(((MK + kMe) * (MK + kMe) / (MK * kMe) * Egap / 4.0)), 175.6e6 / 2.0 * T->ion.Mass);
+    }
+    const int NE = (int)gE.size(), NH = (int)gH.size(), NS = (int)gS.size();
+    const int vb = T->shell_index[0][m.atoms[0].N_shl - 1];
+
+    // jobs
+    std::vector<Job> jobs;
+    jobs.reserve((size_t)nsh * (NE + NH + NS + 1));
+    for (int k = 0; k < nsh; ++k)
+        for (int i = 0; i < NE; ++i) {
+            Job J{}; limits_eh(T, T->atom_of[k], T->shell_of[k], gE[i], false, J); J.sh = k; J.store = 1; jobs.push_back(J);
+        }
+    const size_t j_h0 = jobs.size();
+    for (int k = 0; k < nsh; ++k)
+        for (int i = 0; i < NH; ++i) {
+            Job J{}; limits_eh(T, T->atom_of[k], T->shell_of[k], gH[i], true, J); J.sh = k; J.store = (k == vb) ? 1 : 0;
+            jobs.push_back(J);
+        }
+    const size_t j_s0 = jobs.size();
+    std::vector<int> shi_nodes;
+    if (cfg.build_shi) {
+        for (int i = 0; i < NS; ++i) {
+            bool in = true;
+            if (cfg.shi_E_window_lo > 0 && i + 1 < NS && gS[i + 1] < cfg.shi_E_window_lo) in = false;
+            if (cfg.shi_E_window_hi > 0 && i > 0 && gS[i - 1] > cfg.shi_E_window_hi) in = false;
+            if (in) shi_nodes.push_back(i);
+        }
+        for (int k = 0; k < nsh; ++k)
+            for (int i : shi_nodes) { Job J{}; limits_shi(T, T->atom_of[k], T->shell_of[k], gS[i], J); J.sh = k; J.store = 0; jobs.push_back(J); }
+    }
+    const size_t j_d0 = jobs.size();
+    if (cfg.build_shi)
+        for (int k = 0; k < nsh; ++k) { Job J{}; limits_shi(T, T->atom_of[k], T->shell_of[k], T->ion.E, J); J.sh = k; J.store = 2; jobs.push_back(J); }
+    const int nj = (int)jobs.size();
+
+    Job* d_jobs = (Job*)T->buf.alloc(sizeof(Job) * nj);
+    if (!d_jobs) return TREKIS_ENOMEM;
+    CK(cudaMemcpy(d_jobs, jobs.data(), sizeof(Job) * nj, cudaMemcpyHostToDevice));
+    const int bs = 128;
+    k_count<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj);
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(jobs.data(), d_jobs, sizeof(Job) * nj, cudaMemcpyDeviceToHost));
+    int64_t np = 0, nr = 0;
+    for (Job& J : jobs) {
+        J.pt_off = np; np += 1 + 2 * (int64_t)J.n_steps;
+        J.row_len = 0; J.row_off = nr;
+        if (J.store == 1) J.row_len = std::max(J.n_steps, J.nsiz);
+        if (J.store == 2) J.row_len = J.n_steps;
+        nr += J.row_len;
+    }
+    CK(cudaMemcpy(d_jobs, jobs.data(), sizeof(Job) * nj, cudaMemcpyHostToDevice));
+    tk::Buffers scratch;
+    double* d_pts = (double*)scratch.alloc(8 * np);
+    int* d_pj = (int*)scratch.alloc(4 * np);
+    double* d_val = (double*)scratch.alloc(8 * np);
+    double* d_sig = (double*)scratch.alloc(8 * nj);
+    double* d_ded = (double*)scratch.alloc(8 * nj);
+    double* d_rhw = (double*)scratch.alloc(8 * std::max<int64_t>(nr, 1));
+    double* d_rL = (double*)scratch.alloc(8 * std::max<int64_t>(nr, 1));
+    double* d_rX = (double*)scratch.alloc(8 * std::max<int64_t>(nr, 1));
+    if (!d_pts || !d_pj || !d_val || !d_sig || !d_ded || !d_rhw || !d_rL || !d_rX) return TREKIS_ENOMEM;
+    k_points<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj, d_pts, d_pj);
+    CK(cudaGetLastError());
+    k_diff<<<(unsigned)((np + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np);
+    CK(cudaGetLastError());
+    k_accum<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj, d_val, d_sig, d_ded, d_rhw, d_rL, d_rX);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ev1));
+    std::vector<double> sig(nj), ded(nj), rhw(nr), rL(nr), rX(nr);
+    CK(cudaMemcpy(sig.data(), d_sig, 8 * nj, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ded.data(), d_ded, 8 * nj, cudaMemcpyDeviceToHost));
+    if (nr) {
+        CK(cudaMemcpy(rhw.data(), d_rhw, 8 * nr, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(rL.data(), d_rL, 8 * nr, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(rX.data(), d_rX, 8 * nr, cudaMemcpyDeviceToHost));
+    }
+    float ms = 0.f;
+    CK(cudaEventSynchronize(ev1));
+    CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    T->build_ms = ms;
+    T->build_points = (uint64_t)np;
+    cudaEventDestroy(ev0); cudaEventDestroy(ev1);
+
+    // host mirror
+    T->el.assign(nsh, {}); T->hole.assign(nsh, {}); T->shi.assign(nsh, {}); T->dsde.assign(nsh, {});
+    T->phot.assign(nsh, {}); T->el_rows.assign(nsh, {});
+    for (int k = 0; k < nsh; ++k) {
+        HTab& t = T->el[k];
+        t.E = gE; t.L.resize(NE); t.dEdx.resize(NE);
+        HRowSet& R = T->el_rows[k];
+        R.E = gE; R.rows.resize(NE);
+        for (int i = 0; i < NE; ++i) {
+            const Job& J = jobs[(size_t)k * NE + i];
+            t.L[i] = sig[(size_t)k * NE + i]; t.dEdx[i] = ded[(size_t)k * NE + i];
+            R.rows[i].hw.assign(rhw.begin() + J.row_off, rhw.begin() + J.row_off + J.row_len);
+            R.rows[i].L.assign(rL.begin() + J.row_off, rL.begin() + J.row_off + J.row_len);
+        }
+        HTab& h = T->hole[k];
+        h.E = gH; h.L.resize(NH); h.dEdx.resize(NH);
+        for (int i = 0; i < NH; ++i) { h.L[i] = sig[j_h0 + (size_t)k * NH + i]; h.dEdx[i] = ded[j_h0 + (size_t)k * NH + i]; }
+    }
+    T->hole_rows.E = gH; T->hole_rows.rows.assign(NH, {});
+    for (int i = 0; i < NH; ++i) {
+        const Job& J = jobs[j_h0 + (size_t)vb * NH + i];
+        T->hole_rows.rows[i].hw.assign(rhw.begin() + J.row_off, rhw.begin() + J.row_off + J.row_len);
+        T->hole_rows.rows[i].L.assign(rL.begin() + J.row_off, rL.begin() + J.row_off + J.row_len);
+    }
+    if (cfg.build_shi) {
+        const int nn = (int)shi_nodes.size();
+        for (int k = 0; k < nsh; ++k) {
+            HTab& t = T->shi[k];
+            t.E = gS; t.L.assign(NS, 1.0e24); t.dEdx.assign(NS, 0.0);
+            for (int q = 0; q < nn; ++q) {
+                double inv = sig[j_s0 + (size_t)k * nn + q];
+                double L = (inv > 1.0e-10) ? 1.0 / inv : 1.0e28;
+                t.L[shi_nodes[q]] = L > 1e30 ? 1e30 : L;
+                t.dEdx[shi_nodes[q]] = ded[j_s0 + (size_t)k * nn + q];
+            }
+            const Job& J = jobs[j_d0 + k];
+            HTab& d = T->dsde[k];
+            d.E.assign(rhw.begin() + J.row_off, rhw.begin() + J.row_off + J.row_len);
+            d.L.assign(rL.begin() + J.row_off, rL.begin() + J.row_off + J.row_len);
+            d.dEdx.assign(rX.begin() + J.row_off, rX.begin() + J.row_off + J.row_len);
+        }
+        T->has_shi = true;
+    }
+    // elastic Mott MFPs (Elastic_cross_section, Cross_sections.f90:2939-2962): closed form
+    if (m.kind_of_EMFP != 0) { set_error("only the Mott elastic cross section is built"); return TREKIS_EUNSUPPORTED; }
+    double Psum = 0.0;
+    for (int a = 0; a < m.N_atoms; ++a) Psum += m.atoms[a].Pers;
+    auto mott = [&](const std::vector<double>& g, bool hole, HTab& t) {
+        t.E = g; t.L.resize(g.size()); t.dEdx.assign(g.size(), 0.0);
+        for (size_t i = 0; i < g.size(); ++i) {
+            double mass = 1.0;
+            if (hole) mass = (m.hole_mass >= 0) ? m.hole_mass
+                           : T->dos_M[find_mono_h(T->dos_E.data(), (int)T->dos_E.size(), g[i]) - 1];
+            double sgm = 0.0;
+            for (int a = 0; a < m.N_atoms; ++a) sgm += mott_sigma(m.atoms[a].Zat, g[i]) * m.atoms[a].Pers;
+            sgm = sgm / Psum * mass;
+            t.L[i] = 1.0e8 / (sgm * m.At_Dens);
+        }
+    };
+    mott(grid_4CS(m, 0.01, Emax_e), false, T->el_elast);
+    mott(grid_4CS(m, 0.01, dosmax + 1.0), true, T->hole_elast);
+    // photons (Tot_Phot_IMFP, Cross_sections.f90:833-878): Im(-1/eps) at q = 0
+    if (cfg.build_photon && m.include_photons) {
+        std::vector<double> gP = grid_4CS(m, 0.1, Emax_e);
+        for (int k = 0; k < nsh; ++k) {
+            const trekis_atom& at = m.atoms[T->atom_of[k]];
+            int s = T->shell_of[k];
+            HTab& t = T->phot[k];
+            t.E = gP; t.L.resize(gP.size()); t.dEdx.resize(gP.size());
+            for (size_t i = 0; i < gP.size(); ++i) {
+                double Ele = gP[i];
+                if (Ele < at.Ip[s]) { t.L[i] = 1e30; t.dEdx[i] = Ele / 1e30; continue; }
+                double ImE = 0.0;
+                for (int o = 0; o < at.N_osc[s]; ++o) {
+                    double E0 = at.E0[s][o], G = at.Gamma[s][o];
+                    ImE += at.A[s][o] * G * Ele / ((Ele * Ele - E0 * E0) * (Ele * Ele - E0 * E0) + G * G * Ele * Ele);
+                }
+                t.L[i] = kC * kH / (ImE * Ele * kE) * 1e10;
+                t.dEdx[i] = Ele / t.L[i];
+            }
+        }
+        T->has_phot = true;
+    }
+    // totals (How_many_electrons, Monte_Carlo.f90:1902-2057)
+    auto total = [&](const std::vector<HTab>& v, bool guard, HTab& out) {
+        out.E = v[0].E; out.L.assign(out.E.size(), 0.0); out.dEdx.assign(out.E.size(), 0.0);
+        for (int k = 0; k < nsh; ++k)
+            for (size_t i = 0; i < out.E.size(); ++i) {
+                if (!guard || v[k].L[i] > 1.0e-10) out.L[i] += 1.0 / v[k].L[i];
+                out.dEdx[i] += v[k].dEdx[i];
+            }
+        for (size_t i = 0; i < out.E.size(); ++i) out.L[i] = (out.L[i] < 1.0e-10) ? 1.0e30 : 1.0 / out.L[i];
+    };
+    total(T->el, true, T->El_IMFP);
+    total(T->hole, false, T->Hole_IMFP);
+    if (T->has_phot) total(T->phot, false, T->Phot_IMFP);
+    if (T->has_shi) total(T->shi, false, T->SHI_path);
+    if (st) st->n_kernel_launches += 4;
+    return TREKIS_OK;
+}
+
+}  // namespace tk

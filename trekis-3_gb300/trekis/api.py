@@ -1,0 +1,168 @@
+"""do_Monte_Carlo-style API over the C ABI.
+
+``Tables`` replaces the reference's table build (Analytical_ion_dEdx,
+Analytical_electron_dEdx and the SHI transfer table), ``mc_run`` replaces
+``do_Monte_Carlo`` (Source_files/Monte_Carlo.f90:39): it accumulates the
+un-normalised tallies of NMC iterations into arrays laid out as the Fortran
+``Out_*`` arrays (time index fastest).  Everything runs on the GPU through
+``libtrekis_gb300.so``; there is no CPU fallback.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+
+TALLY_2D = ("Out_ne", "Out_Ee", "Out_nphot", "Out_Ephot", "Out_Elat")
+TALLY_4D = ("Out_nh", "Out_Eh", "Out_Ehkin")
+TALLY_1D = ("Out_tot_Ne", "Out_tot_Nphot", "Out_tot_E", "Out_E_e", "Out_E_phot", "Out_E_at")
+
+
+def n_time_points(Tim, dt, dt_flag=0):
+    """Tallied time-grid points (Monte_Carlo.f90:2118-2149 and 572-580)."""
+    if dt_flag <= 0:
+        n = int(np.ceil(Tim / dt)) + 1
+        raw = [0.0] * n
+        raw[0] = dt
+        for i in range(n - 2):
+            raw[i + 1] = raw[i] + dt
+        raw[-1] = Tim + dt
+    else:
+        i, t = 0, 0.01
+        while t <= Tim:
+            i += 1
+            t *= dt
+        raw = [0.0] * (i + 1)
+        raw[0] = 0.01
+        for k in range(i - 1):
+            raw[k + 1] = raw[k] * dt
+        raw[i] = Tim + dt
+    out, tim, i = [], 0.0, 0
+    while tim <= Tim - 1e-6 and i < len(raw):
+        tim = min(raw[i], Tim)
+        out.append(tim)
+        i += 1
+    return out
+
+
+class TallySet:
+    """Caller-owned tally arrays (numpy, float64), Fortran layout."""
+
+    def __init__(self, Nt, NR, Nat, Nshl):
+        self.Nt, self.NR, self.Nat, self.Nshl = Nt, NR, Nat, Nshl
+        self.a = {}
+        for k in TALLY_2D:
+            self.a[k] = np.zeros(Nt * NR)
+        for k in TALLY_4D:
+            self.a[k] = np.zeros(Nt * NR * Nat * Nshl)
+        for k in TALLY_1D:
+            self.a[k] = np.zeros(Nt)
+        self.a["Out_E_h"] = np.zeros(Nt * Nat * Nshl)
+
+    def c(self):
+        return abi.Tallies(Nt=self.Nt, N_R=self.NR, Nat=self.Nat, Nshl=self.Nshl,
+                           **{k: abi.dptr(v) for k, v in self.a.items()})
+
+    def view(self, name):
+        v = self.a[name]
+        if name in TALLY_2D:
+            return v.reshape(self.NR, self.Nt).T          # [t, R]
+        if name in TALLY_4D:
+            return v.reshape(self.Nshl, self.Nat, self.NR, self.Nt).transpose(3, 2, 1, 0)  # [t, R, atom, shell]
+        if name == "Out_E_h":
+            return v.reshape(self.Nshl, self.Nat, self.Nt).transpose(2, 1, 0)
+        return v
+
+    def __getitem__(self, k):
+        return self.a[k]
+
+
+def ion_struct(w):
+    return abi.Ion(Zat=w.ion_Z, Kind_Zeff=0, Kind_ion=0, Mass=w.ion_mass, E=w.ion_E, fixed_Zeff=float(w.ion_Z))
+
+
+@dataclass
+class RunOptions:
+    precision: int = 0          # 0 FP32 kinematics, 1 FP64
+    seed: int = 1
+    iteration_offset: int = 0
+    block_size: int = 0
+    events_per_step: int = 0
+    queue_capacity: int = 0
+    iterations_per_batch: int = 0
+    use_graph: int = 0
+
+
+def run_cfg(w, opt, NMC=None):
+    R = np.ascontiguousarray(w.R_edges, dtype=np.float64)
+    cfg = abi.RunCfg(NMC=int(NMC if NMC is not None else w.NMC), dt_flag=0, Tim=w.Tim, dt=w.dt, N_R=len(R),
+                     precision=opt.precision, Out_R=abi.dptr(R), seed=opt.seed,
+                     iteration_offset=opt.iteration_offset, block_size=opt.block_size,
+                     events_per_step=opt.events_per_step, queue_capacity=opt.queue_capacity,
+                     iterations_per_batch=opt.iterations_per_batch, use_graph=opt.use_graph)
+    return cfg, R
+
+
+class Tables:
+    """GPU-built cross-section tables of one material and ion."""
+
+    def __init__(self, w, build_photon=None, shi_window=True, lib=None):
+        self.lib = lib or abi.load()
+        self.w = w
+        self.mat = w.material.to_c()
+        self.ion = ion_struct(w)
+        bp = w.material.include_photons if build_photon is None else build_photon
+        lo, hi = (w.ion_E * 0.5, w.ion_E * 1.01) if shi_window else (0.0, 0.0)
+        tc = abi.TableCfg(build_shi=1, build_photon=int(bp), shi_E_window_lo=lo, shi_E_window_hi=hi)
+        self.h = C.c_void_p()
+        self.status = abi.Status.fresh()
+        rc = self.lib.trekis_tables_build(self.mat.ref(), C.byref(self.ion), C.byref(tc), C.byref(self.h),
+                                          C.byref(self.status))
+        abi.check(rc, self.lib)
+
+    def export(self, kind, atom=0, shell=0):
+        n = C.c_int64()
+        abi.check(self.lib.trekis_tables_size(self.h, kind, atom, shell, C.byref(n)), self.lib)
+        E, L, D = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+        abi.check(self.lib.trekis_tables_export(self.h, kind, atom, shell, abi.dptr(E), abi.dptr(L), abi.dptr(D),
+                                                n.value), self.lib)
+        return E, L, D
+
+    def row(self, kind, atom, shell, iE, cap=1 << 16):
+        hw, L = np.zeros(cap), np.zeros(cap)
+        n = C.c_int64()
+        abi.check(self.lib.trekis_tables_row(self.h, kind, atom, shell, iE, abi.dptr(hw), abi.dptr(L), cap,
+                                             C.byref(n)), self.lib)
+        return hw[:n.value].copy(), L[:n.value].copy()
+
+    def close(self):
+        if self.h:
+            self.lib.trekis_tables_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def new_tallies(w):
+    Nt = len(n_time_points(w.Tim, w.dt))
+    m = w.material
+    return TallySet(Nt, len(w.R_edges), len(m.atoms), m.n_shells_max)
+
+
+def mc_run(tables, opt=None, NMC=None, tallies=None):
+    """Run NMC iterations on the GPU; returns (TallySet, Status)."""
+    opt = opt or RunOptions()
+    w = tables.w
+    tal = tallies or new_tallies(w)
+    cfg, R = run_cfg(w, opt, NMC)
+    st = abi.Status.fresh()
+    ct = tal.c()
+    rc = tables.lib.trekis_mc_run(tables.h, tables.mat.ref(), C.byref(tables.ion), C.byref(cfg), C.byref(ct),
+                                  C.byref(st))
+    abi.check(rc, tables.lib)
+    return tal, st

@@ -267,7 +267,9 @@ def resample_dos(e_file, dos_file, N_VB_el, At_Dens, Pers_sum):
         Eg[i] = E
         D[i] = val
     Eg = np.abs(Eg - Eg[-1])[::-1].copy()
-    D = D[::-1].copy()
+    # linear extrapolation at a band edge where the file goes to zero can
+    # leave -1e-16 instead of 0; a negative DOS would make k NaN
+    D = np.maximum(D[::-1], 0.0)
     s = 0.0
     I = np.zeros(M)
     for i in range(M):
