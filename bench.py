@@ -1,0 +1,337 @@
+"""Benchmark of the GB300 Monte Carlo track loop.
+
+Workload: the plain-method-at-scale configuration -- Al2O3-like target, Xe
+167 MeV, 10 nm layer, t = 0-1000 fs at 1 fs, 100 log radial bins 1-1000 A,
+mobile valence holes, radiative decay and photon transport; the full job is
+10^4 MC iterations.  A "step" is one batch of iterations of that job (one
+do_Monte_Carlo call over ``--iters`` iterations).  The metric is collision
+events per second (SHI, electron, hole, Auger, radiative, photon events, each
+a dispatch of the reference's grid_do body, Monte_Carlo.f90:587-627).
+
+  value  -- events/s with tables and tallies resident on the device, timed
+            with CUDA events on the launching stream (trekis_mc_run_device);
+  e2e    -- the same through trekis_mc_run with host tally arrays (the
+            drop-in call), wall-clocked, host<->device copies included.
+
+``--impl reference`` times the CPU restatement of the reference loop (the
+FP64 oracle, all host threads) on the same workload and metric.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "trekis-3_gb300"))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+METRIC = "collisions/s on 1 GB300, neural vs table sampler, tallies within 3σ of FP64 ref"
+UNIT = "collisions/s"
+JOB_NMC = 10000
+
+
+def workload():
+    from trekis import configs
+    return configs.cfg1(NMC=JOB_NMC)
+
+
+def config_dict(w, iters, extra=None):
+    d = {"workload": "cfg1: Al2O3-like (rho 3.95, gap 6.7 eV), Xe 131u 167 MeV, 10 nm, 0-1000 fs dt 1 fs, "
+                     "100 log radial bins 1-1000 A, mobile VB holes (m_h=1), radiative decay + photons; "
+                     f"job = {JOB_NMC} MC iterations, step = {iters} iterations",
+         "iterations_per_step": iters, "job_iterations": JOB_NMC, "sampler": "table",
+         "kinematics": "fp32", "tables": "fp64 build", "tallies": "int64 fixed point",
+         "l2": "512 MiB buffer written between steps (working set is L2-resident by design)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.p = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.close()
+
+    def summary(self, dev=0):
+        try:
+            rows = [l.split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return None
+        rows = [[x.strip() for x in r] for r in rows if r and r[0].strip() == str(dev)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        load = [s for s in sm if s > 0.5 * mx] or sm
+        return {"sm_mhz": float(np.median(load)) if load else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        return json.load(open(ROOT / "MEASURED_PEAKS.json"))
+    except Exception:
+        return {}
+
+
+def profile_traffic():
+    """DRAM bytes per k_step launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "k_step_cfg1_traffic.json"
+    try:
+        d = json.load(open(p))
+        return d.get("dram_bytes_per_launch"), d.get("events_per_launch")
+    except Exception:
+        return None, None
+
+
+def alg_bytes_per_event(st, n_shells):
+    """Algorithmic bytes per collision: 96 B particle state read+write, 64 B
+    for two total-MFP lookups (2 nodes x (E,L) x 2 energies), and for events
+    that create an electron-hole pair the shell pick (16 B per shell), the
+    transfer-row nodes (32 B), the new pair's state (96 B) and its MFP lookup
+    (32 B); Mott elastic events read no transfer rows."""
+    ev = max(st.step_events, 1)
+    p_inel = (st.n_el_inelastic + st.n_photon_abs + st.n_auger) / ev
+    return 96 + 64 + p_inel * (16 * n_shells + 32 + 96 + 32)
+
+
+def run_gpu(args):
+    import torch
+    from trekis import abi, api
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    lib = abi.load()
+    if not lib.trekis_device_ok():
+        raise RuntimeError("no usable sm_103a device")
+    w = workload()
+    t = api.Tables(w, lib=lib)
+    tal_h = api.new_tallies(w)
+    Nt, NR, Nat, Nshl = tal_h.Nt, tal_h.NR, tal_h.Nat, tal_h.Nshl
+    dev_arrays = {k: torch.zeros(v.size, dtype=torch.float64, device=dev) for k, v in tal_h.a.items()}
+    dptr = lambda x: C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double))
+    tal_d = abi.Tallies(Nt=Nt, N_R=NR, Nat=Nat, Nshl=Nshl, **{k: dptr(v) for k, v in dev_arrays.items()})
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+    iters = args.iters
+    per_rank_steps = args.warmup + args.steps
+    base_it = rank * per_rank_steps * iters
+
+    def step(i, host=False):
+        opt = api.RunOptions(seed=args.seed, iteration_offset=base_it + i * iters, queue_capacity=args.queue_cap,
+                             events_per_step=args.events_per_step)
+        cfg, R = api.run_cfg(w, opt, NMC=iters)
+        st = abi.Status.fresh()
+        if host:
+            tl = api.new_tallies(w)
+            ct = tl.c()
+            t0 = time.perf_counter()
+            rc = lib.trekis_mc_run(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(ct), C.byref(st))
+            dt = time.perf_counter() - t0
+        else:
+            rc = lib.trekis_mc_run_device(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(tal_d),
+                                          C.byref(st))
+            dt = None
+        abi.check(rc, lib)
+        return st, dt
+
+    for i in range(args.warmup):
+        step(i)
+        flush.fill_(i & 0xFF)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = Clocks(str(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").exists()
+                 else f"/tmp/trekis_clocks_{rank}.csv")
+    tot_ev = tot_ms = step_ms = step_ev = 0.0
+    launches = 0
+    sts = []
+    with clk:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            st, _ = step(args.warmup + i)
+            sts.append(st)
+            tot_ev += st.n_events
+            tot_ms += st.device_ms
+            step_ms += st.step_ms
+            step_ev += st.step_events
+            launches += st.n_kernel_launches
+            flush.fill_((i + 7) & 0xFF)
+        torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        v = torch.tensor([tot_ms, tot_ev], dtype=torch.float64, device=dev)
+        mx = v.clone(); dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
+        sm = v.clone(); dist.all_reduce(sm[1:], op=dist.ReduceOp.SUM)
+        tot_ms_all, tot_ev_all = float(mx[0]), float(sm[1])
+    else:
+        tot_ms_all, tot_ev_all = tot_ms, tot_ev
+    # end-to-end through the drop-in call with host tally arrays
+    e2e_ev = e2e_s = 0.0
+    h2d = d2h = 0
+    for i in range(args.e2e_steps):
+        st, dt = step(args.warmup + args.steps + i, host=True)
+        e2e_ev += st.n_events
+        e2e_s += dt
+        h2d += st.h2d_bytes
+        d2h += st.d2h_bytes
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+        return
+    value = tot_ev_all / (tot_ms_all / 1e3)
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    n_sh = sum(len(a.shells) for a in w.material.atoms)
+    merged = abi.Status.fresh()
+    for st in sts:
+        for f in ("step_events", "n_el_inelastic", "n_photon_abs", "n_auger"):
+            setattr(merged, f, getattr(merged, f) + getattr(st, f))
+    bpe = alg_bytes_per_event(merged, n_sh)
+    launches_step = sum(s.step_launches for s in sts)
+    achieved = bpe * step_ev / (step_ms / 1e3) / 1e9           # GB/s over the step kernels
+    traffic_b, traffic_ev = profile_traffic()
+    traffic = None
+    if traffic_b and traffic_ev:
+        traffic = traffic_b / traffic_ev * (step_ev / max(launches_step, 1))
+    roof = {"bound": "hbm", "kernel": "k_step<float> (wavefront step)", "achieved": achieved,
+            "peak": hbm if hbm else 6800.0, "peak_source": "measured" if hbm else "fallback",
+            "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "traffic": traffic,
+            "bytes_per_event": bpe, "step_kernel_ms": step_ms, "step_kernel_launches": launches_step,
+            "events_per_step_kernel_s": step_ev / (step_ms / 1e3)}
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tot_ms_all / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
+        "config": config_dict(w, iters, {"parallelism": f"iterations sharded over {world} GPU(s), no collective"}),
+        "e2e": {"value": e2e_ev / e2e_s if e2e_s else None, "unit": UNIT,
+                "h2d_bytes_per_step": h2d // max(args.e2e_steps, 1), "d2h_bytes_per_step": d2h // max(args.e2e_steps, 1)},
+        "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
+        "clocks": clk.summary(local),
+        "events": {"total": tot_ev, "per_iteration": tot_ev / (args.steps * iters),
+                   "elastic_frac": sum(s.n_el_elastic for s in sts) / max(tot_ev, 1)},
+    }
+    print(json.dumps(out))
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(args, n_it=None, nthreads=None):
+    """The FP64 oracle (restatement of the reference's loop) on the host cores:
+    one cfg1 iteration per thread, heap-ordered earliest-event loop."""
+    import oracle_py
+    from trekis import abi, api
+    w = workload()
+    nthreads = nthreads or os.cpu_count() or 1
+    n_it = n_it or args.cpu_iters or nthreads
+    h = w.material.to_c()
+    ion = api.ion_struct(w)
+    tc = abi.TableCfg(build_shi=1, build_photon=1, shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+    o = oracle_py.OracleTables(h, ion, tc, nthreads=nthreads)
+    tal = api.new_tallies(w)
+    cfg, R = api.run_cfg(w, api.RunOptions(precision=1, seed=args.seed, iteration_offset=900000), NMC=n_it)
+    st = abi.Status.fresh()
+    t0 = time.perf_counter()
+    o.mc_run(cfg, tal, st, nthreads=nthreads, sched=1)
+    dt = time.perf_counter() - t0
+    return {"value": st.n_events / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n_it} cfg1 iterations ({st.n_events} events) in {dt:.1f} s, FP64 oracle, "
+                      "OpenMP over iterations, heap event queue"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    w = workload()
+    tot_ev = tot_s = 0.0
+    cpu = None
+    for i in range(args.warmup + args.steps):
+        c = cpu_baseline(args)
+        if i >= args.warmup:
+            ev = c["value"] * float(c["sample"].split("in ")[1].split(" s")[0])
+            tot_ev += ev
+            tot_s += ev / c["value"]
+            cpu = c
+    value = tot_ev / tot_s
+    cpu["value"] = value
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+           "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
+           "config": config_dict(w, cpu["cores"], {"parallelism": "host threads"}),
+           "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--iters", type=int, default=32, help="MC iterations per step")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-iters", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=20251203)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--queue-cap", type=int, default=0, help="particles per queue buffer (0: library default)")
+    ap.add_argument("--events-per-step", type=int, default=0, help="events per thread per wavefront step (0: tuned)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

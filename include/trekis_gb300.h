@@ -201,6 +201,14 @@ typedef struct {
     uint64_t n_steps;          /* wavefront steps                               */
     double   device_ms;        /* device time of the MC (CUDA events)           */
     uint64_t n_kernel_launches;/* kernels launched by the call                  */
+    double   step_ms;          /* device time of the wavefront-step kernels     */
+    uint64_t step_events;      /* collision events run inside those kernels     */
+    uint64_t step_launches;    /* wavefront-step kernel launches                */
+    uint64_t peak_queue;       /* largest electron or hole queue seen           */
+    int32_t  batch_iterations; /* iterations per batch finally used             */
+    int32_t  pad_;
+    uint64_t h2d_bytes;        /* host-to-device bytes copied by the call       */
+    uint64_t d2h_bytes;        /* device-to-host bytes copied by the call       */
 } trekis_status;
 
 /* ---- entry points ------------------------------------------------------ */

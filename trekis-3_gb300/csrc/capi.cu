@@ -107,28 +107,74 @@ static int upload_mc(trekis_tables* t, DevTabs<T>& d) {
     return TREKIS_OK;
 }
 
-static int upload_shi(trekis_tables* t) {
+static int find_mono_d(const double* A, int N, double V) {
+    if (V < A[0]) return 1;
+    if (V >= A[N - 1]) return N;
+    int i1 = 1, i2 = N;
+    while (i1 != i2 - 1) { int ic = (i1 + i2) / 2; if (A[ic - 1] <= V) i1 = ic; else i2 = ic; }
+    return i1 + 1;
+}
+
+// Interpolate (Cross_sections.f90:4051-4086) on the host
+static double interp_h(int flag, double E1, double E2, double S1, double S2, double Ex) {
+    if (std::fabs(E2 - E1) < 1.0e-6) return std::max(S1, S2);
+    if (Ex == E1) return S1;
+    if (flag == 5) {
+        double l1 = std::log(E1), l2 = std::log(E2), lx = std::log(Ex), s1 = std::log(S1), s2 = std::log(S2);
+        return std::exp(s1 + (s2 - s1) / (l2 - l1) * (lx - l1));
+    }
+    return S1 + (S2 - S1) / (E2 - E1) * (Ex - E1);
+}
+
+template <class T>
+static int upload_shi(trekis_tables* t, DevShi<T>& s) {
     Buffers& b = t->buf;
-    DevShi& s = t->dshi;
+    const int nsh = t->nsh;
+    auto logs = [](const std::vector<double>& v) {
+        std::vector<double> o(v.size());
+        for (size_t i = 0; i < v.size(); ++i) o[i] = std::log(v[i]);
+        return o;
+    };
     s.nS = (int)t->shi[0].E.size();
-    s.sE = upload<double>(b, t->shi[0].E);
-    std::vector<double> L, dE, dL, dI;
-    std::vector<int> off(1, 0);
-    for (int k = 0; k < t->nsh; ++k) {
+    s.sE = upload<T>(b, t->shi[0].E);
+    s.lE = upload<T>(b, logs(t->shi[0].E));
+    std::vector<double> L, dE, dI;
+    std::vector<double> ia(nsh), ib(nsh);
+    std::vector<int> off(1, 0), mt(nsh);
+    for (int k = 0; k < nsh; ++k) {
         L.insert(L.end(), t->shi[k].L.begin(), t->shi[k].L.end());
         const HTab& r = t->dsde[k];
         dE.insert(dE.end(), r.E.begin(), r.E.end());
-        dL.insert(dL.end(), r.L.begin(), r.L.end());
         for (double x : r.L) dI.push_back(1.0 / x);
         off.push_back((int)dE.size());
+        const int N = (int)r.L.size();
+        ia[k] = ib[k] = 0.0; mt[k] = 1;
+        if (N > 0) {
+            // the constant part of SHI_energy_transfer (Monte_Carlo.f90:1736-1757)
+            const double Ip = t->mat.atoms[t->atom_of[k]].Ip[t->shell_of[k]];
+            const int M = find_mono_d(r.E.data(), N, Ip);
+            double dL;
+            if (M > 1) dL = (r.L[M - 2] > 1.0e-10) ? interp_h(5, r.E[M - 2], r.E[M - 1], r.L[M - 2], r.L[M - 1], Ip)
+                                                   : interp_h(1, r.E[M - 2], r.E[M - 1], r.L[M - 2], r.L[M - 1], Ip);
+            else dL = r.L[0];
+            mt[k] = M;
+            if (dL > 0.0 && r.L[N - 1] > 0.0) { ia[k] = 1.0 / dL; ib[k] = 1.0 / r.L[N - 1]; }
+        }
     }
-    s.sL = upload<double>(b, L);
-    s.path = upload<double>(b, t->SHI_path.L);
+    s.sL = upload<T>(b, L);
+    s.lL = upload<T>(b, logs(L));
+    s.pL = upload<T>(b, t->SHI_path.L);
+    s.lpL = upload<T>(b, logs(t->SHI_path.L));
     s.d_off = upload_i(b, off);
-    s.dE = upload<double>(b, dE);
-    s.dL = upload<double>(b, dL);
-    s.dInvL = upload<double>(b, dI);
-    if (!s.sE || !s.sL || !s.path || !s.d_off || !s.dE) { set_error("SHI table upload failed"); return TREKIS_ENOMEM; }
+    s.dE = upload<T>(b, dE);
+    s.ldE = upload<T>(b, logs(dE));
+    s.dI = upload<T>(b, dI);
+    s.ldI = upload<T>(b, logs(dI));
+    s.invdL_ip = upload<T>(b, ia);
+    s.invL_last = upload<T>(b, ib);
+    s.Mt = upload_i(b, mt);
+    s.pow_zp = (T)std::pow((double)t->ion.Zat, 0.66666666);
+    if (!s.sE || !s.sL || !s.pL || !s.d_off || !s.dE || !s.Mt) { set_error("SHI table upload failed"); return TREKIS_ENOMEM; }
     return TREKIS_OK;
 }
 
@@ -184,6 +230,18 @@ __global__ void k_derive(int Nt, int nhs, int phot, const double* Ee, const doub
     totE[i] += s + Eat[i];
 }
 
+// dst[blk*map[k] + x] += src[blk*k + x]: compact shells -> (atom + Nat*shell) slices
+__global__ void k_add_slices(double* dst, const double* src, size_t blk, int ns, const int* map) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= blk * ns) return;
+    size_t k = i / blk, x = i % blk;
+    dst[blk * map[k] + x] += src[i];
+}
+__global__ void k_add(double* dst, const double* src, size_t n) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] += src[i];
+}
+
 // Device FP64 accumulators laid out exactly as the caller's tallies.
 struct DevOut {
     double *ne, *Ee, *np, *Ep, *lat, *nh, *Eh, *Ek, *totNe, *totNp, *totE, *E_e, *E_p, *E_at, *E_h;
@@ -192,13 +250,114 @@ struct DevOut {
 template <class T> static const DevTabs<T>& tabs_of(const trekis_tables* t);
 template <> const DevTabs<float>& tabs_of<float>(const trekis_tables* t) { return t->d32; }
 template <> const DevTabs<double>& tabs_of<double>(const trekis_tables* t) { return t->d64; }
+template <class T> static const DevShi<T>& shi_of(const trekis_tables* t);
+template <> const DevShi<float>& shi_of<float>(const trekis_tables* t) { return t->dshi32; }
+template <> const DevShi<double>& shi_of<double>(const trekis_tables* t) { return t->dshi64; }
+
+// Everything a call needs on the device, kept across calls of the same shape.
+template <class T>
+struct Workspace {
+    Buffers b;
+    int64_t cap = 0;
+    int Nt = 0, NR = 0, nsh = 0, Nat = 0, Nshl = 0;
+    QBuf<T> qa, qb;
+    unsigned long long* tall = nullptr;
+    size_t n_all = 0;
+    Tal tal;
+    Ctrs* ctr = nullptr;
+    McConst<T>* dC = nullptr;
+    T *tg = nullptr, *Rg = nullptr;
+    double* V = nullptr;
+    int* hmap = nullptr;
+    double *hstage = nullptr, *hn = nullptr, *hE = nullptr, *hK = nullptr, *htn = nullptr, *htE = nullptr;
+    size_t hstage_n = 0;
+    double* calls = nullptr;   // per-call E_e, E_phot, E_at [Nt each] and E_h [Nt*Nat*Nshl]
+    double* out = nullptr;     // FP64 tally staging of the host-array entry point
+    size_t out_n = 0;
+    void* evs = nullptr;       // SHI collision records of a batch
+    int64_t cap_ev = 0;
+    long long* lat_rows = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, s0 = nullptr, s1 = nullptr;
+    ~Workspace() {
+        for (cudaEvent_t e : {e0, e1, s0, s1}) if (e) cudaEventDestroy(e);
+    }
+};
+
+static uint64_t ws_key(int prec, int64_t cap, int Nt, int NR, int Nat, int Nshl) {
+    uint64_t k = (uint64_t)prec;
+    k = k * 1000003ull + (uint64_t)cap;
+    k = k * 1000003ull + (uint64_t)Nt;
+    k = k * 1000003ull + (uint64_t)NR;
+    k = k * 1000003ull + (uint64_t)Nat;
+    return k * 1000003ull + (uint64_t)Nshl;
+}
 
 template <class T>
-static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nshl_out, DevOut out, trekis_status* st,
-                  cudaStream_t strm) {
+static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, int* rc) {
+    const int64_t cap = cfg.queue_capacity > 0 ? cfg.queue_capacity : (int64_t)(sizeof(T) == 4 ? 24 : 12) << 20;
+    const uint64_t key = ws_key(sizeof(T), cap, Nt, cfg.N_R, Nat, Nshl);
+    if (t->ws && t->ws_key == key) { *rc = 0; return (Workspace<T>*)t->ws.get(); }
+    t->ws.reset();
+    auto* w = new Workspace<T>();
+    std::shared_ptr<void> holder(w, [](void* p) { delete (Workspace<T>*)p; });
+    const trekis_material& m = t->mat;
+    w->cap = cap; w->Nt = Nt; w->NR = cfg.N_R; w->nsh = t->nsh; w->Nat = Nat; w->Nshl = Nshl;
+    Buffers& b = w->b;
+    const int64_t capp = std::max<int64_t>(cap / 8, 1 << 16);
+    *rc = TREKIS_ENOMEM;
+    for (QBuf<T>* q : {&w->qa, &w->qb}) {
+        if (alloc_queue(b, q->q[0], cap, false) || alloc_queue(b, q->q[1], cap, true) ||
+            alloc_queue(b, q->q[2], m.include_photons ? capp : 1, false))
+            return nullptr;
+    }
+    const int NR = cfg.N_R, nsh = t->nsh;
+    const size_t rows = (size_t)Nt + 2;
+    const size_t n_e = rows * NR, n_h = rows * nsh * NR, n_l = (size_t)Nt * NR;
+    w->n_all = 4 * n_e + 3 * n_h + n_l;
+    w->tall = (unsigned long long*)b.alloc(8 * w->n_all);
+    w->ctr = (Ctrs*)b.alloc(sizeof(Ctrs));
+    w->dC = (McConst<T>*)b.alloc(sizeof(McConst<T>));
+    w->tg = (T*)b.alloc(sizeof(T) * Nt);
+    w->Rg = (T*)b.alloc(sizeof(T) * NR);
+    w->V = (double*)b.alloc(8 * NR);
+    w->hmap = (int*)b.alloc(sizeof(int) * nsh);
+    w->hstage_n = (size_t)Nt * NR * nsh * 3 + (size_t)Nt * nsh * 2;
+    w->hstage = (double*)b.alloc(8 * w->hstage_n);
+    const size_t n3 = (size_t)Nt * Nat * Nshl;
+    w->calls = (double*)b.alloc(8 * (3 * (size_t)Nt + n3));
+    const size_t n2 = (size_t)Nt * NR, n4 = n2 * Nat * Nshl;
+    w->out_n = 5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3;
+    w->out = (double*)b.alloc(8 * w->out_n);
+    w->cap_ev = std::max<int64_t>(cap / 2, 1 << 16);
+    w->evs = b.alloc(shi_event_bytes() * w->cap_ev);
+    w->lat_rows = (long long*)b.alloc(8 * Nt);
+    if (!w->evs || !w->lat_rows) return nullptr;
+    if (!w->tall || !w->ctr || !w->dC || !w->tg || !w->Rg || !w->V || !w->hmap || !w->hstage || !w->calls || !w->out)
+        return nullptr;
+    Tal& tal = w->tal;
+    tal.e_cnt = w->tall; tal.e_E = w->tall + n_e; tal.p_cnt = w->tall + 2 * n_e; tal.p_E = w->tall + 3 * n_e;
+    tal.h_cnt = w->tall + 4 * n_e; tal.h_E = tal.h_cnt + n_h; tal.h_Ek = tal.h_E + n_h; tal.lat = tal.h_Ek + n_h;
+    w->hn = w->hstage; w->hE = w->hn + (size_t)Nt * NR * nsh; w->hK = w->hE + (size_t)Nt * NR * nsh;
+    w->htn = w->hK + (size_t)Nt * NR * nsh; w->htE = w->htn + (size_t)Nt * nsh;
+    std::vector<int> hs(nsh);
+    for (int k = 0; k < nsh; ++k) hs[k] = t->atom_of[k] + Nat * t->shell_of[k];
+    if (cudaMemcpy(w->hmap, hs.data(), sizeof(int) * nsh, cudaMemcpyHostToDevice) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
+    for (cudaEvent_t* e : {&w->e0, &w->e1, &w->s0, &w->s1})
+        if (cudaEventCreate(e) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
+    t->ws = holder;
+    t->ws_key = key;
+    *rc = 0;
+    return w;
+}
+
+template <class T>
+static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, DevOut out,
+                  trekis_status* st, cudaStream_t strm) {
     const trekis_material& m = t->mat;
     const DevTabs<T>& tb = tabs_of<T>(t);
-    Buffers b;
+    int rc = 0;
+    Workspace<T>* ws = get_ws<T>(t, cfg, Nt, Nat, Nshl, &rc);
+    if (!ws) { if (rc == TREKIS_ENOMEM) set_error("device workspace allocation failed"); return rc; }
     // constants
     McConst<T> C;
     std::memset(&C, 0, sizeof C);
@@ -226,108 +385,97 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nshl_
     C.mec2 = (T)(kMe * kC * kC / kE);
     C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
     std::vector<double> tg = tallied_times(cfg.Tim, cfg.dt, cfg.dt_flag);
-    C.tg = upload<T>(b, tg);
-    C.Rg = upload<T>(b, std::vector<double>(cfg.Out_R, cfg.Out_R + cfg.N_R));
+    std::vector<T> tgT(tg.begin(), tg.end()), RgT(cfg.Out_R, cfg.Out_R + cfg.N_R);
     std::vector<double> V(cfg.N_R);
     double R0 = 0.0;
     for (int j = 0; j < cfg.N_R; ++j) { V[j] = 1.0 / ((cfg.Out_R[j] * cfg.Out_R[j] - R0 * R0) * kPi * m.Layer); R0 = cfg.Out_R[j]; }
-    const double* dV = upload<double>(b, V);
-    McConst<T>* dC = (McConst<T>*)b.alloc(sizeof C);
-    if (!C.tg || !C.Rg || !dV || !dC) return TREKIS_ENOMEM;
-
-    // queues
-    const int64_t cap = cfg.queue_capacity > 0 ? cfg.queue_capacity : (int64_t)(sizeof(T) == 4 ? 24 : 12) << 20;
-    const int64_t capp = std::max<int64_t>(cap / 8, 1 << 16);
-    QBuf<T> qa, qb;
-    for (QBuf<T>* q : {&qa, &qb}) {
-        int rc;
-        if ((rc = alloc_queue(b, q->q[0], cap, false))) return rc;
-        if ((rc = alloc_queue(b, q->q[1], cap, true))) return rc;
-        if ((rc = alloc_queue(b, q->q[2], m.include_photons ? capp : 1, false))) return rc;
-    }
-    // int64 tallies of one batch
+    CK(cudaMemcpyAsync(ws->tg, tgT.data(), sizeof(T) * Nt, cudaMemcpyHostToDevice, strm));
+    CK(cudaMemcpyAsync(ws->Rg, RgT.data(), sizeof(T) * cfg.N_R, cudaMemcpyHostToDevice, strm));
+    CK(cudaMemcpyAsync(ws->V, V.data(), 8 * cfg.N_R, cudaMemcpyHostToDevice, strm));
+    C.tg = ws->tg; C.Rg = ws->Rg;
     const int NR = cfg.N_R, nsh = t->nsh;
-    const size_t rows = (size_t)Nt + 2;
-    const size_t n_e = rows * NR, n_h = rows * nsh * NR, n_l = (size_t)Nt * NR;
-    const size_t n_all = 4 * n_e + 3 * n_h + n_l;
-    unsigned long long* tall = (unsigned long long*)b.alloc(8 * n_all);
-    if (!tall) return TREKIS_ENOMEM;
-    Tal tal;
-    tal.e_cnt = tall; tal.e_E = tall + n_e; tal.p_cnt = tall + 2 * n_e; tal.p_E = tall + 3 * n_e;
-    tal.h_cnt = tall + 4 * n_e; tal.h_E = tal.h_cnt + n_h; tal.h_Ek = tal.h_E + n_h; tal.lat = tal.h_Ek + n_h;
-    Ctrs* dctr = (Ctrs*)b.alloc(sizeof(Ctrs));
-    if (!dctr) return TREKIS_ENOMEM;
-    // per-shell staging for holes: slice k -> caller slice (atom + Nat*shell)
-    std::vector<int> hs(nsh);
-    for (int k = 0; k < nsh; ++k) hs[k] = t->atom_of[k] + m.N_atoms * t->shell_of[k];
-    (void)Nshl_out;
-    double* h_stage = (double*)b.alloc(8 * ((size_t)Nt * NR * nsh * 3 + (size_t)Nt * nsh * 2));
-    if (!h_stage) return TREKIS_ENOMEM;
-    double* hn = h_stage;
-    double* hE = hn + (size_t)Nt * NR * nsh;
-    double* hK = hE + (size_t)Nt * NR * nsh;
-    double* htn = hK + (size_t)Nt * NR * nsh;
-    double* htE = htn + (size_t)Nt * nsh;
-    CK(cudaMemsetAsync(h_stage, 0, 8 * ((size_t)Nt * NR * nsh * 3 + (size_t)Nt * nsh * 2), strm));
-    double* scratch_t = (double*)b.alloc(8 * (size_t)Nt * 4);
-    if (!scratch_t) return TREKIS_ENOMEM;
-    CK(cudaMemsetAsync(scratch_t, 0, 8 * (size_t)Nt * 4, strm));
+    Tal tal = ws->tal;
+    Ctrs* dctr = ws->ctr;
+    McConst<T>* dC = ws->dC;
+    const double* dV = ws->V;
+    CK(cudaMemsetAsync(ws->hstage, 0, 8 * ws->hstage_n, strm));
 
     const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
     const int bs = cfg.block_size > 0 ? std::min(cfg.block_size, 256) : 256;
+    const int64_t cap = ws->cap;
     int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 64);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, strm));
-    uint64_t steps = 0, launches = 0;
+    CK(cudaEventRecord(ws->e0, strm));
+    uint64_t steps = 0, launches = 0, ev_tot[8] = {0}, peak_all = 0;
+    uint64_t h2d = sizeof(T) * (Nt + cfg.N_R) + 8 * cfg.N_R, d2h = 0;
+    double step_ms = 0.0;
     Ctrs hc;
     std::memset(&hc, 0, sizeof hc);
-    uint64_t ev_tot[8] = {0};
     unsigned err_bits = 0;
     int done = 0;
     while (done < cfg.NMC) {
         const int nb = std::min(B, cfg.NMC - done);
         C.it0 = cfg.iteration_offset + done;
         CK(cudaMemcpyAsync(dC, &C, sizeof C, cudaMemcpyHostToDevice, strm));
-        CK(cudaMemsetAsync(tall, 0, 8 * n_all, strm));
+        h2d += sizeof C;
+        CK(cudaMemsetAsync(ws->tall, 0, 8 * ws->n_all, strm));
         CK(cudaMemsetAsync(dctr, 0, sizeof(Ctrs), strm));
-        QBuf<T>* in = &qa;
-        QBuf<T>* ot = &qb;
-        launch_shi<T>(dC, tb, t->dshi, ot->q[0], ot->q[1], tal, dctr, nb, bs, strm);
+        QBuf<T>* in = &ws->qa;
+        QBuf<T>* ot = &ws->qb;
+        launch_shi<T>(dC, shi_of<T>(t), ws->evs, ws->cap_ev, dctr, nb, strm);
         ++launches;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
+        d2h += sizeof hc;
         CK(cudaStreamSynchronize(strm));
+        if (!hc.overflow) {
+            launch_pairs<T>(dC, tb, ws->evs, (int64_t)hc.ev[0], ot->q[0], ot->q[1], tal, dctr, strm);
+            ++launches;
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
+            d2h += sizeof hc;
+            CK(cudaStreamSynchronize(strm));
+        }
         int64_t peak = std::max(hc.n_out[0], hc.n_out[1]);
         bool overflow = hc.overflow != 0;
+        uint64_t bsteps = 0, blaunch = 0;
+        double bms = 0.0;
         while (!overflow && (hc.n_out[0] + hc.n_out[1] + hc.n_out[2]) > 0) {
-            if (steps > (1ull << 24)) { set_error("wavefront did not drain"); return TREKIS_ETIMEOUT; }
+            if (steps + bsteps > (1ull << 24)) { set_error("wavefront did not drain"); return TREKIS_ETIMEOUT; }
             std::swap(in, ot);
             int ne = hc.n_out[0], nh = hc.n_out[1], np = hc.n_out[2];
             CK(cudaMemsetAsync(dctr, 0, 3 * sizeof(int), strm));
+            CK(cudaEventRecord(ws->s0, strm));
             launch_step<T>(dC, tb, in->q[0], ne, in->q[1], nh, in->q[2], np, ot->q[0], ot->q[1], ot->q[2], tal,
                            dctr, K, bs, strm);
-            ++launches; ++steps;
+            CK(cudaEventRecord(ws->s1, strm));
+            ++blaunch; ++bsteps;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
+            d2h += sizeof hc;
             CK(cudaStreamSynchronize(strm));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ws->s0, ws->s1));
+            bms += ms;
             peak = std::max<int64_t>(peak, std::max(hc.n_out[0], hc.n_out[1]));
             overflow = hc.overflow != 0;
         }
         if (overflow) {
-            if (nb == 1) { set_error("particle queue capacity too small for one iteration"); return TREKIS_EOVERFLOW; }
+            if (nb == 1) { set_error("particle queue overflow: capacity too small for one iteration"); return TREKIS_EOVERFLOW; }
             B = std::max(1, nb / 4);   // retry the batch smaller; nothing of it was flushed
             continue;
         }
+        steps += bsteps; launches += blaunch; step_ms += bms;
         for (int q = 0; q < 8; ++q) ev_tot[q] += hc.ev[q];
+        ev_tot[7] += 2 * hc.ev[0];   // the pair of every SHI collision
         err_bits |= hc.err_bits;
+        peak_all = std::max<uint64_t>(peak_all, (uint64_t)peak);
         // flush the batch into the FP64 accumulators
         fin_block(tal.e_cnt, tal.e_E, nullptr, Nt, NR, 1, dV, out.ne, out.Ee, nullptr, out.totNe, out.E_e, strm);
         fin_block(tal.p_cnt, tal.p_E, nullptr, Nt, NR, 1, dV, out.np, out.Ep, nullptr, out.totNp, out.E_p, strm);
-        fin_block(tal.h_cnt, tal.h_E, tal.h_Ek, Nt, NR, nsh, dV, hn, hE, hK, htn, htE, strm);
-        fin_lat(tal.lat, Nt, NR, dV, out.lat, out.E_at, strm);
-        launches += 7;
+        fin_block(tal.h_cnt, tal.h_E, tal.h_Ek, Nt, NR, nsh, dV, ws->hn, ws->hE, ws->hK, ws->htn, ws->htE, strm);
+        fin_lat(tal.lat, Nt, NR, dV, out.lat, out.E_at, ws->lat_rows, strm);
+        launches += 8;
         CK(cudaGetLastError());
         done += nb;
         if (tune_batch && peak > 0) {   // size the next batch to half the queue capacity
@@ -335,48 +483,47 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nshl_
             B = std::max(1, std::min<int>((int)(0.5 * cap / per_it), 1 << 16));
         }
     }
-    // holes: compact shells -> caller layout; derived totals
-    for (int k = 0; k < nsh; ++k) {
-        const size_t blk = (size_t)Nt * NR;
-        const size_t dst = blk * hs[k];
-        // out.nh/Eh/Ek are [Nt*NR*Nat*Nshl]; accumulate with a device add (copy + add kernel-free path)
-        std::vector<double> tmp(blk), cur(blk);
-        double* srcs[3] = {hn, hE, hK};
-        double* dsts[3] = {out.nh, out.Eh, out.Ek};
-        for (int q = 0; q < 3; ++q) {
-            if (!dsts[q]) continue;
-            CK(cudaMemcpyAsync(tmp.data(), srcs[q] + blk * k, 8 * blk, cudaMemcpyDeviceToHost, strm));
-            CK(cudaMemcpyAsync(cur.data(), dsts[q] + dst, 8 * blk, cudaMemcpyDeviceToHost, strm));
-            CK(cudaStreamSynchronize(strm));
-            for (size_t x = 0; x < blk; ++x) cur[x] += tmp[x];
-            CK(cudaMemcpyAsync(dsts[q] + dst, cur.data(), 8 * blk, cudaMemcpyHostToDevice, strm));
-        }
-        if (out.E_h) {
-            std::vector<double> a((size_t)Nt), c2((size_t)Nt);
-            CK(cudaMemcpyAsync(a.data(), htE + (size_t)Nt * k, 8 * Nt, cudaMemcpyDeviceToHost, strm));
-            CK(cudaMemcpyAsync(c2.data(), out.E_h + (size_t)Nt * hs[k], 8 * Nt, cudaMemcpyDeviceToHost, strm));
-            CK(cudaStreamSynchronize(strm));
-            for (int x = 0; x < Nt; ++x) c2[x] += a[x];
-            CK(cudaMemcpyAsync(out.E_h + (size_t)Nt * hs[k], c2.data(), 8 * Nt, cudaMemcpyHostToDevice, strm));
-        }
+    // holes: compact shells -> caller slices
+    {
+        const size_t blk = (size_t)Nt * NR, nn = blk * nsh;
+        const unsigned g = (unsigned)((nn + 255) / 256);
+        if (out.nh) k_add_slices<<<g, 256, 0, strm>>>(out.nh, ws->hn, blk, nsh, ws->hmap);
+        if (out.Eh) k_add_slices<<<g, 256, 0, strm>>>(out.Eh, ws->hE, blk, nsh, ws->hmap);
+        if (out.Ek) k_add_slices<<<g, 256, 0, strm>>>(out.Ek, ws->hK, blk, nsh, ws->hmap);
+        if (out.E_h) k_add_slices<<<(unsigned)((Nt * nsh + 255) / 256), 256, 0, strm>>>(out.E_h, ws->htE, (size_t)Nt, nsh, ws->hmap);
+        launches += 4;
+        CK(cudaGetLastError());
     }
-    CK(cudaEventRecord(e1, strm));
-    CK(cudaEventSynchronize(e1));
+    CK(cudaEventRecord(ws->e1, strm));
+    CK(cudaEventSynchronize(ws->e1));
     float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    CK(cudaEventElapsedTime(&ms, ws->e0, ws->e1));
     if (st) {
         st->n_shi += ev_tot[0]; st->n_el_inelastic += ev_tot[1]; st->n_el_elastic += ev_tot[2];
         st->n_hole_events += ev_tot[3]; st->n_auger += ev_tot[4]; st->n_radiative += ev_tot[5];
         st->n_photon_abs += ev_tot[6]; st->n_particles += ev_tot[7];
-        st->n_events += ev_tot[0] + ev_tot[1] + ev_tot[2] + ev_tot[3] + ev_tot[4] + ev_tot[5] + ev_tot[6];
+        uint64_t step_ev = ev_tot[1] + ev_tot[2] + ev_tot[3] + ev_tot[4] + ev_tot[5] + ev_tot[6];
+        st->n_events += ev_tot[0] + step_ev;
         st->error_bits |= err_bits;
         st->n_steps += steps;
         st->device_ms += ms;
         st->n_kernel_launches += launches;
+        st->step_ms += step_ms;
+        st->step_events += step_ev;
+        st->step_launches += steps;
+        st->peak_queue = std::max<uint64_t>(st->peak_queue, peak_all);
+        st->batch_iterations = B;
+        st->h2d_bytes += h2d;
+        st->d2h_bytes += d2h;
     }
     return TREKIS_OK;
 }
+
+template <class T>
+static double* calls_of(trekis_tables* t) { return ((Workspace<T>*)t->ws.get())->calls; }
+
+template <class T>
+static double* out_of(trekis_tables* t, size_t* n) { auto* w = (Workspace<T>*)t->ws.get(); *n = w->out_n; return w->out; }
 
 }  // namespace tk
 
@@ -425,7 +572,8 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
     rc = build_tables_device(t, *cfg, st);
     if (!rc) rc = upload_mc<float>(t, t->d32);
     if (!rc) rc = upload_mc<double>(t, t->d64);
-    if (!rc && t->has_shi) rc = upload_shi(t);
+    if (!rc && t->has_shi) rc = upload_shi<float>(t, t->dshi32);
+    if (!rc && t->has_shi) rc = upload_shi<double>(t, t->dshi64);
     if (rc) { delete t; if (st) st->code = rc; return rc; }
     *out = t;
     if (st) st->code = TREKIS_OK;
@@ -500,15 +648,50 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
     return TREKIS_OK;
 }
 
-static int run_dispatch(const trekis_tables* tc, const trekis_run_cfg* cfg, int Nt, int Nshl, DevOut d,
-                        trekis_status* st) {
+static int run_dispatch(const trekis_tables* tc, const trekis_run_cfg* cfg, int Nt, int Nat, int Nshl, DevOut d,
+                        trekis_status* st, cudaStream_t s) {
     trekis_tables* t = const_cast<trekis_tables*>(tc);
-    cudaStream_t s;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return TREKIS_ECUDA;
-    int rc = (cfg->precision == 1) ? run_mc<double>(t, *cfg, Nt, Nshl, d, st, s) : run_mc<float>(t, *cfg, Nt, Nshl, d, st, s);
-    cudaStreamSynchronize(s);
-    cudaStreamDestroy(s);
-    return rc;
+    return (cfg->precision == 1) ? run_mc<double>(t, *cfg, Nt, Nat, Nshl, d, st, s)
+                                 : run_mc<float>(t, *cfg, Nt, Nat, Nshl, d, st, s);
+}
+
+// Accumulate into device tallies; `scratch` (n_scr doubles, zeroed) backs outputs the caller skipped.
+static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, int Nt, trekis_tallies* o,
+                           trekis_status* st, cudaStream_t s, double* scratch_host_path) {
+    trekis_tables* t = const_cast<trekis_tables*>(tc);
+    const size_t n2 = (size_t)Nt * cfg->N_R, n4 = n2 * o->Nat * o->Nshl, n3 = (size_t)Nt * o->Nat * o->Nshl;
+    // the workspace holds the per-call sums; create it first
+    int rc = 0;
+    double* calls;
+    if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) return rc; calls = calls_of<double>(t); }
+    else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) return rc; calls = calls_of<float>(t); }
+    (void)scratch_host_path;
+    CK(cudaMemsetAsync(calls, 0, 8 * (3 * (size_t)Nt + n3), s));
+    double* Ee_call = calls;
+    double* Ep_call = calls + Nt;
+    double* Eat_call = calls + 2 * (size_t)Nt;
+    double* Eh_call = calls + 3 * (size_t)Nt;
+    DevOut d;
+    d.ne = o->Out_ne; d.Ee = o->Out_Ee; d.np = o->Out_nphot; d.Ep = o->Out_Ephot; d.lat = o->Out_Elat;
+    d.nh = o->Out_nh; d.Eh = o->Out_Eh; d.Ek = o->Out_Ehkin;
+    d.totNe = o->Out_tot_Ne; d.totNp = o->Out_tot_Nphot; d.totE = o->Out_tot_E;
+    d.E_e = Ee_call; d.E_p = Ep_call; d.E_at = Eat_call; d.E_h = Eh_call;
+    if (!d.ne || !d.Ee || !d.np || !d.Ep || !d.lat || !d.totNe || !d.totNp) {
+        set_error("the device entry point needs every radial and count tally array");
+        return TREKIS_EINVAL;
+    }
+    rc = run_dispatch(t, cfg, Nt, o->Nat, o->Nshl, d, st, s);
+    if (rc) return rc;
+    const int phot = t->mat.include_photons;
+    if (o->Out_tot_E) k_derive<<<(Nt + 127) / 128, 128, 0, s>>>(Nt, o->Nat * o->Nshl, phot, Ee_call, Eh_call, Ep_call, Eat_call, o->Out_tot_E);
+    if (o->Out_E_e) k_add<<<(Nt + 127) / 128, 128, 0, s>>>(o->Out_E_e, Ee_call, Nt);
+    if (o->Out_E_phot) k_add<<<(Nt + 127) / 128, 128, 0, s>>>(o->Out_E_phot, Ep_call, Nt);
+    if (o->Out_E_at) k_add<<<(Nt + 127) / 128, 128, 0, s>>>(o->Out_E_at, Eat_call, Nt);
+    if (o->Out_E_h) k_add<<<(unsigned)((n3 + 127) / 128), 128, 0, s>>>(o->Out_E_h, Eh_call, n3);
+    CK(cudaGetLastError());
+    if (st) st->n_kernel_launches += 5;
+    (void)n4;
+    return TREKIS_OK;
 }
 
 int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat, const trekis_ion* ion,
@@ -518,62 +701,30 @@ int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
     int rc = check_run(t, mat, cfg, o, &Nt);
     if (!rc && !device_ok()) rc = TREKIS_ENODEVICE;
     if (rc) { if (st) st->code = rc; return rc; }
-    // scratch for outputs the caller skipped
-    Buffers b;
-    const size_t n2 = (size_t)Nt * cfg->N_R, n4 = n2 * o->Nat * o->Nshl, n3 = (size_t)Nt * o->Nat * o->Nshl;
-    auto need = [&](double* p, size_t n) -> double* {
-        if (p) return p;
-        double* q = (double*)b.alloc(8 * n);
-        if (q) cudaMemset(q, 0, 8 * n);
-        return q;
-    };
-    DevOut d;
-    d.ne = need(o->Out_ne, n2); d.Ee = need(o->Out_Ee, n2); d.np = need(o->Out_nphot, n2); d.Ep = need(o->Out_Ephot, n2);
-    d.lat = need(o->Out_Elat, n2); d.nh = need(o->Out_nh, n4); d.Eh = need(o->Out_Eh, n4); d.Ek = need(o->Out_Ehkin, n4);
-    d.totNp = need(o->Out_tot_Nphot, Nt); d.totE = need(o->Out_tot_E, Nt);
-    // per-call copies of the summed quantities that feed tot_E
-    d.totNe = need(o->Out_tot_Ne, Nt);
-    double* Ee_call = (double*)b.alloc(8 * Nt);
-    double* Ep_call = (double*)b.alloc(8 * Nt);
-    double* Eat_call = (double*)b.alloc(8 * Nt);
-    double* Eh_call = (double*)b.alloc(8 * n3);
-    if (!Ee_call || !Ep_call || !Eat_call || !Eh_call) return TREKIS_ENOMEM;
-    cudaMemset(Ee_call, 0, 8 * Nt); cudaMemset(Ep_call, 0, 8 * Nt); cudaMemset(Eat_call, 0, 8 * Nt);
-    cudaMemset(Eh_call, 0, 8 * n3);
-    d.E_e = Ee_call; d.E_p = Ep_call; d.E_at = Eat_call; d.E_h = Eh_call;
-    rc = run_dispatch(t, cfg, Nt, o->Nshl, d, st);
-    if (rc) { if (st) st->code = rc; return rc; }
-    // fold the per-call sums into the caller's arrays and tot_E
-    k_derive<<<(Nt + 127) / 128, 128>>>(Nt, o->Nat * o->Nshl, t->mat.include_photons, Ee_call, Eh_call, Ep_call, Eat_call, d.totE);
-    auto addv = [&](double* dst, const double* src, size_t n) -> int {
-        if (!dst) return 0;
-        std::vector<double> a(n), c(n);
-        if (cudaMemcpy(a.data(), src, 8 * n, cudaMemcpyDeviceToHost) != cudaSuccess) return TREKIS_ECUDA;
-        if (cudaMemcpy(c.data(), dst, 8 * n, cudaMemcpyDeviceToHost) != cudaSuccess) return TREKIS_ECUDA;
-        for (size_t x = 0; x < n; ++x) c[x] += a[x];
-        if (cudaMemcpy(dst, c.data(), 8 * n, cudaMemcpyHostToDevice) != cudaSuccess) return TREKIS_ECUDA;
-        return 0;
-    };
-    rc = addv(o->Out_E_e, Ee_call, Nt);
-    if (!rc) rc = addv(o->Out_E_phot, Ep_call, Nt);
-    if (!rc) rc = addv(o->Out_E_at, Eat_call, Nt);
-    if (!rc) rc = addv(o->Out_E_h, Eh_call, n3);
-    if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = TREKIS_ECUDA;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return TREKIS_ECUDA;
+    rc = run_device_core(t, cfg, Nt, o, st, s, nullptr);
+    if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = TREKIS_ECUDA;
+    cudaStreamDestroy(s);
     if (st) st->code = rc;
     return rc;
 }
 
-int32_t trekis_mc_run(const trekis_tables* t, const trekis_material* mat, const trekis_ion* ion,
+int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const trekis_ion* ion,
                       const trekis_run_cfg* cfg, trekis_tallies* o, trekis_status* st) {
+    (void)ion;
     int Nt = 0;
-    int rc = check_run(t, mat, cfg, o, &Nt);
+    int rc = check_run(tc, mat, cfg, o, &Nt);
     if (!rc && !device_ok()) rc = TREKIS_ENODEVICE;
     if (rc) { if (st) st->code = rc; return rc; }
+    trekis_tables* t = const_cast<trekis_tables*>(tc);
     const size_t n2 = (size_t)Nt * cfg->N_R, n4 = n2 * o->Nat * o->Nshl, n3 = (size_t)Nt * o->Nat * o->Nshl;
-    Buffers b;
-    double* base = (double*)b.alloc(8 * (5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3));
-    if (!base) return TREKIS_ENOMEM;
-    if (cudaMemset(base, 0, 8 * (5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3)) != cudaSuccess) return TREKIS_ECUDA;
+    if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) { if (st) st->code = rc; return rc; } }
+    else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) { if (st) st->code = rc; return rc; } }
+    size_t nout = 0;
+    double* base = (cfg->precision == 1) ? out_of<double>(t, &nout) : out_of<float>(t, &nout);
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return TREKIS_ECUDA;
     trekis_tallies d = *o;
     double* p = base;
     double** fld[] = {&d.Out_ne, &d.Out_Ee, &d.Out_nphot, &d.Out_Ephot, &d.Out_Elat};
@@ -582,16 +733,21 @@ int32_t trekis_mc_run(const trekis_tables* t, const trekis_material* mat, const 
     double** f1[] = {&d.Out_tot_Ne, &d.Out_tot_Nphot, &d.Out_tot_E, &d.Out_E_e, &d.Out_E_phot, &d.Out_E_at};
     for (double** f : f1) { *f = p; p += Nt; }
     d.Out_E_h = p;
-    rc = trekis_mc_run_device(t, mat, ion, cfg, &d, st);
-    if (rc) return rc;
-    std::vector<double> h(5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3);
-    if (cudaMemcpy(h.data(), base, 8 * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess) return TREKIS_ECUDA;
+    rc = (cudaMemsetAsync(base, 0, 8 * nout, s) == cudaSuccess) ? 0 : TREKIS_ECUDA;
+    if (!rc) rc = run_device_core(t, cfg, Nt, &d, st, s, base);
+    std::vector<double> h(nout);
+    if (!rc && cudaMemcpyAsync(h.data(), base, 8 * nout, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = TREKIS_ECUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = TREKIS_ECUDA;
+    cudaStreamDestroy(s);
+    if (rc) { if (st) st->code = rc; return rc; }
+    if (st) st->d2h_bytes += 8 * nout;
     size_t off = 0;
     auto add = [&](double* dst, size_t n) { if (dst) for (size_t x = 0; x < n; ++x) dst[x] += h[off + x]; off += n; };
     add(o->Out_ne, n2); add(o->Out_Ee, n2); add(o->Out_nphot, n2); add(o->Out_Ephot, n2); add(o->Out_Elat, n2);
     add(o->Out_nh, n4); add(o->Out_Eh, n4); add(o->Out_Ehkin, n4);
     add(o->Out_tot_Ne, Nt); add(o->Out_tot_Nphot, Nt); add(o->Out_tot_E, Nt); add(o->Out_E_e, Nt);
     add(o->Out_E_phot, Nt); add(o->Out_E_at, Nt); add(o->Out_E_h, n3);
+    if (st) st->code = TREKIS_OK;
     return TREKIS_OK;
 }
 

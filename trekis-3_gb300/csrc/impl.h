@@ -1,6 +1,7 @@
 // impl.h -- host-side structures of the library (not part of the C ABI).
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <vector>
 #include "../../include/trekis_gb300.h"
@@ -53,15 +54,20 @@ struct DevTabs {
     const T* dosE; const T* dosD; const T* dosI; const T* dosM; int nD;
 };
 
-// SHI tables are always FP64 (the ion energy is ~1e8 eV).
+// SHI tables in the precision of the run, with host-precomputed logarithms so
+// the serial ion track evaluates each log-log interpolation with one exp.
+template <class T>
 struct DevShi {
-    const double* sE; int nS;
-    const double* sL;      // [nsh][nS]
-    const double* path;    // [nS] total
-    const int* d_off;      // [nsh+1] transfer rows at the initial energy
-    const double* dE;      // lower edges
-    const double* dL;      // cumulative MFP
-    const double* dInvL;   // 1/L
+    const T* sE; const T* lE; int nS;  // SHI energy grid and log(E)
+    const T* sL; const T* lL;          // [nsh][nS] per-shell MFP and log
+    const T* pL; const T* lpL;         // [nS] total MFP (SHI_path) and log
+    const int* d_off;                  // [nsh+1] transfer rows at the initial energy
+    const T* dE; const T* ldE;         // lower edges of the transfer rows and log
+    const T* dI; const T* ldI;         // 1/L of the rows and log
+    const T* invdL_ip;                 // [nsh] 1/L at the ionisation potential (0: none)
+    const T* invL_last;                // [nsh] 1/L at the end of the row
+    const int* Mt;                     // [nsh] index of Ip in the row (Find_in_array_monoton)
+    T pow_zp;                          // Z_ion^0.66666666
 };
 
 struct Buffers {          // device allocations owned by a table set
@@ -89,9 +95,14 @@ struct trekis_tables {
     tk::Buffers buf;
     tk::DevTabs<float> d32;
     tk::DevTabs<double> d64;
-    tk::DevShi dshi;
+    tk::DevShi<float> dshi32;
+    tk::DevShi<double> dshi64;
     double build_ms = 0.0;
     uint64_t build_points = 0;
+    // reusable MC workspace (queues, int64 tallies, staging), rebuilt when the
+    // precision, capacity or tally shape of a call changes
+    std::shared_ptr<void> ws;
+    uint64_t ws_key = 0;
 };
 
 namespace tk {

@@ -447,130 +447,197 @@ __device__ __forceinline__ void push(const McConst<T>& C, const Tal& tal, const 
     if (i >= 0) store(q, i, p);
 }
 
-// ---- SHI track: one thread per iteration (FP64 ion) -----------------------------------
+// ---- SHI track ----------------------------------------------------------------------
+// log-log interpolation with precomputed logs: Interpolate(5, ...) (CS:4051-4086)
 template <class T>
-__global__ void __launch_bounds__(128) k_shi(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, DevShi sh, PQ<T> qe,
-                                             PQ<T> qh, Tal tal, Ctrs* ctr, int nit) {
+__device__ __forceinline__ T interp5_pre(T E1, T E2, T lE1, T lE2, T S1, T lS1, T lS2, T Ex, T lx) {
+    if (m_abs(E2 - E1) < T(1.0e-6)) { return S1; }   // caller passes S1 = max(S1,S2) in that case
+    if (Ex == E1) return S1;
+    return m_exp(lS1 + (lS2 - lS1) / (lE2 - lE1) * (lx - lE1));
+}
+
+// per-shell / total SHI MFP at the bracket nb (Which_shell MC:1803-1813, Next_free_path_2d MC:1874-1899)
+template <class T>
+__device__ __forceinline__ T shi_mfp_shell(const DevShi<T>& sh, const T* L, const T* lL, int nb, T E, T lx) {
+    if (nb == 1) return T(1.0e20);
+    const T L1 = L[nb - 2], L2 = L[nb - 1];
+    if (L1 == L2 || L1 > T(1e20)) return L1;
+    const T E1 = sh.sE[nb - 2], E2 = sh.sE[nb - 1];
+    if (m_abs(E2 - E1) < T(1.0e-6)) return L1 > L2 ? L1 : L2;
+    return interp5_pre(E1, E2, sh.lE[nb - 2], sh.lE[nb - 1], L1, lL[nb - 2], lL[nb - 1], E, lx);
+}
+template <class T>
+__device__ __forceinline__ T shi_path(const DevShi<T>& sh, int nb, T E, T lx) {
+    const T* L = sh.pL;
+    if (nb == 1) {
+        T M = interp<T>(1, sh.sE[0], sh.sE[1], L[0], L[1], E);
+        return M < L[0] ? L[0] : M;
+    }
+    const T L1 = L[nb - 2], L2 = L[nb - 1];
+    if (L1 >= T(1.0e16)) return L1;
+    const T E1 = sh.sE[nb - 2], E2 = sh.sE[nb - 1];
+    if (m_abs(E2 - E1) < T(1.0e-6)) return L1 > L2 ? L1 : L2;
+    return interp5_pre(E1, E2, sh.lE[nb - 2], sh.lE[nb - 1], L1, sh.lpL[nb - 2], sh.lpL[nb - 1], E, lx);
+}
+
+struct ShiEv {  // one SHI collision: the ion state after it and the transfer
+    double E, Zeff, t0, Z, dE;
+    int k;
+    uint32_t ord;
+    int it;
+    int pad;
+};
+
+// The ion of each iteration, one thread each: Which_shell, SHI_energy_transfer,
+// next free path and the charge update (SHI_Monte_Carlo, MC:2153-2196).  The
+// energy, depth and time accumulate in FP64; the table arithmetic is in T.
+template <class T>
+__global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__ Cp, DevShi<T> sh,
+                                                  ShiEv* __restrict__ evs, int64_t cap_ev, Ctrs* ctr, int nit) {
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= nit) return;
     const McConst<T>& C = *Cp;
     unsigned err = 0;
     unsigned long long nev = 0;
     const uint64_t pid = shi_pid(C.it0 + it);
-    double E = C.ion_E0, t0 = 0.0, tn = 0.0, X = 0.0, Y = 0.0, Z = 0.0, L;
-    const double MSHI = C.MSHI;
-    const Tab<double> path{sh.sE, sh.path, sh.nS};
+    double E = C.ion_E0, t0 = 0.0, tn, Z = 0.0, L;
     {
         EvStream<T> s(C.seed, pid, 0xFFFFFFFFu);
-        L = nfp2(path, E);
-        L = -L * log(s.next_d());
-        double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
+        const T Et = (T)E, lx = m_log(Et);
+        const int nb = find_monoton(sh.sE, sh.nS, Et);
+        L = (double)shi_path(sh, nb, Et, lx);
+        L = -L * (double)m_log(s.next());
+        const double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
         tn = (V > 1.0e-10) ? t0 + L / V * 1e5 : 1.0e25;
     }
-    Out<T> o{qe, qh, qe, ctr};
     uint32_t ord = 0;
     while (tn < (double)C.Tim) {
         if (ord >= (1u << 26)) { err |= TREKIS_ERR_NAN; break; }   // no SHI track has this many collisions
         EvStream<T> s(C.seed, pid, ord);
-        // Which_shell over the SHI tables
-        int k;
+        const T Et = (T)E, lx = m_log(Et);
+        const int nb = find_monoton(sh.sE, sh.nS, Et);
+        // Which_shell
+        int k = C.nsh - 1;
         {
-            double inv[MAXSH], tot = 0.0;
-            int nb = find_monoton(sh.sE, sh.nS, E);
+            T inv[MAXSH], tot = T(0);
             for (int q = 0; q < C.nsh; ++q) {
-                const double* Lq = sh.sL + (size_t)q * sh.nS;
-                double M;
-                if (nb == 1) M = 1.0e20;
-                else if (Lq[nb - 2] == Lq[nb - 1] || Lq[nb - 2] > 1e20) M = Lq[nb - 2];
-                else M = interp<double>(5, sh.sE[nb - 2], sh.sE[nb - 1], Lq[nb - 2], Lq[nb - 1], E);
-                inv[q] = 1.0 / M;
+                inv[q] = T(1) / shi_mfp_shell(sh, sh.sL + (size_t)q * sh.nS, sh.lL + (size_t)q * sh.nS, nb, Et, lx);
                 tot += inv[q];
             }
-            tot = s.next_d() * tot;
-            double sum = 0.0;
-            k = C.nsh - 1;
+            tot = s.next() * tot;
+            T sum = T(0);
             for (int q = 0; q < C.nsh; ++q) { sum += inv[q]; if (sum >= tot) { k = q; break; } }
         }
-        // SHI_energy_transfer (MC:1719-1780), CDF branch
+        // SHI_energy_transfer (MC:1719-1780): inverse of the cumulative row at the initial energy
         double dE;
         {
+            const T RN = s.next();
             const int o0 = sh.d_off[k], N = sh.d_off[k + 1] - o0;
-            const double* DE = sh.dE + o0;
-            const double* DL = sh.dL + o0;
-            const double* DI = sh.dInvL + o0;
-            double RN = s.next_d();
-            const double Ip = C.Ipd[k];
-            if (N < 1) { dE = Ip; goto transferred; }   // shell beyond the SHI's maximum transfer
-            {
-            int Mt = find_monoton(DE, N, Ip);
-            double dL;
-            if (Mt > 1) dL = (DL[Mt - 2] > 1.0e-10) ? interp<double>(5, DE[Mt - 2], DE[Mt - 1], DL[Mt - 2], DL[Mt - 1], Ip)
-                                                    : interp<double>(1, DE[Mt - 2], DE[Mt - 1], DL[Mt - 2], DL[Mt - 1], Ip);
-            else dL = DL[0];
-            double Tot = (dL > 0.0 && DL[N - 1] > 0.0) ? 1.0 / dL + RN * (1.0 / DL[N - 1] - 1.0 / dL) : 1.5e21;
-            int nt;
-            if (Tot < 1e20) {  // first index with 1/L >= Tot (Find_in_1D_array, RF:3348), by bisection
-                int lo = 0, hi = N - 1;
-                while (lo < hi) { int mid = (lo + hi) >> 1; if (DI[mid] < Tot) lo = mid + 1; else hi = mid; }
-                nt = lo + 1;
-            } else nt = Mt;
-            dE = (nt > Mt) ? interp<double>(5, DI[nt - 2], DI[nt - 1], DE[nt - 2], DE[nt - 1], Tot) : Ip;
+            const T Ip = C.Ip[k];
+            if (N < 1) dE = (double)Ip;
+            else {
+                const int Mt = sh.Mt[k];
+                const T a = sh.invdL_ip[k], b = sh.invL_last[k];
+                const T Tot = (a > T(0) && b > T(0)) ? a + RN * (b - a) : T(1.5e21);
+                int nt;
+                if (Tot < T(1e20)) {
+                    const T* DI = sh.dI + o0;
+                    int lo = 0, hi = N - 1;
+                    while (lo < hi) { int mid = (lo + hi) >> 1; if (DI[mid] < Tot) lo = mid + 1; else hi = mid; }
+                    nt = lo + 1;
+                } else nt = Mt;
+                if (nt > Mt) {
+                    const T* DI = sh.dI + o0;
+                    const T* DE = sh.dE + o0;
+                    const T E1 = DI[nt - 2], E2 = DI[nt - 1];
+                    T r;
+                    if (m_abs(E2 - E1) < T(1.0e-6)) r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
+                    else if (Tot == E1) r = DE[nt - 2];
+                    else r = m_exp(sh.ldE[o0 + nt - 2] + (sh.ldE[o0 + nt - 1] - sh.ldE[o0 + nt - 2]) /
+                                   (sh.ldI[o0 + nt - 1] - sh.ldI[o0 + nt - 2]) * (m_log(Tot) - sh.ldI[o0 + nt - 2]));
+                    dE = (double)r;
+                } else dE = (double)Ip;
             }
         }
-    transferred:
-        double Lnew = nfp2(path, E);
-        Lnew = -Lnew * log(s.next_d());
-        const double Znew = Z + L;
-        E -= dE; t0 = tn; Z = Znew; L = Lnew;
-        {
-            double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
-            tn = (V > 1.0e-10) ? t0 + L / V * 1e5 : 1.0e25;
-        }
+        // next flight with the energy before the loss
+        double Lnew = (double)shi_path(sh, nb, Et, lx);
+        Lnew = -Lnew * (double)m_log(s.next());
+        Z = Z + L;
+        E -= dE; t0 = tn; L = Lnew;
+        const double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
+        tn = (V > 1.0e-10) ? t0 + L / V * 1e5 : 1.0e25;
         // Equilibrium_charge_SHI (CS:2641-2680)
         double Zeff;
         {
-            double vp = E > 0.0 ? sqrt(2.0 * E * kE / (C.ion_mass_p * kMp)) : 0.0;
-            double Zp = C.ion_Z, v0 = sqrt(2.0 * kRy * kE / kMe);
-            switch (C.ion_kind_zeff) {
-            case 1: Zeff = Zp * (1.0 - exp(-(vp / v0 / pow(Zp, 0.66666666)))); break;
-            case 2: Zeff = Zp * pow(1.0 + pow(vp / (pow(Zp, 0.45) * v0 * 4.0 / 3.0), -1.0 / 0.6), -0.6); break;
-            case 3: {
-                double Zt = C.Zt, c1 = 1.0 - 0.26 * exp(-Zt / 11.0 - (Zt - Zp) * (Zt - Zp) / 9.0);
-                double vpvo = pow(Zp, -0.543) * vp / v0, c2 = 1.0 + 0.03 * vpvo * log(Zt);
-                double x = c1 * pow(vpvo / c2 / 1.54, 1.0 + 1.83 / Zp), x2 = x * x, x4 = x2 * x2;
-                Zeff = Zp * (8.29 * x + x4) / (0.06 / x + 4.0 + 7.4 * x + x4);
-            } break;
-            case 4: Zeff = C.ion_fixed_zeff; break;
-            default: Zeff = Zp * (1.0 - exp(-(vp * 125.0 / kC / pow(Zp, 0.66666666))));
+            const double vp = E > 0.0 ? sqrt(2.0 * E * kE / (C.ion_mass_p * kMp)) : 0.0;
+            const double Zp = C.ion_Z;
+            if (C.ion_kind_zeff == 0) Zeff = Zp * (1.0 - exp(-(vp * 125.0 / kC / (double)sh.pow_zp)));
+            else {
+                const double v0 = sqrt(2.0 * kRy * kE / kMe);
+                switch (C.ion_kind_zeff) {
+                case 1: Zeff = Zp * (1.0 - exp(-(vp / v0 / (double)sh.pow_zp))); break;
+                case 2: Zeff = Zp * pow(1.0 + pow(vp / (pow(Zp, 0.45) * v0 * 4.0 / 3.0), -1.0 / 0.6), -0.6); break;
+                case 3: {
+                    double Zt = C.Zt, c1 = 1.0 - 0.26 * exp(-Zt / 11.0 - (Zt - Zp) * (Zt - Zp) / 9.0);
+                    double vpvo = pow(Zp, -0.543) * vp / v0, c2 = 1.0 + 0.03 * vpvo * log(Zt);
+                    double x = c1 * pow(vpvo / c2 / 1.54, 1.0 + 1.83 / Zp), x2 = x * x, x4 = x2 * x2;
+                    Zeff = Zp * (8.29 * x + x4) / (0.06 / x + 4.0 + 7.4 * x + x4);
+                } break;
+                default: Zeff = C.ion_fixed_zeff;
+                }
             }
         }
-        // the electron-hole pair
-        P<T> el;
-        el.pid = child_pid(pid, ord, 0); el.ord = 0; el.sh = 0; el.Ek = T(0); el.M = T(0);
-        T dEc = electron_receives(C, tb, (T)dE, k, s, err);
-        T theta = (E <= 0.0) ? pi_<T>() / T(2)
-            : (T)acos(sqrt((MSHI + kMe) * (MSHI + kMe) / (4.0 * MSHI * kMe) * dE / E));
-        T phi = T(2) * pi_<T>() * s.next();
-        el.E = dEc; el.t0 = (T)t0;
-        electron_flight(tb, el, s);
-        double Aa = 1.0 + MSHI / kMe;
-        double b = kA0 * Zeff * kRy / E * sqrt(4.0 * E / dE * MSHI / kMe - Aa * Aa);
-        el.X = (T)(X + b * sin((double)phi)); el.Y = (T)(Y + b * cos((double)phi)); el.Z = (T)Z;
-        el.th = theta; el.ph = phi;
-        cut_e(C, el);
-        if (el.E < T(-1.0e-9) || m_isnan(el.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
-        emit_electron(C, tal, el);
-        push(C, tal, o, 0, el);
-        P<T> hh;
-        hh.pid = child_pid(pid, ord, 1); hh.ord = 0;
-        make_hole(C, tb, hh, (T)t0, el.X, el.Y, el.Z, k, (T)dE - dEc, s, err);
-        emit_hole(C, tal, hh);
-        push(C, tal, o, 1, hh);
+        const int64_t slot = atomicAdd((unsigned long long*)&ctr->ev[0], 1ull);
+        if (slot < cap_ev) {
+            ShiEv ev;
+            ev.E = E; ev.Zeff = Zeff; ev.t0 = t0; ev.Z = Z; ev.dE = dE; ev.k = k; ev.ord = ord; ev.it = it; ev.pad = 0;
+            evs[slot] = ev;
+        } else atomicExch(&ctr->overflow, 1);
         ++ord; ++nev;
         if (Z >= C.Layer) tn = 1.0e16;
     }
-    atomicAdd(&ctr->ev[0], nev);
-    atomicAdd(&ctr->ev[7], 2ull * nev);
+    if (err) atomicOr(&ctr->err_bits, err);
+}
+
+// The electron-hole pair of each SHI collision, one thread each (MC:2198-2247);
+// draws continue in the collision's stream after the ion's three.
+template <class T>
+__global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp, DevTabs<T> tb,
+                                               const ShiEv* __restrict__ evs, int64_t n_ev, PQ<T> qe, PQ<T> qh,
+                                               Tal tal, Ctrs* ctr) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_ev) return;
+    const McConst<T>& C = *Cp;
+    const ShiEv ev = evs[i];
+    const uint64_t pid = shi_pid(C.it0 + ev.it);
+    EvStream<T> s(C.seed, pid, ev.ord);
+    s.word(); s.word(); s.word();
+    unsigned err = 0;
+    const int k = ev.k;
+    const double E = ev.E, dE = ev.dE, MSHI = C.MSHI;
+    Out<T> o{qe, qh, qe, ctr};
+    P<T> el;
+    el.pid = child_pid(pid, ev.ord, 0); el.ord = 0; el.sh = 0; el.Ek = T(0); el.M = T(0);
+    const T dEc = electron_receives(C, tb, (T)dE, k, s, err);
+    const T theta = (E <= 0.0) ? pi_<T>() / T(2)
+        : (T)acos(sqrt((MSHI + kMe) * (MSHI + kMe) / (4.0 * MSHI * kMe) * dE / E));
+    const T phi = T(2) * pi_<T>() * s.next();
+    el.E = dEc; el.t0 = (T)ev.t0;
+    electron_flight(tb, el, s);
+    // Impact_parameter (MC:1113-1126)
+    const double Aa = 1.0 + MSHI / kMe;
+    const double b = kA0 * ev.Zeff * kRy / E * sqrt(4.0 * E / dE * MSHI / kMe - Aa * Aa);
+    el.X = (T)(b * sin((double)phi)); el.Y = (T)(b * cos((double)phi)); el.Z = (T)ev.Z;
+    el.th = theta; el.ph = phi;
+    cut_e(C, el);
+    if (el.E < T(-1.0e-9) || m_isnan(el.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
+    emit_electron(C, tal, el);
+    push(C, tal, o, 0, el);
+    P<T> hh;
+    hh.pid = child_pid(pid, ev.ord, 1); hh.ord = 0;
+    make_hole(C, tb, hh, (T)ev.t0, el.X, el.Y, el.Z, k, (T)dE - dEc, s, err);
+    emit_hole(C, tal, hh);
+    push(C, tal, o, 1, hh);
     if (err) atomicOr(&ctr->err_bits, err);
 }
 
@@ -878,11 +945,17 @@ __global__ void __launch_bounds__(256) k_step(const McConst<T>* __restrict__ Cp,
 }
 
 template <class T>
-void launch_shi(const McConst<T>* C, const DevTabs<T>& tb, const DevShi& sh, PQ<T> qe, PQ<T> qh, Tal tal, Ctrs* ctr,
-                int nit, int bs, cudaStream_t s) {
-    bs = bs > 128 ? 128 : bs;
-    k_shi<T><<<(nit + bs - 1) / bs, bs, 0, s>>>(C, tb, sh, qe, qh, tal, ctr, nit);
+void launch_shi(const McConst<T>* C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
+                cudaStream_t s) {
+    k_shi_track<T><<<(nit + 63) / 64, 64, 0, s>>>(C, sh, (ShiEv*)evs, cap_ev, ctr, nit);
 }
+template <class T>
+void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qh,
+                  Tal tal, Ctrs* ctr, cudaStream_t s) {
+    if (n_ev <= 0) return;
+    k_pairs<T><<<(unsigned)((n_ev + 127) / 128), 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qh, tal, ctr);
+}
+size_t shi_event_bytes() { return sizeof(ShiEv); }
 
 template <class T>
 void launch_step(const McConst<T>* C, const DevTabs<T>& tb, PQ<T> ie, int ne, PQ<T> ih, int nh, PQ<T> ip, int np,
@@ -893,10 +966,12 @@ void launch_step(const McConst<T>* C, const DevTabs<T>& tb, PQ<T> ie, int ne, PQ
     k_step<T><<<be + bh + bp, bs, 0, s>>>(C, tb, ie, ne, ih, nh, ip, np, o, tal, K, be, bh);
 }
 
-template void launch_shi<float>(const McConst<float>*, const DevTabs<float>&, const DevShi&, PQ<float>, PQ<float>, Tal,
-                                Ctrs*, int, int, cudaStream_t);
-template void launch_shi<double>(const McConst<double>*, const DevTabs<double>&, const DevShi&, PQ<double>, PQ<double>,
-                                 Tal, Ctrs*, int, int, cudaStream_t);
+template void launch_shi<float>(const McConst<float>*, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t);
+template void launch_shi<double>(const McConst<double>*, const DevShi<double>&, void*, int64_t, Ctrs*, int, cudaStream_t);
+template void launch_pairs<float>(const McConst<float>*, const DevTabs<float>&, const void*, int64_t, PQ<float>,
+                                  PQ<float>, Tal, Ctrs*, cudaStream_t);
+template void launch_pairs<double>(const McConst<double>*, const DevTabs<double>&, const void*, int64_t, PQ<double>,
+                                   PQ<double>, Tal, Ctrs*, cudaStream_t);
 template void launch_step<float>(const McConst<float>*, const DevTabs<float>&, PQ<float>, int, PQ<float>, int,
                                  PQ<float>, int, PQ<float>, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, cudaStream_t);
 template void launch_step<double>(const McConst<double>*, const DevTabs<double>&, PQ<double>, int, PQ<double>, int,
@@ -938,18 +1013,22 @@ __global__ void k_fin(const unsigned long long* cnt, const unsigned long long* e
     if (tn_) tn_[i + (size_t)Nt * s] += (double)sc;
     if (tE) tE[i + (size_t)Nt * s] += (double)se / kEScale;
 }
-__global__ void k_fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t != 0) return;
-    long long cum = 0;
-    for (int i = 0; i < Nt; ++i) {
-        for (int j = 0; j < NR; ++j) {
-            long long v = (long long)lat[(size_t)i * NR + j];
-            oL[(size_t)i + (size_t)Nt * j] += (double)v / kLatScale * V[j];
-            cum += v;
-        }
-        Eat[i] += (double)cum / kLatScale;
+__global__ void k_fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL,
+                          long long* rows) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= Nt) return;
+    long long sum = 0;
+    for (int j = 0; j < NR; ++j) {
+        long long v = (long long)lat[(size_t)t * NR + j];
+        oL[(size_t)t + (size_t)Nt * j] += (double)v / kLatScale * V[j];
+        sum += v;
     }
+    rows[t] = sum;
+}
+__global__ void k_fin_lat_scan(const long long* rows, int Nt, double* Eat) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long cum = 0;
+    for (int i = 0; i < Nt; ++i) { cum += rows[i]; Eat[i] += (double)cum / kLatScale; }
 }
 
 void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
@@ -959,7 +1038,9 @@ void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long lo
     int n2 = ns * Nt;
     k_fin<<<(n2 + 127) / 128, 128, 0, s>>>(cnt, en, ek, Nt, NR, ns, V, on, oE, oK, tn_, tE);
 }
-void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat, cudaStream_t s) {
-    k_fin_lat<<<1, 32, 0, s>>>(lat, Nt, NR, V, oL, Eat);
+void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,
+             long long* rows, cudaStream_t s) {
+    k_fin_lat<<<(Nt + 127) / 128, 128, 0, s>>>(lat, Nt, NR, V, oL, rows);
+    k_fin_lat_scan<<<1, 32, 0, s>>>(rows, Nt, Eat);
 }
 }  // namespace tk

@@ -59,13 +59,18 @@ struct Ctrs {
 };
 
 template <class T>
-void launch_shi(const McConst<T>* C, const DevTabs<T>& tb, const DevShi& sh, PQ<T> qe, PQ<T> qh, Tal tal,
-                Ctrs* ctr, int nit, int bs, cudaStream_t s);
+void launch_shi(const McConst<T>* C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
+                cudaStream_t s);
+template <class T>
+void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qh,
+                  Tal tal, Ctrs* ctr, cudaStream_t s);
+size_t shi_event_bytes();
 template <class T>
 void launch_step(const McConst<T>* C, const DevTabs<T>& tb, PQ<T> ie, int ne, PQ<T> ih, int nh, PQ<T> ip, int np,
                  PQ<T> oe, PQ<T> oh, PQ<T> op, Tal tal, Ctrs* ctr, int K, int bs, cudaStream_t s);
 void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
                const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s);
-void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat, cudaStream_t s);
+void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,
+             long long* rows, cudaStream_t s);
 
 }  // namespace tk

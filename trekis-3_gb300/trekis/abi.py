@@ -100,6 +100,9 @@ class Status(C.Structure):
         ("n_el_elastic", C.c_uint64), ("n_hole_events", C.c_uint64), ("n_auger", C.c_uint64),
         ("n_radiative", C.c_uint64), ("n_photon_abs", C.c_uint64), ("n_particles", C.c_uint64),
         ("n_steps", C.c_uint64), ("device_ms", C.c_double), ("n_kernel_launches", C.c_uint64),
+        ("step_ms", C.c_double), ("step_events", C.c_uint64), ("step_launches", C.c_uint64),
+        ("peak_queue", C.c_uint64), ("batch_iterations", C.c_int32), ("pad_", C.c_int32),
+        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
     ]
 
     @classmethod
