@@ -113,8 +113,8 @@ def peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per k_step launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "k_step_cfg1_traffic.json"
+    """DRAM bytes per wavefront-step launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "k_hot_cfg1_traffic.json"
     try:
         d = json.load(open(p))
         return d.get("dram_bytes_per_launch"), d.get("events_per_launch")
@@ -237,7 +237,7 @@ def run_gpu(args):
     traffic = None
     if traffic_b and traffic_ev:
         traffic = traffic_b / traffic_ev * (step_ev / max(launches_step, 1))
-    roof = {"bound": "hbm", "kernel": "k_step<float> (wavefront step)", "achieved": achieved,
+    roof = {"bound": "hbm", "kernel": "k_hot<float> + k_rare<float> (wavefront step)", "achieved": achieved,
             "peak": hbm if hbm else 6800.0, "peak_source": "measured" if hbm else "fallback",
             "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "traffic": traffic,
             "bytes_per_event": bpe, "step_kernel_ms": step_ms, "step_kernel_launches": launches_step,

@@ -33,6 +33,8 @@ static int device_ok() {
     return (p.major == 10 && p.minor == 3) ? 1 : 0;
 }
 
+static bool n_fast_fail(int rc) { return rc != 0; }
+
 template <class T>
 static const T* upload(Buffers& b, const std::vector<double>& v) {
     std::vector<T> h(v.begin(), v.end());
@@ -48,10 +50,47 @@ static const int* upload_i(Buffers& b, const std::vector<int>& v) {
     return d;
 }
 
+static int find_mono_h2(const double* A, int N, double V) {
+    if (V < A[0]) return 1;
+    if (V >= A[N - 1]) return N;
+    int i1 = 1, i2 = N;
+    while (i1 != i2 - 1) { int ic = (i1 + i2) / 2; if (A[ic - 1] <= V) i1 = ic; else i2 = ic; }
+    return i1 + 1;
+}
+
+// FastTab: logs of both columns and a log-bucket index that never exceeds
+// the bisection result for any energy in the bucket after it
+template <class T>
+static int make_fast(Buffers& b, const std::vector<double>& E, const std::vector<double>& L, FastTab<T>& f) {
+    const int n = (int)E.size(), nb = 4096;
+    std::vector<double> lE(n), lL(n), Et(n);
+    for (int i = 0; i < n; ++i) { lE[i] = std::log(E[i]); lL[i] = std::log(L[i]); Et[i] = (double)(T)E[i]; }
+    f.E = upload<T>(b, E); f.L = upload<T>(b, L); f.lE = upload<T>(b, lE); f.lL = upload<T>(b, lL);
+    const double lo = std::log(E[0]) - 0.5, hi = std::log(E[n - 1]) + 0.5;
+    const double inv = nb / (hi - lo);
+    std::vector<uint16_t> h(nb);
+    for (int q = 0; q < nb; ++q) {
+        double eb = (double)(T)std::exp(lo + q / inv);
+        h[q] = (uint16_t)find_mono_h2(Et.data(), n, eb);
+    }
+    uint16_t* d = (uint16_t*)b.alloc(2 * nb);
+    if (!d || !f.E || !f.L || !f.lE || !f.lL) return TREKIS_ENOMEM;
+    if (cudaMemcpy(d, h.data(), 2 * nb, cudaMemcpyHostToDevice) != cudaSuccess) return TREKIS_ECUDA;
+    f.hint = d; f.lo = (T)lo; f.inv = (T)inv; f.n = n; f.nb = nb;
+    return TREKIS_OK;
+}
+
 template <class T>
 static int upload_mc(trekis_tables* t, DevTabs<T>& d) {
     Buffers& b = t->buf;
     const int nsh = t->nsh;
+    if (n_fast_fail(make_fast<T>(b, t->el[0].E, t->El_IMFP.L, d.fIMFP)) ||
+        n_fast_fail(make_fast<T>(b, t->el_elast.E, t->el_elast.L, d.fEMFP)) ||
+        n_fast_fail(make_fast<T>(b, t->hole[0].E, t->Hole_IMFP.L, d.fHIMFP)) ||
+        n_fast_fail(make_fast<T>(b, t->hole_elast.E, t->hole_elast.L, d.fHEMFP))) {
+        set_error("table upload failed");
+        return TREKIS_ENOMEM;
+    }
     auto cat = [&](const std::vector<HTab>& v) {
         std::vector<double> o;
         for (int k = 0; k < nsh; ++k) o.insert(o.end(), v[k].L.begin(), v[k].L.end());
@@ -200,10 +239,6 @@ static std::vector<double> tallied_times(double Tim, double dt, int flag) {
     return out;
 }
 
-template <class T>
-struct QBuf {
-    PQ<T> q[3];
-};
 
 template <class T>
 static int alloc_queue(Buffers& b, PQ<T>& q, int64_t cap, bool hole) {
@@ -260,7 +295,8 @@ struct Workspace {
     Buffers b;
     int64_t cap = 0;
     int Nt = 0, NR = 0, nsh = 0, Nat = 0, Nshl = 0;
-    QBuf<T> qa, qb;
+    QSet<T> qa, qb;
+    PQ<T> e_inel, h_inel;
     unsigned long long* tall = nullptr;
     size_t n_all = 0;
     Tal tal;
@@ -305,11 +341,14 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     Buffers& b = w->b;
     const int64_t capp = std::max<int64_t>(cap / 8, 1 << 16);
     *rc = TREKIS_ENOMEM;
-    for (QBuf<T>* q : {&w->qa, &w->qb}) {
-        if (alloc_queue(b, q->q[0], cap, false) || alloc_queue(b, q->q[1], cap, true) ||
-            alloc_queue(b, q->q[2], m.include_photons ? capp : 1, false))
+    for (QSet<T>* q : {&w->qa, &w->qb}) {
+        if (alloc_queue(b, q->q[Q_E], cap, false) || alloc_queue(b, q->q[Q_HVB], m.hole_mass < 1e3 ? cap : 1, true) ||
+            alloc_queue(b, q->q[Q_HDEEP], std::max<int64_t>(cap / 2, 1 << 16), true) ||
+            alloc_queue(b, q->q[Q_P], m.include_photons ? capp : 1, false))
             return nullptr;
     }
+    if (alloc_queue(b, w->e_inel, cap, false) || alloc_queue(b, w->h_inel, m.hole_mass < 1e3 ? cap : 1, true))
+        return nullptr;
     const int NR = cfg.N_R, nsh = t->nsh;
     const size_t rows = (size_t)Nt + 2;
     const size_t n_e = rows * NR, n_h = rows * nsh * NR, n_l = (size_t)Nt * NR;
@@ -420,8 +459,8 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         h2d += sizeof C;
         CK(cudaMemsetAsync(ws->tall, 0, 8 * ws->n_all, strm));
         CK(cudaMemsetAsync(dctr, 0, sizeof(Ctrs), strm));
-        QBuf<T>* in = &ws->qa;
-        QBuf<T>* ot = &ws->qb;
+        QSet<T>* in = &ws->qa;
+        QSet<T>* ot = &ws->qb;
         launch_shi<T>(dC, shi_of<T>(t), ws->evs, ws->cap_ev, dctr, nb, strm);
         ++launches;
         CK(cudaGetLastError());
@@ -429,27 +468,28 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         d2h += sizeof hc;
         CK(cudaStreamSynchronize(strm));
         if (!hc.overflow) {
-            launch_pairs<T>(dC, tb, ws->evs, (int64_t)hc.ev[0], ot->q[0], ot->q[1], tal, dctr, strm);
+            launch_pairs<T>(dC, tb, ws->evs, (int64_t)hc.ev[0], ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], tal, dctr, strm);
             ++launches;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
             d2h += sizeof hc;
             CK(cudaStreamSynchronize(strm));
         }
-        int64_t peak = std::max(hc.n_out[0], hc.n_out[1]);
+        auto live = [&]() { return (int64_t)hc.n_out[Q_E] + hc.n_out[Q_HVB] + hc.n_out[Q_HDEEP] + hc.n_out[Q_P]; };
+        int64_t peak = std::max(hc.n_out[Q_E], hc.n_out[Q_HVB]);
         bool overflow = hc.overflow != 0;
         uint64_t bsteps = 0, blaunch = 0;
         double bms = 0.0;
-        while (!overflow && (hc.n_out[0] + hc.n_out[1] + hc.n_out[2]) > 0) {
+        const int rare_blocks = 2 * 152;
+        while (!overflow && live() > 0) {
             if (steps + bsteps > (1ull << 24)) { set_error("wavefront did not drain"); return TREKIS_ETIMEOUT; }
             std::swap(in, ot);
-            int ne = hc.n_out[0], nh = hc.n_out[1], np = hc.n_out[2];
-            CK(cudaMemsetAsync(dctr, 0, 3 * sizeof(int), strm));
+            int n_in[4] = {hc.n_out[Q_E], hc.n_out[Q_HVB], hc.n_out[Q_HDEEP], hc.n_out[Q_P]};
+            CK(cudaMemsetAsync(dctr, 0, NQ * sizeof(int), strm));
             CK(cudaEventRecord(ws->s0, strm));
-            launch_step<T>(dC, tb, in->q[0], ne, in->q[1], nh, in->q[2], np, ot->q[0], ot->q[1], ot->q[2], tal,
-                           dctr, K, bs, strm);
+            launch_step<T>(dC, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm);
             CK(cudaEventRecord(ws->s1, strm));
-            ++blaunch; ++bsteps;
+            blaunch += 2; ++bsteps;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
             d2h += sizeof hc;
@@ -457,7 +497,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ws->s0, ws->s1));
             bms += ms;
-            peak = std::max<int64_t>(peak, std::max(hc.n_out[0], hc.n_out[1]));
+            peak = std::max<int64_t>(peak, std::max(hc.n_out[Q_E], hc.n_out[Q_HVB]));
             overflow = hc.overflow != 0;
         }
         if (overflow) {

@@ -9,6 +9,7 @@
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+#include "impl.h"
 
 namespace tk {
 
@@ -168,6 +169,34 @@ __device__ __forceinline__ T nfp1(const Tab<T>& t, T E) {
     T Ll = t.L[n - 2];
     if (Ll >= T(1.0e16)) return Ll;
     return interp<T>(5, t.E[n - 2], t.E[n - 1], Ll, t.L[n - 1], E);
+}
+
+
+// Next_free_path_2d on a FastTab: same result as nfp2 (same comparisons,
+// same log-log formula with precomputed logs); lx = log(E) is shared.
+template <class T>
+__device__ __forceinline__ int fast_find(const FastTab<T>& t, T E, T lx) {
+    if (!(E > T(0))) return find_monoton(t.E, t.n, E);
+    int b = (int)m_floor((lx - t.lo) * t.inv) - 1;
+    b = b < 0 ? 0 : (b >= t.nb ? t.nb - 1 : b);
+    int j = t.hint[b];
+    while (j < t.n && t.E[j - 1] <= E) ++j;
+    return j;
+}
+template <class T>
+__device__ __forceinline__ T nfp2_fast(const FastTab<T>& t, T E, T lx) {
+    const int n = fast_find(t, E, lx);
+    if (n == 1) {
+        T M = interp<T>(1, t.E[0], t.E[1], t.L[0], t.L[1], E);
+        return M < t.L[0] ? t.L[0] : M;
+    }
+    const T L1 = t.L[n - 2];
+    if (L1 >= T(1.0e16)) return L1;
+    const T L2 = t.L[n - 1], E1 = t.E[n - 2], E2 = t.E[n - 1];
+    if (m_abs(E2 - E1) < T(1.0e-6)) return L1 > L2 ? L1 : L2;
+    if (E == E1) return L1;
+    const T l1 = t.lE[n - 2];
+    return m_exp(t.lL[n - 2] + (t.lL[n - 1] - t.lL[n - 2]) / (t.lE[n - 1] - l1) * (lx - l1));
 }
 
 }  // namespace tk

@@ -29,9 +29,22 @@ struct BuildMat {
     const double* dos_Eff_m;
 };
 
+// A mean-free-path table prepared for the hot loop: logarithms of both
+// columns (one exp per log-log interpolation) and a bucket index over log(E)
+// whose entry never exceeds the bisection result, so a short forward walk
+// returns exactly the index of Find_in_monotonous_1D_array.
+template <class T>
+struct FastTab {
+    const T* E; const T* L; const T* lE; const T* lL;
+    const uint16_t* hint;
+    T lo, inv;
+    int n, nb;
+};
+
 // Device copies of a table set, one per precision.
 template <class T>
 struct DevTabs {
+    FastTab<T> fIMFP, fEMFP, fHIMFP, fHEMFP;   // electron / hole total inelastic and elastic
     // electron grid shared by the per-shell IMFPs and the cumulative rows
     const T* elE; int nE;
     const T* elL;          // [nsh][nE] per-shell IMFP

@@ -8,19 +8,21 @@
 //     which makes each history independent of the processing order;
 //   * the SHI track of an iteration is one thread (k_shi, FP64), emitting
 //     the primary electron-hole pairs into SoA queues;
-//   * k_step runs up to K events per live particle per launch, appending
-//     secondaries and survivors to the next queues with warp-aggregated
-//     atomics (one atomic per warp per append site);
+//   * a wavefront step is two kernels: k_hot runs up to K elastic collisions
+//     per electron / mobile valence hole (a small, icache-friendly body) and
+//     diverts a particle whose next event ionises to a side queue; k_rare
+//     runs those ionisations, deep-hole decays and photon absorptions.  New
+//     and surviving particles are appended to the next generation's queues
+//     (electrons, mobile valence holes, deep holes, photons) with
+//     warp-aggregated atomics (one atomic per warp per append site);
 //   * each free-flight segment [t0, tn) is tallied once, when it starts, into
 //     int64 difference arrays over the time grid (run-length over the radial
 //     bin), which makes the tallies bit-exact and order-independent.
 // The event bodies follow, draw for draw, SHI_Monte_Carlo (MC:2153-2249),
 // Electron_Monte_Carlo (MC:2253-2474), Hole_Monte_Carlo (MC:2517-2869) and
 // Photon_Monte_Carlo (MC:2873-2965).
-#include <cooperative_groups.h>
 #include "mc.cuh"
 
-namespace cg = cooperative_groups;
 
 namespace tk {
 
@@ -32,13 +34,20 @@ struct P {  // one particle in registers
     int sh;
 };
 
-// warp-aggregated append; returns -1 (and raises the overflow flag) when full
+// warp-aggregated append; returns -1 (and raises the overflow flag) when full.
+// The lanes that arrive together may append to different queues (a hole goes
+// to the valence or the deep queue by its shell), so lanes are grouped by the
+// counter they bump and each group takes one atomic.  Blocks are 1-D.
 __device__ __forceinline__ int64_t agg_append(int* ctr, int64_t cap, int* overflow) {
-    cg::coalesced_group g = cg::coalesced_threads();
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, (unsigned long long)(uintptr_t)ctr);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    const int rank = __popc(peers & ((1u << lane) - 1u));
     int base = 0;
-    if (g.thread_rank() == 0) base = atomicAdd(ctr, (int)g.size());
-    base = g.shfl(base, 0);
-    int64_t idx = (int64_t)base + g.thread_rank();
+    if (lane == leader) base = atomicAdd(ctr, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    int64_t idx = (int64_t)base + rank;
     if (idx >= cap) { atomicExch(overflow, 1); return -1; }
     return idx;
 }
@@ -187,6 +196,14 @@ struct LatAcc {
     }
 };
 
+// the MFPs of the energy a particle leaves an event with are the MFPs its
+// next event starts from; a thread keeps them across its events
+template <class T>
+struct MfpCache {
+    T E = T(-1), I = T(0), Em = T(0);
+    __device__ __forceinline__ bool hit(T e) const { return e == E; }
+};
+
 // ---- samplers ----------------------------------------------------------------------
 
 // Which_shell (MC:1786-1832) over per-shell tables sharing one grid
@@ -254,9 +271,11 @@ __device__ T electron_receives(const McConst<T>& C, const DevTabs<T>& tb, T dE, 
     return out;
 }
 
-// Hole_parameters + Assign_holes_mass (MC:724-792); p.sh, p.t0 set by the caller
+// Hole_parameters + Assign_holes_mass (MC:724-792); p.sh, p.t0 set by the caller.
+// A cache, when given, receives the MFPs at the new kinetic energy.
 template <class T, class S>
-__device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>& h, T Eh, S& s) {
+__device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>& h, T Eh, S& s,
+                                MfpCache<T>* cache = nullptr) {
     if (h.sh == C.vb) {
         T Etemp = h.Ek;
         h.Ek = Eh - C.Egap;
@@ -264,8 +283,14 @@ __device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>&
         if (C.hole_mass > T(0)) h.M = C.hole_mass;
         else h.M = tb.dosM[find_monoton(tb.dosE, tb.nD, h.Ek) - 1];
         if (h.M < T(1.0e3)) {
-            T HI = nfp2(Tab<T>{tb.hE, tb.hIMFP, tb.nH}, h.Ek);
-            T HE = (Etemp == Eh - C.Egap) ? T(1.0e30) : nfp2(Tab<T>{tb.hElastE, tb.hElastL, tb.nHel}, h.Ek);
+            const T lx = m_log(h.Ek);
+            const T HI = nfp2_fast(tb.fHIMFP, h.Ek, lx);
+            T HE;
+            if (Etemp == Eh - C.Egap) HE = T(1.0e30);   // the reference skips elastic scattering here (MC:746)
+            else {
+                HE = nfp2_fast(tb.fHEMFP, h.Ek, lx);
+                if (cache) { cache->E = h.Ek; cache->I = HI; cache->Em = HE; }
+            }
             T RN = s.next();
             T Mt = -m_log(RN) / (T(1) / HI + T(1) / HE);
             h.tn = tn_of(h.t0, Mt, v_hole(h.Ek, h.M));
@@ -301,13 +326,32 @@ __device__ __forceinline__ void new_angles(T phi0, T theta0, T theta, T psi, T& 
     if (phi1 < T(0)) phi1 = phi1 + m_ceil(m_abs(phi1) / twoPi) * twoPi;
 }
 
+// total inelastic and elastic MFPs of an electron at E (both tables share log E)
+template <class T>
+__device__ __forceinline__ void el_mfps(const DevTabs<T>& tb, T E, T& I, T& Em) {
+    const T lx = m_log(E);
+    I = nfp2_fast(tb.fIMFP, E, lx);
+    Em = nfp2_fast(tb.fEMFP, E, lx);
+}
+template <class T>
+__device__ __forceinline__ void h_mfps(const DevTabs<T>& tb, T E, T& I, T& Em) {
+    const T lx = m_log(E);
+    I = nfp2_fast(tb.fHIMFP, E, lx);
+    Em = nfp2_fast(tb.fHEMFP, E, lx);
+}
+
 template <class T, class S>
-__device__ __forceinline__ void electron_flight(const DevTabs<T>& tb, P<T>& p, S& s) {
-    T I = nfp2(Tab<T>{tb.elE, tb.elIMFP, tb.nE}, p.E);
-    T Em = nfp2(Tab<T>{tb.elastE, tb.elastL, tb.nEl}, p.E);
-    T RN = s.next();
+__device__ __forceinline__ void flight_with(P<T>& p, T I, T Em, S& s) {
+    const T RN = s.next();
     p.L = -m_log(RN) / (T(1) / I + T(1) / Em);
     p.tn = tn_of(p.t0, p.L, v_el(p.E));
+}
+
+template <class T, class S>
+__device__ __forceinline__ void electron_flight(const DevTabs<T>& tb, P<T>& p, S& s) {
+    T I, Em;
+    el_mfps(tb, p.E, I, Em);
+    flight_with(p, I, Em, s);
 }
 
 // Mott energy transfer, Pers-weighted average over species (MC:2394-2407, CS:3517-3613).
@@ -435,16 +479,23 @@ __device__ void make_hole(const McConst<T>& C, const DevTabs<T>& tb, P<T>& hh, T
 }
 
 template <class T>
-struct Out {  // where a thread puts new particles
-    PQ<T> e, h, p;
+struct Out {  // where a thread puts particles that still have events before Tim
+    PQ<T> q[4];     // Q_E, Q_HVB, Q_HDEEP, Q_P
     Ctrs* ctr;
 };
 
 template <class T>
-__device__ __forceinline__ void push(const McConst<T>& C, const Tal& tal, const Out<T>& o, int kind, const P<T>& p) {
-    const PQ<T>& q = kind == 0 ? o.e : kind == 1 ? o.h : o.p;
-    int64_t i = agg_append(&o.ctr->n_out[kind], q.cap, &o.ctr->overflow);
+__device__ __forceinline__ void append(const PQ<T>& q, int* n, int* overflow, const P<T>& p) {
+    int64_t i = agg_append(n, q.cap, overflow);
     if (i >= 0) store(q, i, p);
+}
+
+// kind 0 electron, 1 hole, 2 photon; holes go to the mobile-valence or the deep queue
+template <class T>
+__device__ __forceinline__ void push(const McConst<T>& C, const Tal& tal, const Out<T>& o, int kind, const P<T>& p) {
+    if (!(p.tn < C.Tim)) return;           // no event left inside the run
+    const int qi = kind == 0 ? Q_E : kind == 2 ? Q_P : (p.sh == C.vb ? Q_HVB : Q_HDEEP);
+    append(o.q[qi], &o.ctr->n_out[qi], &o.ctr->overflow, p);
 }
 
 // ---- SHI track ----------------------------------------------------------------------
@@ -603,8 +654,8 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
 // draws continue in the collision's stream after the ion's three.
 template <class T>
 __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp, DevTabs<T> tb,
-                                               const ShiEv* __restrict__ evs, int64_t n_ev, PQ<T> qe, PQ<T> qh,
-                                               Tal tal, Ctrs* ctr) {
+                                               const ShiEv* __restrict__ evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
+                                               PQ<T> qhdeep, Tal tal, Ctrs* ctr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_ev) return;
     const McConst<T>& C = *Cp;
@@ -615,7 +666,7 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
     unsigned err = 0;
     const int k = ev.k;
     const double E = ev.E, dE = ev.dE, MSHI = C.MSHI;
-    Out<T> o{qe, qh, qe, ctr};
+    Out<T> o{{qe, qhvb, qhdeep, qe}, ctr};
     P<T> el;
     el.pid = child_pid(pid, ev.ord, 0); el.ord = 0; el.sh = 0; el.Ek = T(0); el.M = T(0);
     const T dEc = electron_receives(C, tb, (T)dE, k, s, err);
@@ -642,21 +693,28 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
 }
 
 // ---- cascade events ------------------------------------------------------------------------
-template <class T>
-__device__ void electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
-                               P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev) {
-    const uint32_t ord = p.ord++;
+// One electron event.  FULL=false compiles only the elastic branch (the hot
+// kernel): an ionising draw returns false with the particle untouched, and the
+// event is redone from the same stream by the FULL version.
+template <class T, bool FULL>
+__device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
+                               P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc) {
+    const uint32_t ord = p.ord;
     EvStream<T> s(C.seed, p.pid, ord);
     const T Eel = p.E;
-    const T I = nfp2(Tab<T>{tb.elE, tb.elIMFP, tb.nE}, Eel);
-    const T Em = nfp2(Tab<T>{tb.elastE, tb.elastL, tb.nEl}, Eel);
+    T I, Em;
+    if (mc.hit(Eel)) { I = mc.I; Em = mc.Em; }
+    else el_mfps(tb, Eel, I, Em);
     const T RN = s.next();
+    const bool ionise = RN * (T(1) / I + T(1) / Em) < T(1) / I;
+    if constexpr (!FULL) { if (ionise) return false; }
+    p.ord = ord + 1;
     const T th0 = p.th, ph0 = p.ph, tev = p.tn;
     const T X = p.X + p.L * m_sin(th0) * m_sin(ph0);
     const T Y = p.Y + p.L * m_sin(th0) * m_cos(ph0);
     const T Z = p.Z + p.L * m_cos(th0);
     T dE, theta, phi;
-    if (RN * (T(1) / I + T(1) / Em) < T(1) / I) {  // impact ionisation
+    if (FULL && ionise) {  // impact ionisation
         const int k = which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next());
         const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
         dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err);
@@ -689,13 +747,16 @@ __device__ void electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     }
     p.E = Eel - dE;
     p.t0 = tev;
-    electron_flight(tb, p, s);
+    el_mfps(tb, p.E, mc.I, mc.Em);
+    mc.E = p.E;
+    flight_with(p, mc.I, mc.Em, s);
     T ph1, th1;
     new_angles(ph0, th0, theta, phi, ph1, th1);
     p.X = X; p.Y = Y; p.Z = Z; p.th = th1; p.ph = ph1;
     cut_e(C, p);
     if (p.E < T(-1.0e-9) || m_isnan(p.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
     emit_electron(C, tal, p);
+    return true;
 }
 
 // check_hole_parameters (MC:682-721); the downward search stops at the first DOS node
@@ -719,22 +780,28 @@ __device__ T check_hole(const DevTabs<T>& tb, T Eel, T& dE, P<T>* el) {
     return Eh;
 }
 
-template <class T>
-__device__ void hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& h,
-                           unsigned& err, LatAcc& lat, unsigned long long* nev) {
-    const uint32_t ord = h.ord++;
+// One hole event; FULL=false compiles only valence-hole elastic scattering.
+template <class T, bool FULL>
+__device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& h,
+                           unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc) {
+    const uint32_t ord = h.ord;
     EvStream<T> s(C.seed, h.pid, ord);
+    if (!FULL && h.sh != C.vb) return false;
     if (h.sh == C.vb) {
         const T Eel = h.Ek;
-        const T HI = nfp2(Tab<T>{tb.hE, tb.hIMFP, tb.nH}, Eel);
-        const T HE = nfp2(Tab<T>{tb.hElastE, tb.hElastL, tb.nHel}, Eel);
+        T HI, HE;
+        if (mc.hit(Eel)) { HI = mc.I; HE = mc.Em; }
+        else h_mfps(tb, Eel, HI, HE);
         const T RN = s.next();
+        const bool ionise = RN * (T(1) / HI + T(1) / HE) < T(1) / HI && HI < T(1e15);
+        if constexpr (!FULL) { if (ionise) return false; }
+        h.ord = ord + 1;
         const T th0 = h.th, ph0 = h.ph, tev = h.tn, hm = h.M;
         const T X = h.X + h.L * m_sin(th0) * m_sin(ph0);
         const T Y = h.Y + h.L * m_sin(th0) * m_cos(ph0);
         const T Z = h.Z + h.L * m_cos(th0);
         T dE, th1, ph1, Eh;
-        if (RN * (T(1) / HI + T(1) / HE) < T(1) / HI && HI < T(1e15)) {
+        if (FULL && ionise) {
             const int k = which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
             const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
             dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err);
@@ -781,12 +848,15 @@ __device__ void hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         T hp2, ht2;
         new_angles(ph0, th0, th1, ph1, hp2, ht2);
         h.t0 = tev; h.X = X; h.Y = Y; h.Z = Z; h.th = ht2; h.ph = hp2;
-        hole_parameters(C, tb, h, Eh + C.Egap, s);
+        mc.E = T(-1);
+        hole_parameters(C, tb, h, Eh + C.Egap, s, &mc);
         cut_h(C, h);
         if (h.Ek < T(-1.0e-9) || m_isnan(h.Ek)) err |= TREKIS_ERR_NEG_ENERGY_H;
         emit_hole(C, tal, h);
-        return;
+        return true;
     }
+    if constexpr (!FULL) return false;
+    h.ord = ord + 1;
     // deep hole: Auger vs radiative decay (MC:2739-2868)
     const int KS = h.sh;
     const T IpK = C.Ip[KS];
@@ -883,6 +953,7 @@ __device__ void hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         emit_photon(C, tal, pp); push(C, tal, o, 2, pp);
         nev[5]++; nev[7] += 1;
     }
+    return true;
 }
 
 template <class T>
@@ -916,29 +987,63 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
     nev[6]++; nev[7] += 2;
 }
 
-// One wavefront step: each thread runs up to K events of one particle.
+// Hot kernel of a wavefront step: electrons and mobile valence holes run up to
+// K elastic collisions each.  A particle whose next event ionises goes to a
+// side queue; survivors go to the next generation's queue.
 template <class T>
-__global__ void __launch_bounds__(256) k_step(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> ie, int ne,
-                                              PQ<T> ih, int nh, PQ<T> ip, int np, Out<T> o, Tal tal, int K,
-                                              int blocks_e, int blocks_h) {
+__global__ void __launch_bounds__(256) k_hot(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> ie, int ne,
+                                             PQ<T> ih, int nh, Out<T> o, PQ<T> e_inel, PQ<T> h_inel, Tal tal, int K,
+                                             int blocks_e) {
     const McConst<T>& C = *Cp;
-    int kind, idx;
-    if ((int)blockIdx.x < blocks_e) { kind = 0; idx = blockIdx.x * blockDim.x + threadIdx.x; if (idx >= ne) return; }
-    else if ((int)blockIdx.x < blocks_e + blocks_h) { kind = 1; idx = (blockIdx.x - blocks_e) * blockDim.x + threadIdx.x; if (idx >= nh) return; }
-    else { kind = 2; idx = (blockIdx.x - blocks_e - blocks_h) * blockDim.x + threadIdx.x; if (idx >= np) return; }
-    const PQ<T>& in = kind == 0 ? ie : kind == 1 ? ih : ip;
+    const bool is_e = (int)blockIdx.x < blocks_e;
+    const int idx = (is_e ? blockIdx.x : blockIdx.x - blocks_e) * blockDim.x + threadIdx.x;
+    if (idx >= (is_e ? ne : nh)) return;
     P<T> p;
-    load(in, idx, p);
+    load(is_e ? ie : ih, idx, p);
     unsigned err = 0;
     unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     LatAcc lat;
+    MfpCache<T> mc;
+    bool diverted = false;
     for (int e = 0; e < K && p.tn < C.Tim; ++e) {
-        if (kind == 0) electron_event(C, tb, tal, o, p, err, lat, nev);
-        else if (kind == 1) hole_event(C, tb, tal, o, p, err, lat, nev);
-        else photon_event(C, tb, tal, o, p, err, nev);
+        const bool done = is_e ? electron_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc)
+                               : hole_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc);
+        if (!done) { diverted = true; break; }
     }
     lat.flush(tal);
-    if (p.tn < C.Tim) push(C, tal, o, kind, p);
+    if (diverted) {
+        if (is_e) append(e_inel, &o.ctr->n_out[Q_EINEL], &o.ctr->overflow, p);
+        else append(h_inel, &o.ctr->n_out[Q_HINEL], &o.ctr->overflow, p);
+    } else push(C, tal, o, is_e ? 0 : 1, p);
+    if (nev[2]) atomicAdd(&o.ctr->ev[2], nev[2]);
+    if (nev[3]) atomicAdd(&o.ctr->ev[3], nev[3]);
+    if (err) atomicOr(&o.ctr->err_bits, err);
+}
+
+// Rare kernel of a wavefront step (grid-stride; counts read on the device):
+// one full event for each particle of the ionisation side queues, each deep
+// hole (Auger or radiative decay) and each photon (absorption).
+template <class T>
+__global__ void __launch_bounds__(128) k_rare(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> e_inel,
+                                              PQ<T> h_inel, PQ<T> hdeep, int n_deep, PQ<T> ph, int n_ph, Out<T> o,
+                                              Tal tal) {
+    const McConst<T>& C = *Cp;
+    const int n_e = o.ctr->n_out[Q_EINEL], n_h = o.ctr->n_out[Q_HINEL];
+    const int total = n_e + n_h + n_deep + n_ph;
+    unsigned err = 0;
+    unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        P<T> p;
+        LatAcc lat;
+        MfpCache<T> mc;
+        int kind;
+        if (g < n_e) { load(e_inel, g, p); electron_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 0; }
+        else if (g < n_e + n_h) { load(h_inel, g - n_e, p); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
+        else if (g < n_e + n_h + n_deep) { load(hdeep, g - n_e - n_h, p); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
+        else { load(ph, g - n_e - n_h - n_deep, p); photon_event(C, tb, tal, o, p, err, nev); kind = 2; }
+        lat.flush(tal);
+        push(C, tal, o, kind, p);
+    }
     for (int q = 1; q < 8; ++q)
         if (nev[q]) atomicAdd(&o.ctr->ev[q], nev[q]);
     if (err) atomicOr(&o.ctr->err_bits, err);
@@ -950,33 +1055,35 @@ void launch_shi(const McConst<T>* C, const DevShi<T>& sh, void* evs, int64_t cap
     k_shi_track<T><<<(nit + 63) / 64, 64, 0, s>>>(C, sh, (ShiEv*)evs, cap_ev, ctr, nit);
 }
 template <class T>
-void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qh,
-                  Tal tal, Ctrs* ctr, cudaStream_t s) {
+void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
+                  PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s) {
     if (n_ev <= 0) return;
-    k_pairs<T><<<(unsigned)((n_ev + 127) / 128), 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qh, tal, ctr);
+    k_pairs<T><<<(unsigned)((n_ev + 127) / 128), 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qhvb, qhdeep, tal, ctr);
 }
 size_t shi_event_bytes() { return sizeof(ShiEv); }
 
 template <class T>
-void launch_step(const McConst<T>* C, const DevTabs<T>& tb, PQ<T> ie, int ne, PQ<T> ih, int nh, PQ<T> ip, int np,
-                 PQ<T> oe, PQ<T> oh, PQ<T> op, Tal tal, Ctrs* ctr, int K, int bs, cudaStream_t s) {
-    int be = (ne + bs - 1) / bs, bh = (nh + bs - 1) / bs, bp = (np + bs - 1) / bs;
-    if (be + bh + bp == 0) return;
-    Out<T> o{oe, oh, op, ctr};
-    k_step<T><<<be + bh + bp, bs, 0, s>>>(C, tb, ie, ne, ih, nh, ip, np, o, tal, K, be, bh);
+void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
+                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s) {
+    Out<T> o{{out.q[0], out.q[1], out.q[2], out.q[3]}, ctr};
+    const int be = (n_in[Q_E] + bs - 1) / bs, bh = (n_in[Q_HVB] + bs - 1) / bs;
+    if (be + bh > 0)
+        k_hot<T><<<be + bh, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], in.q[Q_HVB], n_in[Q_HVB], o, e_inel, h_inel,
+                                        tal, K, be);
+    k_rare<T><<<rare_blocks, 128, 0, s>>>(C, tb, e_inel, h_inel, in.q[Q_HDEEP], n_in[Q_HDEEP], in.q[Q_P],
+                                          n_in[Q_P], o, tal);
 }
 
 template void launch_shi<float>(const McConst<float>*, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t);
 template void launch_shi<double>(const McConst<double>*, const DevShi<double>&, void*, int64_t, Ctrs*, int, cudaStream_t);
 template void launch_pairs<float>(const McConst<float>*, const DevTabs<float>&, const void*, int64_t, PQ<float>,
-                                  PQ<float>, Tal, Ctrs*, cudaStream_t);
+                                  PQ<float>, PQ<float>, Tal, Ctrs*, cudaStream_t);
 template void launch_pairs<double>(const McConst<double>*, const DevTabs<double>&, const void*, int64_t, PQ<double>,
-                                   PQ<double>, Tal, Ctrs*, cudaStream_t);
-template void launch_step<float>(const McConst<float>*, const DevTabs<float>&, PQ<float>, int, PQ<float>, int,
-                                 PQ<float>, int, PQ<float>, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, cudaStream_t);
-template void launch_step<double>(const McConst<double>*, const DevTabs<double>&, PQ<double>, int, PQ<double>, int,
-                                  PQ<double>, int, PQ<double>, PQ<double>, PQ<double>, Tal, Ctrs*, int, int,
-                                  cudaStream_t);
+                                   PQ<double>, PQ<double>, Tal, Ctrs*, cudaStream_t);
+template void launch_step<float>(const McConst<float>*, const DevTabs<float>&, const QSet<float>&, const int*,
+                                 const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t);
+template void launch_step<double>(const McConst<double>*, const DevTabs<double>&, const QSet<double>&, const int*,
+                                  const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t);
 
 // ---- finalize: difference arrays -> FP64 tallies -----------------------------------------
 // One thread per (slice, bin): prefix over time rows, in place (exact int64).

@@ -50,8 +50,12 @@ constexpr double kEScale = 16777216.0;      // 2^24 per eV for particle energies
 constexpr double kLatScale = 1099511627776.0;  // 2^40 per eV for lattice energy
 
 // Counters written by the kernels.
+// queue slots: electrons, mobile valence holes, deep holes, photons, and the
+// two side queues of particles whose next event is an ionisation
+enum { Q_E = 0, Q_HVB = 1, Q_HDEEP = 2, Q_P = 3, Q_EINEL = 4, Q_HINEL = 5, NQ = 6 };
+
 struct Ctrs {
-    int n_out[3];                 // appended electrons, holes, photons
+    int n_out[NQ];                // appended particles per queue
     int overflow;
     unsigned int err_bits;
     int first_bad_it;
@@ -62,12 +66,17 @@ template <class T>
 void launch_shi(const McConst<T>* C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
                 cudaStream_t s);
 template <class T>
-void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qh,
-                  Tal tal, Ctrs* ctr, cudaStream_t s);
+void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
+                  PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s);
 size_t shi_event_bytes();
 template <class T>
-void launch_step(const McConst<T>* C, const DevTabs<T>& tb, PQ<T> ie, int ne, PQ<T> ih, int nh, PQ<T> ip, int np,
-                 PQ<T> oe, PQ<T> oh, PQ<T> op, Tal tal, Ctrs* ctr, int K, int bs, cudaStream_t s);
+struct QSet {   // the four particle queues of one generation
+    PQ<T> q[4];
+};
+
+template <class T>
+void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
+                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s);
 void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
                const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s);
 void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,
