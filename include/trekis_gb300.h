@@ -273,6 +273,48 @@ int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
                              const trekis_ion* ion, const trekis_run_cfg* cfg,
                              trekis_tallies* dev_out, trekis_status* st);
 
+/* Fixed-footprint variant of trekis_mc_run_device.  No counterpart in the
+ * reference (its Fortran loop allocates and grows its particle arrays freely).
+ *
+ * Who needs it: a caller that must not allocate device memory while the track
+ * loop runs -- a host code that has already handed the GPU's free memory to
+ * its own pool allocator, a job that runs under a fixed device-memory budget
+ * shared with other solvers, or a service that cannot afford an out-of-memory
+ * failure half-way through a request.  trekis_mc_run_device keeps a workspace
+ * per table handle that it (re)allocates with cudaMalloc whenever the queue
+ * capacity or the tally shape changes; this entry point allocates nothing.
+ * It carves its particle queues, int64 tallies, counters and staging from
+ * TREKIS_NOALLOC_SCRATCH_BYTES of static device memory that the CUDA runtime
+ * reserves once, when it loads this part of the library, and it creates no
+ * stream and no event.  The tables themselves come from trekis_tables_build,
+ * which does allocate, before the run.
+ *
+ * Same arguments and the same results as trekis_mc_run_device (tallies are
+ * added into the caller's device arrays), plus `stream`: the caller's
+ * cudaStream_t (NULL: the default stream), on which every copy and kernel
+ * of the call is issued; the call returns after that stream has drained.
+ * Differences:
+ *   - the queue capacity is the largest that fits the scratch after the
+ *     tallies of this (Nt, N_R, shells) shape; cfg->queue_capacity, when set,
+ *     must not exceed it.  A tally shape that leaves too little room, or a
+ *     requested capacity beyond it, returns TREKIS_EINVAL with the reason in
+ *     trekis_last_error(); a single iteration that overflows the queues
+ *     returns TREKIS_EOVERFLOW, as the allocating entry point does.
+ *   - status->device_ms and status->step_ms stay 0 (no timing events).
+ *   - the scratch is zeroed by each call where the kernels need zeros
+ *     (tallies, counters, staging), so nothing has to be cleared between
+ *     calls.
+ * The first call on each device looks up the scratch address with that
+ * device current, which may load this module; make that first call before
+ * any stream capture begins on the device.  There is one scratch per device
+ * and process: calls that overlap in time on the same device (from several
+ * host threads) share it and race, so such callers must serialise them. */
+#define TREKIS_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int32_t trekis_mc_run_device_noalloc(const trekis_tables* t, const trekis_material* mat,
+                                     const trekis_ion* ion, const trekis_run_cfg* cfg,
+                                     trekis_tallies* dev_out, trekis_status* st,
+                                     void* stream);
+
 /* Human-readable text of the last error on this thread. */
 const char* trekis_last_error(void);
 

@@ -1,0 +1,91 @@
+"""trekis_mc_run_device_noalloc (the entry point that allocates no device
+memory; its scratch is a fixed static device array) against the allocating
+trekis_mc_run_device on the same tables, seed and tally shape.
+
+Two no-alloc calls in a row must each reproduce the allocating call: the
+second one checks that every call clears what its kernels accumulate into.
+The tallies are int64 fixed point per batch and the batches are summed in
+FP64, so a different batch partition (the no-alloc queue capacity differs)
+only reorders those sums: rtol 1e-12 of each value plus 1e-12 of the array
+maximum.  Event counts are exact.  The file is collected last so the test
+runs both alone and after every other GPU test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from trekis import abi, api, configs
+
+RTOL = 1e-12
+
+
+def _device_tallies(torch, w):
+    tal = api.new_tallies(w)
+    dev = {k: torch.zeros(v.size, dtype=torch.float64, device="cuda") for k, v in tal.a.items()}
+    ptr = lambda x: C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double))
+    ct = abi.Tallies(Nt=tal.Nt, N_R=tal.NR, Nat=tal.Nat, Nshl=tal.Nshl, **{k: ptr(v) for k, v in dev.items()})
+    return dev, ct
+
+
+def _run(lib, t, w, opt, noalloc):
+    import torch
+    dev, ct = _device_tallies(torch, w)
+    cfg, _R = api.run_cfg(w, opt)
+    st = abi.Status.fresh()
+    if noalloc:
+        rc = lib.trekis_mc_run_device_noalloc(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(ct),
+                                              C.byref(st), None)
+    else:
+        rc = lib.trekis_mc_run_device(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(ct), C.byref(st))
+    abi.check(rc, lib)
+    torch.cuda.synchronize()
+    return {k: v.cpu().numpy() for k, v in dev.items()}, st
+
+
+def _close(a, b, what):
+    for k in b:
+        x, y = a[k], b[k]
+        tol = RTOL * np.abs(y) + RTOL * (np.max(np.abs(y)) + 1e-300)
+        bad = np.abs(x - y) > tol
+        assert not np.any(bad), f"{what} {k}: {np.sum(bad)} cells differ, max {np.max(np.abs(x - y)):.3e}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_noalloc_matches_allocating_entry_point(gpu_lib, precision):
+    pytest.importorskip("torch")
+    w = configs.small(configs.cfg1, NMC=6, Tim=30.0)   # mobile valence holes, radiative decay, photons
+    for atom in w.material.atoms:
+        for sh in atom.shells:
+            if sh.designator < 63:
+                sh.Radiat = sh.Auger * 2.0
+    t = api.Tables(w, lib=gpu_lib)
+    opt = api.RunOptions(precision=precision, seed=23)
+    ref, sr = _run(gpu_lib, t, w, opt, noalloc=False)
+    assert sr.n_events > 0
+    for call in range(2):
+        got, sg = _run(gpu_lib, t, w, opt, noalloc=True)
+        assert sg.code == 0
+        for f in ("n_events", "n_shi", "n_el_inelastic", "n_el_elastic", "n_hole_events", "n_auger",
+                  "n_radiative", "n_photon_abs", "n_particles"):
+            assert getattr(sg, f) == getattr(sr, f), (call, f)
+        assert sg.error_bits == sr.error_bits
+        _close(got, ref, f"call {call}")
+    t.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_capacity_beyond_scratch(gpu_lib):
+    pytest.importorskip("torch")
+    import torch
+    w = configs.small(configs.cfg0, NMC=1)
+    t = api.Tables(w, lib=gpu_lib)
+    dev, ct = _device_tallies(torch, w)
+    cfg, _R = api.run_cfg(w, api.RunOptions(queue_capacity=abi.NOALLOC_SCRATCH_BYTES))
+    st = abi.Status.fresh()
+    rc = gpu_lib.trekis_mc_run_device_noalloc(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(ct),
+                                              C.byref(st), None)
+    assert rc == -1 and b"exceeds" in gpu_lib.trekis_last_error()
+    assert float(sum(v.abs().sum().item() for v in dev.values())) == 0.0
+    t.close()

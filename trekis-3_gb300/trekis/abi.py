@@ -16,6 +16,8 @@ MAX_PH_OSC = 8
 TAB_EL_INEL, TAB_EL_ELAST, TAB_H_INEL, TAB_H_ELAST, TAB_PHOT, TAB_SHI, TAB_SHI_DSDE = range(7)
 ROW_EL_INEL, ROW_H_INEL, ROW_EL_ELAST = range(3)
 
+NOALLOC_SCRATCH_BYTES = 64 << 20   # TREKIS_NOALLOC_SCRATCH_BYTES
+
 ERRORS = {
     0: "ok", -1: "invalid argument", -2: "no usable sm_103a device", -3: "CUDA call failed",
     -4: "device allocation failed", -5: "particle queue overflow", -6: "bounded device wait ran out",
@@ -130,6 +132,8 @@ SIGNATURES = {
                                   C.POINTER(Tallies), C.POINTER(Status)]),
     "trekis_mc_run_device": (C.c_int32, [C.c_void_p, C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
                                          C.POINTER(Tallies), C.POINTER(Status)]),
+    "trekis_mc_run_device_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
+                                                 C.POINTER(Tallies), C.POINTER(Status), C.c_void_p]),
     "trekis_last_error": (C.c_char_p, []),
 }
 
