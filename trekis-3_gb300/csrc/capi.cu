@@ -303,6 +303,7 @@ struct Workspace {
     Ctrs* ctr = nullptr;
     McConst<T>* dC = nullptr;
     T *tg = nullptr, *Rg = nullptr;
+    int *th = nullptr, *rh = nullptr;   // grid bucket hints
     double* V = nullptr;
     int* hmap = nullptr;
     double *hstage = nullptr, *hn = nullptr, *hE = nullptr, *hK = nullptr, *htn = nullptr, *htE = nullptr;
@@ -358,6 +359,9 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     w->dC = (McConst<T>*)b.alloc(sizeof(McConst<T>));
     w->tg = (T*)b.alloc(sizeof(T) * Nt);
     w->Rg = (T*)b.alloc(sizeof(T) * NR);
+    w->th = (int*)b.alloc(sizeof(int) * (2 * (size_t)Nt + 2));
+    w->rh = (int*)b.alloc(sizeof(int) * kRgHintMax);
+    if (!w->th || !w->rh) return nullptr;
     w->V = (double*)b.alloc(8 * NR);
     w->hmap = (int*)b.alloc(sizeof(int) * nsh);
     w->hstage_n = (size_t)Nt * NR * nsh * 3 + (size_t)Nt * nsh * 2;
@@ -432,6 +436,9 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     CK(cudaMemcpyAsync(ws->Rg, RgT.data(), sizeof(T) * cfg.N_R, cudaMemcpyHostToDevice, strm));
     CK(cudaMemcpyAsync(ws->V, V.data(), 8 * cfg.N_R, cudaMemcpyHostToDevice, strm));
     C.tg = ws->tg; C.Rg = ws->Rg;
+    set_grid_hint_sizes<T>(C, tgT[0], tgT[Nt - 1], RgT[0], RgT[cfg.N_R - 1]);
+    C.tg_hint = ws->th; C.rg_hint = C.rg_nb ? ws->rh : nullptr;
+    launch_grid_hints<T>(C, ws->th, ws->rh, strm);
     const int NR = cfg.N_R, nsh = t->nsh;
     Tal tal = ws->tal;
     Ctrs* dctr = ws->ctr;
@@ -445,7 +452,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 64);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
     CK(cudaEventRecord(ws->e0, strm));
-    uint64_t steps = 0, launches = 0, ev_tot[8] = {0}, peak_all = 0;
+    uint64_t steps = 0, launches = 1, ev_tot[8] = {0}, peak_all = 0;   // the grid hints
     uint64_t h2d = sizeof(T) * (Nt + cfg.N_R) + 8 * cfg.N_R, d2h = 0;
     double step_ms = 0.0;
     Ctrs hc;
@@ -468,7 +475,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         d2h += sizeof hc;
         CK(cudaStreamSynchronize(strm));
         if (!hc.overflow) {
-            launch_pairs<T>(dC, tb, ws->evs, (int64_t)hc.ev[0], ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], tal, dctr, strm);
+            launch_pairs<T>(dC, tb, ws->evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)ws->cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], tal, dctr, strm);
             ++launches;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
@@ -489,7 +496,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             CK(cudaEventRecord(ws->s0, strm));
             launch_step<T>(dC, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm);
             CK(cudaEventRecord(ws->s1, strm));
-            blaunch += 2; ++bsteps;
+            blaunch += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0); ++bsteps;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
             d2h += sizeof hc;

@@ -86,11 +86,35 @@ template <class T> __device__ __forceinline__ T pi_() { return T(kPi); }
 // ---- tallies ------------------------------------------------------------------------
 __device__ __forceinline__ void add64(unsigned long long* p, long long v) { atomicAdd(p, (unsigned long long)v); }
 
-template <class T>
-__device__ __forceinline__ long long fixE(T E) { return __double2ll_rn((double)E * kEScale); }
+// Fixed point of a particle energy.  Scaling by 2^24 is exact in either
+// precision, so the FP32 form rounds the same real number as the FP64 one.
+__device__ __forceinline__ long long fixE(float E) { return __float2ll_rn(E * 16777216.0f); }
+__device__ __forceinline__ long long fixE(double E) { return __double2ll_rn(E * kEScale); }
+__device__ __forceinline__ long long fixLat(float E) { return __float2ll_rn(E * 1099511627776.0f); }
+__device__ __forceinline__ long long fixLat(double E) { return __double2ll_rn(E * kLatScale); }
 
+// find_monoton over the radius grid: bucket hint by the bits of R, then a
+// forward walk (at most a step or two) to the bisection's index
 template <class T>
-__device__ __forceinline__ int rbin(const McConst<T>& C, T R) { return find_monoton(C.Rg, C.NR, R); }
+__device__ __forceinline__ int rbin(const McConst<T>& C, T R) {
+    if (!(R >= C.rg_lo)) return (R < C.rg_lo) ? 1 : find_monoton(C.Rg, C.NR, R);   // below, or NaN
+    if (R >= C.rg_hi) return C.NR;
+    if (!C.rg_hint) return find_monoton(C.Rg, C.NR, R);
+    int j = C.rg_hint[(int)radius_key(R) - C.rg_key0];
+    while (j < C.NR && C.Rg[j - 1] <= R) ++j;
+    return j;
+}
+// find_monoton over the tallied times, by a uniform bucket hint
+template <class T>
+__device__ __forceinline__ int tbin(const McConst<T>& C, T t) {
+    if (!(t >= C.tg_lo)) return (t < C.tg_lo) ? 1 : find_monoton(C.tg, C.Nt, t);
+    if (t >= C.tg_hi) return C.Nt;
+    int b = (int)(t * C.tg_inv) - 1;   // one bucket of margin for the rounding of t * inv
+    b = b < 0 ? 0 : (b >= C.tg_nb ? C.tg_nb - 1 : b);
+    int j = C.tg_hint[b];
+    while (j < C.Nt && C.tg[j - 1] <= t) ++j;
+    return j;
+}
 
 // one run of equal radial bin over rows [r0, r1] (1-based)
 template <class T>
@@ -123,10 +147,10 @@ template <class T>
 __device__ void emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn, T X, T Y,
                          T th, T ph, T V /* m/s, 0: static */) {
     const int Nt = C.Nt;
-    if (!(t0 < C.tg[Nt - 1])) return;
-    const int ia = find_monoton(C.tg, Nt, t0);
+    if (!(t0 < C.tg_hi)) return;
+    const int ia = tbin(C, t0);
     const T tend = tn < C.Tim ? tn : C.Tim;
-    const int ib = (tend >= C.tg[Nt - 1]) ? Nt : find_monoton(C.tg, Nt, tend) - 1;
+    const int ib = (tend >= C.tg_hi) ? Nt : tbin(C, tend) - 1;
     if (ib < ia) return;
     const long long qE = fixE(E), qK = fixE(Ek);
     if (V == T(0)) {
@@ -186,9 +210,10 @@ __device__ __forceinline__ void emit_photon(const McConst<T>& C, const Tal& tal,
 struct LatAcc {
     int cell = -1;
     long long sum = 0;
-    __device__ __forceinline__ void add(const Tal& tal, int c, double v) {
+    template <class T>
+    __device__ __forceinline__ void add(const Tal& tal, int c, T v) {
         if (c != cell) { flush(tal); cell = c; }
-        sum += __double2ll_rn(v * kLatScale);
+        sum += fixLat(v);
     }
     __device__ __forceinline__ void flush(const Tal& tal) {
         if (cell >= 0 && sum != 0) add64(tal.lat + cell, sum);
@@ -542,6 +567,12 @@ struct ShiEv {  // one SHI collision: the ion state after it and the transfer
 // The ion of each iteration, one thread each: Which_shell, SHI_energy_transfer,
 // next free path and the charge update (SHI_Monte_Carlo, MC:2153-2196).  The
 // energy, depth and time accumulate in FP64; the table arithmetic is in T.
+// In FP32 mode the velocity, flight time and Bohr charge are FP32 too (a
+// serial FP64 chain is slow on this part); FP64 mode keeps the reference's
+// expressions.  Record slots are reserved kSlotChunk at a time; slots a
+// thread leaves unused are marked it = -1 and skipped by the pair kernel.
+constexpr int kSlotChunk = 32;
+
 template <class T>
 __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__ Cp, DevShi<T> sh,
                                                   ShiEv* __restrict__ evs, int64_t cap_ev, Ctrs* ctr, int nit) {
@@ -551,6 +582,19 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
     unsigned err = 0;
     unsigned long long nev = 0;
     const uint64_t pid = shi_pid(C.it0 + it);
+    constexpr bool F32 = sizeof(T) == 4;
+    const double vfac = 2.0 * kE / (C.ion_mass_p * kMp);   // v^2 = vfac E
+    const T vfac_t = (T)vfac;
+    const T zfac = T(125.0 / kC) / sh.pow_zp;              // Bohr-velocity factor of Zeff (kind 0)
+    auto flight_time = [&](double E_, double L_) -> double {
+        if constexpr (F32) {
+            const T V = m_sqrt((T)E_ * vfac_t);
+            return (V > T(1.0e-10)) ? (double)((T)L_ / V * T(1e5)) : -1.0;
+        } else {
+            const double V = sqrt(2.0 * E_ * kE / (C.ion_mass_p * kMp));
+            return (V > 1.0e-10) ? L_ / V * 1e5 : -1.0;
+        }
+    };
     double E = C.ion_E0, t0 = 0.0, tn, Z = 0.0, L;
     {
         EvStream<T> s(C.seed, pid, 0xFFFFFFFFu);
@@ -558,10 +602,11 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
         const int nb = find_monoton(sh.sE, sh.nS, Et);
         L = (double)shi_path(sh, nb, Et, lx);
         L = -L * (double)m_log(s.next());
-        const double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
-        tn = (V > 1.0e-10) ? t0 + L / V * 1e5 : 1.0e25;
+        const double dt = flight_time(E, L);
+        tn = dt >= 0.0 ? t0 + dt : 1.0e25;
     }
     uint32_t ord = 0;
+    int64_t slot = 0, slot_end = 0;
     while (tn < (double)C.Tim) {
         if (ord >= (1u << 26)) { err |= TREKIS_ERR_NAN; break; }   // no SHI track has this many collisions
         EvStream<T> s(C.seed, pid, ord);
@@ -615,11 +660,14 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
         Lnew = -Lnew * (double)m_log(s.next());
         Z = Z + L;
         E -= dE; t0 = tn; L = Lnew;
-        const double V = sqrt(2.0 * E * kE / (C.ion_mass_p * kMp));
-        tn = (V > 1.0e-10) ? t0 + L / V * 1e5 : 1.0e25;
+        const double dt = flight_time(E, L);
+        tn = dt >= 0.0 ? t0 + dt : 1.0e25;
         // Equilibrium_charge_SHI (CS:2641-2680)
         double Zeff;
-        {
+        if (F32 && C.ion_kind_zeff == 0) {
+            const T vp = E > 0.0 ? m_sqrt((T)E * vfac_t) : T(0);
+            Zeff = (double)(T(C.ion_Z) * (T(1) - m_exp(-(vp * zfac))));
+        } else {
             const double vp = E > 0.0 ? sqrt(2.0 * E * kE / (C.ion_mass_p * kMp)) : 0.0;
             const double Zp = C.ion_Z;
             if (C.ion_kind_zeff == 0) Zeff = Zp * (1.0 - exp(-(vp * 125.0 / kC / (double)sh.pow_zp)));
@@ -638,15 +686,22 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
                 }
             }
         }
-        const int64_t slot = atomicAdd((unsigned long long*)&ctr->ev[0], 1ull);
+        if (slot == slot_end) {
+            slot = (int64_t)atomicAdd(&ctr->shi_slots, (unsigned long long)kSlotChunk);
+            slot_end = slot + kSlotChunk;
+        }
         if (slot < cap_ev) {
             ShiEv ev;
             ev.E = E; ev.Zeff = Zeff; ev.t0 = t0; ev.Z = Z; ev.dE = dE; ev.k = k; ev.ord = ord; ev.it = it; ev.pad = 0;
             evs[slot] = ev;
         } else atomicExch(&ctr->overflow, 1);
+        ++slot;
         ++ord; ++nev;
         if (Z >= C.Layer) tn = 1.0e16;
     }
+    for (; slot < slot_end; ++slot)   // mark the rest of the last chunk unused
+        if (slot < cap_ev) evs[slot].it = -1;
+    if (nev) atomicAdd(&ctr->ev[0], nev);
     if (err) atomicOr(&ctr->err_bits, err);
 }
 
@@ -660,6 +715,7 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
     if (i >= n_ev) return;
     const McConst<T>& C = *Cp;
     const ShiEv ev = evs[i];
+    if (ev.it < 0) return;   // an unused slot of a reserved chunk
     const uint64_t pid = shi_pid(C.it0 + ev.it);
     EvStream<T> s(C.seed, pid, ev.ord);
     s.word(); s.word(); s.word();
@@ -740,9 +796,9 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     } else {  // elastic (Mott)
         dE = mott_transfer(C, Eel, T(1), s);
         angles_lat(C, Eel, dE, T(1), s, theta, phi);
-        const int i = find_monoton(C.tg, C.Nt, tev);  // the interval t_{i-1} <= t < t_i
+        const int i = tbin(C, tev);  // the interval t_{i-1} <= t < t_i
         const int j = rbin(C, m_sqrt(X * X + Y * Y));
-        lat.add(tal, (i - 1) * C.NR + (j - 1), (double)dE);
+        lat.add(tal, (i - 1) * C.NR + (j - 1), dE);
         nev[2]++;
     }
     p.E = Eel - dE;
@@ -840,9 +896,9 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             dE = mott_transfer(C, Eel, hm, s);
             angles_lat(C, Eel, dE, hm, s, th1, ph1);
             Eh = check_hole(tb, Eel, dE, (P<T>*)nullptr);
-            const int i = find_monoton(C.tg, C.Nt, tev);
+            const int i = tbin(C, tev);
             const int j = rbin(C, m_sqrt(X * X + Y * Y));
-            lat.add(tal, (i - 1) * C.NR + (j - 1), (double)dE);
+            lat.add(tal, (i - 1) * C.NR + (j - 1), dE);
             nev[3]++;
         }
         T hp2, ht2;
@@ -987,36 +1043,34 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
     nev[6]++; nev[7] += 2;
 }
 
-// Hot kernel of a wavefront step: electrons and mobile valence holes run up to
-// K elastic collisions each.  A particle whose next event ionises goes to a
-// side queue; survivors go to the next generation's queue.
-template <class T>
-__global__ void __launch_bounds__(256) k_hot(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> ie, int ne,
-                                             PQ<T> ih, int nh, Out<T> o, PQ<T> e_inel, PQ<T> h_inel, Tal tal, int K,
-                                             int blocks_e) {
+// Hot kernel of a wavefront step, one per particle kind (electrons, mobile
+// valence holes) so each carries only its own event code: every particle
+// runs up to K elastic collisions.  A particle whose next event ionises goes
+// to a side queue; survivors go to the next generation's queue.
+template <class T, bool IS_E>
+__global__ void __launch_bounds__(256) k_hot(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> in, int n,
+                                             Out<T> o, PQ<T> side, Tal tal, int K) {
     const McConst<T>& C = *Cp;
-    const bool is_e = (int)blockIdx.x < blocks_e;
-    const int idx = (is_e ? blockIdx.x : blockIdx.x - blocks_e) * blockDim.x + threadIdx.x;
-    if (idx >= (is_e ? ne : nh)) return;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
     P<T> p;
-    load(is_e ? ie : ih, idx, p);
+    load(in, idx, p);
     unsigned err = 0;
     unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     LatAcc lat;
     MfpCache<T> mc;
     bool diverted = false;
     for (int e = 0; e < K && p.tn < C.Tim; ++e) {
-        const bool done = is_e ? electron_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc)
-                               : hole_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc);
+        bool done;
+        if constexpr (IS_E) done = electron_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc);
+        else done = hole_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc);
         if (!done) { diverted = true; break; }
     }
     lat.flush(tal);
-    if (diverted) {
-        if (is_e) append(e_inel, &o.ctr->n_out[Q_EINEL], &o.ctr->overflow, p);
-        else append(h_inel, &o.ctr->n_out[Q_HINEL], &o.ctr->overflow, p);
-    } else push(C, tal, o, is_e ? 0 : 1, p);
-    if (nev[2]) atomicAdd(&o.ctr->ev[2], nev[2]);
-    if (nev[3]) atomicAdd(&o.ctr->ev[3], nev[3]);
+    if (diverted) append(side, &o.ctr->n_out[IS_E ? Q_EINEL : Q_HINEL], &o.ctr->overflow, p);
+    else push(C, tal, o, IS_E ? 0 : 1, p);
+    const unsigned long long ne = IS_E ? nev[2] : nev[3];
+    if (ne) atomicAdd(&o.ctr->ev[IS_E ? 2 : 3], ne);
     if (err) atomicOr(&o.ctr->err_bits, err);
 }
 
@@ -1066,10 +1120,10 @@ template <class T>
 void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
                  PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s) {
     Out<T> o{{out.q[0], out.q[1], out.q[2], out.q[3]}, ctr};
-    const int be = (n_in[Q_E] + bs - 1) / bs, bh = (n_in[Q_HVB] + bs - 1) / bs;
-    if (be + bh > 0)
-        k_hot<T><<<be + bh, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], in.q[Q_HVB], n_in[Q_HVB], o, e_inel, h_inel,
-                                        tal, K, be);
+    if (n_in[Q_E] > 0)
+        k_hot<T, true><<<(n_in[Q_E] + bs - 1) / bs, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+    if (n_in[Q_HVB] > 0)
+        k_hot<T, false><<<(n_in[Q_HVB] + bs - 1) / bs, bs, 0, s>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
     k_rare<T><<<rare_blocks, 128, 0, s>>>(C, tb, e_inel, h_inel, in.q[Q_HDEEP], n_in[Q_HDEEP], in.q[Q_P],
                                           n_in[Q_P], o, tal);
 }
@@ -1084,6 +1138,30 @@ template void launch_step<float>(const McConst<float>*, const DevTabs<float>&, c
                                  const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t);
 template void launch_step<double>(const McConst<double>*, const DevTabs<double>&, const QSet<double>&, const int*,
                                   const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t);
+
+// ---- grid hints ----------------------------------------------------------------------------
+// hint of a bucket = the search result at the bucket's lowest value, which
+// never exceeds the result of any value the lookup maps to that bucket
+template <class T>
+__global__ void k_grid_hints(const T* tg, int Nt, T tg_inv, int* th, int tnb, const T* Rg, int NR, int key0,
+                             int* rh, int rnb) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < tnb) th[b] = find_monoton(tg, Nt, T(b) / tg_inv);
+    if (rh && b < rnb) {
+        T lo;
+        if constexpr (sizeof(T) == 4) lo = __uint_as_float((uint32_t)(key0 + b) << 19);
+        else lo = __longlong_as_double((long long)((uint64_t)(uint32_t)(key0 + b) << 48));
+        rh[b] = find_monoton(Rg, NR, lo);
+    }
+}
+template <class T>
+void launch_grid_hints(const McConst<T>& C, int* th, int* rh, cudaStream_t s) {
+    const int n = C.tg_nb > C.rg_nb ? C.tg_nb : C.rg_nb;
+    k_grid_hints<T><<<(n + 127) / 128, 128, 0, s>>>(C.tg, C.Nt, C.tg_inv, th, C.tg_nb, C.Rg, C.NR, C.rg_key0,
+                                                    C.rg_nb ? rh : nullptr, C.rg_nb);
+}
+template void launch_grid_hints<float>(const McConst<float>&, int*, int*, cudaStream_t);
+template void launch_grid_hints<double>(const McConst<double>&, int*, int*, cudaStream_t);
 
 // ---- finalize: difference arrays -> FP64 tallies -----------------------------------------
 // One thread per (slice, bin): prefix over time rows, in place (exact int64).

@@ -1,6 +1,7 @@
 // mc.cuh -- data layout of the event-based wavefront (shared by mc.cu and capi.cu).
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include "common.cuh"
 #include "impl.h"
 
@@ -24,6 +25,14 @@ struct McConst {
     int Nt, NR;
     const T* tg;        // [Nt] tallied times
     const T* Rg;        // [NR] outer radii
+    // bucket hints that turn the time and radius searches into a short
+    // forward walk (same index as the bisection; see launch_grid_hints)
+    const int* tg_hint; // [tg_nb] over [0, tg_hi), buckets of width 1/tg_inv
+    T tg_lo, tg_hi, tg_inv;
+    int tg_nb;
+    const int* rg_hint; // [rg_nb] by the top bits of R (16 buckets per octave); null: bisection
+    T rg_lo, rg_hi;
+    int rg_key0, rg_nb;
     uint64_t seed;
     int64_t it0;        // global index of iteration 0 of the batch
     int mobile_holes;   // hole_mass < 1e3
@@ -60,6 +69,7 @@ struct Ctrs {
     unsigned int err_bits;
     int first_bad_it;
     unsigned long long ev[8];     // shi, el inel, el elastic, hole, auger, radiative, photon abs, particles
+    unsigned long long shi_slots; // SHI record slots handed out (some unused, marked it = -1)
 };
 
 template <class T>
@@ -77,6 +87,27 @@ struct QSet {   // the four particle queues of one generation
 template <class T>
 void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
                  PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s);
+// Bucket hints of the time and radius grids.  A radius bucket is the bit
+// pattern of R without its low mantissa bits (monotone in R, 16 per octave).
+constexpr int kRgHintMax = 4096;
+__host__ __device__ inline uint32_t radius_key(float x) { uint32_t u; memcpy(&u, &x, 4); return u >> 19; }
+__host__ __device__ inline uint32_t radius_key(double x) { uint64_t u; memcpy(&u, &x, 8); return (uint32_t)(u >> 48); }
+
+// the hint sizes and end values from the first and last grid points (host)
+template <class T>
+inline void set_grid_hint_sizes(McConst<T>& C, T tg_first, T tg_last, T rg_first, T rg_last) {
+    C.tg_lo = tg_first; C.tg_hi = tg_last;
+    C.tg_nb = 2 * C.Nt + 2;
+    C.tg_inv = T(C.tg_nb) / tg_last;
+    C.rg_lo = rg_first; C.rg_hi = rg_last;
+    C.rg_key0 = (int)radius_key(rg_first);
+    const long long nb = (long long)radius_key(rg_last) - C.rg_key0 + 1;
+    C.rg_nb = (nb >= 1 && nb <= kRgHintMax) ? (int)nb : 0;
+}
+// fills th[C.tg_nb] and rh[C.rg_nb] from the device grids C.tg, C.Rg
+template <class T>
+void launch_grid_hints(const McConst<T>& C, int* th, int* rh, cudaStream_t s);
+
 void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
                const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s);
 void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,

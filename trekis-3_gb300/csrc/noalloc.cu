@@ -111,7 +111,7 @@ struct Shape { int Nt, NR, nsh, Nat, Nshl; bool mobile, photons; };
 
 template <class T>
 struct Layout {
-    McConst<T>* dC; Ctrs* ctr; T* tg; T* Rg; double* V; int* hmap;
+    McConst<T>* dC; Ctrs* ctr; T* tg; T* Rg; int* th; int* rh; double* V; int* hmap;
     unsigned long long* tall; size_t n_all; Tal tal;
     double *hstage, *hn, *hE, *hK, *htn, *htE; size_t hstage_n;
     double* calls; size_t calls_n;
@@ -128,6 +128,8 @@ size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
     L.ctr = c.take<Ctrs>(1);
     L.tg = c.take<T>((size_t)s.Nt);
     L.Rg = c.take<T>((size_t)s.NR);
+    L.th = c.take<int>(2 * (size_t)s.Nt + 2);
+    L.rh = c.take<int>((size_t)kRgHintMax);
     L.V = c.take<double>((size_t)s.NR);
     L.hmap = c.take<int>((size_t)s.nsh);
     const size_t rows = (size_t)s.Nt + 2;
@@ -309,13 +311,20 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     McConst<T> C;
     fill_const<T>(t, cfg, Nt, C);
     C.tg = L.tg; C.Rg = L.Rg;
+    {
+        T first = T(0), last = T(0);
+        walk_times(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int i, double x) { if (i == 0) first = (T)x; last = (T)x; });
+        set_grid_hint_sizes<T>(C, first, last, (T)cfg.Out_R[0], (T)cfg.Out_R[NR - 1]);
+    }
+    C.tg_hint = L.th; C.rg_hint = C.rg_nb ? L.rh : nullptr;
+    launch_grid_hints<T>(C, L.th, L.rh, strm);
 
     const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
     const int bs = cfg.block_size > 0 ? std::min(cfg.block_size, 256) : 256;
     const int rare_blocks = 2 * 152;
     int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 64);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
-    uint64_t steps = 0, launches = 0, ev_tot[8] = {0}, peak_all = 0;
+    uint64_t steps = 0, launches = 1, ev_tot[8] = {0}, peak_all = 0;   // the grid hints
     uint64_t h2d = sizeof(T) * (Nt + NR) + 8 * NR + sizeof(int) * nsh, d2h = 0;
     unsigned err_bits = 0;
     Ctrs hc;
@@ -337,7 +346,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
         NA_CK(cudaStreamSynchronize(strm));
         d2h += sizeof hc;
         if (!hc.overflow) {
-            launch_pairs<T>(L.dC, tb, L.evs, (int64_t)hc.ev[0], ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], L.tal,
+            launch_pairs<T>(L.dC, tb, L.evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)L.cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], L.tal,
                             L.ctr, strm);
             ++bl;
             NA_CK(cudaGetLastError());
@@ -353,7 +362,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
             const int n_in[4] = {hc.n_out[Q_E], hc.n_out[Q_HVB], hc.n_out[Q_HDEEP], hc.n_out[Q_P]};
             NA_CK(cudaMemsetAsync(L.ctr, 0, NQ * sizeof(int), strm));
             launch_step<T>(L.dC, tb, *in, n_in, *ot, L.e_inel, L.h_inel, L.tal, L.ctr, K, bs, rare_blocks, strm);
-            bl += 2; ++bsteps;
+            bl += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0); ++bsteps;
             NA_CK(cudaGetLastError());
             NA_CK(cudaMemcpyAsync(&hc, L.ctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
             NA_CK(cudaStreamSynchronize(strm));
