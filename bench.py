@@ -255,7 +255,12 @@ def run_gpu(args):
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
         "clocks": clk.summary(local),
         "events": {"total": tot_ev, "per_iteration": tot_ev / (args.steps * iters),
-                   "elastic_frac": sum(s.n_el_elastic for s in sts) / max(tot_ev, 1)},
+                   "elastic_frac": sum(s.n_el_elastic for s in sts) / max(tot_ev, 1),
+                   "by_kind_per_iteration": {f: sum(getattr(s, f) for s in sts) / (args.steps * iters) for f in (
+                       "n_shi", "n_el_inelastic", "n_el_elastic", "n_hole_events", "n_auger", "n_radiative",
+                       "n_photon_abs")},
+                   "wavefront_steps_per_step": sum(s.n_steps for s in sts) / args.steps,
+                   "peak_queue": max(s.peak_queue for s in sts)},
     }
     print(json.dumps(out))
     if world > 1:

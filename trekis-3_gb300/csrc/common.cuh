@@ -49,6 +49,20 @@ __device__ __forceinline__ double m_abs(double x) { return fabs(x); }
 __device__ __forceinline__ bool m_isnan(float x) { return isnan(x); }
 __device__ __forceinline__ bool m_isnan(double x) { return isnan(x); }
 
+// Fast forms for places where a few-ulp error is immaterial in FP32
+// kinematics (angles, positions, log-log table interpolation): the hardware
+// approximations.  FP64 keeps the correctly rounded functions, so FP64 runs
+// stay draw-for-draw equal to the oracle.  Flight lengths -log(RN) always use
+// the accurate log (its absolute error near RN = 1 would matter).
+__device__ __forceinline__ float f_sin(float x) { return __sinf(x); }
+__device__ __forceinline__ double f_sin(double x) { return sin(x); }
+__device__ __forceinline__ float f_cos(float x) { return __cosf(x); }
+__device__ __forceinline__ double f_cos(double x) { return cos(x); }
+__device__ __forceinline__ float f_log(float x) { return __logf(x); }
+__device__ __forceinline__ double f_log(double x) { return log(x); }
+__device__ __forceinline__ float f_exp(float x) { return __expf(x); }
+__device__ __forceinline__ double f_exp(double x) { return exp(x); }
+
 // ---- Philox4x32-10 -----------------------------------------------------------
 __host__ __device__ __forceinline__ void philox4x32(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
                                                     uint32_t k0, uint32_t k1, uint32_t out[4]) {
@@ -196,7 +210,7 @@ __device__ __forceinline__ T nfp2_fast(const FastTab<T>& t, T E, T lx) {
     if (m_abs(E2 - E1) < T(1.0e-6)) return L1 > L2 ? L1 : L2;
     if (E == E1) return L1;
     const T l1 = t.lE[n - 2];
-    return m_exp(t.lL[n - 2] + (t.lL[n - 1] - t.lL[n - 2]) / (t.lE[n - 1] - l1) * (lx - l1));
+    return f_exp(t.lL[n - 2] + (t.lL[n - 1] - t.lL[n - 2]) / (t.lE[n - 1] - l1) * (lx - l1));
 }
 
 }  // namespace tk

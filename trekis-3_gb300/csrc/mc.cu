@@ -157,7 +157,7 @@ __device__ void emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, 
         flush_run(C, tal, kind, sh, rbin(C, m_sqrt(X * X + Y * Y)), ia, ib, qE, qK);
         return;
     }
-    const T s_t = m_sin(th), s_p = m_sin(ph), c_p = m_cos(ph);
+    const T s_t = f_sin(th), s_p = f_sin(ph), c_p = f_cos(ph);
     int cur = -1, start = ia;
     for (int i = ia; i <= ib; ++i) {
         T L0 = V * (C.tg[i - 1] - t0) * T(1.0e-5);
@@ -308,7 +308,7 @@ __device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>&
         if (C.hole_mass > T(0)) h.M = C.hole_mass;
         else h.M = tb.dosM[find_monoton(tb.dosE, tb.nD, h.Ek) - 1];
         if (h.M < T(1.0e3)) {
-            const T lx = m_log(h.Ek);
+            const T lx = f_log(h.Ek);
             const T HI = nfp2_fast(tb.fHIMFP, h.Ek, lx);
             T HE;
             if (Etemp == Eh - C.Egap) HE = T(1.0e30);   // the reference skips elastic scattering here (MC:746)
@@ -343,8 +343,8 @@ __device__ __forceinline__ void cut_h(const McConst<T>& C, P<T>& p) {
 template <class T>
 __device__ __forceinline__ void new_angles(T phi0, T theta0, T theta, T psi, T& phi1, T& theta1) {
     const T twoPi = T(2.0) * pi_<T>();
-    phi1 = phi0 + theta * m_cos(theta0) * m_sin(psi);
-    theta1 = theta0 + theta * m_cos(psi);
+    phi1 = phi0 + theta * f_cos(theta0) * f_sin(psi);
+    theta1 = theta0 + theta * f_cos(psi);
     for (int g = 0; g < 64 && theta1 < T(0); ++g) { theta1 = m_abs(theta1); phi1 = phi1 + pi_<T>(); }
     for (int g = 0; g < 64 && theta1 > pi_<T>(); ++g) { theta1 = twoPi - theta1; phi1 = phi1 - pi_<T>(); }
     if (phi1 > twoPi) phi1 = phi1 - m_floor(phi1 / twoPi) * twoPi;
@@ -354,13 +354,13 @@ __device__ __forceinline__ void new_angles(T phi0, T theta0, T theta, T psi, T& 
 // total inelastic and elastic MFPs of an electron at E (both tables share log E)
 template <class T>
 __device__ __forceinline__ void el_mfps(const DevTabs<T>& tb, T E, T& I, T& Em) {
-    const T lx = m_log(E);
+    const T lx = f_log(E);
     I = nfp2_fast(tb.fIMFP, E, lx);
     Em = nfp2_fast(tb.fEMFP, E, lx);
 }
 template <class T>
 __device__ __forceinline__ void h_mfps(const DevTabs<T>& tb, T E, T& I, T& Em) {
-    const T lx = m_log(E);
+    const T lx = f_log(E);
     I = nfp2_fast(tb.fHIMFP, E, lx);
     Em = nfp2_fast(tb.fHEMFP, E, lx);
 }
@@ -441,7 +441,7 @@ __device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& thet
     T E2mc = E + T(2) * Ein, EmW = E - W;
     T W1 = E * E2mc - W * (E + Ein + Et), W2 = E * E2mc * EmW * (E2mc - W);
     T mu = (W2 > T(0)) ? W1 / m_sqrt(W2) : T(0);
-    if (m_abs(mu) > T(1)) { T RN = s.next(); mu = m_cos(pi_<T>() * RN); }
+    if (m_abs(mu) > T(1)) { T RN = s.next(); mu = f_cos(pi_<T>() * RN); }
     theta = m_acos(mu);
     phi = T(2) * pi_<T>() * s.next();
 }
@@ -529,7 +529,7 @@ template <class T>
 __device__ __forceinline__ T interp5_pre(T E1, T E2, T lE1, T lE2, T S1, T lS1, T lS2, T Ex, T lx) {
     if (m_abs(E2 - E1) < T(1.0e-6)) { return S1; }   // caller passes S1 = max(S1,S2) in that case
     if (Ex == E1) return S1;
-    return m_exp(lS1 + (lS2 - lS1) / (lE2 - lE1) * (lx - lE1));
+    return f_exp(lS1 + (lS2 - lS1) / (lE2 - lE1) * (lx - lE1));
 }
 
 // per-shell / total SHI MFP at the bracket nb (Which_shell MC:1803-1813, Next_free_path_2d MC:1874-1899)
@@ -766,9 +766,9 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     if constexpr (!FULL) { if (ionise) return false; }
     p.ord = ord + 1;
     const T th0 = p.th, ph0 = p.ph, tev = p.tn;
-    const T X = p.X + p.L * m_sin(th0) * m_sin(ph0);
-    const T Y = p.Y + p.L * m_sin(th0) * m_cos(ph0);
-    const T Z = p.Z + p.L * m_cos(th0);
+    const T X = p.X + p.L * f_sin(th0) * f_sin(ph0);
+    const T Y = p.Y + p.L * f_sin(th0) * f_cos(ph0);
+    const T Z = p.Z + p.L * f_cos(th0);
     T dE, theta, phi;
     if (FULL && ionise) {  // impact ionisation
         const int k = which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next());
@@ -853,9 +853,9 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         if constexpr (!FULL) { if (ionise) return false; }
         h.ord = ord + 1;
         const T th0 = h.th, ph0 = h.ph, tev = h.tn, hm = h.M;
-        const T X = h.X + h.L * m_sin(th0) * m_sin(ph0);
-        const T Y = h.Y + h.L * m_sin(th0) * m_cos(ph0);
-        const T Z = h.Z + h.L * m_cos(th0);
+        const T X = h.X + h.L * f_sin(th0) * f_sin(ph0);
+        const T Y = h.Y + h.L * f_sin(th0) * f_cos(ph0);
+        const T Z = h.Z + h.L * f_cos(th0);
         T dE, th1, ph1, Eh;
         if (FULL && ionise) {
             const int k = which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
@@ -1018,9 +1018,9 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
     const uint32_t ord = p.ord++;
     EvStream<T> s(C.seed, p.pid, ord);
     const T Eel = p.E;
-    const T X = p.X + p.L * m_sin(p.th) * m_sin(p.ph);
-    const T Y = p.Y + p.L * m_sin(p.th) * m_cos(p.ph);
-    const T Z = p.Z + p.L * m_cos(p.th);
+    const T X = p.X + p.L * f_sin(p.th) * f_sin(p.ph);
+    const T Y = p.Y + p.L * f_sin(p.th) * f_cos(p.ph);
+    const T Z = p.Z + p.L * f_cos(p.th);
     const int k = which_shell(C, tb.pE, tb.pL, tb.nP, Eel, s.next());
     const T dEc = electron_receives(C, tb, Eel, k, s, err);
     P<T> ne;
@@ -1048,7 +1048,7 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
 // runs up to K elastic collisions.  A particle whose next event ionises goes
 // to a side queue; survivors go to the next generation's queue.
 template <class T, bool IS_E>
-__global__ void __launch_bounds__(256) k_hot(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> in, int n,
+__global__ void __launch_bounds__(256, 4) k_hot(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> in, int n,
                                              Out<T> o, PQ<T> side, Tal tal, int K) {
     const McConst<T>& C = *Cp;
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
