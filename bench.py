@@ -113,13 +113,16 @@ def peaks():
 
 
 def profile_traffic():
-    """DRAM bytes per wavefront-step launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "k_hot_cfg1_traffic.json"
+    """DRAM bytes per collision of the wavefront-step kernels, from the committed
+    ncu summary (cold-cache capture of a smaller case of the same workload)."""
+    p = ROOT / "profiles" / "step_kernels_cfg1_traffic.txt"
     try:
-        d = json.load(open(p))
-        return d.get("dram_bytes_per_launch"), d.get("events_per_launch")
+        for line in open(p):
+            if line.startswith("dram_bytes_per_event"):
+                return float(line.split("=")[1])
     except Exception:
-        return None, None
+        pass
+    return None
 
 
 def alg_bytes_per_event(st, n_shells):
@@ -233,10 +236,8 @@ def run_gpu(args):
     bpe = alg_bytes_per_event(merged, n_sh)
     launches_step = sum(s.step_launches for s in sts)
     achieved = bpe * step_ev / (step_ms / 1e3) / 1e9           # GB/s over the step kernels
-    traffic_b, traffic_ev = profile_traffic()
-    traffic = None
-    if traffic_b and traffic_ev:
-        traffic = traffic_b / traffic_ev * (step_ev / max(launches_step, 1))
+    dram_per_event = profile_traffic()
+    traffic = dram_per_event * (step_ev / max(launches_step, 1)) if dram_per_event else None
     roof = {"bound": "hbm", "kernel": "k_hot<float> + k_rare<float> (wavefront step)", "achieved": achieved,
             "peak": hbm if hbm else 6800.0, "peak_source": "measured" if hbm else "fallback",
             "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "traffic": traffic,
