@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TREKIS_ABI_VERSION 1
+#define TREKIS_ABI_VERSION 2
 
 #define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
 #define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
@@ -182,6 +182,20 @@ typedef struct {
     double* Out_E_phot;    /* [Nt]                                     */
     double* Out_E_at;      /* [Nt]                                     */
     double* Out_E_h;       /* [Nt*Nat*Nshl]                            */
+    /* Spectra of Calculated_statistics (Monte_Carlo.f90:1019-1081).  Each
+     * iteration adds, at every grid time, its particle histogram divided by
+     * its own particle count at that time (electrons: all electrons; holes:
+     * all valence holes), as the reference does. */
+    int32_t N_dos;         /* rows of Out_Eh_vs_E: the material's N_dos */
+    int32_t pad_;
+    double* Out_Ee_vs_E;   /* [Nt*N_R] electrons per eV; the bins are the
+                              Out_R values read as energies in eV (as in the
+                              reference, Monte_Carlo.f90:1024-1029)       */
+    double* Out_Eh_vs_E;   /* [Nt*N_dos] valence holes per eV of kinetic
+                              energy on the DOS grid                      */
+    double* Out_theta;     /* [(Nt+1)*180] electron polar angle of flight,
+                              1-degree bins (row Nt+1 stays zero)          */
+    double* Out_theta_h;   /* [(Nt+1)*180] the same for mobile valence holes */
 } trekis_tallies;
 
 /* Counters and error record. */
@@ -301,6 +315,9 @@ int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
  *     trekis_last_error(); a single iteration that overflows the queues
  *     returns TREKIS_EOVERFLOW, as the allocating entry point does.
  *   - status->device_ms and status->step_ms stay 0 (no timing events).
+ *   - the spectra (Out_Ee_vs_E, Out_Eh_vs_E, Out_theta, Out_theta_h) must be
+ *     NULL: their per-iteration histograms do not fit the fixed scratch
+ *     (TREKIS_EUNSUPPORTED otherwise).
  *   - the scratch is zeroed by each call where the kernels need zeros
  *     (tallies, counters, staging), so nothing has to be cleared between
  *     calls.

@@ -163,6 +163,9 @@ struct Ctx {
     uint32_t err;
     // tallies (thread-local)
     double *ne, *Ee, *nph, *Eph, *Elat, *nh, *Eh, *Ehk, *totNe, *totNph, *totE, *Ee_t, *Eph_t, *Eat, *Eh_t;
+    // spectra (null when not requested)
+    double *sEe = nullptr, *sEh = nullptr, *sth = nullptr, *sthh = nullptr;
+    int N_dos = 0;
     uint64_t cnt[8];
 };
 
@@ -717,6 +720,46 @@ void photon_event(Ctx& c, int NOP, int i) {
     (void)i;
 }
 
+// ---- Calculated_statistics spectra (Monte_Carlo.f90:1019-1081) ------------------------
+// Per grid time, each particle adds 1/(bin width)/(particles of its kind in this
+// iteration now).  Electron energies are binned on the radius grid read as eV
+// (MC:1024-1029); angles on 1-degree bins (Out_theta1 = 1..180, SO:1191-1196);
+// valence-hole kinetic energies on the DOS grid (MC:1032-1040).
+void spectra(Ctx& c, int i, double co) {
+    const int Nt = c.Nt, NR = c.NR;
+    static const std::array<double, 180> deg = [] {
+        std::array<double, 180> d{};
+        for (int k = 0; k < 180; ++k) d[k] = k + 1;
+        return d;
+    }();
+    const double Ne = (double)c.el.size();
+    int Nvb = 0;
+    for (const H& hh : c.ho) if (is_vb(c, hh.KOA, hh.Shl)) ++Nvb;
+    for (const P& p : c.el) {
+        int j = find_monoton(c.Rg.data(), NR, p.E);
+        const double w = (j > 1) ? c.Rg[j - 1] - c.Rg[j - 2] : c.Rg[0];
+        c.sEe[(i - 1) + (size_t)Nt * (j - 1)] += 1.0 / w / Ne;
+        if (p.E > 0.0) {
+            const double th = (p.E > co) ? p.theta : 0.0;   // the stopped electron's angle reads as 0 (MC:966-970)
+            j = find_monoton(deg.data(), 180, th / Pi * 180.0);
+            c.sth[(i - 1) + (size_t)(Nt + 1) * (j - 1)] += 1.0 / Ne;
+        }
+    }
+    const double* dE = c.m->dos_E;
+    for (const H& hh : c.ho) {
+        if (!is_vb(c, hh.KOA, hh.Shl)) continue;
+        if (c.N_dos > 1) {
+            int j = find_monoton(dE, c.N_dos, hh.Ehkin);
+            const double w = (j > 1) ? dE[j - 1] - dE[j - 2] : dE[1] - dE[0];
+            c.sEh[(i - 1) + (size_t)Nt * (j - 1)] += 1.0 / w / (double)Nvb;
+        }
+        if (hh.Mass < 1.0e3 && hh.Ehkin > co) {
+            int j = find_monoton(deg.data(), 180, hh.theta / Pi * 180.0);
+            c.sthh[(i - 1) + (size_t)(Nt + 1) * (j - 1)] += 1.0 / (double)Nvb;
+        }
+    }
+}
+
 // ---- Calculated_statistics (Monte_Carlo.f90:881-1110), main tallies ----------------
 void statistics(Ctx& c, int i, double tim) {
     const int Nt = c.Nt, NR = c.NR, Nat = c.Nat;
@@ -760,6 +803,7 @@ void statistics(Ctx& c, int i, double tim) {
         c.Eh_t[(i - 1) + Nt * (hh.KOA + Nat * hh.Shl)] += hh.E + hh.Ehkin;
         sumH += hh.E + hh.Ehkin;
     }
+    if (c.sEe) spectra(c, i, co);
     c.totNe[i - 1] += (double)c.el.size();
     if (c.m->include_photons) {
         c.totNph[i - 1] += (double)nph;
@@ -881,7 +925,10 @@ int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, con
     double R0 = 0.0;
     for (int j = 0; j < NR; ++j) { Vg[j] = 1.0 / ((Rg[j] * Rg[j] - R0 * R0) * Pi * m.Layer); R0 = Rg[j]; }
     const size_t n2 = (size_t)Nt * NR, n4 = n2 * m.N_atoms * Nshl, n1 = Nt, n3 = (size_t)Nt * m.N_atoms * Nshl;
-    const size_t per = 5 * n2 + 3 * n4 + 6 * n1 + n3;
+    const bool spec = out.Out_Ee_vs_E || out.Out_Eh_vs_E || out.Out_theta || out.Out_theta_h;
+    if (spec && out.N_dos != m.N_dos) return TREKIS_EINVAL;
+    const size_t nth2 = (size_t)(Nt + 1) * 180, nd2 = (size_t)Nt * std::max(m.N_dos, 0);
+    const size_t per = 5 * n2 + 3 * n4 + 6 * n1 + n3 + (spec ? n2 + nd2 + 2 * nth2 : 0);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
     int nth = omp_get_max_threads();
@@ -915,6 +962,10 @@ int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, con
         double* t1 = c.Ehk + n4;
         c.totNe = t1; c.totNph = t1 + n1; c.totE = t1 + 2 * n1; c.Ee_t = t1 + 3 * n1; c.Eph_t = t1 + 4 * n1; c.Eat = t1 + 5 * n1;
         c.Eh_t = t1 + 6 * n1;
+        if (spec) {
+            c.sEe = c.Eh_t + n3; c.sEh = c.sEe + n2; c.sth = c.sEh + nd2; c.sthh = c.sth + nth2;
+            c.N_dos = m.N_dos;
+        }
         std::memset(c.cnt, 0, sizeof c.cnt);
 #pragma omp for schedule(dynamic)
         for (int it = 0; it < cfg.NMC; ++it) {
@@ -949,6 +1000,12 @@ int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, con
     addto(out.Out_E_phot, off, n1); off += n1;
     addto(out.Out_E_at, off, n1); off += n1;
     addto(out.Out_E_h, off, n3); off += n3;
+    if (spec) {
+        addto(out.Out_Ee_vs_E, off, n2); off += n2;
+        addto(out.Out_Eh_vs_E, off, nd2); off += nd2;
+        addto(out.Out_theta, off, nth2); off += nth2;
+        addto(out.Out_theta_h, off, nth2); off += nth2;
+    }
     if (st) {
         uint32_t eb = 0;
         uint64_t tot[8] = {0};

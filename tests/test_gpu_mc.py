@@ -175,3 +175,28 @@ def test_invalid_arguments(small0, gpu_lib):
     cfg, R = api.run_cfg(w, api.RunOptions())
     rc = gpu_lib.trekis_mc_run(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(bad.c()), C.byref(st))
     assert rc == -1
+
+
+@pytest.mark.gpu
+def test_fp64_spectra_match_oracle(small1):
+    """Out_Ee_vs_E, Out_Eh_vs_E, Out_theta, Out_theta_h (per-iteration
+    normalised histograms) on the GPU equal the oracle's in FP64 mode; the
+    main tallies are unchanged by asking for spectra."""
+    w, t, o = small1
+    opt = api.RunOptions(precision=1, seed=11)
+    g = api.new_tallies(w, spectra=True)
+    g, sg = api.mc_run(t, opt, tallies=g)
+    r = api.new_tallies(w, spectra=True)
+    cfg, _R = api.run_cfg(w, opt)
+    sr = abi.Status.fresh()
+    o.mc_run(cfg, r, sr)
+    assert sg.n_events == sr.n_events
+    for k in api.SPECTRA:
+        a, b = g[k], r[k]
+        assert np.max(np.abs(b)) > 0, k
+        tol = 1e-9 * np.abs(b) + 1e-12 * np.max(np.abs(b))
+        bad = np.abs(a - b) > tol
+        assert not np.any(bad), f"{k}: {np.sum(bad)} cells differ, max {np.max(np.abs(a - b)):.3e}"
+    plain, _ = api.mc_run(t, opt)
+    for k in plain.a:
+        assert np.array_equal(plain[k], g[k]), k

@@ -188,3 +188,34 @@ def test_edge_cases():
     w = configs.small(configs.cfg0, NMC=2, n_R=1)
     t, st = _oracle_run(w, api.RunOptions(seed=1))
     assert np.allclose(t["Out_ne"] * np.pi * w.material.Layer * w.R_edges[0] ** 2, t["Out_tot_Ne"])
+
+
+def test_spectra_normalisation():
+    """Spectra of Calculated_statistics are normalised per iteration by the
+    current counts (Monte_Carlo.f90:1019-1081): at every grid time each
+    iteration with electrons adds exactly 1 to sum_j width_j * Out_Ee_vs_E,
+    and at most 1 to sum_j Out_theta; valence holes likewise."""
+    import oracle_py
+    w = configs.small(configs.cfg1, NMC=3, Tim=20.0)
+    tc = abi.TableCfg(build_shi=1, build_photon=1, shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+    o = oracle_py.OracleTables(w.material.to_c(), api.ion_struct(w), tc, nthreads=2)
+    tal = api.new_tallies(w, spectra=True)
+    cfg, _R = api.run_cfg(w, api.RunOptions(precision=1, seed=4))
+    st = abi.Status.fresh()
+    o.mc_run(cfg, tal, st, nthreads=2, sched=1)
+    R = np.asarray(w.R_edges)
+    wE = np.diff(np.concatenate([[0.0], R]))
+    ee = tal.view("Out_Ee_vs_E")                       # [t, bin]
+    has_e = tal["Out_tot_Ne"] > 0
+    s_e = (ee * wE[None, :]).sum(1)
+    assert np.allclose(s_e[has_e], np.round(s_e[has_e]), atol=1e-9)
+    assert np.all(s_e <= 3 + 1e-9) and s_e[-1] == pytest.approx(3.0)
+    th = tal.view("Out_theta")
+    assert np.all(th[-1] == 0.0)                       # row Nt+1 is never written
+    assert np.all(th[:-1].sum(1) <= s_e + 1e-9) and th.sum() > 0
+    E = w.material.dos.E
+    wD = np.diff(E, prepend=E[0] - (E[1] - E[0]))
+    hh = tal.view("Out_Eh_vs_E")
+    s_h = (hh * wD[None, :]).sum(1)
+    assert s_h[-1] == pytest.approx(3.0)
+    assert tal.view("Out_theta_h").sum() > 0

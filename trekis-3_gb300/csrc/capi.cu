@@ -247,7 +247,8 @@ static int alloc_queue(Buffers& b, PQ<T>& q, int64_t cap, bool hole) {
     for (T** p : f) { *p = (T*)b.alloc(sizeof(T) * cap); if (!*p) return TREKIS_ENOMEM; }
     q.pid = (uint64_t*)b.alloc(8 * cap);
     q.ord = (uint32_t*)b.alloc(4 * cap);
-    if (!q.pid || !q.ord) return TREKIS_ENOMEM;
+    q.it = (uint16_t*)b.alloc(2 * cap);
+    if (!q.pid || !q.ord || !q.it) return TREKIS_ENOMEM;
     if (hole) {
         q.Ek = (T*)b.alloc(sizeof(T) * cap); q.M = (T*)b.alloc(sizeof(T) * cap); q.sh = (uint16_t*)b.alloc(2 * cap);
         if (!q.Ek || !q.M || !q.sh) return TREKIS_ENOMEM;
@@ -280,6 +281,8 @@ __global__ void k_add(double* dst, const double* src, size_t n) {
 // Device FP64 accumulators laid out exactly as the caller's tallies.
 struct DevOut {
     double *ne, *Ee, *np, *Ep, *lat, *nh, *Eh, *Ek, *totNe, *totNp, *totE, *E_e, *E_p, *E_at, *E_h;
+    double *sEe = nullptr, *sEh = nullptr, *sth = nullptr, *sthh = nullptr;   // spectra
+    bool spectra() const { return sEe || sEh || sth || sthh; }
 };
 
 template <class T> static const DevTabs<T>& tabs_of(const trekis_tables* t);
@@ -314,14 +317,19 @@ struct Workspace {
     void* evs = nullptr;       // SHI collision records of a batch
     int64_t cap_ev = 0;
     long long* lat_rows = nullptr;
+    // spectra: per-iteration int32 histograms of up to spec_cap iterations
+    int* spec = nullptr;
+    int spec_cap = 0;
+    size_t spec_it = 0, spec_row = 0;
+    double *wE = nullptr, *wD = nullptr;   // bin widths [eV]
     cudaEvent_t e0 = nullptr, e1 = nullptr, s0 = nullptr, s1 = nullptr;
     ~Workspace() {
         for (cudaEvent_t e : {e0, e1, s0, s1}) if (e) cudaEventDestroy(e);
     }
 };
 
-static uint64_t ws_key(int prec, int64_t cap, int Nt, int NR, int Nat, int Nshl) {
-    uint64_t k = (uint64_t)prec;
+static uint64_t ws_key(int prec, int64_t cap, int Nt, int NR, int Nat, int Nshl, bool spec) {
+    uint64_t k = (uint64_t)prec * 2 + (spec ? 1 : 0);
     k = k * 1000003ull + (uint64_t)cap;
     k = k * 1000003ull + (uint64_t)Nt;
     k = k * 1000003ull + (uint64_t)NR;
@@ -330,9 +338,10 @@ static uint64_t ws_key(int prec, int64_t cap, int Nt, int NR, int Nat, int Nshl)
 }
 
 template <class T>
-static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, int* rc) {
+static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, bool spec,
+                            int* rc) {
     const int64_t cap = cfg.queue_capacity > 0 ? cfg.queue_capacity : (int64_t)(sizeof(T) == 4 ? 24 : 12) << 20;
-    const uint64_t key = ws_key(sizeof(T), cap, Nt, cfg.N_R, Nat, Nshl);
+    const uint64_t key = ws_key(sizeof(T), cap, Nt, cfg.N_R, Nat, Nshl, spec);
     if (t->ws && t->ws_key == key) { *rc = 0; return (Workspace<T>*)t->ws.get(); }
     t->ws.reset();
     auto* w = new Workspace<T>();
@@ -369,17 +378,34 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     const size_t n3 = (size_t)Nt * Nat * Nshl;
     w->calls = (double*)b.alloc(8 * (3 * (size_t)Nt + n3));
     const size_t n2 = (size_t)Nt * NR, n4 = n2 * Nat * Nshl;
-    w->out_n = 5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3;
+    const size_t nsp = n2 + (size_t)Nt * t->dos_E.size() + 2 * (size_t)(Nt + 1) * kNTheta;
+    w->out_n = 5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3 + nsp;
     w->out = (double*)b.alloc(8 * w->out_n);
     w->cap_ev = std::max<int64_t>(cap / 2, 1 << 16);
     w->evs = b.alloc(shi_event_bytes() * w->cap_ev);
     w->lat_rows = (long long*)b.alloc(8 * Nt);
     if (!w->evs || !w->lat_rows) return nullptr;
+    if (spec) {   // histograms of up to 1 GiB worth of iterations per batch
+        const int nD = (int)t->dos_E.size();
+        w->spec_row = sp_row_ints(NR, nD);
+        w->spec_it = (size_t)(Nt + 2) * w->spec_row;
+        w->spec_cap = (int)std::max<size_t>(1, std::min<size_t>((1ull << 30) / (4 * w->spec_it), 65535));
+        w->spec = (int*)b.alloc(4 * w->spec_it * w->spec_cap);
+        w->wE = (double*)b.alloc(8 * NR);
+        w->wD = (double*)b.alloc(8 * std::max(nD, 1));
+        if (!w->spec || !w->wE || !w->wD) return nullptr;
+        std::vector<double> wd(std::max(nD, 1), 1.0);
+        for (int j = 0; j < nD; ++j)   // Monte_Carlo.f90:1034-1039
+            wd[j] = j > 0 ? t->dos_E[j] - t->dos_E[j - 1] : (nD > 1 ? t->dos_E[1] - t->dos_E[0] : 1.0);
+        if (cudaMemcpy(w->wD, wd.data(), 8 * wd.size(), cudaMemcpyHostToDevice) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
+    }
     if (!w->tall || !w->ctr || !w->dC || !w->tg || !w->Rg || !w->V || !w->hmap || !w->hstage || !w->calls || !w->out)
         return nullptr;
     Tal& tal = w->tal;
     tal.e_cnt = w->tall; tal.e_E = w->tall + n_e; tal.p_cnt = w->tall + 2 * n_e; tal.p_E = w->tall + 3 * n_e;
     tal.h_cnt = w->tall + 4 * n_e; tal.h_E = tal.h_cnt + n_h; tal.h_Ek = tal.h_E + n_h; tal.lat = tal.h_Ek + n_h;
+    tal.spec = w->spec; tal.sp_nE = NR; tal.sp_nD = (int)t->dos_E.size(); tal.sp_row = w->spec_row;
+    tal.sp_it = w->spec_it;
     w->hn = w->hstage; w->hE = w->hn + (size_t)Nt * NR * nsh; w->hK = w->hE + (size_t)Nt * NR * nsh;
     w->htn = w->hK + (size_t)Nt * NR * nsh; w->htE = w->htn + (size_t)Nt * nsh;
     std::vector<int> hs(nsh);
@@ -399,7 +425,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     const trekis_material& m = t->mat;
     const DevTabs<T>& tb = tabs_of<T>(t);
     int rc = 0;
-    Workspace<T>* ws = get_ws<T>(t, cfg, Nt, Nat, Nshl, &rc);
+    Workspace<T>* ws = get_ws<T>(t, cfg, Nt, Nat, Nshl, out.spectra(), &rc);
     if (!ws) { if (rc == TREKIS_ENOMEM) set_error("device workspace allocation failed"); return rc; }
     // constants
     McConst<T> C;
@@ -427,6 +453,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     C.mobile_holes = m.hole_mass < 1e3;
     C.mec2 = (T)(kMe * kC * kC / kE);
     C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
+    C.dosE = tb.dosE; C.nD = tb.nD;
     std::vector<double> tg = tallied_times(cfg.Tim, cfg.dt, cfg.dt_flag);
     std::vector<T> tgT(tg.begin(), tg.end()), RgT(cfg.Out_R, cfg.Out_R + cfg.N_R);
     std::vector<double> V(cfg.N_R);
@@ -435,12 +462,16 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     CK(cudaMemcpyAsync(ws->tg, tgT.data(), sizeof(T) * Nt, cudaMemcpyHostToDevice, strm));
     CK(cudaMemcpyAsync(ws->Rg, RgT.data(), sizeof(T) * cfg.N_R, cudaMemcpyHostToDevice, strm));
     CK(cudaMemcpyAsync(ws->V, V.data(), 8 * cfg.N_R, cudaMemcpyHostToDevice, strm));
+    std::vector<double> wE(cfg.N_R);   // electron energy bins are the radius values (Monte_Carlo.f90:1024-1029)
+    for (int j = 0; j < cfg.N_R; ++j) wE[j] = j > 0 ? cfg.Out_R[j] - cfg.Out_R[j - 1] : cfg.Out_R[0];
+    if (ws->wE) CK(cudaMemcpyAsync(ws->wE, wE.data(), 8 * cfg.N_R, cudaMemcpyHostToDevice, strm));
     C.tg = ws->tg; C.Rg = ws->Rg;
     set_grid_hint_sizes<T>(C, tgT[0], tgT[Nt - 1], RgT[0], RgT[cfg.N_R - 1]);
     C.tg_hint = ws->th; C.rg_hint = C.rg_nb ? ws->rh : nullptr;
     launch_grid_hints<T>(C, ws->th, ws->rh, strm);
     const int NR = cfg.N_R, nsh = t->nsh;
     Tal tal = ws->tal;
+    if (!out.spectra()) tal.spec = nullptr;
     Ctrs* dctr = ws->ctr;
     McConst<T>* dC = ws->dC;
     const double* dV = ws->V;
@@ -449,7 +480,10 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
     const int bs = cfg.block_size > 0 ? std::min(cfg.block_size, 256) : 256;
     const int64_t cap = ws->cap;
+    // the spectra hold one histogram per iteration of a batch
+    const int B_max = tal.spec ? ws->spec_cap : (1 << 16);
     int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 64);
+    B = std::min(B, B_max);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
     CK(cudaEventRecord(ws->e0, strm));
     uint64_t steps = 0, launches = 1, ev_tot[8] = {0}, peak_all = 0;   // the grid hints
@@ -465,6 +499,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         CK(cudaMemcpyAsync(dC, &C, sizeof C, cudaMemcpyHostToDevice, strm));
         h2d += sizeof C;
         CK(cudaMemsetAsync(ws->tall, 0, 8 * ws->n_all, strm));
+        if (tal.spec) CK(cudaMemsetAsync(tal.spec, 0, 4 * ws->spec_it * nb, strm));
         CK(cudaMemsetAsync(dctr, 0, sizeof(Ctrs), strm));
         QSet<T>* in = &ws->qa;
         QSet<T>* ot = &ws->qb;
@@ -523,11 +558,15 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         fin_block(tal.h_cnt, tal.h_E, tal.h_Ek, Nt, NR, nsh, dV, ws->hn, ws->hE, ws->hK, ws->htn, ws->htE, strm);
         fin_lat(tal.lat, Nt, NR, dV, out.lat, out.E_at, ws->lat_rows, strm);
         launches += 8;
+        if (tal.spec) {
+            fin_spectra(tal, nb, Nt, ws->wE, ws->wD, out.sEe, out.sEh, out.sth, out.sthh, strm);
+            launches += 2;
+        }
         CK(cudaGetLastError());
         done += nb;
         if (tune_batch && peak > 0) {   // size the next batch to half the queue capacity
             double per_it = (double)peak / nb;
-            B = std::max(1, std::min<int>((int)(0.5 * cap / per_it), 1 << 16));
+            B = std::max(1, std::min<int>((int)(0.5 * cap / per_it), B_max));
         }
     }
     // holes: compact shells -> caller slices
@@ -692,6 +731,7 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
     *Nt = (int)tallied_times(cfg->Tim, cfg->dt, cfg->dt_flag).size();
     if (o->Nt != *Nt || o->N_R != cfg->N_R || o->Nat != t->mat.N_atoms) { set_error("tally dimensions do not match"); return TREKIS_EINVAL; }
     for (int a = 0; a < t->mat.N_atoms; ++a) if (t->mat.atoms[a].N_shl > o->Nshl) return TREKIS_EINVAL;
+    if (o->Out_Eh_vs_E && o->N_dos != (int)t->dos_E.size()) { set_error("N_dos of the tallies differs from the material's"); return TREKIS_EINVAL; }
     return TREKIS_OK;
 }
 
@@ -710,8 +750,9 @@ static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, i
     // the workspace holds the per-call sums; create it first
     int rc = 0;
     double* calls;
-    if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) return rc; calls = calls_of<double>(t); }
-    else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) return rc; calls = calls_of<float>(t); }
+    const bool spec = o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h;
+    if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) return rc; calls = calls_of<double>(t); }
+    else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) return rc; calls = calls_of<float>(t); }
     (void)scratch_host_path;
     CK(cudaMemsetAsync(calls, 0, 8 * (3 * (size_t)Nt + n3), s));
     double* Ee_call = calls;
@@ -723,6 +764,7 @@ static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, i
     d.nh = o->Out_nh; d.Eh = o->Out_Eh; d.Ek = o->Out_Ehkin;
     d.totNe = o->Out_tot_Ne; d.totNp = o->Out_tot_Nphot; d.totE = o->Out_tot_E;
     d.E_e = Ee_call; d.E_p = Ep_call; d.E_at = Eat_call; d.E_h = Eh_call;
+    d.sEe = o->Out_Ee_vs_E; d.sEh = o->Out_Eh_vs_E; d.sth = o->Out_theta; d.sthh = o->Out_theta_h;
     if (!d.ne || !d.Ee || !d.np || !d.Ep || !d.lat || !d.totNe || !d.totNp) {
         set_error("the device entry point needs every radial and count tally array");
         return TREKIS_EINVAL;
@@ -766,8 +808,10 @@ int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const
     if (rc) { if (st) st->code = rc; return rc; }
     trekis_tables* t = const_cast<trekis_tables*>(tc);
     const size_t n2 = (size_t)Nt * cfg->N_R, n4 = n2 * o->Nat * o->Nshl, n3 = (size_t)Nt * o->Nat * o->Nshl;
-    if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) { if (st) st->code = rc; return rc; } }
-    else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, &rc)) { if (st) st->code = rc; return rc; } }
+    const bool spec = o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h;
+    const size_t nD2 = (size_t)Nt * t->dos_E.size(), nth2 = (size_t)(Nt + 1) * kNTheta;
+    if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) { if (st) st->code = rc; return rc; } }
+    else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) { if (st) st->code = rc; return rc; } }
     size_t nout = 0;
     double* base = (cfg->precision == 1) ? out_of<double>(t, &nout) : out_of<float>(t, &nout);
     cudaStream_t s;
@@ -779,7 +823,13 @@ int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const
     d.Out_nh = p; p += n4; d.Out_Eh = p; p += n4; d.Out_Ehkin = p; p += n4;
     double** f1[] = {&d.Out_tot_Ne, &d.Out_tot_Nphot, &d.Out_tot_E, &d.Out_E_e, &d.Out_E_phot, &d.Out_E_at};
     for (double** f : f1) { *f = p; p += Nt; }
-    d.Out_E_h = p;
+    d.Out_E_h = p; p += n3;
+    // spectra go through the same staging, only those the caller asked for
+    d.Out_Ee_vs_E = o->Out_Ee_vs_E ? p : nullptr; p += n2;
+    d.Out_Eh_vs_E = o->Out_Eh_vs_E ? p : nullptr; p += nD2;
+    d.Out_theta = o->Out_theta ? p : nullptr; p += nth2;
+    d.Out_theta_h = o->Out_theta_h ? p : nullptr; p += nth2;
+    if (!spec) nout = (size_t)(d.Out_E_h - base) + n3;   // stage and copy back only the main tallies
     rc = (cudaMemsetAsync(base, 0, 8 * nout, s) == cudaSuccess) ? 0 : TREKIS_ECUDA;
     if (!rc) rc = run_device_core(t, cfg, Nt, &d, st, s, base);
     std::vector<double> h(nout);
@@ -794,6 +844,7 @@ int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const
     add(o->Out_nh, n4); add(o->Out_Eh, n4); add(o->Out_Ehkin, n4);
     add(o->Out_tot_Ne, Nt); add(o->Out_tot_Nphot, Nt); add(o->Out_tot_E, Nt); add(o->Out_E_e, Nt);
     add(o->Out_E_phot, Nt); add(o->Out_E_at, Nt); add(o->Out_E_h, n3);
+    if (spec) { add(o->Out_Ee_vs_E, n2); add(o->Out_Eh_vs_E, nD2); add(o->Out_theta, nth2); add(o->Out_theta_h, nth2); }
     if (st) st->code = TREKIS_OK;
     return TREKIS_OK;
 }

@@ -32,6 +32,7 @@ struct P {  // one particle in registers
     uint64_t pid;
     uint32_t ord;
     int sh;
+    int it;     // iteration within the batch
 };
 
 // warp-aggregated append; returns -1 (and raises the overflow flag) when full.
@@ -55,13 +56,13 @@ __device__ __forceinline__ int64_t agg_append(int* ctr, int64_t cap, int* overfl
 template <class T>
 __device__ __forceinline__ void store(const PQ<T>& q, int64_t i, const P<T>& p) {
     q.E[i] = p.E; q.t0[i] = p.t0; q.tn[i] = p.tn; q.X[i] = p.X; q.Y[i] = p.Y; q.Z[i] = p.Z;
-    q.L[i] = p.L; q.th[i] = p.th; q.ph[i] = p.ph; q.pid[i] = p.pid; q.ord[i] = p.ord;
+    q.L[i] = p.L; q.th[i] = p.th; q.ph[i] = p.ph; q.pid[i] = p.pid; q.ord[i] = p.ord; q.it[i] = (uint16_t)p.it;
     if (q.Ek) { q.Ek[i] = p.Ek; q.M[i] = p.M; q.sh[i] = (uint16_t)p.sh; }
 }
 template <class T>
 __device__ __forceinline__ void load(const PQ<T>& q, int64_t i, P<T>& p) {
     p.E = q.E[i]; p.t0 = q.t0[i]; p.tn = q.tn[i]; p.X = q.X[i]; p.Y = q.Y[i]; p.Z = q.Z[i];
-    p.L = q.L[i]; p.th = q.th[i]; p.ph = q.ph[i]; p.pid = q.pid[i]; p.ord = q.ord[i];
+    p.L = q.L[i]; p.th = q.th[i]; p.ph = q.ph[i]; p.pid = q.pid[i]; p.ord = q.ord[i]; p.it = q.it[i];
     if (q.Ek) { p.Ek = q.Ek[i]; p.M = q.M[i]; p.sh = q.sh[i]; } else { p.Ek = T(0); p.M = T(0); p.sh = 0; }
 }
 
@@ -140,18 +141,53 @@ __device__ void flush_run(const McConst<T>& C, const Tal& tal, int kind, int sh,
     }
 }
 
+// 1-degree bin of a polar angle on the grid 1..180 (Find_in_array_monoton)
+template <class T>
+__device__ __forceinline__ int theta_bin(T th) {
+    const T xx = th / pi_<T>() * T(180);
+    if (!(xx >= T(1))) return (xx < T(1)) ? 1 : 2;   // NaN lands where the bisection puts it
+    if (xx >= T(180)) return kNTheta;
+    return (int)xx + 1;
+}
+
+// Spectra of one segment over rows [ia, ib] of its iteration
+// (Calculated_statistics, Monte_Carlo.f90:1019-1081): the particle count,
+// its energy bin and, when the angle counts, its angle bin.
+template <class T>
+__device__ void emit_spec(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T th, bool ang, int it,
+                          int ia, int ib) {
+    int* base = tal.spec + (size_t)it * tal.sp_it;
+    const size_t r0 = (size_t)ia * tal.sp_row, r1 = (size_t)(ib + 1) * tal.sp_row;
+    const bool end = ib < C.Nt;
+    auto put = [&](int off) {
+        atomicAdd(base + r0 + off, 1);
+        if (end) atomicAdd(base + r1 + off, -1);
+    };
+    const int nE = tal.sp_nE;
+    if (kind == 0) {
+        put(sp_ne());
+        put(sp_eE() + rbin(C, E) - 1);                        // energy binned on the radius grid values
+        if (E > T(0)) put(sp_eth(nE) + theta_bin(th) - 1);    // th is 0 for a stopped electron
+    } else if (sh == C.vb) {
+        put(sp_nh(nE));
+        if (C.nD > 1) put(sp_hE(nE) + find_monoton(C.dosE, C.nD, Ek) - 1);
+        if (ang) put(sp_hth(nE, tal.sp_nD) + theta_bin(th) - 1);
+    }
+}
+
 // Tally the free-flight segment [t0, tn) at every grid time t_i with
 // t0 < t_i <= min(tn, Tim), exactly as Calculated_statistics sees it:
 // position X + V (t_i - t0) 1e-5 along (th, ph) for moving particles.
 template <class T>
 __device__ void emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn, T X, T Y,
-                         T th, T ph, T V /* m/s, 0: static */) {
+                         T th, T ph, T V /* m/s, 0: static */, int it, bool ang) {
     const int Nt = C.Nt;
     if (!(t0 < C.tg_hi)) return;
     const int ia = tbin(C, t0);
     const T tend = tn < C.Tim ? tn : C.Tim;
     const int ib = (tend >= C.tg_hi) ? Nt : tbin(C, tend) - 1;
     if (ib < ia) return;
+    if (tal.spec && kind != 2) emit_spec(C, tal, kind, sh, E, Ek, th, ang, it, ia, ib);
     const long long qE = fixE(E), qK = fixE(Ek);
     if (V == T(0)) {
         flush_run(C, tal, kind, sh, rbin(C, m_sqrt(X * X + Y * Y)), ia, ib, qE, qK);
@@ -191,17 +227,18 @@ template <class T>
 __device__ __forceinline__ void emit_electron(const McConst<T>& C, const Tal& tal, const P<T>& p) {
     const T co = C.cut_off > T(0) ? C.cut_off : T(0);
     const bool mv = p.E > co;
-    emit_seg(C, tal, 0, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0), mv ? v_el(p.E) : T(0));
+    emit_seg(C, tal, 0, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0), mv ? v_el(p.E) : T(0),
+             p.it, true);
 }
 template <class T>
 __device__ __forceinline__ void emit_hole(const McConst<T>& C, const Tal& tal, const P<T>& p) {
     const T co = C.cut_off > T(0) ? C.cut_off : T(0);
     const bool mv = (p.M < T(1.0e3)) && (p.Ek > co);
-    emit_seg(C, tal, 1, p.sh, p.E, p.Ek, p.t0, p.tn, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0));
+    emit_seg(C, tal, 1, p.sh, p.E, p.Ek, p.t0, p.tn, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0), p.it, mv);
 }
 template <class T>
 __device__ __forceinline__ void emit_photon(const McConst<T>& C, const Tal& tal, const P<T>& p) {
-    if (p.E > T(0)) emit_seg(C, tal, 2, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, p.th, p.ph, T(kC));
+    if (p.E > T(0)) emit_seg(C, tal, 2, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, p.th, p.ph, T(kC), p.it, false);
 }
 
 // per-thread accumulator of the lattice energy (one atomic per change of
@@ -724,7 +761,7 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
     const double E = ev.E, dE = ev.dE, MSHI = C.MSHI;
     Out<T> o{{qe, qhvb, qhdeep, qe}, ctr};
     P<T> el;
-    el.pid = child_pid(pid, ev.ord, 0); el.ord = 0; el.sh = 0; el.Ek = T(0); el.M = T(0);
+    el.pid = child_pid(pid, ev.ord, 0); el.ord = 0; el.sh = 0; el.Ek = T(0); el.M = T(0); el.it = ev.it;
     const T dEc = electron_receives(C, tb, (T)dE, k, s, err);
     const T theta = (E <= 0.0) ? pi_<T>() / T(2)
         : (T)acos(sqrt((MSHI + kMe) * (MSHI + kMe) / (4.0 * MSHI * kMe) * dE / E));
@@ -741,7 +778,7 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
     emit_electron(C, tal, el);
     push(C, tal, o, 0, el);
     P<T> hh;
-    hh.pid = child_pid(pid, ev.ord, 1); hh.ord = 0;
+    hh.pid = child_pid(pid, ev.ord, 1); hh.ord = 0; hh.it = ev.it;
     make_hole(C, tb, hh, (T)ev.t0, el.X, el.Y, el.Z, k, (T)dE - dEc, s, err);
     emit_hole(C, tal, hh);
     push(C, tal, o, 1, hh);
@@ -779,7 +816,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         phi = T(2) * pi_<T>() * s.next();
         const T dEc = electron_receives(C, tb, dE, k, s, err);
         P<T> ne;
-        ne.pid = child_pid(p.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+        ne.pid = child_pid(p.pid, ord, 0); ne.ord = 0; ne.it = p.it; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
         ne.E = dEc; ne.t0 = tev;
         electron_flight(tb, ne, s);
         T ph1, th1;
@@ -788,7 +825,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         cut_e(C, ne);
         if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
         P<T> hh;
-        hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0;
+        hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0; hh.it = p.it;
         make_hole(C, tb, hh, tev, X, Y, Z, k, dE - dEc, s, err);
         emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
         emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
@@ -875,7 +912,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             if (m_isnan(th1)) th1 = pi_<T>() * s.next();
             const T dEc = electron_receives(C, tb, dE, k, s, err);
             P<T> ne;
-            ne.pid = child_pid(h.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+            ne.pid = child_pid(h.pid, ord, 0); ne.ord = 0; ne.it = h.it; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
             ne.E = dEc; ne.t0 = tev;
             electron_flight(tb, ne, s);
             (void)s.next();  // the reference draws one unused number here (MC:2611)
@@ -885,7 +922,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             cut_e(C, ne);
             if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
             P<T> hh;
-            hh.pid = child_pid(h.pid, ord, 1); hh.ord = 0;
+            hh.pid = child_pid(h.pid, ord, 1); hh.ord = 0; hh.it = h.it;
             make_hole(C, tb, hh, tev, X, Y, Z, k, dE - dEc, s, err);
             if (hh.E + hh.Ek < C.Egap - T(1.0e-12)) err |= TREKIS_ERR_HOLE_IN_GAP;
             Eh = check_hole(tb, Eel, dE, &ne);
@@ -964,10 +1001,10 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             hole_parameters(C, tb, h, En1, s);
             cut_h(C, h);
             P<T> hh;
-            hh.pid = child_pid(h.pid, ord, 1); hh.ord = 0;
+            hh.pid = child_pid(h.pid, ord, 1); hh.ord = 0; hh.it = h.it;
             make_hole(C, tb, hh, h.t0, h.X, h.Y, h.Z, K2, En2, s, err);
             P<T> ne;
-            ne.pid = child_pid(h.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+            ne.pid = child_pid(h.pid, ord, 0); ne.ord = 0; ne.it = h.it; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
             ne.E = Ee; ne.t0 = h.t0;
             electron_flight(tb, ne, s);
             ne.ph = T(2) * pi_<T>() * s.next();
@@ -996,7 +1033,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         hole_parameters(C, tb, h, En1, s);
         cut_h(C, h);
         P<T> pp;
-        pp.pid = child_pid(h.pid, ord, 2); pp.ord = 0; pp.sh = 0; pp.Ek = T(0); pp.M = T(0);
+        pp.pid = child_pid(h.pid, ord, 2); pp.ord = 0; pp.it = h.it; pp.sh = 0; pp.Ek = T(0); pp.M = T(0);
         const T Ip_ = nfp2(Tab<T>{tb.pE, tb.pIMFP, tb.nP}, dE);
         const T RN2 = s.next();
         const T Mt = -m_log(RN2) * Ip_;
@@ -1024,7 +1061,7 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
     const int k = which_shell(C, tb.pE, tb.pL, tb.nP, Eel, s.next());
     const T dEc = electron_receives(C, tb, Eel, k, s, err);
     P<T> ne;
-    ne.pid = child_pid(p.pid, ord, 0); ne.ord = 0; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
+    ne.pid = child_pid(p.pid, ord, 0); ne.ord = 0; ne.it = p.it; ne.sh = 0; ne.Ek = T(0); ne.M = T(0);
     ne.E = dEc; ne.t0 = p.tn;
     electron_flight(tb, ne, s);
     T ph1, th1;
@@ -1033,7 +1070,7 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
     cut_e(C, ne);
     if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
     P<T> hh;
-    hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0;
+    hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0; hh.it = p.it;
     make_hole(C, tb, hh, p.tn, X, Y, Z, k, Eel - dEc, s, err);
     if (hh.E + hh.Ek < C.Egap) err |= TREKIS_ERR_HOLE_IN_GAP;
     emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
@@ -1223,6 +1260,52 @@ void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long lo
     int n2 = ns * Nt;
     k_fin<<<(n2 + 127) / 128, 128, 0, s>>>(cnt, en, ek, Nt, NR, ns, V, on, oE, oK, tn_, tE);
 }
+// Spectra: one thread per (iteration, column) turns the difference rows into
+// per-time counts in place; then one thread per (time, bin) adds, over the
+// iterations in order, count / (particles of that iteration at that time).
+__global__ void k_spec_prefix(int* sp, int nit, int Nt, size_t row, size_t per_it) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)nit * row) return;
+    int* b = sp + (t / row) * per_it + t % row;
+    int c = 0;
+    for (int r = 1; r <= Nt; ++r) { c += b[(size_t)r * row]; b[(size_t)r * row] = c; }
+}
+__global__ void k_spec_fin(const int* sp, int nit, int Nt, int nE, int nD, size_t row, size_t per_it,
+                           const double* wE, const double* wD, double* oEe, double* oEh, double* oth, double* othh) {
+    const int nb = nE + nD + 2 * kNTheta;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)Nt * nb) return;
+    const int i = (int)(t / nb), b = (int)(t % nb);   // time row i+1, column b
+    int col, ncol;
+    double* out;
+    size_t o;
+    double w = 1.0;
+    if (b < nE) { col = sp_eE() + b; ncol = sp_ne(); out = oEe; o = i + (size_t)Nt * b; }
+    else if (b < nE + kNTheta) { const int k = b - nE; col = sp_eth(nE) + k; ncol = sp_ne(); out = oth; o = i + (size_t)(Nt + 1) * k; }
+    else if (b < nE + kNTheta + nD) { const int k = b - nE - kNTheta; col = sp_hE(nE) + k; ncol = sp_nh(nE); out = oEh; o = i + (size_t)Nt * k; }
+    else { const int k = b - nE - kNTheta - nD; col = sp_hth(nE, nD) + k; ncol = sp_nh(nE); out = othh; o = i + (size_t)(Nt + 1) * k; }
+    if (!out) return;
+    if (b < nE) w = wE[b];
+    else if (b >= nE + kNTheta && b < nE + kNTheta + nD) w = wD[b - nE - kNTheta];
+    const size_t r = (size_t)(i + 1) * row;
+    double acc = 0.0;
+    for (int it = 0; it < nit; ++it) {
+        const int* p = sp + (size_t)it * per_it + r;
+        const int n = p[ncol], c = p[col];
+        if (n > 0 && c != 0) acc += (double)c / (double)n;
+    }
+    if (acc != 0.0) out[o] += acc / w;
+}
+
+void fin_spectra(const Tal& tal, int nit, int Nt, const double* wE, const double* wD, double* oEe, double* oEh,
+                 double* oth, double* othh, cudaStream_t s) {
+    const size_t n1 = (size_t)nit * tal.sp_row;
+    k_spec_prefix<<<(unsigned)((n1 + 127) / 128), 128, 0, s>>>(tal.spec, nit, Nt, tal.sp_row, tal.sp_it);
+    const size_t n2 = (size_t)Nt * (tal.sp_nE + tal.sp_nD + 2 * kNTheta);
+    k_spec_fin<<<(unsigned)((n2 + 127) / 128), 128, 0, s>>>(tal.spec, nit, Nt, tal.sp_nE, tal.sp_nD, tal.sp_row,
+                                                           tal.sp_it, wE, wD, oEe, oEh, oth, othh);
+}
+
 void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,
              long long* rows, cudaStream_t s) {
     k_fin_lat<<<(Nt + 127) / 128, 128, 0, s>>>(lat, Nt, NR, V, oL, rows);

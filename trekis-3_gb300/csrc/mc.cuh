@@ -37,6 +37,8 @@ struct McConst {
     int64_t it0;        // global index of iteration 0 of the batch
     int mobile_holes;   // hole_mass < 1e3
     T mec2, alpha;      // electron rest energy [eV], fine-structure constant
+    const T* dosE;      // DOS energies (the valence-hole spectrum's bins)
+    int nD;
 };
 
 // Structure-of-arrays particle queue.
@@ -46,6 +48,7 @@ struct PQ {
     uint64_t* pid;
     uint32_t* ord;
     uint16_t* sh;
+    uint16_t* it;       // iteration within the batch (the spectra normalise per iteration)
     int64_t cap;
 };
 
@@ -53,7 +56,22 @@ struct PQ {
 // arrays over the time index (rows 0..Nt+1); lat is per interval.
 struct Tal {
     unsigned long long *e_cnt, *e_E, *p_cnt, *p_E, *h_cnt, *h_E, *h_Ek, *lat;
+    // Spectra (null when not tallied): int32 difference arrays over the time
+    // rows of each iteration of the batch, laid out [it][row][column].
+    int* spec;          // base of the block below
+    int sp_nE, sp_nD;   // energy bins of electrons (N_R) and of valence holes (N_dos)
+    size_t sp_row;      // ints per row: 1 + nE + 180 + 1 + nD + 180
+    size_t sp_it;       // ints per iteration: (Nt + 2) * sp_row
 };
+constexpr int kNTheta = 180;
+// offsets inside one spectra row
+__host__ __device__ inline int sp_ne() { return 0; }
+__host__ __device__ inline int sp_eE() { return 1; }
+__host__ __device__ inline int sp_eth(int nE) { return 1 + nE; }
+__host__ __device__ inline int sp_nh(int nE) { return 1 + nE + kNTheta; }
+__host__ __device__ inline int sp_hE(int nE) { return 2 + nE + kNTheta; }
+__host__ __device__ inline int sp_hth(int nE, int nD) { return 2 + nE + kNTheta + nD; }
+__host__ __device__ inline size_t sp_row_ints(int nE, int nD) { return (size_t)(2 + nE + 2 * kNTheta + nD); }
 
 constexpr double kEScale = 16777216.0;      // 2^24 per eV for particle energies
 constexpr double kLatScale = 1099511627776.0;  // 2^40 per eV for lattice energy
@@ -112,5 +130,9 @@ void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long lo
                const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s);
 void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,
              long long* rows, cudaStream_t s);
+// spectra of one batch of nit iterations -> FP64 outputs (any may be null);
+// wE[nE], wD[nD]: bin widths in eV
+void fin_spectra(const Tal& tal, int nit, int Nt, const double* wE, const double* wD, double* oEe, double* oEh,
+                 double* oth, double* othh, cudaStream_t s);
 
 }  // namespace tk

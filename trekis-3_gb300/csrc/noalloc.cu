@@ -103,6 +103,7 @@ void take_queue(Carve& c, PQ<T>& q, int64_t cap, bool hole) {
     for (T** f : {&q.E, &q.t0, &q.tn, &q.X, &q.Y, &q.Z, &q.L, &q.th, &q.ph}) *f = c.take<T>((size_t)cap);
     q.pid = c.take<uint64_t>((size_t)cap);
     q.ord = c.take<uint32_t>((size_t)cap);
+    q.it = c.take<uint16_t>((size_t)cap);
     if (hole) { q.Ek = c.take<T>((size_t)cap); q.M = c.take<T>((size_t)cap); q.sh = c.take<uint16_t>((size_t)cap); }
     else { q.Ek = nullptr; q.M = nullptr; q.sh = nullptr; }
 }
@@ -140,6 +141,7 @@ size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
         Tal& t = L.tal;
         t.e_cnt = L.tall; t.e_E = L.tall + n_e; t.p_cnt = L.tall + 2 * n_e; t.p_E = L.tall + 3 * n_e;
         t.h_cnt = L.tall + 4 * n_e; t.h_E = t.h_cnt + n_h; t.h_Ek = t.h_E + n_h; t.lat = t.h_Ek + n_h;
+        t.spec = nullptr; t.sp_nE = 0; t.sp_nD = 0; t.sp_row = 0; t.sp_it = 0;   // no spectra on this path
     }
     const size_t blk = (size_t)s.Nt * s.NR * s.nsh;
     L.hstage_n = 3 * blk + (size_t)s.Nt * s.nsh * 2;
@@ -311,6 +313,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     McConst<T> C;
     fill_const<T>(t, cfg, Nt, C);
     C.tg = L.tg; C.Rg = L.Rg;
+    C.dosE = tb.dosE; C.nD = tb.nD;
     {
         T first = T(0), last = T(0);
         walk_times(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int i, double x) { if (i == 0) first = (T)x; last = (T)x; });
@@ -447,6 +450,10 @@ int check_args(const trekis_tables* t, const trekis_material* mat, const trekis_
     }
     for (int a = 0; a < t->mat.N_atoms; ++a)
         if (t->mat.atoms[a].N_shl > o->Nshl) { set_error("tally shell dimension too small"); return TREKIS_EINVAL; }
+    if (o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h) {
+        set_error("spectra are not tallied by the no-alloc entry point (their per-iteration histograms would not fit)");
+        return TREKIS_EUNSUPPORTED;
+    }
     if (!o->Out_ne || !o->Out_Ee || !o->Out_nphot || !o->Out_Ephot || !o->Out_Elat || !o->Out_tot_Ne ||
         !o->Out_tot_Nphot) {
         set_error("the device entry point needs every radial and count tally array");

@@ -92,6 +92,8 @@ class Tallies(C.Structure):
         (n, _DP) for n in (
             "Out_ne", "Out_Ee", "Out_nphot", "Out_Ephot", "Out_Elat", "Out_nh", "Out_Eh", "Out_Ehkin",
             "Out_tot_Ne", "Out_tot_Nphot", "Out_tot_E", "Out_E_e", "Out_E_phot", "Out_E_at", "Out_E_h")
+    ] + [("N_dos", C.c_int32), ("pad_", C.c_int32)] + [
+        (n, _DP) for n in ("Out_Ee_vs_E", "Out_Eh_vs_E", "Out_theta", "Out_theta_h")
     ]
 
 

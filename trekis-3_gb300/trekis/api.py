@@ -46,11 +46,16 @@ def n_time_points(Tim, dt, dt_flag=0):
     return out
 
 
-class TallySet:
-    """Caller-owned tally arrays (numpy, float64), Fortran layout."""
+SPECTRA = ("Out_Ee_vs_E", "Out_Eh_vs_E", "Out_theta", "Out_theta_h")
+N_THETA = 180   # 1-degree bins of Out_theta (Sorting_output_data.f90:1191-1196)
 
-    def __init__(self, Nt, NR, Nat, Nshl):
-        self.Nt, self.NR, self.Nat, self.Nshl = Nt, NR, Nat, Nshl
+
+class TallySet:
+    """Caller-owned tally arrays (numpy, float64), Fortran layout.  With
+    ``spectra`` the four spectra of Calculated_statistics are tallied too."""
+
+    def __init__(self, Nt, NR, Nat, Nshl, N_dos=0, spectra=False):
+        self.Nt, self.NR, self.Nat, self.Nshl, self.N_dos = Nt, NR, Nat, Nshl, N_dos
         self.a = {}
         for k in TALLY_2D:
             self.a[k] = np.zeros(Nt * NR)
@@ -59,19 +64,28 @@ class TallySet:
         for k in TALLY_1D:
             self.a[k] = np.zeros(Nt)
         self.a["Out_E_h"] = np.zeros(Nt * Nat * Nshl)
+        if spectra:
+            self.a["Out_Ee_vs_E"] = np.zeros(Nt * NR)
+            self.a["Out_Eh_vs_E"] = np.zeros(Nt * N_dos)
+            self.a["Out_theta"] = np.zeros((Nt + 1) * N_THETA)
+            self.a["Out_theta_h"] = np.zeros((Nt + 1) * N_THETA)
 
     def c(self):
-        return abi.Tallies(Nt=self.Nt, N_R=self.NR, Nat=self.Nat, Nshl=self.Nshl,
+        return abi.Tallies(Nt=self.Nt, N_R=self.NR, Nat=self.Nat, Nshl=self.Nshl, N_dos=self.N_dos,
                            **{k: abi.dptr(v) for k, v in self.a.items()})
 
     def view(self, name):
         v = self.a[name]
-        if name in TALLY_2D:
+        if name in TALLY_2D or name == "Out_Ee_vs_E":
             return v.reshape(self.NR, self.Nt).T          # [t, R]
         if name in TALLY_4D:
             return v.reshape(self.Nshl, self.Nat, self.NR, self.Nt).transpose(3, 2, 1, 0)  # [t, R, atom, shell]
         if name == "Out_E_h":
             return v.reshape(self.Nshl, self.Nat, self.Nt).transpose(2, 1, 0)
+        if name == "Out_Eh_vs_E":
+            return v.reshape(self.N_dos, self.Nt).T       # [t, DOS node]
+        if name in ("Out_theta", "Out_theta_h"):
+            return v.reshape(N_THETA, self.Nt + 1).T      # [t (Nt+1 rows), degree]
         return v
 
     def __getitem__(self, k):
@@ -148,10 +162,11 @@ class Tables:
             pass
 
 
-def new_tallies(w):
+def new_tallies(w, spectra=False):
     Nt = len(n_time_points(w.Tim, w.dt))
     m = w.material
-    return TallySet(Nt, len(w.R_edges), len(m.atoms), m.n_shells_max)
+    nd = len(m.dos.E) if m.dos is not None else 0
+    return TallySet(Nt, len(w.R_edges), len(m.atoms), m.n_shells_max, N_dos=nd, spectra=spectra)
 
 
 def mc_run(tables, opt=None, NMC=None, tallies=None):
