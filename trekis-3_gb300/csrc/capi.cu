@@ -482,7 +482,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     const int64_t cap = ws->cap;
     // the spectra hold one histogram per iteration of a batch
     const int B_max = tal.spec ? ws->spec_cap : (1 << 16);
-    int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 64);
+    int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 256);
     B = std::min(B, B_max);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
     CK(cudaEventRecord(ws->e0, strm));

@@ -325,7 +325,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
     const int bs = cfg.block_size > 0 ? std::min(cfg.block_size, 256) : 256;
     const int rare_blocks = 2 * 152;
-    int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 64);
+    int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 256);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
     uint64_t steps = 0, launches = 1, ev_tot[8] = {0}, peak_all = 0;   // the grid hints
     uint64_t h2d = sizeof(T) * (Nt + NR) + 8 * NR + sizeof(int) * nsh, d2h = 0;

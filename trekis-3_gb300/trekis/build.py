@@ -19,6 +19,10 @@ OUT = PKG / "_build"
 LIB = OUT / "libtrekis_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# The track-loop kernels: single-precision division and square root to about
+# one ulp and FP32 denormals flushed.  These flags touch only FP32 arithmetic,
+# so FP64 runs keep IEEE division and square root (and their oracle parity).
+PER_FILE_FLAGS = {"mc": ["--prec-div=false", "--prec-sqrt=false", "--ftz=true"]}
 
 
 def nvcc():
@@ -46,7 +50,8 @@ def build_library(verbose=False, extra=()):
         o = OUT / (s.stem + ".o")
         objs.append(o)
         if not o.exists() or o.stat().st_mtime < max(s.stat().st_mtime, newest_dep):
-            jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", str(s), "-o", str(o)])
+            jobs.append([nvcc(), *ARCH, *NVCC_FLAGS, *PER_FILE_FLAGS.get(s.stem, []), *extra, "-c", str(s), "-o",
+                         str(o)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
         for out in ex.map(_run, jobs):
             if verbose and out.strip():
