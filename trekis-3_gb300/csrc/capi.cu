@@ -362,7 +362,7 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     const int NR = cfg.N_R, nsh = t->nsh;
     const size_t rows = (size_t)Nt + 2;
     const size_t n_e = rows * NR, n_h = rows * nsh * NR, n_l = (size_t)Nt * NR;
-    w->n_all = 4 * n_e + 3 * n_h + n_l;
+    w->n_all = 2 * (4 * n_e + 3 * n_h) + n_l;   // difference + single-row blocks, lattice
     w->tall = (unsigned long long*)b.alloc(8 * w->n_all);
     w->ctr = (Ctrs*)b.alloc(sizeof(Ctrs));
     w->dC = (McConst<T>*)b.alloc(sizeof(McConst<T>));
@@ -402,8 +402,9 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     if (!w->tall || !w->ctr || !w->dC || !w->tg || !w->Rg || !w->V || !w->hmap || !w->hstage || !w->calls || !w->out)
         return nullptr;
     Tal& tal = w->tal;
-    tal.e_cnt = w->tall; tal.e_E = w->tall + n_e; tal.p_cnt = w->tall + 2 * n_e; tal.p_E = w->tall + 3 * n_e;
-    tal.h_cnt = w->tall + 4 * n_e; tal.h_E = tal.h_cnt + n_h; tal.h_Ek = tal.h_E + n_h; tal.lat = tal.h_Ek + n_h;
+    tal.e_cnt = w->tall; tal.e_E = w->tall + 2 * n_e; tal.p_cnt = w->tall + 4 * n_e; tal.p_E = w->tall + 6 * n_e;
+    tal.h_cnt = w->tall + 8 * n_e; tal.h_E = tal.h_cnt + 2 * n_h; tal.h_Ek = tal.h_E + 2 * n_h;
+    tal.lat = tal.h_Ek + 2 * n_h;
     tal.spec = w->spec; tal.sp_nE = NR; tal.sp_nD = (int)t->dos_E.size(); tal.sp_row = w->spec_row;
     tal.sp_it = w->spec_it;
     w->hn = w->hstage; w->hE = w->hn + (size_t)Nt * NR * nsh; w->hK = w->hE + (size_t)Nt * NR * nsh;

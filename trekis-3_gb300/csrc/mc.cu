@@ -33,6 +33,7 @@ struct P {  // one particle in registers
     uint32_t ord;
     int sh;
     int it;     // iteration within the batch
+    int ti;     // time-grid index of tn (find_monoton over the tallied times), kept in registers
 };
 
 // warp-aggregated append; returns -1 (and raises the overflow flag) when full.
@@ -122,9 +123,18 @@ template <class T>
 __device__ void flush_run(const McConst<T>& C, const Tal& tal, int kind, int sh, int j, int r0, int r1,
                           long long qE, long long qK) {
     const int NR = C.NR;
+    // A run of a single grid time goes to the single-row block that follows
+    // each difference block (one entry instead of a start and an end entry);
+    // the finalize adds it after the prefix sum.
     if (kind == 0 || kind == 2) {
         unsigned long long* cnt = kind == 0 ? tal.e_cnt : tal.p_cnt;
         unsigned long long* en = kind == 0 ? tal.e_E : tal.p_E;
+        if (r0 == r1) {
+            const size_t a = (size_t)(C.Nt + 2 + r0) * NR + (j - 1);
+            add64(cnt + a, 1);
+            add64(en + a, qE);
+            return;
+        }
         add64(cnt + (size_t)r0 * NR + (j - 1), 1);
         add64(en + (size_t)r0 * NR + (j - 1), qE);
         if (r1 < C.Nt) {
@@ -132,6 +142,11 @@ __device__ void flush_run(const McConst<T>& C, const Tal& tal, int kind, int sh,
             add64(en + (size_t)(r1 + 1) * NR + (j - 1), -qE);
         }
     } else {
+        if (r0 == r1) {
+            const size_t a = ((size_t)(C.Nt + 2 + r0) * C.nsh + sh) * NR + (j - 1);
+            add64(tal.h_cnt + a, 1); add64(tal.h_E + a, qE); add64(tal.h_Ek + a, qK);
+            return;
+        }
         const size_t a = ((size_t)r0 * C.nsh + sh) * NR + (j - 1);
         add64(tal.h_cnt + a, 1); add64(tal.h_E + a, qE); add64(tal.h_Ek + a, qK);
         if (r1 < C.Nt) {
@@ -178,20 +193,24 @@ __device__ void emit_spec(const McConst<T>& C, const Tal& tal, int kind, int sh,
 // Tally the free-flight segment [t0, tn) at every grid time t_i with
 // t0 < t_i <= min(tn, Tim), exactly as Calculated_statistics sees it:
 // position X + V (t_i - t0) 1e-5 along (th, ph) for moving particles.
+// ia is the time-grid index of t0 (the caller has it: t0 is the time of the
+// event that started the segment); returns the index of min(tn, Tim), which is
+// the next segment's ia.  Consecutive segments of a particle tile the time
+// axis, so one search per segment suffices.
 template <class T>
-__device__ void emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn, T X, T Y,
-                         T th, T ph, T V /* m/s, 0: static */, int it, bool ang) {
+__device__ int emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn, T X, T Y,
+                        T th, T ph, T V /* m/s, 0: static */, int it, bool ang, int ia) {
     const int Nt = C.Nt;
-    if (!(t0 < C.tg_hi)) return;
-    const int ia = tbin(C, t0);
+    if (!(t0 < C.tg_hi)) return Nt;
     const T tend = tn < C.Tim ? tn : C.Tim;
     const int ib = (tend >= C.tg_hi) ? Nt : tbin(C, tend) - 1;
-    if (ib < ia) return;
+    const int tnext = (tend >= C.tg_hi) ? Nt : ib + 1;
+    if (ib < ia) return tnext;
     if (tal.spec && kind != 2) emit_spec(C, tal, kind, sh, E, Ek, th, ang, it, ia, ib);
     const long long qE = fixE(E), qK = fixE(Ek);
     if (V == T(0)) {
         flush_run(C, tal, kind, sh, rbin(C, m_sqrt(X * X + Y * Y)), ia, ib, qE, qK);
-        return;
+        return tnext;
     }
     const T s_t = f_sin(th), s_p = f_sin(ph), c_p = f_cos(ph);
     int cur = -1, start = ia;
@@ -207,6 +226,7 @@ __device__ void emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, 
         }
     }
     flush_run(C, tal, kind, sh, cur, start, ib, qE, qK);
+    return tnext;
 }
 
 template <class T> __device__ __forceinline__ T v_el(T E) { return m_sqrt(T(2.0) * E * T(kE) / T(kMe)); }
@@ -224,21 +244,22 @@ template <class T> __device__ __forceinline__ T tn_of(T t0, T L, T V) {
 }
 
 template <class T>
-__device__ __forceinline__ void emit_electron(const McConst<T>& C, const Tal& tal, const P<T>& p) {
+__device__ __forceinline__ int emit_electron(const McConst<T>& C, const Tal& tal, const P<T>& p, int ia) {
     const T co = C.cut_off > T(0) ? C.cut_off : T(0);
     const bool mv = p.E > co;
-    emit_seg(C, tal, 0, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0), mv ? v_el(p.E) : T(0),
-             p.it, true);
+    return emit_seg(C, tal, 0, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0),
+                    mv ? v_el(p.E) : T(0), p.it, true, ia);
 }
 template <class T>
-__device__ __forceinline__ void emit_hole(const McConst<T>& C, const Tal& tal, const P<T>& p) {
+__device__ __forceinline__ int emit_hole(const McConst<T>& C, const Tal& tal, const P<T>& p, int ia) {
     const T co = C.cut_off > T(0) ? C.cut_off : T(0);
     const bool mv = (p.M < T(1.0e3)) && (p.Ek > co);
-    emit_seg(C, tal, 1, p.sh, p.E, p.Ek, p.t0, p.tn, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0), p.it, mv);
+    return emit_seg(C, tal, 1, p.sh, p.E, p.Ek, p.t0, p.tn, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0), p.it,
+                    mv, ia);
 }
 template <class T>
-__device__ __forceinline__ void emit_photon(const McConst<T>& C, const Tal& tal, const P<T>& p) {
-    if (p.E > T(0)) emit_seg(C, tal, 2, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, p.th, p.ph, T(kC), p.it, false);
+__device__ __forceinline__ void emit_photon(const McConst<T>& C, const Tal& tal, const P<T>& p, int ia) {
+    if (p.E > T(0)) emit_seg(C, tal, 2, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, p.th, p.ph, T(kC), p.it, false, ia);
 }
 
 // per-thread accumulator of the lattice energy (one atomic per change of
@@ -775,12 +796,13 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
     el.th = theta; el.ph = phi;
     cut_e(C, el);
     if (el.E < T(-1.0e-9) || m_isnan(el.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
-    emit_electron(C, tal, el);
+    const int ti0 = tbin(C, el.t0);   // both particles start at the collision time
+    emit_electron(C, tal, el, ti0);
     push(C, tal, o, 0, el);
     P<T> hh;
     hh.pid = child_pid(pid, ev.ord, 1); hh.ord = 0; hh.it = ev.it;
     make_hole(C, tb, hh, (T)ev.t0, el.X, el.Y, el.Z, k, (T)dE - dEc, s, err);
-    emit_hole(C, tal, hh);
+    emit_hole(C, tal, hh, ti0);
     push(C, tal, o, 1, hh);
     if (err) atomicOr(&ctr->err_bits, err);
 }
@@ -794,6 +816,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
                                P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc) {
     const uint32_t ord = p.ord;
     EvStream<T> s(C.seed, p.pid, ord);
+    const int ti0 = p.ti;   // time-grid index of the event time
     const T Eel = p.E;
     T I, Em;
     if (mc.hit(Eel)) { I = mc.I; Em = mc.Em; }
@@ -827,13 +850,13 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         P<T> hh;
         hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0; hh.it = p.it;
         make_hole(C, tb, hh, tev, X, Y, Z, k, dE - dEc, s, err);
-        emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
-        emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
+        emit_electron(C, tal, ne, ti0); push(C, tal, o, 0, ne);
+        emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
         nev[1]++; nev[7] += 2;
     } else {  // elastic (Mott)
         dE = mott_transfer(C, Eel, T(1), s);
         angles_lat(C, Eel, dE, T(1), s, theta, phi);
-        const int i = tbin(C, tev);  // the interval t_{i-1} <= t < t_i
+        const int i = ti0;  // the interval t_{i-1} <= t < t_i
         const int j = rbin(C, m_sqrt(X * X + Y * Y));
         lat.add(tal, (i - 1) * C.NR + (j - 1), dE);
         nev[2]++;
@@ -848,7 +871,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     p.X = X; p.Y = Y; p.Z = Z; p.th = th1; p.ph = ph1;
     cut_e(C, p);
     if (p.E < T(-1.0e-9) || m_isnan(p.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
-    emit_electron(C, tal, p);
+    p.ti = emit_electron(C, tal, p, ti0);
     return true;
 }
 
@@ -880,6 +903,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
     const uint32_t ord = h.ord;
     EvStream<T> s(C.seed, h.pid, ord);
     if (!FULL && h.sh != C.vb) return false;
+    const int ti0 = h.ti;   // time-grid index of the event time
     if (h.sh == C.vb) {
         const T Eel = h.Ek;
         T HI, HE;
@@ -926,14 +950,14 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             make_hole(C, tb, hh, tev, X, Y, Z, k, dE - dEc, s, err);
             if (hh.E + hh.Ek < C.Egap - T(1.0e-12)) err |= TREKIS_ERR_HOLE_IN_GAP;
             Eh = check_hole(tb, Eel, dE, &ne);
-            emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
-            emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
+            emit_electron(C, tal, ne, ti0); push(C, tal, o, 0, ne);
+            emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
             nev[3]++; nev[7] += 2;
         } else {
             dE = mott_transfer(C, Eel, hm, s);
             angles_lat(C, Eel, dE, hm, s, th1, ph1);
             Eh = check_hole(tb, Eel, dE, (P<T>*)nullptr);
-            const int i = tbin(C, tev);
+            const int i = ti0;
             const int j = rbin(C, m_sqrt(X * X + Y * Y));
             lat.add(tal, (i - 1) * C.NR + (j - 1), dE);
             nev[3]++;
@@ -945,7 +969,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         hole_parameters(C, tb, h, Eh + C.Egap, s, &mc);
         cut_h(C, h);
         if (h.Ek < T(-1.0e-9) || m_isnan(h.Ek)) err |= TREKIS_ERR_NEG_ENERGY_H;
-        emit_hole(C, tal, h);
+        h.ti = emit_hole(C, tal, h, ti0);
         return true;
     }
     if constexpr (!FULL) return false;
@@ -1012,13 +1036,13 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             ne.X = h.X; ne.Y = h.Y; ne.Z = h.Z;
             cut_e(C, ne);
             if (ne.E < T(-1.0e-9) || m_isnan(ne.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
-            emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
-            emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
+            emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
+            emit_electron(C, tal, ne, ti0); push(C, tal, o, 0, ne);
             nev[7] += 2;
         } else {
             h.t0 = h.tn; h.tn = T(1.0e21);
         }
-        emit_hole(C, tal, h);
+        h.ti = emit_hole(C, tal, h, ti0);
         nev[4]++;
     } else {  // Radiative_decay (MC:2969-2997)
         T coun = count_sh(IpK, true);
@@ -1042,8 +1066,8 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         pp.E = dE; pp.t0 = h.t0; pp.X = h.X; pp.Y = h.Y; pp.Z = h.Z; pp.L = Mt;
         pp.tn = tn_of(pp.t0, Mt, T(kC));
         if (pp.E < T(-1.0e-9) || m_isnan(pp.E)) err |= TREKIS_ERR_PHOTON_ENERGY;
-        emit_hole(C, tal, h);
-        emit_photon(C, tal, pp); push(C, tal, o, 2, pp);
+        h.ti = emit_hole(C, tal, h, ti0);
+        emit_photon(C, tal, pp, ti0); push(C, tal, o, 2, pp);
         nev[5]++; nev[7] += 1;
     }
     return true;
@@ -1054,6 +1078,7 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
                              unsigned& err, unsigned long long* nev) {
     const uint32_t ord = p.ord++;
     EvStream<T> s(C.seed, p.pid, ord);
+    const int ti0 = p.ti;
     const T Eel = p.E;
     const T X = p.X + p.L * f_sin(p.th) * f_sin(p.ph);
     const T Y = p.Y + p.L * f_sin(p.th) * f_cos(p.ph);
@@ -1073,8 +1098,8 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
     hh.pid = child_pid(p.pid, ord, 1); hh.ord = 0; hh.it = p.it;
     make_hole(C, tb, hh, p.tn, X, Y, Z, k, Eel - dEc, s, err);
     if (hh.E + hh.Ek < C.Egap) err |= TREKIS_ERR_HOLE_IN_GAP;
-    emit_electron(C, tal, ne); push(C, tal, o, 0, ne);
-    emit_hole(C, tal, hh); push(C, tal, o, 1, hh);
+    emit_electron(C, tal, ne, ti0); push(C, tal, o, 0, ne);
+    emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
     // absorbed: the photon leaves the queues (its slot is not reused, unlike MC:2963)
     p.E = T(0); p.tn = T(1.0e27);
     nev[6]++; nev[7] += 2;
@@ -1092,6 +1117,7 @@ __global__ void __launch_bounds__(256, 4) k_hot(const McConst<T>* __restrict__ C
     if (idx >= n) return;
     P<T> p;
     load(in, idx, p);
+    p.ti = tbin(C, p.tn);
     unsigned err = 0;
     unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     LatAcc lat;
@@ -1128,10 +1154,10 @@ __global__ void __launch_bounds__(128) k_rare(const McConst<T>* __restrict__ Cp,
         LatAcc lat;
         MfpCache<T> mc;
         int kind;
-        if (g < n_e) { load(e_inel, g, p); electron_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 0; }
-        else if (g < n_e + n_h) { load(h_inel, g - n_e, p); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
-        else if (g < n_e + n_h + n_deep) { load(hdeep, g - n_e - n_h, p); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
-        else { load(ph, g - n_e - n_h - n_deep, p); photon_event(C, tb, tal, o, p, err, nev); kind = 2; }
+        if (g < n_e) { load(e_inel, g, p); p.ti = tbin(C, p.tn); electron_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 0; }
+        else if (g < n_e + n_h) { load(h_inel, g - n_e, p); p.ti = tbin(C, p.tn); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
+        else if (g < n_e + n_h + n_deep) { load(hdeep, g - n_e - n_h, p); p.ti = tbin(C, p.tn); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
+        else { load(ph, g - n_e - n_h - n_deep, p); p.ti = tbin(C, p.tn); photon_event(C, tb, tal, o, p, err, nev); kind = 2; }
         lat.flush(tal);
         push(C, tal, o, kind, p);
     }
@@ -1207,12 +1233,13 @@ __global__ void k_prefix(unsigned long long* cnt, unsigned long long* en, unsign
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns * NR) return;
     const int s = t / NR, j = t % NR;
+    const size_t blk = (size_t)(Nt + 2) * ns * NR;   // the single-row block follows the difference block
     long long c = 0, e = 0, k = 0;
     for (int r = 1; r <= Nt; ++r) {
         size_t a = ((size_t)r * ns + s) * NR + j;
-        c += (long long)cnt[a]; cnt[a] = (unsigned long long)c;
-        e += (long long)en[a]; en[a] = (unsigned long long)e;
-        if (ek) { k += (long long)ek[a]; ek[a] = (unsigned long long)k; }
+        c += (long long)cnt[a]; cnt[a] = (unsigned long long)(c + (long long)cnt[a + blk]);
+        e += (long long)en[a]; en[a] = (unsigned long long)(e + (long long)en[a + blk]);
+        if (ek) { k += (long long)ek[a]; ek[a] = (unsigned long long)(k + (long long)ek[a + blk]); }
     }
 }
 // One thread per (slice, row): weighted bins and per-time totals.

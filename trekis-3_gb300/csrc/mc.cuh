@@ -53,7 +53,8 @@ struct PQ {
 };
 
 // int64 fixed-point tallies of one batch.  *_cnt/_E/_Ek are difference
-// arrays over the time index (rows 0..Nt+1); lat is per interval.
+// arrays over the time index (rows 0..Nt+1), each followed by a block of the
+// same shape for runs that cover a single grid time; lat is per interval.
 struct Tal {
     unsigned long long *e_cnt, *e_E, *p_cnt, *p_E, *h_cnt, *h_E, *h_Ek, *lat;
     // Spectra (null when not tallied): int32 difference arrays over the time

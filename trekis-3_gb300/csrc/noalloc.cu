@@ -135,12 +135,12 @@ size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
     L.hmap = c.take<int>((size_t)s.nsh);
     const size_t rows = (size_t)s.Nt + 2;
     const size_t n_e = rows * s.NR, n_h = rows * s.nsh * s.NR, n_l = (size_t)s.Nt * s.NR;
-    L.n_all = 4 * n_e + 3 * n_h + n_l;
+    L.n_all = 2 * (4 * n_e + 3 * n_h) + n_l;   // difference + single-row blocks, lattice
     L.tall = c.take<unsigned long long>(L.n_all);
     if (L.tall) {
         Tal& t = L.tal;
-        t.e_cnt = L.tall; t.e_E = L.tall + n_e; t.p_cnt = L.tall + 2 * n_e; t.p_E = L.tall + 3 * n_e;
-        t.h_cnt = L.tall + 4 * n_e; t.h_E = t.h_cnt + n_h; t.h_Ek = t.h_E + n_h; t.lat = t.h_Ek + n_h;
+        t.e_cnt = L.tall; t.e_E = L.tall + 2 * n_e; t.p_cnt = L.tall + 4 * n_e; t.p_E = L.tall + 6 * n_e;
+        t.h_cnt = L.tall + 8 * n_e; t.h_E = t.h_cnt + 2 * n_h; t.h_Ek = t.h_E + 2 * n_h; t.lat = t.h_Ek + 2 * n_h;
         t.spec = nullptr; t.sp_nE = 0; t.sp_nD = 0; t.sp_row = 0; t.sp_it = 0;   // no spectra on this path
     }
     const size_t blk = (size_t)s.Nt * s.NR * s.nsh;
