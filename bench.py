@@ -45,7 +45,7 @@ def config_dict(w, iters, extra=None):
     d = {"workload": "cfg1: Al2O3-like (rho 3.95, gap 6.7 eV), Xe 131u 167 MeV, 10 nm, 0-1000 fs dt 1 fs, "
                      "100 log radial bins 1-1000 A, mobile VB holes (m_h=1), radiative decay + photons; "
                      f"job = {JOB_NMC} MC iterations, step = one batch of {iters} iterations",
-         "iterations_per_step": iters, "job_iterations": JOB_NMC, "sampler": "table",
+         "iterations_per_step": iters, "job_iterations": JOB_NMC, "sampler": "table (learned proposal: the neural object)",
          "kinematics": "fp32", "tables": "fp64 build", "tallies": "int64 fixed point",
          "l2": "512 MiB buffer written between steps (working set is L2-resident by design)"}
     if extra:
@@ -162,9 +162,9 @@ def run_gpu(args):
     per_rank_steps = args.warmup + args.steps
     base_it = rank * per_rank_steps * iters
 
-    def step(i, host=False):
+    def step(i, host=False, sampler=0):
         opt = api.RunOptions(seed=args.seed, iteration_offset=base_it + i * iters, queue_capacity=args.queue_cap,
-                             events_per_step=args.events_per_step)
+                             events_per_step=args.events_per_step, sampler=sampler)
         cfg, R = api.run_cfg(w, opt, NMC=iters)
         st = abi.Status.fresh()
         if host:
@@ -220,6 +220,26 @@ def run_gpu(args):
         e2e_s += dt
         h2d += st.h2d_bytes
         d2h += st.d2h_bytes
+    # the learned proposal ("neural" sampler): trained on the GPU from the
+    # tables, then the same timed steps again with sampler = 1; the draws are
+    # identical by construction, so the collision count must match
+    neural = None
+    if not args.no_neural:
+        rep = api.train_proposal(t, n_samples=args.mlp_samples, epochs=3, batch=8192, E_lo=1.0, E_hi=1.0e5)
+        n_ev = n_ms = 0.0
+        for i in range(args.steps):
+            st, _ = step(args.warmup + i, sampler=1)
+            n_ev += st.n_events
+            n_ms += st.device_ms
+            flush.fill_((i + 11) & 0xFF)
+        torch.cuda.synchronize()
+        nv = n_ev / (n_ms / 1e3)
+        neural = {"value": nv, "unit": UNIT, "vs_table": nv / (tot_ev / (tot_ms / 1e3)),
+                  "same_collisions_as_table": bool(n_ev == tot_ev),
+                  "training": {"samples_per_network": args.mlp_samples, "epochs": 3, "batch": 8192,
+                               "energies_eV": [1.0, 1.0e5], **rep},
+                  "note": "proposal only for the energy-transfer draw of ionising collisions "
+                          f"({sum(s_.n_el_inelastic for s_ in sts) / max(tot_ev, 1):.2e} of collisions here)"}
     if rank != 0:
         if world > 1:
             torch.distributed.barrier()
@@ -253,7 +273,7 @@ def run_gpu(args):
         "config": config_dict(w, iters, {"parallelism": f"iterations sharded over {world} GPU(s), no collective"}),
         "e2e": {"value": e2e_ev / e2e_s if e2e_s else None, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // max(args.e2e_steps, 1), "d2h_bytes_per_step": d2h // max(args.e2e_steps, 1)},
-        "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
+        "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "neural": neural,
         "clocks": clk.summary(local),
         "events": {"total": tot_ev, "per_iteration": tot_ev / (args.steps * iters),
                    "elastic_frac": sum(s.n_el_elastic for s in sts) / max(tot_ev, 1),
@@ -345,6 +365,8 @@ def main():
     ap.add_argument("--seed", type=int, default=20251203)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-neural", action="store_true", help="skip the learned-proposal arm")
+    ap.add_argument("--mlp-samples", type=int, default=10_000_000, help="training samples per network")
     ap.add_argument("--queue-cap", type=int, default=0, help="particles per queue buffer (0: library default)")
     ap.add_argument("--events-per-step", type=int, default=0, help="events per thread per wavefront step (0: tuned)")
     args = ap.parse_args()

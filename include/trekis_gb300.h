@@ -159,6 +159,10 @@ typedef struct {
     int64_t  queue_capacity;    /* particles per queue buffer                    */
     int32_t  iterations_per_batch;
     int32_t  use_graph;         /* capture the wavefront loop in a CUDA graph    */
+    int32_t  sampler;           /* 0: table inversion of the energy-transfer draw;
+                                   1: learned proposal + exact correction (needs
+                                   trekis_mlp_train; the draws are identical)    */
+    int32_t  pad2_;
 } trekis_run_cfg;
 
 /* Caller-owned tally arrays (un-normalised, accumulated with +=).  Any
@@ -331,6 +335,60 @@ int32_t trekis_mc_run_device_noalloc(const trekis_tables* t, const trekis_materi
                                      const trekis_ion* ion, const trekis_run_cfg* cfg,
                                      trekis_tallies* dev_out, trekis_status* st,
                                      void* stream);
+
+/* ---- learned proposal (no counterpart in the reference) -------------------
+ * The tensor-core product the proposal network trains and runs with:
+ * C[M x N] = A B (or C += A B when accumulate != 0), where
+ * A(m,k) = A[m*as_m + k*as_k] and B(k,n) = B[k*bs_k + n*bs_n] are FP32
+ * device arrays rounded to BF16, and the products accumulate in FP32
+ * (tcgen05.mma).  C is row-major with leading dimension ldc.  Synchronous.
+ * TREKIS_ETIMEOUT if a bounded wait for the tensor core ran out. */
+int32_t trekis_tc_gemm_bf16(const float* A, int64_t as_m, int64_t as_k,
+                            const float* B, int64_t bs_k, int64_t bs_n,
+                            float* C, int64_t ldc, int32_t M, int32_t N, int32_t K,
+                            int32_t accumulate);
+
+/* Learned proposal of the energy-transfer draw.  Per electron shell (and for
+ * valence holes) a network 2 -> 64 -> 64 -> 1 (SiLU; BF16 weights on the
+ * tensor cores, FP32 accumulation) maps (log E, u) onto the position of the
+ * bracket in the cumulative transfer row that sample_transfer inverts.  The
+ * table search then walks from that guess to the exact bracket, so a run with
+ * sampler = 1 draws exactly what the table sampler draws; the guess only
+ * replaces the bisection when it is right ("accepted").  Training samples
+ * come from the tables themselves (E log-uniform in [E_lo, E_hi], u uniform). */
+typedef struct {
+    int64_t  n_samples;   /* training samples per network                       */
+    int32_t  epochs;
+    int32_t  batch;       /* minibatch rows                                     */
+    double   lr;          /* Adam step size (decays x0.35 per epoch)            */
+    double   E_lo, E_hi;  /* [eV] training energies                             */
+    uint64_t seed;
+    int32_t  n_eval_E;    /* evaluation energies per network                    */
+    int32_t  n_eval_u;    /* stratified uniforms per evaluation energy          */
+} trekis_mlp_cfg;
+
+typedef struct {
+    int32_t n_nets, pad_;
+    double  train_ms;      /* device time of data generation, training, evaluation */
+    double  tc_gflop;      /* tensor-core work of the training passes            */
+    double  loss_first;    /* mean squared error of the first minibatch          */
+    double  loss_last;     /* mean squared error over the last epoch             */
+    double  kl_mean;       /* KL(table || proposal) of the bracket distributions */
+    double  kl_max;
+    double  accept_rate;   /* guesses that are the exact bracket                 */
+    double  mean_walk;     /* brackets walked from the guess to the exact one    */
+    double  mean_bisect;   /* probes a bisection of the same rows takes          */
+} trekis_mlp_report;
+
+/* Train the proposal networks of a table set (replaces any previous ones). */
+int32_t trekis_mlp_train(trekis_tables* t, const trekis_mlp_cfg* cfg, trekis_mlp_report* report);
+
+/* One forward and backward pass of a network on n rows (host arrays):
+ * params[4417] (W1[2][64], b1[64], W2[64][64], b2[64], w3[64], b3),
+ * X[n][2], targets[n]; writes the gradient of the mean squared error and the
+ * loss.  The same kernels as the training, for checking the gradients. */
+int32_t trekis_mlp_grad(const float* params, int64_t n, const float* X, const float* targets,
+                        float* grad, double* loss);
 
 /* Human-readable text of the last error on this thread. */
 const char* trekis_last_error(void);

@@ -50,6 +50,18 @@ static const int* upload_i(Buffers& b, const std::vector<int>& v) {
     return d;
 }
 
+// 1 for each cumulative row that is non-increasing in the precision T (rows
+// shorter than their slot end in 1e15 padding and are not); a proposal guess
+// is only used on such rows, where walking and bisecting agree
+template <class T>
+static std::vector<int> mono_flags(const std::vector<int>& off, const std::vector<double>& L) {
+    std::vector<int> f(off.size() > 0 ? off.size() - 1 : 0, 1);
+    for (size_t r = 0; r + 1 < off.size(); ++r)
+        for (int i = off[r] + 1; i < off[r + 1]; ++i)
+            if ((T)L[i] > (T)L[i - 1]) { f[r] = 0; break; }
+    return f;
+}
+
 static int find_mono_h2(const double* A, int N, double V) {
     if (V < A[0]) return 1;
     if (V >= A[N - 1]) return N;
@@ -114,6 +126,7 @@ static int upload_mc(trekis_tables* t, DevTabs<T>& d) {
     d.row_off = upload_i(b, off);
     d.row_hw = upload<T>(b, hw);
     d.row_L = upload<T>(b, L);
+    d.row_mono = upload_i(b, mono_flags<T>(off, L));
     d.nH = (int)t->hole[0].E.size();
     d.hE = upload<T>(b, t->hole[0].E);
     d.hL = upload<T>(b, cat(t->hole));
@@ -131,6 +144,7 @@ static int upload_mc(trekis_tables* t, DevTabs<T>& d) {
     d.hrow_off = upload_i(b, hoff);
     d.hrow_hw = upload<T>(b, hhw);
     d.hrow_L = upload<T>(b, hL);
+    d.hrow_mono = upload_i(b, mono_flags<T>(hoff, hL));
     if (t->has_phot) {
         d.nP = (int)t->phot[0].E.size();
         d.pE = upload<T>(b, t->phot[0].E);
@@ -313,6 +327,8 @@ struct Workspace {
     size_t hstage_n = 0;
     double* calls = nullptr;   // per-call E_e, E_phot, E_at [Nt each] and E_h [Nt*Nat*Nshl]
     double* out = nullptr;     // FP64 tally staging of the host-array entry point
+    float* guess = nullptr;    // proposal guesses of a step's pending ionisations
+    int* prop_err = nullptr;
     size_t out_n = 0;
     void* evs = nullptr;       // SHI collision records of a batch
     int64_t cap_ev = 0;
@@ -385,6 +401,10 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     w->evs = b.alloc(shi_event_bytes() * w->cap_ev);
     w->lat_rows = (long long*)b.alloc(8 * Nt);
     if (!w->evs || !w->lat_rows) return nullptr;
+    w->guess = (float*)b.alloc(4 * (size_t)(w->e_inel.cap + w->h_inel.cap));
+    w->prop_err = (int*)b.alloc(16);
+    if (!w->guess || !w->prop_err) return nullptr;
+    if (cudaMemset(w->prop_err, 0, 16) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
     if (spec) {   // histograms of up to 1 GiB worth of iterations per batch
         const int nD = (int)t->dos_E.size();
         w->spec_row = sp_row_ints(NR, nD);
@@ -478,6 +498,15 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     const double* dV = ws->V;
     CK(cudaMemsetAsync(ws->hstage, 0, 8 * ws->hstage_n, strm));
 
+    // learned proposal of the energy-transfer draw (exact: it only steers the search)
+    Proposer prop;
+    const Proposer* pp = nullptr;
+    if (cfg.sampler == 1) {
+        const MlpDev* md = mlp_device(t);
+        if (!md) { set_error("sampler 1 needs trained proposal networks (trekis_mlp_train)"); return TREKIS_EINVAL; }
+        prop.net = *md; prop.guess = ws->guess; prop.err = ws->prop_err; prop.blocks = 152;
+        pp = &prop;
+    }
     const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
     const int bs = cfg.block_size > 0 ? std::min(cfg.block_size, 256) : 256;
     const int64_t cap = ws->cap;
@@ -530,9 +559,10 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             int n_in[4] = {hc.n_out[Q_E], hc.n_out[Q_HVB], hc.n_out[Q_HDEEP], hc.n_out[Q_P]};
             CK(cudaMemsetAsync(dctr, 0, NQ * sizeof(int), strm));
             CK(cudaEventRecord(ws->s0, strm));
-            launch_step<T>(dC, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm);
+            launch_step<T>(dC, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm,
+                           ws->guess, pp);
             CK(cudaEventRecord(ws->s1, strm));
-            blaunch += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0); ++bsteps;
+            blaunch += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0) + (pp ? 1 : 0); ++bsteps;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
             d2h += sizeof hc;
@@ -728,6 +758,7 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
     if (t->ion.Kind_ion != 0) { set_error("Brandt-Kitagawa ions are not supported"); return TREKIS_EUNSUPPORTED; }
     if (cfg->NMC < 0 || cfg->N_R < 1 || !cfg->Out_R || !(cfg->Tim > 0) || !(cfg->dt > 0)) return TREKIS_EINVAL;
     if (cfg->dt_flag != 0 && cfg->dt_flag != 1) return TREKIS_EINVAL;
+    if (cfg->sampler != 0 && cfg->sampler != 1) { set_error("sampler must be 0 or 1"); return TREKIS_EINVAL; }
     for (int j = 1; j < cfg->N_R; ++j) if (!(cfg->Out_R[j] > cfg->Out_R[j - 1])) return TREKIS_EINVAL;
     *Nt = (int)tallied_times(cfg->Tim, cfg->dt, cfg->dt_flag).size();
     if (o->Nt != *Nt || o->N_R != cfg->N_R || o->Nat != t->mat.N_atoms) { set_error("tally dimensions do not match"); return TREKIS_EINVAL; }

@@ -141,6 +141,16 @@ __device__ __forceinline__ int find_decreasing(const T* __restrict__ A, int N, T
     return ic;
 }
 
+// find_decreasing started from a guess g: walks to the same index (the number
+// of leading nodes above V, clamped to [1, N]) in |g - result| steps
+template <class T>
+__device__ __forceinline__ int find_decreasing_from(const T* __restrict__ A, int N, T V, int g) {
+    int j = g < 1 ? 1 : (g > N ? N : g);
+    if (A[j - 1] > V) { while (j < N && A[j] > V) ++j; }
+    else { while (j > 1 && !(A[j - 1] > V)) --j; }
+    return j;
+}
+
 template <class T>
 __device__ __forceinline__ T interp(int flag, T E1, T E2, T S1, T S2, T Ex) {
     if (m_abs(E2 - E1) < T(1.0e-6)) return S1 > S2 ? S1 : S2;

@@ -52,6 +52,7 @@ struct DevTabs {
     const T* elastE; const T* elastL; int nEl;
     const int* row_off;    // [nsh*nE + 1]
     const T* row_hw; const T* row_L;
+    const int* row_mono;   // [nsh*nE] 1: the row is non-increasing in T
     // holes
     const T* hE; int nH;
     const T* hL;           // [nsh][nH]
@@ -59,6 +60,7 @@ struct DevTabs {
     const T* hElastE; const T* hElastL; int nHel;
     const int* hrow_off;   // [nH + 1]
     const T* hrow_hw; const T* hrow_L;
+    const int* hrow_mono;  // [nH]
     // photons
     const T* pE; int nP;
     const T* pL;           // [nsh][nP]
@@ -116,10 +118,14 @@ struct trekis_tables {
     // precision, capacity or tally shape of a call changes
     std::shared_ptr<void> ws;
     uint64_t ws_key = 0;
+    // trained proposal networks of the energy-transfer draw (mlp.cu), if any
+    std::shared_ptr<void> mlp;
 };
 
 namespace tk {
 void set_error(const std::string& s);
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st);
 std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax);
+struct MlpDev;
+const MlpDev* mlp_device(const trekis_tables* t);
 }  // namespace tk

@@ -22,6 +22,7 @@
 // Electron_Monte_Carlo (MC:2253-2474), Hole_Monte_Carlo (MC:2517-2869) and
 // Photon_Monte_Carlo (MC:2873-2965).
 #include "mc.cuh"
+#include "tc.cuh"
 
 
 namespace tk {
@@ -504,16 +505,21 @@ __device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& thet
     phi = T(2) * pi_<T>() * s.next();
 }
 
-// interpolate_transferred_energy (CS:1968-2045) over one table of cumulative rows
+// interpolate_transferred_energy (CS:1968-2045) over one table of cumulative rows.
+// fg >= 0: a proposed bracket position (fraction of the row) from the learned
+// proposal; the search walks from it to the same bracket the bisection finds.
 template <class T>
-__device__ T interp_transfer(const T* Eg, int nE, const int* roff, const T* rhw, const T* rL, T Ele, T L_need) {
+__device__ T interp_transfer(const T* Eg, int nE, const int* roff, const T* rhw, const T* rL, T Ele, T L_need,
+                             float fg = -1.f, const int* rmono = nullptr) {
     int iE = find_monoton(Eg, nE, Ele);
     if (iE > 1 && m_abs(Eg[iE - 2] - Ele) < T(1.0e-6)) iE -= 1;
     auto one = [&](int ie) -> T {
         const int o = roff[ie - 1], len = roff[ie] - o;
         const T* hw = rhw + o;
         const T* L = rL + o;
-        int ih = find_decreasing(L, len, L_need);
+        const int ih = (fg >= 0.f && rmono && rmono[ie - 1])
+                           ? find_decreasing_from(L, len, L_need, 1 + (int)(fg * (float)(len - 1)))
+                           : find_decreasing(L, len, L_need);
         if (ih == 1 || ih == len) return hw[ih - 1];
         return interp<T>(5, L[ih - 1], L[ih], hw[ih - 1], hw[ih], L_need);
     };
@@ -531,7 +537,7 @@ __device__ T interp_transfer(const T* Eg, int nE, const int* roff, const T* rhw,
 // Electron_energy_transfer_inelastic (CS:1793-1871), tabulated rows (CS_method = 1)
 template <class T>
 __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hole, int k, T Ele, T L_tot, T RN,
-                             unsigned& err) {
+                             unsigned& err, float fg = -1.f) {
     T L_need = L_tot / RN;
     T Emin = C.Ip[k];
     if (Emin <= T(1.0e-3)) Emin = T(1.0e-3);
@@ -540,8 +546,9 @@ __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hol
         Mass = (C.hole_mass >= T(0)) ? C.hole_mass : tb.dosM[find_monoton(tb.dosE, tb.nD, Ele) - 1];
         Emax = T(4) * Ele * Mass / ((Mass + T(1)) * (Mass + T(1)));
     } else Emax = (Ele + Emin) / T(2);
-    T E = hole ? interp_transfer(tb.hE, tb.nH, tb.hrow_off, tb.hrow_hw, tb.hrow_L, Ele, L_need)
-               : interp_transfer(tb.elE, tb.nE, tb.row_off + (size_t)k * tb.nE, tb.row_hw, tb.row_L, Ele, L_need);
+    T E = hole ? interp_transfer(tb.hE, tb.nH, tb.hrow_off, tb.hrow_hw, tb.hrow_L, Ele, L_need, fg, tb.hrow_mono)
+               : interp_transfer(tb.elE, tb.nE, tb.row_off + (size_t)k * tb.nE, tb.row_hw, tb.row_L, Ele, L_need, fg,
+                                 tb.row_mono + (size_t)k * tb.nE);
     if (E < Emin) E = Emin;
     if (E > Emax) E = Emax;
     if (E < C.Egap) err |= TREKIS_ERR_NEG_TRANSFER;
@@ -813,7 +820,8 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
 // event is redone from the same stream by the FULL version.
 template <class T, bool FULL>
 __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
-                               P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc) {
+                               P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc,
+                               float fg = -1.f) {
     const uint32_t ord = p.ord;
     EvStream<T> s(C.seed, p.pid, ord);
     const int ti0 = p.ti;   // time-grid index of the event time
@@ -833,7 +841,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     if (FULL && ionise) {  // impact ionisation
         const int k = which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next());
         const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
-        dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err);
+        dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err, fg);
         theta = m_acos((Eel - dE) / m_sqrt(Eel * (Eel - dE)));
         if (m_isnan(theta)) theta = s.next() * pi_<T>();
         phi = T(2) * pi_<T>() * s.next();
@@ -899,7 +907,7 @@ __device__ T check_hole(const DevTabs<T>& tb, T Eel, T& dE, P<T>* el) {
 // One hole event; FULL=false compiles only valence-hole elastic scattering.
 template <class T, bool FULL>
 __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& h,
-                           unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc) {
+                           unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc, float fg = -1.f) {
     const uint32_t ord = h.ord;
     EvStream<T> s(C.seed, h.pid, ord);
     if (!FULL && h.sh != C.vb) return false;
@@ -921,7 +929,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         if (FULL && ionise) {
             const int k = which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
             const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
-            dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err);
+            dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err, fg);
             // Update_holes_angles_el (MC:1142-1168)
             // masses in kg as the reference writes them (FP64); in electron
             // masses for FP32, where (Mh+me)^2 would underflow
@@ -1143,7 +1151,7 @@ __global__ void __launch_bounds__(256, 4) k_hot(const McConst<T>* __restrict__ C
 template <class T>
 __global__ void __launch_bounds__(128) k_rare(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> e_inel,
                                               PQ<T> h_inel, PQ<T> hdeep, int n_deep, PQ<T> ph, int n_ph, Out<T> o,
-                                              Tal tal) {
+                                              Tal tal, const float* __restrict__ guess) {
     const McConst<T>& C = *Cp;
     const int n_e = o.ctr->n_out[Q_EINEL], n_h = o.ctr->n_out[Q_HINEL];
     const int total = n_e + n_h + n_deep + n_ph;
@@ -1154,8 +1162,15 @@ __global__ void __launch_bounds__(128) k_rare(const McConst<T>* __restrict__ Cp,
         LatAcc lat;
         MfpCache<T> mc;
         int kind;
-        if (g < n_e) { load(e_inel, g, p); p.ti = tbin(C, p.tn); electron_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 0; }
-        else if (g < n_e + n_h) { load(h_inel, g - n_e, p); p.ti = tbin(C, p.tn); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
+        if (g < n_e) {
+            load(e_inel, g, p); p.ti = tbin(C, p.tn);
+            electron_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc, guess ? guess[g] : -1.f);
+            kind = 0;
+        } else if (g < n_e + n_h) {
+            load(h_inel, g - n_e, p); p.ti = tbin(C, p.tn);
+            hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc, guess ? guess[g] : -1.f);
+            kind = 1;
+        }
         else if (g < n_e + n_h + n_deep) { load(hdeep, g - n_e - n_h, p); p.ti = tbin(C, p.tn); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
         else { load(ph, g - n_e - n_h - n_deep, p); p.ti = tbin(C, p.tn); photon_event(C, tb, tal, o, p, err, nev); kind = 2; }
         lat.flush(tal);
@@ -1165,6 +1180,120 @@ __global__ void __launch_bounds__(128) k_rare(const McConst<T>* __restrict__ Cp,
         if (nev[q]) atomicAdd(&o.ctr->ev[q], nev[q]);
     if (err) atomicOr(&o.ctr->err_bits, err);
 }
+
+// ---- learned proposal: bracket guesses for the pending ionisations of a step --------------
+__device__ __forceinline__ float silu_f(float z) { return z / (1.f + __expf(-z)); }
+
+// One warpgroup per 128 pending draws (side-queue entries g < n_e + n_h, the
+// indexing of k_rare).  Each thread replays its event's stream up to the
+// transfer draw (ionise, shell, u), maps (log E, u) onto the inputs of the
+// network of that shell, and the tile runs every network present in it: the
+// 2 -> 64 layer on the CUDA cores, the 64 -> 64 layer as one tcgen05 MMA
+// (BF16 operands, FP32 accumulator in TMEM), the 64 -> 1 layer on the CUDA
+// cores.  A guess only steers the search; any value gives the same draw.
+template <class T>
+__global__ void __launch_bounds__(128) k_propose(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> e_inel,
+                                                 PQ<T> h_inel, const Ctrs* __restrict__ ctr, MlpDev net,
+                                                 float* __restrict__ guess, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char psm[];
+    unsigned char* sA = psm;                          // 128 x 64 BF16 hidden activations
+    unsigned char* sB = psm + 128 * 64 * 2;           // 64 x 64 BF16 weights of one network
+    uint64_t* mbar = (uint64_t*)(sB + 64 * 64 * 2);
+    uint32_t* tslot = (uint32_t*)(mbar + 1);
+    const McConst<T>& C = *Cp;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int n_e = ctr->n_out[Q_EINEL], n_h = ctr->n_out[Q_HINEL], n = n_e + n_h;
+    const int ntiles = (n + 127) / 128;
+    if ((int)blockIdx.x >= ntiles) return;            // the whole CTA, before any TMEM is held
+    if (warp == 0) tc::tmem_alloc(tslot, 64);
+    if (tid == 0) tc::mbar_init(mbar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    constexpr uint32_t idesc = tc::idesc_bf16(128, 64);
+    constexpr long long kWait = 2000000000ll;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int g = tile * 128 + tid;
+        int q = -1;
+        float x0 = 0.f, x1 = 0.f, y = -1.f;
+        if (g < n) {
+            P<T> p;
+            const bool e = g < n_e;
+            if (e) load(e_inel, g, p); else load(h_inel, g - n_e, p);
+            EvStream<T> s(C.seed, p.pid, p.ord);
+            (void)s.next();                                // the draw that chose ionisation
+            const T Eel = e ? p.E : p.Ek;
+            const int k = e ? which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next())
+                            : which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
+            const float u = (float)s.next();
+            q = e ? net.e_net[k] : (k == C.vb ? net.h_net : -1);
+            if (q >= 0) {
+                const float a = (__logf((float)Eel) - net.lo[q]) / (net.hi[q] - net.lo[q]);
+                x0 = fminf(fmaxf(2.f * a - 1.f, -2.f), 2.f);
+                x1 = prop_u_feature(u);
+            }
+        }
+        for (int qq = 0; qq < net.n_nets && ok; ++qq) {
+            if (!__syncthreads_or(q == qq)) continue;
+            const uint4* src = (const uint4*)(net.w2t + (size_t)qq * 4096);
+            for (int i = tid; i < 512; i += 128) ((uint4*)sB)[i] = src[i];
+            const float* sm = net.small + (size_t)qq * kNetSmall;
+            for (int j = 0; j < 64; ++j) {
+                const float h = (q == qq) ? silu_f(fmaf(x0, sm[j], fmaf(x1, sm[64 + j], sm[128 + j]))) : 0.f;
+                *(__nv_bfloat16*)(sA + tc::kmaj_off(tid, j, 64)) = __float2bfloat16_rn(h);
+            }
+            tc::fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB);
+#pragma unroll
+                for (int st = 0; st < 4; ++st)
+                    tc::mma_bf16(tmem, tc::smem_desc(a0 + st * 256, 128, 1024), tc::smem_desc(b0 + st * 256, 128, 1024),
+                                 idesc, st > 0 ? 1u : 0u);
+                tc::mma_commit(mbar);
+            }
+            const int late = __syncthreads_or(tc::mbar_wait(mbar, phase, kWait) ? 0 : 1);
+            if (late) {
+                tc::mbar_wait(mbar, phase, kWait);         // a second bounded wait for the MMA in flight
+                ok = false;
+                break;
+            }
+            phase ^= 1u;
+            tc::fence_after_sync();
+            float acc = sm[320];
+#pragma unroll
+            for (int c = 0; c < 64; c += 16) {
+                float v[16];
+                tc::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) acc = fmaf(sm[256 + c + j], silu_f(v[j] + sm[192 + c + j]), acc);
+            }
+            if (q == qq) y = fminf(fmaxf(acc, 0.f), 1.f);
+            tc::fence_before_sync();
+            __syncthreads();                               // sA, sB and TMEM are reused by the next network
+        }
+        if (g < n) guess[g] = ok ? y : -1.f;
+    }
+    if (!ok && tid == 0) atomicExch(err, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+template <class T>
+void launch_propose(const Proposer& p, const McConst<T>* C, const DevTabs<T>& tb, PQ<T> e_inel, PQ<T> h_inel,
+                    const Ctrs* ctr, cudaStream_t s) {
+    // 24 KB used; asking for 48 KB keeps at most four CTAs (256 TMEM columns) per SM
+    k_propose<T><<<p.blocks, 128, 48 * 1024, s>>>(C, tb, e_inel, h_inel, ctr, p.net, p.guess, p.err);
+}
+template void launch_propose<float>(const Proposer&, const McConst<float>*, const DevTabs<float>&, PQ<float>,
+                                    PQ<float>, const Ctrs*, cudaStream_t);
+template void launch_propose<double>(const Proposer&, const McConst<double>*, const DevTabs<double>&, PQ<double>,
+                                     PQ<double>, const Ctrs*, cudaStream_t);
 
 template <class T>
 void launch_shi(const McConst<T>* C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
@@ -1181,14 +1310,16 @@ size_t shi_event_bytes() { return sizeof(ShiEv); }
 
 template <class T>
 void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
-                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s) {
+                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
+                 const float* guess, const Proposer* prop) {
     Out<T> o{{out.q[0], out.q[1], out.q[2], out.q[3]}, ctr};
     if (n_in[Q_E] > 0)
         k_hot<T, true><<<(n_in[Q_E] + bs - 1) / bs, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
     if (n_in[Q_HVB] > 0)
         k_hot<T, false><<<(n_in[Q_HVB] + bs - 1) / bs, bs, 0, s>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+    if (prop) launch_propose<T>(*prop, C, tb, e_inel, h_inel, ctr, s);
     k_rare<T><<<rare_blocks, 128, 0, s>>>(C, tb, e_inel, h_inel, in.q[Q_HDEEP], n_in[Q_HDEEP], in.q[Q_P],
-                                          n_in[Q_P], o, tal);
+                                          n_in[Q_P], o, tal, prop ? guess : nullptr);
 }
 
 template void launch_shi<float>(const McConst<float>*, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t);
@@ -1198,9 +1329,11 @@ template void launch_pairs<float>(const McConst<float>*, const DevTabs<float>&, 
 template void launch_pairs<double>(const McConst<double>*, const DevTabs<double>&, const void*, int64_t, PQ<double>,
                                    PQ<double>, PQ<double>, Tal, Ctrs*, cudaStream_t);
 template void launch_step<float>(const McConst<float>*, const DevTabs<float>&, const QSet<float>&, const int*,
-                                 const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t);
+                                 const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t,
+                                 const float*, const Proposer*);
 template void launch_step<double>(const McConst<double>*, const DevTabs<double>&, const QSet<double>&, const int*,
-                                  const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t);
+                                  const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t,
+                                  const float*, const Proposer*);
 
 // ---- grid hints ----------------------------------------------------------------------------
 // hint of a bucket = the search result at the bucket's lowest value, which

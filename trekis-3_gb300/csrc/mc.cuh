@@ -103,9 +103,43 @@ struct QSet {   // the four particle queues of one generation
     PQ<T> q[4];
 };
 
+// A trained set of proposal networks on the device (mlp.cu): one per
+// electron shell with transfer rows and one for valence holes.  The hidden
+// layer product runs on the tensor cores; the 2-input layer and the output
+// layer are small enough for the CUDA cores.
+constexpr int MAXNET = MAXSH + 1;
+constexpr int kNetHidden = 64;
+constexpr int kNetSmall = 324;   // per network: W1[2][64], b1[64], b2[64], w3[64], b3 (FP32, padded)
+struct MlpDev {
+    int n_nets = 0;
+    int e_net[MAXSH];            // network of each electron shell, -1 if none
+    int h_net = -1;              // network of valence holes, -1 if none
+    float lo[MAXNET], hi[MAXNET];   // range of log E mapped onto the input [-1, 1]
+    const float* small = nullptr;   // [n_nets][kNetSmall]
+    const uint16_t* w2t = nullptr;  // [n_nets][64 x 64] BF16 hidden weights, tensor-core operand layout
+};
+// Second input of a proposal network: the bracket follows log(L_tot / u), so
+// the uniform enters as -log u compressed onto (-1, 1]
+__host__ __device__ inline float prop_u_feature(float u) {
+    const float t = -logf(u);
+    return 1.f - 2.f * t / (1.f + t);
+}
+
+// What a wavefront step needs to run the proposal before its rare-event kernel
+struct Proposer {
+    MlpDev net;
+    float* guess;    // [side-queue capacity x 2]: bracket fractions, -1 = none
+    int* err;        // set when a bounded tensor-core wait ran out (the guesses then stay -1)
+    int blocks;      // persistent CTAs of the proposal kernel
+};
+template <class T>
+void launch_propose(const Proposer& p, const McConst<T>* C, const DevTabs<T>& tb, PQ<T> e_inel, PQ<T> h_inel,
+                    const Ctrs* ctr, cudaStream_t s);
+
 template <class T>
 void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
-                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s);
+                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
+                 const float* guess = nullptr, const Proposer* prop = nullptr);
 // Bucket hints of the time and radius grids.  A radius bucket is the bit
 // pattern of R without its low mantissa bits (monotone in R, 16 per octave).
 constexpr int kRgHintMax = 4096;

@@ -450,6 +450,10 @@ int check_args(const trekis_tables* t, const trekis_material* mat, const trekis_
     }
     for (int a = 0; a < t->mat.N_atoms; ++a)
         if (t->mat.atoms[a].N_shl > o->Nshl) { set_error("tally shell dimension too small"); return TREKIS_EINVAL; }
+    if (cfg->sampler != 0) {
+        set_error("the no-alloc entry point runs the table sampler only (sampler = 0)");
+        return TREKIS_EUNSUPPORTED;
+    }
     if (o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h) {
         set_error("spectra are not tallied by the no-alloc entry point (their per-iteration histograms would not fit)");
         return TREKIS_EUNSUPPORTED;

@@ -80,8 +80,25 @@ class RunCfg(C.Structure):
         ("N_R", C.c_int32), ("precision", C.c_int32), ("Out_R", C.POINTER(C.c_double)),
         ("seed", C.c_uint64), ("iteration_offset", C.c_int64),
         ("block_size", C.c_int32), ("events_per_step", C.c_int32), ("queue_capacity", C.c_int64),
-        ("iterations_per_batch", C.c_int32), ("use_graph", C.c_int32),
+        ("iterations_per_batch", C.c_int32), ("use_graph", C.c_int32), ("sampler", C.c_int32), ("pad2_", C.c_int32),
     ]
+
+
+class MlpCfg(C.Structure):
+    _fields_ = [
+        ("n_samples", C.c_int64), ("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_double),
+        ("E_lo", C.c_double), ("E_hi", C.c_double), ("seed", C.c_uint64), ("n_eval_E", C.c_int32),
+        ("n_eval_u", C.c_int32),
+    ]
+
+
+class MlpReport(C.Structure):
+    _fields_ = [("n_nets", C.c_int32), ("pad_", C.c_int32)] + [(n, C.c_double) for n in (
+        "train_ms", "tc_gflop", "loss_first", "loss_last", "kl_mean", "kl_max", "accept_rate", "mean_walk",
+        "mean_bisect")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad_"}
 
 
 _DP = C.POINTER(C.c_double)
@@ -136,6 +153,11 @@ SIGNATURES = {
                                          C.POINTER(Tallies), C.POINTER(Status)]),
     "trekis_mc_run_device_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
                                                  C.POINTER(Tallies), C.POINTER(Status), C.c_void_p]),
+    "trekis_tc_gemm_bf16": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.c_int64,
+                                        C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "trekis_mlp_train": (C.c_int32, [C.c_void_p, C.POINTER(MlpCfg), C.POINTER(MlpReport)]),
+    "trekis_mlp_grad": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.POINTER(C.c_double)]),
     "trekis_last_error": (C.c_char_p, []),
 }
 

@@ -106,6 +106,7 @@ class RunOptions:
     queue_capacity: int = 0
     iterations_per_batch: int = 0
     use_graph: int = 0
+    sampler: int = 0            # 0 table inversion, 1 learned proposal + exact correction
 
 
 def run_cfg(w, opt, NMC=None):
@@ -114,7 +115,8 @@ def run_cfg(w, opt, NMC=None):
                      precision=opt.precision, Out_R=abi.dptr(R), seed=opt.seed,
                      iteration_offset=opt.iteration_offset, block_size=opt.block_size,
                      events_per_step=opt.events_per_step, queue_capacity=opt.queue_capacity,
-                     iterations_per_batch=opt.iterations_per_batch, use_graph=opt.use_graph)
+                     iterations_per_batch=opt.iterations_per_batch, use_graph=opt.use_graph,
+                     sampler=opt.sampler)
     return cfg, R
 
 
@@ -181,3 +183,14 @@ def mc_run(tables, opt=None, NMC=None, tallies=None):
                                   C.byref(st))
     abi.check(rc, tables.lib)
     return tal, st
+
+
+def train_proposal(tables, n_samples=1_000_000, epochs=3, batch=8192, lr=2e-3, E_lo=1.0, E_hi=1.0e5, seed=7,
+                   n_eval_E=64, n_eval_u=1024):
+    """Train the learned proposal of the energy-transfer draw on the GPU
+    (trekis_mlp_train); returns the report as a dict."""
+    cfg = abi.MlpCfg(n_samples=n_samples, epochs=epochs, batch=batch, lr=lr, E_lo=E_lo, E_hi=E_hi, seed=seed,
+                     n_eval_E=n_eval_E, n_eval_u=n_eval_u)
+    rep = abi.MlpReport()
+    abi.check(tables.lib.trekis_mlp_train(tables.h, C.byref(cfg), C.byref(rep)), tables.lib)
+    return rep.as_dict()
