@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TREKIS_ABI_VERSION 2
+#define TREKIS_ABI_VERSION 3
 
 #define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
 #define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
@@ -270,6 +270,7 @@ int32_t trekis_tables_export(const trekis_tables* t, int32_t kind, int32_t atom,
 #define TREKIS_ROW_EL_INEL 0   /* aidCS%EIdCS(atom)%Int_diff_CS(shell) */
 #define TREKIS_ROW_H_INEL  1   /* aidCS%HIdCS (valence band)          */
 #define TREKIS_ROW_EL_ELAST 2  /* aidCS%EEdCS (phonon elastic)        */
+#define TREKIS_ROW_H_ELAST  3  /* aidCS%HEdCS (phonon elastic, holes) */
 
 /* Copy the cumulative row at energy node iE: hw[n] and the MFP column dsdhw[n]. */
 int32_t trekis_tables_row(const trekis_tables* t, int32_t kind, int32_t atom,

@@ -53,7 +53,9 @@ int oracle_tables_export(void* t, int kind, int a, int s, double* E, double* L, 
 int oracle_tables_row(void* t, int kind, int a, int s, int iE, double* hw, double* L, int64_t cap, int64_t* n) {
     Tables* T = (Tables*)t;
     const RowSet* R = (kind == TREKIS_ROW_EL_INEL) ? &T->el_rows[a * TREKIS_MAX_SHELLS + s]
-                      : (kind == TREKIS_ROW_H_INEL) ? &T->hole_rows : nullptr;
+                      : (kind == TREKIS_ROW_H_INEL) ? &T->hole_rows
+                      : (kind == TREKIS_ROW_EL_ELAST) ? &T->el_elast_rows
+                      : (kind == TREKIS_ROW_H_ELAST) ? &T->hole_elast_rows : nullptr;
     if (!R || iE < 0 || iE >= (int)R->rows.size()) return TREKIS_EINVAL;
     const Row& r = R->rows[iE];
     *n = (int64_t)r.hw.size();
@@ -76,7 +78,9 @@ int oracle_tables_set(void* t, int kind, int a, int s, const double* E, const do
 int oracle_tables_set_row(void* t, int kind, int a, int s, int iE, const double* hw, const double* L, int64_t n) {
     Tables* T = (Tables*)t;
     RowSet* R = (kind == TREKIS_ROW_EL_INEL) ? &T->el_rows[a * TREKIS_MAX_SHELLS + s]
-                : (kind == TREKIS_ROW_H_INEL) ? &T->hole_rows : nullptr;
+                : (kind == TREKIS_ROW_H_INEL) ? &T->hole_rows
+                : (kind == TREKIS_ROW_EL_ELAST) ? &T->el_elast_rows
+                : (kind == TREKIS_ROW_H_ELAST) ? &T->hole_elast_rows : nullptr;
     if (!R || iE < 0 || iE >= (int)R->rows.size()) return TREKIS_EINVAL;
     R->rows[iE].hw.assign(hw, hw + n);
     R->rows[iE].L.assign(L, L + n);

@@ -64,6 +64,7 @@ struct Tables {
     MFPTab el_elast, hole_elast;
     std::vector<RowSet> el_rows;   // per atom,shell
     RowSet hole_rows;              // valence band only
+    RowSet el_elast_rows, hole_elast_rows;   // phonon-CDF elastic (aidCS%EEdCS, %HEdCS)
     // totals as Monte_Carlo.f90:1902-2057 builds them (E, L)
     MFPTab El_IMFP, El_EMFP, Hole_IMFP, Hole_EMFP, Phot_IMFP, SHI_path;
     bool has_shi = false, has_phot = false;
@@ -92,5 +93,6 @@ double sample_transfer_inelastic(const Tables& T, const trekis_material& m, int 
                                  double Ele, double L_tot, double u, uint32_t* flags);
 double next_free_path_2d(const MFPTab& t, double E);
 double next_free_path_1d(const MFPTab& t, double E);
+double interp_transfer(const RowSet& R, double Ele, double L_need);
 
 }  // namespace orc

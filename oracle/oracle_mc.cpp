@@ -87,7 +87,7 @@ double next_free_path_1d(const MFPTab& t, double E) {
 }
 
 // interpolate_transferred_energy (Cross_sections.f90:1968-2045)
-static double interp_transfer(const RowSet& R, double Ele, double L_need) {
+double interp_transfer(const RowSet& R, double Ele, double L_need) {
     const int NE = (int)R.E.size();
     int iE = find_monoton(R.E.data(), NE, Ele);
     if (iE > 1 && std::fabs(R.E[iE - 2] - Ele) < 1.0e-6) iE -= 1;
@@ -305,6 +305,16 @@ void electron_flight(Ctx& c, P& p, double E, Stream& s) {  // -log(RN)/(1/IMFP+1
 
 // Mott elastic energy transfer averaged over species (Monte_Carlo.f90:2394-2407;
 // Cross_sections.f90:3517-3613)
+// Electron_energy_transfer_elastic with tabulated rows (CS:2285-2428, CS_method 1):
+// L_need = EMFP / RN inverted on the elastic cumulative rows, at most the energy
+double phonon_transfer(const Ctx& c, bool hole, double Eel, Stream& s) {
+    const double EMFP = next_free_path_1d(hole ? c.T->hole_elast : c.T->el_elast, Eel);
+    const double RN = s.next();
+    double hw = interp_transfer(hole ? c.T->hole_elast_rows : c.T->el_elast_rows, Eel, EMFP / RN);
+    if (hw >= Eel) hw = Eel;
+    return hw;
+}
+
 double mott_transfer(const Ctx& c, double Ee, double M_eff, Stream& s) {
     const trekis_material& m = *c.m;
     double dE = 0.0;
@@ -471,8 +481,8 @@ void electron_event(Ctx& c, int NOP, int i) {
         c.el.push_back(ne);
         c.ho.push_back(hh);
         c.cnt[1]++;
-    } else {  // elastic, Mott (kind_of_EMFP = 0)
-        dE = mott_transfer(c, Eel, 1.0, s);
+    } else {  // elastic: Mott (kind_of_EMFP = 0) or phonon CDF (1)
+        dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, false, Eel, s) : mott_transfer(c, Eel, 1.0, s);
         angles_lat(c, Eel, dE, 1.0, s, theta, phi);
         c.At_NRG += dE;
         add_elat(c, i, X, Y, dE);
@@ -562,8 +572,8 @@ void hole_event(Ctx& c, int NOP, int i, double t_cur) {
             c.el.push_back(ne);
             c.ho.push_back(hh);
             c.cnt[3]++;
-        } else {  // elastic, Mott with the hole mass
-            dE = mott_transfer(c, Eel, hmass, s);
+        } else {  // elastic, Mott with the hole mass, or phonon CDF
+            dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, true, Eel, s) : mott_transfer(c, Eel, hmass, s);
             angles_lat(c, Eel, dE, hmass, s, th1, ph1);
             Ehole = check_hole(c, Eel, dE, nullptr);
             c.At_NRG += dE;
@@ -899,7 +909,8 @@ void one_iteration(Ctx& c, int64_t it_global, int sched) {
 int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, const trekis_run_cfg& cfg,
            trekis_tallies& out, trekis_status* st, int nthreads, int sched) {
     if (cfg.dt_flag != 0 && cfg.dt_flag != 1) return TREKIS_EINVAL;
-    if (m.work_function > 0.0 || m.kind_of_EMFP != 0 || ion.Kind_ion != 0) return TREKIS_EUNSUPPORTED;
+    if (m.work_function > 0.0 || m.kind_of_EMFP < 0 || m.kind_of_EMFP > 1 || ion.Kind_ion != 0) return TREKIS_EUNSUPPORTED;
+    if (m.kind_of_EMFP == 1 && T.el_elast_rows.rows.empty()) return TREKIS_EINVAL;
     if (!T.has_shi) return TREKIS_EINVAL;
     if (m.include_photons && !T.has_phot) return TREKIS_EINVAL;
     std::vector<double> tg = time_grid(cfg.Tim, cfg.dt, cfg.dt_flag);

@@ -401,6 +401,107 @@ static void shi_totimfp(const trekis_material& m, const trekis_ion& ion, int a, 
 
 static inline int sidx(int a, int s) { return a * TREKIS_MAX_SHELLS + s; }
 
+// ---- phonon-CDF elastic scattering (kind_of_EMFP = 1) -----------------------------------
+// Imewq_phonon (Cross_sections.f90:3409-3433) with Loss_func's atomic dispersion
+// E0 -> E0 + (hbar q)^2 / (2 Mtarget) (Extend_E0_to_finite_q, CS:357-359)
+static double imewq_phonon(const trekis_material& m, double hw, double hq, double Mtarget) {
+    const double hq2 = h * h * hq * hq, dE2 = hw * hw;
+    double sum = 0.0;
+    for (int i = 0; i < m.N_ph_osc; ++i) {
+        const double E0 = m.ph_E0[i] + hq2 / (2.0 * Mtarget), G = m.ph_Gamma[i], E02 = E0 * E0;
+        sum += m.ph_A[i] * G * hw / ((dE2 - E02) * (dE2 - E02) + G * G * dE2);
+    }
+    return sum;
+}
+
+// Diff_cross_section_phonon (CS:3142-3300) with the unscreened potential 1/q
+// (CDF_elast_Zeff 0 or 1; the target charge enters through Zeff^2 in Tot_EMFP).
+// The q loop is bounded: qmin = 0 (hw below the resolution of sqrt(Ele)) would
+// never end in the reference; it contributes nothing here.
+static double diff_cs_phonon(const trekis_material& m, double Ele, double hw, double Mass, double Mtarget) {
+    const double eps = 1.0e-12, pre = std::sqrt(2.0 * Mass * me) / h;
+    double qmin;
+    if (std::fabs(hw) < eps) return 1.31e30;
+    if (hw > Ele - eps) qmin = pre * std::sqrt(Ele);
+    else qmin = pre * (std::sqrt(Ele) - std::sqrt(std::fabs(Ele - hw)));
+    const double qmax = pre * (std::sqrt(Ele) + std::sqrt(std::fabs(Ele - hw)));
+    double dLs = 0.0, hq = qmin, dLs0 = 0.0;
+    if (!(qmin > 0.0)) return 0.0;
+    for (int it = 0; it < 1000000 && std::fabs(hq) < std::fabs(qmax); ++it) {
+        const double dq = hq / 100.0;
+        const double t1 = imewq_phonon(m, hw, hq + dq / 2.0, Mtarget);
+        const double dL = imewq_phonon(m, hw, hq + dq, Mtarget);
+        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) * (1.0 / hq);
+        dLs0 = dL;
+        hq = hq + dq;
+    }
+    if (m.temp > 1.0e-6) return 1.0 / (Pi * a0 * Ele) * dLs / (1.0 - std::exp(-hw / m.temp * kb));
+    return 1.0 / (Pi * a0 * Ele) * dLs;
+}
+
+// get_E_low (CS:1251-1274)
+static void get_E_low(double lo_b, double hi_b, double Emin, double Emax, double& lo, double& hi) {
+    if (Emin > hi_b || Emax < lo_b) { lo = Emin; hi = Emax; return; }
+    lo = std::max(lo_b, Emin);
+    hi = std::min(hi_b, Emax);
+    if (std::fabs(lo - hi) < 1.0e-3) { lo = Emin; hi = Emax; return; }
+    lo = std::min(lo, hi - (hi_b - lo_b));
+    lo = std::max(lo, Emin);
+}
+
+// Debye_energy (CS:692-702), times 3 as Tot_EMFP uses it
+static double edebye3(const trekis_material& m) {
+    const double qd = std::pow(6.0 * Pi * Pi * (m.At_Dens * 1e6), 0.33333333);
+    return 3.0 * h * m.Vsound * qd / e;
+}
+
+// the target charge the electron sees (Elastic_cross_section, CS:2913-2921)
+static double elastic_zeff(const trekis_material& m, double Ee) {
+    if (m.CDF_elast_Zeff != 0) return 1.0;
+    double zs = 0.0, ps = 0.0;
+    for (int a = 0; a < m.N_atoms; ++a) { zs += m.atoms[a].Zat * m.atoms[a].Pers; ps += m.atoms[a].Pers; }
+    const double Zt = zs / ps, vp = std::sqrt(2.0 * Ee * e / me);
+    return 1.0 + Zt * (1.0 - std::exp(-(vp * 125.0 / cvel / std::pow(Zt, 0.66666666))));
+}
+
+// Tot_EMFP (CS:2966-3139): elastic MFP, dE/dx and the cumulative row
+static void tot_emfp(const trekis_material& m, double Ele, double Mass, double Mtarget, double& Sigma, double& dEdx,
+                     Row* row) {
+    const double Zeff = elastic_zeff(m, Ele);
+    const double Emin = 0.1e-8;
+    double Emax = 4.0 * Ele * Mass * me * Mtarget / ((Mtarget + Mass * me) * (Mtarget + Mass * me));
+    const double Ed = edebye3(m);
+    if (Ed >= Emax) Emax = Ed;
+    if (Ele < Emax) Emax = Ele;
+    double mn = 1e300, mx = -1e300;
+    for (int i = 0; i < m.N_ph_osc; ++i) {
+        mn = std::min(mn, m.ph_E0[i] - 5.0 * m.ph_Gamma[i]);
+        mx = std::max(mx, m.ph_E0[i] + 5.0 * m.ph_Gamma[i]);
+    }
+    double E_low, E_high;
+    get_E_low(mn, mx, Emin, Emax, E_low, E_high);
+    double E = E_low, Ltot1 = 0.0, Ltot0 = diff_cs_phonon(m, Ele, E, Mass, Mtarget), ddEdx = 0.0;
+    std::vector<double> cum;
+    if (row) { row->hw.clear(); row->L.clear(); }
+    while (std::fabs(E) <= std::fabs(Emax)) {
+        const double dE = define_dE(20, E, E_low, E_high, 1.0e-5);
+        const double t1 = diff_cs_phonon(m, Ele, E + dE / 2.0, Mass, Mtarget);
+        const double dL = diff_cs_phonon(m, Ele, E + dE, Mass, Mtarget);
+        const double t2 = std::fabs(dE) / 6.0 * (Ltot0 + 4.0 * t1 + dL);
+        Ltot1 += t2;
+        ddEdx += E * t2;
+        Ltot0 = dL;
+        E = E + dE;
+        if (row) { row->hw.push_back(E); cum.push_back(Ltot1); }
+    }
+    if (Mass < 1.0e-20 || Ltot1 < 1.0e-15) Sigma = 1.0e29;
+    else Sigma = 1.0 / (Zeff * Zeff * Mass * Ltot1);
+    if (Sigma > 1e30) Sigma = 1e30;
+    dEdx = Zeff * Zeff * Mass * ddEdx;
+    if (row)
+        for (double c : cum) row->L.push_back(c < 1.0e-15 ? 1.0e20 : 1.0 / (Zeff * Zeff * Mass * c));
+}
+
 int build_tables(const trekis_material& m, const trekis_ion& ion, const trekis_table_cfg& cfg, Tables& T,
                  int nthreads, int stride) {
 #ifdef _OPENMP
@@ -463,16 +564,32 @@ int build_tables(const trekis_material& m, const trekis_ion& ion, const trekis_t
             t.L[i] = 1.0e8 / (sig * m.At_Dens);
         }
     };
-    if (m.kind_of_EMFP != 0) return TREKIS_EUNSUPPORTED;
-    mott_tab(grid_4CS(m, 0.01, Emax_e), 1.0, T.el_elast);
-    {
+    if (m.kind_of_EMFP == 1) {   // phonon-CDF elastic (Elastic_cross_section CS:2902-2935, Tot_EMFP)
+        if (m.N_ph_osc < 1 || m.CDF_elast_Zeff < 0 || m.CDF_elast_Zeff > 1) return TREKIS_EUNSUPPORTED;
+        double Mt = 0.0;
+        for (int a = 0; a < m.N_atoms; ++a) Mt += m.atoms[a].Mass * m.atoms[a].Pers;
+        const double Mtarget = Mp * Mt / Psum;
+        auto phon = [&](const std::vector<double>& g, bool hole, MFPTab& t, RowSet& R) {
+            t.E = g; t.L.assign(g.size(), 0.0); t.dEdx.assign(g.size(), 0.0);
+            R.E = g; R.rows.assign(g.size(), {});
+#pragma omp parallel for schedule(dynamic)
+            for (int i = 0; i < (int)g.size(); ++i) {
+                double Mass = 1.0;
+                if (hole) Mass = (m.hole_mass >= 0) ? m.hole_mass : m.dos_Eff_m[find_monoton(m.dos_E, m.N_dos, g[i]) - 1];
+                tot_emfp(m, g[i], Mass, Mtarget, t.L[i], t.dEdx[i], &R.rows[i]);
+            }
+        };
+        phon(grid_4CS(m, 0.01, Emax_e), false, T.el_elast, T.el_elast_rows);
+        phon(grid_4CS(m, 0.01, dosmax + 1.0), true, T.hole_elast, T.hole_elast_rows);
+    } else if (m.kind_of_EMFP == 0) {
+        mott_tab(grid_4CS(m, 0.01, Emax_e), 1.0, T.el_elast);
         double hm = m.hole_mass;
         if (hm < 0) hm = 1.0;  // DOS mass varies per energy; restated below when needed
         mott_tab(grid_4CS(m, 0.01, dosmax + 1.0), hm, T.hole_elast);
         if (m.hole_mass < 0)
             for (size_t i = 0; i < T.hole_elast.E.size(); ++i)
                 T.hole_elast.L[i] /= m.dos_Eff_m[find_monoton(m.dos_E, m.N_dos, T.hole_elast.E[i]) - 1];
-    }
+    } else return TREKIS_EUNSUPPORTED;
     // photons (AI:153, All_shells_Photon_MFP AI:2146)
     if (cfg.build_photon && m.include_photons) {
         std::vector<double> gP = grid_4CS(m, 0.1, 175.6e6 * 2.0 / 1836.0);

@@ -54,6 +54,14 @@ def small1(gpu_lib):
     return w, t, _oracle_on(t, w)
 
 
+@pytest.fixture(scope="module")
+def small4(gpu_lib):
+    # SiO2-like target with phonon-CDF elastic scattering, mobile holes, photons
+    w = configs.small(configs.cfg4, NMC=4, Tim=20.0, ion_E=50e6)
+    t = api.Tables(w, lib=gpu_lib)
+    return w, t, _oracle_on(t, w)
+
+
 def _assert_tallies_equal(g, r, what):
     for k in g.a:
         a, b = g[k], r[k]
@@ -63,7 +71,7 @@ def _assert_tallies_equal(g, r, what):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["small0", "small1"])
+@pytest.mark.parametrize("case", ["small0", "small1", "small4"])
 def test_fp64_matches_oracle(case, request):
     w, t, o = request.getfixturevalue(case)
     opt = api.RunOptions(precision=1, seed=11)

@@ -91,3 +91,33 @@ def test_mfp_physical(pair):
             assert np.all(L[E < sh.Ip] >= 1e20)
             above = E > 2 * sh.Ip + 1
             assert np.all(L[above] < 1e20)
+
+
+@pytest.fixture(scope="module")
+def phonon_pair(gpu_lib):
+    """SiO2-like target with phonon-CDF elastic scattering (cfg4's material)."""
+    import oracle_py
+    w = configs.small(configs.cfg4, NMC=1, Tim=20.0, ion_E=50e6)
+    t = api.Tables(w, lib=gpu_lib)
+    tc = abi.TableCfg(build_shi=1, build_photon=1, shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+    o = oracle_py.OracleTables(t.mat, t.ion, tc)
+    return w, t, o
+
+
+@pytest.mark.gpu
+def test_phonon_elastic_tables(phonon_pair):
+    """Tot_EMFP / Diff_cross_section_phonon (Cross_sections.f90:2966-3300):
+    elastic MFP, dE/dx and every cumulative row of electrons and holes."""
+    w, t, o = phonon_pair
+    for tab, row in ((abi.TAB_EL_ELAST, abi.ROW_EL_ELAST), (abi.TAB_H_ELAST, abi.ROW_H_ELAST)):
+        E1, L1, D1 = t.export(tab)
+        E2, L2, D2 = o.export(tab)
+        assert np.array_equal(E1, E2)
+        assert _close(L1, L2) and _close(D1, D2), tab
+        assert np.all(L1 > 0) and np.all(L1 < 1e30)
+        for i in range(len(E1)):
+            hw1, R1 = t.row(row, 0, 0, i)
+            hw2, R2 = o.row(row, 0, 0, i)
+            assert len(hw1) == len(hw2) > 1, (tab, i)
+            assert _close(hw1, hw2, 1e-12) and _close(R1, R2), (tab, i)
+            assert np.all(np.diff(R1) <= 0), (tab, i)

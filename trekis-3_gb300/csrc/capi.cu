@@ -145,6 +145,21 @@ static int upload_mc(trekis_tables* t, DevTabs<T>& d) {
     d.hrow_hw = upload<T>(b, hhw);
     d.hrow_L = upload<T>(b, hL);
     d.hrow_mono = upload_i(b, mono_flags<T>(hoff, hL));
+    // phonon-CDF elastic rows
+    auto rowset = [&](const HRowSet& R, const int*& o, const T*& hwp, const T*& Lp, const int*& mono) {
+        o = nullptr; hwp = Lp = nullptr; mono = nullptr;
+        if (R.rows.empty()) return;
+        std::vector<int> ro(1, 0);
+        std::vector<double> rh, rl;
+        for (const HRow& r : R.rows) {
+            rh.insert(rh.end(), r.hw.begin(), r.hw.end());
+            rl.insert(rl.end(), r.L.begin(), r.L.end());
+            ro.push_back((int)rh.size());
+        }
+        o = upload_i(b, ro); hwp = upload<T>(b, rh); Lp = upload<T>(b, rl); mono = upload_i(b, mono_flags<T>(ro, rl));
+    };
+    rowset(t->el_elast_rows, d.erow_off, d.erow_hw, d.erow_L, d.erow_mono);
+    rowset(t->hole_elast_rows, d.herow_off, d.herow_hw, d.herow_L, d.herow_mono);
     if (t->has_phot) {
         d.nP = (int)t->phot[0].E.size();
         d.pE = upload<T>(b, t->phot[0].E);
@@ -475,6 +490,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     C.mec2 = (T)(kMe * kC * kC / kE);
     C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
     C.dosE = tb.dosE; C.nD = tb.nD;
+    C.elast_cdf = (m.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
     std::vector<double> tg = tallied_times(cfg.Tim, cfg.dt, cfg.dt_flag);
     std::vector<T> tgT(tg.begin(), tg.end()), RgT(cfg.Out_R, cfg.Out_R + cfg.N_R);
     std::vector<double> V(cfg.N_R);
@@ -740,6 +756,8 @@ int32_t trekis_tables_row(const trekis_tables* t, int32_t kind, int32_t a, int32
         if (a < 0 || a >= t->mat.N_atoms || s < 0 || s >= t->mat.atoms[a].N_shl) return TREKIS_EINVAL;
         R = &t->el_rows[t->shell_index[a][s]];
     } else if (kind == TREKIS_ROW_H_INEL) R = &t->hole_rows;
+    else if (kind == TREKIS_ROW_EL_ELAST) R = &t->el_elast_rows;
+    else if (kind == TREKIS_ROW_H_ELAST) R = &t->hole_elast_rows;
     if (!R || iE < 0 || iE >= (int)R->rows.size()) return TREKIS_EINVAL;
     const HRow& r = R->rows[iE];
     *n = (int64_t)r.hw.size();

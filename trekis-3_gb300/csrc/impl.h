@@ -27,6 +27,10 @@ struct BuildMat {
     double E0[MAXSH * MAXOSC], A[MAXSH * MAXOSC], G[MAXSH * MAXOSC];
     const double* dos_k;   // device
     const double* dos_Eff_m;
+    // phonon loss function (elastic kind 1) and the mean target-atom mass [kg]
+    int n_ph;
+    double Mtarget;
+    double phE0[TREKIS_MAX_PH_OSC], phA[TREKIS_MAX_PH_OSC], phG[TREKIS_MAX_PH_OSC];
 };
 
 // A mean-free-path table prepared for the hot loop: logarithms of both
@@ -61,6 +65,9 @@ struct DevTabs {
     const int* hrow_off;   // [nH + 1]
     const T* hrow_hw; const T* hrow_L;
     const int* hrow_mono;  // [nH]
+    // phonon-CDF elastic rows (electrons on elastE, holes on hElastE); null for Mott
+    const int* erow_off; const T* erow_hw; const T* erow_L; const int* erow_mono;
+    const int* herow_off; const T* herow_hw; const T* herow_L; const int* herow_mono;
     // photons
     const T* pE; int nP;
     const T* pL;           // [nsh][nP]
@@ -105,6 +112,7 @@ struct trekis_tables {
     tk::HTab el_elast, hole_elast, El_IMFP, Hole_IMFP, Phot_IMFP, SHI_path;
     std::vector<tk::HRowSet> el_rows;   // per compact shell
     tk::HRowSet hole_rows;
+    tk::HRowSet el_elast_rows, hole_elast_rows;   // phonon-CDF elastic (kind_of_EMFP = 1)
     bool has_shi = false, has_phot = false;
     // device
     tk::Buffers buf;

@@ -556,6 +556,20 @@ __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hol
     return E;
 }
 
+// Electron_energy_transfer_elastic with tabulated rows (CS:2285-2428,
+// CS_method 1): L_need = EMFP / RN (EMFP by Next_free_path_1d) inverted on the
+// phonon-CDF cumulative rows, at most the particle's energy
+template <class T, class S>
+__device__ T phonon_transfer(const DevTabs<T>& tb, bool hole, T Eel, S& s) {
+    const T EMFP = hole ? nfp1(Tab<T>{tb.hElastE, tb.hElastL, tb.nHel}, Eel)
+                        : nfp1(Tab<T>{tb.elastE, tb.elastL, tb.nEl}, Eel);
+    const T L_need = EMFP / s.next();
+    T hw = hole ? interp_transfer(tb.hElastE, tb.nHel, tb.herow_off, tb.herow_hw, tb.herow_L, Eel, L_need)
+                : interp_transfer(tb.elastE, tb.nEl, tb.erow_off, tb.erow_hw, tb.erow_L, Eel, L_need);
+    if (hw >= Eel) hw = Eel;
+    return hw;
+}
+
 // a hole created at (X,Y,Z) with random angles (Update_holes_angles_SHI, MC:1132-1140)
 template <class T, class S>
 __device__ void make_hole(const McConst<T>& C, const DevTabs<T>& tb, P<T>& hh, T t0, T X, T Y, T Z, int k, T Eh,
@@ -861,8 +875,8 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         emit_electron(C, tal, ne, ti0); push(C, tal, o, 0, ne);
         emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
         nev[1]++; nev[7] += 2;
-    } else {  // elastic (Mott)
-        dE = mott_transfer(C, Eel, T(1), s);
+    } else {  // elastic: Mott, or the phonon CDF
+        dE = C.elast_cdf ? phonon_transfer(tb, false, Eel, s) : mott_transfer(C, Eel, T(1), s);
         angles_lat(C, Eel, dE, T(1), s, theta, phi);
         const int i = ti0;  // the interval t_{i-1} <= t < t_i
         const int j = rbin(C, m_sqrt(X * X + Y * Y));
@@ -962,7 +976,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
             nev[3]++; nev[7] += 2;
         } else {
-            dE = mott_transfer(C, Eel, hm, s);
+            dE = C.elast_cdf ? phonon_transfer(tb, true, Eel, s) : mott_transfer(C, Eel, hm, s);
             angles_lat(C, Eel, dE, hm, s, th1, ph1);
             Eh = check_hole(tb, Eel, dE, (P<T>*)nullptr);
             const int i = ti0;

@@ -39,6 +39,7 @@ struct McConst {
     T mec2, alpha;      // electron rest energy [eV], fine-structure constant
     const T* dosE;      // DOS energies (the valence-hole spectrum's bins)
     int nD;
+    int elast_cdf;      // 1: phonon-CDF elastic transfers from the rows, 0: Mott
 };
 
 // Structure-of-arrays particle queue.

@@ -314,6 +314,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     fill_const<T>(t, cfg, Nt, C);
     C.tg = L.tg; C.Rg = L.Rg;
     C.dosE = tb.dosE; C.nD = tb.nD;
+    C.elast_cdf = (t->mat.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
     {
         T first = T(0), last = T(0);
         walk_times(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int i, double x) { if (i == 0) first = (T)x; last = (T)x; });

@@ -24,7 +24,8 @@ namespace tk {
 
 struct Job {
     double Ele, Emin, Emax, Mass, E_low, E_high, Zeff;
-    int sh, kind, n, store;     // kind 0: electron/hole, 1: SHI
+    double E_start, dmin;       // first abscissa and smallest step of the hbar-omega grid
+    int sh, kind, n, store;     // kind 0: electron/hole, 1: SHI, 2: phonon-CDF elastic
     int n_steps, nsiz;
     int64_t pt_off, row_off;
     int row_len;
@@ -81,6 +82,40 @@ __device__ double d_diff_cs(const BuildMat* __restrict__ bm, int sh, double Ele,
     return 1.0 / (kPi * kA0 * Ele) * dLs * T;
 }
 
+// Imewq_phonon (Cross_sections.f90:3409-3433): phonon oscillators with the
+// atomic dispersion E0 + (hbar q)^2 / (2 Mtarget) (Extend_E0_to_finite_q, CS:357-359)
+__device__ double d_imewq_phonon(const BuildMat* __restrict__ bm, double hw, double hq) {
+    const double hq2 = kH * kH * hq * hq, dE2 = hw * hw;
+    double sum = 0.0;
+    for (int i = 0; i < bm->n_ph; ++i) {
+        const double E0 = bm->phE0[i] + hq2 / (2.0 * bm->Mtarget), G = bm->phG[i], E02 = E0 * E0;
+        sum += bm->phA[i] * G * hw / ((dE2 - E02) * (dE2 - E02) + G * G * dE2);
+    }
+    return sum;
+}
+
+// Diff_cross_section_phonon (Cross_sections.f90:3142-3300) with the
+// unscreened potential 1/q (CDF_elast_Zeff 0 or 1).  The q loop is bounded;
+// qmin = 0 (hw below the resolution of sqrt(Ele)) contributes nothing.
+__device__ double d_phonon_diff(const BuildMat* __restrict__ bm, double Ele, double hw, double Mass) {
+    const double eps = 1.0e-12, pre = sqrt(2.0 * Mass * kMe) / kH;
+    if (fabs(hw) < eps) return 1.31e30;
+    const double qmin = (hw > Ele - eps) ? pre * sqrt(Ele) : pre * (sqrt(Ele) - sqrt(fabs(Ele - hw)));
+    const double qmax = pre * (sqrt(Ele) + sqrt(fabs(Ele - hw)));
+    if (!(qmin > 0.0)) return 0.0;
+    double dLs = 0.0, hq = qmin, dLs0 = 0.0;
+    for (int it = 0; it < 1000000 && fabs(hq) < fabs(qmax); ++it) {
+        const double dq = hq / 100.0;
+        const double t1 = d_imewq_phonon(bm, hw, hq + dq / 2.0);
+        const double dL = d_imewq_phonon(bm, hw, hq + dq);
+        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) * (1.0 / hq);
+        dLs0 = dL;
+        hq = hq + dq;
+    }
+    if (bm->temp > 1.0e-6) return 1.0 / (kPi * kA0 * Ele) * dLs / (1.0 - exp(-hw / bm->temp * kKb));
+    return 1.0 / (kPi * kA0 * Ele) * dLs;
+}
+
 // SHI_Diff_cross_section (Cross_sections.f90:2683-2744)
 __device__ double d_shi_diff(const BuildMat* __restrict__ bm, int sh, double Ele, double MSHI, double Emax, double hw) {
     double qmin = (Ele > 0.0) ? hw / kH / sqrt(2.0 * Ele / MSHI) : 0.0;
@@ -104,10 +139,11 @@ __global__ void k_count(Job* jobs, int nj) {
     if (j >= nj) return;
     Job& J = jobs[j];
     int c = 0;
-    for (double E = J.Emin; E <= J.Emax;) { ++c; E = E + d_define_dE(J.n, E, J.E_low, J.E_high, 0.001); }
-    int s = 0;   // get_diff_CS_grid_size (Cross_sections.f90:1278): steps counted from E_low
-    for (double E = J.E_low; E <= J.Emax;) { ++s; E = E + d_define_dE(J.n, E, J.E_low, J.E_high, 0.001); }
+    for (double E = J.E_start; E <= J.Emax;) { ++c; E = E + d_define_dE(J.n, E, J.E_low, J.E_high, J.dmin); }
     J.n_steps = c;
+    if (J.kind == 2) { J.nsiz = c; return; }   // the elastic rows are sized from E_low too (CS:1206-1216)
+    int s = 0;   // get_diff_CS_grid_size (Cross_sections.f90:1278): steps counted from E_low
+    for (double E = J.E_low; E <= J.Emax;) { ++s; E = E + d_define_dE(J.n, E, J.E_low, J.E_high, J.dmin); }
     J.nsiz = s > 10 ? s : 10;
 }
 
@@ -116,10 +152,10 @@ __global__ void k_points(const Job* __restrict__ jobs, int nj, double* __restric
     if (j >= nj) return;
     const Job J = jobs[j];
     int64_t p = J.pt_off;
-    pts[p] = J.Emin; pjob[p] = j; ++p;
-    double E = J.Emin;
+    pts[p] = J.E_start; pjob[p] = j; ++p;
+    double E = J.E_start;
     for (int i = 0; i < J.n_steps; ++i) {
-        double dE = d_define_dE(J.n, E, J.E_low, J.E_high, 0.001);
+        double dE = d_define_dE(J.n, E, J.E_low, J.E_high, J.dmin);
         pts[p] = E + dE / 2.0; pjob[p] = j; ++p;
         pts[p] = E + dE; pjob[p] = j; ++p;
         E = E + dE;
@@ -132,7 +168,8 @@ __global__ void k_diff(const BuildMat* __restrict__ bm, const Job* __restrict__ 
     if (p >= np) return;
     const Job& J = jobs[pjob[p]];
     val[p] = (J.kind == 0) ? d_diff_cs(bm, J.sh, J.Ele, pts[p], J.Mass)
-                           : d_shi_diff(bm, J.sh, J.Ele, J.Mass, J.Emax, pts[p]);
+           : (J.kind == 1) ? d_shi_diff(bm, J.sh, J.Ele, J.Mass, J.Emax, pts[p])
+                           : d_phonon_diff(bm, J.Ele, pts[p], J.Mass);
 }
 
 // Simpson accumulation in the reference's order; writes (Sigma, dEdx) and rows
@@ -143,21 +180,30 @@ __global__ void k_accum(const Job* __restrict__ jobs, int nj, const double* __re
     if (j >= nj) return;
     const Job J = jobs[j];
     const double* v = val + J.pt_off;
-    double Ltot0 = v[0], Ltot1 = 0.0, dd = 0.0, E = J.Emin;
+    double Ltot0 = v[0], Ltot1 = 0.0, dd = 0.0, E = J.E_start;
     const double pref = kPi * kA0 * J.Ele * kMe / (J.Mass * J.Zeff * J.Zeff);
     for (int i = 0; i < J.n_steps; ++i) {
-        double dE = d_define_dE(J.n, E, J.E_low, J.E_high, 0.001);
+        double dE = d_define_dE(J.n, E, J.E_low, J.E_high, J.dmin);
         double t1 = v[1 + 2 * i], dL = v[2 + 2 * i];
-        double t2 = dE / 6.0 * (Ltot0 + 4.0 * t1 + dL);
+        double t2 = fabs(dE) / 6.0 * (Ltot0 + 4.0 * t1 + dL);
         Ltot1 += t2;
-        if (J.kind == 0) dd += E * t2;
+        if (J.kind != 1) dd += E * t2;
         else dd += dE / 6.0 * (E * Ltot0 + (E + dE / 2.0) * 4.0 * t1 + (E + dE) * dL);
         Ltot0 = dL;
         if (J.store == 1) { rhw[J.row_off + i] = E + dE; rL[J.row_off + i] = Ltot1; }
         if (J.store == 2) { rhw[J.row_off + i] = E; rL[J.row_off + i] = pref / Ltot1; rX[J.row_off + i] = pref / dd; }
         E = E + dE;
     }
-    if (J.kind == 0) {
+    if (J.kind == 2) {   // Tot_EMFP (CS:3096-3136): MFP and rows scaled by Zeff^2 Mass
+        const double zz = J.Zeff * J.Zeff * J.Mass;
+        double sg = (J.Mass < 1.0e-20 || Ltot1 < 1.0e-15) ? 1.0e29 : 1.0 / (zz * Ltot1);
+        sig[j] = sg > 1e30 ? 1e30 : sg;
+        dedx[j] = zz * dd;
+        for (int i = 0; i < J.row_len; ++i) {
+            const double c = rL[J.row_off + i];
+            rL[J.row_off + i] = (c < 1.0e-15) ? 1.0e20 : 1.0 / (zz * c);
+        }
+    } else if (J.kind == 0) {
         if (Ltot1 < 1.0e-15) { sig[j] = 1.0e20; dedx[j] = 0.0; }
         else { sig[j] = 1.0 / (J.Mass * Ltot1); dedx[j] = J.Mass * dd; }
         if (J.store == 1) {
@@ -268,7 +314,7 @@ static void limits_eh(const trekis_tables* T, int a, int s, double Ele, bool hol
     }
     J.Ele = Ele; J.Emin = Emin; J.Emax = Emax; J.Mass = Mass;
     J.E_low = std::max(mn, Emin); J.E_high = std::min(mx, Emax);
-    J.kind = 0; J.n = 100; J.Zeff = 1.0;
+    J.kind = 0; J.n = 100; J.Zeff = 1.0; J.E_start = Emin; J.dmin = 0.001;
 }
 
 static void limits_shi(const trekis_tables* T, int a, int s, double Ele, Job& J) {
@@ -288,7 +334,45 @@ static void limits_shi(const trekis_tables* T, int a, int s, double Ele, Job& J)
     }
     J.Ele = Ele; J.Emin = Emin; J.Emax = Emax; J.Mass = MSHI;
     J.E_low = std::max(mn, Emin); J.E_high = std::min(mx, Emax);
-    J.kind = 1; J.n = 1000; J.Zeff = zeff_of(T->ion, m, Ele);
+    J.kind = 1; J.n = 1000; J.Zeff = zeff_of(T->ion, m, Ele); J.E_start = Emin; J.dmin = 0.001;
+}
+
+// Phonon-CDF elastic job (Tot_EMFP, Cross_sections.f90:2966-3060): the
+// hbar-omega grid starts at E_low of get_E_low (CS:1251-1274) with steps of at
+// least 1e-5 eV, n = 20; the target charge of Elastic_cross_section
+// (CS:2913-2921) and 3 x the Debye energy (CS:692-702) as in Tot_EMFP.
+static void limits_phonon(const trekis_tables* T, double Ele, bool hole, Job& J) {
+    const trekis_material& m = T->mat;
+    double Mass = 1.0;
+    if (hole) Mass = (m.hole_mass >= 0) ? m.hole_mass
+                   : T->dos_M[find_mono_h(T->dos_E.data(), (int)T->dos_E.size(), Ele) - 1];
+    double Mt = 0.0, Ps = 0.0, zs = 0.0;
+    for (int a = 0; a < m.N_atoms; ++a) { Mt += m.atoms[a].Mass * m.atoms[a].Pers; Ps += m.atoms[a].Pers; zs += m.atoms[a].Zat * m.atoms[a].Pers; }
+    const double Mtarget = kMp * Mt / Ps;
+    const double Emin = 0.1e-8;
+    double Emax = 4.0 * Ele * Mass * kMe * Mtarget / ((Mtarget + Mass * kMe) * (Mtarget + Mass * kMe));
+    const double Ed = 3.0 * kH * m.Vsound * std::pow(6.0 * kPi * kPi * (m.At_Dens * 1e6), 0.33333333) / kE;
+    if (Ed >= Emax) Emax = Ed;
+    if (Ele < Emax) Emax = Ele;
+    double lo_b = 1e300, hi_b = -1e300;
+    for (int i = 0; i < m.N_ph_osc; ++i) {
+        lo_b = std::min(lo_b, m.ph_E0[i] - 5.0 * m.ph_Gamma[i]);
+        hi_b = std::max(hi_b, m.ph_E0[i] + 5.0 * m.ph_Gamma[i]);
+    }
+    double lo, hi;
+    if (Emin > hi_b || Emax < lo_b) { lo = Emin; hi = Emax; }
+    else {
+        lo = std::max(lo_b, Emin); hi = std::min(hi_b, Emax);
+        if (std::fabs(lo - hi) < 1.0e-3) { lo = Emin; hi = Emax; }
+        else { lo = std::min(lo, hi - (hi_b - lo_b)); lo = std::max(lo, Emin); }
+    }
+    double Zeff = 1.0;
+    if (m.CDF_elast_Zeff == 0) {
+        const double Zt = zs / Ps, vp = std::sqrt(2.0 * Ele * kE / kMe);
+        Zeff = 1.0 + Zt * (1.0 - std::exp(-(vp * 125.0 / kC / std::pow(Zt, 0.66666666))));
+    }
+    J.Ele = Ele; J.Emin = Emin; J.Emax = Emax; J.Mass = Mass; J.E_low = lo; J.E_high = hi;
+    J.kind = 2; J.n = 20; J.Zeff = Zeff; J.E_start = lo; J.dmin = 1.0e-5; J.sh = 0; J.store = 1;
 }
 
 // Mott atomic elastic cross section [cm^2] (Cross_sections.f90:3495-3514)
@@ -315,6 +399,13 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     BuildMat bm;
     std::memset(&bm, 0, sizeof bm);
     bm.nsh = nsh; bm.kind_of_DR = m.kind_of_DR; bm.El_eff_mass = m.El_eff_mass; bm.v_f = m.v_f; bm.temp = m.temp;
+    {
+        double Mt = 0.0, Ps = 0.0;
+        for (int a = 0; a < m.N_atoms; ++a) { Mt += m.atoms[a].Mass * m.atoms[a].Pers; Ps += m.atoms[a].Pers; }
+        bm.Mtarget = kMp * Mt / Ps;
+        bm.n_ph = std::min(std::max(m.N_ph_osc, 0), TREKIS_MAX_PH_OSC);
+        for (int i = 0; i < bm.n_ph; ++i) { bm.phE0[i] = m.ph_E0[i]; bm.phA[i] = m.ph_A[i]; bm.phG[i] = m.ph_Gamma[i]; }
+    }
     const bool metal = m.atoms[0].Ip[m.atoms[0].N_shl - 1] < 0.2;
     bm.dos_mass = (m.El_eff_mass == 0.0 && m.N_dos > 0 && !metal) ? 1 : 0;
     bm.N_dos = m.N_dos;
@@ -381,6 +472,22 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     const size_t j_d0 = jobs.size();
     if (cfg.build_shi)
         for (int k = 0; k < nsh; ++k) { Job J{}; limits_shi(T, T->atom_of[k], T->shell_of[k], T->ion.E, J); J.sh = k; J.store = 2; jobs.push_back(J); }
+    // phonon-CDF elastic (kind_of_EMFP = 1) on the elastic grids (Analytical_IMFPs.f90:210)
+    const size_t j_el0 = jobs.size();
+    std::vector<double> gEl, gHel;
+    if (m.kind_of_EMFP == 1) {
+        if (m.N_ph_osc < 1 || m.CDF_elast_Zeff < 0 || m.CDF_elast_Zeff > 1) {
+            set_error("phonon-CDF elastic needs phonon oscillators and CDF_elast_Zeff 0 or 1");
+            return TREKIS_EUNSUPPORTED;
+        }
+        gEl = grid_4CS(m, 0.01, Emax_e);
+        gHel = grid_4CS(m, 0.01, dosmax + 1.0);
+        for (double E : gEl) { Job J{}; limits_phonon(T, E, false, J); jobs.push_back(J); }
+        for (double E : gHel) { Job J{}; limits_phonon(T, E, true, J); jobs.push_back(J); }
+    } else if (m.kind_of_EMFP != 0) {
+        set_error("elastic kind not supported");
+        return TREKIS_EUNSUPPORTED;
+    }
     const int nj = (int)jobs.size();
 
     Job* d_jobs = (Job*)T->buf.alloc(sizeof(Job) * nj);
@@ -474,8 +581,22 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
         }
         T->has_shi = true;
     }
+    // phonon-CDF elastic MFPs and rows
+    auto phon = [&](const std::vector<double>& g, size_t j0, HTab& t, HRowSet& R) {
+        t.E = g; t.L.resize(g.size()); t.dEdx.resize(g.size());
+        R.E = g; R.rows.assign(g.size(), {});
+        for (size_t i = 0; i < g.size(); ++i) {
+            const Job& J = jobs[j0 + i];
+            t.L[i] = sig[j0 + i]; t.dEdx[i] = ded[j0 + i];
+            R.rows[i].hw.assign(rhw.begin() + J.row_off, rhw.begin() + J.row_off + J.row_len);
+            R.rows[i].L.assign(rL.begin() + J.row_off, rL.begin() + J.row_off + J.row_len);
+        }
+    };
+    if (m.kind_of_EMFP == 1) {
+        phon(gEl, j_el0, T->el_elast, T->el_elast_rows);
+        phon(gHel, j_el0 + gEl.size(), T->hole_elast, T->hole_elast_rows);
+    }
     // elastic Mott MFPs (Elastic_cross_section, Cross_sections.f90:2939-2962): closed form
-    if (m.kind_of_EMFP != 0) { set_error("only the Mott elastic cross section is built"); return TREKIS_EUNSUPPORTED; }
     double Psum = 0.0;
     for (int a = 0; a < m.N_atoms; ++a) Psum += m.atoms[a].Pers;
     auto mott = [&](const std::vector<double>& g, bool hole, HTab& t) {
@@ -490,8 +611,10 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
             t.L[i] = 1.0e8 / (sgm * m.At_Dens);
         }
     };
-    mott(grid_4CS(m, 0.01, Emax_e), false, T->el_elast);
-    mott(grid_4CS(m, 0.01, dosmax + 1.0), true, T->hole_elast);
+    if (m.kind_of_EMFP == 0) {
+        mott(grid_4CS(m, 0.01, Emax_e), false, T->el_elast);
+        mott(grid_4CS(m, 0.01, dosmax + 1.0), true, T->hole_elast);
+    }
     // photons (Tot_Phot_IMFP, Cross_sections.f90:833-878): Im(-1/eps) at q = 0
     if (cfg.build_photon && m.include_photons) {
         std::vector<double> gP = grid_4CS(m, 0.1, Emax_e);

@@ -14,7 +14,7 @@ MAX_OSC = 16
 MAX_PH_OSC = 8
 
 TAB_EL_INEL, TAB_EL_ELAST, TAB_H_INEL, TAB_H_ELAST, TAB_PHOT, TAB_SHI, TAB_SHI_DSDE = range(7)
-ROW_EL_INEL, ROW_H_INEL, ROW_EL_ELAST = range(3)
+ROW_EL_INEL, ROW_H_INEL, ROW_EL_ELAST, ROW_H_ELAST = range(4)
 
 NOALLOC_SCRATCH_BYTES = 64 << 20   # TREKIS_NOALLOC_SCRATCH_BYTES
 
