@@ -272,6 +272,11 @@ int32_t trekis_tables_export(const trekis_tables* t, int32_t kind, int32_t atom,
 #define TREKIS_ROW_EL_ELAST 2  /* aidCS%EEdCS (phonon elastic)        */
 #define TREKIS_ROW_H_ELAST  3  /* aidCS%HEdCS (phonon elastic, holes) */
 
+/* Release the device workspace (particle queues, int64 tallies) a table set
+ * keeps between runs; the next run allocates it again.  For callers holding
+ * many table sets at once. */
+void trekis_tables_trim(trekis_tables* t);
+
 /* Copy the cumulative row at energy node iE: hw[n] and the MFP column dsdhw[n]. */
 int32_t trekis_tables_row(const trekis_tables* t, int32_t kind, int32_t atom,
                           int32_t shell, int32_t iE, double* hw, double* dsdhw,
@@ -336,6 +341,41 @@ int32_t trekis_mc_run_device_noalloc(const trekis_tables* t, const trekis_materi
                                      const trekis_ion* ion, const trekis_run_cfg* cfg,
                                      trekis_tallies* dev_out, trekis_status* st,
                                      void* stream);
+
+/* ---- many instances on one GPU (no counterpart in the reference) ----------
+ * Runs n independent track-loop calls (each one what trekis_mc_run does with
+ * tables[i], mats[i], ions[i], cfgs[i] into the host tallies[i]) with up to
+ * max_concurrent of them in flight on their own CUDA streams, so instances
+ * of very different cascade size share the GPU.  Instances that share a
+ * table handle run one after the other.  Every table set's workspace is
+ * allocated before the runs with an even share of device_budget (<= 0: three
+ * quarters of the free device memory) unless its cfg sets queue_capacity,
+ * and released at the end (trekis_tables_trim).  With autotune, the largest
+ * instance of each material (among those without their own events_per_step)
+ * first runs one probe iteration per candidate events_per_step (16, 32, 64)
+ * and all instances of that material take the fastest; the choices land in
+ * tune[i] (may be NULL).  Returns the first instance's error, if any. */
+typedef struct {
+    int32_t max_concurrent;   /* 0: 16 */
+    int32_t autotune;
+    int64_t device_budget;    /* bytes */
+} trekis_batch_cfg;
+
+typedef struct {
+    int32_t events_per_step;
+    int32_t block_size;
+    int64_t queue_capacity;   /* the workspace's share of the budget            */
+    int64_t needed_capacity;  /* twice the live-particle peak of a 256-iteration
+                                 batch, as the probes measured it (0: no probe) */
+    double  probe_ms;         /* wall time of the probe runs */
+    double  run_ms;           /* wall time of the instance's run */
+} trekis_tune;
+
+int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables,
+                            const trekis_material* const* mats, const trekis_ion* const* ions,
+                            const trekis_run_cfg* cfgs, trekis_tallies* tallies,
+                            trekis_status* status, const trekis_batch_cfg* bcfg,
+                            trekis_tune* tune);
 
 /* ---- learned proposal (no counterpart in the reference) -------------------
  * The tensor-core product the proposal network trains and runs with:

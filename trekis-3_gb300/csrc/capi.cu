@@ -371,7 +371,7 @@ static uint64_t ws_key(int prec, int64_t cap, int Nt, int NR, int Nat, int Nshl,
 template <class T>
 static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, bool spec,
                             int* rc) {
-    const int64_t cap = cfg.queue_capacity > 0 ? cfg.queue_capacity : (int64_t)(sizeof(T) == 4 ? 24 : 12) << 20;
+    const int64_t cap = cfg.queue_capacity > 0 ? cfg.queue_capacity : (int64_t)(sizeof(T) == 4 ? 8 : 4) << 20;
     const uint64_t key = ws_key(sizeof(T), cap, Nt, cfg.N_R, Nat, Nshl, spec);
     if (t->ws && t->ws_key == key) { *rc = 0; return (Workspace<T>*)t->ws.get(); }
     t->ws.reset();
@@ -714,6 +714,10 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
 }
 
 void trekis_tables_free(trekis_tables* t) { delete t; }
+
+void trekis_tables_trim(trekis_tables* t) {
+    if (t) { t->ws.reset(); t->ws_key = 0; }
+}
 
 static const HTab* tab_of(const trekis_tables* t, int kind, int a, int s) {
     if (!t || a < 0 || a >= t->mat.N_atoms || s < 0 || s >= t->mat.atoms[a].N_shl) return nullptr;

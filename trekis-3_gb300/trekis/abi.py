@@ -84,6 +84,15 @@ class RunCfg(C.Structure):
     ]
 
 
+class BatchCfg(C.Structure):
+    _fields_ = [("max_concurrent", C.c_int32), ("autotune", C.c_int32), ("device_budget", C.c_int64)]
+
+
+class Tune(C.Structure):
+    _fields_ = [("events_per_step", C.c_int32), ("block_size", C.c_int32), ("queue_capacity", C.c_int64),
+                ("needed_capacity", C.c_int64), ("probe_ms", C.c_double), ("run_ms", C.c_double)]
+
+
 class MlpCfg(C.Structure):
     _fields_ = [
         ("n_samples", C.c_int64), ("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_double),
@@ -143,6 +152,7 @@ SIGNATURES = {
     "trekis_tables_build": (C.c_int32, [C.POINTER(Material), C.POINTER(Ion), C.POINTER(TableCfg),
                                         C.POINTER(C.c_void_p), C.POINTER(Status)]),
     "trekis_tables_free": (None, [C.c_void_p]),
+    "trekis_tables_trim": (None, [C.c_void_p]),
     "trekis_tables_size": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
     "trekis_tables_export": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _DP, _DP, _DP, C.c_int64]),
     "trekis_tables_row": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _DP, _DP,
@@ -155,6 +165,9 @@ SIGNATURES = {
                                                  C.POINTER(Tallies), C.POINTER(Status), C.c_void_p]),
     "trekis_tc_gemm_bf16": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.c_int64,
                                         C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
+    "trekis_mc_run_batch": (C.c_int32, [C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                        C.POINTER(C.c_void_p), C.POINTER(RunCfg), C.POINTER(Tallies),
+                                        C.POINTER(Status), C.POINTER(BatchCfg), C.POINTER(Tune)]),
     "trekis_mlp_train": (C.c_int32, [C.c_void_p, C.POINTER(MlpCfg), C.POINTER(MlpReport)]),
     "trekis_mlp_grad": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.POINTER(C.c_double)]),

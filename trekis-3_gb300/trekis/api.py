@@ -194,3 +194,30 @@ def train_proposal(tables, n_samples=1_000_000, epochs=3, batch=8192, lr=2e-3, E
     rep = abi.MlpReport()
     abi.check(tables.lib.trekis_mlp_train(tables.h, C.byref(cfg), C.byref(rep)), tables.lib)
     return rep.as_dict()
+
+
+def mc_run_batch(tables_list, opts, tallies_list=None, autotune=True, max_concurrent=0, device_budget=0):
+    """Run many instances at once (trekis_mc_run_batch); returns
+    (tallies list, status list, tune list as dicts)."""
+    n = len(tables_list)
+    lib = tables_list[0].lib
+    tallies_list = tallies_list or [new_tallies(t.w) for t in tables_list]
+    cfgs = (abi.RunCfg * n)()
+    keep = []
+    for i, (t, opt) in enumerate(zip(tables_list, opts)):
+        cfg, R = run_cfg(t.w, opt)
+        cfgs[i] = cfg
+        keep.append(R)
+    tabs = (C.c_void_p * n)(*[t.h.value for t in tables_list])
+    mats = (C.c_void_p * n)(*[C.addressof(t.mat.struct) for t in tables_list])
+    ions = (C.c_void_p * n)(*[C.addressof(t.ion) for t in tables_list])
+    cts = (abi.Tallies * n)(*[tl.c() for tl in tallies_list])
+    sts = (abi.Status * n)()
+    for s_ in sts:
+        s_.first_offender = -1
+    tunes = (abi.Tune * n)()
+    bc = abi.BatchCfg(max_concurrent=max_concurrent, autotune=int(autotune), device_budget=device_budget)
+    rc = lib.trekis_mc_run_batch(n, tabs, mats, ions, cfgs, cts, sts, C.byref(bc), tunes)
+    abi.check(rc, lib)
+    tune = [{f: getattr(tu, f) for f, _ in abi.Tune._fields_} for tu in tunes]
+    return tallies_list, list(sts), tune

@@ -161,3 +161,82 @@ def small(cfg_fn=cfg0, **kw):
     args = dict(layer=5.0, Tim=20.0, NMC=8, ion_E=20e6)
     args.update(kw)
     return cfg_fn(**args)
+
+
+# ---- cfg2: many instances of uneven cascade size --------------------------------------
+# standard atomic weights [u] of Z = 1..92 (the ion masses of the synthetic instances)
+ATOMIC_WEIGHT = [
+    1.008, 4.003, 6.94, 9.012, 10.81, 12.011, 14.007, 15.999, 18.998, 20.180, 22.990, 24.305, 26.982, 28.085,
+    30.974, 32.06, 35.45, 39.948, 39.098, 40.078, 44.956, 47.867, 50.942, 51.996, 54.938, 55.845, 58.933,
+    58.693, 63.546, 65.38, 69.723, 72.630, 74.922, 78.971, 79.904, 83.798, 85.468, 87.62, 88.906, 91.224,
+    92.906, 95.95, 98.0, 101.07, 102.906, 106.42, 107.868, 112.414, 114.818, 118.710, 121.760, 127.60,
+    126.904, 131.293, 132.905, 137.327, 138.905, 140.116, 140.908, 144.242, 145.0, 150.36, 151.964, 157.25,
+    158.925, 162.500, 164.930, 167.259, 168.934, 173.045, 174.967, 178.49, 180.948, 183.84, 186.207, 190.23,
+    192.217, 195.084, 196.967, 200.592, 204.38, 207.2, 208.980, 209.0, 210.0, 222.0, 223.0, 226.0, 227.0,
+    232.038, 231.036, 238.029]
+
+# target elements of the synthetic materials: Z, core levels [(Ip eV, electrons, designator)], valence electrons
+_ELEMENTS = {
+    3: ([(54.7, 2.0, 1)], 1), 6: ([(284.2, 2.0, 1)], 4), 7: ([(409.9, 2.0, 1)], 5), 8: ([(543.1, 2.0, 1)], 6),
+    9: ([(696.7, 2.0, 1)], 7), 11: ([(1070.8, 2.0, 1), (63.5, 2.0, 2), (30.65, 6.0, 4)], 1),
+    12: ([(1303.0, 2.0, 1), (88.7, 2.0, 2), (49.8, 6.0, 4)], 2),
+    13: ([(1559.0, 2.0, 1), (117.8, 2.0, 2), (72.9, 6.0, 4)], 3),
+    14: ([(1839.0, 2.0, 1), (149.7, 2.0, 2), (99.8, 6.0, 4)], 4),
+    15: ([(2145.5, 2.0, 1), (189.0, 2.0, 2), (136.0, 6.0, 4)], 5),
+    16: ([(2472.0, 2.0, 1), (230.9, 2.0, 2), (163.6, 6.0, 4)], 6),
+    20: ([(4038.5, 2.0, 1), (438.4, 2.0, 2), (346.2, 6.0, 4), (44.3, 2.0, 5), (25.4, 6.0, 6)], 2),
+}
+
+
+def synthetic_material(rng, n_elements, Layer):
+    """A seeded target of 1-3 elements with 2-8 shells and 1-6 valence oscillators."""
+    while True:
+        zs = list(rng.choice(sorted(_ELEMENTS), size=n_elements, replace=False))
+        pers = [float(rng.integers(1, 4)) for _ in zs]
+        shells = []
+        for z in zs:
+            cores = _ELEMENTS[int(z)][0]
+            k = int(rng.integers(1, len(cores) + 1))
+            shells.append(cores[:k])
+        n_sh = sum(len(c) for c in shells) + 1
+        if 2 <= n_sh <= 8:
+            break
+    egap = float(rng.uniform(1.0, 10.0))
+    nvb = float(sum(_ELEMENTS[int(z)][1] * p for z, p in zip(zs, pers)))
+    atoms = []
+    for i, (z, p, cores) in enumerate(zip(zs, pers, shells)):
+        sh = [Shell(Ip=ip, Nel=ne, designator=d, Auger=float(rng.uniform(1.0, 10.0))) for ip, ne, d in cores]
+        if i == 0:
+            sh.append(Shell(Ip=egap, Nel=nvb, designator=63, Auger=1.0e23))
+        atoms.append(AtomKind(Z=int(z), Pers=p, shells=sh))
+    mat = MaterialModel(name=f"synthetic-{n_elements}el", atoms=atoms, Dens=float(rng.uniform(1.5, 5.0)),
+                        Egap=egap, Layer=Layer)
+    n_osc = int(rng.integers(1, 7))
+    vb = atoms[0].shells[-1]
+    normalise_vb(mat, vb, list(rng.uniform(0.5, 1.5, n_osc)), list(rng.uniform(10.0, 40.0, n_osc)),
+                 list(rng.uniform(5.0, 20.0, n_osc)))
+    for atom in mat.atoms:
+        for s_ in atom.shells:
+            if s_.designator < 63:
+                normalise_core(mat, atom, s_)
+    e, d = parabolic_dos_file(float(rng.uniform(5.0, 20.0)))
+    mat.cut_off = 1.0
+    return attach_dos(mat, e, d)
+
+
+def cfg2(n_inst=64, layer=100.0, Tim=100.0, nmc_scale=1.0, n_R=100):
+    """Batched instances: ion Z uniform in {8..92}, energy log-uniform in
+    [1, 1000] MeV, one of three seeded materials (1, 2 or 3 elements),
+    iterations uniform in {100..5000} (times nmc_scale, at least 1)."""
+    rng = np.random.Generator(np.random.PCG64(1002))
+    mats = [synthetic_material(rng, k, layer) for k in (1, 2, 3)]
+    out = []
+    for i in range(n_inst):
+        Z = int(rng.integers(8, 93))
+        E = float(math.exp(rng.uniform(math.log(1e6), math.log(1e9))))
+        mi = int(rng.integers(0, 3))
+        nmc = max(1, int(round(int(rng.integers(100, 5001)) * nmc_scale)))
+        out.append(Workload(name=f"cfg2-{i}", material=mats[mi], ion_Z=Z, ion_mass=ATOMIC_WEIGHT[Z - 1], ion_E=E,
+                            Tim=Tim, dt=1.0, NMC=nmc, R_edges=log_radial_grid(n_R, 1.0, 1000.0), seed=1002,
+                            notes={"material": mi}))
+    return out
