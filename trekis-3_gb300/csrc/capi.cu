@@ -333,7 +333,6 @@ struct Workspace {
     size_t n_all = 0;
     Tal tal;
     Ctrs* ctr = nullptr;
-    McConst<T>* dC = nullptr;
     T *tg = nullptr, *Rg = nullptr;
     int *th = nullptr, *rh = nullptr;   // grid bucket hints
     double* V = nullptr;
@@ -396,7 +395,6 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     w->n_all = 2 * (4 * n_e + 3 * n_h) + n_l;   // difference + single-row blocks, lattice
     w->tall = (unsigned long long*)b.alloc(8 * w->n_all);
     w->ctr = (Ctrs*)b.alloc(sizeof(Ctrs));
-    w->dC = (McConst<T>*)b.alloc(sizeof(McConst<T>));
     w->tg = (T*)b.alloc(sizeof(T) * Nt);
     w->Rg = (T*)b.alloc(sizeof(T) * NR);
     w->th = (int*)b.alloc(sizeof(int) * (2 * (size_t)Nt + 2));
@@ -434,7 +432,7 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
             wd[j] = j > 0 ? t->dos_E[j] - t->dos_E[j - 1] : (nD > 1 ? t->dos_E[1] - t->dos_E[0] : 1.0);
         if (cudaMemcpy(w->wD, wd.data(), 8 * wd.size(), cudaMemcpyHostToDevice) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
     }
-    if (!w->tall || !w->ctr || !w->dC || !w->tg || !w->Rg || !w->V || !w->hmap || !w->hstage || !w->calls || !w->out)
+    if (!w->tall || !w->ctr || !w->tg || !w->Rg || !w->V || !w->hmap || !w->hstage || !w->calls || !w->out)
         return nullptr;
     Tal& tal = w->tal;
     tal.e_cnt = w->tall; tal.e_E = w->tall + 2 * n_e; tal.p_cnt = w->tall + 4 * n_e; tal.p_E = w->tall + 6 * n_e;
@@ -489,6 +487,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     C.mobile_holes = m.hole_mass < 1e3;
     C.mec2 = (T)(kMe * kC * kC / kE);
     C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
+    finish_const(C);
     C.dosE = tb.dosE; C.nD = tb.nD;
     C.elast_cdf = (m.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
     std::vector<double> tg = tallied_times(cfg.Tim, cfg.dt, cfg.dt_flag);
@@ -510,7 +509,6 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     Tal tal = ws->tal;
     if (!out.spectra()) tal.spec = nullptr;
     Ctrs* dctr = ws->ctr;
-    McConst<T>* dC = ws->dC;
     const double* dV = ws->V;
     CK(cudaMemsetAsync(ws->hstage, 0, 8 * ws->hstage_n, strm));
 
@@ -524,7 +522,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         pp = &prop;
     }
     const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
-    const int bs = cfg.block_size > 0 ? std::min(cfg.block_size, 256) : 256;
+    const int bs = cfg.block_size > 0 ? std::max(32, std::min(cfg.block_size, 256) & ~31) : 256;   // whole warps
     const int64_t cap = ws->cap;
     // the spectra hold one histogram per iteration of a batch
     const int B_max = tal.spec ? ws->spec_cap : (1 << 16);
@@ -542,21 +540,19 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     while (done < cfg.NMC) {
         const int nb = std::min(B, cfg.NMC - done);
         C.it0 = cfg.iteration_offset + done;
-        CK(cudaMemcpyAsync(dC, &C, sizeof C, cudaMemcpyHostToDevice, strm));
-        h2d += sizeof C;
         CK(cudaMemsetAsync(ws->tall, 0, 8 * ws->n_all, strm));
         if (tal.spec) CK(cudaMemsetAsync(tal.spec, 0, 4 * ws->spec_it * nb, strm));
         CK(cudaMemsetAsync(dctr, 0, sizeof(Ctrs), strm));
         QSet<T>* in = &ws->qa;
         QSet<T>* ot = &ws->qb;
-        launch_shi<T>(dC, shi_of<T>(t), ws->evs, ws->cap_ev, dctr, nb, strm);
+        launch_shi<T>(C, shi_of<T>(t), ws->evs, ws->cap_ev, dctr, nb, strm);
         ++launches;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
         d2h += sizeof hc;
         CK(cudaStreamSynchronize(strm));
         if (!hc.overflow) {
-            launch_pairs<T>(dC, tb, ws->evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)ws->cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], tal, dctr, strm);
+            launch_pairs<T>(C, tb, ws->evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)ws->cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], tal, dctr, strm);
             ++launches;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
@@ -575,7 +571,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             int n_in[4] = {hc.n_out[Q_E], hc.n_out[Q_HVB], hc.n_out[Q_HDEEP], hc.n_out[Q_P]};
             CK(cudaMemsetAsync(dctr, 0, NQ * sizeof(int), strm));
             CK(cudaEventRecord(ws->s0, strm));
-            launch_step<T>(dC, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm,
+            launch_step<T>(C, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm,
                            ws->guess, pp);
             CK(cudaEventRecord(ws->s1, strm));
             blaunch += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0) + (pp ? 1 : 0); ++bsteps;

@@ -71,13 +71,13 @@ __device__ __forceinline__ void load(const PQ<T>& q, int64_t i, P<T>& p) {
 // mixed-precision event stream: draws for the FP64 SHI state use next_d()
 template <class T>
 struct EvStream {
-    uint32_t k0, k1, c0, c1, c2, c3, buf[4];
+    const uint32_t* rk;   // round keys of the run's seed
+    uint32_t c0, c1, c2, c3, buf[4];
     int used;
-    __device__ EvStream(uint64_t seed, uint64_t pid, uint32_t ordinal)
-        : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), c0((uint32_t)pid), c1((uint32_t)(pid >> 32)),
-          c2(ordinal), c3(0), used(4) {}
+    __device__ EvStream(const uint32_t* rk_, uint64_t pid, uint32_t ordinal)
+        : rk(rk_), c0((uint32_t)pid), c1((uint32_t)(pid >> 32)), c2(ordinal), c3(0), used(4) {}
     __device__ __forceinline__ uint32_t word() {
-        if (used == 4) { philox4x32(c0, c1, c2, c3, k0, k1, buf); ++c3; used = 0; }
+        if (used == 4) { philox4x32_rk(c0, c1, c2, c3, rk, buf); ++c3; used = 0; }
         return buf[used++];
     }
     __device__ __forceinline__ T next() { return Uni<T>::of(word()); }
@@ -191,27 +191,26 @@ __device__ void emit_spec(const McConst<T>& C, const Tal& tal, int kind, int sh,
     }
 }
 
-// Tally the free-flight segment [t0, tn) at every grid time t_i with
-// t0 < t_i <= min(tn, Tim), exactly as Calculated_statistics sees it:
-// position X + V (t_i - t0) 1e-5 along (th, ph) for moving particles.
-// ia is the time-grid index of t0 (the caller has it: t0 is the time of the
-// event that started the segment); returns the index of min(tn, Tim), which is
-// the next segment's ia.  Consecutive segments of a particle tile the time
-// axis, so one search per segment suffices.
+// The grid rows a segment covers: sets ib (rows ia..ib, none when ib < ia)
+// and returns the time-grid index of min(tn, Tim).
 template <class T>
-__device__ int emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn, T X, T Y,
-                        T th, T ph, T V /* m/s, 0: static */, int it, bool ang, int ia) {
+__device__ __forceinline__ int seg_span(const McConst<T>& C, T t0, T tn, int& ib) {
     const int Nt = C.Nt;
-    if (!(t0 < C.tg_hi)) return Nt;
+    if (!(t0 < C.tg_hi)) { ib = -1; return Nt; }
     const T tend = tn < C.Tim ? tn : C.Tim;
-    const int ib = (tend >= C.tg_hi) ? Nt : tbin(C, tend) - 1;
-    const int tnext = (tend >= C.tg_hi) ? Nt : ib + 1;
-    if (ib < ia) return tnext;
+    ib = (tend >= C.tg_hi) ? Nt : tbin(C, tend) - 1;
+    return (tend >= C.tg_hi) ? Nt : ib + 1;
+}
+
+// Tally rows ia..ib (ia <= ib) of one segment.
+template <class T>
+__device__ void seg_body(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T X, T Y,
+                         T th, T ph, T V, int it, bool ang, int ia, int ib) {
     if (tal.spec && kind != 2) emit_spec(C, tal, kind, sh, E, Ek, th, ang, it, ia, ib);
     const long long qE = fixE(E), qK = fixE(Ek);
     if (V == T(0)) {
         flush_run(C, tal, kind, sh, rbin(C, m_sqrt(X * X + Y * Y)), ia, ib, qE, qK);
-        return tnext;
+        return;
     }
     const T s_t = f_sin(th), s_p = f_sin(ph), c_p = f_cos(ph);
     int cur = -1, start = ia;
@@ -227,6 +226,21 @@ __device__ int emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T
         }
     }
     flush_run(C, tal, kind, sh, cur, start, ib, qE, qK);
+}
+
+// Tally the free-flight segment [t0, tn) at every grid time t_i with
+// t0 < t_i <= min(tn, Tim), exactly as Calculated_statistics sees it:
+// position X + V (t_i - t0) 1e-5 along (th, ph) for moving particles.
+// ia is the time-grid index of t0 (the caller has it: t0 is the time of the
+// event that started the segment); returns the index of min(tn, Tim), which is
+// the next segment's ia.  Consecutive segments of a particle tile the time
+// axis, so one search per segment suffices.
+template <class T>
+__device__ __forceinline__ int emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn,
+                                        T X, T Y, T th, T ph, T V /* m/s, 0: static */, int it, bool ang, int ia) {
+    int ib;
+    const int tnext = seg_span(C, t0, tn, ib);
+    if (ib >= ia) seg_body(C, tal, kind, sh, E, Ek, t0, X, Y, th, ph, V, it, ang, ia, ib);
     return tnext;
 }
 
@@ -261,6 +275,44 @@ __device__ __forceinline__ int emit_hole(const McConst<T>& C, const Tal& tal, co
 template <class T>
 __device__ __forceinline__ void emit_photon(const McConst<T>& C, const Tal& tal, const P<T>& p, int ia) {
     if (p.E > T(0)) emit_seg(C, tal, 2, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, p.th, p.ph, T(kC), p.it, false, ia);
+}
+
+// ---- deferred segments of the hot kernel ---------------------------------------------
+// Only a fraction of collisions start a segment that reaches a grid time, so
+// tallying in place runs the tally code for a whole warp with a few lanes
+// active.  The hot kernel instead parks such segments in a per-warp ring in
+// shared memory and tallies them 32 at a time, all lanes busy.
+constexpr int kSegQ = 64;       // ring slots per warp: < 32 parked + up to 32 new
+constexpr int kHotWarps = 8;    // k_hot blocks have at most 256 threads
+static_assert(MAXSH <= 256, "a parked segment packs its shell in 8 bits");
+
+template <class T>
+struct SegRing {
+    T f[8][kHotWarps][kSegQ];   // E, Ek, t0, X, Y, th, ph, V
+    int ia[kHotWarps][kSegQ], ib[kHotWarps][kSegQ];
+    int meta[kHotWarps][kSegQ];  // iteration | shell << 16 | angle counted << 24
+};
+
+template <class T>
+__device__ __forceinline__ void park_seg(SegRing<T>& R, int w, int slot, T E, T Ek, T t0, T X, T Y, T th, T ph, T V,
+                                         int ia, int ib, int it, int sh, bool ang) {
+    R.f[0][w][slot] = E; R.f[1][w][slot] = Ek; R.f[2][w][slot] = t0; R.f[3][w][slot] = X;
+    R.f[4][w][slot] = Y; R.f[5][w][slot] = th; R.f[6][w][slot] = ph; R.f[7][w][slot] = V;
+    R.ia[w][slot] = ia; R.ib[w][slot] = ib;
+    R.meta[w][slot] = (it & 0xffff) | (sh << 16) | ((int)ang << 24);
+}
+
+// lanes 0..cnt-1 of the warp tally the segments at ring slots head..head+cnt-1
+template <class T>
+__device__ __forceinline__ void drain_segs(const McConst<T>& C, const Tal& tal, const SegRing<T>& R, int kind, int w,
+                                           int lane, int head, int cnt) {
+    if (lane < cnt) {
+        const int q = (head + lane) & (kSegQ - 1);
+        const int m = R.meta[w][q];
+        seg_body(C, tal, kind, (m >> 16) & 0xff, R.f[0][w][q], R.f[1][w][q], R.f[2][w][q], R.f[3][w][q],
+                 R.f[4][w][q], R.f[5][w][q], R.f[6][w][q], R.f[7][w][q], m & 0xffff, ((m >> 24) & 1) != 0,
+                 R.ia[w][q], R.ib[w][q]);
+    }
 }
 
 // per-thread accumulator of the lattice energy (one atomic per change of
@@ -439,32 +491,60 @@ __device__ __forceinline__ void electron_flight(const DevTabs<T>& tb, P<T>& p, S
 }
 
 // Mott energy transfer, Pers-weighted average over species (MC:2394-2407, CS:3517-3613).
-// FP64 keeps the reference's expressions; FP32 uses algebraically identical
-// forms without cancellation: beta^2 = tau(tau+2)/(tau+1)^2, and with
-// mu = (u(2nu+1)-nu)/(u+nu) the exact 1-mu = 2nu(1-u)/(u+nu).
+// FP64 keeps the reference's expressions.  FP32 evaluates the same quantity
+// without cancellation and with two divisions per species: with tau = E/mc^2,
+// g = (1-beta^2)/beta^2 = 1/(tau(tau+2)), 1/beta^2 = (tau+1)^2 g, the exact
+// 1-mu = 2nu(1-RN)/(RN+nu), and everything scaled by the target's rest energy
+// M (iM = 1/M, mu2 = (M_eff mc^2/M)^2, e = (E+M_eff mc^2)/M, n = E(E+2M_eff mc^2)/M^2):
+//   W1 W2 = M (p q + ct mu2 st2) n / (q d),  q = 1 + sqrt(1 - mu2 st2),
+//   p = e st2 + (1-ct),  d = (e+1)^2 - n ct^2.
+template <class S>
+__device__ __forceinline__ float mott_transfer_f32(const McConst<float>& C, float Ee, float M_eff, S& s) {
+    const float tau = Ee * C.inv_mec2;
+    const float t1 = tau + 1.f, tt = tau * (tau + 2.f);
+    // v = c beta < 1e-6 m/s leaves the direction unchanged (the reference's test)
+    const bool moving = !(tt < 1.1126500560536185e-29f * t1 * t1);
+    const float g = moving ? __fdividef(1.f, tt) : 0.f;
+    const float h = t1 * t1 * g * sqrtf(__fdividef(tau, t1));   // sqrt(tau/(1+tau)) / beta^2
+    const float mc2 = M_eff * C.mec2, mc2sq = mc2 * mc2;
+    const float Emc = Ee + mc2, N = Ee * (Ee + 2.f * mc2);
+    float dE = 0.f;
+    for (int a = 0; a < C.nat; ++a) {
+        const float RN = s.next();
+        float omc = 0.f;
+        if (moving) {
+            const float nu = C.mott_c1[a] * g * (1.13f + C.mott_c2[a] * h);
+            omc = __fdividef(2.f * nu * (1.f - RN), RN + nu);
+        }
+        const float ct = 1.f - omc, st2 = omc * (2.f - omc);
+        const float iM = C.mott_iM[a], mu2 = mc2sq * C.mott_iM2[a];
+        const float e = Emc * iM, n = N * C.mott_iM2[a];
+        const float q = 1.f + sqrtf(1.f - mu2 * st2);
+        const float p = e * st2 + omc;
+        const float d = (e + 1.f) * (e + 1.f) - n * ct * ct;
+        dE += C.mott_wM[a] * __fdividef((p * q + ct * mu2 * st2) * n, q * d);
+    }
+    return dE;
+}
+
 template <class T, class S>
 __device__ T mott_transfer(const McConst<T>& C, T Ee, T M_eff, S& s) {
-    T dE = T(0);
-    const T Erest = C.mec2;
-    const T tau = Ee / Erest;
-    T beta2, v;
-    if constexpr (sizeof(T) == 8) {
-        const T fact = Ee / Erest + T(1);
-        v = T(kC) * m_sqrt(T(1) - T(1) / (fact * fact));
-        const T beta = v / T(kC);
-        beta2 = beta * beta;
+    if constexpr (sizeof(T) == 4) {
+        return mott_transfer_f32(C, Ee, M_eff, s);
     } else {
-        beta2 = tau * (tau + T(2)) / ((tau + T(1)) * (tau + T(1)));
-        v = T(kC) * m_sqrt(beta2);
-    }
-    const T sq = m_sqrt(tau / (T(1) + tau));
-    const T mc2 = M_eff * C.mec2;
-    for (int a = 0; a < C.nat; ++a) {
-        const T Z = T(C.Zat[a]);
-        const T RN = s.next();
-        const T Mct2 = C.Mass_kg[a] * T(kC) * T(kC) / T(kE);
-        T W1, ct2;
-        if constexpr (sizeof(T) == 8) {
+        T dE = T(0);
+        const T Erest = C.mec2;
+        const T tau = Ee / Erest;
+        const T fact = Ee / Erest + T(1);
+        const T v = T(kC) * m_sqrt(T(1) - T(1) / (fact * fact));
+        const T beta = v / T(kC);
+        const T beta2 = beta * beta;
+        const T sq = m_sqrt(tau / (T(1) + tau));
+        const T mc2 = M_eff * C.mec2;
+        for (int a = 0; a < C.nat; ++a) {
+            const T Z = T(C.Zat[a]);
+            const T RN = s.next();
+            const T Mct2 = C.Mass_kg[a] * T(kC) * T(kC) / T(kE);
             T ct;
             if (v < T(1.0e-6)) ct = T(1);
             else {
@@ -472,34 +552,26 @@ __device__ T mott_transfer(const McConst<T>& C, T Ee, T M_eff, S& s) {
                 T mu = (RN * (T(2) * nu + T(1)) - nu) / (RN + nu);
                 ct = m_cos(m_acos(mu));
             }
-            ct2 = ct * ct;
+            const T ct2 = ct * ct;
             const T st2 = T(1) - ct2;
-            W1 = (Ee + mc2) * st2 + Mct2 - ct * m_sqrt(Mct2 * Mct2 - mc2 * mc2 * st2);
-        } else {
-            T omc = T(0);
-            if (!(v < T(1.0e-6))) {
-                T nu = T(1.7e-5) * C.Z23[a] * (T(1) - beta2) / beta2 * (T(1.13) + T(3.76) * C.alpha * C.alpha / beta2 * Z * Z * sq);
-                omc = T(2) * nu * (T(1) - RN) / (RN + nu);
-            }
-            const T ct = T(1) - omc, st2 = omc * (T(2) - omc);
-            ct2 = ct * ct;
-            const T r = m_sqrt(Mct2 * Mct2 - mc2 * mc2 * st2);
-            W1 = (Ee + mc2) * st2 + Mct2 * omc + ct * (mc2 * mc2 * st2) / (Mct2 + r);
+            const T W1 = (Ee + mc2) * st2 + Mct2 - ct * m_sqrt(Mct2 * Mct2 - mc2 * mc2 * st2);
+            const T E2mc = Ee + T(2) * mc2, EmcMc = Ee + mc2 + Mct2;
+            const T W2 = Ee * E2mc / (EmcMc * EmcMc - Ee * E2mc * ct2);
+            dE += W1 * W2 * C.Pers[a];
         }
-        const T E2mc = Ee + T(2) * mc2, EmcMc = Ee + mc2 + Mct2;
-        const T W2 = Ee * E2mc / (EmcMc * EmcMc - Ee * E2mc * ct2);
-        dE += W1 * W2 * C.Pers[a];
+        return dE / C.Psum;
     }
-    return dE / C.Psum;
 }
 
 // Update_particle_angles_lat (MC:1252-1299)
 template <class T, class S>
 __device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& theta, T& phi) {
-    T Ein = M_eff * C.mec2, Et = C.Mtarget * T(kC) * T(kC) / T(kE);
+    T Ein = M_eff * C.mec2, Et = (sizeof(T) == 4) ? C.Et_lat : C.Mtarget * T(kC) * T(kC) / T(kE);
     T E2mc = E + T(2) * Ein, EmW = E - W;
     T W1 = E * E2mc - W * (E + Ein + Et), W2 = E * E2mc * EmW * (E2mc - W);
-    T mu = (W2 > T(0)) ? W1 / m_sqrt(W2) : T(0);
+    T mu;
+    if constexpr (sizeof(T) == 4) mu = (W2 > T(0)) ? W1 * rsqrtf(W2) : T(0);
+    else mu = (W2 > T(0)) ? W1 / m_sqrt(W2) : T(0);
     if (m_abs(mu) > T(1)) { T RN = s.next(); mu = f_cos(pi_<T>() * RN); }
     theta = m_acos(mu);
     phi = T(2) * pi_<T>() * s.next();
@@ -653,11 +725,10 @@ struct ShiEv {  // one SHI collision: the ion state after it and the transfer
 constexpr int kSlotChunk = 32;
 
 template <class T>
-__global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__ Cp, DevShi<T> sh,
+__global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McConst<T> C, const __grid_constant__ DevShi<T> sh,
                                                   ShiEv* __restrict__ evs, int64_t cap_ev, Ctrs* ctr, int nit) {
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= nit) return;
-    const McConst<T>& C = *Cp;
     unsigned err = 0;
     unsigned long long nev = 0;
     const uint64_t pid = shi_pid(C.it0 + it);
@@ -676,7 +747,7 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
     };
     double E = C.ion_E0, t0 = 0.0, tn, Z = 0.0, L;
     {
-        EvStream<T> s(C.seed, pid, 0xFFFFFFFFu);
+        EvStream<T> s(C.rk, pid, 0xFFFFFFFFu);
         const T Et = (T)E, lx = m_log(Et);
         const int nb = find_monoton(sh.sE, sh.nS, Et);
         L = (double)shi_path(sh, nb, Et, lx);
@@ -688,7 +759,7 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
     int64_t slot = 0, slot_end = 0;
     while (tn < (double)C.Tim) {
         if (ord >= (1u << 26)) { err |= TREKIS_ERR_NAN; break; }   // no SHI track has this many collisions
-        EvStream<T> s(C.seed, pid, ord);
+        EvStream<T> s(C.rk, pid, ord);
         const T Et = (T)E, lx = m_log(Et);
         const int nb = find_monoton(sh.sE, sh.nS, Et);
         // Which_shell
@@ -787,16 +858,15 @@ __global__ void __launch_bounds__(64) k_shi_track(const McConst<T>* __restrict__
 // The electron-hole pair of each SHI collision, one thread each (MC:2198-2247);
 // draws continue in the collision's stream after the ion's three.
 template <class T>
-__global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp, DevTabs<T> tb,
+__global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ McConst<T> C, const __grid_constant__ DevTabs<T> tb,
                                                const ShiEv* __restrict__ evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
-                                               PQ<T> qhdeep, Tal tal, Ctrs* ctr) {
+                                               PQ<T> qhdeep, const __grid_constant__ Tal tal, Ctrs* ctr) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_ev) return;
-    const McConst<T>& C = *Cp;
     const ShiEv ev = evs[i];
     if (ev.it < 0) return;   // an unused slot of a reserved chunk
     const uint64_t pid = shi_pid(C.it0 + ev.it);
-    EvStream<T> s(C.seed, pid, ev.ord);
+    EvStream<T> s(C.rk, pid, ev.ord);
     s.word(); s.word(); s.word();
     unsigned err = 0;
     const int k = ev.k;
@@ -831,13 +901,14 @@ __global__ void __launch_bounds__(128) k_pairs(const McConst<T>* __restrict__ Cp
 // ---- cascade events ------------------------------------------------------------------------
 // One electron event.  FULL=false compiles only the elastic branch (the hot
 // kernel): an ionising draw returns false with the particle untouched, and the
-// event is redone from the same stream by the FULL version.
-template <class T, bool FULL>
+// event is redone from the same stream by the FULL version.  DEFER leaves the
+// tally of the new segment to the caller (p.ti stays the event's grid index).
+template <class T, bool FULL, bool DEFER = false>
 __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
                                P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc,
                                float fg = -1.f) {
     const uint32_t ord = p.ord;
-    EvStream<T> s(C.seed, p.pid, ord);
+    EvStream<T> s(C.rk, p.pid, ord);
     const int ti0 = p.ti;   // time-grid index of the event time
     const T Eel = p.E;
     T I, Em;
@@ -893,7 +964,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     p.X = X; p.Y = Y; p.Z = Z; p.th = th1; p.ph = ph1;
     cut_e(C, p);
     if (p.E < T(-1.0e-9) || m_isnan(p.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
-    p.ti = emit_electron(C, tal, p, ti0);
+    if constexpr (!DEFER) p.ti = emit_electron(C, tal, p, ti0);
     return true;
 }
 
@@ -918,12 +989,13 @@ __device__ T check_hole(const DevTabs<T>& tb, T Eel, T& dE, P<T>* el) {
     return Eh;
 }
 
-// One hole event; FULL=false compiles only valence-hole elastic scattering.
-template <class T, bool FULL>
+// One hole event; FULL=false compiles only valence-hole elastic scattering;
+// DEFER as for electron_event.
+template <class T, bool FULL, bool DEFER = false>
 __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& h,
                            unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc, float fg = -1.f) {
     const uint32_t ord = h.ord;
-    EvStream<T> s(C.seed, h.pid, ord);
+    EvStream<T> s(C.rk, h.pid, ord);
     if (!FULL && h.sh != C.vb) return false;
     const int ti0 = h.ti;   // time-grid index of the event time
     if (h.sh == C.vb) {
@@ -991,7 +1063,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         hole_parameters(C, tb, h, Eh + C.Egap, s, &mc);
         cut_h(C, h);
         if (h.Ek < T(-1.0e-9) || m_isnan(h.Ek)) err |= TREKIS_ERR_NEG_ENERGY_H;
-        h.ti = emit_hole(C, tal, h, ti0);
+        if constexpr (!DEFER) h.ti = emit_hole(C, tal, h, ti0);
         return true;
     }
     if constexpr (!FULL) return false;
@@ -1099,7 +1171,7 @@ template <class T>
 __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& p,
                              unsigned& err, unsigned long long* nev) {
     const uint32_t ord = p.ord++;
-    EvStream<T> s(C.seed, p.pid, ord);
+    EvStream<T> s(C.rk, p.pid, ord);
     const int ti0 = p.ti;
     const T Eel = p.E;
     const T X = p.X + p.L * f_sin(p.th) * f_sin(p.ph);
@@ -1130,27 +1202,76 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
 // Hot kernel of a wavefront step, one per particle kind (electrons, mobile
 // valence holes) so each carries only its own event code: every particle
 // runs up to K elastic collisions.  A particle whose next event ionises goes
-// to a side queue; survivors go to the next generation's queue.
+// to a side queue; survivors go to the next generation's queue.  The warps
+// iterate together (a lane whose particle is done idles) so that segments
+// reaching a grid time can be parked in the warp's ring and tallied 32 at a
+// time; the tallies are integer sums, so the order does not matter.
 template <class T, bool IS_E>
-__global__ void __launch_bounds__(256, 4) k_hot(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> in, int n,
-                                             Out<T> o, PQ<T> side, Tal tal, int K) {
-    const McConst<T>& C = *Cp;
+__global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<T> C,
+                                             const __grid_constant__ DevTabs<T> tb, const __grid_constant__ PQ<T> in,
+                                             int n, const __grid_constant__ Out<T> o, const __grid_constant__ PQ<T> side,
+                                             const __grid_constant__ Tal tal, int K) {
+    __shared__ SegRing<T> ring;
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (blockIdx.x * blockDim.x + (threadIdx.x & ~31) >= n) return;   // whole warp past the end
+    const bool valid = idx < n;
     P<T> p;
-    load(in, idx, p);
-    p.ti = tbin(C, p.tn);
+    if (valid) {
+        load(in, idx, p);
+        p.ti = tbin(C, p.tn);
+    }
     unsigned err = 0;
     unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     LatAcc lat;
     MfpCache<T> mc;
     bool diverted = false;
-    for (int e = 0; e < K && p.tn < C.Tim; ++e) {
-        bool done;
-        if constexpr (IS_E) done = electron_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc);
-        else done = hole_event<T, false>(C, tb, tal, o, p, err, lat, nev, mc);
-        if (!done) { diverted = true; break; }
+    bool act = valid && K > 0 && p.tn < C.Tim;
+    const T co = C.cut_off > T(0) ? C.cut_off : T(0);
+    int head = 0, cnt = 0;   // the warp's ring: parked segments at head..head+cnt-1
+    for (int e = 0; e < K; ++e) {
+        if (!__any_sync(0xffffffffu, act)) break;
+        bool pend = false;
+        int ia = 0, ib = -1;
+        if (act) {
+            bool done;
+            if constexpr (IS_E) done = electron_event<T, false, true>(C, tb, tal, o, p, err, lat, nev, mc);
+            else done = hole_event<T, false, true>(C, tb, tal, o, p, err, lat, nev, mc);
+            if (!done) { diverted = true; act = false; }
+            else {
+                ia = p.ti;
+                p.ti = seg_span(C, p.t0, p.tn, ib);
+                pend = ib >= ia;
+                act = p.tn < C.Tim;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, pend);
+        if (m) {
+            if (pend) {
+                const int slot = (head + cnt + __popc(m & ((1u << lane) - 1u))) & (kSegQ - 1);
+                if constexpr (IS_E) {
+                    const bool mv = p.E > co;
+                    park_seg(ring, w, slot, p.E, T(0), p.t0, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0),
+                             mv ? v_el(p.E) : T(0), ia, ib, p.it, 0, true);
+                } else {
+                    const bool mv = (p.M < T(1.0e3)) && (p.Ek > co);
+                    park_seg(ring, w, slot, p.E, p.Ek, p.t0, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0),
+                             ia, ib, p.it, p.sh, mv);
+                }
+            }
+            cnt += __popc(m);
+            if (cnt >= 32) {
+                __syncwarp();
+                drain_segs(C, tal, ring, IS_E ? 0 : 1, w, lane, head, 32);
+                __syncwarp();
+                head = (head + 32) & (kSegQ - 1);
+                cnt -= 32;
+            }
+        }
     }
+    __syncwarp();
+    drain_segs(C, tal, ring, IS_E ? 0 : 1, w, lane, head, cnt);
+    if (!valid) return;
     lat.flush(tal);
     if (diverted) append(side, &o.ctr->n_out[IS_E ? Q_EINEL : Q_HINEL], &o.ctr->overflow, p);
     else push(C, tal, o, IS_E ? 0 : 1, p);
@@ -1163,10 +1284,12 @@ __global__ void __launch_bounds__(256, 4) k_hot(const McConst<T>* __restrict__ C
 // one full event for each particle of the ionisation side queues, each deep
 // hole (Auger or radiative decay) and each photon (absorption).
 template <class T>
-__global__ void __launch_bounds__(128) k_rare(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> e_inel,
-                                              PQ<T> h_inel, PQ<T> hdeep, int n_deep, PQ<T> ph, int n_ph, Out<T> o,
-                                              Tal tal, const float* __restrict__ guess) {
-    const McConst<T>& C = *Cp;
+__global__ void __launch_bounds__(128) k_rare(const __grid_constant__ McConst<T> C,
+                                              const __grid_constant__ DevTabs<T> tb, const __grid_constant__ PQ<T> e_inel,
+                                              const __grid_constant__ PQ<T> h_inel, const __grid_constant__ PQ<T> hdeep,
+                                              int n_deep, const __grid_constant__ PQ<T> ph, int n_ph,
+                                              const __grid_constant__ Out<T> o, const __grid_constant__ Tal tal,
+                                              const float* __restrict__ guess) {
     const int n_e = o.ctr->n_out[Q_EINEL], n_h = o.ctr->n_out[Q_HINEL];
     const int total = n_e + n_h + n_deep + n_ph;
     unsigned err = 0;
@@ -1206,7 +1329,7 @@ __device__ __forceinline__ float silu_f(float z) { return z / (1.f + __expf(-z))
 // (BF16 operands, FP32 accumulator in TMEM), the 64 -> 1 layer on the CUDA
 // cores.  A guess only steers the search; any value gives the same draw.
 template <class T>
-__global__ void __launch_bounds__(128) k_propose(const McConst<T>* __restrict__ Cp, DevTabs<T> tb, PQ<T> e_inel,
+__global__ void __launch_bounds__(128) k_propose(const __grid_constant__ McConst<T> C, const __grid_constant__ DevTabs<T> tb, PQ<T> e_inel,
                                                  PQ<T> h_inel, const Ctrs* __restrict__ ctr, MlpDev net,
                                                  float* __restrict__ guess, int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char psm[];
@@ -1214,7 +1337,6 @@ __global__ void __launch_bounds__(128) k_propose(const McConst<T>* __restrict__ 
     unsigned char* sB = psm + 128 * 64 * 2;           // 64 x 64 BF16 weights of one network
     uint64_t* mbar = (uint64_t*)(sB + 64 * 64 * 2);
     uint32_t* tslot = (uint32_t*)(mbar + 1);
-    const McConst<T>& C = *Cp;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int n_e = ctr->n_out[Q_EINEL], n_h = ctr->n_out[Q_HINEL], n = n_e + n_h;
     const int ntiles = (n + 127) / 128;
@@ -1237,7 +1359,7 @@ __global__ void __launch_bounds__(128) k_propose(const McConst<T>* __restrict__ 
             P<T> p;
             const bool e = g < n_e;
             if (e) load(e_inel, g, p); else load(h_inel, g - n_e, p);
-            EvStream<T> s(C.seed, p.pid, p.ord);
+            EvStream<T> s(C.rk, p.pid, p.ord);
             (void)s.next();                                // the draw that chose ionisation
             const T Eel = e ? p.E : p.Ek;
             const int k = e ? which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next())
@@ -1299,23 +1421,23 @@ __global__ void __launch_bounds__(128) k_propose(const McConst<T>* __restrict__ 
 }
 
 template <class T>
-void launch_propose(const Proposer& p, const McConst<T>* C, const DevTabs<T>& tb, PQ<T> e_inel, PQ<T> h_inel,
+void launch_propose(const Proposer& p, const McConst<T>& C, const DevTabs<T>& tb, PQ<T> e_inel, PQ<T> h_inel,
                     const Ctrs* ctr, cudaStream_t s) {
     // 24 KB used; asking for 48 KB keeps at most four CTAs (256 TMEM columns) per SM
     k_propose<T><<<p.blocks, 128, 48 * 1024, s>>>(C, tb, e_inel, h_inel, ctr, p.net, p.guess, p.err);
 }
-template void launch_propose<float>(const Proposer&, const McConst<float>*, const DevTabs<float>&, PQ<float>,
+template void launch_propose<float>(const Proposer&, const McConst<float>&, const DevTabs<float>&, PQ<float>,
                                     PQ<float>, const Ctrs*, cudaStream_t);
-template void launch_propose<double>(const Proposer&, const McConst<double>*, const DevTabs<double>&, PQ<double>,
+template void launch_propose<double>(const Proposer&, const McConst<double>&, const DevTabs<double>&, PQ<double>,
                                      PQ<double>, const Ctrs*, cudaStream_t);
 
 template <class T>
-void launch_shi(const McConst<T>* C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
+void launch_shi(const McConst<T>& C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
                 cudaStream_t s) {
     k_shi_track<T><<<(nit + 63) / 64, 64, 0, s>>>(C, sh, (ShiEv*)evs, cap_ev, ctr, nit);
 }
 template <class T>
-void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
+void launch_pairs(const McConst<T>& C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
                   PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s) {
     if (n_ev <= 0) return;
     k_pairs<T><<<(unsigned)((n_ev + 127) / 128), 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qhvb, qhdeep, tal, ctr);
@@ -1323,7 +1445,7 @@ void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, in
 size_t shi_event_bytes() { return sizeof(ShiEv); }
 
 template <class T>
-void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
+void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
                  PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
                  const float* guess, const Proposer* prop) {
     Out<T> o{{out.q[0], out.q[1], out.q[2], out.q[3]}, ctr};
@@ -1336,16 +1458,16 @@ void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, c
                                           n_in[Q_P], o, tal, prop ? guess : nullptr);
 }
 
-template void launch_shi<float>(const McConst<float>*, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t);
-template void launch_shi<double>(const McConst<double>*, const DevShi<double>&, void*, int64_t, Ctrs*, int, cudaStream_t);
-template void launch_pairs<float>(const McConst<float>*, const DevTabs<float>&, const void*, int64_t, PQ<float>,
+template void launch_shi<float>(const McConst<float>&, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t);
+template void launch_shi<double>(const McConst<double>&, const DevShi<double>&, void*, int64_t, Ctrs*, int, cudaStream_t);
+template void launch_pairs<float>(const McConst<float>&, const DevTabs<float>&, const void*, int64_t, PQ<float>,
                                   PQ<float>, PQ<float>, Tal, Ctrs*, cudaStream_t);
-template void launch_pairs<double>(const McConst<double>*, const DevTabs<double>&, const void*, int64_t, PQ<double>,
+template void launch_pairs<double>(const McConst<double>&, const DevTabs<double>&, const void*, int64_t, PQ<double>,
                                    PQ<double>, PQ<double>, Tal, Ctrs*, cudaStream_t);
-template void launch_step<float>(const McConst<float>*, const DevTabs<float>&, const QSet<float>&, const int*,
+template void launch_step<float>(const McConst<float>&, const DevTabs<float>&, const QSet<float>&, const int*,
                                  const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t,
                                  const float*, const Proposer*);
-template void launch_step<double>(const McConst<double>*, const DevTabs<double>&, const QSet<double>&, const int*,
+template void launch_step<double>(const McConst<double>&, const DevTabs<double>&, const QSet<double>&, const int*,
                                   const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t,
                                   const float*, const Proposer*);
 

@@ -40,7 +40,34 @@ struct McConst {
     const T* dosE;      // DOS energies (the valence-hole spectrum's bins)
     int nD;
     int elast_cdf;      // 1: phonon-CDF elastic transfers from the rows, 0: Mott
+    // derived per species for the FP32 Mott transfer (finish_const): with
+    // M = M_a c^2 / e [eV], c1 = 1.7e-5 Z^(2/3), c2 = 3.76 alpha^2 Z^2,
+    // iM = 1/M, iM2 = 1/M^2, wM = M Pers / Psum
+    T mott_c1[TREKIS_MAX_ATOMS], mott_c2[TREKIS_MAX_ATOMS];
+    T mott_iM[TREKIS_MAX_ATOMS], mott_iM2[TREKIS_MAX_ATOMS], mott_wM[TREKIS_MAX_ATOMS];
+    T inv_mec2;
+    T Et_lat;           // Mtarget c^2 / e [eV]
+    uint32_t rk[20];    // Philox round keys of seed
 };
+
+// Fills the derived fields of C from the species data, Psum, Mtarget and seed.
+template <class T>
+inline void finish_const(McConst<T>& C) {
+    const double mec2 = kMe * kC * kC / kE, al = kE * kE / (kH * kC * 4.0 * kPi * kE0), ps = (double)C.Psum;
+    C.inv_mec2 = (T)(1.0 / mec2);
+    C.Et_lat = (T)((double)C.Mtarget * kC * kC / kE);
+    philox_round_keys(C.seed, C.rk);
+    for (int a = 0; a < TREKIS_MAX_ATOMS; ++a) {
+        if (a >= C.nat) { C.mott_c1[a] = C.mott_c2[a] = C.mott_iM[a] = C.mott_iM2[a] = C.mott_wM[a] = T(0); continue; }
+        const double Z = (double)C.Zat[a];
+        const double M = (double)C.Mass_kg[a] * kC * kC / kE;
+        C.mott_c1[a] = (T)(1.7e-5 * (double)C.Z23[a]);
+        C.mott_c2[a] = (T)(3.76 * al * al * Z * Z);
+        C.mott_iM[a] = (T)(1.0 / M);
+        C.mott_iM2[a] = (T)(1.0 / (M * M));
+        C.mott_wM[a] = (T)(M * (double)C.Pers[a] / ps);
+    }
+}
 
 // Structure-of-arrays particle queue.
 template <class T>
@@ -93,10 +120,10 @@ struct Ctrs {
 };
 
 template <class T>
-void launch_shi(const McConst<T>* C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
+void launch_shi(const McConst<T>& C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
                 cudaStream_t s);
 template <class T>
-void launch_pairs(const McConst<T>* C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
+void launch_pairs(const McConst<T>& C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
                   PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s);
 size_t shi_event_bytes();
 template <class T>
@@ -134,11 +161,11 @@ struct Proposer {
     int blocks;      // persistent CTAs of the proposal kernel
 };
 template <class T>
-void launch_propose(const Proposer& p, const McConst<T>* C, const DevTabs<T>& tb, PQ<T> e_inel, PQ<T> h_inel,
+void launch_propose(const Proposer& p, const McConst<T>& C, const DevTabs<T>& tb, PQ<T> e_inel, PQ<T> h_inel,
                     const Ctrs* ctr, cudaStream_t s);
 
 template <class T>
-void launch_step(const McConst<T>* C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
+void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
                  PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
                  const float* guess = nullptr, const Proposer* prop = nullptr);
 // Bucket hints of the time and radius grids.  A radius bucket is the bit

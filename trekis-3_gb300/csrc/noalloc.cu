@@ -6,8 +6,8 @@
 // during a run (a host code whose pool allocator already owns the GPU's
 // memory, a job under a fixed device-memory budget, a service that must not
 // fail with out-of-memory mid-request) call this one instead: the particle
-// queues, int64 tallies, counters, run constants and staging all live in
-// g_scratch below, which the CUDA runtime reserves when it loads this module.
+// queues, int64 tallies, counters and staging all live in
+// g_scratch below (the run constants travel as kernel parameters), which the CUDA runtime reserves when it loads this module.
 // Nothing here calls cudaMalloc, cudaFree, cudaMallocAsync, cudaStreamCreate
 // or cudaEventCreate; host data reaches the device through cudaMemcpyAsync
 // from small host buffers on the stack.
@@ -112,7 +112,7 @@ struct Shape { int Nt, NR, nsh, Nat, Nshl; bool mobile, photons; };
 
 template <class T>
 struct Layout {
-    McConst<T>* dC; Ctrs* ctr; T* tg; T* Rg; int* th; int* rh; double* V; int* hmap;
+    Ctrs* ctr; T* tg; T* Rg; int* th; int* rh; double* V; int* hmap;
     unsigned long long* tall; size_t n_all; Tal tal;
     double *hstage, *hn, *hE, *hK, *htn, *htE; size_t hstage_n;
     double* calls; size_t calls_n;
@@ -125,7 +125,6 @@ struct Layout {
 // Lays the whole call out in `c`; returns the bytes used.
 template <class T>
 size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
-    L.dC = c.take<McConst<T>>(1);
     L.ctr = c.take<Ctrs>(1);
     L.tg = c.take<T>((size_t)s.Nt);
     L.Rg = c.take<T>((size_t)s.NR);
@@ -234,6 +233,7 @@ void fill_const(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, McCon
     C.mobile_holes = m.hole_mass < 1e3;
     C.mec2 = (T)(kMe * kC * kC / kE);
     C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
+    finish_const(C);
 }
 
 // Host values to the device through a fixed stack buffer (pageable copies are
@@ -324,7 +324,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     launch_grid_hints<T>(C, L.th, L.rh, strm);
 
     const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
-    const int bs = cfg.block_size > 0 ? std::min(cfg.block_size, 256) : 256;
+    const int bs = cfg.block_size > 0 ? std::max(32, std::min(cfg.block_size, 256) & ~31) : 256;   // whole warps
     const int rare_blocks = 2 * 152;
     int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 256);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
@@ -336,21 +336,19 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     while (done < cfg.NMC) {
         const int nb = std::min(B, cfg.NMC - done);
         C.it0 = cfg.iteration_offset + done;
-        NA_CK(cudaMemcpyAsync(L.dC, &C, sizeof C, cudaMemcpyHostToDevice, strm));
-        h2d += sizeof C;
         NA_CK(cudaMemsetAsync(L.tall, 0, 8 * L.n_all, strm));
         NA_CK(cudaMemsetAsync(L.ctr, 0, sizeof(Ctrs), strm));
         QSet<T>* in = &L.qa;
         QSet<T>* ot = &L.qb;
         uint64_t bl = 0, bsteps = 0;
-        launch_shi<T>(L.dC, sh, L.evs, L.cap_ev, L.ctr, nb, strm);
+        launch_shi<T>(C, sh, L.evs, L.cap_ev, L.ctr, nb, strm);
         ++bl;
         NA_CK(cudaGetLastError());
         NA_CK(cudaMemcpyAsync(&hc, L.ctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
         NA_CK(cudaStreamSynchronize(strm));
         d2h += sizeof hc;
         if (!hc.overflow) {
-            launch_pairs<T>(L.dC, tb, L.evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)L.cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], L.tal,
+            launch_pairs<T>(C, tb, L.evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)L.cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], L.tal,
                             L.ctr, strm);
             ++bl;
             NA_CK(cudaGetLastError());
@@ -365,7 +363,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
             std::swap(in, ot);
             const int n_in[4] = {hc.n_out[Q_E], hc.n_out[Q_HVB], hc.n_out[Q_HDEEP], hc.n_out[Q_P]};
             NA_CK(cudaMemsetAsync(L.ctr, 0, NQ * sizeof(int), strm));
-            launch_step<T>(L.dC, tb, *in, n_in, *ot, L.e_inel, L.h_inel, L.tal, L.ctr, K, bs, rare_blocks, strm);
+            launch_step<T>(C, tb, *in, n_in, *ot, L.e_inel, L.h_inel, L.tal, L.ctr, K, bs, rare_blocks, strm);
             bl += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0); ++bsteps;
             NA_CK(cudaGetLastError());
             NA_CK(cudaMemcpyAsync(&hc, L.ctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
