@@ -77,7 +77,13 @@ static int make_fast(Buffers& b, const std::vector<double>& E, const std::vector
     const int n = (int)E.size(), nb = 4096;
     std::vector<double> lE(n), lL(n), Et(n);
     for (int i = 0; i < n; ++i) { lE[i] = std::log(E[i]); lL[i] = std::log(L[i]); Et[i] = (double)(T)E[i]; }
-    f.E = upload<T>(b, E); f.L = upload<T>(b, L); f.lE = upload<T>(b, lE); f.lL = upload<T>(b, lL);
+    f.E = upload<T>(b, E);
+    std::vector<FNode<T>> nodes(n);
+    for (int i = 0; i < n; ++i) nodes[i] = FNode<T>{(T)E[i], (T)lE[i], (T)lL[i], (T)L[i]};
+    FNode<T>* dn = (FNode<T>*)b.alloc(sizeof(FNode<T>) * std::max(n, 1));
+    if (dn && n > 0 && cudaMemcpy(dn, nodes.data(), sizeof(FNode<T>) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+        return TREKIS_ECUDA;
+    f.node = dn;
     const double lo = std::log(E[0]) - 0.5, hi = std::log(E[n - 1]) + 0.5;
     const double inv = nb / (hi - lo);
     std::vector<uint16_t> h(nb);
@@ -86,7 +92,7 @@ static int make_fast(Buffers& b, const std::vector<double>& E, const std::vector
         h[q] = (uint16_t)find_mono_h2(Et.data(), n, eb);
     }
     uint16_t* d = (uint16_t*)b.alloc(2 * nb);
-    if (!d || !f.E || !f.L || !f.lE || !f.lL) return TREKIS_ENOMEM;
+    if (!d || !f.E || !f.node) return TREKIS_ENOMEM;
     if (cudaMemcpy(d, h.data(), 2 * nb, cudaMemcpyHostToDevice) != cudaSuccess) return TREKIS_ECUDA;
     f.hint = d; f.lo = (T)lo; f.inv = (T)inv; f.n = n; f.nb = nb;
     return TREKIS_OK;
@@ -334,7 +340,7 @@ struct Workspace {
     Tal tal;
     Ctrs* ctr = nullptr;
     T *tg = nullptr, *Rg = nullptr;
-    int *th = nullptr, *rh = nullptr;   // grid bucket hints
+    GHint<T> *th = nullptr, *rh = nullptr;   // grid bucket hints
     double* V = nullptr;
     int* hmap = nullptr;
     double *hstage = nullptr, *hn = nullptr, *hE = nullptr, *hK = nullptr, *htn = nullptr, *htE = nullptr;
@@ -397,8 +403,8 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     w->ctr = (Ctrs*)b.alloc(sizeof(Ctrs));
     w->tg = (T*)b.alloc(sizeof(T) * Nt);
     w->Rg = (T*)b.alloc(sizeof(T) * NR);
-    w->th = (int*)b.alloc(sizeof(int) * (2 * (size_t)Nt + 2));
-    w->rh = (int*)b.alloc(sizeof(int) * kRgHintMax);
+    w->th = (GHint<T>*)b.alloc(sizeof(GHint<T>) * (2 * (size_t)Nt + 2));
+    w->rh = (GHint<T>*)b.alloc(sizeof(GHint<T>) * kRgHintMax);
     if (!w->th || !w->rh) return nullptr;
     w->V = (double*)b.alloc(8 * NR);
     w->hmap = (int*)b.alloc(sizeof(int) * nsh);

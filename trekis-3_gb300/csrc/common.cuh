@@ -222,29 +222,36 @@ __device__ __forceinline__ T nfp1(const Tab<T>& t, T E) {
 
 // Next_free_path_2d on a FastTab: same result as nfp2 (same comparisons,
 // same log-log formula with precomputed logs); lx = log(E) is shared.
-template <class T>
-__device__ __forceinline__ int fast_find(const FastTab<T>& t, T E, T lx) {
-    if (!(E > T(0))) return find_monoton(t.E, t.n, E);
-    int b = (int)m_floor((lx - t.lo) * t.inv) - 1;
-    b = b < 0 ? 0 : (b >= t.nb ? t.nb - 1 : b);
-    int j = t.hint[b];
-    while (j < t.n && t.E[j - 1] <= E) ++j;
-    return j;
-}
+// The walk carries the nodes it passes, so the bracketing interval
+// (n-2, n-1) is in registers when it stops.
 template <class T>
 __device__ __forceinline__ T nfp2_fast(const FastTab<T>& t, T E, T lx) {
-    const int n = fast_find(t, E, lx);
-    if (n == 1) {
-        T M = interp<T>(1, t.E[0], t.E[1], t.L[0], t.L[1], E);
-        return M < t.L[0] ? t.L[0] : M;
+    int n;
+    FNode<T> lo, hi;
+    if (E > T(0)) {
+        int b = (int)m_floor((lx - t.lo) * t.inv) - 1;
+        b = b < 0 ? 0 : (b >= t.nb ? t.nb - 1 : b);
+        n = t.hint[b];
+        hi = t.node[n - 1];
+        lo = t.node[n > 1 ? n - 2 : 0];
+        while (n < t.n && hi.E <= E) { lo = hi; ++n; hi = t.node[n - 1]; }
+    } else {
+        n = find_monoton(t.E, t.n, E);
+        hi = t.node[n - 1];
+        lo = t.node[n > 1 ? n - 2 : 0];
     }
-    const T L1 = t.L[n - 2];
+    if (n == 1) {
+        const FNode<T> a = t.node[0], c = t.node[1];
+        T M = interp<T>(1, a.E, c.E, a.L, c.L, E);
+        return M < a.L ? a.L : M;
+    }
+    const T L1 = lo.L;
     if (L1 >= T(1.0e16)) return L1;
-    const T L2 = t.L[n - 1], E1 = t.E[n - 2], E2 = t.E[n - 1];
+    const T L2 = hi.L, E1 = lo.E, E2 = hi.E;
     if (m_abs(E2 - E1) < T(1.0e-6)) return L1 > L2 ? L1 : L2;
     if (E == E1) return L1;
-    const T l1 = t.lE[n - 2];
-    return f_exp(t.lL[n - 2] + (t.lL[n - 1] - t.lL[n - 2]) / (t.lE[n - 1] - l1) * (lx - l1));
+    const T l1 = lo.lE;
+    return f_exp(lo.lL + (hi.lL - lo.lL) / (hi.lE - l1) * (lx - l1));
 }
 
 }  // namespace tk

@@ -36,10 +36,14 @@ struct BuildMat {
 // A mean-free-path table prepared for the hot loop: logarithms of both
 // columns (one exp per log-log interpolation) and a bucket index over log(E)
 // whose entry never exceeds the bisection result, so a short forward walk
-// returns exactly the index of Find_in_monotonous_1D_array.
+// returns exactly the index of Find_in_monotonous_1D_array.  Each node keeps
+// E, log E, log L and L together, so an interval is two vector loads.
+template <class T>
+struct alignas(4 * sizeof(T)) FNode { T E, lE, lL, L; };
 template <class T>
 struct FastTab {
-    const T* E; const T* L; const T* lE; const T* lL;
+    const T* E;            // node energies alone (the bisection fallback)
+    const FNode<T>* node;
     const uint16_t* hint;
     T lo, inv;
     int n, nb;

@@ -103,8 +103,12 @@ __device__ __forceinline__ int rbin(const McConst<T>& C, T R) {
     if (!(R >= C.rg_lo)) return (R < C.rg_lo) ? 1 : find_monoton(C.Rg, C.NR, R);   // below, or NaN
     if (R >= C.rg_hi) return C.NR;
     if (!C.rg_hint) return find_monoton(C.Rg, C.NR, R);
-    int j = C.rg_hint[(int)radius_key(R) - C.rg_key0];
-    while (j < C.NR && C.Rg[j - 1] <= R) ++j;
+    const GHint<T> h = C.rg_hint[(int)radius_key(R) - C.rg_key0];
+    int j = h.j;
+    if (j < C.NR && h.b1 <= R) {
+        ++j;
+        if (j < C.NR && h.b2 <= R) { ++j; while (j < C.NR && C.Rg[j - 1] <= R) ++j; }
+    }
     return j;
 }
 // find_monoton over the tallied times, by a uniform bucket hint
@@ -114,8 +118,12 @@ __device__ __forceinline__ int tbin(const McConst<T>& C, T t) {
     if (t >= C.tg_hi) return C.Nt;
     int b = (int)(t * C.tg_inv) - 1;   // one bucket of margin for the rounding of t * inv
     b = b < 0 ? 0 : (b >= C.tg_nb ? C.tg_nb - 1 : b);
-    int j = C.tg_hint[b];
-    while (j < C.Nt && C.tg[j - 1] <= t) ++j;
+    const GHint<T> h = C.tg_hint[b];
+    int j = h.j;
+    if (j < C.Nt && h.b1 <= t) {
+        ++j;
+        if (j < C.Nt && h.b2 <= t) { ++j; while (j < C.Nt && C.tg[j - 1] <= t) ++j; }
+    }
     return j;
 }
 
@@ -1475,25 +1483,34 @@ template void launch_step<double>(const McConst<double>&, const DevTabs<double>&
 // hint of a bucket = the search result at the bucket's lowest value, which
 // never exceeds the result of any value the lookup maps to that bucket
 template <class T>
-__global__ void k_grid_hints(const T* tg, int Nt, T tg_inv, int* th, int tnb, const T* Rg, int NR, int key0,
-                             int* rh, int rnb) {
+__device__ __forceinline__ GHint<T> grid_hint(const T* g, int N, T v) {
+    GHint<T> h;
+    h.j = find_monoton(g, N, v);
+    h.b1 = g[h.j < N ? h.j - 1 : N - 1];
+    h.b2 = g[h.j + 1 < N ? h.j : N - 1];
+    h.pad_ = 0;
+    return h;
+}
+template <class T>
+__global__ void k_grid_hints(const T* tg, int Nt, T tg_inv, GHint<T>* th, int tnb, const T* Rg, int NR, int key0,
+                             GHint<T>* rh, int rnb) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < tnb) th[b] = find_monoton(tg, Nt, T(b) / tg_inv);
+    if (b < tnb) th[b] = grid_hint(tg, Nt, T(b) / tg_inv);
     if (rh && b < rnb) {
         T lo;
         if constexpr (sizeof(T) == 4) lo = __uint_as_float((uint32_t)(key0 + b) << 19);
         else lo = __longlong_as_double((long long)((uint64_t)(uint32_t)(key0 + b) << 48));
-        rh[b] = find_monoton(Rg, NR, lo);
+        rh[b] = grid_hint(Rg, NR, lo);
     }
 }
 template <class T>
-void launch_grid_hints(const McConst<T>& C, int* th, int* rh, cudaStream_t s) {
+void launch_grid_hints(const McConst<T>& C, GHint<T>* th, GHint<T>* rh, cudaStream_t s) {
     const int n = C.tg_nb > C.rg_nb ? C.tg_nb : C.rg_nb;
     k_grid_hints<T><<<(n + 127) / 128, 128, 0, s>>>(C.tg, C.Nt, C.tg_inv, th, C.tg_nb, C.Rg, C.NR, C.rg_key0,
                                                     C.rg_nb ? rh : nullptr, C.rg_nb);
 }
-template void launch_grid_hints<float>(const McConst<float>&, int*, int*, cudaStream_t);
-template void launch_grid_hints<double>(const McConst<double>&, int*, int*, cudaStream_t);
+template void launch_grid_hints<float>(const McConst<float>&, GHint<float>*, GHint<float>*, cudaStream_t);
+template void launch_grid_hints<double>(const McConst<double>&, GHint<double>*, GHint<double>*, cudaStream_t);
 
 // ---- finalize: difference arrays -> FP64 tallies -----------------------------------------
 // One thread per (slice, bin): prefix over time rows, in place (exact int64).

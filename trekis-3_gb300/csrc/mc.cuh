@@ -7,6 +7,12 @@
 
 namespace tk {
 
+// One bucket of a grid search hint: the search result j at the bucket's
+// lowest value and the next two grid values g[j-1], g[j], so that a lookup
+// usually advances past them without reading the grid.
+template <class T>
+struct alignas(16) GHint { T b1, b2; int j, pad_; };
+
 // Run constants, in the precision T of the kinematics (SHI quantities stay FP64).
 template <class T>
 struct McConst {
@@ -27,10 +33,10 @@ struct McConst {
     const T* Rg;        // [NR] outer radii
     // bucket hints that turn the time and radius searches into a short
     // forward walk (same index as the bisection; see launch_grid_hints)
-    const int* tg_hint; // [tg_nb] over [0, tg_hi), buckets of width 1/tg_inv
+    const GHint<T>* tg_hint; // [tg_nb] over [0, tg_hi), buckets of width 1/tg_inv
     T tg_lo, tg_hi, tg_inv;
     int tg_nb;
-    const int* rg_hint; // [rg_nb] by the top bits of R (16 buckets per octave); null: bisection
+    const GHint<T>* rg_hint; // [rg_nb] by the top bits of R (16 buckets per octave); null: bisection
     T rg_lo, rg_hi;
     int rg_key0, rg_nb;
     uint64_t seed;
@@ -187,7 +193,7 @@ inline void set_grid_hint_sizes(McConst<T>& C, T tg_first, T tg_last, T rg_first
 }
 // fills th[C.tg_nb] and rh[C.rg_nb] from the device grids C.tg, C.Rg
 template <class T>
-void launch_grid_hints(const McConst<T>& C, int* th, int* rh, cudaStream_t s);
+void launch_grid_hints(const McConst<T>& C, GHint<T>* th, GHint<T>* rh, cudaStream_t s);
 
 void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
                const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s);

@@ -112,7 +112,7 @@ struct Shape { int Nt, NR, nsh, Nat, Nshl; bool mobile, photons; };
 
 template <class T>
 struct Layout {
-    Ctrs* ctr; T* tg; T* Rg; int* th; int* rh; double* V; int* hmap;
+    Ctrs* ctr; T* tg; T* Rg; GHint<T>* th; GHint<T>* rh; double* V; int* hmap;
     unsigned long long* tall; size_t n_all; Tal tal;
     double *hstage, *hn, *hE, *hK, *htn, *htE; size_t hstage_n;
     double* calls; size_t calls_n;
@@ -128,8 +128,8 @@ size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
     L.ctr = c.take<Ctrs>(1);
     L.tg = c.take<T>((size_t)s.Nt);
     L.Rg = c.take<T>((size_t)s.NR);
-    L.th = c.take<int>(2 * (size_t)s.Nt + 2);
-    L.rh = c.take<int>((size_t)kRgHintMax);
+    L.th = c.take<GHint<T>>(2 * (size_t)s.Nt + 2);
+    L.rh = c.take<GHint<T>>((size_t)kRgHintMax);
     L.V = c.take<double>((size_t)s.NR);
     L.hmap = c.take<int>((size_t)s.nsh);
     const size_t rows = (size_t)s.Nt + 2;
