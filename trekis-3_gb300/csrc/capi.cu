@@ -177,6 +177,27 @@ static int upload_mc(trekis_tables* t, DevTabs<T>& d) {
     d.dosD = upload<T>(b, t->dos_D);
     d.dosI = upload<T>(b, t->dos_I);
     d.dosM = upload<T>(b, t->dos_M);
+    d.dos_hint = nullptr; d.dos_nb = 0;
+    if (d.nD >= 2 && t->dos_E.back() > t->dos_E.front()) {
+        // the hint of a bucket is the search result at its lowest value, on the
+        // grid as stored in precision T; lookups start one bucket lower
+        const int nD = d.nD, nb = 4 * nD;
+        std::vector<double> gt(nD);
+        for (int i = 0; i < nD; ++i) gt[i] = (double)(T)t->dos_E[i];
+        const double lo = gt[0], inv = nb / (gt[nD - 1] - gt[0]);
+        std::vector<GHint<T>> h(nb);
+        for (int q = 0; q < nb; ++q) {
+            const int j = find_mono_h2(gt.data(), nD, (double)(T)(lo + q / inv));
+            h[q] = GHint<T>{(T)gt[j < nD ? j - 1 : nD - 1], (T)gt[j + 1 < nD ? j : nD - 1], j, 0};
+        }
+        GHint<T>* dh = (GHint<T>*)b.alloc(sizeof(GHint<T>) * nb);
+        if (!dh || cudaMemcpy(dh, h.data(), sizeof(GHint<T>) * nb, cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("table upload failed");
+            return TREKIS_ENOMEM;
+        }
+        d.dos_hint = dh; d.dos_nb = nb;
+        d.dos_lo = (T)lo; d.dos_hi = (T)gt[nD - 1]; d.dos_inv = (T)inv;
+    }
     if (!d.elE || !d.elL || !d.row_off || !d.hE || !d.dosE) { set_error("table upload failed"); return TREKIS_ENOMEM; }
     return TREKIS_OK;
 }

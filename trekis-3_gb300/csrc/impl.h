@@ -40,6 +40,12 @@ struct BuildMat {
 // E, log E, log L and L together, so an interval is two vector loads.
 template <class T>
 struct alignas(4 * sizeof(T)) FNode { T E, lE, lL, L; };
+
+// One bucket of a grid search hint: the search result j at the bucket's
+// lowest value and the next two grid values g[j-1], g[j], so that a lookup
+// usually advances past them without reading the grid.
+template <class T>
+struct alignas(16) GHint { T b1, b2; int j, pad_; };
 template <class T>
 struct FastTab {
     const T* E;            // node energies alone (the bisection fallback)
@@ -78,6 +84,9 @@ struct DevTabs {
     const T* pIMFP;
     // DOS
     const T* dosE; const T* dosD; const T* dosI; const T* dosM; int nD;
+    const GHint<T>* dos_hint;   // uniform buckets over [dosE[0], dosE[nD-1]); null: bisection
+    T dos_lo, dos_hi, dos_inv;
+    int dos_nb;
 };
 
 // SHI tables in the precision of the run, with host-precomputed logarithms so

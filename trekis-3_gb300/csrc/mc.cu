@@ -165,6 +165,22 @@ __device__ void flush_run(const McConst<T>& C, const Tal& tal, int kind, int sh,
     }
 }
 
+// find_monoton over the DOS energies, by a uniform bucket hint
+template <class T>
+__device__ __forceinline__ int dos_find(const DevTabs<T>& tb, T E) {
+    if (!tb.dos_hint || !(E >= tb.dos_lo)) return find_monoton(tb.dosE, tb.nD, E);   // below, NaN, no hint
+    if (E >= tb.dos_hi) return tb.nD;
+    int b = (int)((E - tb.dos_lo) * tb.dos_inv) - 1;
+    b = b < 0 ? 0 : (b >= tb.dos_nb ? tb.dos_nb - 1 : b);
+    const GHint<T> h = tb.dos_hint[b];
+    int j = h.j;
+    if (j < tb.nD && h.b1 <= E) {
+        ++j;
+        if (j < tb.nD && h.b2 <= E) { ++j; while (j < tb.nD && tb.dosE[j - 1] <= E) ++j; }
+    }
+    return j;
+}
+
 // 1-degree bin of a polar angle on the grid 1..180 (Find_in_array_monoton)
 template <class T>
 __device__ __forceinline__ int theta_bin(T th) {
@@ -382,7 +398,7 @@ __device__ T from_where_in_vb(const DevTabs<T>& tb, S& s, bool hasE, T E) {
     T sum;
     if (!hasE) sum = tb.dosI[N - 1];
     else {
-        int Mt = (E < tb.dosE[N - 1]) ? find_monoton(tb.dosE, N, E) : N + 1;
+        int Mt = (E < tb.dosE[N - 1]) ? dos_find(tb, E) : N + 1;
         if (Mt <= 1) return T(0);
         sum = tb.dosI[Mt - 2];
     }
@@ -400,7 +416,7 @@ __device__ T electron_receives(const McConst<T>& C, const DevTabs<T>& tb, T dE, 
     T out = E;
     if (k == C.vb && tb.nD > 0 && dE > C.Ip[k]) {
         const int N = tb.nD;
-        int Mt = (E < tb.dosE[N - 1]) ? find_monoton(tb.dosE, N, E) : N + 1;
+        int Mt = (E < tb.dosE[N - 1]) ? dos_find(tb, E) : N + 1;
         if (Mt > 1) {
             T sum = tb.dosI[Mt - 2];
             T Tot = s.next() * sum;
@@ -425,7 +441,7 @@ __device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>&
         h.Ek = Eh - C.Egap;
         h.E = C.Egap;
         if (C.hole_mass > T(0)) h.M = C.hole_mass;
-        else h.M = tb.dosM[find_monoton(tb.dosE, tb.nD, h.Ek) - 1];
+        else h.M = tb.dosM[dos_find(tb, h.Ek) - 1];
         if (h.M < T(1.0e3)) {
             const T lx = f_log(h.Ek);
             const T HI = nfp2_fast(tb.fHIMFP, h.Ek, lx);
@@ -623,7 +639,7 @@ __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hol
     if (Emin <= T(1.0e-3)) Emin = T(1.0e-3);
     T Emax, Mass;
     if (hole) {
-        Mass = (C.hole_mass >= T(0)) ? C.hole_mass : tb.dosM[find_monoton(tb.dosE, tb.nD, Ele) - 1];
+        Mass = (C.hole_mass >= T(0)) ? C.hole_mass : tb.dosM[dos_find(tb, Ele) - 1];
         Emax = T(4) * Ele * Mass / ((Mass + T(1)) * (Mass + T(1)));
     } else Emax = (Ele + Emin) / T(2);
     T E = hole ? interp_transfer(tb.hE, tb.nH, tb.hrow_off, tb.hrow_hw, tb.hrow_L, Ele, L_need, fg, tb.hrow_mono)
@@ -980,7 +996,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
 template <class T>
 __device__ T check_hole(const DevTabs<T>& tb, T Eel, T& dE, P<T>* el) {
     T Eh = Eel - dE;
-    int mh = find_monoton(tb.dosE, tb.nD, Eh);
+    int mh = dos_find(tb, Eh);
     if (tb.dosD[mh - 1] < T(1.0e-4)) {
         if (el) {
             while (mh > 1 && tb.dosD[mh - 1] < T(1.0e-4)) --mh;

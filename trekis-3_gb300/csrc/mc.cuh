@@ -7,12 +7,6 @@
 
 namespace tk {
 
-// One bucket of a grid search hint: the search result j at the bucket's
-// lowest value and the next two grid values g[j-1], g[j], so that a lookup
-// usually advances past them without reading the grid.
-template <class T>
-struct alignas(16) GHint { T b1, b2; int j, pad_; };
-
 // Run constants, in the precision T of the kinematics (SHI quantities stay FP64).
 template <class T>
 struct McConst {
