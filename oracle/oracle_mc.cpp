@@ -345,17 +345,23 @@ double mott_transfer(const Ctx& c, double Ee, double M_eff, Stream& s) {
     return dE / c.Psum;
 }
 
-// Update_particle_angles_lat (Monte_Carlo.f90:1252-1299)
-void angles_lat(const Ctx& c, double E, double W, double M_eff, Stream& s, double& theta, double& phi) {
+// Update_particle_angles_lat (Monte_Carlo.f90:1252-1299).  The azimuth takes
+// u_phi, the choice number of the collision recycled (elastic_uniform), where
+// the reference draws a fresh number.
+void angles_lat(const Ctx& c, double E, double W, double M_eff, Stream& s, double& theta, double& phi,
+                double u_phi) {
     double Ein = M_eff * me * cvel * cvel / e, Et = c.Mtarget * cvel * cvel / e;
     double E2mc = E + 2.0 * Ein, EmW = E - W;
     double W1 = E * E2mc - W * (E + Ein + Et), W2 = E * E2mc * EmW * (E2mc - W);
     double mu = (W2 > 0.0) ? W1 / std::sqrt(W2) : 0.0;
     if (std::fabs(mu) > 1.0) { double RN = s.next(); mu = std::cos(Pi * RN); }
     theta = std::acos(mu);
-    double RN2 = s.next();
-    phi = 2.0 * Pi * RN2;
+    phi = 2.0 * Pi * u_phi;
 }
+
+// Given x = RN (1/IMFP + 1/EMFP) >= 1/IMFP (an elastic collision),
+// (x - 1/IMFP) EMFP is uniform on [0, 1) and independent of the choice.
+double elastic_uniform(double x, double inv_I, double Em) { return (x - inv_I) * Em; }
 
 int rbin(const Ctx& c, double R) { return find_monoton(c.Rg.data(), c.NR, R); }
 
@@ -455,7 +461,8 @@ void electron_event(Ctx& c, int NOP, int i) {
     double Y = p0.Y + L * std::sin(th0) * std::cos(ph0);
     double Z = p0.Z + L * std::cos(th0);
     double dE, theta, phi;
-    if (RN * (1.0 / I + 1.0 / Em) < 1.0 / I) {  // inelastic
+    const double x = RN * (1.0 / I + 1.0 / Em);
+    if (x < 1.0 / I) {  // inelastic
         int A, S;
         which_shell(c, c.T->el, Eel, s, A, S);
         double Ish = next_free_path_1d(c.T->el[sidx(A, S)], Eel);
@@ -483,7 +490,7 @@ void electron_event(Ctx& c, int NOP, int i) {
         c.cnt[1]++;
     } else {  // elastic: Mott (kind_of_EMFP = 0) or phonon CDF (1)
         dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, false, Eel, s) : mott_transfer(c, Eel, 1.0, s);
-        angles_lat(c, Eel, dE, 1.0, s, theta, phi);
+        angles_lat(c, Eel, dE, 1.0, s, theta, phi, elastic_uniform(x, 1.0 / I, Em));
         c.At_NRG += dE;
         add_elat(c, i, X, Y, dE);
         c.cnt[2]++;
@@ -538,7 +545,8 @@ void hole_event(Ctx& c, int NOP, int i, double t_cur) {
         double Y = h0.Y + L * std::sin(th0) * std::cos(ph0);
         double Z = h0.Z + L * std::cos(th0);
         double dE, th1, ph1, Ehole;
-        if (RN * (1.0 / HI + 1.0 / HE) < 1.0 / HI && HI < 1e15) {  // inelastic
+        const double x = RN * (1.0 / HI + 1.0 / HE);
+        if (x < 1.0 / HI && HI < 1e15) {  // inelastic
             int A, S;
             which_shell(c, c.T->hole, Eel, s, A, S);
             double HIs = next_free_path_1d(c.T->hole[sidx(A, S)], Eel);
@@ -574,7 +582,8 @@ void hole_event(Ctx& c, int NOP, int i, double t_cur) {
             c.cnt[3]++;
         } else {  // elastic, Mott with the hole mass, or phonon CDF
             dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, true, Eel, s) : mott_transfer(c, Eel, hmass, s);
-            angles_lat(c, Eel, dE, hmass, s, th1, ph1);
+            // no ionisation channel (HI >= 1e15): RN chose nothing and is reused whole
+            angles_lat(c, Eel, dE, hmass, s, th1, ph1, HI < 1e15 ? elastic_uniform(x, 1.0 / HI, HE) : RN);
             Ehole = check_hole(c, Eel, dE, nullptr);
             c.At_NRG += dE;
             add_elat(c, i, X, Y, dE);

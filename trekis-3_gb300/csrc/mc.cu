@@ -587,9 +587,10 @@ __device__ T mott_transfer(const McConst<T>& C, T Ee, T M_eff, S& s) {
     }
 }
 
-// Update_particle_angles_lat (MC:1252-1299)
+// Update_particle_angles_lat (MC:1252-1299); u_phi is the azimuth's uniform
+// number (the recycled choice number of the collision, elastic_uniform)
 template <class T, class S>
-__device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& theta, T& phi) {
+__device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& theta, T& phi, T u_phi) {
     T Ein = M_eff * C.mec2, Et = (sizeof(T) == 4) ? C.Et_lat : C.Mtarget * T(kC) * T(kC) / T(kE);
     T E2mc = E + T(2) * Ein, EmW = E - W;
     T W1 = E * E2mc - W * (E + Ein + Et), W2 = E * E2mc * EmW * (E2mc - W);
@@ -598,8 +599,16 @@ __device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& thet
     else mu = (W2 > T(0)) ? W1 / m_sqrt(W2) : T(0);
     if (m_abs(mu) > T(1)) { T RN = s.next(); mu = f_cos(pi_<T>() * RN); }
     theta = m_acos(mu);
-    phi = T(2) * pi_<T>() * s.next();
+    phi = T(2) * pi_<T>() * u_phi;
 }
+
+// The number that chose the collision type, reused when the collision is
+// elastic: given x = RN (1/IMFP + 1/EMFP) >= 1/IMFP, u = (x - 1/IMFP) EMFP is
+// uniform on [0, 1) and independent of the choice, so it serves as the
+// azimuth draw of Update_particle_angles_lat (one number fewer per elastic
+// collision: four in all with two species, one Philox block).
+template <class T>
+__device__ __forceinline__ T elastic_uniform(T x, T inv_I, T Em) { return (x - inv_I) * Em; }
 
 // interpolate_transferred_energy (CS:1968-2045) over one table of cumulative rows.
 // fg >= 0: a proposed bracket position (fraction of the row) from the learned
@@ -939,7 +948,8 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     if (mc.hit(Eel)) { I = mc.I; Em = mc.Em; }
     else el_mfps(tb, Eel, I, Em);
     const T RN = s.next();
-    const bool ionise = RN * (T(1) / I + T(1) / Em) < T(1) / I;
+    const T x = RN * (T(1) / I + T(1) / Em);
+    const bool ionise = x < T(1) / I;
     if constexpr (!FULL) { if (ionise) return false; }
     p.ord = ord + 1;
     const T th0 = p.th, ph0 = p.ph, tev = p.tn;
@@ -972,7 +982,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         nev[1]++; nev[7] += 2;
     } else {  // elastic: Mott, or the phonon CDF
         dE = C.elast_cdf ? phonon_transfer(tb, false, Eel, s) : mott_transfer(C, Eel, T(1), s);
-        angles_lat(C, Eel, dE, T(1), s, theta, phi);
+        angles_lat(C, Eel, dE, T(1), s, theta, phi, elastic_uniform(x, T(1) / I, Em));
         const int i = ti0;  // the interval t_{i-1} <= t < t_i
         const int j = rbin(C, m_sqrt(X * X + Y * Y));
         lat.add(tal, (i - 1) * C.NR + (j - 1), dE);
@@ -1028,7 +1038,8 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         if (mc.hit(Eel)) { HI = mc.I; HE = mc.Em; }
         else h_mfps(tb, Eel, HI, HE);
         const T RN = s.next();
-        const bool ionise = RN * (T(1) / HI + T(1) / HE) < T(1) / HI && HI < T(1e15);
+        const T x = RN * (T(1) / HI + T(1) / HE);
+        const bool ionise = x < T(1) / HI && HI < T(1e15);
         if constexpr (!FULL) { if (ionise) return false; }
         h.ord = ord + 1;
         const T th0 = h.th, ph0 = h.ph, tev = h.tn, hm = h.M;
@@ -1073,7 +1084,8 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             nev[3]++; nev[7] += 2;
         } else {
             dE = C.elast_cdf ? phonon_transfer(tb, true, Eel, s) : mott_transfer(C, Eel, hm, s);
-            angles_lat(C, Eel, dE, hm, s, th1, ph1);
+            // no ionisation channel (HI >= 1e15): RN chose nothing and is reused whole
+            angles_lat(C, Eel, dE, hm, s, th1, ph1, HI < T(1e15) ? elastic_uniform(x, T(1) / HI, HE) : RN);
             Eh = check_hole(tb, Eel, dE, (P<T>*)nullptr);
             const int i = ti0;
             const int j = rbin(C, m_sqrt(X * X + Y * Y));
