@@ -352,7 +352,7 @@ int32_t trekis_mc_run_device_noalloc(const trekis_tables* t, const trekis_materi
  * quarters of the free device memory) unless its cfg sets queue_capacity,
  * and released at the end (trekis_tables_trim).  With autotune, the largest
  * instance of each material (among those without their own events_per_step)
- * first runs one probe iteration per candidate events_per_step (16, 32, 64)
+ * first runs one probe iteration per candidate events_per_step (32, 64, 128)
  * and all instances of that material take the fastest; the choices land in
  * tune[i] (may be NULL).  Returns the first instance's error, if any. */
 typedef struct {

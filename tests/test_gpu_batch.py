@@ -17,7 +17,7 @@ def test_batch_matches_single_runs(gpu_lib):
     opts = [api.RunOptions(precision=0, seed=41) for _ in ws]
     opts.append(api.RunOptions(precision=0, seed=41, iteration_offset=1000))
     tb, sb, tune = api.mc_run_batch(tables, opts, autotune=True, max_concurrent=3)
-    assert all(t_["events_per_step"] in (16, 32, 64) and t_["queue_capacity"] >= 1 << 16 for t_ in tune)
+    assert all(t_["events_per_step"] in (32, 64, 128) and t_["queue_capacity"] >= 1 << 16 for t_ in tune)
     total = 0
     for t, opt, got, st in zip(tables, opts, tb, sb):
         ref, sr = api.mc_run(t, opt)

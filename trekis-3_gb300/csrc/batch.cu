@@ -15,7 +15,7 @@
 //
 // Autotuning (optional): per material, the largest instance runs one probe
 // iteration per candidate compaction interval (events a particle runs before
-// it is re-queued: 16, 32, 64) on its own workspace before the batch starts;
+// it is re-queued: 32, 64, 128) on its own workspace before the batch starts;
 // every instance of that material runs with the fastest.  A probe call costs
 // about as much as a whole small instance (host-side tally staging), so
 // probing per instance would not pay.  The probes also report the live-
@@ -34,7 +34,7 @@
 namespace tk {
 namespace {
 
-constexpr int kProbeK[3] = {16, 32, 64};
+constexpr int kProbeK[3] = {32, 64, 128};
 constexpr double kBytesPerSlot = 480.0;   // device bytes per particle slot of a workspace (queues, side queues, SHI records)
 
 // host tallies of a run's shape, for probes whose results are dropped
@@ -200,7 +200,7 @@ extern "C" int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables, 
                 trekis_tune* tr = tune ? &tune[i] : nullptr;
                 if (tr) {
                     std::memset(tr, 0, sizeof *tr);
-                    tr->events_per_step = c.events_per_step > 0 ? c.events_per_step : 32;
+                    tr->events_per_step = c.events_per_step > 0 ? c.events_per_step : 64;
                     tr->block_size = c.block_size > 0 ? c.block_size : 256;
                     tr->queue_capacity = c.queue_capacity;
                 }

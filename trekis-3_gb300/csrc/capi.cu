@@ -548,7 +548,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         prop.net = *md; prop.guess = ws->guess; prop.err = ws->prop_err; prop.blocks = 152;
         pp = &prop;
     }
-    const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
+    const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 64;
     const int bs = cfg.block_size > 0 ? std::max(32, std::min(cfg.block_size, 256) & ~31) : 256;   // whole warps
     const int64_t cap = ws->cap;
     // the spectra hold one histogram per iteration of a batch

@@ -323,7 +323,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     C.tg_hint = L.th; C.rg_hint = C.rg_nb ? L.rh : nullptr;
     launch_grid_hints<T>(C, L.th, L.rh, strm);
 
-    const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 32;
+    const int K = cfg.events_per_step > 0 ? cfg.events_per_step : 64;
     const int bs = cfg.block_size > 0 ? std::max(32, std::min(cfg.block_size, 256) & ~31) : 256;   // whole warps
     const int rare_blocks = 2 * 152;
     int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 256);
