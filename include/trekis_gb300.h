@@ -431,6 +431,31 @@ int32_t trekis_mlp_train(trekis_tables* t, const trekis_mlp_cfg* cfg, trekis_mlp
 int32_t trekis_mlp_grad(const float* params, int64_t n, const float* X, const float* targets,
                         float* grad, double* loss);
 
+/* ---- output files --------------------------------------------------------
+ * Replaces the averaging of Universal_MC_for_SHI_MAIN.f90:281-314 and the
+ * files of Save_output (Source_files/Sorting_output_data.f90:340-1140).
+ * Names the reference takes from Target_atoms and the ion object. */
+typedef struct {
+    const char* out_dir;        /* Output_path: the run folder is created inside it   */
+    const char* ion_name;       /* SHI%Name, e.g. "Xe"                                 */
+    const char* material_name;  /* Material_name, for !Parameters.txt (may be null)   */
+    const char* atom_names[TREKIS_MAX_ATOMS];                   /* Target_atoms(i)%Name          */
+    const char* shell_names[TREKIS_MAX_ATOMS][TREKIS_MAX_SHELLS];  /* Target_atoms(i)%Shell_name(j) */
+    double  ion_Zeff;           /* equilibrium charge for !Parameters.txt (<0: omitted) */
+    double  duration_s;         /* wall time of the run for !Parameters.txt (<0: omitted) */
+    int32_t NMC;                /* iterations the sums cover (the divisor)             */
+    int32_t pad_;
+} trekis_output_cfg;
+
+/* Divides the un-normalised sums of a run (host tallies, as trekis_mc_run
+ * accumulates them) by NMC and writes the reference's output files into a new
+ * folder <out_dir>/<ion>_E_<MeV>_MeV_<Tim>_fs (with _1, _2, ... when taken),
+ * whose path is copied to folder[folder_cap].  The tallies are not modified.
+ * Values use the reference's edit descriptors (E25.16E3 for the default-width
+ * `e`, f10.2 times, f9.1 radii and energies).  Host only: needs no GPU. */
+int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_material* m, const trekis_ion* ion,
+                           const trekis_run_cfg* cfg, const trekis_tallies* t, char* folder, int32_t folder_cap);
+
 /* Human-readable text of the last error on this thread. */
 const char* trekis_last_error(void);
 

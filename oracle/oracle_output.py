@@ -1,0 +1,243 @@
+"""Test oracle for the output files: a Python restatement of the averaging in
+Universal_MC_for_SHI_MAIN.f90:281-314 and of the files Save_output writes
+(Sorting_output_data.f90:340-1140), used only by tests/ to check the
+library's writer byte for byte.  Numbers are formatted through the exact
+decimal value of each double (decimal module), independently of the C
+library's printf.
+
+Edit descriptors as the reference writes them: f10.2 (header times), f9.1
+(radii, energies), and `e` without a width, which for REAL(8) is E25.16E3
+under the compilers the reference builds with.
+"""
+import math
+import os
+from decimal import ROUND_HALF_EVEN, Decimal
+
+KB = 11604.0   # g_kb [K/eV], Universal_Constants.f90
+
+
+def fe(x, w=25, d=16, e=3):
+    """Fortran Ew.dEe with a leading '0.'."""
+    if not math.isfinite(x):
+        s = "NaN" if math.isnan(x) else ("Infinity" if x > 0 else "-Infinity")
+        return s.rjust(w) if len(s) <= w else "*" * w
+    if x == 0.0:
+        mant, k = "0" * d, 0
+    else:
+        dx = Decimal(abs(x))
+        k = dx.adjusted() + 1
+        q = dx.scaleb(-k).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+        if q >= 1:
+            k += 1
+            q = dx.scaleb(-k).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+        mant = format(q, "f")[2:]
+    ex = f"{abs(k):0{e}d}"
+    if len(ex) > e:
+        return "*" * w
+    s = ("-" if x < 0 else "") + "0." + mant + "E" + ("-" if k < 0 else "+") + ex
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def ff(x, w, d):
+    """Fortran Fw.d."""
+    q = Decimal(x).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+    s = format(q, "f")
+    if s.startswith("-") and q == 0:
+        s = s[1:] if x >= 0 else s
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def out_times(Tim, dt, dt_flag, N):
+    """Save_output's time grid (Sorting_output_data.f90:393-418)."""
+    if dt_flag <= 0:
+        n = math.ceil(Tim / dt) + 1
+        g = [dt]
+        for _ in range(n - 1):
+            g.append(min(g[-1] + dt, Tim))
+    else:
+        i, tg = 0, 0.01
+        while tg <= Tim:
+            i += 1
+            tg *= dt
+        g = [0.01]
+        for _ in range(i):
+            g.append(g[-1] * dt)
+        g[-1] = min(g[-1], Tim)
+    return (g + [g[-1]] * N)[:N]
+
+
+def vb_numbers(atoms):
+    """Find_VB_numbers (Reading_files_and_parameters.f90:3252-3268)."""
+    lo, res = 1e10, (0, 0)
+    for a, at in enumerate(atoms):
+        for s, sh in enumerate(at["shells"]):
+            if sh["Ip"] < lo or sh["designator"] >= 63:
+                lo, res = sh["Ip"], (a, s)
+            if sh["designator"] >= 63:
+                break
+    return res
+
+
+def write(out_dir, run, T, NMC):
+    """run: dict with ion (name, Z, Mass, E, Kind_Zeff, fixed_Zeff), material
+    (name, Dens, At_Dens, Layer, temp, hole_mass, kind_of_EMFP,
+    include_photons, dos_E, atoms=[{name, shells=[{name, designator, Ip}]}]),
+    Tim, dt, dt_flag, R, ion_Zeff, duration_s.  T: dict of the tally arrays
+    (Fortran order, un-normalised) and Nt, NR, Nat.  Returns the folder."""
+    ion, mat = run["ion"], run["material"]
+    N, NR, Nat = T["Nt"], T["NR"], T["Nat"]
+    inv = 1.0 / NMC
+    photons = bool(mat["include_photons"])
+    base = os.path.join(out_dir, f"{ion['name']}_E_{ff(ion['E'] / 1e6, 8, 2).strip()}_MeV_"
+                                 f"{ff(run['Tim'], 10, 2).strip()}_fs")
+    d, i = base, 0
+    while os.path.exists(d):
+        i += 1
+        d = f"{base}_{i}"
+    os.mkdir(d)
+    tg = out_times(run["Tim"], run["dt"], run["dt_flag"], N)
+    R = run["R"]
+
+    def a2(name, k, i):
+        return T[name][k + N * i] * inv
+
+    def a4(name, k, i, at, s):
+        return T[name][k + N * (i + NR * (at + Nat * s))] * inv
+
+    def header(first):
+        return first + "".join(ff(t, 10, 2) + "[fs]   " for t in tg) + " \n"
+
+    def radial(fname, val):
+        with open(os.path.join(d, fname), "w") as f:
+            f.write(header("#Radius[A] "))
+            for i in range(NR):
+                f.write(ff(R[i], 9, 1) + "".join(fe(val(k, i)) for k in range(N)) + " \n")
+
+    atoms = mat["atoms"]
+
+    def label(a, s):
+        sh = atoms[a]["shells"][s]
+        return f"{atoms[a]['name']}_{sh['name']}" if sh["designator"] < 63 else sh["name"]
+
+    # !Parameters.txt: the lines of print_parameters this boundary carries, then Save_output's
+    with open(os.path.join(d, "!Parameters.txt"), "w") as f:
+        if mat.get("name"):
+            f.write(f" Performing calculations for {ion['name']} in {mat['name']}\n")
+        f.write(f" Ion {ion['name']} (Element #{ion['Z']}, Mass {ff(ion['Mass'], 12, 3).strip()})\n")
+        f.write(f" With energy {ff(ion['E'] / 1e6, 9, 2).strip()} [MeV]\n")
+        f.write(f" Material density: {ff(mat['Dens'], 12, 3).strip()} [g/cm^3] or "
+                f"{fe(mat['At_Dens'], 16, 7, 2).strip()} [1/cm^3]\n")
+        f.write(f" Thickness of the analysed layer: {ff(mat['Layer'], 12, 3).strip()} [A]\n")
+        f.write(f" Temperature of the target: {ff(mat['temp'], 12, 3).strip()} [K]\n")
+        hm = mat["hole_mass"]
+        if hm > 0:
+            txt = ff(hm, 10, 2) if abs(hm) < 1e6 else fe(hm, 16, 7, 2)
+            f.write(f" Effective mass of valence holes: {txt.strip()} [me]\n")
+        else:
+            f.write(" Effective mass of valence holes is calculated from DOS\n")
+        f.write(f" Total time to be analysed: {ff(run['Tim'], 12, 3).strip()} [fs]\n")
+        if run["dt_flag"] <= 0:
+            f.write(f" with the timestep of {ff(run['dt'], 12, 3).strip()} [fs], linear time-scale\n")
+        else:
+            f.write(f" starting with 0.01 [fs] increasing by {ff(run['dt'], 12, 3).strip()} in logarithmic time-scale\n")
+        if ion["Kind_Zeff"] == 4:
+            f.write(f" Ion fixed charge {ff(ion['fixed_Zeff'], 7, 3).strip()} [e] is used with point-like charge model for SHI.\n")
+        else:
+            names = ["Barkas", "Bohr", "Nikolaev-Dmitriev", "Schiwietz-Grande"]
+            kz = ion["Kind_Zeff"] if 0 <= ion["Kind_Zeff"] < 4 else 0
+            f.write(f" Ion equilibrium charge is used with {names[kz]} formula, point-like charge model for SHI.\n")
+        f.write(" Elastic scattering: " + ("phonon CDF" if mat["kind_of_EMFP"] == 1 else "Mott atomic cross sections") + "\n")
+        f.write(f" Number of MC iterations: {NMC}\n")
+        if run["ion_Zeff"] >= 0:
+            f.write(f" Ion equilibrium charge:         {ff(run['ion_Zeff'], 6, 3).strip()} [electron charge]\n")
+        f.write(f" MC calculated energy loss (Se): {ff(T['Out_tot_E'][N - 1] * inv / mat['Layer'], 9, 2).strip()} [eV/A]\n")
+        if run["duration_s"] >= 0:
+            f.write(f" Duration of calculation:        {ff(run['duration_s'], 12, 3).strip()} [sec]\n")
+
+    def theta(fname, first, arr):
+        with open(os.path.join(d, fname), "w") as f:
+            f.write(header(first))
+            for i in range(180):
+                vals = "".join(fe(arr[k + (N + 1) * i] * inv if arr is not None else 0.0) for k in range(N))
+                f.write(fe(float(i + 1)) + vals + " \n")
+
+    theta("Electrons_theta_distribution.txt", "#Angle[deg] ", T.get("Out_theta"))
+    theta("VB_holes_theta_distribution.txt", "Angle[deg] ", T.get("Out_theta_h"))
+
+    with open(os.path.join(d, "Total_numbers.txt"), "w") as f:
+        f.write("#Time[fs]    Ne    Ne_Emitted    Energy[eV]     Energy_Emitted[eV]" + (" N_photons" if photons else "") + "\n")
+        for k in range(N):
+            row = [tg[k], T["Out_tot_Ne"][k] * inv, 0.0, T["Out_tot_E"][k] * inv, 0.0]
+            if photons:
+                row.append(T["Out_tot_Nphot"][k] * inv)
+            f.write("".join(fe(v) for v in row) + "\n")
+
+    with open(os.path.join(d, "Total_energies.txt"), "w") as f:
+        f.write("#Time[fs]    Electrons[eV]   Atoms[eV]   Field[eV]  " + ("Photons[eV] " if photons else ""))
+        for a, at in enumerate(atoms):
+            for s in range(len(at["shells"])):
+                f.write(label(a, s) + "[eV]    ")
+        f.write(" \n")
+        for k in range(N):
+            row = [tg[k], T["Out_E_e"][k] * inv, T["Out_E_at"][k] * inv, 0.0]
+            if photons:
+                row.append(T["Out_E_phot"][k] * inv)
+            for a, at in enumerate(atoms):
+                for s in range(len(at["shells"])):
+                    row.append(T["Out_E_h"][k + N * (a + Nat * s)] * inv)
+            f.write("".join(fe(v) for v in row) + " \n")
+
+    radial("Radial_electron_density[1_cm^-3].txt", lambda k, i: a2("Out_ne", k, i) * 1.0e24)
+    radial("Radial_electron_energy[eV_A^-3].txt", lambda k, i: a2("Out_Ee", k, i))
+    radial("Radial_electron_temperature[K].txt",
+           lambda k, i: a2("Out_Ee", k, i) / a2("Out_ne", k, i) * KB * 2.0 / 3.0 if a2("Out_ne", k, i) > 0 else 0.0)
+    if photons:
+        radial("Radial_photon_density[1_cm^-3].txt", lambda k, i: a2("Out_nphot", k, i) * 1.0e24)
+        radial("Radial_photon_energy[eV_A^-3].txt", lambda k, i: a2("Out_Ephot", k, i))
+
+    with open(os.path.join(d, "Electron_distribution_vs_E[1_eV].txt"), "w") as f:
+        f.write("#Energy[eV]   Spectrum[arb.units]\n")
+        f.write("#time[fs]:  " + "".join(ff(t, 10, 2) for t in tg) + " \n")
+        for i in range(NR):
+            f.write(ff(R[i], 9, 1) + "".join(fe(a2("Out_Ee_vs_E", k, i) if "Out_Ee_vs_E" in T else 0.0)
+                                             for k in range(N)) + " \n")
+    with open(os.path.join(d, "VB_holes_distribution_vs_E[1_eV].txt"), "w") as f:
+        f.write(header("#Energy[eV] "))
+        for i, e in enumerate(mat["dos_E"]):
+            f.write(ff(e, 9, 1) + "".join(fe(a2("Out_Eh_vs_E", k, i) if "Out_Eh_vs_E" in T else 0.0)
+                                          for k in range(N)) + " \n")
+
+    lat = [[0.0] * NR for _ in range(N)]
+    for i in range(NR):
+        c = 0.0
+        for k in range(N):
+            c += a2("Out_Elat", k, i)
+            lat[k][i] = c
+    va, vs = vb_numbers(atoms)
+    radial("Radial_Lattice_energy[eV_A^-3].txt", lambda k, i: lat[k][i])
+    radial("Radial_Track_energy[eV_A^-3].txt",
+           lambda k, i: lat[k][i] + a4("Out_Eh", k, i, va, vs) + a4("Out_Ehkin", k, i, va, vs))
+    radial("Radial_Lattice_temperature[K].txt", lambda k, i: lat[k][i] / (mat["At_Dens"] * 1e-24) * KB * 2.0 / 3.0)
+
+    for a, at in enumerate(atoms):
+        for s in range(len(at["shells"])):
+            radial(f"Radial_{label(a, s)}_holes_density[1_cm^-3].txt",
+                   lambda k, i, a=a, s=s: a4("Out_nh", k, i, a, s) * 1.0e24)
+    for a, at in enumerate(atoms):
+        for s, sh in enumerate(at["shells"]):
+            if sh["designator"] < 63:
+                radial(f"Radial_{label(a, s)}_holes_energy[eV_A^-3].txt",
+                       lambda k, i, a=a, s=s: a4("Out_Eh", k, i, a, s))
+            else:
+                radial(f"Radial_{label(a, s)}_holes_pot_energy[eV_A^-3].txt",
+                       lambda k, i, a=a, s=s: a4("Out_Eh", k, i, a, s))
+                radial(f"Radial_{label(a, s)}_holes_kin_energy[eV_A^-3].txt",
+                       lambda k, i, a=a, s=s: a4("Out_Ehkin", k, i, a, s))
+    for a, at in enumerate(atoms):
+        for s, sh in enumerate(at["shells"]):
+            if sh["designator"] == 63:
+                def tv(k, i, a=a, s=s):
+                    nh = a4("Out_nh", k, i, a, s)
+                    return a4("Out_Ehkin", k, i, a, s) / nh * KB * 2.0 / 3.0 if nh > 0 else 0.0
+                radial(f"Radial_{label(a, s)}_holes_temperature[K].txt", tv)
+    return d

@@ -1,0 +1,364 @@
+// output.cpp -- the run's output files as the reference writes them.
+//
+// Replaces the averaging of Universal_MC_for_SHI_MAIN.f90:281-314 (every sum
+// divided by NMC) and the files of Save_output
+// (Source_files/Sorting_output_data.f90:340-1140): a run folder named after
+// the ion, its energy and the analysed time, and in it one text file per
+// distribution, each a table over (radius or energy or angle) x (time).
+//
+// Numbers follow the reference's edit descriptors: f10.2 for the times of the
+// header, f9.1 for radii and energies, and the default-width `e` descriptor
+// for every value, which the compilers the reference builds with (ifort, and
+// gfortran with -fdec-format-defaults) give for REAL(8) as E25.16E3:
+// "  0.1234567890123456E+003".
+//
+// Written: !Parameters.txt (the run's parameters known to this library, the
+// ion's equilibrium charge, the MC energy loss and the duration),
+// Electrons_theta_distribution.txt, VB_holes_theta_distribution.txt,
+// Total_numbers.txt, Total_energies.txt, Radial_electron_density,
+// Radial_electron_energy, Radial_electron_temperature, Radial_photon_density
+// and _energy (with photons), Electron_distribution_vs_E,
+// VB_holes_distribution_vs_E, Radial_Lattice_energy, Radial_Track_energy,
+// Radial_Lattice_temperature, and per shell the holes' density, energy
+// (valence band: potential and kinetic) and the valence holes' temperature.
+// Not written: the copy of the input file (there is none at this boundary),
+// the electric-field and emission files (no fields, no emission on this
+// path) and Hole_mean_diffusion_coefficient.txt (not computed: the
+// reference's value depends on its OpenMP schedule).
+#include <sys/stat.h>
+#include <sys/types.h>
+
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "impl.h"
+
+namespace {
+
+constexpr double kKbOut = 11604.0;   // g_kb [K/eV] (Universal_Constants.f90)
+
+// Fortran Fw.d: right-justified, asterisks when the number does not fit
+std::string f_fmt(double x, int w, int d) {
+    char b[128];
+    std::snprintf(b, sizeof b, "%*.*f", w, d, x);
+    std::string s(b);
+    if ((int)s.size() > w) return std::string(w, '*');
+    return s;
+}
+
+// Fortran Ew.dEe with a leading "0.": sign, 0., d digits, E, sign, e digits
+std::string e_fmt(double x, int w = 25, int d = 16, int e = 3) {
+    std::string out;
+    if (!std::isfinite(x)) {
+        out = std::isnan(x) ? "NaN" : (x > 0 ? "Infinity" : "-Infinity");
+    } else {
+        std::string mant;
+        int ex = 0;
+        if (x == 0.0) {
+            mant = std::string(d, '0');
+        } else {
+            char b[64];
+            std::snprintf(b, sizeof b, "%.*e", d - 1, std::fabs(x));   // d.ddd...e+XX, d significant digits
+            const char* p = b;
+            std::string digits;
+            for (; *p && *p != 'e'; ++p)
+                if (*p >= '0' && *p <= '9') digits += *p;
+            ex = std::atoi(p + 1) + 1;   // 0.ddd form
+            mant = digits;
+        }
+        char es[16];
+        std::snprintf(es, sizeof es, "%c%0*d", ex < 0 ? '-' : '+', e, std::abs(ex));
+        if ((int)std::strlen(es) > e + 1) return std::string(w, '*');
+        out = std::string(x < 0 ? "-" : "") + "0." + mant + "E" + es;
+    }
+    if ((int)out.size() > w) return std::string(w, '*');
+    return std::string(w - out.size(), ' ') + out;
+}
+
+std::string trim(const std::string& s) {
+    size_t a = s.find_first_not_of(' '), b = s.find_last_not_of(' ');
+    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+struct Out {
+    FILE* f = nullptr;
+    bool ok = true;
+    explicit Out(const std::string& path) { f = std::fopen(path.c_str(), "w"); ok = f != nullptr; }
+    ~Out() { if (f) std::fclose(f); }
+    void put(const std::string& s) { if (f && std::fputs(s.c_str(), f) < 0) ok = false; }
+};
+
+// Save_output's time grid (Sorting_output_data.f90:393-418), first N points
+std::vector<double> out_times(double Tim, double dt, int dt_flag, int N) {
+    std::vector<double> g;
+    if (dt_flag <= 0) {
+        const int n = (int)std::ceil(Tim / dt) + 1;
+        g.assign(n, 0.0);
+        g[0] = dt;
+        for (int i = 0; i + 1 < n; ++i) g[i + 1] = std::fmin(g[i] + dt, Tim);
+    } else {
+        int i = 0;
+        double tg = 0.01;
+        while (tg <= Tim) { ++i; tg *= dt; }
+        g.assign(i + 1, 0.0);
+        g[0] = 0.01;
+        for (int k = 0; k + 1 < (int)g.size(); ++k) g[k + 1] = g[k] * dt;
+        g.back() = std::fmin(g.back(), Tim);
+    }
+    g.resize(N, g.empty() ? 0.0 : g.back());
+    return g;
+}
+
+}  // namespace
+
+extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_material* m, const trekis_ion* ion,
+                                      const trekis_run_cfg* cfg, const trekis_tallies* t, char* folder,
+                                      int32_t folder_cap) {
+    if (!oc || !m || !ion || !cfg || !t || !oc->out_dir || !oc->ion_name || oc->NMC <= 0 || !cfg->Out_R ||
+        t->Nt <= 0 || t->N_R != cfg->N_R || t->Nat != m->N_atoms || m->N_atoms < 1 ||
+        m->N_atoms > TREKIS_MAX_ATOMS) {
+        tk::set_error("invalid output arguments");
+        return TREKIS_EINVAL;
+    }
+    const int N = t->Nt, NR = t->N_R, Nat = t->Nat, Nshl = t->Nshl;
+    for (int a = 0; a < Nat; ++a) {
+        if (m->atoms[a].N_shl > Nshl || !oc->atom_names[a]) { tk::set_error("invalid output arguments"); return TREKIS_EINVAL; }
+        for (int s = 0; s < m->atoms[a].N_shl; ++s)
+            if (!oc->shell_names[a][s]) { tk::set_error("missing shell name"); return TREKIS_EINVAL; }
+    }
+    const double inv = 1.0 / (double)oc->NMC;
+    const bool photons = m->include_photons != 0;
+    auto need = [&](const double* p, const char* what) {
+        if (!p) tk::set_error(std::string("tally array missing: ") + what);
+        return p != nullptr;
+    };
+    if (!need(t->Out_ne, "Out_ne") || !need(t->Out_Ee, "Out_Ee") || !need(t->Out_Elat, "Out_Elat") ||
+        !need(t->Out_nh, "Out_nh") || !need(t->Out_Eh, "Out_Eh") || !need(t->Out_Ehkin, "Out_Ehkin") ||
+        !need(t->Out_tot_Ne, "Out_tot_Ne") || !need(t->Out_tot_E, "Out_tot_E") || !need(t->Out_E_e, "Out_E_e") ||
+        !need(t->Out_E_at, "Out_E_at") || !need(t->Out_E_h, "Out_E_h") ||
+        (photons && (!need(t->Out_nphot, "Out_nphot") || !need(t->Out_Ephot, "Out_Ephot") ||
+                     !need(t->Out_tot_Nphot, "Out_tot_Nphot") || !need(t->Out_E_phot, "Out_E_phot"))))
+        return TREKIS_EINVAL;
+
+    // run folder: <ion>_E_<MeV f8.2>_MeV_<fs f10.2>_fs, then _1, _2, ... if taken
+    const std::string base = std::string(oc->out_dir) + "/" + trim(oc->ion_name) + "_E_" +
+                             trim(f_fmt(ion->E / 1e6, 8, 2)) + "_MeV_" + trim(f_fmt(cfg->Tim, 10, 2)) + "_fs";
+    std::string dir = base;
+    struct stat st;
+    for (int i = 1; stat(dir.c_str(), &st) == 0; ++i) dir = base + "_" + std::to_string(i);
+    if (mkdir(dir.c_str(), 0755) != 0) {
+        tk::set_error("cannot create " + dir + ": " + std::strerror(errno));
+        return TREKIS_EINVAL;
+    }
+    if (folder && folder_cap > 0) {
+        std::strncpy(folder, dir.c_str(), (size_t)folder_cap - 1);
+        folder[folder_cap - 1] = '\0';
+    }
+
+    const std::vector<double> tg = out_times(cfg->Tim, cfg->dt, cfg->dt_flag, N);
+    const double* R = cfg->Out_R;
+    auto at2 = [&](const double* a, int k, int i) { return a[(size_t)k + (size_t)N * i] * inv; };
+    auto at4 = [&](const double* a, int k, int i, int at, int s) {
+        return a[(size_t)k + (size_t)N * ((size_t)i + (size_t)NR * ((size_t)at + (size_t)Nat * s))] * inv;
+    };
+    auto time_header = [&](Out& o, const char* first) {
+        o.put(first);
+        for (int k = 0; k < N; ++k) o.put(f_fmt(tg[k], 10, 2) + "[fs]   ");
+        o.put(" \n");
+    };
+    bool ok = true;
+    // a table over radii x times of value(k, i)
+    auto radial = [&](const std::string& name, auto value) {
+        Out o(dir + "/" + name);
+        time_header(o, "#Radius[A] ");
+        for (int i = 0; i < NR; ++i) {
+            o.put(f_fmt(R[i], 9, 1));
+            for (int k = 0; k < N; ++k) o.put(e_fmt(value(k, i)));
+            o.put(" \n");
+        }
+        ok = ok && o.ok;
+    };
+    auto shell_label = [&](int a, int s) {
+        return m->atoms[a].Shl_num[s] < 63 ? trim(oc->atom_names[a]) + "_" + trim(oc->shell_names[a][s])
+                                           : trim(oc->shell_names[a][s]);
+    };
+
+    // !Parameters.txt (print_parameters, Sorting_output_data.f90:42-337, the
+    // fields this boundary carries; then the lines Save_output adds, :496-505)
+    {
+        Out o(dir + "/!Parameters.txt");
+        char b[512];
+        std::snprintf(b, sizeof b, " Ion %s (Element #%s, Mass %s)\n", trim(oc->ion_name).c_str(),
+                      trim(std::to_string(ion->Zat)).c_str(), trim(f_fmt(ion->Mass, 12, 3)).c_str());
+        if (oc->material_name) o.put(" Performing calculations for " + trim(oc->ion_name) + " in " + trim(oc->material_name) + "\n");
+        o.put(b);
+        o.put(" With energy " + trim(f_fmt(ion->E / 1e6, 9, 2)) + " [MeV]\n");
+        o.put(" Material density: " + trim(f_fmt(m->Dens, 12, 3)) + " [g/cm^3] or " + trim(e_fmt(m->At_Dens, 16, 7, 2)) +
+              " [1/cm^3]\n");
+        o.put(" Thickness of the analysed layer: " + trim(f_fmt(m->Layer, 12, 3)) + " [A]\n");
+        o.put(" Temperature of the target: " + trim(f_fmt(m->temp, 12, 3)) + " [K]\n");
+        if (m->hole_mass > 0)
+            o.put(" Effective mass of valence holes: " +
+                  trim(std::fabs(m->hole_mass) < 1e6 ? f_fmt(m->hole_mass, 10, 2) : e_fmt(m->hole_mass, 16, 7, 2)) +
+                  " [me]\n");
+        else
+            o.put(" Effective mass of valence holes is calculated from DOS\n");
+        o.put(" Total time to be analysed: " + trim(f_fmt(cfg->Tim, 12, 3)) + " [fs]\n");
+        if (cfg->dt_flag <= 0) o.put(" with the timestep of " + trim(f_fmt(cfg->dt, 12, 3)) + " [fs], linear time-scale\n");
+        else o.put(" starting with 0.01 [fs] increasing by " + trim(f_fmt(cfg->dt, 12, 3)) + " in logarithmic time-scale\n");
+        static const char* zn[] = {"Barkas", "Bohr", "Nikolaev-Dmitriev", "Schiwietz-Grande", "fixed"};
+        if (ion->Kind_Zeff == 4)
+            o.put(" Ion fixed charge " + trim(f_fmt(ion->fixed_Zeff, 7, 3)) + " [e] is used with point-like charge model for SHI.\n");
+        else
+            o.put(std::string(" Ion equilibrium charge is used with ") + zn[(ion->Kind_Zeff >= 0 && ion->Kind_Zeff < 4) ? ion->Kind_Zeff : 0] +
+                  " formula, point-like charge model for SHI.\n");
+        o.put(std::string(" Elastic scattering: ") + (m->kind_of_EMFP == 1 ? "phonon CDF" : "Mott atomic cross sections") + "\n");
+        o.put(" Number of MC iterations: " + std::to_string(oc->NMC) + "\n");
+        if (oc->ion_Zeff >= 0) o.put(" Ion equilibrium charge:         " + trim(f_fmt(oc->ion_Zeff, 6, 3)) + " [electron charge]\n");
+        o.put(" MC calculated energy loss (Se): " + trim(f_fmt(t->Out_tot_E[N - 1] * inv / m->Layer, 9, 2)) + " [eV/A]\n");
+        if (oc->duration_s >= 0) o.put(" Duration of calculation:        " + trim(f_fmt(oc->duration_s, 12, 3)) + " [sec]\n");
+        ok = ok && o.ok;
+    }
+
+    // angular distributions (:540-597)
+    auto theta = [&](const char* name, const char* first, const double* a) {
+        Out o(dir + "/" + name);
+        time_header(o, first);
+        for (int i = 0; i < 180; ++i) {
+            o.put(e_fmt((double)(i + 1)));
+            for (int k = 0; k < N; ++k) o.put(e_fmt(a ? a[(size_t)k + (size_t)(N + 1) * i] * inv : 0.0));
+            o.put(" \n");
+        }
+        ok = ok && o.ok;
+    };
+    theta("Electrons_theta_distribution.txt", "#Angle[deg] ", t->Out_theta);
+    theta("VB_holes_theta_distribution.txt", "Angle[deg] ", t->Out_theta_h);
+
+    // Total_numbers.txt (:625-647): no emission on this path, so Ne_Emitted and Energy_Emitted are 0
+    {
+        Out o(dir + "/Total_numbers.txt");
+        o.put(photons ? "#Time[fs]    Ne    Ne_Emitted    Energy[eV]     Energy_Emitted[eV] N_photons\n"
+                      : "#Time[fs]    Ne    Ne_Emitted    Energy[eV]     Energy_Emitted[eV]\n");
+        for (int k = 0; k < N; ++k) {
+            o.put(e_fmt(tg[k]) + e_fmt(t->Out_tot_Ne[k] * inv) + e_fmt(0.0) + e_fmt(t->Out_tot_E[k] * inv) + e_fmt(0.0));
+            if (photons) o.put(e_fmt(t->Out_tot_Nphot[k] * inv));
+            o.put("\n");
+        }
+        ok = ok && o.ok;
+    }
+
+    // Total_energies.txt (:671-705): no field, so Field[eV] is 0
+    {
+        Out o(dir + "/Total_energies.txt");
+        o.put(photons ? "#Time[fs]    Electrons[eV]   Atoms[eV]   Field[eV]  Photons[eV] "
+                      : "#Time[fs]    Electrons[eV]   Atoms[eV]   Field[eV]  ");
+        for (int a = 0; a < Nat; ++a)
+            for (int s = 0; s < m->atoms[a].N_shl; ++s) o.put(shell_label(a, s) + "[eV]    ");
+        o.put(" \n");
+        for (int k = 0; k < N; ++k) {
+            o.put(e_fmt(tg[k]) + e_fmt(t->Out_E_e[k] * inv) + e_fmt(t->Out_E_at[k] * inv) + e_fmt(0.0));
+            if (photons) o.put(e_fmt(t->Out_E_phot[k] * inv));
+            for (int a = 0; a < Nat; ++a)
+                for (int s = 0; s < m->atoms[a].N_shl; ++s)
+                    o.put(e_fmt(t->Out_E_h[(size_t)k + (size_t)N * ((size_t)a + (size_t)Nat * s)] * inv));
+            o.put(" \n");
+        }
+        ok = ok && o.ok;
+    }
+
+    // electrons (:708-787)
+    radial("Radial_electron_density[1_cm^-3].txt", [&](int k, int i) { return at2(t->Out_ne, k, i) * 1.0e24; });
+    radial("Radial_electron_energy[eV_A^-3].txt", [&](int k, int i) { return at2(t->Out_Ee, k, i); });
+    radial("Radial_electron_temperature[K].txt", [&](int k, int i) {
+        const double ne = at2(t->Out_ne, k, i);
+        return ne > 0.0 ? at2(t->Out_Ee, k, i) / ne * kKbOut * 2.0 / 3.0 : 0.0;
+    });
+    if (photons) {   // (:789-841)
+        radial("Radial_photon_density[1_cm^-3].txt", [&](int k, int i) { return at2(t->Out_nphot, k, i) * 1.0e24; });
+        radial("Radial_photon_energy[eV_A^-3].txt", [&](int k, int i) { return at2(t->Out_Ephot, k, i); });
+    }
+
+    // spectra (:847-900)
+    {
+        Out o(dir + "/Electron_distribution_vs_E[1_eV].txt");
+        o.put("#Energy[eV]   Spectrum[arb.units]\n");
+        o.put("#time[fs]:  ");
+        for (int k = 0; k < N; ++k) o.put(f_fmt(tg[k], 10, 2));
+        o.put(" \n");
+        for (int i = 0; i < NR; ++i) {
+            o.put(f_fmt(R[i], 9, 1));
+            for (int k = 0; k < N; ++k) o.put(e_fmt(t->Out_Ee_vs_E ? at2(t->Out_Ee_vs_E, k, i) : 0.0));
+            o.put(" \n");
+        }
+        ok = ok && o.ok;
+    }
+    {
+        Out o(dir + "/VB_holes_distribution_vs_E[1_eV].txt");
+        time_header(o, "#Energy[eV] ");
+        for (int i = 0; i < m->N_dos; ++i) {
+            o.put(f_fmt(m->dos_E[i], 9, 1));
+            for (int k = 0; k < N; ++k)
+                o.put(e_fmt(t->Out_Eh_vs_E && t->N_dos == m->N_dos ? at2(t->Out_Eh_vs_E, k, i) : 0.0));
+            o.put(" \n");
+        }
+        ok = ok && o.ok;
+    }
+
+    // lattice (:903-990): energy accumulated up to each grid time
+    std::vector<double> lat((size_t)N * NR);
+    for (int i = 0; i < NR; ++i) {
+        double c = 0.0;
+        for (int k = 0; k < N; ++k) { c += at2(t->Out_Elat, k, i); lat[(size_t)k + (size_t)N * i] = c; }
+    }
+    // Find_VB_numbers (Reading_files_and_parameters.f90:3252-3268)
+    int vb_a = 0, vb_s = 0;
+    {
+        double lo = 1e10;
+        for (int a = 0; a < Nat; ++a)
+            for (int s = 0; s < m->atoms[a].N_shl; ++s) {
+                if (m->atoms[a].Ip[s] < lo || m->atoms[a].Shl_num[s] >= 63) { lo = m->atoms[a].Ip[s]; vb_a = a; vb_s = s; }
+                if (m->atoms[a].Shl_num[s] >= 63) break;
+            }
+    }
+    radial("Radial_Lattice_energy[eV_A^-3].txt", [&](int k, int i) { return lat[(size_t)k + (size_t)N * i]; });
+    radial("Radial_Track_energy[eV_A^-3].txt", [&](int k, int i) {
+        return lat[(size_t)k + (size_t)N * i] + at4(t->Out_Eh, k, i, vb_a, vb_s) + at4(t->Out_Ehkin, k, i, vb_a, vb_s);
+    });
+    radial("Radial_Lattice_temperature[K].txt", [&](int k, int i) {
+        return lat[(size_t)k + (size_t)N * i] / (m->At_Dens * 1e-24) * kKbOut * 2.0 / 3.0;
+    });
+
+    // holes per shell (:992-1138)
+    for (int a = 0; a < Nat; ++a)
+        for (int s = 0; s < m->atoms[a].N_shl; ++s)
+            radial("Radial_" + shell_label(a, s) + "_holes_density[1_cm^-3].txt",
+                   [&](int k, int i) { return at4(t->Out_nh, k, i, a, s) * 1.0e24; });
+    for (int a = 0; a < Nat; ++a)
+        for (int s = 0; s < m->atoms[a].N_shl; ++s) {
+            if (m->atoms[a].Shl_num[s] < 63) {
+                radial("Radial_" + shell_label(a, s) + "_holes_energy[eV_A^-3].txt",
+                       [&](int k, int i) { return at4(t->Out_Eh, k, i, a, s); });
+            } else {
+                radial("Radial_" + shell_label(a, s) + "_holes_pot_energy[eV_A^-3].txt",
+                       [&](int k, int i) { return at4(t->Out_Eh, k, i, a, s); });
+                radial("Radial_" + shell_label(a, s) + "_holes_kin_energy[eV_A^-3].txt",
+                       [&](int k, int i) { return at4(t->Out_Ehkin, k, i, a, s); });
+            }
+        }
+    for (int a = 0; a < Nat; ++a)
+        for (int s = 0; s < m->atoms[a].N_shl; ++s)
+            if (m->atoms[a].Shl_num[s] == 63)
+                radial("Radial_" + shell_label(a, s) + "_holes_temperature[K].txt", [&](int k, int i) {
+                    const double nh = at4(t->Out_nh, k, i, a, s);
+                    return nh > 0.0 ? at4(t->Out_Ehkin, k, i, a, s) / nh * kKbOut * 2.0 / 3.0 : 0.0;
+                });
+    if (!ok) {
+        tk::set_error("writing the output files in " + dir + " failed");
+        return TREKIS_EINVAL;
+    }
+    return TREKIS_OK;
+}

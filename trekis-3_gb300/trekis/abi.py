@@ -113,6 +113,13 @@ class MlpReport(C.Structure):
 _DP = C.POINTER(C.c_double)
 
 
+class OutputCfg(C.Structure):
+    """trekis_output_cfg: names and divisor for the output files."""
+    _fields_ = [("out_dir", C.c_char_p), ("ion_name", C.c_char_p), ("material_name", C.c_char_p),
+                ("atom_names", C.c_char_p * MAX_ATOMS), ("shell_names", (C.c_char_p * MAX_SHELLS) * MAX_ATOMS),
+                ("ion_Zeff", C.c_double), ("duration_s", C.c_double), ("NMC", C.c_int32), ("pad_", C.c_int32)]
+
+
 class Tallies(C.Structure):
     _fields_ = [("Nt", C.c_int32), ("N_R", C.c_int32), ("Nat", C.c_int32), ("Nshl", C.c_int32)] + [
         (n, _DP) for n in (
@@ -171,6 +178,8 @@ SIGNATURES = {
     "trekis_mlp_train": (C.c_int32, [C.c_void_p, C.POINTER(MlpCfg), C.POINTER(MlpReport)]),
     "trekis_mlp_grad": (C.c_int32, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.POINTER(C.c_double)]),
+    "trekis_save_output": (C.c_int32, [C.POINTER(OutputCfg), C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
+                                       C.POINTER(Tallies), C.c_char_p, C.c_int32]),
     "trekis_last_error": (C.c_char_p, []),
 }
 

@@ -185,6 +185,67 @@ def mc_run(tables, opt=None, NMC=None, tallies=None):
     return tal, st
 
 
+# element symbols by Z (Target_atoms(i)%Name)
+ELEMENTS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br Kr "
+            "Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb "
+            "Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn Fr Ra Ac Th Pa U").split()
+
+
+def shell_name(designator):
+    """Shell name of an EADL designator, as define_PQN writes it
+    (Dealing_with_EADL.f90:1016-1150): K, L, L1, L23, L2, L3, M, ... ; 63 and
+    above is the valence band."""
+    d = int(designator)
+    if d >= 63:
+        return "Valence"
+    if d <= 1:
+        return "K-shell"
+    # per main shell: the whole shell, then its subshells in designator order
+    groups = [("L", ["1", "23", "2", "3"]), ("M", ["1", "23", "2", "3", "45", "4", "5"]),
+              ("N", ["1", "23", "2", "3", "45", "4", "5", "67", "6", "7"]),
+              ("O", ["1", "23", "2", "3", "45", "4", "5", "67", "6", "7", "89", "8", "9"]),
+              ("P", ["1", "23", "2", "3", "45", "4", "5", "67", "6", "7", "89", "8", "9", "1011", "10", "11"]),
+              ("Q", ["1", "23", "2", "3", "..."])]
+    code = 2
+    for letter, subs in groups:
+        if d == code:
+            return letter + "-shell"
+        code += 1
+        for sub in subs:
+            if d == code:
+                return letter + sub + "-shell"
+            code += 1
+    return "K-shell"
+
+
+def save_output(w, tallies, NMC, out_dir, ion_name=None, ion_Zeff=-1.0, duration_s=-1.0, opt=None, lib=None):
+    """Write the reference's output files (Save_output) for the un-normalised
+    sums of NMC iterations of workload w; returns the run folder's path.
+    Host code only (no GPU needed)."""
+    lib = lib or abi.load()
+    m = w.material
+    mat = m.to_c()
+    ion = ion_struct(w)
+    cfg, R = run_cfg(w, opt or RunOptions(), NMC)
+    enc = lambda x: x.encode()
+    keep = []
+    oc = abi.OutputCfg(out_dir=enc(str(out_dir)), ion_name=enc(ion_name or ELEMENTS[w.ion_Z - 1]),
+                       material_name=enc(m.name), ion_Zeff=ion_Zeff, duration_s=duration_s, NMC=int(NMC))
+    for a, atom in enumerate(m.atoms):
+        nm = enc(ELEMENTS[atom.Z - 1])
+        keep.append(nm)
+        oc.atom_names[a] = nm
+        for s_, sh in enumerate(atom.shells):
+            sn = enc(shell_name(sh.designator))
+            keep.append(sn)
+            oc.shell_names[a][s_] = sn
+    ct = tallies.c()
+    buf = C.create_string_buffer(4096)
+    abi.check(lib.trekis_save_output(C.byref(oc), mat.ref(), C.byref(ion), C.byref(cfg), C.byref(ct), buf,
+                                     len(buf)), lib)
+    return buf.value.decode()
+
+
 def train_proposal(tables, n_samples=1_000_000, epochs=3, batch=8192, lr=2e-3, E_lo=1.0, E_hi=1.0e5, seed=7,
                    n_eval_E=64, n_eval_u=1024):
     """Train the learned proposal of the energy-transfer draw on the GPU

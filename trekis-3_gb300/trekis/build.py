@@ -41,7 +41,7 @@ def _run(cmd):
 
 def build_library(verbose=False, extra=()):
     OUT.mkdir(exist_ok=True)
-    srcs = sorted(CSRC.glob("*.cu"))
+    srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))   # .cpp: host-only units
     deps = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "trekis_gb300.h"]
     newest_dep = max(p.stat().st_mtime for p in deps)
     objs = []
