@@ -208,3 +208,25 @@ def test_fp64_spectra_match_oracle(small1):
     plain, _ = api.mc_run(t, opt)
     for k in plain.a:
         assert np.array_equal(plain[k], g[k]), k
+
+
+@pytest.mark.gpu
+def test_output_files_of_a_gpu_run(small1, tmp_path):
+    """A GPU run's sums through trekis_save_output: the files hold the run's
+    tallies divided by NMC."""
+    import os
+    w, t, o = small1
+    opt = api.RunOptions(precision=1, seed=5)
+    NMC = 4
+    g, _ = api.mc_run(t, opt, NMC=NMC, tallies=api.new_tallies(w, spectra=True))
+    (tmp_path / "gpu").mkdir()
+    d = api.save_output(w, g, NMC, tmp_path / "gpu", lib=t.lib)
+    tot = np.array([[float(x) for x in ln.split()] for ln in
+                    open(os.path.join(d, "Total_numbers.txt")).read().splitlines()[1:]])
+    assert np.allclose(tot[:, 1], g["Out_tot_Ne"] / NMC, rtol=1e-15)
+    assert np.allclose(tot[:, 5], g["Out_tot_Nphot"] / NMC, rtol=1e-15)
+    assert np.max(tot[:, 1]) > 0
+    rows = [ln.split() for ln in open(os.path.join(d, "Radial_Valence_holes_density[1_cm^-3].txt")).read().splitlines()[1:]]
+    vb = [(a, s) for a, at in enumerate(w.material.atoms) for s, sh in enumerate(at.shells) if sh.designator >= 63][0]
+    want = g.view("Out_nh")[:, :, vb[0], vb[1]].T / NMC * 1e24
+    assert np.allclose(np.array([[float(x) for x in r[1:]] for r in rows]), want, rtol=1e-15, atol=0.0)
