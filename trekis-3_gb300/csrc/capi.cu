@@ -380,8 +380,10 @@ struct Workspace {
     size_t spec_it = 0, spec_row = 0;
     double *wE = nullptr, *wD = nullptr;   // bin widths [eV]
     cudaEvent_t e0 = nullptr, e1 = nullptr, s0 = nullptr, s1 = nullptr;
+    Fork fk;   // second stream for the hole kernel of a step
     ~Workspace() {
-        for (cudaEvent_t e : {e0, e1, s0, s1}) if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : {e0, e1, s0, s1, fk.fork, fk.join}) if (e) cudaEventDestroy(e);
+        if (fk.s2) cudaStreamDestroy(fk.s2);
     }
 };
 
@@ -474,6 +476,9 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     if (cudaMemcpy(w->hmap, hs.data(), sizeof(int) * nsh, cudaMemcpyHostToDevice) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
     for (cudaEvent_t* e : {&w->e0, &w->e1, &w->s0, &w->s1})
         if (cudaEventCreate(e) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
+    if (cudaStreamCreateWithFlags(&w->fk.s2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->fk.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->fk.join, cudaEventDisableTiming) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
     t->ws = holder;
     t->ws_key = key;
     *rc = 0;
@@ -599,7 +604,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             CK(cudaMemsetAsync(dctr, 0, NQ * sizeof(int), strm));
             CK(cudaEventRecord(ws->s0, strm));
             launch_step<T>(C, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm,
-                           ws->guess, pp);
+                           ws->guess, pp, &ws->fk);
             CK(cudaEventRecord(ws->s1, strm));
             blaunch += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0) + (pp ? 1 : 0); ++bsteps;
             CK(cudaGetLastError());

@@ -1483,12 +1483,23 @@ size_t shi_event_bytes() { return sizeof(ShiEv); }
 template <class T>
 void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
                  PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
-                 const float* guess, const Proposer* prop) {
+                 const float* guess, const Proposer* prop, const Fork* fk) {
     Out<T> o{{out.q[0], out.q[1], out.q[2], out.q[3]}, ctr};
+    // the two hot kernels touch disjoint queues; counters and tallies are atomics
+    const bool two = fk && fk->s2 && fk->fork && fk->join && n_in[Q_E] > 0 && n_in[Q_HVB] > 0;
+    if (two) {
+        cudaEventRecord(fk->fork, s);
+        cudaStreamWaitEvent(fk->s2, fk->fork, 0);
+    }
     if (n_in[Q_E] > 0)
         k_hot<T, true><<<(n_in[Q_E] + bs - 1) / bs, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
     if (n_in[Q_HVB] > 0)
-        k_hot<T, false><<<(n_in[Q_HVB] + bs - 1) / bs, bs, 0, s>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+        k_hot<T, false><<<(n_in[Q_HVB] + bs - 1) / bs, bs, 0, two ? fk->s2 : s>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o,
+                                                                                h_inel, tal, K);
+    if (two) {
+        cudaEventRecord(fk->join, fk->s2);
+        cudaStreamWaitEvent(s, fk->join, 0);
+    }
     if (prop) launch_propose<T>(*prop, C, tb, e_inel, h_inel, ctr, s);
     k_rare<T><<<rare_blocks, 128, 0, s>>>(C, tb, e_inel, h_inel, in.q[Q_HDEEP], n_in[Q_HDEEP], in.q[Q_P],
                                           n_in[Q_P], o, tal, prop ? guess : nullptr);
@@ -1502,10 +1513,10 @@ template void launch_pairs<double>(const McConst<double>&, const DevTabs<double>
                                    PQ<double>, PQ<double>, Tal, Ctrs*, cudaStream_t);
 template void launch_step<float>(const McConst<float>&, const DevTabs<float>&, const QSet<float>&, const int*,
                                  const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t,
-                                 const float*, const Proposer*);
+                                 const float*, const Proposer*, const Fork*);
 template void launch_step<double>(const McConst<double>&, const DevTabs<double>&, const QSet<double>&, const int*,
                                   const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t,
-                                  const float*, const Proposer*);
+                                  const float*, const Proposer*, const Fork*);
 
 // ---- grid hints ----------------------------------------------------------------------------
 // hint of a bucket = the search result at the bucket's lowest value, which

@@ -164,10 +164,18 @@ template <class T>
 void launch_propose(const Proposer& p, const McConst<T>& C, const DevTabs<T>& tb, PQ<T> e_inel, PQ<T> h_inel,
                     const Ctrs* ctr, cudaStream_t s);
 
+// One wavefront step on stream s.  With a second stream s2 and two events,
+// the electron and hole kernels run side by side (s2 forks after the work
+// queued on s and s joins before the rare kernel); without, one after the
+// other on s.
+struct Fork {
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
 template <class T>
 void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
                  PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
-                 const float* guess = nullptr, const Proposer* prop = nullptr);
+                 const float* guess = nullptr, const Proposer* prop = nullptr, const Fork* fk = nullptr);
 // Bucket hints of the time and radius grids.  A radius bucket is the bit
 // pattern of R without its low mantissa bits (monotone in R, 16 per octave).
 constexpr int kRgHintMax = 4096;
