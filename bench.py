@@ -359,7 +359,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--iters", type=int, default=256, help="MC iterations per step (one batch)")
+    ap.add_argument("--iters", type=int, default=2048, help="MC iterations per step (one call)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-iters", type=int, default=0)
     ap.add_argument("--seed", type=int, default=20251203)
@@ -367,7 +367,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-neural", action="store_true", help="skip the learned-proposal arm")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000, help="training samples per network")
-    ap.add_argument("--queue-cap", type=int, default=0, help="particles per queue buffer (0: library default)")
+    ap.add_argument("--queue-cap", type=int, default=64_000_000,
+                    help="particles per queue buffer (0: library default); 64 M holds about 2,400 cfg1 "
+                         "iterations in flight, so a 2048-iteration step runs as two batches")
     ap.add_argument("--events-per-step", type=int, default=0, help="events per thread per wavefront step (0: tuned)")
     args = ap.parse_args()
     if args.warmup < 3:

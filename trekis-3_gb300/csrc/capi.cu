@@ -379,6 +379,7 @@ struct Workspace {
     int spec_cap = 0;
     size_t spec_it = 0, spec_row = 0;
     double *wE = nullptr, *wD = nullptr;   // bin widths [eV]
+    double per_it_peak = 0.0;   // live particles per iteration at the peak of the last batch (batch sizing)
     cudaEvent_t e0 = nullptr, e1 = nullptr, s0 = nullptr, s1 = nullptr;
     Fork fk;   // second stream for the hole kernel of a step
     ~Workspace() {
@@ -558,9 +559,12 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     const int64_t cap = ws->cap;
     // the spectra hold one histogram per iteration of a batch
     const int B_max = tal.spec ? ws->spec_cap : (1 << 16);
-    int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 256);
-    B = std::min(B, B_max);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
+    // first batch: what the last call on this workspace measured fits half the
+    // queues, else 256 iterations; later batches follow the measured peak
+    int B = !tune_batch ? cfg.iterations_per_batch
+          : (ws->per_it_peak > 0.0 ? (int)std::min<double>(0.5 * (double)cap / ws->per_it_peak, 1 << 30) : 256);
+    B = std::max(1, std::min(std::min(B, B_max), cfg.NMC));
     CK(cudaEventRecord(ws->e0, strm));
     uint64_t steps = 0, launches = 1, ev_tot[8] = {0}, peak_all = 0;   // the grid hints
     uint64_t h2d = sizeof(T) * (Nt + cfg.N_R) + 8 * cfg.N_R, d2h = 0;
@@ -641,6 +645,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         done += nb;
         if (tune_batch && peak > 0) {   // size the next batch to half the queue capacity
             double per_it = (double)peak / nb;
+            ws->per_it_peak = per_it;
             B = std::max(1, std::min<int>((int)(0.5 * cap / per_it), B_max));
         }
     }
