@@ -456,6 +456,22 @@ typedef struct {
 int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_material* m, const trekis_ion* ion,
                            const trekis_run_cfg* cfg, const trekis_tallies* t, char* folder, int32_t folder_cap);
 
+/* SHI stopping power and range (Get_ion_range, Source_files/Analytical_IMFPs.f90:
+ * 2462-2504): E [eV] of the SHI grid, total dE/dx [eV/A] over all shells and
+ * the range [A] by trapezoids of 1/(dE/dx) from the first grid energy.  Needs
+ * SHI tables over the whole grid (trekis_table_cfg.shi_E_window_lo = hi = 0);
+ * n receives the grid size.  Host only. */
+int32_t trekis_shi_range(const trekis_tables* t, double* E, double* dEdx, double* range, int64_t cap,
+                         int64_t* n);
+
+/* The SHI table files Analytical_ion_dEdx writes (Analytical_IMFPs.f90:2316-2349
+ * names, :2660-2700 and :2497-2502 contents) into dir:
+ * OUTPUT_<ion>_CDF<_Barkas|_Bohr|_ND|_SG|_fixed><_P|_BK>_IMFP.dat, _dEdx.dat,
+ * _effective_charges.dat and _Range.dat; the common prefix is copied to
+ * prefix[prefix_cap].  Same requirement as trekis_shi_range. */
+int32_t trekis_save_shi_tables(const trekis_tables* t, const char* dir, const char* ion_name, char* prefix,
+                               int32_t prefix_cap);
+
 /* Human-readable text of the last error on this thread. */
 const char* trekis_last_error(void);
 

@@ -1,7 +1,9 @@
 """Test oracle for the output files: a Python restatement of the averaging in
-Universal_MC_for_SHI_MAIN.f90:281-314 and of the files Save_output writes
-(Sorting_output_data.f90:340-1140), used only by tests/ to check the
-library's writer byte for byte.  Numbers are formatted through the exact
+Universal_MC_for_SHI_MAIN.f90:281-314, of the files Save_output writes
+(Sorting_output_data.f90:340-1140) and of the SHI table files of
+Analytical_ion_dEdx with Get_ion_range (Analytical_IMFPs.f90:2316-2349,
+2462-2504, 2660-2700), used only by tests/ to check the library's writers
+byte for byte.  Numbers are formatted through the exact
 decimal value of each double (decimal module), independently of the C
 library's printf.
 
@@ -241,3 +243,71 @@ def write(out_dir, run, T, NMC):
                     return a4("Out_Ehkin", k, i, a, s) / nh * KB * 2.0 / 3.0 if nh > 0 else 0.0
                 radial(f"Radial_{label(a, s)}_holes_temperature[K].txt", tv)
     return d
+
+
+def fes(x, w=25, d=16, e=3):
+    """Fortran ESw.dEe."""
+    if not math.isfinite(x):
+        s = "NaN" if math.isnan(x) else ("Infinity" if x > 0 else "-Infinity")
+        return s.rjust(w) if len(s) <= w else "*" * w
+    if x == 0.0:
+        mant, k = "0." + "0" * d, 0
+    else:
+        dx = Decimal(abs(x))
+        k = dx.adjusted()
+        q = dx.scaleb(-k).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+        if q >= 10:
+            k += 1
+            q = dx.scaleb(-k).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+        mant = format(q, "f")
+    ex = f"{abs(k):0{e}d}"
+    if len(ex) > e:
+        return "*" * w
+    s = ("-" if x < 0 else "") + mant + "E" + ("-" if k < 0 else "+") + ex
+    return s.rjust(w) if len(s) <= w else "*" * w
+
+
+def shi_range(E, dEdx_shells):
+    """Get_ion_range (Analytical_IMFPs.f90:2462-2504): total dE/dx and the
+    range by trapezoids of 1/(dE/dx); dEdx_shells[s][i] in (atom, shell) order."""
+    N = len(E)
+    D = [0.0] * N
+    for i in range(N):
+        for d in dEdx_shells:
+            D[i] = D[i] + d[i]
+    R = [0.0] * N
+    acc = 0.0
+    for j in range(1, N):
+        if D[j - 1] == 0.0:
+            acc = acc + 0.5 / D[j] * (E[j] - E[j - 1])
+        else:
+            acc = acc + 0.5 * (1.0 / D[j] + 1.0 / D[j - 1]) * (E[j] - E[j - 1])
+        R[j] = acc
+    return D, R
+
+
+def write_shi_tables(d, ion_name, Kind_Zeff, Kind_ion, E, L_shells, dEdx_shells, zeff):
+    """The four SHI files of Analytical_ion_dEdx (names :2316-2349, contents
+    :2660-2700 and :2497-2502); returns the common prefix."""
+    cn = ["_Barkas", "_Bohr", "_ND", "_SG", "_fixed"][Kind_Zeff if 0 <= Kind_Zeff <= 4 else 0]
+    base = os.path.join(d, f"OUTPUT_{ion_name}_CDF{cn}{'_BK' if Kind_ion == 1 else '_P'}")
+    with open(base + "_IMFP.dat", "w") as fi, open(base + "_dEdx.dat", "w") as fd, \
+            open(base + "_effective_charges.dat", "w") as fz:
+        for i, e in enumerate(E):
+            fi.write(fe(e / 1.0e6))
+            fd.write(fe(e / 1.0e6))
+            fz.write(fe(e / 1.0e6) + fe(zeff[i]) + "\n")
+            inv, ded = 0.0, 0.0
+            for L, D in zip(L_shells, dEdx_shells):
+                fi.write(fe(L[i]))
+                fd.write(fe(D[i]))
+                inv = inv + 1.0 / L[i] if L[i] > 1.0e-10 else 1.1e29
+                ded = ded + D[i]
+            fi.write(fe(1.0 / inv) + "\n")
+            fd.write(fe(ded) + "\n")
+    D, R = shi_range(E, dEdx_shells)
+    with open(base + "_Range.dat", "w") as fr:
+        fr.write("# Energy dEdx    Range\n# [eV] [eV/A]    [A]\n")
+        for i, e in enumerate(E):
+            fr.write(fes(e) + fes(D[i]) + fes(R[i]) + "\n")
+    return base

@@ -1,5 +1,7 @@
 """GPU FP64 table build against the oracle's FP64 restatement (tolerance 1e-6
 relative, the bound the track-loop specification sets for tables)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -121,3 +123,38 @@ def test_phonon_elastic_tables(phonon_pair):
             assert len(hw1) == len(hw2) > 1, (tab, i)
             assert _close(hw1, hw2, 1e-12) and _close(R1, R2), (tab, i)
             assert np.all(np.diff(R1) <= 0), (tab, i)
+
+
+@pytest.mark.gpu
+def test_shi_range_and_table_files(gpu_lib, tmp_path):
+    """SHI tables over the whole grid: stopping power and range
+    (Get_ion_range) and the four SHI table files equal the test oracle's
+    restatement computed from the exported per-shell tables."""
+    import os
+    import oracle_output
+    import oracle_py
+    w = configs.small(configs.cfg0, NMC=1)
+    t = api.Tables(w, lib=gpu_lib, shi_window=False)
+    E, D, R = t.shi_range()
+    shells = [(a, s) for a, at in enumerate(w.material.atoms) for s in range(len(at.shells))]
+    ex = [t.export(abi.TAB_SHI, a, s) for a, s in shells]
+    assert np.array_equal(E, ex[0][0])
+    D2, R2 = oracle_output.shi_range(list(E), [list(e[2]) for e in ex])
+    assert np.array_equal(D, np.array(D2)) and np.array_equal(R, np.array(R2))
+    assert np.all(np.diff(R) > 0) and np.all(D[1:] > 0)
+    # the ion's range at its energy is far beyond the layer, as a 20 MeV Xe ion's is (micrometres)
+    assert np.interp(w.ion_E, E, R) > 1e4
+    (tmp_path / "lib").mkdir()
+    (tmp_path / "ref").mkdir()
+    p1 = t.save_shi_tables(tmp_path / "lib")
+    lib_o = oracle_py.load()
+    zeff = [lib_o.oracle_zeff(C.byref(t.ion), float(e), t.mat.ref()) for e in E]
+    p2 = oracle_output.write_shi_tables(str(tmp_path / "ref"), api.ELEMENTS[w.ion_Z - 1], t.ion.Kind_Zeff,
+                                        t.ion.Kind_ion, list(E), [list(e[1]) for e in ex], [list(e[2]) for e in ex],
+                                        zeff)
+    assert os.path.basename(p1) == os.path.basename(p2) == "OUTPUT_Xe_CDF_Barkas_P"
+    for suf in ("_IMFP.dat", "_dEdx.dat", "_Range.dat"):
+        assert open(p1 + suf, "rb").read() == open(p2 + suf, "rb").read(), suf
+    z1 = np.loadtxt(p1 + "_effective_charges.dat")
+    z2 = np.loadtxt(p2 + "_effective_charges.dat")
+    assert np.allclose(z1, z2, rtol=1e-14, atol=0.0)

@@ -102,3 +102,6 @@ def test_fortran_number_formats():
     assert oracle_output.ff(1.0, 10, 2) == "      1.00"
     assert oracle_output.ff(1234567.0, 9, 1) == "1234567.0"
     assert oracle_output.ff(12345678.0, 9, 1) == "*********"
+    assert oracle_output.fes(123.456) == "  1.2345600000000000E+002"
+    assert oracle_output.fes(-1.0e-5) == " -1.0000000000000001E-005"
+    assert oracle_output.fes(0.0) == "  0.0000000000000000E+000"

@@ -127,6 +127,7 @@ struct trekis_tables {
     tk::HRowSet hole_rows;
     tk::HRowSet el_elast_rows, hole_elast_rows;   // phonon-CDF elastic (kind_of_EMFP = 1)
     bool has_shi = false, has_phot = false;
+    bool shi_full = false;   // SHI tables over the whole SHI grid (no energy window)
     // device
     tk::Buffers buf;
     tk::DevTabs<float> d32;
@@ -147,6 +148,7 @@ namespace tk {
 void set_error(const std::string& s);
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st);
 std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax);
+double zeff_of(const trekis_ion& ion, const trekis_material& m, double E);   // Equilibrium_charge_SHI
 struct MlpDev;
 const MlpDev* mlp_device(const trekis_tables* t);
 }  // namespace tk

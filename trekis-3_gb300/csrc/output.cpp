@@ -25,6 +25,10 @@
 // the electric-field and emission files (no fields, no emission on this
 // path) and Hole_mean_diffusion_coefficient.txt (not computed: the
 // reference's value depends on its OpenMP schedule).
+//
+// Also here: the SHI table files of Analytical_ion_dEdx (IMFP and dE/dx per
+// shell, the ion's effective charge, its stopping power and range) written
+// from a table handle.
 #include <sys/stat.h>
 #include <sys/types.h>
 
@@ -74,6 +78,25 @@ std::string e_fmt(double x, int w = 25, int d = 16, int e = 3) {
         std::snprintf(es, sizeof es, "%c%0*d", ex < 0 ? '-' : '+', e, std::abs(ex));
         if ((int)std::strlen(es) > e + 1) return std::string(w, '*');
         out = std::string(x < 0 ? "-" : "") + "0." + mant + "E" + es;
+    }
+    if ((int)out.size() > w) return std::string(w, '*');
+    return std::string(w - out.size(), ' ') + out;
+}
+
+// Fortran ESw.dEe: one nonzero digit before the point
+std::string es_fmt(double x, int w = 25, int d = 16, int e = 3) {
+    std::string out;
+    if (!std::isfinite(x)) {
+        out = std::isnan(x) ? "NaN" : (x > 0 ? "Infinity" : "-Infinity");
+    } else {
+        char b[64];
+        std::snprintf(b, sizeof b, "%.*e", d, std::fabs(x));   // d.ddd...e+XX with d digits after the point
+        const char* p = std::strchr(b, 'e');
+        const int ex = std::atoi(p + 1);
+        char es[16];
+        std::snprintf(es, sizeof es, "%c%0*d", ex < 0 ? '-' : '+', e, std::abs(ex));
+        if ((int)std::strlen(es) > e + 1) return std::string(w, '*');
+        out = std::string(x < 0 ? "-" : "") + std::string(b, p - b) + "E" + es;
     }
     if ((int)out.size() > w) return std::string(w, '*');
     return std::string(w - out.size(), ' ') + out;
@@ -360,5 +383,98 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
         tk::set_error("writing the output files in " + dir + " failed");
         return TREKIS_EINVAL;
     }
+    return TREKIS_OK;
+}
+
+// ---- SHI tables as Analytical_ion_dEdx writes them ------------------------------------------
+
+namespace {
+// Get_ion_range (Analytical_IMFPs.f90:2462-2504): total dE/dx over the shells
+// and the range by trapezoids of 1/(dE/dx) from the first grid energy
+void shi_range(const trekis_tables* t, std::vector<double>& E, std::vector<double>& D, std::vector<double>& R) {
+    E = t->shi[0].E;
+    const size_t N = E.size();
+    D.assign(N, 0.0);
+    for (size_t i = 0; i < N; ++i)
+        for (int a = 0; a < t->mat.N_atoms; ++a)
+            for (int s = 0; s < t->mat.atoms[a].N_shl; ++s) D[i] = D[i] + t->shi[t->shell_index[a][s]].dEdx[i];
+    R.assign(N, 0.0);
+    double acc = 0.0;
+    for (size_t j = 1; j < N; ++j) {
+        if (D[j - 1] == 0.0) acc = acc + 0.5 / D[j] * (E[j] - E[j - 1]);
+        else acc = acc + 0.5 * (1.0 / D[j] + 1.0 / D[j - 1]) * (E[j] - E[j - 1]);
+        R[j] = acc;
+    }
+}
+bool shi_ready(const trekis_tables* t) {
+    if (!t || !t->has_shi || t->shi.empty()) { tk::set_error("the tables hold no SHI tables"); return false; }
+    if (!t->shi_full) {
+        tk::set_error("SHI tables were built in an energy window; build them with shi_E_window_lo = hi = 0");
+        return false;
+    }
+    return true;
+}
+}  // namespace
+
+extern "C" int32_t trekis_shi_range(const trekis_tables* t, double* E, double* dEdx, double* range, int64_t cap,
+                                    int64_t* n) {
+    if (!n || !shi_ready(t)) return TREKIS_EINVAL;
+    std::vector<double> e, d, r;
+    shi_range(t, e, d, r);
+    *n = (int64_t)e.size();
+    if (*n > cap) { tk::set_error("output arrays too small"); return TREKIS_EINVAL; }
+    if (E) std::memcpy(E, e.data(), 8 * e.size());
+    if (dEdx) std::memcpy(dEdx, d.data(), 8 * d.size());
+    if (range) std::memcpy(range, r.data(), 8 * r.size());
+    return TREKIS_OK;
+}
+
+// Files OUTPUT_<ion>_CDF<charge><kind>_{IMFP,dEdx,effective_charges,Range}.dat
+// (Analytical_IMFPs.f90:2316-2349 names, :2660-2700 and :2497-2502 contents)
+extern "C" int32_t trekis_save_shi_tables(const trekis_tables* t, const char* dir, const char* ion_name,
+                                          char* prefix, int32_t prefix_cap) {
+    if (!dir || !ion_name || !shi_ready(t)) return TREKIS_EINVAL;
+    static const char* cn[] = {"_Barkas", "_Bohr", "_ND", "_SG", "_fixed"};
+    const int kz = (t->ion.Kind_Zeff >= 0 && t->ion.Kind_Zeff <= 4) ? t->ion.Kind_Zeff : 0;
+    const std::string base = std::string(dir) + "/OUTPUT_" + trim(ion_name) + "_CDF" + cn[kz] +
+                             (t->ion.Kind_ion == 1 ? "_BK" : "_P");
+    if (prefix && prefix_cap > 0) {
+        std::strncpy(prefix, base.c_str(), (size_t)prefix_cap - 1);
+        prefix[prefix_cap - 1] = '\0';
+    }
+    const std::vector<double>& E = t->shi[0].E;
+    const size_t N = E.size();
+    bool ok = true;
+    {
+        Out fi(base + "_IMFP.dat"), fd(base + "_dEdx.dat"), fz(base + "_effective_charges.dat");
+        for (size_t i = 0; i < N; ++i) {
+            fi.put(e_fmt(E[i] / 1.0e6));
+            fd.put(e_fmt(E[i] / 1.0e6));
+            fz.put(e_fmt(E[i] / 1.0e6) + e_fmt(tk::zeff_of(t->ion, t->mat, E[i])) + "\n");
+            double inv = 0.0, ded = 0.0;
+            for (int a = 0; a < t->mat.N_atoms; ++a)
+                for (int s = 0; s < t->mat.atoms[a].N_shl; ++s) {
+                    const tk::HTab& h = t->shi[t->shell_index[a][s]];
+                    fi.put(e_fmt(h.L[i]));
+                    fd.put(e_fmt(h.dEdx[i]));
+                    if (h.L[i] > 1.0e-10) inv = inv + 1.0 / h.L[i];
+                    else inv = 1.1e29;
+                    ded = ded + h.dEdx[i];
+                }
+            fi.put(e_fmt(1.0 / inv) + "\n");
+            fd.put(e_fmt(ded) + "\n");
+        }
+        ok = fi.ok && fd.ok && fz.ok;
+    }
+    {
+        std::vector<double> e, d, r;
+        shi_range(t, e, d, r);
+        Out fr(base + "_Range.dat");
+        fr.put("# Energy dEdx    Range\n");
+        fr.put("# [eV] [eV/A]    [A]\n");
+        for (size_t i = 0; i < N; ++i) fr.put(es_fmt(e[i]) + es_fmt(d[i]) + es_fmt(r[i]) + "\n");
+        ok = ok && fr.ok;
+    }
+    if (!ok) { tk::set_error("writing the SHI table files failed"); return TREKIS_EINVAL; }
     return TREKIS_OK;
 }

@@ -265,7 +265,7 @@ std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax)
     return g;
 }
 
-static double zeff_of(const trekis_ion& ion, const trekis_material& m, double E) {  // CS:2641-2680
+double zeff_of(const trekis_ion& ion, const trekis_material& m, double E) {  // CS:2641-2680
     double vp = E > 0 ? std::sqrt(2.0 * E * kE / (ion.Mass * kMp)) : 0.0;
     double zs = 0, ps = 0;
     for (int a = 0; a < m.N_atoms; ++a) { zs += m.atoms[a].Zat * m.atoms[a].Pers; ps += m.atoms[a].Pers; }
@@ -580,6 +580,7 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
             d.dEdx.assign(rX.begin() + J.row_off, rX.begin() + J.row_off + J.row_len);
         }
         T->has_shi = true;
+        T->shi_full = cfg.shi_E_window_lo <= 0 && cfg.shi_E_window_hi <= 0;
     }
     // phonon-CDF elastic MFPs and rows
     auto phon = [&](const std::vector<double>& g, size_t j0, HTab& t, HRowSet& R) {

@@ -180,6 +180,8 @@ SIGNATURES = {
                                     C.POINTER(C.c_double)]),
     "trekis_save_output": (C.c_int32, [C.POINTER(OutputCfg), C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
                                        C.POINTER(Tallies), C.c_char_p, C.c_int32]),
+    "trekis_shi_range": (C.c_int32, [C.c_void_p, _DP, _DP, _DP, C.c_int64, C.POINTER(C.c_int64)]),
+    "trekis_save_shi_tables": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]),
     "trekis_last_error": (C.c_char_p, []),
 }
 

@@ -152,6 +152,23 @@ class Tables:
                                              C.byref(n)), self.lib)
         return hw[:n.value].copy(), L[:n.value].copy()
 
+    def shi_range(self):
+        """SHI stopping power and range over the SHI grid (trekis_shi_range):
+        (E [eV], dE/dx [eV/A], range [A]); needs tables built with shi_window=False."""
+        n = C.c_int64()
+        cap = 1 << 16
+        E, D, R = np.zeros(cap), np.zeros(cap), np.zeros(cap)
+        abi.check(self.lib.trekis_shi_range(self.h, abi.dptr(E), abi.dptr(D), abi.dptr(R), cap, C.byref(n)), self.lib)
+        return E[:n.value].copy(), D[:n.value].copy(), R[:n.value].copy()
+
+    def save_shi_tables(self, out_dir, ion_name=None):
+        """The SHI table files of Analytical_ion_dEdx (trekis_save_shi_tables);
+        returns the files' common prefix."""
+        buf = C.create_string_buffer(4096)
+        name = (ion_name or ELEMENTS[self.w.ion_Z - 1]).encode()
+        abi.check(self.lib.trekis_save_shi_tables(self.h, str(out_dir).encode(), name, buf, len(buf)), self.lib)
+        return buf.value.decode()
+
     def close(self):
         if self.h:
             self.lib.trekis_tables_free(self.h)
