@@ -472,6 +472,18 @@ int32_t trekis_shi_range(const trekis_tables* t, double* E, double* dEdx, double
 int32_t trekis_save_shi_tables(const trekis_tables* t, const char* dir, const char* ion_name, char* prefix,
                                int32_t prefix_cap);
 
+/* The MFP tables and cumulative rows of a table handle written as the files
+ * Analytical_electron_dEdx and its elastic counterpart cache in the material's
+ * output folder (Source_files/Analytical_IMFPs.f90:240-460 names, :592-632
+ * MFP files, :660-790 and :1440-1600 rows): OUTPUT_Electron_IMFPs_..._K.dat,
+ * OUTPUT_Hole_IMFPs_CDF_CDF_<T>_K.dat, OUTPUT_Photon_IMFPs_CDF_<T>_K.dat (with
+ * photon tables), the electron and hole elastic files, and with with_rows the
+ * diff_CS/ folder, one file per (shell, energy) row (every row_stride-th row;
+ * 0 or 1: all).  A Fortran run finds them and skips its own table build.
+ * Names come from oc->atom_names and oc->shell_names.  Host only. */
+int32_t trekis_save_mfp_tables(const trekis_tables* t, const trekis_output_cfg* oc, const char* dir,
+                               int32_t with_rows, int32_t row_stride);
+
 /* Human-readable text of the last error on this thread. */
 const char* trekis_last_error(void);
 

@@ -311,3 +311,72 @@ def write_shi_tables(d, ion_name, Kind_Zeff, Kind_ion, E, L_shells, dEdx_shells,
         for i, e in enumerate(E):
             fr.write(fes(e) + fes(D[i]) + fes(R[i]) + "\n")
     return base
+
+
+def write_mfp_tables(d, mat, names, tabs, rows, stride):
+    """The cached MFP files and diff_CS rows of Analytical_electron_dEdx
+    (Analytical_IMFPs.f90:240-460 names, :592-632, :660-790, :1380-1600).
+    mat: kind_of_DR, El_eff_mass, temp, kind_of_EMFP, CDF_elast_Zeff,
+    has_phot; names: [(atom name, [shell names])]; tabs: dict of
+    'el', 'hole', 'phot' -> [(E, L)] per (atom, shell) and 'el_elast',
+    'hole_elast' -> (E, L); rows: dict 'el' -> [(E grid, [(hw, L)])] per
+    (atom, shell), 'hole', 'el_elast', 'hole_elast' -> (E grid, [(hw, L)])."""
+    T = mat["temp"]
+    dr = {4: "Delta_", 3: "Ritchie_", 2: "Plasmon_pole_"}.get(mat["kind_of_DR"], "Free_")
+    m = mat["El_eff_mass"]
+    if m == 0.0:
+        mass = f"DOS_{ff(T, 9, 2).strip()}_K"
+    elif m < 0.0 or m == 1.0:
+        mass = f"Me_{ff(T, 9, 2).strip()}_K"
+    else:
+        mass = f"{ff(m, 5, 2).strip()}_me_{ff(T, 9, 2).strip()}_K"
+    el_name = f"Electron_IMFPs_{dr}CDF_{mass}"
+    ho_name = f"Hole_IMFPs_CDF_CDF_{ff(T, 7, 2).strip()}_K"
+
+    def mfp(path, shells):
+        with open(path, "w") as f:
+            E = shells[0][0]
+            for i in range(len(E)):
+                inv = 0.0
+                line = ff(E[i], 25, 16)
+                for _, L in shells:
+                    line += fe(L[i])
+                    inv = inv + 1.0 / L[i]
+                f.write(line + fe(1.0 / inv) + "\n")
+
+    mfp(os.path.join(d, f"OUTPUT_{el_name}.dat"), tabs["el"])
+    mfp(os.path.join(d, f"OUTPUT_{ho_name}.dat"), tabs["hole"])
+    if mat["has_phot"]:
+        mfp(os.path.join(d, f"OUTPUT_Photon_IMFPs_CDF_{ff(T, 7, 2).strip()}_K.dat"), tabs["phot"])
+    if mat["kind_of_EMFP"] == 1:
+        zt = "Z=1_" if mat["CDF_elast_Zeff"] == 1 else "Zeff_"
+        ee_name = f"Electron_EMFPs_CDF_{zt}{ff(T, 7, 2).strip()}_K"
+        he_name = f"Hole_CDF_EMFPs_{ff(T, 7, 2).strip()}_K"
+    else:
+        ee_name = "Electron_EMFPs_Mott"
+        he_name = f"Hole_Mott_EMFPs_{ff(T, 7, 2).strip()}_K"
+    for name, (E, L) in ((ee_name, tabs["el_elast"]), (he_name, tabs["hole_elast"])):
+        with open(os.path.join(d, f"OUTPUT_{name}.dat"), "w") as f:
+            for e, l in zip(E, L):
+                f.write(ff(e, 25, 16) + fe(l) + "\n")
+    if rows is None:
+        return
+    fold = os.path.join(d, "diff_CS")
+    os.makedirs(fold, exist_ok=True)
+
+    def put(stem, grid, rws):
+        for i in range(0, len(rws), stride):
+            with open(os.path.join(fold, f"{stem}_{ff(grid[i], 14, 3).strip()}.dat"), "w") as f:
+                for hw, L in zip(*rws[i]):
+                    f.write(fes(hw) + fes(L) + "\n")
+
+    k = 0
+    for an, shells in names:
+        for sn in shells:
+            grid, rws = rows["el"][k]
+            put(f"{el_name}_{an}_{sn}", grid, rws)
+            k += 1
+    put(f"{ho_name}_{names[0][0]}_{names[0][1][-1]}", *rows["hole"])
+    if mat["kind_of_EMFP"] == 1:
+        put(ee_name, *rows["el_elast"])
+        put(he_name, *rows["hole_elast"])

@@ -158,3 +158,60 @@ def test_shi_range_and_table_files(gpu_lib, tmp_path):
     z1 = np.loadtxt(p1 + "_effective_charges.dat")
     z2 = np.loadtxt(p2 + "_effective_charges.dat")
     assert np.allclose(z1, z2, rtol=1e-14, atol=0.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg_name", ["cfg1", "cfg4"])
+def test_table_cache_files(gpu_lib, tmp_path, cfg_name):
+    """The MFP files and diff_CS rows written from GPU tables equal the test
+    oracle's restatement byte for byte (every 37th row), and read back to
+    the exported tables (MFPs to 16 digits, rows exactly)."""
+    import os
+    import oracle_output
+    w = configs.small(getattr(configs, cfg_name), NMC=1)
+    t = api.Tables(w, lib=gpu_lib)
+    (tmp_path / "lib").mkdir()
+    (tmp_path / "ref").mkdir()
+    stride = 37
+    t.save_mfp_tables(tmp_path / "lib", with_rows=True, row_stride=stride)
+    m = w.material
+    shells = [(a, s) for a, at in enumerate(m.atoms) for s in range(len(at.shells))]
+    names = [(api.ELEMENTS[at.Z - 1], [api.shell_name(sh.designator) for sh in at.shells]) for at in m.atoms]
+    has_phot = bool(m.include_photons)
+    tabs = {k: [t.export(kind, a, s)[:2] for a, s in shells] for k, kind in
+            (("el", abi.TAB_EL_INEL), ("hole", abi.TAB_H_INEL)) }
+    if has_phot:
+        tabs["phot"] = [t.export(abi.TAB_PHOT, a, s)[:2] for a, s in shells]
+    tabs["el_elast"] = t.export(abi.TAB_EL_ELAST)[:2]
+    tabs["hole_elast"] = t.export(abi.TAB_H_ELAST)[:2]
+
+    def rowset(kind, a, s, grid):   # only the rows the files hold
+        return grid, [t.row(kind, a, s, i) if i % stride == 0 else None for i in range(len(grid))]
+
+    rows = {"el": [rowset(abi.ROW_EL_INEL, a, s, tabs["el"][q][0]) for q, (a, s) in enumerate(shells)]}
+    vb = (0, len(m.atoms[0].shells) - 1)
+    rows["hole"] = rowset(abi.ROW_H_INEL, *vb, tabs["hole"][shells.index(vb)][0])
+    if m.kind_of_EMFP == 1:
+        rows["el_elast"] = rowset(abi.ROW_EL_ELAST, 0, 0, tabs["el_elast"][0])
+        rows["hole_elast"] = rowset(abi.ROW_H_ELAST, 0, 0, tabs["hole_elast"][0])
+    mat = {"kind_of_DR": m.kind_of_DR, "El_eff_mass": m.El_eff_mass, "temp": m.temp, "kind_of_EMFP": m.kind_of_EMFP,
+           "CDF_elast_Zeff": m.CDF_elast_Zeff, "has_phot": has_phot}
+    oracle_output.write_mfp_tables(str(tmp_path / "ref"), mat, names, tabs, rows, stride)
+    got = sorted(os.listdir(tmp_path / "lib"))
+    assert got == sorted(os.listdir(tmp_path / "ref"))
+    rdir = sorted(os.listdir(tmp_path / "lib" / "diff_CS"))
+    assert rdir == sorted(os.listdir(tmp_path / "ref" / "diff_CS")) and len(rdir) > 10
+    for n in [g for g in got if g.endswith(".dat")]:
+        assert open(tmp_path / "lib" / n, "rb").read() == open(tmp_path / "ref" / n, "rb").read(), n
+    for n in rdir:
+        assert open(tmp_path / "lib" / "diff_CS" / n, "rb").read() == \
+            open(tmp_path / "ref" / "diff_CS" / n, "rb").read(), n
+    # read back
+    el_file = [g for g in got if g.startswith("OUTPUT_Electron_IMFPs_")][0]
+    back = api.read_table_file(tmp_path / "lib" / el_file)
+    assert np.allclose(back[:, 0], tabs["el"][0][0], rtol=1e-15, atol=0.0)   # F25.16: 16 decimals
+    for q in range(len(shells)):
+        assert np.allclose(back[:, 1 + q], tabs["el"][q][1], rtol=1e-15, atol=0.0)
+    grid, rws = rows["el"][0]
+    r0 = api.read_table_file(tmp_path / "lib" / "diff_CS" / [n for n in rdir if n.startswith(el_file[7:-4])][0])
+    assert r0.shape[1] == 2

@@ -478,3 +478,109 @@ extern "C" int32_t trekis_save_shi_tables(const trekis_tables* t, const char* di
     if (!ok) { tk::set_error("writing the SHI table files failed"); return TREKIS_EINVAL; }
     return TREKIS_OK;
 }
+
+// ---- MFP tables and cumulative rows as Analytical_electron_dEdx caches them -------------------
+
+namespace {
+// the default-width F descriptor for REAL(8): F25.16
+std::string f_def(double x) { return f_fmt(x, 25, 16); }
+
+// MFP file: E, the MFP of every (atom, shell), the total (Analytical_IMFPs.f90:592-632)
+bool write_mfp(const std::string& path, const std::vector<double>& E, const std::vector<const tk::HTab*>& shells) {
+    Out o(path);
+    for (size_t i = 0; i < E.size(); ++i) {
+        o.put(f_def(E[i]));
+        double inv = 0.0;
+        for (const tk::HTab* h : shells) {
+            o.put(e_fmt(h->L[i]));
+            inv = inv + 1.0 / h->L[i];
+        }
+        o.put(e_fmt(1.0 / inv) + "\n");
+    }
+    return o.ok;
+}
+// one cumulative row per file: hbar-omega and the cumulative MFP, (es,es) (:686-693)
+bool write_row(const std::string& path, const tk::HRow& r) {
+    Out o(path);
+    for (size_t i = 0; i < r.hw.size(); ++i) o.put(es_fmt(r.hw[i]) + es_fmt(r.L[i]) + "\n");
+    return o.ok;
+}
+std::string temp_tag(double T, int w) { return trim(f_fmt(T, w, 2)); }
+}  // namespace
+
+// Files of Analytical_electron_dEdx / Analytical_elastic (Analytical_IMFPs.f90:240-460 names,
+// :592-632 MFP files, :660-790 and :1440-1600 the diff_CS rows, :1380-1420 elastic files)
+extern "C" int32_t trekis_save_mfp_tables(const trekis_tables* t, const trekis_output_cfg* oc, const char* dir,
+                                          int32_t with_rows, int32_t row_stride) {
+    if (!t || !oc || !dir || row_stride < 0) { tk::set_error("invalid arguments"); return TREKIS_EINVAL; }
+    const trekis_material& m = t->mat;
+    for (int a = 0; a < m.N_atoms; ++a) {
+        if (!oc->atom_names[a]) { tk::set_error("missing atom name"); return TREKIS_EINVAL; }
+        for (int s = 0; s < m.atoms[a].N_shl; ++s)
+            if (!oc->shell_names[a][s]) { tk::set_error("missing shell name"); return TREKIS_EINVAL; }
+    }
+    const int stride = row_stride > 0 ? row_stride : 1;
+    const std::string D(dir);
+    std::vector<const tk::HTab*> el, ho, ph;
+    for (int a = 0; a < m.N_atoms; ++a)
+        for (int s = 0; s < m.atoms[a].N_shl; ++s) {
+            const int k = t->shell_index[a][s];
+            el.push_back(&t->el[k]);
+            ho.push_back(&t->hole[k]);
+            if (t->has_phot) ph.push_back(&t->phot[k]);
+        }
+    // electron inelastic: OUTPUT_Electron_IMFPs_<dispersion>_CDF_<mass>_<T>_K.dat
+    const char* dr = m.kind_of_DR == 4 ? "Delta_" : m.kind_of_DR == 3 ? "Ritchie_" : m.kind_of_DR == 2 ? "Plasmon_pole_" : "Free_";
+    std::string mass;
+    if (m.El_eff_mass == 0.0) mass = "DOS_" + temp_tag(m.temp, 9) + "_K";
+    else if (m.El_eff_mass < 0.0 || m.El_eff_mass == 1.0) mass = "Me_" + temp_tag(m.temp, 9) + "_K";
+    else mass = trim(f_fmt(m.El_eff_mass, 5, 2)) + "_me_" + temp_tag(m.temp, 9) + "_K";
+    const std::string el_name = std::string("Electron_IMFPs_") + dr + "CDF_" + mass;
+    const std::string ho_name = "Hole_IMFPs_CDF_CDF_" + temp_tag(m.temp, 7) + "_K";
+    bool ok = write_mfp(D + "/OUTPUT_" + el_name + ".dat", el[0]->E, el);
+    ok = ok && write_mfp(D + "/OUTPUT_" + ho_name + ".dat", ho[0]->E, ho);
+    if (t->has_phot) ok = ok && write_mfp(D + "/OUTPUT_Photon_IMFPs_CDF_" + temp_tag(m.temp, 7) + "_K.dat", ph[0]->E, ph);
+    // elastic: Mott, or the phonon CDF with the target-charge tag
+    std::string ee_name, he_name;
+    if (m.kind_of_EMFP == 1) {
+        ee_name = std::string("Electron_EMFPs_CDF_") + (m.CDF_elast_Zeff == 1 ? "Z=1_" : "Zeff_") + temp_tag(m.temp, 7) + "_K";
+        he_name = "Hole_CDF_EMFPs_" + temp_tag(m.temp, 7) + "_K";
+    } else {
+        ee_name = "Electron_EMFPs_Mott";
+        he_name = "Hole_Mott_EMFPs_" + temp_tag(m.temp, 7) + "_K";
+    }
+    for (auto [name, tab] : {std::make_pair(ee_name, &t->el_elast), std::make_pair(he_name, &t->hole_elast)}) {
+        Out o(D + "/OUTPUT_" + name + ".dat");
+        for (size_t i = 0; i < tab->E.size(); ++i) o.put(f_def(tab->E[i]) + e_fmt(tab->L[i]) + "\n");
+        ok = ok && o.ok;
+    }
+    if (with_rows) {
+        const std::string fold = D + "/diff_CS";
+        struct stat st;
+        if (stat(fold.c_str(), &st) != 0 && mkdir(fold.c_str(), 0755) != 0) {
+            tk::set_error("cannot create " + fold + ": " + std::strerror(errno));
+            return TREKIS_EINVAL;
+        }
+        auto row_file = [&](const std::string& stem, double E) { return fold + "/" + stem + "_" + trim(f_fmt(E, 14, 3)) + ".dat"; };
+        for (int a = 0; a < m.N_atoms; ++a)
+            for (int s = 0; s < m.atoms[a].N_shl; ++s) {
+                const tk::HRowSet& R = t->el_rows[t->shell_index[a][s]];
+                const std::string stem = el_name + "_" + trim(oc->atom_names[a]) + "_" + trim(oc->shell_names[a][s]);
+                for (size_t i = 0; i < R.rows.size(); i += stride) ok = ok && write_row(row_file(stem, R.E[i]), R.rows[i]);
+            }
+        {   // valence holes: the last shell of the first atom
+            const int a = 0, s = m.atoms[0].N_shl - 1;
+            const std::string stem = ho_name + "_" + trim(oc->atom_names[a]) + "_" + trim(oc->shell_names[a][s]);
+            for (size_t i = 0; i < t->hole_rows.rows.size(); i += stride)
+                ok = ok && write_row(row_file(stem, t->hole_rows.E[i]), t->hole_rows.rows[i]);
+        }
+        if (m.kind_of_EMFP == 1) {
+            for (size_t i = 0; i < t->el_elast_rows.rows.size(); i += stride)
+                ok = ok && write_row(row_file(ee_name, t->el_elast_rows.E[i]), t->el_elast_rows.rows[i]);
+            for (size_t i = 0; i < t->hole_elast_rows.rows.size(); i += stride)
+                ok = ok && write_row(row_file(he_name, t->hole_elast_rows.E[i]), t->hole_elast_rows.rows[i]);
+        }
+    }
+    if (!ok) { tk::set_error("writing the table files in " + D + " failed"); return TREKIS_EINVAL; }
+    return TREKIS_OK;
+}

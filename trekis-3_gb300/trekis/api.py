@@ -169,6 +169,13 @@ class Tables:
         abi.check(self.lib.trekis_save_shi_tables(self.h, str(out_dir).encode(), name, buf, len(buf)), self.lib)
         return buf.value.decode()
 
+    def save_mfp_tables(self, out_dir, with_rows=True, row_stride=1):
+        """The MFP and cumulative-row files a Fortran run caches
+        (trekis_save_mfp_tables) written from these tables into out_dir."""
+        oc, keep = output_names(self.w)
+        abi.check(self.lib.trekis_save_mfp_tables(self.h, C.byref(oc), str(out_dir).encode(), int(with_rows),
+                                                  int(row_stride)), self.lib)
+
     def close(self):
         if self.h:
             self.lib.trekis_tables_free(self.h)
@@ -235,6 +242,29 @@ def shell_name(designator):
     return "K-shell"
 
 
+def output_names(w, **kw):
+    """trekis_output_cfg with the element and shell names of workload w (and
+    the byte strings it points to, which the caller keeps alive)."""
+    enc = lambda x: x.encode()
+    keep = []
+    oc = abi.OutputCfg(**kw)
+    for a, atom in enumerate(w.material.atoms):
+        nm = enc(ELEMENTS[atom.Z - 1])
+        keep.append(nm)
+        oc.atom_names[a] = nm
+        for s_, sh in enumerate(atom.shells):
+            sn = enc(shell_name(sh.designator))
+            keep.append(sn)
+            oc.shell_names[a][s_] = sn
+    return oc, keep
+
+
+def read_table_file(path):
+    """A cached MFP or row file of the reference's format as an array of its
+    numeric columns (rows x columns)."""
+    return np.loadtxt(path, ndmin=2)
+
+
 def save_output(w, tallies, NMC, out_dir, ion_name=None, ion_Zeff=-1.0, duration_s=-1.0, opt=None, lib=None):
     """Write the reference's output files (Save_output) for the un-normalised
     sums of NMC iterations of workload w; returns the run folder's path.
@@ -245,17 +275,8 @@ def save_output(w, tallies, NMC, out_dir, ion_name=None, ion_Zeff=-1.0, duration
     ion = ion_struct(w)
     cfg, R = run_cfg(w, opt or RunOptions(), NMC)
     enc = lambda x: x.encode()
-    keep = []
-    oc = abi.OutputCfg(out_dir=enc(str(out_dir)), ion_name=enc(ion_name or ELEMENTS[w.ion_Z - 1]),
-                       material_name=enc(m.name), ion_Zeff=ion_Zeff, duration_s=duration_s, NMC=int(NMC))
-    for a, atom in enumerate(m.atoms):
-        nm = enc(ELEMENTS[atom.Z - 1])
-        keep.append(nm)
-        oc.atom_names[a] = nm
-        for s_, sh in enumerate(atom.shells):
-            sn = enc(shell_name(sh.designator))
-            keep.append(sn)
-            oc.shell_names[a][s_] = sn
+    oc, keep = output_names(w, out_dir=enc(str(out_dir)), ion_name=enc(ion_name or ELEMENTS[w.ion_Z - 1]),
+                            material_name=enc(m.name), ion_Zeff=ion_Zeff, duration_s=duration_s, NMC=int(NMC))
     ct = tallies.c()
     buf = C.create_string_buffer(4096)
     abi.check(lib.trekis_save_output(C.byref(oc), mat.ref(), C.byref(ion), C.byref(cfg), C.byref(ct), buf,
