@@ -289,6 +289,9 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+_ORACLE_TABLES = {}
+
+
 def cpu_baseline(args, n_it=None, nthreads=None):
     """The FP64 oracle (restatement of the reference's loop) on the host cores:
     one cfg1 iteration per thread, heap-ordered earliest-event loop."""
@@ -297,10 +300,12 @@ def cpu_baseline(args, n_it=None, nthreads=None):
     w = workload()
     nthreads = nthreads or os.cpu_count() or 1
     n_it = n_it or args.cpu_iters or nthreads
-    h = w.material.to_c()
-    ion = api.ion_struct(w)
-    tc = abi.TableCfg(build_shi=1, build_photon=1, shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
-    o = oracle_py.OracleTables(h, ion, tc, nthreads=nthreads)
+    if nthreads not in _ORACLE_TABLES:   # built once per thread count (the reference arm times several steps)
+        h = w.material.to_c()
+        ion = api.ion_struct(w)
+        tc = abi.TableCfg(build_shi=1, build_photon=1, shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+        _ORACLE_TABLES[nthreads] = (h, oracle_py.OracleTables(h, ion, tc, nthreads=nthreads))
+    o = _ORACLE_TABLES[nthreads][1]
     tal = api.new_tallies(w)
     cfg, R = api.run_cfg(w, api.RunOptions(precision=1, seed=args.seed, iteration_offset=900000), NMC=n_it)
     st = abi.Status.fresh()
