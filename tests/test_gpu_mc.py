@@ -5,7 +5,9 @@
   (2^-24 eV per particle energy, 2^-40 eV per lattice deposit).
 * FP32 mode: radial electron density and energy density agree with the FP64
   oracle within 3 combined standard errors in >= 97 % of the populated
-  (time, radius) bins (batch-means errors over independent seeds).
+  (time, radius) bins (batch-means errors over independent seeds); with
+  mobile holes and photons (cfg1) and phonon-CDF elastic scattering (cfg4)
+  also the lattice energy and the valence holes' density and kinetic energy.
 * Scheduling knobs (events per step, block size) do not change a single bit;
   batch sizes only change the order of the FP64 batch sums.
 """
@@ -151,6 +153,53 @@ def test_fp32_statistically_equal_to_oracle(gpu_lib):
         live = se > 1e-12 * np.max(np.abs(mr))
         frac = np.mean(np.abs(mg[live] - mr[live]) <= 3 * se[live])
         assert live.sum() > 100
+        assert frac >= 0.97, (k, frac)
+
+
+def _vb(w):
+    return [(a, s) for a, at in enumerate(w.material.atoms) for s, sh in enumerate(at.shells) if sh.designator >= 63][0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["cfg1", "cfg4"])
+def test_fp32_statistically_equal_to_oracle_mobile_holes(gpu_lib, case):
+    """FP32 kinematics of mobile valence holes, photons (cfg1) and the
+    phonon-CDF elastic draw (cfg4): electron density and energy, lattice
+    energy, and the valence holes' density and kinetic energy agree with the
+    FP64 oracle within 3 batch-means standard errors in >= 97 % of the live
+    (time, radius) bins, independent seeds."""
+    if case == "cfg1":
+        w = configs.small(configs.cfg1, NMC=4, Tim=30.0)
+    else:
+        w = configs.small(configs.cfg4, NMC=4, Tim=20.0, ion_E=50e6)
+    t = api.Tables(w, lib=gpu_lib)
+    o = _oracle_on(t, w)
+    a, s = _vb(w)
+    keys = ("Out_ne", "Out_Ee", "Out_Elat", "vb_nh", "vb_Ehkin")
+
+    def pick(tal):
+        d = {k: tal[k] / w.NMC for k in ("Out_ne", "Out_Ee", "Out_Elat")}
+        d["vb_nh"] = tal.view("Out_nh")[:, :, a, s].ravel() / w.NMC
+        d["vb_Ehkin"] = tal.view("Out_Ehkin")[:, :, a, s].ravel() / w.NMC
+        return d
+
+    nb = 16
+    G = {k: [] for k in keys}
+    R = {k: [] for k in keys}
+    for b in range(nb):
+        g, _ = api.mc_run(t, api.RunOptions(seed=2000 + b))
+        r, _ = _oracle_run(o, w, api.RunOptions(precision=1, seed=7000 + b))
+        pg, pr = pick(g), pick(r)
+        for k in keys:
+            G[k].append(pg[k])
+            R[k].append(pr[k])
+    for k in keys:
+        g, r = np.array(G[k]), np.array(R[k])
+        mg, mr = g.mean(0), r.mean(0)
+        se = np.sqrt(g.var(0, ddof=1) / nb + r.var(0, ddof=1) / nb)
+        live = se > 1e-12 * np.max(np.abs(mr))
+        frac = np.mean(np.abs(mg[live] - mr[live]) <= 3 * se[live])
+        assert live.sum() > 50, (k, live.sum())
         assert frac >= 0.97, (k, frac)
 
 
