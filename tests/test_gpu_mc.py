@@ -4,7 +4,7 @@
   equals the oracle's chronological loop to the fixed-point resolution
   (2^-24 eV per particle energy, 2^-40 eV per lattice deposit).
 * FP32 mode: radial electron density and energy density agree with the FP64
-  oracle within 3 combined standard errors in >= 97 % of the populated
+  oracle within 3 combined standard errors in >= 98 % of the populated
   (time, radius) bins (batch-means errors over independent seeds); with
   mobile holes and photons (cfg1) and phonon-CDF elastic scattering (cfg4)
   also the lattice energy and the valence holes' density and kinetic energy.
@@ -133,11 +133,11 @@ def test_shards_sum(small0):
 @pytest.mark.gpu
 def test_fp32_statistically_equal_to_oracle(gpu_lib):
     """3-sigma agreement of Out_ne / Out_Ee between FP32 GPU and FP64 oracle,
-    independent seeds, batch-means standard errors."""
+    independent seeds, batch-means standard errors (32 batches)."""
     w = configs.small(configs.cfg0, NMC=4, layer=10.0, Tim=20.0)
     t = api.Tables(w, lib=gpu_lib)
     o = _oracle_on(t, w)
-    nb = 16
+    nb = 32
     G = {k: [] for k in ("Out_ne", "Out_Ee")}
     R = {k: [] for k in ("Out_ne", "Out_Ee")}
     for b in range(nb):
@@ -147,13 +147,27 @@ def test_fp32_statistically_equal_to_oracle(gpu_lib):
             G[k].append(g[k] / w.NMC)
             R[k].append(r[k] / w.NMC)
     for k in G:
-        g, r = np.array(G[k]), np.array(R[k])
-        mg, mr = g.mean(0), r.mean(0)
-        se = np.sqrt(g.var(0, ddof=1) / nb + r.var(0, ddof=1) / nb)
-        live = se > 1e-12 * np.max(np.abs(mr))
-        frac = np.mean(np.abs(mg[live] - mr[live]) <= 3 * se[live])
-        assert live.sum() > 100
-        assert frac >= 0.97, (k, frac)
+        _assert_3sigma(k, np.array(G[k]), np.array(R[k]), min_live=100)
+
+
+def _assert_3sigma(k, g, r, min_live):
+    """>= 98 % of the live bins within 3 combined batch-means standard errors
+    and chi^2 per bin of the standardised differences below 1.5 (both
+    printed).  Bins of one radius are strongly correlated in time (a stopped
+    particle stays in its bin), so one fluctuation can move a whole column;
+    measured fractions are 98.9-99.9 %.  FP32 bias is bounded separately by
+    the paired test against FP64 runs of the same streams."""
+    nb = g.shape[0]
+    mg, mr = g.mean(0), r.mean(0)
+    se = np.sqrt(g.var(0, ddof=1) / nb + r.var(0, ddof=1) / nb)
+    live = se > 1e-12 * np.max(np.abs(mr))
+    z = (mg[live] - mr[live]) / se[live]
+    frac = np.mean(np.abs(z) <= 3)
+    chi2 = float(np.mean(z * z))
+    print(f"{k}: {live.sum()} live bins, {100 * frac:.2f} % within 3 sigma, chi2/bin {chi2:.3f}")
+    assert live.sum() > min_live, (k, live.sum())
+    assert frac >= 0.98, (k, frac, chi2)
+    assert chi2 < 1.5, (k, chi2)
 
 
 def _vb(w):
@@ -166,7 +180,7 @@ def test_fp32_statistically_equal_to_oracle_mobile_holes(gpu_lib, case):
     """FP32 kinematics of mobile valence holes, photons (cfg1) and the
     phonon-CDF elastic draw (cfg4): electron density and energy, lattice
     energy, and the valence holes' density and kinetic energy agree with the
-    FP64 oracle within 3 batch-means standard errors in >= 97 % of the live
+    FP64 oracle within 3 batch-means standard errors in >= 98 % of the live
     (time, radius) bins, independent seeds."""
     if case == "cfg1":
         w = configs.small(configs.cfg1, NMC=4, Tim=30.0)
@@ -183,7 +197,7 @@ def test_fp32_statistically_equal_to_oracle_mobile_holes(gpu_lib, case):
         d["vb_Ehkin"] = tal.view("Out_Ehkin")[:, :, a, s].ravel() / w.NMC
         return d
 
-    nb = 16
+    nb = 32
     G = {k: [] for k in keys}
     R = {k: [] for k in keys}
     for b in range(nb):
@@ -194,13 +208,33 @@ def test_fp32_statistically_equal_to_oracle_mobile_holes(gpu_lib, case):
             G[k].append(pg[k])
             R[k].append(pr[k])
     for k in keys:
-        g, r = np.array(G[k]), np.array(R[k])
-        mg, mr = g.mean(0), r.mean(0)
-        se = np.sqrt(g.var(0, ddof=1) / nb + r.var(0, ddof=1) / nb)
-        live = se > 1e-12 * np.max(np.abs(mr))
-        frac = np.mean(np.abs(mg[live] - mr[live]) <= 3 * se[live])
-        assert live.sum() > 50, (k, live.sum())
-        assert frac >= 0.97, (k, frac)
+        _assert_3sigma(k, np.array(G[k]), np.array(R[k]), min_live=50)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["cfg1", "cfg4"])
+def test_fp32_bias_against_fp64_same_streams(gpu_lib, case):
+    """FP32 and FP64 runs of the same Philox streams differ only by rounding:
+    over 64 seeds the mean relative difference of every total (electrons,
+    electron energy, lattice energy, valence holes, collision counts) stays
+    below 5e-4, against about 7e-2 seed-to-seed spread per run."""
+    if case == "cfg1":
+        w = configs.small(configs.cfg1, NMC=4, Tim=30.0)
+    else:
+        w = configs.small(configs.cfg4, NMC=4, Tim=20.0, ion_E=50e6)
+    t = api.Tables(w, lib=gpu_lib)
+    a, s = _vb(w)
+    rows = []
+    for b in range(64):
+        g, sg = api.mc_run(t, api.RunOptions(seed=9000 + b))
+        d, sd = api.mc_run(t, api.RunOptions(precision=1, seed=9000 + b))
+        rows.append([(g[k].sum(), d[k].sum()) for k in ("Out_ne", "Out_Ee", "Out_Elat")] +
+                    [(g.view("Out_nh")[:, :, a, s].sum(), d.view("Out_nh")[:, :, a, s].sum()),
+                     (sg.n_events, sd.n_events), (sg.n_hole_events, sd.n_hole_events)])
+    x = np.array(rows, dtype=np.float64)          # [seed, quantity, (fp32, fp64)]
+    rel = (x[:, :, 0] - x[:, :, 1]) / np.abs(x[:, :, 1]).mean(0)
+    print("mean relative FP32-FP64 differences:", rel.mean(0))
+    assert np.all(np.abs(rel.mean(0)) < 5e-4), rel.mean(0)
 
 
 @pytest.mark.gpu
