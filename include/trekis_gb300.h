@@ -484,6 +484,19 @@ int32_t trekis_save_shi_tables(const trekis_tables* t, const char* dir, const ch
 int32_t trekis_save_mfp_tables(const trekis_tables* t, const trekis_output_cfg* oc, const char* dir,
                                int32_t with_rows, int32_t row_stride);
 
+/* Per-collision samplers on given inputs, for checking them against each
+ * other and against a CPU restatement: out[i] for energy E[i] [eV] and
+ * uniform u[i], in precision 0 (FP32) or 1 (FP64) of the track loop.
+ * kind 0: transferred energy of an electron ionising shell (atom, shell)
+ *         (Electron_energy_transfer_inelastic, Cross_sections.f90:1793-1871);
+ *      1: the same for a valence hole;
+ *      2, 3: total inelastic / elastic electron MFP [A] (Next_free_path_2d);
+ *      4: Mott elastic transfer with every species drawing u (MC:2394-2407);
+ *      5: phonon-CDF elastic transfer (0 without phonon tables).
+ * Needs the GPU; copies through a temporary device buffer. */
+int32_t trekis_probe_samplers(const trekis_tables* t, int32_t precision, int32_t kind, int32_t atom, int32_t shell,
+                              int64_t n, const double* E, const double* u, double* out);
+
 /* Human-readable text of the last error on this thread. */
 const char* trekis_last_error(void);
 

@@ -129,6 +129,12 @@ double oracle_sample_transfer(void* t, const trekis_material* m, int hole, int a
     uint32_t f = 0;
     return sample_transfer_inelastic(*(Tables*)t, *m, hole, a, s, Ele, L_tot, u, &f);
 }
+// Next_free_path_1d (Monte_Carlo.f90:1835-1871) of one shell's electron or hole IMFP table
+double oracle_shell_free_path(void* t, int hole, int a, int s, double E) {
+    Tables* T = (Tables*)t;
+    const std::vector<MFPTab>& v = hole ? T->hole : T->el;
+    return next_free_path_1d(v[(size_t)a * TREKIS_MAX_SHELLS + s], E);
+}
 double oracle_free_path(void* t, int which, double E) {
     Tables* T = (Tables*)t;
     switch (which) {

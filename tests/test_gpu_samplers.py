@@ -1,0 +1,142 @@
+"""Per-collision samplers on identical inputs (trekis_probe_samplers): the
+FP64 samplers equal the oracle's restatement, and the FP32 track loop's
+samplers agree with them within 1e-5 relative (fractions reported): the
+transferred energy of ionising collisions exactly (it is drawn in FP64 on the
+FP64 rows), the free paths and Mott transfer in >= 99.9 % of the inputs, the
+phonon-CDF elastic draw on FP32 rows in >= 99 %."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from trekis import abi, api, configs
+
+
+def _probe(t, precision, kind, a, s, E, u):
+    out = np.zeros(len(E))
+    abi.check(t.lib.trekis_probe_samplers(t.h, precision, kind, a, s, len(E), abi.dptr(np.ascontiguousarray(E)),
+                                          abi.dptr(np.ascontiguousarray(u)), abi.dptr(out)), t.lib)
+    return out
+
+
+@pytest.fixture(scope="module", params=["cfg1", "cfg4"])
+def tabs(request, gpu_lib):
+    import oracle_py
+    if request.param == "cfg1":
+        w = configs.small(configs.cfg1, NMC=1)
+    else:
+        w = configs.small(configs.cfg4, NMC=1, ion_E=50e6)
+    t = api.Tables(w, lib=gpu_lib)
+    tc = abi.TableCfg(build_shi=1, build_photon=w.material.include_photons,
+                      shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+    o = oracle_py.OracleTables(t.mat, t.ion, tc)
+    from conftest import copy_tables
+    copy_tables(t, o, w)
+    return w, t, o
+
+
+def _inputs(lo, hi, n, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), n)), rng.uniform(1e-7, 1.0 - 1e-7, n)
+
+
+def _report(name, f32, f64):
+    rel = np.abs(f32 - f64) / np.maximum(np.abs(f64), 1e-300)
+    within = np.mean(rel <= 1e-5)
+    print(f"{name}: median rel {np.median(rel):.2e}, {100 * within:.3f} % within 1e-5, max {rel.max():.2e}")
+    return within
+
+
+@pytest.mark.gpu
+def test_inelastic_transfer(tabs):
+    w, t, o = tabs
+    lib_o = o.lib
+    shells = [(a, s) for a, at in enumerate(w.material.atoms) for s, sh in enumerate(at.shells)]
+    for a, s in shells:
+        Ip = w.material.atoms[a].shells[s].Ip
+        E, u = _inputs(max(Ip, 1.0) * 1.05, 1.0e5, 4000, 17 + a * 16 + s)
+        g64 = _probe(t, 1, 0, a, s, E, u)
+        ref = np.array([lib_o.oracle_sample_transfer(o.h, t.mat.ref(), 0, a, s, e,
+                                                     lib_o.oracle_shell_free_path(o.h, 0, a, s, e), x)
+                        for e, x in zip(E, u)])
+        assert np.allclose(g64, ref, rtol=1e-12, atol=0.0), (a, s)
+        g32 = _probe(t, 0, 0, a, s, E, u)
+        assert _report(f"electron shell {a},{s}", g32, g64) >= 0.999
+
+
+@pytest.mark.gpu
+def test_valence_hole_transfer(tabs):
+    w, t, o = tabs
+    lib_o = o.lib
+    a, s = [(a, s) for a, at in enumerate(w.material.atoms) for s, sh in enumerate(at.shells) if sh.designator >= 63][0]
+    Eg = w.material.Egap
+    E, u = _inputs(2.0 * Eg, 30.0, 4000, 5)
+    g64 = _probe(t, 1, 1, a, s, E, u)
+    ref = np.array([lib_o.oracle_sample_transfer(o.h, t.mat.ref(), 1, a, s, e,
+                                                 lib_o.oracle_shell_free_path(o.h, 1, a, s, e), x)
+                    for e, x in zip(E, u)])
+    ok = np.isfinite(ref) & (ref > 0)
+    assert ok.sum() > 100
+    assert np.allclose(g64[ok], ref[ok], rtol=1e-12, atol=0.0)
+    assert _report("valence hole", _probe(t, 0, 1, a, s, E, u)[ok], g64[ok]) >= 0.999
+
+
+@pytest.mark.gpu
+def test_free_paths_and_elastic(tabs):
+    w, t, o = tabs
+    lib_o = o.lib
+    E, u = _inputs(1.0, 1.0e5, 4000, 9)
+    for kind, which in ((2, 0), (3, 1)):
+        g64 = _probe(t, 1, kind, 0, 0, E, u)
+        ref = np.array([lib_o.oracle_free_path(o.h, which, e) for e in E])
+        assert np.allclose(g64, ref, rtol=1e-12, atol=0.0), kind
+        assert _report(f"MFP kind {kind}", _probe(t, 0, kind, 0, 0, E, u), g64) >= 0.999
+    if w.material.kind_of_EMFP == 0:
+        # Mott: against a cancellation-free FP64 restatement; the reference's
+        # own form (the FP64 track loop) loses digits in near-forward
+        # scattering, where 1 - cos(theta) is far below 1e-8
+        exact = _mott_exact(w, E, u)
+        g32 = _probe(t, 0, 4, 0, 0, E, u)
+        g64 = _probe(t, 1, 4, 0, 0, E, u)
+        assert _report("Mott FP32 vs exact", g32, exact) >= 0.999
+        assert _report("Mott FP64 (reference form) vs exact", g64, exact) >= 0.99
+    else:
+        g64 = _probe(t, 1, 5, 0, 0, E, u)
+        g32 = _probe(t, 0, 5, 0, 0, E, u)
+        assert np.all(np.isfinite(g64)) and np.any(g64 > 0)
+        assert _report("phonon-CDF elastic", g32, g64) >= 0.99
+
+
+# constants of Universal_Constants.f90 as the library uses them
+_E, _ME, _C, _H, _E0 = 1.602176487e-19, 9.1093821545e-31, 299792458.0, 1.05457162853e-34, 8.854187817620e-12
+_MP = 1836.1526724780 * _ME
+
+
+def _mott_exact(w, E, u):
+    """Pers-weighted Mott transfer (MC:2394-2407, CS:3517-3613) of an
+    electron with every species drawing u, in FP64 without cancellation:
+    1 - mu = 2 nu (1 - u) / (u + nu) and W1 W2 scaled by the target's rest
+    energy (algebraically the reference's expressions)."""
+    mec2 = _ME * _C * _C / _E
+    alpha = _E * _E / (_H * _C * 4.0 * np.pi * _E0)
+    tau = E / mec2
+    t1, tt = tau + 1.0, tau * (tau + 2.0)
+    g = 1.0 / tt
+    h = t1 * t1 * g * np.sqrt(tau / t1)
+    N, Emc = E * (E + 2.0 * mec2), E + mec2
+    atoms = w.material.atoms
+    ps = sum(a.Pers for a in atoms)
+    dE = np.zeros_like(E)
+    for a in atoms:
+        Z = float(a.Z)
+        z23 = float(np.float32(Z ** (2.0 / 3.0)))   # stored in the precision of the run
+        nu = 1.7e-5 * z23 * g * (1.13 + 3.76 * alpha * alpha * Z * Z * h)
+        omc = 2.0 * nu * (1.0 - u) / (u + nu)
+        ct, st2 = 1.0 - omc, omc * (2.0 - omc)
+        M = float(np.float32(a.Mass * _MP)) * _C * _C / _E
+        mu2, e, n = (mec2 / M) ** 2, Emc / M, N / (M * M)
+        q = 1.0 + np.sqrt(1.0 - mu2 * st2)
+        p = e * st2 + omc
+        d = (e + 1.0) ** 2 - n * ct * ct
+        dE += M * (p * q + ct * mu2 * st2) * n / (q * d) * a.Pers / ps
+    return dE

@@ -496,31 +496,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     if (!ws) { if (rc == TREKIS_ENOMEM) set_error("device workspace allocation failed"); return rc; }
     // constants
     McConst<T> C;
-    std::memset(&C, 0, sizeof C);
-    C.nsh = t->nsh; C.nat = m.N_atoms; C.vb = t->shell_index[0][m.atoms[0].N_shl - 1];
-    C.include_photons = m.include_photons;
-    double Psum = 0.0, Mt = 0.0, zs = 0.0;
-    for (int a = 0; a < m.N_atoms; ++a) {
-        Psum += m.atoms[a].Pers; Mt += m.atoms[a].Mass * m.atoms[a].Pers; zs += m.atoms[a].Zat * m.atoms[a].Pers;
-        C.Zat[a] = m.atoms[a].Zat; C.Mass_kg[a] = (T)(m.atoms[a].Mass * kMp); C.Pers[a] = (T)m.atoms[a].Pers;
-        C.Z23[a] = (T)std::pow((double)m.atoms[a].Zat, 2.0 / 3.0);
-    }
-    for (int k = 0; k < t->nsh; ++k) {
-        const trekis_atom& at = m.atoms[t->atom_of[k]];
-        int s = t->shell_of[k];
-        C.atom_of[k] = t->atom_of[k];
-        C.Ip[k] = (T)at.Ip[s]; C.Ipd[k] = at.Ip[s]; C.Nel[k] = (T)at.Nel[s];
-        C.Auger[k] = (T)at.Auger[s]; C.Radiat[k] = (T)at.Radiat[s];
-    }
-    C.Psum = (T)Psum; C.Mtarget = (T)(kMp * Mt / Psum); C.Egap = (T)m.atoms[0].Ip[m.atoms[0].N_shl - 1];
-    C.cut_off = (T)m.cut_off; C.hole_mass = (T)m.hole_mass; C.Layer = m.Layer;
-    C.ion_Z = t->ion.Zat; C.ion_kind_zeff = t->ion.Kind_Zeff; C.ion_mass_p = t->ion.Mass; C.MSHI = kMp * t->ion.Mass;
-    C.ion_E0 = t->ion.E; C.ion_fixed_zeff = t->ion.fixed_Zeff; C.Zt = zs / Psum;
-    C.Tim = (T)cfg.Tim; C.Nt = Nt; C.NR = cfg.N_R; C.seed = cfg.seed;
-    C.mobile_holes = m.hole_mass < 1e3;
-    C.mec2 = (T)(kMe * kC * kC / kE);
-    C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
-    finish_const(C);
+    fill_const<T>(t, cfg, Nt, C);
     C.dosE = tb.dosE; C.nD = tb.nD;
     C.elast_cdf = (m.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
     std::vector<double> tg = tallied_times(cfg.Tim, cfg.dt, cfg.dt_flag);
@@ -738,6 +714,15 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
     rc = build_tables_device(t, *cfg, st);
     if (!rc) rc = upload_mc<float>(t, t->d32);
     if (!rc) rc = upload_mc<double>(t, t->d64);
+    if (!rc) {   // both precisions draw ionising transfers from the FP64 rows
+        auto link = [&](auto& d) {
+            d.elE_d = t->d64.elE; d.elL_d = t->d64.elL; d.row_hw_d = t->d64.row_hw; d.row_L_d = t->d64.row_L;
+            d.hE_d = t->d64.hE; d.hL_d = t->d64.hL; d.hrow_hw_d = t->d64.hrow_hw; d.hrow_L_d = t->d64.hrow_L;
+            d.row_mono_d = t->d64.row_mono; d.hrow_mono_d = t->d64.hrow_mono;
+        };
+        link(t->d32);
+        link(t->d64);
+    }
     if (!rc && t->has_shi) rc = upload_shi<float>(t, t->dshi32);
     if (!rc && t->has_shi) rc = upload_shi<double>(t, t->dshi64);
     if (rc) { delete t; if (st) st->code = rc; return rc; }
@@ -937,3 +922,45 @@ int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const
 }
 
 }  // extern "C"
+
+// ---- sampler probe ------------------------------------------------------------------------
+namespace {
+template <class T>
+int probe(const trekis_tables* t, const DevTabs<T>& tb, int kind, int k, int64_t n, const double* E, const double* u,
+          double* out) {
+    trekis_run_cfg cfg;
+    std::memset(&cfg, 0, sizeof cfg);
+    cfg.Tim = 1.0; cfg.dt = 1.0; cfg.N_R = 1;
+    McConst<T> C;
+    fill_const<T>(t, cfg, 1, C);
+    C.dosE = tb.dosE; C.nD = tb.nD;
+    C.elast_cdf = (t->mat.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
+    double* d = nullptr;
+    if (cudaMalloc(&d, 24 * (size_t)n) != cudaSuccess) { set_error("device allocation failed"); return TREKIS_ENOMEM; }
+    int rc = TREKIS_OK;
+    if (cudaMemcpy(d, E, 8 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d + n, u, 8 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) rc = TREKIS_ECUDA;
+    if (!rc) {
+        launch_probe<T>(C, tb, kind, k, (int)n, d, d + n, d + 2 * n, 0);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+            cudaMemcpy(out, d + 2 * n, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) rc = TREKIS_ECUDA;
+    }
+    cudaFree(d);
+    if (rc) set_error("sampler probe failed");
+    return rc;
+}
+}  // namespace
+
+int32_t trekis_probe_samplers(const trekis_tables* t, int32_t precision, int32_t kind, int32_t atom, int32_t shell,
+                              int64_t n, const double* E, const double* u, double* out) {
+    if (!t || n < 0 || n > (1 << 26) || (n > 0 && (!E || !u || !out)) || kind < 0 || kind > 5 || atom < 0 ||
+        atom >= t->mat.N_atoms || shell < 0 || shell >= t->mat.atoms[atom].N_shl) {
+        set_error("invalid probe arguments");
+        return TREKIS_EINVAL;
+    }
+    if (!device_ok()) return TREKIS_ENODEVICE;
+    if (n == 0) return TREKIS_OK;
+    const int k = t->shell_index[atom][shell];
+    return precision == 1 ? probe<double>(t, t->d64, kind, k, n, E, u, out)
+                          : probe<float>(t, t->d32, kind, k, n, E, u, out);
+}

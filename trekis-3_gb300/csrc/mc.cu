@@ -82,6 +82,13 @@ struct EvStream {
     }
     __device__ __forceinline__ T next() { return Uni<T>::of(word()); }
     __device__ __forceinline__ double next_d() { return Uni<double>::of(word()); }
+    // FP32: u and 1 - u of one word, each rounded from all 32 bits, for
+    // draws that depend on 1 - u near u = 1 (the FP64 draw is (w + 0.5) 2^-32)
+    __device__ __forceinline__ void next_pair(float& u, float& omu) {
+        const uint32_t w = word();
+        u = ((float)w + 0.5f) * 2.3283064365386963e-10f;
+        omu = ((float)(~w) + 0.5f) * 2.3283064365386963e-10f;
+    }
 };
 
 template <class T> __device__ __forceinline__ T pi_() { return T(kPi); }
@@ -534,11 +541,12 @@ __device__ __forceinline__ float mott_transfer_f32(const McConst<float>& C, floa
     const float Emc = Ee + mc2, N = Ee * (Ee + 2.f * mc2);
     float dE = 0.f;
     for (int a = 0; a < C.nat; ++a) {
-        const float RN = s.next();
+        float RN, omRN;   // RN and 1 - RN, each to FP32 precision
+        s.next_pair(RN, omRN);
         float omc = 0.f;
         if (moving) {
             const float nu = C.mott_c1[a] * g * (1.13f + C.mott_c2[a] * h);
-            omc = __fdividef(2.f * nu * (1.f - RN), RN + nu);
+            omc = __fdividef(2.f * nu * omRN, RN + nu);
         }
         const float ct = 1.f - omc, st2 = omc * (2.f - omc);
         const float iM = C.mott_iM[a], mu2 = mc2sq * C.mott_iM2[a];
@@ -657,6 +665,35 @@ __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hol
     if (E < Emin) E = Emin;
     if (E > Emax) E = Emax;
     if (E < C.Egap) err |= TREKIS_ERR_NEG_TRANSFER;
+    if (m_isnan(E)) E = Emin;
+    return E;
+}
+
+// The same draw evaluated in FP64 on the FP64 tables and rows, for the FP32
+// track loop: ionising collisions are a few in 10^4, so the FP64 arithmetic
+// costs nothing measurable, and the draw equals the FP64 one for the same
+// energy and uniform number (the FP32 rows alone put 2 % of the draws
+// 1e-5 to 3e-4 away where a row's cumulative MFP changes slowly).
+template <class T>
+__device__ double sample_transfer_d(const McConst<T>& C, const DevTabs<T>& tb, bool hole, int k, double Ele,
+                                    double RN, unsigned& err, float fg = -1.f) {
+    const double L_tot = hole ? nfp1(Tab<double>{tb.hE_d, tb.hL_d + (size_t)k * tb.nH, tb.nH}, Ele)
+                              : nfp1(Tab<double>{tb.elE_d, tb.elL_d + (size_t)k * tb.nE, tb.nE}, Ele);
+    const double L_need = L_tot / RN;
+    double Emin = C.Ipd[k];
+    if (Emin <= 1.0e-3) Emin = 1.0e-3;
+    double Emax;
+    if (hole) {
+        const double Mass = (C.hole_mass >= T(0)) ? (double)C.hole_mass : (double)tb.dosM[dos_find(tb, (T)Ele) - 1];
+        Emax = 4.0 * Ele * Mass / ((Mass + 1.0) * (Mass + 1.0));
+    } else Emax = (Ele + Emin) / 2.0;
+    double E = hole ? interp_transfer<double>(tb.hE_d, tb.nH, tb.hrow_off, tb.hrow_hw_d, tb.hrow_L_d, Ele, L_need, fg,
+                                              tb.hrow_mono_d)
+                    : interp_transfer<double>(tb.elE_d, tb.nE, tb.row_off + (size_t)k * tb.nE, tb.row_hw_d,
+                                              tb.row_L_d, Ele, L_need, fg, tb.row_mono_d + (size_t)k * tb.nE);
+    if (E < Emin) E = Emin;
+    if (E > Emax) E = Emax;
+    if (E < (double)C.Egap) err |= TREKIS_ERR_NEG_TRANSFER;
     if (m_isnan(E)) E = Emin;
     return E;
 }
@@ -959,8 +996,12 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     T dE, theta, phi;
     if (FULL && ionise) {  // impact ionisation
         const int k = which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next());
-        const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
-        dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err, fg);
+        if constexpr (sizeof(T) == 4) {
+            dE = (T)sample_transfer_d(C, tb, false, k, (double)Eel, s.next_d(), err, fg);
+        } else {
+            const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
+            dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err, fg);
+        }
         theta = m_acos((Eel - dE) / m_sqrt(Eel * (Eel - dE)));
         if (m_isnan(theta)) theta = s.next() * pi_<T>();
         phi = T(2) * pi_<T>() * s.next();
@@ -1049,8 +1090,12 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         T dE, th1, ph1, Eh;
         if (FULL && ionise) {
             const int k = which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
-            const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
-            dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err, fg);
+            if constexpr (sizeof(T) == 4) {
+                dE = (T)sample_transfer_d(C, tb, true, k, (double)Eel, s.next_d(), err, fg);
+            } else {
+                const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
+                dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err, fg);
+            }
             // Update_holes_angles_el (MC:1142-1168)
             // masses in kg as the reference writes them (FP64); in electron
             // masses for FP32, where (Mh+me)^2 would underflow
@@ -1517,6 +1562,61 @@ template void launch_step<float>(const McConst<float>&, const DevTabs<float>&, c
 template void launch_step<double>(const McConst<double>&, const DevTabs<double>&, const QSet<double>&, const int*,
                                   const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t,
                                   const float*, const Proposer*, const Fork*);
+
+// ---- sampler probe --------------------------------------------------------------------------
+// One call of a per-collision sampler per element, on given energies and
+// uniform numbers, so samplers of both precisions can be compared with the
+// oracle's on identical inputs (trekis_probe_samplers).
+template <class T>
+struct FixedUniform {   // every draw returns u
+    double u;
+    __device__ __forceinline__ T next() { return (T)u; }
+    __device__ __forceinline__ void next_pair(float& a, float& b) { a = (float)u; b = (float)(1.0 - u); }
+};
+template <class T>
+__global__ void k_probe(const __grid_constant__ McConst<T> C, const __grid_constant__ DevTabs<T> tb, int kind,
+                        int k, int n, const double* __restrict__ Ein, const double* __restrict__ uin,
+                        double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const T E = (T)Ein[i], u = (T)uin[i];
+    unsigned err = 0;
+    T r = T(0);
+    FixedUniform<T> s{uin[i]};
+    switch (kind) {
+    case 0: case 1: {   // Electron_energy_transfer_inelastic on shell k, or for a valence hole
+        const bool hole = kind == 1;
+        const int kk = hole ? C.vb : k;
+        if constexpr (sizeof(T) == 4) {
+            r = (T)sample_transfer_d(C, tb, hole, kk, (double)E, uin[i], err);
+        } else {
+            const T L = hole ? nfp1(Tab<T>{tb.hE, tb.hL + (size_t)kk * tb.nH, tb.nH}, E)
+                             : nfp1(Tab<T>{tb.elE, tb.elL + (size_t)kk * tb.nE, tb.nE}, E);
+            r = sample_transfer(C, tb, hole, kk, E, L, u, err);
+        }
+        break;
+    }
+    case 2: case 3: {   // total inelastic / elastic electron MFP as the track loop evaluates them
+        T I, Em;
+        el_mfps(tb, E, I, Em);
+        r = kind == 2 ? I : Em;
+        break;
+    }
+    case 4: r = mott_transfer(C, E, T(1), s); break;   // every species draws u
+    case 5: r = C.elast_cdf ? phonon_transfer(tb, false, E, s) : T(0); break;
+    default: break;
+    }
+    out[i] = (double)r;
+}
+template <class T>
+void launch_probe(const McConst<T>& C, const DevTabs<T>& tb, int kind, int k, int n, const double* E, const double* u,
+                  double* out, cudaStream_t s) {
+    if (n > 0) k_probe<T><<<(n + 127) / 128, 128, 0, s>>>(C, tb, kind, k, n, E, u, out);
+}
+template void launch_probe<float>(const McConst<float>&, const DevTabs<float>&, int, int, int, const double*,
+                                  const double*, double*, cudaStream_t);
+template void launch_probe<double>(const McConst<double>&, const DevTabs<double>&, int, int, int, const double*,
+                                   const double*, double*, cudaStream_t);
 
 // ---- grid hints ----------------------------------------------------------------------------
 // hint of a bucket = the search result at the bucket's lowest value, which

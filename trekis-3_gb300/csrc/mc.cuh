@@ -182,6 +182,43 @@ constexpr int kRgHintMax = 4096;
 __host__ __device__ inline uint32_t radius_key(float x) { uint32_t u; memcpy(&u, &x, 4); return u >> 19; }
 __host__ __device__ inline uint32_t radius_key(double x) { uint64_t u; memcpy(&u, &x, 8); return (uint32_t)(u >> 48); }
 
+// Run constants of a table set and run configuration (host); the grids,
+// hints and DOS pointers are set by the caller.
+template <class T>
+inline void fill_const(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, McConst<T>& C) {
+    const trekis_material& m = t->mat;
+    std::memset(&C, 0, sizeof C);
+    C.nsh = t->nsh; C.nat = m.N_atoms; C.vb = t->shell_index[0][m.atoms[0].N_shl - 1];
+    C.include_photons = m.include_photons;
+    double Psum = 0.0, Mt = 0.0, zs = 0.0;
+    for (int a = 0; a < m.N_atoms; ++a) {
+        const trekis_atom& at = m.atoms[a];
+        Psum += at.Pers; Mt += at.Mass * at.Pers; zs += at.Zat * at.Pers;
+        C.Zat[a] = at.Zat; C.Mass_kg[a] = (T)(at.Mass * kMp); C.Pers[a] = (T)at.Pers;
+        C.Z23[a] = (T)std::pow((double)at.Zat, 2.0 / 3.0);
+    }
+    for (int k = 0; k < t->nsh; ++k) {
+        const trekis_atom& at = m.atoms[t->atom_of[k]];
+        const int s = t->shell_of[k];
+        C.atom_of[k] = t->atom_of[k];
+        C.Ip[k] = (T)at.Ip[s]; C.Ipd[k] = at.Ip[s]; C.Nel[k] = (T)at.Nel[s];
+        C.Auger[k] = (T)at.Auger[s]; C.Radiat[k] = (T)at.Radiat[s];
+    }
+    C.Psum = (T)Psum; C.Mtarget = (T)(kMp * Mt / Psum); C.Egap = (T)m.atoms[0].Ip[m.atoms[0].N_shl - 1];
+    C.cut_off = (T)m.cut_off; C.hole_mass = (T)m.hole_mass; C.Layer = m.Layer;
+    C.ion_Z = t->ion.Zat; C.ion_kind_zeff = t->ion.Kind_Zeff; C.ion_mass_p = t->ion.Mass; C.MSHI = kMp * t->ion.Mass;
+    C.ion_E0 = t->ion.E; C.ion_fixed_zeff = t->ion.fixed_Zeff; C.Zt = zs / Psum;
+    C.Tim = (T)cfg.Tim; C.Nt = Nt; C.NR = cfg.N_R; C.seed = cfg.seed;
+    C.mobile_holes = m.hole_mass < 1e3;
+    C.mec2 = (T)(kMe * kC * kC / kE);
+    C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
+    finish_const(C);
+}
+
+template <class T>
+void launch_probe(const McConst<T>& C, const DevTabs<T>& tb, int kind, int k, int n, const double* E, const double* u,
+                  double* out, cudaStream_t s);
+
 // the hint sizes and end values from the first and last grid points (host)
 template <class T>
 inline void set_grid_hint_sizes(McConst<T>& C, T tg_first, T tg_last, T rg_first, T rg_last) {

@@ -204,38 +204,6 @@ __global__ void k_na_total(int Nt, int nhs, int phot, const double* Ee, const do
     totE[i] += s + Eat[i];
 }
 
-// Run constants of a table set (the same values the allocating path uploads).
-template <class T>
-void fill_const(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, McConst<T>& C) {
-    const trekis_material& m = t->mat;
-    std::memset(&C, 0, sizeof C);
-    C.nsh = t->nsh; C.nat = m.N_atoms; C.vb = t->shell_index[0][m.atoms[0].N_shl - 1];
-    C.include_photons = m.include_photons;
-    double Psum = 0.0, Mt = 0.0, zs = 0.0;
-    for (int a = 0; a < m.N_atoms; ++a) {
-        const trekis_atom& at = m.atoms[a];
-        Psum += at.Pers; Mt += at.Mass * at.Pers; zs += at.Zat * at.Pers;
-        C.Zat[a] = at.Zat; C.Mass_kg[a] = (T)(at.Mass * kMp); C.Pers[a] = (T)at.Pers;
-        C.Z23[a] = (T)std::pow((double)at.Zat, 2.0 / 3.0);
-    }
-    for (int k = 0; k < t->nsh; ++k) {
-        const trekis_atom& at = m.atoms[t->atom_of[k]];
-        const int s = t->shell_of[k];
-        C.atom_of[k] = t->atom_of[k];
-        C.Ip[k] = (T)at.Ip[s]; C.Ipd[k] = at.Ip[s]; C.Nel[k] = (T)at.Nel[s];
-        C.Auger[k] = (T)at.Auger[s]; C.Radiat[k] = (T)at.Radiat[s];
-    }
-    C.Psum = (T)Psum; C.Mtarget = (T)(kMp * Mt / Psum); C.Egap = (T)m.atoms[0].Ip[m.atoms[0].N_shl - 1];
-    C.cut_off = (T)m.cut_off; C.hole_mass = (T)m.hole_mass; C.Layer = m.Layer;
-    C.ion_Z = t->ion.Zat; C.ion_kind_zeff = t->ion.Kind_Zeff; C.ion_mass_p = t->ion.Mass; C.MSHI = kMp * t->ion.Mass;
-    C.ion_E0 = t->ion.E; C.ion_fixed_zeff = t->ion.fixed_Zeff; C.Zt = zs / Psum;
-    C.Tim = (T)cfg.Tim; C.Nt = Nt; C.NR = cfg.N_R; C.seed = cfg.seed;
-    C.mobile_holes = m.hole_mass < 1e3;
-    C.mec2 = (T)(kMe * kC * kC / kE);
-    C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
-    finish_const(C);
-}
-
 // Host values to the device through a fixed stack buffer (pageable copies are
 // staged before cudaMemcpyAsync returns, so the buffer can be refilled).
 template <class U, class G>

@@ -183,6 +183,8 @@ SIGNATURES = {
     "trekis_shi_range": (C.c_int32, [C.c_void_p, _DP, _DP, _DP, C.c_int64, C.POINTER(C.c_int64)]),
     "trekis_save_shi_tables": (C.c_int32, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32]),
     "trekis_save_mfp_tables": (C.c_int32, [C.c_void_p, C.POINTER(OutputCfg), C.c_char_p, C.c_int32, C.c_int32]),
+    "trekis_probe_samplers": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int64,
+                                          _DP, _DP, _DP]),
     "trekis_last_error": (C.c_char_p, []),
 }
 
