@@ -714,15 +714,6 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
     rc = build_tables_device(t, *cfg, st);
     if (!rc) rc = upload_mc<float>(t, t->d32);
     if (!rc) rc = upload_mc<double>(t, t->d64);
-    if (!rc) {   // both precisions draw ionising transfers from the FP64 rows
-        auto link = [&](auto& d) {
-            d.elE_d = t->d64.elE; d.elL_d = t->d64.elL; d.row_hw_d = t->d64.row_hw; d.row_L_d = t->d64.row_L;
-            d.hE_d = t->d64.hE; d.hL_d = t->d64.hL; d.hrow_hw_d = t->d64.hrow_hw; d.hrow_L_d = t->d64.hrow_L;
-            d.row_mono_d = t->d64.row_mono; d.hrow_mono_d = t->d64.hrow_mono;
-        };
-        link(t->d32);
-        link(t->d64);
-    }
     if (!rc && t->has_shi) rc = upload_shi<float>(t, t->dshi32);
     if (!rc && t->has_shi) rc = upload_shi<double>(t, t->dshi64);
     if (rc) { delete t; if (st) st->code = rc; return rc; }

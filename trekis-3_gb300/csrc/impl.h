@@ -78,10 +78,6 @@ struct DevTabs {
     // phonon-CDF elastic rows (electrons on elastE, holes on hElastE); null for Mott
     const int* erow_off; const T* erow_hw; const T* erow_L; const int* erow_mono;
     const int* herow_off; const T* herow_hw; const T* herow_L; const int* herow_mono;
-    // FP64 copies of the inelastic tables and rows (the FP32 track loop draws
-    // the transferred energy of ionising collisions, a few in 10^4, in FP64)
-    const double *elE_d, *elL_d, *row_hw_d, *row_L_d, *hE_d, *hL_d, *hrow_hw_d, *hrow_L_d;
-    const int *row_mono_d, *hrow_mono_d;
     // photons
     const T* pE; int nP;
     const T* pL;           // [nsh][nP]

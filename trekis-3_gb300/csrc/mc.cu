@@ -669,35 +669,6 @@ __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hol
     return E;
 }
 
-// The same draw evaluated in FP64 on the FP64 tables and rows, for the FP32
-// track loop: ionising collisions are a few in 10^4, so the FP64 arithmetic
-// costs nothing measurable, and the draw equals the FP64 one for the same
-// energy and uniform number (the FP32 rows alone put 2 % of the draws
-// 1e-5 to 3e-4 away where a row's cumulative MFP changes slowly).
-template <class T>
-__device__ double sample_transfer_d(const McConst<T>& C, const DevTabs<T>& tb, bool hole, int k, double Ele,
-                                    double RN, unsigned& err, float fg = -1.f) {
-    const double L_tot = hole ? nfp1(Tab<double>{tb.hE_d, tb.hL_d + (size_t)k * tb.nH, tb.nH}, Ele)
-                              : nfp1(Tab<double>{tb.elE_d, tb.elL_d + (size_t)k * tb.nE, tb.nE}, Ele);
-    const double L_need = L_tot / RN;
-    double Emin = C.Ipd[k];
-    if (Emin <= 1.0e-3) Emin = 1.0e-3;
-    double Emax;
-    if (hole) {
-        const double Mass = (C.hole_mass >= T(0)) ? (double)C.hole_mass : (double)tb.dosM[dos_find(tb, (T)Ele) - 1];
-        Emax = 4.0 * Ele * Mass / ((Mass + 1.0) * (Mass + 1.0));
-    } else Emax = (Ele + Emin) / 2.0;
-    double E = hole ? interp_transfer<double>(tb.hE_d, tb.nH, tb.hrow_off, tb.hrow_hw_d, tb.hrow_L_d, Ele, L_need, fg,
-                                              tb.hrow_mono_d)
-                    : interp_transfer<double>(tb.elE_d, tb.nE, tb.row_off + (size_t)k * tb.nE, tb.row_hw_d,
-                                              tb.row_L_d, Ele, L_need, fg, tb.row_mono_d + (size_t)k * tb.nE);
-    if (E < Emin) E = Emin;
-    if (E > Emax) E = Emax;
-    if (E < (double)C.Egap) err |= TREKIS_ERR_NEG_TRANSFER;
-    if (m_isnan(E)) E = Emin;
-    return E;
-}
-
 // Electron_energy_transfer_elastic with tabulated rows (CS:2285-2428,
 // CS_method 1): L_need = EMFP / RN (EMFP by Next_free_path_1d) inverted on the
 // phonon-CDF cumulative rows, at most the particle's energy
@@ -996,12 +967,8 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     T dE, theta, phi;
     if (FULL && ionise) {  // impact ionisation
         const int k = which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next());
-        if constexpr (sizeof(T) == 4) {
-            dE = (T)sample_transfer_d(C, tb, false, k, (double)Eel, s.next_d(), err, fg);
-        } else {
-            const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
-            dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err, fg);
-        }
+        const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
+        dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err, fg);
         theta = m_acos((Eel - dE) / m_sqrt(Eel * (Eel - dE)));
         if (m_isnan(theta)) theta = s.next() * pi_<T>();
         phi = T(2) * pi_<T>() * s.next();
@@ -1090,12 +1057,8 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         T dE, th1, ph1, Eh;
         if (FULL && ionise) {
             const int k = which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
-            if constexpr (sizeof(T) == 4) {
-                dE = (T)sample_transfer_d(C, tb, true, k, (double)Eel, s.next_d(), err, fg);
-            } else {
-                const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
-                dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err, fg);
-            }
+            const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
+            dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err, fg);
             // Update_holes_angles_el (MC:1142-1168)
             // masses in kg as the reference writes them (FP64); in electron
             // masses for FP32, where (Mh+me)^2 would underflow
@@ -1587,13 +1550,9 @@ __global__ void k_probe(const __grid_constant__ McConst<T> C, const __grid_const
     case 0: case 1: {   // Electron_energy_transfer_inelastic on shell k, or for a valence hole
         const bool hole = kind == 1;
         const int kk = hole ? C.vb : k;
-        if constexpr (sizeof(T) == 4) {
-            r = (T)sample_transfer_d(C, tb, hole, kk, (double)E, uin[i], err);
-        } else {
-            const T L = hole ? nfp1(Tab<T>{tb.hE, tb.hL + (size_t)kk * tb.nH, tb.nH}, E)
-                             : nfp1(Tab<T>{tb.elE, tb.elL + (size_t)kk * tb.nE, tb.nE}, E);
-            r = sample_transfer(C, tb, hole, kk, E, L, u, err);
-        }
+        const T L = hole ? nfp1(Tab<T>{tb.hE, tb.hL + (size_t)kk * tb.nH, tb.nH}, E)
+                         : nfp1(Tab<T>{tb.elE, tb.elL + (size_t)kk * tb.nE, tb.nE}, E);
+        r = sample_transfer(C, tb, hole, kk, E, L, u, err);
         break;
     }
     case 2: case 3: {   // total inelastic / elastic electron MFP as the track loop evaluates them
