@@ -186,8 +186,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    clk = Clocks(str(ROOT / "gpurun_out" / f"clocks_rank{rank}.csv") if (ROOT / "gpurun_out").exists()
-                 else f"/tmp/trekis_clocks_{rank}.csv")
+    clk = Clocks(args.clocks_csv.format(rank=rank))
     tot_ev = tot_ms = step_ms = step_ev = 0.0
     launches = 0
     sts = []
@@ -371,6 +370,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-neural", action="store_true", help="skip the learned-proposal arm")
+    ap.add_argument("--clocks-csv", default="/tmp/trekis_clocks_{rank}.csv",
+                    help="where the nvidia-smi clock samples of the timed region go ({rank}: the rank)")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000, help="training samples per network")
     ap.add_argument("--queue-cap", type=int, default=64_000_000,
                     help="particles per queue buffer (0: library default); 64 M holds about 2,400 cfg1 "
