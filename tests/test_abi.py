@@ -44,7 +44,8 @@ def test_struct_layout_matches_c(tmp_path):
     src = tmp_path / "sz.c"
     names = {"trekis_atom": abi.Atom, "trekis_material": abi.Material, "trekis_ion": abi.Ion,
              "trekis_table_cfg": abi.TableCfg, "trekis_run_cfg": abi.RunCfg, "trekis_tallies": abi.Tallies,
-             "trekis_status": abi.Status}
+             "trekis_status": abi.Status, "trekis_output_cfg": abi.OutputCfg, "trekis_batch_cfg": abi.BatchCfg,
+             "trekis_tune": abi.Tune, "trekis_mlp_cfg": abi.MlpCfg, "trekis_mlp_report": abi.MlpReport}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HDR}"', "int main(void){"]
     for cn in names:
         lines.append(f'printf("{cn} %zu\\n", sizeof({cn}));')
