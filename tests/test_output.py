@@ -105,3 +105,17 @@ def test_fortran_number_formats():
     assert oracle_output.fes(123.456) == "  1.2345600000000000E+002"
     assert oracle_output.fes(-1.0e-5) == " -1.0000000000000001E-005"
     assert oracle_output.fes(0.0) == "  0.0000000000000000E+000"
+
+
+def test_shell_names_follow_the_designator_table():
+    """api.shell_name against the designator list of define_PQN
+    (Dealing_with_EADL.f90:1016-1150), written out here in full."""
+    names = ("K L L1 L23 L2 L3 M M1 M23 M2 M3 M45 M4 M5 N N1 N23 N2 N3 N45 N4 N5 N67 N6 N7 "
+             "O O1 O23 O2 O3 O45 O4 O5 O67 O6 O7 O89 O8 O9 P P1 P23 P2 P3 P45 P4 P5 P67 P6 P7 "
+             "P89 P8 P9 P1011 P10 P11 Q Q1 Q23 Q2 Q3 Q...").split()
+    assert len(names) == 62
+    for d, n in enumerate(names, start=1):
+        assert api.shell_name(d) == n + "-shell", d
+    assert api.shell_name(0) == "K-shell"
+    assert api.shell_name(63) == api.shell_name(100) == "Valence"
+    assert len(api.ELEMENTS) == 92 and api.ELEMENTS[0] == "H" and api.ELEMENTS[91] == "U"
