@@ -158,7 +158,7 @@ typedef struct {
     int32_t  events_per_step;   /* events a thread runs before re-queueing       */
     int64_t  queue_capacity;    /* particles per queue buffer                    */
     int32_t  iterations_per_batch;
-    int32_t  use_graph;         /* capture the wavefront loop in a CUDA graph    */
+    int32_t  use_graph;         /* reserved: must be 0 (no graph capture yet)    */
     int32_t  sampler;           /* 0: table inversion of the energy-transfer draw;
                                    1: learned proposal + exact correction (needs
                                    trekis_mlp_train; the draws are identical)    */

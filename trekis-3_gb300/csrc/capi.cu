@@ -790,6 +790,7 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
     if (cfg->NMC < 0 || cfg->N_R < 1 || !cfg->Out_R || !(cfg->Tim > 0) || !(cfg->dt > 0)) return TREKIS_EINVAL;
     if (cfg->dt_flag != 0 && cfg->dt_flag != 1) return TREKIS_EINVAL;
     if (cfg->sampler != 0 && cfg->sampler != 1) { set_error("sampler must be 0 or 1"); return TREKIS_EINVAL; }
+    if (cfg->use_graph != 0) { set_error("graph capture of the wavefront loop is not built (use_graph must be 0)"); return TREKIS_EUNSUPPORTED; }
     for (int j = 1; j < cfg->N_R; ++j) if (!(cfg->Out_R[j] > cfg->Out_R[j - 1])) return TREKIS_EINVAL;
     *Nt = (int)tallied_times(cfg->Tim, cfg->dt, cfg->dt_flag).size();
     if (o->Nt != *Nt || o->N_R != cfg->N_R || o->Nat != t->mat.N_atoms) { set_error("tally dimensions do not match"); return TREKIS_EINVAL; }

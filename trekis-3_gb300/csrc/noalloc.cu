@@ -421,6 +421,7 @@ int check_args(const trekis_tables* t, const trekis_material* mat, const trekis_
         set_error("the no-alloc entry point runs the table sampler only (sampler = 0)");
         return TREKIS_EUNSUPPORTED;
     }
+    if (cfg->use_graph != 0) { set_error("graph capture of the wavefront loop is not built (use_graph must be 0)"); return TREKIS_EUNSUPPORTED; }
     if (o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h) {
         set_error("spectra are not tallied by the no-alloc entry point (their per-iteration histograms would not fit)");
         return TREKIS_EUNSUPPORTED;
