@@ -125,20 +125,6 @@ template <> struct Uni<float> {
     __device__ static float of(uint32_t w) { return ((float)(w >> 8) + 0.5f) * (1.0f / 16777216.0f); }
 };
 
-template <class T>
-struct Stream {
-    uint32_t k0, k1, c0, c1, c2, c3;
-    uint32_t buf[4];
-    int used;
-    __device__ Stream(uint64_t seed, uint64_t pid, uint32_t ordinal)
-        : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), c0((uint32_t)pid), c1((uint32_t)(pid >> 32)),
-          c2(ordinal), c3(0), used(4) {}
-    __device__ T next() {
-        if (used == 4) { philox4x32(c0, c1, c2, c3, k0, k1, buf); ++c3; used = 0; }
-        return Uni<T>::of(buf[used++]);
-    }
-};
-
 // ---- reference search semantics ------------------------------------------------
 // 1-based j with A[j-1] <= V < A[j]; 1 below the range, N at/above the top.
 template <class T>
