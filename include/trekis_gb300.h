@@ -154,10 +154,14 @@ typedef struct {
     uint64_t seed;              /* Philox key                                    */
     int64_t  iteration_offset;  /* global index of the first iteration (shards)  */
     /* scheduler knobs; 0 selects the tuned default */
-    int32_t  block_size;
-    int32_t  events_per_step;   /* events a thread runs before re-queueing       */
-    int64_t  queue_capacity;    /* particles per queue buffer                    */
-    int32_t  iterations_per_batch;
+    int32_t  block_size;        /* threads per hot-kernel block (0: 256; whole
+                                   warps, at most 256)                           */
+    int32_t  events_per_step;   /* events a thread runs before re-queueing (0: 64) */
+    int64_t  queue_capacity;    /* particles per queue buffer (0: 8 M in FP32,
+                                   4 M in FP64)                                  */
+    int32_t  iterations_per_batch;  /* iterations in flight at once (0: half the
+                                   queues' worth of the live-particle peak the
+                                   workspace measured last; 256 the first time) */
     int32_t  use_graph;         /* reserved: must be 0 (no graph capture yet)    */
     int32_t  sampler;           /* 0: table inversion of the energy-transfer draw;
                                    1: learned proposal + exact correction (needs
