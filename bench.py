@@ -125,6 +125,24 @@ def profile_traffic():
     return None
 
 
+def profile_issue():
+    """Issue-slot use of the hot kernels from the committed ncu summary (the
+    step kernels are issue-bound; the HBM roofline counts algorithmic bytes)."""
+    p = ROOT / "profiles" / "k_hot_cfg1_mid.md"
+    out = {}
+    try:
+        for line in open(p):
+            k, _, v = line.partition("=")
+            if v and k.strip() in ("issue_active_electrons", "issue_active_holes", "lanes_per_instruction"):
+                out[k.strip()] = float(v)
+    except Exception:
+        return None
+    if not out:
+        return None
+    out["source"] = "profiles/k_hot_cfg1_mid.md (ncu --set full, cfg1, 64 iterations per call)"
+    return out
+
+
 def alg_bytes_per_event(st, n_shells):
     """Algorithmic bytes per collision: 96 B particle state read+write, 64 B
     for two total-MFP lookups (2 nodes x (E,L) x 2 energies), and for events
@@ -261,7 +279,7 @@ def run_gpu(args):
             "peak": hbm if hbm else 6800.0, "peak_source": "measured" if hbm else "fallback",
             "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "traffic": traffic,
             "bytes_per_event": bpe, "step_kernel_ms": step_ms, "step_kernel_launches": launches_step,
-            "events_per_step_kernel_s": step_ev / (step_ms / 1e3)}
+            "events_per_step_kernel_s": step_ev / (step_ms / 1e3), "issue": profile_issue()}
     cpu = None
     if world == 1 and not args.no_cpu:
         cpu = cpu_baseline(args)
