@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TREKIS_ABI_VERSION 3
+#define TREKIS_ABI_VERSION 4
 
 #define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
 #define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
@@ -76,6 +76,9 @@ typedef struct {
     double  E0[TREKIS_MAX_SHELLS][TREKIS_MAX_OSC];    /* [eV] oscillator energy    */
     double  A[TREKIS_MAX_SHELLS][TREKIS_MAX_OSC];     /* oscillator amplitude      */
     double  Gamma[TREKIS_MAX_SHELLS][TREKIS_MAX_OSC]; /* [eV] oscillator width     */
+    double  form_factor[5];   /* fitted coefficients a1..a5 of the atomic form factor
+                                 (the row Zat of Atomic_form_factors.dat, PENELOPE's
+                                 analytical fit); read only with CDF_elast_Zeff 2 */
 } trekis_atom;
 
 /* Target: mirrors `type(Solid)`, `type(Density_of_states)`, the phonon
@@ -114,7 +117,9 @@ typedef struct {
     const double* dos_Eff_m;  /* [me]                                       */
     /* flags */
     int32_t kind_of_EMFP;     /* 0 = Mott atomic elastic, 1 = phonon CDF      */
-    int32_t CDF_elast_Zeff;   /* target effective charge in the phonon CS     */
+    int32_t CDF_elast_Zeff;   /* target charge in the phonon CS: 0 Barkas-like, 1 one,
+                                 2 nucleus screened by the valence CDF and core form
+                                 factors, 3 screened by the shells' CDFs */
     int32_t kind_of_DR;       /* 1 free electron, 2 plasmon pole, 3 Ritchie   */
     int32_t plasmon_Emax;     /* 1: plasmon energy as upper limit            */
     int32_t include_photons;  /* 1: radiative decay and photon transport     */

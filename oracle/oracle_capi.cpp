@@ -123,6 +123,10 @@ void oracle_sumrules(const double* A, const double* E0, const double* G, int n, 
     sumrules(A, E0, G, n, x_min, Omega, *ksum, *fsum);
 }
 double oracle_mott_sigma(int Z, double E) { return mott_sigma(Z, E); }
+double oracle_form_factor(double q, const double* a, double Z) { return form_factor(q, a, Z); }
+double oracle_phonon_screening(const trekis_material* m, double Ee, double hw, double hq, double Mass) {
+    return phonon_screening(*m, Ee, hw, hq, Mass);
+}
 double oracle_zeff(const trekis_ion* ion, double E, const trekis_material* m) { return zeff_shi(*ion, E, *m); }
 double oracle_sample_transfer(void* t, const trekis_material* m, int hole, int a, int s, double Ele, double L_tot,
                               double u) {

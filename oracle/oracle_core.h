@@ -80,6 +80,8 @@ std::vector<double> time_grid(double Tim, double dt, int dt_flag);
 
 // physics pieces exported for known-answer tests
 double loss_func(const trekis_material& m, double A, double E0, double G, double hw, double hq, bool photon);
+double form_factor(double q, const double* a, double Z);
+double phonon_screening(const trekis_material& m, double Ee, double hw, double hq, double Mass);
 void sumrules(const double* A, const double* E0, const double* G, int n, double x_min, double Omega,
               double& ksum, double& fsum);
 double mott_sigma(int Z, double Ee);  // [cm^2]

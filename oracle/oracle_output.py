@@ -349,7 +349,8 @@ def write_mfp_tables(d, mat, names, tabs, rows, stride):
     if mat["has_phot"]:
         mfp(os.path.join(d, f"OUTPUT_Photon_IMFPs_CDF_{ff(T, 7, 2).strip()}_K.dat"), tabs["phot"])
     if mat["kind_of_EMFP"] == 1:
-        zt = "Z=1_" if mat["CDF_elast_Zeff"] == 1 else "Zeff_"
+        # Analytical_IMFPs.f90:934-943
+        zt = {1: "Z=1_", 2: "Z_CDFe_FF_", 3: "Z_CDFe_"}.get(mat["CDF_elast_Zeff"], "Zeff_")
         ee_name = f"Electron_EMFPs_CDF_{zt}{ff(T, 7, 2).strip()}_K"
         he_name = f"Hole_CDF_EMFPs_{ff(T, 7, 2).strip()}_K"
     else:

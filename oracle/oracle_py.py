@@ -46,6 +46,10 @@ def load():
     lib.oracle_sumrules.argtypes = [dp, dp, dp, C.c_int, C.c_double, C.c_double, dp, dp]
     lib.oracle_mott_sigma.restype = C.c_double
     lib.oracle_mott_sigma.argtypes = [C.c_int, C.c_double]
+    lib.oracle_form_factor.restype = C.c_double
+    lib.oracle_form_factor.argtypes = [C.c_double, dp, C.c_double]
+    lib.oracle_phonon_screening.restype = C.c_double
+    lib.oracle_phonon_screening.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
     lib.oracle_zeff.restype = C.c_double
     lib.oracle_zeff.argtypes = [vp, C.c_double, vp]
     lib.oracle_sample_transfer.restype = C.c_double

@@ -414,10 +414,102 @@ static double imewq_phonon(const trekis_material& m, double hw, double hq, doubl
     return sum;
 }
 
-// Diff_cross_section_phonon (CS:3142-3300) with the unscreened potential 1/q
-// (CDF_elast_Zeff 0 or 1; the target charge enters through Zeff^2 in Tot_EMFP).
-// The q loop is bounded: qmin = 0 (hw below the resolution of sqrt(Ele)) would
-// never end in the reference; it contributes nothing here.
+// ---- dynamic screening of the nucleus (CDF_elast_Zeff 2 and 3) --------------------------
+// Reewq / One_Reewq (CS:253-343): Re(-1/eps) of one shell's oscillators with
+// the same finite-q extension as Loss_func
+static double reewq(const trekis_material& m, int a, int s, double hw, double hq) {
+    const trekis_atom& at = m.atoms[a];
+    double ReE = 0.0;
+    for (int i = 0; i < at.N_osc[s]; ++i) {
+        double E0, G1;
+        extend_E0(m, at.E0[s][i], at.Gamma[s][i], h * h * hq * hq, hq, E0, G1);
+        const double dE2 = hw * hw, E02 = E0 * E0;
+        ReE += at.A[s][i] * (E02 - dE2) / ((dE2 - E02) * (dE2 - E02) + (G1 * G1) * dE2);
+    }
+    return -(1.0 - ReE);
+}
+
+// construct_CDF (CS:184-248) reduced to what the screening uses, 1/|eps|:
+// eps = (-Re/den, Im/den) with den = Re^2 + Im^2 of -1/eps; a core shell whose
+// hw + (hbar q)^2/2me does not exceed its Ip, or a vanishing den, gives eps = 1
+static double inv_abs_eps(const trekis_material& m, int a, int s, double hw, double hq) {
+    const bool vb = (a == 0 && s == m.atoms[0].N_shl - 1);
+    if (!vb) {
+        const double Q = (h * hq) * (h * hq) / (2.0 * me);
+        if (hw + Q <= m.atoms[a].Ip[s]) return 1.0;
+    }
+    const double ImE = imewq(m, a, s, hw, hq, false);
+    const double ReE = reewq(m, a, s, hw, hq);
+    const double den = ReE * ReE + ImE * ImE;
+    if (!(std::fabs(den) > 1.0e-12)) return 1.0;
+    return 1.0 / std::hypot(-ReE / den, ImE / den);
+}
+
+// form_factor (CS:61-82): PENELOPE's analytical atomic form factor at momentum
+// q [kg m/s] (Salvat et al. 2001, Eqs. 2.5-2.9), with the hydrogen-like
+// K-shell bound for Z > 10 where the fit falls below 2
+double form_factor(double q, const double* a, double Z) {
+    const double mc = me * cvel;
+    const double x = q / mc * 20.6074224164, x2 = x * x, x4 = x2 * x2;
+    const double demf = 1.0 + a[3] * x2 + a[4] * x4;
+    const double fxz = Z * (1.0 + a[0] * x2 + a[1] * x * x2 + a[2] * x4) / (demf * demf);
+    double FF = fxz;
+    if (Z > 10.0 && fxz < 2.0) {
+        const double al = g_alpha() * (Z - 5.0 / 16.0), b = std::sqrt(1.0 - al * al), Q = q / (2.0 * mc * al);
+        const double Fk = std::sin(2.0 * b * std::atan(Q)) / (b * Q * std::pow(1.0 + Q * Q, b));
+        if (FF < Fk) FF = Fk;
+    }
+    return FF;
+}
+
+// the squared screened charge per atom, (Z/eps)^2, that multiplies 1/q in
+// Diff_cross_section_phonon (CS:3216-3278):
+//  2: get_screening_ff (CS:3303-3368) -- the valence band screened by its CDF
+//     at (hw, (p + q)/2), core electrons by the form factors at the mean of the
+//     incident and transferred momenta;
+//  3: get_screening_all (CS:3373-3406) -- every shell of atom i screened by the
+//     CDF construct_CDF returns for atom 1, shell size(Ip of atom i), at (hw, q)
+//     (the shell index the reference passes, CS:3267); the builder refuses
+//     compounds where that index would leave atom 1's shells.
+double phonon_screening(const trekis_material& m, double Ee, double hw, double hq, double Mass) {
+    double Zmol = 0.0, pers = 0.0, sc = 0.0;
+    for (int i = 0; i < m.N_atoms; ++i) Zmol += m.atoms[i].Zat * m.atoms[i].Pers;
+    const int n0 = m.atoms[0].N_shl;
+    if (m.CDF_elast_Zeff == 2) {
+        double p_e = std::sqrt(2.0 * Mass * me * Ee * e);
+        p_e = 0.5 * (p_e + hq * h * std::sqrt(e));
+        double pp = std::sqrt(2.0 * Mass * me * Ee) / h;
+        pp = 0.5 * (pp + hq);
+        const double inv_vb = inv_abs_eps(m, 0, n0 - 1, hw, pp);
+        for (int i = 0; i < m.N_atoms; ++i) {
+            const trekis_atom& at = m.atoms[i];
+            double Z = 0.0;
+            for (int j = 0; j < (i == 0 ? at.N_shl - 1 : at.N_shl); ++j) Z += at.Nel[j];
+            double FF = form_factor(p_e, at.form_factor, (double)at.Zat);
+            FF = std::min(FF, Z);
+            sc = sc - FF * at.Pers;
+            if (i == 0) sc = sc + at.Nel[n0 - 1] * (inv_vb - 1.0);
+        }
+    } else {
+        for (int i = 0; i < m.N_atoms; ++i) {
+            const trekis_atom& at = m.atoms[i];
+            const double inv = inv_abs_eps(m, 0, at.N_shl - 1, hw, hq);
+            for (int j = 0; j < at.N_shl; ++j) {
+                const double N_el = (i == 0 && j == n0 - 1) ? at.Nel[j] : at.Nel[j] * at.Pers;
+                sc = sc + N_el * (inv - 1.0);
+            }
+        }
+    }
+    for (int i = 0; i < m.N_atoms; ++i) pers += m.atoms[i].Pers;
+    const double s = (Zmol + sc) / pers;
+    return s * s;
+}
+
+// Diff_cross_section_phonon (CS:3142-3300): the potential is 1/q (CDF_elast_Zeff
+// 0 or 1; the target charge enters through Zeff^2 in Tot_EMFP) or the screened
+// charge (Z/eps)^2 / q (2, 3).  The q loop is bounded: qmin = 0 (hw below the
+// resolution of sqrt(Ele)) would never end in the reference; it contributes
+// nothing here.
 static double diff_cs_phonon(const trekis_material& m, double Ele, double hw, double Mass, double Mtarget) {
     const double eps = 1.0e-12, pre = std::sqrt(2.0 * Mass * me) / h;
     double qmin;
@@ -431,7 +523,8 @@ static double diff_cs_phonon(const trekis_material& m, double Ele, double hw, do
         const double dq = hq / 100.0;
         const double t1 = imewq_phonon(m, hw, hq + dq / 2.0, Mtarget);
         const double dL = imewq_phonon(m, hw, hq + dq, Mtarget);
-        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) * (1.0 / hq);
+        const double scr = (m.CDF_elast_Zeff >= 2) ? phonon_screening(m, Ele, hw, hq, Mass) : 1.0;
+        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) * (scr / hq);
         dLs0 = dL;
         hq = hq + dq;
     }
@@ -565,7 +658,10 @@ int build_tables(const trekis_material& m, const trekis_ion& ion, const trekis_t
         }
     };
     if (m.kind_of_EMFP == 1) {   // phonon-CDF elastic (Elastic_cross_section CS:2902-2935, Tot_EMFP)
-        if (m.N_ph_osc < 1 || m.CDF_elast_Zeff < 0 || m.CDF_elast_Zeff > 1) return TREKIS_EUNSUPPORTED;
+        if (m.N_ph_osc < 1 || m.CDF_elast_Zeff < 0 || m.CDF_elast_Zeff > 3) return TREKIS_EUNSUPPORTED;
+        if (m.CDF_elast_Zeff == 3)
+            for (int a = 0; a < m.N_atoms; ++a)
+                if (m.atoms[a].N_shl > m.atoms[0].N_shl) return TREKIS_EUNSUPPORTED;
         double Mt = 0.0;
         for (int a = 0; a < m.N_atoms; ++a) Mt += m.atoms[a].Mass * m.atoms[a].Pers;
         const double Mtarget = Mp * Mt / Psum;

@@ -219,3 +219,147 @@ def test_spectra_normalisation():
     s_h = (hh * wD[None, :]).sum(1)
     assert s_h[-1] == pytest.approx(3.0)
     assert tal.view("Out_theta_h").sum() > 0
+
+
+# ---- dynamically screened phonon elastic scattering (CDF_elast_Zeff 2, 3) -------------
+# A second, plain-Python restatement of the reference's formulas pins the
+# oracle's screening functions.
+
+_C = 299792458.0
+
+
+def _ff_py(q, a, Z):
+    """form_factor (Cross_sections.f90:61-82)."""
+    mc = material.G_ME * _C
+    x = q / mc * 20.6074224164
+    fxz = Z * (1.0 + a[0] * x ** 2 + a[1] * x ** 3 + a[2] * x ** 4) / (1.0 + a[3] * x ** 2 + a[4] * x ** 4) ** 2
+    FF = fxz
+    if Z > 10.0 and fxz < 2.0:
+        alpha = material.G_E ** 2 / (material.G_H * _C * 4.0 * np.pi * material.G_E0)
+        al = alpha * (Z - 5.0 / 16.0)
+        b = np.sqrt(1.0 - al * al)
+        Q = q / (2.0 * mc * al)
+        FF = max(FF, np.sin(2.0 * b * np.arctan(Q)) / (b * Q * (1.0 + Q * Q) ** b))
+    return FF
+
+
+def _inv_eps_py(mat, a, s, hw, hq):
+    """1/|eps| from construct_CDF (CS:184-248) with Imewq and Reewq (CS:253-343),
+    free-electron dispersion and a constant electron mass."""
+    assert mat.kind_of_DR == 1 and mat.El_eff_mass > 0
+    sh = mat.atoms[a].shells[s]
+    vb = a == 0 and s == len(mat.atoms[0].shells) - 1
+    if not vb and hw + (material.G_H * hq) ** 2 / (2.0 * material.G_ME) <= sh.Ip:
+        return 1.0
+    sqq = (material.G_H * hq) ** 2 / (2.0 * mat.El_eff_mass * material.G_ME)
+    im = re = 0.0
+    for A, E, G in zip(sh.A, sh.E0, sh.Gamma):
+        E0 = E + sqq
+        d = (hw * hw - E0 * E0) ** 2 + G * G * hw * hw
+        im += A * G * hw / d
+        re += A * (E0 * E0 - hw * hw) / d
+    ReE = -(1.0 - re)
+    den = ReE ** 2 + im ** 2
+    if den <= 1e-12:
+        return 1.0
+    return 1.0 / abs(complex(-ReE / den, im / den))
+
+
+def _screening_py(mat, zeff, Ee, hw, hq, Mass):
+    """(Z/eps)^2 of Diff_cross_section_phonon (CS:3216-3278) with
+    get_screening_ff (CS:3303-3368) or get_screening_all (CS:3373-3406)."""
+    atoms = mat.atoms
+    n0 = len(atoms[0].shells)
+    Zmol = sum(a.Z * a.Pers for a in atoms)
+    pers = sum(a.Pers for a in atoms)
+    sc = 0.0
+    if zeff == 2:
+        p_e = 0.5 * (np.sqrt(2.0 * Mass * material.G_ME * Ee * material.G_E) + hq * material.G_H * np.sqrt(material.G_E))
+        pp = 0.5 * (np.sqrt(2.0 * Mass * material.G_ME * Ee) / material.G_H + hq)
+        inv_vb = _inv_eps_py(mat, 0, n0 - 1, hw, pp)
+        for i, at in enumerate(atoms):
+            core = at.shells[:-1] if i == 0 else at.shells
+            sc -= min(_ff_py(p_e, at.form_factor, float(at.Z)), sum(s.Nel for s in core)) * at.Pers
+            if i == 0:
+                sc += at.shells[-1].Nel * (inv_vb - 1.0)
+    else:
+        for i, at in enumerate(atoms):
+            inv = _inv_eps_py(mat, 0, len(at.shells) - 1, hw, hq)   # atom 1, shell size(Ip of atom i) (CS:3267)
+            for j, s in enumerate(at.shells):
+                n_el = s.Nel if (i == 0 and j == n0 - 1) else s.Nel * at.Pers
+                sc += n_el * (inv - 1.0)
+    return ((Zmol + sc) / pers) ** 2
+
+
+def test_form_factor_restated(oracle_lib):
+    """PENELOPE's form factor: Z at q = 0, the restated fit elsewhere, and the
+    hydrogen-like bound taking over for Z > 10 at large q."""
+    q = np.logspace(-27, -21, 61)
+    for Z in (8, 13, 14):
+        a = material.form_factor_coefficients(Z)
+        arr = (C.c_double * 5)(*a)
+        assert oracle_lib.oracle_form_factor(0.0, arr, float(Z)) == Z
+        for qi in q:
+            got = oracle_lib.oracle_form_factor(float(qi), arr, float(Z))
+            ref = _ff_py(float(qi), a, float(Z))
+            assert abs(got - ref) <= 1e-12 * abs(ref), (Z, qi, got, ref)
+    a = material.form_factor_coefficients(14)
+    big = 1e-21
+    x = big / (material.G_ME * _C) * 20.6074224164
+    fit = 14.0 * (1 + a[0] * x ** 2 + a[1] * x ** 3 + a[2] * x ** 4) / (1 + a[3] * x ** 2 + a[4] * x ** 4) ** 2
+    assert oracle_lib.oracle_form_factor(big, (C.c_double * 5)(*a), 14.0) > fit
+
+
+@pytest.mark.parametrize("base,zeff", [("cfg0", 2), ("cfg0", 3), ("cfg4", 2), ("cfg4", 3)])
+def test_phonon_screening_restated(oracle_lib, base, zeff):
+    """The oracle's (Z/eps)^2 equals the plain restatement over energies,
+    transfers and momenta that cross the core-shell thresholds."""
+    w = getattr(configs, base)()
+    mat = w.material
+    mat.kind_of_EMFP, mat.CDF_elast_Zeff = 1, zeff
+    h = mat.to_c()
+    n = 0
+    for Ee in (0.5, 7.0, 80.0, 2500.0):
+        for hw in (1e-3, 0.05, 0.3):
+            for hq in np.logspace(16, 20.5, 19):
+                for Mass in (1.0, 0.7):
+                    got = oracle_lib.oracle_phonon_screening(C.addressof(h.struct), Ee, hw, float(hq), Mass)
+                    ref = _screening_py(mat, zeff, Ee, hw, float(hq), Mass)
+                    assert np.isfinite(got) and got >= 0.0
+                    assert abs(got - ref) <= 1e-11 * abs(ref) + 1e-300, (Ee, hw, hq, Mass, got, ref)
+                    n += 1
+    assert n == 4 * 3 * 19 * 2
+
+
+def test_screened_phonon_tables():
+    """Screened phonon-CDF elastic tables: positive, finite MFPs, cumulative rows
+    decreasing in hw, different from the unscreened charge; option 3 is refused
+    when an atom has more shells than the first (the reference would index past
+    the first atom's shells)."""
+    import functools
+    import oracle_py
+    base = None
+    for zeff in (1, 2, 3):
+        if zeff == 1:
+            w = configs.small(configs.cfg4)
+            w.material.CDF_elast_Zeff = 1
+        else:
+            w = configs.small(functools.partial(configs.cfg4_screened, zeff))
+        h = w.material.to_c()
+        o = oracle_py.OracleTables(h, api.ion_struct(w), abi.TableCfg(build_shi=0, build_photon=0), nthreads=4)
+        E, L, _ = o.export(abi.TAB_EL_ELAST)
+        assert np.all(np.isfinite(L)) and np.all(L > 0)
+        for iE in (len(E) // 3, len(E) - 1):
+            hw, Lr = o.row(abi.ROW_EL_ELAST, 0, 0, iE)
+            assert len(hw) > 3 and np.all(np.diff(hw) > 0) and np.all(np.diff(Lr) <= 0)
+        if base is None:
+            base = L
+        else:
+            assert np.max(np.abs(L / base - 1.0)) > 0.1
+        o.close()
+    w = configs.small(functools.partial(configs.cfg4_screened, 3))
+    ox = w.material.atoms[1]
+    ox.shells = ox.shells + [material.Shell(Ip=5.0 + k, Nel=0.0, designator=40 + k, E0=[20.0], A=[1.0], Gamma=[5.0])
+                             for k in range(len(w.material.atoms[0].shells) - len(ox.shells) + 1)]
+    with pytest.raises(RuntimeError, match="-7"):
+        oracle_py.OracleTables(w.material.to_c(), api.ion_struct(w), abi.TableCfg(build_shi=0, build_photon=0))

@@ -31,6 +31,17 @@ struct BuildMat {
     int n_ph;
     double Mtarget;
     double phE0[TREKIS_MAX_PH_OSC], phA[TREKIS_MAX_PH_OSC], phG[TREKIS_MAX_PH_OSC];
+    // dynamic screening of the nucleus in the phonon potential (CDF_elast_Zeff 2, 3)
+    int elast_zeff;
+    int scr_nat;                          // kinds of atoms
+    int scr_vb;                           // compact index of the valence band
+    int scr_k[TREKIS_MAX_ATOMS];          // 3: compact index of (atom 0, shell N_shl(i) - 1)
+    int scr_nsh[TREKIS_MAX_ATOMS];        // shells of atom i
+    double scr_Zmol, scr_pers, scr_Nvb;   // sum Zat*Pers, sum Pers, valence electrons
+    double scr_Zat[TREKIS_MAX_ATOMS], scr_Pers[TREKIS_MAX_ATOMS];
+    double scr_Zcore[TREKIS_MAX_ATOMS];   // 2: electrons outside the valence band
+    double scr_ff[TREKIS_MAX_ATOMS][5];   // 2: form-factor coefficients
+    double scr_w[TREKIS_MAX_ATOMS][TREKIS_MAX_SHELLS];   // 3: Nel (valence) or Nel*Pers (core)
 };
 
 // A mean-free-path table prepared for the hot loop: logarithms of both

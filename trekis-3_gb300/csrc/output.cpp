@@ -543,7 +543,10 @@ extern "C" int32_t trekis_save_mfp_tables(const trekis_tables* t, const trekis_o
     // elastic: Mott, or the phonon CDF with the target-charge tag
     std::string ee_name, he_name;
     if (m.kind_of_EMFP == 1) {
-        ee_name = std::string("Electron_EMFPs_CDF_") + (m.CDF_elast_Zeff == 1 ? "Z=1_" : "Zeff_") + temp_tag(m.temp, 7) + "_K";
+        // the target-charge tag of Analytical_electron_dEdx (Analytical_IMFPs.f90:934-943)
+        const char* zt = m.CDF_elast_Zeff == 1 ? "Z=1_" : m.CDF_elast_Zeff == 2 ? "Z_CDFe_FF_"
+                       : m.CDF_elast_Zeff == 3 ? "Z_CDFe_" : "Zeff_";
+        ee_name = std::string("Electron_EMFPs_CDF_") + zt + temp_tag(m.temp, 7) + "_K";
         he_name = "Hole_CDF_EMFPs_" + temp_tag(m.temp, 7) + "_K";
     } else {
         ee_name = "Electron_EMFPs_Mott";

@@ -94,9 +94,97 @@ __device__ double d_imewq_phonon(const BuildMat* __restrict__ bm, double hw, dou
     return sum;
 }
 
-// Diff_cross_section_phonon (Cross_sections.f90:3142-3300) with the
-// unscreened potential 1/q (CDF_elast_Zeff 0 or 1).  The q loop is bounded;
-// qmin = 0 (hw below the resolution of sqrt(Ele)) contributes nothing.
+// 1/|eps| of one shell at (hw, q), as construct_CDF (Cross_sections.f90:184-248)
+// builds eps = (-Re, Im) / (Re^2 + Im^2) from Imewq's Im(-1/eps) and Reewq's
+// Re(-1/eps) (CS:253-343, same finite-q dispersion as Loss_func).  A core
+// shell whose hw + (hbar q)^2 / 2me does not exceed its Ip, or a vanishing
+// denominator, gives eps = 1.
+__device__ double d_inv_abs_eps(const BuildMat* __restrict__ bm, int sh, double hw, double hq) {
+    if (sh != bm->scr_vb) {
+        const double Q = (kH * hq) * (kH * hq) / (2.0 * kMe);
+        if (hw + Q <= bm->Ip[sh]) return 1.0;
+    }
+    double Mass;
+    if (bm->dos_mass) {
+        double qlim = fabs(hq) * sqrt(kE);
+        if (qlim <= bm->dos_k[bm->N_dos - 1]) Mass = bm->dos_Eff_m[find_monoton(bm->dos_k, bm->N_dos, qlim) - 1];
+        else Mass = 1.0;
+    } else Mass = bm->El_eff_mass > 0 ? bm->El_eff_mass : 1.0;
+    const double hq2 = kH * kH * hq * hq;
+    const double sqq = hq2 / (2.0 * Mass * kMe);
+    const double dE2 = hw * hw;
+    double im = 0.0, re = 0.0;
+    const int no = bm->nosc[sh];
+    for (int i = 0; i < no; ++i) {
+        double E = bm->E0[sh * MAXOSC + i], G = bm->G[sh * MAXOSC + i], A = bm->A[sh * MAXOSC + i];
+        double E0, G1;
+        if (bm->kind_of_DR == 2) { E0 = sqrt(E * E + bm->v_f * bm->v_f * hq2 * 0.3333333333333 + sqq * sqq); G1 = G; }
+        else if (bm->kind_of_DR == 3) { E0 = pow(pow(E, 0.666666666666) + pow(sqq, 0.666666666666), 1.5); G1 = sqrt(G * G + sqq * sqq); }
+        else { E0 = E + sqq; G1 = G; }
+        const double E02 = E0 * E0;
+        im += A * G1 * hw / ((dE2 - E02) * (dE2 - E02) + G1 * G1 * dE2);
+        re += A * (E02 - dE2) / ((dE2 - E02) * (dE2 - E02) + (G1 * G1) * dE2);
+    }
+    const double ReE = -(1.0 - re);
+    const double den = ReE * ReE + im * im;
+    if (!(fabs(den) > 1.0e-12)) return 1.0;
+    return 1.0 / hypot(-ReE / den, im / den);
+}
+
+// form_factor (Cross_sections.f90:61-82): PENELOPE's analytical atomic form
+// factor at momentum q [kg m/s] (Salvat et al. 2001, Eqs. 2.5-2.9), bounded
+// below by the hydrogen-like K shell for Z > 10 where the fit drops under 2
+__device__ double d_form_factor(double q, const double* __restrict__ a, double Z) {
+    const double mc = kMe * kC;
+    const double x = q / mc * 20.6074224164, x2 = x * x, x4 = x2 * x2;
+    const double demf = 1.0 + a[3] * x2 + a[4] * x4;
+    const double fxz = Z * (1.0 + a[0] * x2 + a[1] * x * x2 + a[2] * x4) / (demf * demf);
+    double FF = fxz;
+    if (Z > 10.0 && fxz < 2.0) {
+        const double alpha = kE * kE / (kH * kC * 4.0 * kPi * kE0);
+        const double al = alpha * (Z - 5.0 / 16.0), b = sqrt(1.0 - al * al), Q = q / (2.0 * mc * al);
+        const double Fk = sin(2.0 * b * atan(Q)) / (b * Q * pow(1.0 + Q * Q, b));
+        if (FF < Fk) FF = Fk;
+    }
+    return FF;
+}
+
+// The squared screened charge per atom (Z/eps)^2 that replaces 1 in the
+// phonon potential 1/q (Diff_cross_section_phonon, CS:3216-3278).
+//  2: get_screening_ff (CS:3303-3368): the valence band screened by its CDF at
+//     (hw, (p/hbar + q)/2), core electrons by their form factors at the mean
+//     of the incident and transferred momenta;
+//  3: get_screening_all (CS:3373-3406): the shells of atom i screened by the
+//     CDF of atom 0's shell N_shl(i) - 1 at (hw, q), the shell the reference
+//     passes to construct_CDF (CS:3267).
+__device__ double d_screening(const BuildMat* __restrict__ bm, double Ee, double hw, double hq, double Mass) {
+    double sc = 0.0;
+    if (bm->elast_zeff == 2) {
+        double p_e = sqrt(2.0 * Mass * kMe * Ee * kE);
+        p_e = 0.5 * (p_e + hq * kH * sqrt(kE));
+        double pp = sqrt(2.0 * Mass * kMe * Ee) / kH;
+        pp = 0.5 * (pp + hq);
+        const double inv_vb = d_inv_abs_eps(bm, bm->scr_vb, hw, pp);
+        for (int i = 0; i < bm->scr_nat; ++i) {
+            double FF = d_form_factor(p_e, bm->scr_ff[i], bm->scr_Zat[i]);
+            FF = (bm->scr_Zcore[i] < FF) ? bm->scr_Zcore[i] : FF;
+            sc = sc - FF * bm->scr_Pers[i];
+            if (i == 0) sc = sc + bm->scr_Nvb * (inv_vb - 1.0);
+        }
+    } else {
+        for (int i = 0; i < bm->scr_nat; ++i) {
+            const double inv = d_inv_abs_eps(bm, bm->scr_k[i], hw, hq);
+            for (int j = 0; j < bm->scr_nsh[i]; ++j) sc = sc + bm->scr_w[i][j] * (inv - 1.0);
+        }
+    }
+    const double s = (bm->scr_Zmol + sc) / bm->scr_pers;
+    return s * s;
+}
+
+// Diff_cross_section_phonon (Cross_sections.f90:3142-3300): the potential is
+// 1/q (CDF_elast_Zeff 0 or 1; the target charge enters as Zeff^2 in Tot_EMFP)
+// or (Z/eps)^2 / q (2, 3).  The q loop is bounded; qmin = 0 (hw below the
+// resolution of sqrt(Ele)) contributes nothing.
 __device__ double d_phonon_diff(const BuildMat* __restrict__ bm, double Ele, double hw, double Mass) {
     const double eps = 1.0e-12, pre = sqrt(2.0 * Mass * kMe) / kH;
     if (fabs(hw) < eps) return 1.31e30;
@@ -108,7 +196,8 @@ __device__ double d_phonon_diff(const BuildMat* __restrict__ bm, double Ele, dou
         const double dq = hq / 100.0;
         const double t1 = d_imewq_phonon(bm, hw, hq + dq / 2.0);
         const double dL = d_imewq_phonon(bm, hw, hq + dq);
-        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) * (1.0 / hq);
+        const double scr = (bm->elast_zeff >= 2) ? d_screening(bm, Ele, hw, hq, Mass) : 1.0;
+        dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) * (scr / hq);
         dLs0 = dL;
         hq = hq + dq;
     }
@@ -162,14 +251,25 @@ __global__ void k_points(const Job* __restrict__ jobs, int nj, double* __restric
     }
 }
 
+// electron/hole and SHI points [0, np)
 __global__ void k_diff(const BuildMat* __restrict__ bm, const Job* __restrict__ jobs, const double* __restrict__ pts,
                        const int* __restrict__ pjob, double* __restrict__ val, int64_t np) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     const Job& J = jobs[pjob[p]];
     val[p] = (J.kind == 0) ? d_diff_cs(bm, J.sh, J.Ele, pts[p], J.Mass)
-           : (J.kind == 1) ? d_shi_diff(bm, J.sh, J.Ele, J.Mass, J.Emax, pts[p])
-                           : d_phonon_diff(bm, J.Ele, pts[p], J.Mass);
+                           : d_shi_diff(bm, J.sh, J.Ele, J.Mass, J.Emax, pts[p]);
+}
+
+// phonon-CDF elastic points [p0, np), the last jobs of the build; a kernel of
+// their own keeps the screening's registers out of k_diff
+__global__ void k_diff_phonon(const BuildMat* __restrict__ bm, const Job* __restrict__ jobs,
+                              const double* __restrict__ pts, const int* __restrict__ pjob,
+                              double* __restrict__ val, int64_t p0, int64_t np) {
+    int64_t p = p0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const Job& J = jobs[pjob[p]];
+    val[p] = d_phonon_diff(bm, J.Ele, pts[p], J.Mass);
 }
 
 // Simpson accumulation in the reference's order; writes (Sigma, dEdx) and rows
@@ -408,6 +508,27 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     }
     const bool metal = m.atoms[0].Ip[m.atoms[0].N_shl - 1] < 0.2;
     bm.dos_mass = (m.El_eff_mass == 0.0 && m.N_dos > 0 && !metal) ? 1 : 0;
+    // screening of the phonon potential: sums in the reference's order
+    bm.elast_zeff = (m.kind_of_EMFP == 1) ? m.CDF_elast_Zeff : 0;
+    bm.scr_nat = m.N_atoms;
+    bm.scr_vb = T->shell_index[0][m.atoms[0].N_shl - 1];
+    bm.scr_Nvb = m.atoms[0].Nel[m.atoms[0].N_shl - 1];
+    bm.scr_Zmol = 0.0; bm.scr_pers = 0.0;
+    for (int a = 0; a < m.N_atoms; ++a) bm.scr_Zmol += m.atoms[a].Zat * m.atoms[a].Pers;
+    for (int a = 0; a < m.N_atoms; ++a) {
+        const trekis_atom& at = m.atoms[a];
+        bm.scr_pers += at.Pers;
+        bm.scr_Zat[a] = (double)at.Zat;
+        bm.scr_Pers[a] = at.Pers;
+        bm.scr_nsh[a] = at.N_shl;
+        bm.scr_k[a] = (at.N_shl <= m.atoms[0].N_shl) ? T->shell_index[0][at.N_shl - 1] : bm.scr_vb;
+        double Z = 0.0;
+        for (int j = 0; j < (a == 0 ? at.N_shl - 1 : at.N_shl); ++j) Z += at.Nel[j];
+        bm.scr_Zcore[a] = Z;
+        for (int c = 0; c < 5; ++c) bm.scr_ff[a][c] = at.form_factor[c];
+        for (int j = 0; j < at.N_shl; ++j)
+            bm.scr_w[a][j] = (a == 0 && j == m.atoms[0].N_shl - 1) ? at.Nel[j] : at.Nel[j] * at.Pers;
+    }
     bm.N_dos = m.N_dos;
     for (int k = 0; k < nsh; ++k) {
         const trekis_atom& at = m.atoms[T->atom_of[k]];
@@ -476,10 +597,17 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     const size_t j_el0 = jobs.size();
     std::vector<double> gEl, gHel;
     if (m.kind_of_EMFP == 1) {
-        if (m.N_ph_osc < 1 || m.CDF_elast_Zeff < 0 || m.CDF_elast_Zeff > 1) {
-            set_error("phonon-CDF elastic needs phonon oscillators and CDF_elast_Zeff 0 or 1");
+        if (m.N_ph_osc < 1 || m.CDF_elast_Zeff < 0 || m.CDF_elast_Zeff > 3) {
+            set_error("phonon-CDF elastic needs phonon oscillators and CDF_elast_Zeff 0 to 3");
             return TREKIS_EUNSUPPORTED;
         }
+        if (m.CDF_elast_Zeff == 3)
+            for (int a = 0; a < m.N_atoms; ++a)
+                if (m.atoms[a].N_shl > m.atoms[0].N_shl) {
+                    set_error("CDF_elast_Zeff 3 screens atom i with shell N_shl(i) of the first atom: "
+                              "no atom may have more shells than the first");
+                    return TREKIS_EUNSUPPORTED;
+                }
         gEl = grid_4CS(m, 0.01, Emax_e);
         gHel = grid_4CS(m, 0.01, dosmax + 1.0);
         for (double E : gEl) { Job J{}; limits_phonon(T, E, false, J); jobs.push_back(J); }
@@ -518,8 +646,15 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     if (!d_pts || !d_pj || !d_val || !d_sig || !d_ded || !d_rhw || !d_rL || !d_rX) return TREKIS_ENOMEM;
     k_points<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj, d_pts, d_pj);
     CK(cudaGetLastError());
-    k_diff<<<(unsigned)((np + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np);
-    CK(cudaGetLastError());
+    const int64_t np_el = (j_el0 < jobs.size()) ? jobs[j_el0].pt_off : np;   // phonon jobs come last
+    if (np_el > 0) {
+        k_diff<<<(unsigned)((np_el + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np_el);
+        CK(cudaGetLastError());
+    }
+    if (np > np_el) {
+        k_diff_phonon<<<(unsigned)((np - np_el + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np_el, np);
+        CK(cudaGetLastError());
+    }
     k_accum<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj, d_val, d_sig, d_ded, d_rhw, d_rL, d_rX);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev1));
@@ -652,7 +787,7 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     total(T->hole, false, T->Hole_IMFP);
     if (T->has_phot) total(T->phot, false, T->Phot_IMFP);
     if (T->has_shi) total(T->shi, false, T->SHI_path);
-    if (st) st->n_kernel_launches += 4;
+    if (st) st->n_kernel_launches += 3 + (np_el > 0 ? 1 : 0) + (np > np_el ? 1 : 0);
     return TREKIS_OK;
 }
 

@@ -30,6 +30,8 @@ ERR_BITS = {
     1 << 6: "queue full", 1 << 7: "photon negative energy",
 }
 
+ABI_VERSION = 4   # TREKIS_ABI_VERSION of the header these structs mirror
+
 _S = MAX_SHELLS
 _O = MAX_OSC
 
@@ -41,6 +43,7 @@ class Atom(C.Structure):
         ("N_osc", C.c_int32 * _S), ("Nel", C.c_double * _S), ("Ip", C.c_double * _S),
         ("Auger", C.c_double * _S), ("Radiat", C.c_double * _S),
         ("E0", (C.c_double * _O) * _S), ("A", (C.c_double * _O) * _S), ("Gamma", (C.c_double * _O) * _S),
+        ("form_factor", C.c_double * 5),
     ]
 
 
@@ -207,6 +210,9 @@ def load(path=None):
         f = getattr(lib, name)
         f.restype = res
         f.argtypes = args
+    if lib.trekis_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{p} has ABI version {lib.trekis_abi_version()}, these bindings expect "
+                           f"{ABI_VERSION}: rebuild it")
     if path is None:
         _lib = lib
     return lib

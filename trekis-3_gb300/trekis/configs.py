@@ -12,7 +12,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .material import AtomKind, MaterialModel, Shell, attach_dos, parabolic_dos_file, sumrules, w_plasma
+from .material import (AtomKind, MaterialModel, Shell, attach_dos, normalise_phonon_for_screening,
+                       parabolic_dos_file, sumrules, w_plasma)
 
 
 @dataclass
@@ -154,6 +155,20 @@ def cfg4(layer=1000.0, Tim=1000.0, NMC=1_000_000, ion_E=2.2e9, n_R=200):
                 sh.Radiat = float(math.exp(rr.uniform(math.log(1e3), math.log(1e5))))
     return Workload(name="cfg4-sio2-u2200-phonon", material=mat, ion_Z=92, ion_mass=238.0, ion_E=ion_E,
                     Tim=Tim, dt=1.0, NMC=NMC, R_edges=log_radial_grid(n_R, 0.5, 5000.0), seed=1004)
+
+
+def cfg4_screened(elast_zeff=3, **kw):
+    """cfg4 with the nucleus screened dynamically in the phonon elastic cross
+    section: CDF_elast_Zeff 2 (valence CDF and core form factors) or 3 (the
+    shells' CDFs), the phonon oscillators renormalised to one per atom as the
+    reference does for these options."""
+    if elast_zeff not in (2, 3):
+        raise ValueError("elast_zeff must be 2 or 3")
+    w = cfg4(**kw)
+    w.material.CDF_elast_Zeff = elast_zeff
+    normalise_phonon_for_screening(w.material)
+    w.name = f"{w.name}-screened{elast_zeff}"
+    return w
 
 
 def small(cfg_fn=cfg0, **kw):

@@ -37,6 +37,28 @@ def element_mass(Z):
     return float(np.float32(_MASS_LITERALS[Z]))
 
 
+# coefficients a1..a5 of PENELOPE's analytical atomic form factor
+# F(x, Z) = Z (1 + a1 x^2 + a2 x^3 + a3 x^4) / (1 + a4 x^2 + a5 x^4)^2
+# (Baro et al., Radiat. Phys. Chem. 44 (1994) 531; Salvat et al., PENELOPE
+# (2001) Eq. 2.7), as the reference's Atomic_form_factors.dat lists them per Z,
+# for the elements of the synthetic targets.  The physical data must be the
+# same numbers for a screened elastic table to equal a Fortran run's.
+_FORM_FACTOR = {
+    3: (43.1, 94.875, 1057.9, 47.367, 55.674), 6: (12.211, -19.572, 78.788, 13.979, 4.8936),
+    7: (9.3229, -12.382, 38.293, 10.766, 2.5506), 8: (3.2455, -3.6827, 12.564, 6.5252, 1.2236),
+    9: (2.4197, -2.4542, 6.9091, 5.1631, 0.74698), 11: (30.926, 134.01, 0.0, 27.145, 4.7809),
+    12: (15.315, 79.717, 0.0, 18.724, 4.6315), 13: (7.7061, 62.164, 1.6759e-9, 14.782, 4.3677),
+    14: (3.9493, 40.3, 13.026, 11.608, 4.9269), 15: (2.2042, 31.682, 3.0569, 9.775, 2.6033),
+    16: (19.453, -13.639, 155.21, 16.17, 9.6229), 20: (57.37, 122.05, 475.08, 41.381, 8.6975),
+}
+
+
+def form_factor_coefficients(Z):
+    if Z not in _FORM_FACTOR:
+        raise KeyError(f"no form-factor coefficients for Z={Z}")
+    return _FORM_FACTOR[Z]
+
+
 @dataclass
 class Shell:
     Ip: float            # [eV]
@@ -55,10 +77,13 @@ class AtomKind:
     Pers: float
     shells: list
     Mass: float = None
+    form_factor: tuple = None   # a1..a5; None: the table's entry for Z, zeros if it has none
 
     def __post_init__(self):
         if self.Mass is None:
             self.Mass = element_mass(self.Z)
+        if self.form_factor is None:
+            self.form_factor = _FORM_FACTOR.get(self.Z, (0.0,) * 5)
 
 
 @dataclass
@@ -138,6 +163,8 @@ class MaterialModel:
                     raise ValueError("too many oscillators")
                 for k in range(len(s.E0)):
                     ca.E0[j][k], ca.A[j][k], ca.Gamma[j][k] = s.E0[k], s.A[k], s.Gamma[k]
+            for k in range(5):
+                ca.form_factor[k] = a.form_factor[k]
         m.Dens, m.At_Dens, m.Vsound, m.E_F, m.Egap = self.Dens, self.At_Dens, self.Vsound, self.E_F, self.Egap
         m.Layer, m.N_VB_el = self.Layer, self.N_VB_el
         m.work_function, m.bar_length, m.bar_height = self.work_function, self.bar_length, self.bar_height
@@ -217,6 +244,28 @@ def sumrules(A, E0, G, x_min, Omega):
     ksum = 2.0 * G_E * G_E / (math.pi * Omega * G_H * G_H) * ne
     fsum = f * 2.0 / math.pi
     return ksum, fsum
+
+
+def normalise_phonon_for_screening(mat):
+    """Scale the phonon oscillators so that their k-sum counts the atoms of a
+    formula unit, as get_single_pole does for a user-given phonon CDF when
+    the nucleus is screened dynamically (CDF_elast_Zeff 2 or 3,
+    Cross_sections.f90:637-653): the mean atomic mass sets the plasma
+    frequency and the sum starts at 1e-8 eV."""
+    N_at_mol = 0.0
+    for a in mat.atoms:
+        N_at_mol += a.Pers
+    mm = 0.0
+    for a in mat.atoms:
+        mm += a.Pers * a.Mass
+    mean_mass = mm * G_MP / N_at_mol
+    omega = w_plasma(1e6 * mat.At_Dens / N_at_mol, mean_mass)
+    E0 = [o[0] for o in mat.ph_osc]
+    A = [o[1] for o in mat.ph_osc]
+    G = [o[2] for o in mat.ph_osc]
+    ksum, _ = sumrules(A, E0, G, 1.0e-8, omega)
+    mat.ph_osc = [(e, a * N_at_mol / ksum, g) for e, a, g in zip(E0, A, G)]
+    return mat
 
 
 # ---- DOS: Reading_files_and_parameters.f90:2317-2454 --------------------------------
