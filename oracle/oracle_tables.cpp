@@ -601,6 +601,7 @@ int build_tables(const trekis_material& m, const trekis_ion& ion, const trekis_t
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
     if (stride < 1) stride = 1;
+    if (m.N_ph_osc < 0 || m.N_ph_osc > TREKIS_MAX_PH_OSC) return TREKIS_EINVAL;
     const int NS = TREKIS_MAX_ATOMS * TREKIS_MAX_SHELLS;
     T.el.assign(NS, {}); T.hole.assign(NS, {}); T.phot.assign(NS, {}); T.shi.assign(NS, {});
     T.shi_dsde.assign(NS, {}); T.el_rows.assign(NS, {});

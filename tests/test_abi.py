@@ -80,3 +80,19 @@ def test_no_cpu_fallback(lib):
     rc = l.trekis_tables_build(h.ref(), C.byref(ion), C.byref(tc), C.byref(out), C.byref(st))
     assert rc == -2 and st.code == -2
     assert b"sm_103a" in l.trekis_last_error()
+
+
+@pytest.mark.parametrize("field,value", [("N_ph_osc", 9), ("N_ph_osc", -1), ("N_atoms", 0), ("N_dos", -1)])
+def test_invalid_material_refused_before_any_device_work(lib, field, value):
+    """Out-of-range counts are refused with TREKIS_EINVAL whether or not a GPU
+    is present (the material is checked before the device)."""
+    from trekis import api, configs
+    l = abi.load()
+    w = configs.small(configs.cfg0)
+    h = w.material.to_c()
+    setattr(h.struct, field, value)
+    out = C.c_void_p()
+    st = abi.Status.fresh()
+    rc = l.trekis_tables_build(h.ref(), C.byref(api.ion_struct(w)), C.byref(abi.TableCfg(build_shi=1)),
+                               C.byref(out), C.byref(st))
+    assert rc == -1 and st.code == -1 and not out.value

@@ -485,9 +485,12 @@ static double mott_sigma(int Zi, double Ee) {
 
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st) {
     const trekis_material& m = T->mat;
-    cudaEvent_t ev0, ev1;
-    CK(cudaEventCreate(&ev0)); CK(cudaEventCreate(&ev1));
-    CK(cudaEventRecord(ev0));
+    struct Events {   // released on every return
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); }
+    } ev;
+    CK(cudaEventCreate(&ev.a)); CK(cudaEventCreate(&ev.b));
+    CK(cudaEventRecord(ev.a));
     // compact shells
     T->nsh = 0;
     for (int a = 0; a < m.N_atoms; ++a)
@@ -657,7 +660,7 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     }
     k_accum<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj, d_val, d_sig, d_ded, d_rhw, d_rL, d_rX);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ev1));
+    CK(cudaEventRecord(ev.b));
     std::vector<double> sig(nj), ded(nj), rhw(nr), rL(nr), rX(nr);
     CK(cudaMemcpy(sig.data(), d_sig, 8 * nj, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(ded.data(), d_ded, 8 * nj, cudaMemcpyDeviceToHost));
@@ -667,11 +670,10 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
         CK(cudaMemcpy(rX.data(), d_rX, 8 * nr, cudaMemcpyDeviceToHost));
     }
     float ms = 0.f;
-    CK(cudaEventSynchronize(ev1));
-    CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    CK(cudaEventSynchronize(ev.b));
+    CK(cudaEventElapsedTime(&ms, ev.a, ev.b));
     T->build_ms = ms;
     T->build_points = (uint64_t)np;
-    cudaEventDestroy(ev0); cudaEventDestroy(ev1);
 
     // host mirror
     T->el.assign(nsh, {}); T->hole.assign(nsh, {}); T->shi.assign(nsh, {}); T->dsde.assign(nsh, {});
