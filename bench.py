@@ -312,6 +312,14 @@ _ORACLE_TABLES = {}
 def cpu_baseline(args, n_it=None, nthreads=None):
     """The FP64 oracle (restatement of the reference's loop) on the host cores:
     one cfg1 iteration per thread, heap-ordered earliest-event loop."""
+    events, dt, nthreads, n_it = cpu_sample(args, n_it, nthreads)
+    return {"value": events / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n_it} cfg1 iterations ({events} events) in {dt:.1f} s, FP64 oracle, "
+                      "OpenMP over iterations, heap event queue"}
+
+
+def cpu_sample(args, n_it=None, nthreads=None):
+    """One timed oracle run: (events, seconds, threads, iterations)."""
     import oracle_py
     from trekis import abi, api
     w = workload()
@@ -329,9 +337,7 @@ def cpu_baseline(args, n_it=None, nthreads=None):
     t0 = time.perf_counter()
     o.mc_run(cfg, tal, st, nthreads=nthreads, sched=1)
     dt = time.perf_counter() - t0
-    return {"value": st.n_events / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n_it} cfg1 iterations ({st.n_events} events) in {dt:.1f} s, FP64 oracle, "
-                      "OpenMP over iterations, heap event queue"}
+    return st.n_events, dt, nthreads, n_it
 
 
 def cpu_warm(args):
@@ -353,19 +359,18 @@ def run_reference(args):
         return
     w = workload()
     tot_ev = tot_s = 0.0
-    cpu = None
     # warm-up: thread pool and tables, on one short iteration per thread (a
     # full cfg1 iteration takes tens of seconds on one core)
     for _ in range(args.warmup):
         cpu_warm(args)
     for i in range(args.steps):
-        c = cpu_baseline(args)
-        ev = c["value"] * float(c["sample"].split("in ")[1].split(" s")[0])
+        ev, dt, nthreads, n_it = cpu_sample(args)
         tot_ev += ev
-        tot_s += ev / c["value"]
-        cpu = c
+        tot_s += dt
     value = tot_ev / tot_s
-    cpu["value"] = value
+    cpu = {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+           "sample": f"{args.steps} x {n_it} cfg1 iterations ({int(tot_ev)} events) in {tot_s:.1f} s, FP64 oracle, "
+                     "OpenMP over iterations, heap event queue"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
