@@ -96,3 +96,58 @@ def test_invalid_material_refused_before_any_device_work(lib, field, value):
     rc = l.trekis_tables_build(h.ref(), C.byref(api.ion_struct(w)), C.byref(abi.TableCfg(build_shi=1)),
                                C.byref(out), C.byref(st))
     assert rc == -1 and st.code == -1 and not out.value
+
+
+def _fortran_types():
+    """The bind(C) derived types of INTEGRATION.md: name -> [(kind, count)]."""
+    txt = (ROOT / "INTEGRATION.md").read_text()
+    consts = {k: getattr(abi, k.replace("TREKIS_", "")) for k in
+              ("TREKIS_MAX_ATOMS", "TREKIS_MAX_SHELLS", "TREKIS_MAX_OSC", "TREKIS_MAX_PH_OSC")}
+    out = {}
+    for m in re.finditer(r"type, bind\(C\) :: (\w+)\n(.*?)\n\s*end type", txt, re.S):
+        body = re.sub(r"!.*", "", m.group(2)).replace("&\n", " ")
+        fields = []
+        for line in body.splitlines():
+            if "::" not in line:
+                continue
+            kind, names = line.split("::")
+            kind = kind.strip()
+            for nm in re.findall(r"\w+(?:\([^)]*\))?", names):
+                count = 1
+                dims = re.search(r"\(([^)]*)\)", nm)
+                if dims:
+                    for d in dims.group(1).split(","):
+                        d = d.strip()
+                        count *= int(d) if d.isdigit() else consts[d]
+                fields.append((kind, count))
+        out[m.group(1)] = fields
+    return out
+
+
+def _c_layout(fields, types):
+    """Size and alignment of a C struct with these members."""
+    prim = {"integer(c_int32_t)": (4, 4), "integer(c_int64_t)": (8, 8), "real(c_double)": (8, 8),
+            "type(c_ptr)": (8, 8)}
+    off = align = 0
+    for kind, count in fields:
+        if kind in prim:
+            sz, al = prim[kind]
+        else:
+            sz, al = _c_layout(types[re.match(r"type\((\w+)\)", kind).group(1)], types)
+        off = (off + al - 1) // al * al + sz * count
+        align = max(align, al)
+    return (off + align - 1) // align * align, align
+
+
+def test_fortran_interface_types_match_c():
+    """Every bind(C) type INTEGRATION.md gives a Fortran maintainer has the size
+    of the C struct it mirrors, so the library never reads past a Fortran
+    argument."""
+    types = _fortran_types()
+    mirrors = {"trekis_atom": abi.Atom, "trekis_material": abi.Material, "trekis_ion": abi.Ion,
+               "trekis_table_cfg": abi.TableCfg, "trekis_run_cfg": abi.RunCfg, "trekis_tallies": abi.Tallies,
+               "trekis_status": abi.Status, "trekis_output_cfg": abi.OutputCfg, "trekis_batch_cfg": abi.BatchCfg}
+    assert set(types) <= set(mirrors), set(types) - set(mirrors)
+    assert {"trekis_material", "trekis_run_cfg", "trekis_tallies", "trekis_status"} <= set(types)
+    for name, fields in types.items():
+        assert _c_layout(fields, types)[0] == C.sizeof(mirrors[name]), name
