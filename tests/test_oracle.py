@@ -363,3 +363,23 @@ def test_screened_phonon_tables():
                              for k in range(len(w.material.atoms[0].shells) - len(ox.shells) + 1)]
     with pytest.raises(RuntimeError, match="-7"):
         oracle_py.OracleTables(w.material.to_c(), api.ion_struct(w), abi.TableCfg(build_shi=0, build_photon=0))
+
+
+def test_phonon_normalisation_for_screening():
+    """get_single_pole's renormalisation for CDF_elast_Zeff 2 and 3
+    (Cross_sections.f90:637-653): the phonon k-sum counts the atoms of a
+    formula unit, with the plasma frequency of the mean atomic mass."""
+    import functools
+    w = configs.cfg4_screened(2, NMC=1)
+    m = w.material
+    n_at = sum(a.Pers for a in m.atoms)
+    mean_mass = sum(a.Pers * a.Mass for a in m.atoms) * material.G_MP / n_at
+    om = material.w_plasma(1e6 * m.At_Dens / n_at, mean_mass)
+    E0, A, G = zip(*m.ph_osc)
+    ks, _ = material.sumrules(A, E0, G, 1e-8, om)
+    assert abs(ks - n_at) < 1e-9 * n_at
+    base = configs.cfg4(NMC=1).material.ph_osc
+    ratios = [a2 / a1 for (_, a1, _), (_, a2, _) in zip(base, m.ph_osc)]
+    assert max(ratios) - min(ratios) < 1e-12 * max(ratios)   # one common factor
+    with pytest.raises(ValueError):
+        functools.partial(configs.cfg4_screened, 1)()
