@@ -242,6 +242,14 @@ typedef struct {
 
 int32_t trekis_abi_version(void);
 
+/* Nt, the leading dimension of every Out_* array of a run with this time
+ * grid: the points of set_time_grid (Monte_Carlo.f90:2118-2149) that
+ * Monte_Carlo_modelling tallies (Monte_Carlo.f90:572-580).  dt_flag 0:
+ * linear steps dt; 1: logarithmic from 0.01 fs with ratio dt > 1.  Host only
+ * (no device needed); TREKIS_EINVAL for a grid that would not end or would
+ * exceed 4194304 points. */
+int32_t trekis_time_points(double Tim, double dt, int32_t dt_flag);
+
 /* Is an sm_103a device usable?  Returns 1 if yes, 0 if not. */
 int32_t trekis_device_ok(void);
 

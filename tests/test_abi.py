@@ -151,3 +151,20 @@ def test_fortran_interface_types_match_c():
     assert {"trekis_material", "trekis_run_cfg", "trekis_tallies", "trekis_status"} <= set(types)
     for name, fields in types.items():
         assert _c_layout(fields, types)[0] == C.sizeof(mirrors[name]), name
+
+
+def test_time_points(lib, oracle_lib):
+    """trekis_time_points equals the tallied points of the oracle's and the
+    Python host's time grids, and refuses grids that would not end."""
+    from trekis import api
+    l = abi.load()
+    for Tim, dt, flag in [(100.0, 1.0, 0), (1000.0, 1.0, 0), (20.0, 0.7, 0), (5.0, 10.0, 0), (1000.0, 1.1, 1),
+                          (0.005, 2.0, 1), (1e4, 1.5, 1), (99.9999999, 1.0, 0)]:
+        n = l.trekis_time_points(Tim, dt, flag)
+        buf = (C.c_double * 100000)()
+        m = C.c_int64()
+        oracle_lib.oracle_time_grid(Tim, dt, flag, buf, 100000, C.byref(m))
+        assert n == m.value == len(api.n_time_points(Tim, dt, flag)) > 0, (Tim, dt, flag)
+    for Tim, dt, flag in [(100.0, 0.5, 1), (100.0, 1.0, 1), (100.0, 0.0, 0), (-1.0, 1.0, 0), (1e9, 1e-3, 0),
+                          (100.0, 1.0, 2), (float("nan"), 1.0, 0)]:
+        assert l.trekis_time_points(Tim, dt, flag) == -1, (Tim, dt, flag)

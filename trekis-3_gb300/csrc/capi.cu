@@ -674,6 +674,11 @@ using namespace tk;
 extern "C" {
 
 int32_t trekis_abi_version(void) { return TREKIS_ABI_VERSION; }
+
+int32_t trekis_time_points(double Tim, double dt, int32_t dt_flag) {
+    if (!time_grid_ok(Tim, dt, dt_flag)) { set_error("invalid time grid"); return TREKIS_EINVAL; }
+    return (int32_t)tallied_times(Tim, dt, dt_flag).size();
+}
 int32_t trekis_device_ok(void) { return device_ok(); }
 const char* trekis_last_error(void) { return g_err.c_str(); }
 
@@ -789,7 +794,10 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
     if (t->mat.work_function > 0.0) { set_error("surface emission is not supported"); return TREKIS_EUNSUPPORTED; }
     if (t->ion.Kind_ion != 0) { set_error("Brandt-Kitagawa ions are not supported"); return TREKIS_EUNSUPPORTED; }
     if (cfg->NMC < 0 || cfg->N_R < 1 || !cfg->Out_R || !(cfg->Tim > 0) || !(cfg->dt > 0)) return TREKIS_EINVAL;
-    if (cfg->dt_flag != 0 && cfg->dt_flag != 1) return TREKIS_EINVAL;
+    if (!time_grid_ok(cfg->Tim, cfg->dt, cfg->dt_flag)) {
+        set_error("time grid: dt_flag 0 or 1, a logarithmic ratio dt > 1, at most 4194304 points");
+        return TREKIS_EINVAL;
+    }
     if (cfg->sampler != 0 && cfg->sampler != 1) { set_error("sampler must be 0 or 1"); return TREKIS_EINVAL; }
     if (cfg->use_graph != 0) { set_error("graph capture of the wavefront loop is not built (use_graph must be 0)"); return TREKIS_EUNSUPPORTED; }
     for (int j = 1; j < cfg->N_R; ++j) if (!(cfg->Out_R[j] > cfg->Out_R[j - 1])) return TREKIS_EINVAL;

@@ -1,5 +1,6 @@
 // impl.h -- host-side structures of the library (not part of the C ABI).
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <memory>
 #include <string>
@@ -156,6 +157,17 @@ struct trekis_tables {
 };
 
 namespace tk {
+// Bound on the raw time grid of a run (set_time_grid, Monte_Carlo.f90:2118-2149)
+// before anything walks it: a logarithmic grid with a ratio dt <= 1 would
+// never end, and no tally holds more than kMaxTimePoints rows.
+constexpr double kMaxTimePoints = 4194304.0;
+inline bool time_grid_ok(double Tim, double dt, int flag) {
+    if (!(Tim > 0.0) || !(dt > 0.0) || !std::isfinite(Tim) || !std::isfinite(dt)) return false;
+    if (flag != 0 && flag != 1) return false;
+    if (flag == 0) return Tim / dt + 2.0 <= kMaxTimePoints;
+    if (!(dt > 1.0)) return false;
+    return Tim < 0.01 || std::log(Tim / 0.01) / std::log(dt) + 3.0 <= kMaxTimePoints;
+}
 void set_error(const std::string& s);
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st);
 std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax);

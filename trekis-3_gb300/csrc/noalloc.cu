@@ -408,7 +408,10 @@ int check_args(const trekis_tables* t, const trekis_material* mat, const trekis_
     if (cfg->NMC < 0 || cfg->N_R < 1 || !cfg->Out_R || !(cfg->Tim > 0) || !(cfg->dt > 0)) {
         set_error("invalid run configuration"); return TREKIS_EINVAL;
     }
-    if (cfg->dt_flag != 0 && cfg->dt_flag != 1) { set_error("dt_flag must be 0 or 1"); return TREKIS_EINVAL; }
+    if (!time_grid_ok(cfg->Tim, cfg->dt, cfg->dt_flag)) {
+        set_error("time grid: dt_flag 0 or 1, a logarithmic ratio dt > 1, at most 4194304 points");
+        return TREKIS_EINVAL;
+    }
     for (int j = 1; j < cfg->N_R; ++j)
         if (!(cfg->Out_R[j] > cfg->Out_R[j - 1])) { set_error("radii must increase"); return TREKIS_EINVAL; }
     *Nt = walk_times(cfg->Tim, cfg->dt, cfg->dt_flag, [](int, double) {});

@@ -158,6 +158,7 @@ class Status(C.Structure):
 # every symbol the header declares, with its ctypes signature
 SIGNATURES = {
     "trekis_abi_version": (C.c_int32, []),
+    "trekis_time_points": (C.c_int32, [C.c_double, C.c_double, C.c_int32]),
     "trekis_device_ok": (C.c_int32, []),
     "trekis_tables_build": (C.c_int32, [C.POINTER(Material), C.POINTER(Ion), C.POINTER(TableCfg),
                                         C.POINTER(C.c_void_p), C.POINTER(Status)]),

@@ -21,6 +21,8 @@ TALLY_1D = ("Out_tot_Ne", "Out_tot_Nphot", "Out_tot_E", "Out_E_e", "Out_E_phot",
 
 def n_time_points(Tim, dt, dt_flag=0):
     """Tallied time-grid points (Monte_Carlo.f90:2118-2149 and 572-580)."""
+    if not (Tim > 0 and dt > 0) or (dt_flag > 0 and not dt > 1.0):
+        raise ValueError("time grid needs Tim > 0, dt > 0 and a logarithmic ratio dt > 1")
     if dt_flag <= 0:
         n = int(np.ceil(Tim / dt)) + 1
         raw = [0.0] * n
