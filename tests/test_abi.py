@@ -168,3 +168,21 @@ def test_time_points(lib, oracle_lib):
     for Tim, dt, flag in [(100.0, 0.5, 1), (100.0, 1.0, 1), (100.0, 0.0, 0), (-1.0, 1.0, 0), (1e9, 1e-3, 0),
                           (100.0, 1.0, 2), (float("nan"), 1.0, 0)]:
         assert l.trekis_time_points(Tim, dt, flag) == -1, (Tim, dt, flag)
+
+
+def test_c_caller_example(lib, tmp_path):
+    """The C caller of INTEGRATION.md compiles against the header alone, links
+    the library and runs: without a GB300 it stops at TREKIS_ENODEVICE."""
+    txt = (ROOT / "INTEGRATION.md").read_text()
+    src = txt.split("## 7. Calling from C", 1)[1].split("```c\n", 1)[1].split("```", 1)[0]
+    (tmp_path / "caller.c").write_text(src)
+    exe = tmp_path / "caller"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-o", str(exe),
+                    str(tmp_path / "caller.c"), "-L", str(build.LIB.parent), "-ltrekis_gb300",
+                    f"-Wl,-rpath,{build.LIB.parent}"], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    if abi.load().trekis_device_ok():
+        assert "collisions" in r.stdout
+    else:
+        assert r.stdout.startswith("no device")
