@@ -95,6 +95,17 @@ def test_folder_names_do_not_clash(lib, tmp_path):
     assert d2 == d1 + "_1"
 
 
+def test_tallies_of_another_time_grid_are_refused(lib, tmp_path):
+    """The tallies' Nt must be the run's number of tallied times; nothing is
+    written otherwise."""
+    w = configs.small(configs.cfg0, Tim=12.0, n_R=5)
+    tal = seeded_tallies(w, 4)
+    bad = api.TallySet(tal.Nt + 1, tal.NR, tal.Nat, tal.Nshl, N_dos=tal.N_dos, spectra=True)
+    with pytest.raises(RuntimeError):
+        api.save_output(w, bad, 2, tmp_path, lib=lib)
+    assert os.listdir(tmp_path) == []
+
+
 def test_fortran_number_formats():
     assert oracle_output.fe(123.456) == "  0.1234560000000000E+003"
     assert oracle_output.fe(-1.0e-5) == " -0.1000000000000000E-004"

@@ -147,6 +147,10 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
         tk::set_error("invalid output arguments");
         return TREKIS_EINVAL;
     }
+    if (!tk::time_grid_ok(cfg->Tim, cfg->dt, cfg->dt_flag) || trekis_time_points(cfg->Tim, cfg->dt, cfg->dt_flag) != t->Nt) {
+        tk::set_error("the tallies' Nt does not match the run's time grid");
+        return TREKIS_EINVAL;
+    }
     const int N = t->Nt, NR = t->N_R, Nat = t->Nat, Nshl = t->Nshl;
     for (int a = 0; a < Nat; ++a) {
         if (m->atoms[a].N_shl > Nshl || !oc->atom_names[a]) { tk::set_error("invalid output arguments"); return TREKIS_EINVAL; }
