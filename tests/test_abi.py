@@ -82,7 +82,8 @@ def test_no_cpu_fallback(lib):
     assert b"sm_103a" in l.trekis_last_error()
 
 
-@pytest.mark.parametrize("field,value", [("N_ph_osc", 9), ("N_ph_osc", -1), ("N_atoms", 0), ("N_dos", -1)])
+@pytest.mark.parametrize("field,value", [("N_ph_osc", 9), ("N_ph_osc", -1), ("N_atoms", 0), ("N_dos", -1),
+                                         ("Layer", 0.0), ("At_Dens", -1.0), ("Dens", float("nan"))])
 def test_invalid_material_refused_before_any_device_work(lib, field, value):
     """Out-of-range counts are refused with TREKIS_EINVAL whether or not a GPU
     is present (the material is checked before the device)."""
