@@ -286,7 +286,7 @@ def run_gpu(args):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tot_ms_all / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
+        "iterations_per_s": world * args.steps * iters / (tot_ms_all / 1e3), "dtype": "f32", "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
         "config": config_dict(w, iters, {"parallelism": f"iterations sharded over {world} GPU(s), no collective"}),
         "e2e": {"value": e2e_ev / e2e_s if e2e_s else None, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // max(args.e2e_steps, 1), "d2h_bytes_per_step": d2h // max(args.e2e_steps, 1)},
@@ -373,6 +373,7 @@ def run_reference(args):
                      "OpenMP over iterations, heap event queue"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps, "higher_is_better": True,
+           "iterations_per_s": args.steps * n_it / tot_s,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
            "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
            "config": config_dict(w, args.iters, {"parallelism": "host threads",
