@@ -383,3 +383,99 @@ def test_phonon_normalisation_for_screening():
     assert max(ratios) - min(ratios) < 1e-12 * max(ratios)   # one common factor
     with pytest.raises(ValueError):
         functools.partial(configs.cfg4_screened, 1)()
+
+
+# ---- the reference's material file format ------------------------------------------
+_CDF_NUMERIC = """Test oxide ! name
+2\t\t! elements
+13 2 ! Z, share
+8  3
+3.95  6510.0  4.4  6.7d0  ! density, sound, Fermi, gap
+3   ! shells of the first element
+1  1  1559.1e0  2  1.8d0
+1565  178  1200
+
+1  2  89.0e0  8  20.6e0
+80  620  160
+2  63  6.7  24  1.0d23
+25.4  275  12.5
+38  520  38
+1   ! shells of the second element
+0  1  538.0  2  3.98
+2   ! phonon oscillators
+0.1125 0.003 0.005
+0.061  0.000045  0.0021
+"""
+
+_CDF_FORMULA = """Forsterite-like
+Mg2SiO4  ! a formula instead of a count
+3.2  8000.0  5.0   ! no gap: a metal's minimum gap
+1
+1  -1  1839.0  2  1.0
+1900  200  1900
+1
+1  1  1305.0  2  1.5
+1350  150  1350
+2
+1  1  543.1  2  3.0
+560  300  560
+1  63  0.05  24  1d23
+20  500  10
+"""
+
+
+def test_cdf_reader_numeric_layout(tmp_path):
+    p = tmp_path / "oxide.cdf"
+    p.write_text(_CDF_NUMERIC)
+    m = material.read_cdf(p, Layer=50.0)
+    assert m.name == "Test oxide ! name"   # the name line keeps text after '!' when it has no tab
+    assert [(a.Z, a.Pers, len(a.shells)) for a in m.atoms] == [(13, 2.0, 3), (8, 3.0, 1)]
+    assert m.atoms[0].Mass == float(np.float32(26.9815386))   # Find_element_name's single-precision literal
+    assert (m.Dens, m.Vsound, m.E_F, m.Egap, m.Layer) == (3.95, 6510.0, 4.4, 6.7, 50.0)
+    vb = m.atoms[0].shells[2]
+    assert (vb.designator, vb.Nel, vb.Auger, vb.E0, vb.A, vb.Gamma) == (63, 24.0, 1e23, [25.4, 38.0], [275.0, 520.0],
+                                                                          [12.5, 38.0])
+    assert m.N_VB_el == 24.0
+    o1s = m.atoms[1].shells[0]
+    assert (o1s.KOCS, o1s.KOCS_SHI, o1s.E0) == (2, 2, [])   # no oscillators: BEB in the reference
+    assert m.ph_osc == [(0.1125, 0.003, 0.005), (0.061, 0.000045, 0.0021)]
+
+
+def test_cdf_reader_formula_and_single_pole_phonon(tmp_path):
+    p = tmp_path / "fo.cdf"
+    p.write_text(_CDF_FORMULA)
+    m = material.read_cdf(p)
+    # Decompose_compound: Mg2 Si O4, sorted by descending Z, double-precision masses
+    assert [(a.Z, a.Pers) for a in m.atoms] == [(14, 1.0), (12, 2.0), (8, 4.0)]
+    assert m.atoms[0].Mass == 28.0854 and m.atoms[0].shells[0].KOCS == 2   # negative designator: BEB electrons
+    assert m.atoms[0].shells[0].KOCS_SHI == 1 and m.atoms[0].shells[0].designator == 1
+    assert m.Egap == 0.1 and m.atoms[2].shells[1].Ip == 0.1
+    (e0, a, g), = m.ph_osc                            # the file ends: get_single_pole's phonon
+    assert g == 0.5 * e0 > 0
+    n_at = sum(x.Pers for x in m.atoms)
+    mean_mass = sum(x.Pers * x.Mass for x in m.atoms) * material.G_MP / n_at
+    ks, _ = material.sumrules([a], [e0], [g], 1e-8, material.w_plasma(1e6 * m.At_Dens / n_at, mean_mass))
+    assert abs(ks - n_at) < 1e-9 * n_at
+    assert material.formula_mass(56) == 136.327 and material.element_mass(56) == float(np.float32(137.327))
+
+
+def test_cdf_reader_refusals(tmp_path):
+    bad = tmp_path / "bad.cdf"
+    bad.write_text(_CDF_NUMERIC.replace("3.95  6510.0  4.4  6.7d0  !", "3.95  6510.0  !"))
+    with pytest.raises(ValueError):
+        material.read_cdf(bad)                        # the reference's reader fails on this line too
+    sp = tmp_path / "sp.cdf"
+    sp.write_text("Silicon\nSi\n2.33 8430.0 0.56 1.2\nVALENCE\n")
+    with pytest.raises(NotImplementedError):
+        material.read_cdf(sp)                         # single-pole files need the EADL database
+    assert material.ELEMENT_SYMBOLS[:92] == list(api.ELEMENTS) and len(material.ELEMENT_SYMBOLS) == 118
+
+
+def test_dos_reader(tmp_path):
+    p = tmp_path / "x.dos"
+    p.write_text("  -0.3d1   0.5\n-2.0, 0.25E+00\n -1.0 1.0 ! top region\n0.0 0.0\n")
+    e, d = material.read_dos(p)
+    assert list(e) == [-3.0, -2.0, -1.0, 0.0] and list(d) == [0.5, 0.25, 1.0, 0.0]
+    p.write_text("-1.0 0.5\n\n0.0 0.0\n")   # a blank record: fewer pairs than records
+    with pytest.raises(ValueError):
+        material.read_dos(p)

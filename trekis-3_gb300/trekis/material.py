@@ -11,6 +11,7 @@ plain float64 arithmetic in the reference's order of operations.
 """
 from dataclasses import dataclass, field
 import math
+import re
 
 import numpy as np
 
@@ -23,12 +24,40 @@ G_MP = 1836.1526724780 * G_ME
 G_H = 1.05457162853e-34
 G_E0 = 8.854187817620e-12
 
-# element masses [proton masses] as Find_element_name stores them
-# (Dealing_with_EADL.f90:1217): single-precision literals widened to double
-_MASS_LITERALS = {1: 1.0082, 6: 12.0112, 7: 14.0072, 8: 15.9992, 13: 26.9815386, 14: 28.0854,
-                  54: 131.293, 79: 196.966569, 92: 238.02891, 11: 22.98976928, 12: 24.3059,
-                  15: 30.973762, 16: 32.062, 20: 40.078, 22: 47.867, 26: 55.845, 29: 63.546,
-                  36: 83.798, 18: 39.948, 10: 20.1797, 9: 18.9984032, 3: 6.942, 4: 9.012182, 5: 10.812}
+# Element symbols and masses [proton masses], Z = 1..118, as Find_element_name
+# lists them (Dealing_with_EADL.f90:1217-1703).  Its masses are
+# single-precision literals, so a target whose CDF file gives atomic numbers
+# gets them rounded to single precision; a target given by a chemical formula
+# takes its masses from INPUT_atomic_data.dat in double precision
+# (Decompose_compound, Dealing_with_EADL.f90:28-146), where four entries
+# differ from the literals (_FORMULA_MASS).  The numbers must be the
+# reference's for the atomic density, and hence every table, to agree.
+_ELEMENT_TABLE = """
+    H 1.0082 He 4.002602 Li 6.942 Be 9.012182 B 10.812 C 12.0112 N 14.0072 O 15.9992
+    F 18.9984032 Ne 20.1797 Na 22.98976928 Mg 24.3059 Al 26.9815386 Si 28.0854 P 30.973762 S 32.062
+    Cl 35.452 Ar 39.948 K 39.0983 Ca 40.078 Sc 44.955912 Ti 47.867 V 50.9415 Cr 51.9961
+    Mn 54.938045 Fe 55.845 Co 58.933195 Ni 58.6934 Cu 63.546 Zn 65.38 Ga 69.723 Ge 72.630
+    As 74.92160 Se 78.96 Br 79.9049 Kr 83.798 Rb 85.4678 Sr 87.62 Y 88.90585 Zr 91.224
+    Nb 92.90638 Mo 95.96 Tc 98 Ru 101.07 Rh 102.90550 Pd 106.42 Ag 107.8682 Cd 112.411
+    In 114.818 Sn 118.710 Sb 121.760 Te 127.60 I 126.90447 Xe 131.293 Cs 132.9054519 Ba 137.327
+    La 138.90547 Ce 140.116 Pr 140.90765 Nd 144.242 Pm 145 Sm 150.36 Eu 151.964 Gd 157.25
+    Tb 158.92535 Dy 162.500 Ho 164.93032 Er 167.259 Tm 168.93421 Yb 173.054 Lu 174.9668 Hf 178.49
+    Ta 180.94788 W 183.84 Re 186.207 Os 190.23 Ir 192.217 Pt 195.084 Au 196.966569 Hg 200.592
+    Tl 204.389 Pb 207.2 Bi 208.98040 Po 209.0 At 210.0 Rn 222.0 Fr 223.0 Ra 226.0
+    Ac 227.0 Th 232.03806 Pa 231.035880 U 238.02891 Np 237.0 Pu 244.0 Am 243.0 Cm 247.0
+    Bk 247.0 Cf 251.0 Es 252.0 Fm 257.0 Md 258.0 No 259.0 Lr 262.0 Rf 267.0
+    Db 268.0 Sg 269.0 Bh 270.0 Hs 269.0 Mt 278.0 Ds 281.0 Rg 281.0 Cn 285.0
+    Uut 286.0 Fl 289.0 Uup 288.0 Lv 293.0 Uus 294.0 Uuo 294.0
+"""
+_ELEMENT_PAIRS = _ELEMENT_TABLE.split()
+ELEMENT_SYMBOLS = _ELEMENT_PAIRS[0::2]
+_MASS_LITERALS = {z + 1: float(m) for z, m in enumerate(_ELEMENT_PAIRS[1::2])}
+_FORMULA_MASS = {56: 136.327, 77: 192.317, 111: 282.0, 115: 290.0}
+
+
+def formula_mass(Z):
+    """Mass of an element named in a chemical formula (double precision)."""
+    return _FORMULA_MASS.get(Z, _MASS_LITERALS[Z])
 
 
 def element_mass(Z):
@@ -69,6 +98,8 @@ class Shell:
     E0: list = field(default_factory=list)
     A: list = field(default_factory=list)
     Gamma: list = field(default_factory=list)
+    KOCS: int = 1        # electron cross section: 1 CDF, 2 BEB (unsupported by the library)
+    KOCS_SHI: int = 1    # SHI cross section: 1 CDF, 2 BEB
 
 
 @dataclass
@@ -155,8 +186,8 @@ class MaterialModel:
                 raise ValueError("too many shells")
             for j, s in enumerate(a.shells):
                 ca.Shl_num[j] = s.designator
-                ca.KOCS[j] = 1
-                ca.KOCS_SHI[j] = 1
+                ca.KOCS[j] = s.KOCS
+                ca.KOCS_SHI[j] = s.KOCS_SHI
                 ca.N_osc[j] = len(s.E0)
                 ca.Nel[j], ca.Ip[j], ca.Auger[j], ca.Radiat[j] = s.Nel, s.Ip, s.Auger, s.Radiat
                 if len(s.E0) > abi.MAX_OSC:
@@ -353,45 +384,188 @@ def attach_dos(mat, e_file, d_file):
 
 # ---- readers of the reference's input formats ---------------------------------------
 
-def read_cdf(path, Layer=100.0):
-    """Full-CDF *.cdf reader (Reading_files_and_parameters.f90:1185-1644), numeric layout only."""
-    lines = [ln.split("!")[0].strip() for ln in open(path, encoding="latin-1")]
-    lines = [ln for ln in lines if ln]
-    it = iter(lines)
-    name = next(it)
-    n_el = int(next(it).split()[0])
-    kinds = []
-    for _ in range(n_el):
-        z, p = next(it).split()[:2]
-        kinds.append((int(z), float(p)))
-    nums = [float(x) for x in next(it).split()]
-    dens, vs, ef = nums[:3]
-    egap = nums[3] if len(nums) > 3 else 0.0
+_FORTRAN_INT = re.compile(r"^[+-]?\d+$")
+_FORTRAN_REAL = re.compile(r"^[+-]?(\d+\.?\d*|\.\d+)([eEdDqQ][+-]?\d+)?$")
+
+
+def _fortran_value(tok, kind):
+    """One item of a Fortran list-directed read; ValueError where the
+    reference's READ sets IOSTAT > 0."""
+    if kind is str:
+        return tok
+    if kind is int:
+        if not _FORTRAN_INT.match(tok):
+            raise ValueError(f"not an integer: {tok!r}")
+        return int(tok)
+    if not _FORTRAN_REAL.match(tok):
+        raise ValueError(f"not a number: {tok!r}")
+    return float(re.sub("[dDqQ]", "e", tok))
+
+
+class _ListDirected:
+    """Fortran list-directed READs over the records of a text file: a READ
+    takes its items from as many records as it needs (blank records give
+    none) and drops the rest of its last record; ``record`` reads one whole
+    record as READ(u,'(a)') does."""
+
+    def __init__(self, text):
+        self.recs = text.splitlines()
+        self.i = 0
+
+    def record(self):
+        if self.i >= len(self.recs):
+            raise EOFError
+        self.i += 1
+        return self.recs[self.i - 1]
+
+    def back(self):
+        self.i -= 1
+
+    @staticmethod
+    def items(rec, kinds, whole=True):
+        """Items of one record; with ``whole`` (a READ from that record alone)
+        a record with too few items is an error."""
+        out = []
+        for tok in re.split(r"[\s,]+", rec.strip()):
+            if tok and len(out) < len(kinds):
+                out.append(_fortran_value(tok, kinds[len(out)]))
+        if whole and len(out) < len(kinds):
+            raise ValueError(f"{len(kinds)} items wanted in {rec!r}")
+        return out
+
+    def read(self, *kinds):
+        out = []
+        while len(out) < len(kinds):
+            out += self.items(self.record(), kinds[len(out):], whole=False)
+        return out
+
+
+def decompose_formula(formula):
+    """Decompose_compound (Dealing_with_EADL.f90:28-146): element symbols (an
+    upper-case letter and lower-case letters) each followed by an optional
+    integer count; atoms sorted by descending Z as
+    sort_elements_in_chem_formula does (bubble sort, equal Z kept in order)."""
+    found, el, cnt = [], "", 0
+    for ch in formula:
+        if ch.isdigit():
+            cnt = cnt * 10 + int(ch)
+        elif "A" <= ch <= "Z":
+            if el:
+                found.append((el, float(cnt) if cnt > 0 else 1.0))
+            el, cnt = ch, 0
+        elif "a" <= ch <= "z":
+            el += ch
+    if el:
+        found.append((el, float(cnt) if cnt > 0 else 1.0))
     atoms = []
-    for z, p in kinds:
-        nsh = int(next(it).split()[0])
-        shells = []
-        for _ in range(nsh):
-            f = next(it).split()
-            ncdf, des, ip, nel, aug = int(f[0]), int(f[1]), float(f[2]), float(f[3]), float(f[4])
-            sh = Shell(Ip=max(ip, 0.1), Nel=nel, designator=abs(des), Auger=aug)
-            for _ in range(ncdf):
-                e0, a, g = [float(x) for x in next(it).split()[:3]]
-                sh.E0.append(e0); sh.A.append(a); sh.Gamma.append(g)
-            shells.append(sh)
-        atoms.append(AtomKind(Z=z, Pers=p, shells=shells))
-    ph = []
+    for sym, n in found:
+        if sym not in ELEMENT_SYMBOLS:
+            raise ValueError(f"unknown element {sym!r} in {formula!r}")
+        Z = ELEMENT_SYMBOLS.index(sym) + 1
+        atoms.append(AtomKind(Z=Z, Pers=n, shells=[], Mass=formula_mass(Z)))
+    for j in range(len(atoms) - 1, 0, -1):
+        for i in range(j):
+            if atoms[i].Z < atoms[i + 1].Z:
+                atoms[i], atoms[i + 1] = atoms[i + 1], atoms[i]
+    return atoms
+
+
+def single_pole_phonon(mat):
+    """The phonon loss function get_single_pole builds when the CDF file has
+    none (Cross_sections.f90:656-684): one oscillator at twice the Einstein
+    energy, Debye_energy and Einstein_energy (CS:690-709), width half of it,
+    strength normalised to the atoms of a formula unit."""
+    qd = (6.0 * math.pi * math.pi * (mat.At_Dens * 1e6)) ** 0.33333333
+    e_debye = G_H * mat.Vsound * qd / G_E
+    e0 = 2.0 * (e_debye * (math.pi / 6.0) ** (1.0 / 3.0))
+    n_at = 0.0
+    for a in mat.atoms:
+        n_at += a.Pers
+    mm = 0.0
+    for a in mat.atoms:
+        mm += a.Pers * a.Mass
+    omega = w_plasma(1e6 * mat.At_Dens / n_at, mm * G_MP / n_at)
+    ks, _ = sumrules([1.0], [e0], [e0 * 0.5], 1.0e-8, omega)
+    return [(e0, n_at / ks, e0 * 0.5)]
+
+
+def read_cdf(path, Layer=100.0):
+    """A full-CDF material file (*.cdf) as reading_material_parameters reads
+    it (Reading_files_and_parameters.f90:1185-1644): the name; the number of
+    elements and their (Z, share) lines, or a chemical formula; density,
+    speed of sound, Fermi energy and gap (gap 0 if only three numbers, at
+    least 0.1 eV); per element its shells (oscillator count, designator,
+    Ip >= 0.1 eV, electrons, Auger time) and oscillators; then the phonon
+    oscillators, or the single-pole phonon when the file ends there.  Shells
+    without oscillators, or with a negative designator, take BEB cross
+    sections in the reference (KOCS 2), which this library refuses.  Files
+    without shell data (single-pole CDF) need the EADL database, which the
+    reference does not ship: NotImplementedError."""
+    with open(path, encoding="latin-1") as f:
+        rd = _ListDirected(f.read())
+    line = rd.record()
+    tab = line.find("\t")
+    name = line[:tab] if tab > 0 else (line[1:] if tab == 0 else line.strip())
+    name = name.strip()
     try:
-        nph = int(next(it).split()[0])
-        for _ in range(nph):
-            e0, a, g = [float(x) for x in next(it).split()[:3]]
-            ph.append((e0, a, g))
-    except StopIteration:
-        pass
-    return MaterialModel(name=name, atoms=atoms, Dens=dens, Egap=max(egap, 0.1), Layer=Layer, Vsound=vs,
-                         E_F=ef, ph_osc=ph)
+        (n_el,) = rd.read(int)
+        atoms = []
+        for _ in range(n_el):
+            z, p_ = rd.read(int, float)
+            atoms.append(AtomKind(Z=z, Pers=p_, shells=[]))
+    except ValueError:
+        rd.back()
+        (formula,) = rd.read(str)
+        atoms = decompose_formula(formula)
+    rec = rd.record()
+    try:
+        dens, vs, ef, egap = rd.items(rec, (float, float, float, float))
+    except ValueError:
+        try:
+            dens, vs, ef = rd.items(rec, (float, float, float))
+        except ValueError:
+            raise ValueError(f"{path}: density, speed of sound and Fermi energy expected in {rec!r}") from None
+        egap = 0.0
+    egap = max(egap, 0.1)
+    try:
+        rd.items(rd.record(), (int,))
+    except (ValueError, EOFError):
+        raise NotImplementedError(f"{path}: single-pole CDF files need the EADL database") from None
+    rd.back()
+    n_vb = None
+    for atom in atoms:
+        (nsh,) = rd.read(int)
+        for _ in range(nsh):
+            ncdf, des, ip, nel, aug = rd.read(int, int, float, float, float)
+            sh = Shell(Ip=max(ip, 0.1), Nel=nel, designator=abs(des), Auger=aug)
+            if abs(des) >= 63:
+                n_vb = nel
+            if ncdf > 0:
+                sh.KOCS, sh.KOCS_SHI = (1 if des > 0 else 2), 1
+                for _ in range(ncdf):
+                    e0, a_, g = rd.read(float, float, float)
+                    sh.E0.append(e0); sh.A.append(a_); sh.Gamma.append(g)
+            else:
+                sh.KOCS = sh.KOCS_SHI = 2
+            atom.shells.append(sh)
+    mat = MaterialModel(name=name, atoms=atoms, Dens=dens, Egap=egap, Layer=Layer, Vsound=vs, E_F=ef)
+    try:
+        (nph,) = rd.read(int)
+        mat.ph_osc = [tuple(rd.read(float, float, float)) for _ in range(nph)]
+    except EOFError:
+        mat.ph_osc = single_pole_phonon(mat)
+    if n_vb is None:
+        raise ValueError(f"{path}: no valence band (designator >= 63)")
+    return mat
 
 
 def read_dos(path):
-    rows = [ln.split() for ln in open(path) if ln.strip()]
-    return np.array([float(r[0]) for r in rows]), np.array([float(r[1]) for r in rows])
+    """A *.dos file as the reference reads it (Reading_files_and_parameters.f90:2374-2380):
+    one (energy, DOS) pair per record, as many pairs as the file has records."""
+    with open(path, encoding="latin-1") as f:
+        rd = _ListDirected(f.read())
+    try:
+        rows = [rd.read(float, float) for _ in range(len(rd.recs))]
+    except EOFError:
+        raise ValueError(f"{path}: fewer (energy, DOS) pairs than records") from None
+    return np.array([r[0] for r in rows]), np.array([r[1] for r in rows])
