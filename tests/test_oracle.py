@@ -479,3 +479,62 @@ def test_dos_reader(tmp_path):
     p.write_text("-1.0 0.5\n\n0.0 0.0\n")   # a blank record: fewer pairs than records
     with pytest.raises(ValueError):
         material.read_dos(p)
+
+
+_INPUT = """Oxide         ! material name
+54         ! SHI atomic number
+20        ! [MeV] total SHI energy
+-1          ! [proton mass] nonstandard isotope if positive
+20.0         ! [fs] total time analyzed
+50.0d0 0    ! [fs] timestep (larger than the total time: clamped); linear grid
+1.0d0       ! [eV] cut-off
+5.0        ! [A] layer
+0.0       ! [K] temperature
+4   80.0     ! fixed Zeff above Z: clamped to Z
+0           ! point charge
+0   1       ! Mott elastic; target charge 1
+7   -1      ! unknown dispersion -> 1; negative mass -> 1
+0           ! plasmon limit off
+1.0         ! [me] valence-hole mass
+0           ! no radiative decay
+-1.0 10.0d0  6.18d0  ! no emission
+3           ! MC iterations
+-1          ! threads
+!DOS Other.dos   ! commented out: ignored
+CDF oxide.cdf
+"""
+
+
+def test_run_from_reference_input_files(tmp_path):
+    """INPUT_PARAMETERS.txt, a CDF and a DOS file in the reference's formats
+    give a workload the oracle runs; out-of-range inputs are corrected as
+    Read_input_file corrects them."""
+    import oracle_py
+    (tmp_path / "cdf").mkdir()
+    (tmp_path / "dos").mkdir()
+    (tmp_path / "cdf" / "oxide.cdf").write_text(_CDF_NUMERIC)
+    e, d = material.parabolic_dos_file(12.0)
+    (tmp_path / "dos" / "Oxide.dos").write_text("".join(f"{x:.6f} {y:.6f}\n" for x, y in zip(e, d)))
+    (tmp_path / "INPUT_PARAMETERS.txt").write_text(_INPUT)
+    w = configs.workload_from_input(tmp_path / "INPUT_PARAMETERS.txt", tmp_path / "cdf", tmp_path / "dos")
+    m = w.material
+    assert (w.name, w.ion_Z, w.ion_E, w.Tim, w.dt, w.dt_flag, w.NMC) == ("Oxide", 54, 20e6, 20.0, 20.0, 0, 3)
+    assert w.ion_mass == material.element_mass(54) and (w.ion_kind_zeff, w.ion_fixed_zeff) == (4, 54.0)
+    assert (m.kind_of_DR, m.El_eff_mass, m.hole_mass, m.include_photons, m.work_function) == (1, 1.0, 1.0, 0, 0.0)
+    assert (m.Layer, m.cut_off, m.kind_of_EMFP, m.CDF_elast_Zeff) == (5.0, 1.0, 0, 1)
+    assert len(w.R_edges) == 50 and w.R_edges[10] == 15.0 and w.R_edges[-1] == 1e5
+    assert m.dos is not None and abs(m.dos.int_DOS[-1] - m.N_VB_el) < 1e-9
+    assert api.n_time_points(w.Tim, w.dt, w.dt_flag) == [20.0]
+    m.atoms[1].shells[0].KOCS = m.atoms[1].shells[0].KOCS_SHI = 1   # the file's BEB shell, made CDF for the oracle
+    m.atoms[1].shells[0].E0, m.atoms[1].shells[0].A, m.atoms[1].shells[0].Gamma = [548.0], [300.0], [548.0]
+    w.dt = 1.0
+    h = m.to_c()
+    o = oracle_py.OracleTables(h, api.ion_struct(w), abi.TableCfg(build_shi=1, build_photon=0,
+                                                                  shi_E_window_lo=w.ion_E * 0.5,
+                                                                  shi_E_window_hi=w.ion_E * 1.01), nthreads=4)
+    tal = api.new_tallies(w)
+    cfg, _R = api.run_cfg(w, api.RunOptions(precision=1, seed=2))
+    st = abi.Status.fresh()
+    o.mc_run(cfg, tal, st, nthreads=2)
+    assert st.n_shi > 0 and st.n_events > st.n_shi and st.error_bits == 0
+    assert api.ion_struct(w).Kind_Zeff == 4 and api.ion_struct(w).fixed_Zeff == 54.0

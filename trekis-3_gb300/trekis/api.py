@@ -95,7 +95,9 @@ class TallySet:
 
 
 def ion_struct(w):
-    return abi.Ion(Zat=w.ion_Z, Kind_Zeff=0, Kind_ion=0, Mass=w.ion_mass, E=w.ion_E, fixed_Zeff=float(w.ion_Z))
+    fz = w.ion_fixed_zeff if 0.0 < w.ion_fixed_zeff <= w.ion_Z else float(w.ion_Z)
+    return abi.Ion(Zat=w.ion_Z, Kind_Zeff=w.ion_kind_zeff, Kind_ion=w.ion_kind, Mass=w.ion_mass, E=w.ion_E,
+                   fixed_Zeff=fz)
 
 
 @dataclass
@@ -113,7 +115,7 @@ class RunOptions:
 
 def run_cfg(w, opt, NMC=None):
     R = np.ascontiguousarray(w.R_edges, dtype=np.float64)
-    cfg = abi.RunCfg(NMC=int(NMC if NMC is not None else w.NMC), dt_flag=0, Tim=w.Tim, dt=w.dt, N_R=len(R),
+    cfg = abi.RunCfg(NMC=int(NMC if NMC is not None else w.NMC), dt_flag=w.dt_flag, Tim=w.Tim, dt=w.dt, N_R=len(R),
                      precision=opt.precision, Out_R=abi.dptr(R), seed=opt.seed,
                      iteration_offset=opt.iteration_offset, block_size=opt.block_size,
                      events_per_step=opt.events_per_step, queue_capacity=opt.queue_capacity,
@@ -191,7 +193,7 @@ class Tables:
 
 
 def new_tallies(w, spectra=False):
-    Nt = len(n_time_points(w.Tim, w.dt))
+    Nt = len(n_time_points(w.Tim, w.dt, w.dt_flag))
     m = w.material
     nd = len(m.dos.E) if m.dos is not None else 0
     return TallySet(Nt, len(w.R_edges), len(m.atoms), m.n_shells_max, N_dos=nd, spectra=spectra)

@@ -29,6 +29,31 @@ class Workload:
     R_edges: np.ndarray      # [A] outer radii of the radial bins
     seed: int = 1
     notes: dict = field(default_factory=dict)
+    dt_flag: int = 0         # time grid: 0 linear steps dt, 1 logarithmic from 0.01 fs with ratio dt
+    ion_kind_zeff: int = 0   # 0 Barkas, 1 Bohr, 2 Nikolaev-Dmitriev, 3 Schiwietz-Grande, 4 fixed
+    ion_fixed_zeff: float = 0.0   # the fixed charge of kind 4 (<= 0: the atomic number)
+    ion_kind: int = 0        # 0 point charge (1 Brandt-Kitagawa: refused by the library)
+
+
+def reference_radial_grid():
+    """The 50 outer radii [A] of the reference's cylindrical layers
+    (Radius_for_distributions, Sorting_output_data.f90:1363-1436): 1-10 by 1,
+    15, 20-100 by 10, 150, 200-1000 by 100, 1500, 2000-10000 by 1000, 15000,
+    then 20000-100000 by 10000."""
+    R = []
+    for i in range(1, 51):
+        if i < 11:
+            r = i
+        elif i < 21:
+            r = 15 if i == 11 else (i - 10) * 10
+        elif i < 31:
+            r = 150 if i == 21 else (i - 20) * 100
+        elif i < 41:
+            r = 1500 if i == 31 else (i - 30) * 1000
+        else:
+            r = 15000 if i == 41 else (i - 40) * 10000
+        R.append(float(r))
+    return np.array(R)
 
 
 def log_radial_grid(n, r_lo, r_hi):
@@ -255,3 +280,94 @@ def cfg2(n_inst=64, layer=100.0, Tim=100.0, nmc_scale=1.0, n_R=100):
                             Tim=Tim, dt=1.0, NMC=nmc, R_edges=log_radial_grid(n_R, 1.0, 1000.0), seed=1002,
                             notes={"material": mi}))
     return out
+
+
+# ---- a run described by the reference's own input files -------------------------------
+
+def read_input_parameters(path):
+    """INPUT_PARAMETERS.txt as Read_input_file reads it
+    (Reading_files_and_parameters.f90:262-404, optional flags :407-414 and
+    interpret_additional_data_INPUT), with its corrections of out-of-range
+    values: dt at most Tim on a linear grid and at least 2 on a logarithmic
+    one, a fixed ion charge in (0, Z], dispersion 1 outside 1..4, free-electron
+    mass for a negative effective mass, no emission without a positive work
+    function, barrier length and height.  Returns a dict of the values."""
+    from .material import _ListDirected, element_mass
+    with open(path, encoding="latin-1") as f:
+        rd = _ListDirected(f.read())
+    p = {}
+    (p["material"],) = rd.read(str)
+    (p["ion_Z"],) = rd.read(int)
+    (E_MeV,) = rd.read(float)
+    p["ion_E"] = E_MeV * 1.0e6
+    (M,) = rd.read(float)
+    p["ion_mass"] = M if M > 0.0 else (element_mass(abs(p["ion_Z"])) if p["ion_Z"] != 0 else 0.0)
+    (p["Tim"],) = rd.read(float)
+    p["dt"], p["dt_flag"] = rd.read(float, int)
+    if p["dt"] > p["Tim"] and p["dt_flag"] <= 0:
+        p["dt"] = p["Tim"]
+    if p["dt"] < 2 and p["dt_flag"] >= 1:
+        p["dt"] = 2.0
+    (p["cut_off"],) = rd.read(float)
+    (p["Layer"],) = rd.read(float)
+    (p["temp"],) = rd.read(float)
+    p["Kind_Zeff"], fz = rd.read(int, float)
+    p["fixed_Zeff"] = float(p["ion_Z"]) if (fz <= 0.0 or fz > p["ion_Z"]) else fz
+    (p["Kind_ion"],) = rd.read(int)
+    p["kind_of_EMFP"], p["CDF_elast_Zeff"] = rd.read(int, int)
+    p["kind_of_DR"], p["El_eff_mass"] = rd.read(int, float)
+    if p["kind_of_DR"] <= 0 or p["kind_of_DR"] > 4:
+        p["kind_of_DR"] = 1
+    if p["El_eff_mass"] < 0:
+        p["El_eff_mass"] = 1.0
+    (pl,) = rd.read(int)
+    p["plasmon_Emax"] = 1 if pl == 1 else 0
+    (p["hole_mass"],) = rd.read(float)
+    (ph,) = rd.read(int)
+    p["include_photons"] = 1 if ph == 1 else 0
+    wf, bl, bh = rd.read(float, float, float)
+    if wf <= 0.0 or bl <= 0.0 or bh <= 0.0:
+        wf = 0.0
+    p["work_function"], p["bar_length"], p["bar_height"] = wf, bl, bh
+    (p["NMC"],) = rd.read(int)
+    (p["threads"],) = rd.read(int)
+    p["cdf_file"] = p["dos_file"] = None
+    while True:   # optional flags, one or more per record
+        try:
+            rec = rd.record()
+        except EOFError:
+            break
+        words = rec.split()
+        if len(words) >= 2 and words[0].lower() in ("cdf", "dos"):
+            p[words[0].lower() + "_file"] = words[1]
+    return p
+
+
+def workload_from_input(input_path, cdf_dir, dos_dir, R_edges=None, seed=1):
+    """The run an INPUT_PARAMETERS.txt describes, with its material read from
+    ``cdf_dir`` (<material>.cdf or the file the CDF flag names) and its DOS
+    from ``dos_dir`` (<material>.dos or the DOS flag's file; none if absent),
+    on the reference's 50 radial layers unless ``R_edges`` is given.  The
+    phonon oscillators of a file are renormalised for a dynamically screened
+    nucleus as get_single_pole does."""
+    import os
+    from .material import _FORM_FACTOR, read_cdf, read_dos
+    p = read_input_parameters(input_path)
+    m = read_cdf(os.path.join(cdf_dir, p["cdf_file"] or p["material"] + ".cdf"), Layer=p["Layer"])
+    dos = os.path.join(dos_dir, p["dos_file"] or p["material"] + ".dos")
+    if os.path.exists(dos):
+        attach_dos(m, *read_dos(dos))
+    for k in ("cut_off", "temp", "hole_mass", "El_eff_mass", "kind_of_EMFP", "CDF_elast_Zeff", "kind_of_DR",
+              "plasmon_Emax", "include_photons", "work_function", "bar_length", "bar_height"):
+        setattr(m, k, p[k])
+    if m.kind_of_EMFP == 1 and m.CDF_elast_Zeff in (2, 3) and not m.ph_single_pole:
+        normalise_phonon_for_screening(m)
+    if m.kind_of_EMFP == 1 and m.CDF_elast_Zeff == 2:
+        missing = [a.Z for a in m.atoms if a.Z not in _FORM_FACTOR]
+        if missing:
+            raise ValueError(f"form-factor coefficients needed for Z = {missing}: set AtomKind.form_factor")
+    return Workload(name=p["material"], material=m, ion_Z=p["ion_Z"], ion_mass=p["ion_mass"], ion_E=p["ion_E"],
+                    Tim=p["Tim"], dt=p["dt"], NMC=p["NMC"],
+                    R_edges=reference_radial_grid() if R_edges is None else np.asarray(R_edges, dtype=float),
+                    seed=seed, notes={"threads": p["threads"]}, dt_flag=p["dt_flag"],
+                    ion_kind_zeff=p["Kind_Zeff"], ion_fixed_zeff=p["fixed_Zeff"], ion_kind=p["Kind_ion"])

@@ -148,6 +148,7 @@ class MaterialModel:
     plasmon_Emax: int = 0
     include_photons: int = 0
     ph_osc: list = field(default_factory=list)   # [(E0, A, Gamma)]
+    ph_single_pole: bool = False   # ph_osc built by get_single_pole (the file had none)
     dos: DOS = None
 
     # derived (Reading_files_and_parameters.f90:1352-1354)
@@ -554,6 +555,7 @@ def read_cdf(path, Layer=100.0):
         mat.ph_osc = [tuple(rd.read(float, float, float)) for _ in range(nph)]
     except EOFError:
         mat.ph_osc = single_pole_phonon(mat)
+        mat.ph_single_pole = True
     if n_vb is None:
         raise ValueError(f"{path}: no valence band (designator >= 63)")
     return mat
