@@ -338,3 +338,20 @@ def test_edge_cases_match_oracle(gpu_lib):
         else:
             assert np.allclose(g["Out_ne"] * np.pi * w.material.Layer * w.R_edges[0] ** 2, g["Out_tot_Ne"],
                                rtol=1e-12)
+
+
+@pytest.mark.gpu
+def test_plasmon_limit_matches_oracle(gpu_lib):
+    """plasmon_Emax: valence-band transfers may reach the plasmon energy, in
+    the tables (Cross_sections.f90:930-936) and in the sampler's clamp
+    (CS:1833-1839); an FP64 run with mobile holes equals the oracle's."""
+    w = configs.small(configs.cfg1, NMC=4, Tim=20.0)
+    w.material.plasmon_Emax = 1
+    t = api.Tables(w, lib=gpu_lib)
+    o = _oracle_on(t, w)
+    opt = api.RunOptions(precision=1, seed=21)
+    g, sg = api.mc_run(t, opt)
+    r, sr = _oracle_run(o, w, opt)
+    assert sg.n_events == sr.n_events > 0 and sg.n_el_inelastic == sr.n_el_inelastic > 0
+    assert sg.n_hole_events == sr.n_hole_events > 0 and sg.error_bits == sr.error_bits
+    _assert_tallies_equal(g, r, "plasmon_Emax")

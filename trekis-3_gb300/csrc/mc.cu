@@ -659,6 +659,10 @@ __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hol
         Mass = (C.hole_mass >= T(0)) ? C.hole_mass : tb.dosM[dos_find(tb, Ele) - 1];
         Emax = T(4) * Ele * Mass / ((Mass + T(1)) * (Mass + T(1)));
     } else Emax = (Ele + Emin) / T(2);
+    if (C.plasmon && Emin == C.Egap) {   // the plasmon energy as upper limit (CS:1833-1839)
+        if (C.Eplasmon >= Emax) Emax = C.Eplasmon;
+        if (Ele < Emax) Emax = Ele;
+    }
     T E = hole ? interp_transfer(tb.hE, tb.nH, tb.hrow_off, tb.hrow_hw, tb.hrow_L, Ele, L_need, fg, tb.hrow_mono)
                : interp_transfer(tb.elE, tb.nE, tb.row_off + (size_t)k * tb.nE, tb.row_hw, tb.row_L, Ele, L_need, fg,
                                  tb.row_mono + (size_t)k * tb.nE);

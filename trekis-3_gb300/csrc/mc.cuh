@@ -40,6 +40,8 @@ struct McConst {
     const T* dosE;      // DOS energies (the valence-hole spectrum's bins)
     int nD;
     int elast_cdf;      // 1: phonon-CDF elastic transfers from the rows, 0: Mott
+    int plasmon;        // plasmon_Emax: valence-band transfers may reach the plasmon energy
+    T Eplasmon;         // sqrt(N_VB_el At_Dens hbar^2 / (me e0) + Egap^2) [eV]
     // derived per species for the FP32 Mott transfer (finish_const): with
     // M = M_a c^2 / e [eV], c1 = 1.7e-5 Z^(2/3), c2 = 3.76 alpha^2 Z^2,
     // iM = 1/M, iM2 = 1/M^2, wM = M Pers / Psum
@@ -205,6 +207,11 @@ inline void fill_const(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt
         C.Auger[k] = (T)at.Auger[s]; C.Radiat[k] = (T)at.Radiat[s];
     }
     C.Psum = (T)Psum; C.Mtarget = (T)(kMp * Mt / Psum); C.Egap = (T)m.atoms[0].Ip[m.atoms[0].N_shl - 1];
+    {
+        const double Eg = m.atoms[0].Ip[m.atoms[0].N_shl - 1];
+        C.plasmon = m.plasmon_Emax ? 1 : 0;
+        C.Eplasmon = (T)std::sqrt(m.N_VB_el * m.At_Dens * 1e6 * kH * kH / (kMe * kE0) + Eg * Eg);
+    }
     C.cut_off = (T)m.cut_off; C.hole_mass = (T)m.hole_mass; C.Layer = m.Layer;
     C.ion_Z = t->ion.Zat; C.ion_kind_zeff = t->ion.Kind_Zeff; C.ion_mass_p = t->ion.Mass; C.MSHI = kMp * t->ion.Mass;
     C.ion_E0 = t->ion.E; C.ion_fixed_zeff = t->ion.fixed_Zeff; C.Zt = zs / Psum;
