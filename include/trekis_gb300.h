@@ -120,7 +120,8 @@ typedef struct {
     int32_t CDF_elast_Zeff;   /* target charge in the phonon CS: 0 Barkas-like, 1 one,
                                  2 nucleus screened by the valence CDF and core form
                                  factors, 3 screened by the shells' CDFs */
-    int32_t kind_of_DR;       /* 1 free electron, 2 plasmon pole, 3 Ritchie   */
+    int32_t kind_of_DR;       /* 1 free electron, 2 plasmon pole, 3 Ritchie
+                                 (4, the delta CDF: TREKIS_EUNSUPPORTED)     */
     int32_t plasmon_Emax;     /* 1: plasmon energy as upper limit            */
     int32_t include_photons;  /* 1: radiative decay and photon transport     */
 } trekis_material;

@@ -99,6 +99,17 @@ def test_invalid_material_refused_before_any_device_work(lib, field, value):
     assert rc == -1 and st.code == -1 and not out.value
 
 
+def test_delta_cdf_dispersion_refused(lib):
+    from trekis import api, configs
+    l = abi.load()
+    w = configs.small(configs.cfg0)
+    w.material.kind_of_DR = 4
+    out, st = C.c_void_p(), abi.Status.fresh()
+    rc = l.trekis_tables_build(w.material.to_c().ref(), C.byref(api.ion_struct(w)), C.byref(abi.TableCfg(build_shi=1)),
+                               C.byref(out), C.byref(st))
+    assert rc == -7 and not out.value
+
+
 def _fortran_types():
     """The bind(C) derived types of INTEGRATION.md: name -> [(kind, count)]."""
     txt = (ROOT / "INTEGRATION.md").read_text()

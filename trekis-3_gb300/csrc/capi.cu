@@ -694,6 +694,7 @@ static int validate_material(const trekis_material* m) {
     }
     if (m->N_ph_osc < 0 || m->N_ph_osc > TREKIS_MAX_PH_OSC) return TREKIS_EINVAL;
     if (!(m->Layer > 0.0) || !(m->At_Dens > 0.0) || !(m->Dens > 0.0)) return TREKIS_EINVAL;
+    if (m->kind_of_DR == 4) return TREKIS_EUNSUPPORTED;   // delta-CDF dispersion (define_alpha): not built
     if (m->N_dos < 0 || (m->N_dos > 0 && (!m->dos_E || !m->dos_DOS || !m->dos_int || !m->dos_k || !m->dos_Eff_m)))
         return TREKIS_EINVAL;
     // mobile valence holes and DOS-derived masses read the DOS arrays
