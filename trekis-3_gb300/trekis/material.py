@@ -69,17 +69,112 @@ def element_mass(Z):
 # coefficients a1..a5 of PENELOPE's analytical atomic form factor
 # F(x, Z) = Z (1 + a1 x^2 + a2 x^3 + a3 x^4) / (1 + a4 x^2 + a5 x^4)^2
 # (Baro et al., Radiat. Phys. Chem. 44 (1994) 531; Salvat et al., PENELOPE
-# (2001) Eq. 2.7), as the reference's Atomic_form_factors.dat lists them per Z,
-# for the elements of the synthetic targets.  The physical data must be the
-# same numbers for a screened elastic table to equal a Fortran run's.
-_FORM_FACTOR = {
-    3: (43.1, 94.875, 1057.9, 47.367, 55.674), 6: (12.211, -19.572, 78.788, 13.979, 4.8936),
-    7: (9.3229, -12.382, 38.293, 10.766, 2.5506), 8: (3.2455, -3.6827, 12.564, 6.5252, 1.2236),
-    9: (2.4197, -2.4542, 6.9091, 5.1631, 0.74698), 11: (30.926, 134.01, 0.0, 27.145, 4.7809),
-    12: (15.315, 79.717, 0.0, 18.724, 4.6315), 13: (7.7061, 62.164, 1.6759e-9, 14.782, 4.3677),
-    14: (3.9493, 40.3, 13.026, 11.608, 4.9269), 15: (2.2042, 31.682, 3.0569, 9.775, 2.6033),
-    16: (19.453, -13.639, 155.21, 16.17, 9.6229), 20: (57.37, 122.05, 475.08, 41.381, 8.6975),
-}
+# (2001) Eq. 2.7) for Z = 1..99, as the reference's Atomic_form_factors.dat
+# lists them (one row per Z).  The physical data must be the same numbers for
+# a screened elastic table to equal a Fortran run's.
+_FORM_FACTOR_TABLE = """
+    1 0 0 0 11.055 0
+    2 3.9265 0.13426 2.2648 6.3519 4.9828
+    3 43.1 94.875 1057.9 47.367 55.674
+    4 52.757 -108.96 861.77 39.402 30.902
+    5 25.021 -45.494 244.22 22.896 11.496
+    6 12.211 -19.572 78.788 13.979 4.8936
+    7 9.3229 -12.382 38.293 10.766 2.5506
+    8 3.2455 -3.6827 12.564 6.5252 1.2236
+    9 2.4197 -2.4542 6.9091 5.1631 0.74698
+    10 1.5985 -1.4453 3.7926 4.0524 0.47042
+    11 30.926 134.01 0 27.145 4.7809
+    12 15.315 79.717 0 18.724 4.6315
+    13 7.7061 62.164 1.6759E-9 14.782 4.3677
+    14 3.9493 40.3 13.026 11.608 4.9269
+    15 2.2042 31.682 3.0569 9.775 2.6033
+    16 19.453 -13.639 155.21 16.17 9.6229
+    17 19.354 -15.95 128.15 15.249 7.2592
+    18 8.0374 -5.1523 47.378 9.1916 4.1634
+    19 83.779 183.51 928.02 54.499 13.999
+    20 57.37 122.05 475.08 41.381 8.6975
+    21 52.31 100.07 366.12 37.395 6.963
+    22 47.514 85.632 275.82 33.815 5.4681
+    23 43.785 79.145 210.08 31.135 4.2653
+    24 42.048 63.675 159.03 28.273 3.2848
+    25 36.972 62.954 123.22 26.14 2.7354
+    26 33.849 56.601 92.898 23.948 2.1617
+    27 31.609 54.171 71.345 22.406 1.703
+    28 28.763 48.752 51.651 20.484 1.2826
+    29 27.217 38.062 38.474 18.453 0.9708
+    30 24.263 39.933 27.41 17.386 0.72227
+    31 22.403 48.343 19.126 17.301 0.50874
+    32 18.606 42.137 10.889 15.388 0.31402
+    33 15.143 34.617 5.3479 13.411 0.1636
+    34 14.226 29.43 8.2223 12.668 0.32918
+    35 11.792 24.01 5.0837 11.133 0.2357
+    36 9.7574 19.744 2.8905 9.8081 0.15868
+    37 12.796 40.009 2.7457 13.031 0.15146
+    38 12.854 51.614 0.67082 14.143 0.097662
+    39 12.368 50.456 0 13.815 0.073151
+    40 10.208 39.088 0 12.077 0.064206
+    41 8.2823 26.824 0 10.033 0.048945
+    42 7.4677 22.953 0 9.2549 0.043189
+    43 7.6028 24.773 0 9.5338 0.044368
+    44 6.109 16.893 0 7.9076 0.033976
+    45 5.5346 14.548 0 7.3263 0.030466
+    46 4.234 9.7226 0 5.9996 0.024477
+    47 4.0444 10.192 0 6.0087 0.037202
+    48 4.2905 11.153 0 6.266 0.037093
+    49 4.795 13.188 0 6.7914 0.038161
+    50 5.1112 14.733 0 7.1501 0.038576
+    51 5.2407 15.644 0 7.3367 0.038403
+    52 5.2153 15.939 0 7.3729 0.037806
+    53 5.1639 15.923 0 7.3508 0.034958
+    54 4.8814 15.254 0 7.1465 0.036029
+    55 5.8054 20.748 0 8.2731 0.043087
+    56 6.6724 26.901 0 9.3745 0.047069
+    57 6.5104 27.032 0 9.3508 0.046452
+    58 6.3364 24.938 0 8.9897 0.042486
+    59 6.2889 21.528 0.17264 8.4566 0.041517
+    60 6.3028 20.362 0.27322 8.269 0.041691
+    61 6.3853 19.474 0.39444 8.1398 0.042813
+    62 6.3475 18.238 0.45648 7.9183 0.042294
+    63 6.5779 17.898 0.62286 7.9123 0.045287
+    64 6.8486 19.174 0.72468 8.1677 0.048462
+    65 7.0993 19.023 0.84296 8.1871 0.049726
+    66 7.6122 18.194 1.1698 8.1766 0.055097
+    67 7.9681 18.504 1.2994 8.2881 0.056568
+    68 8.3481 18.955 1.4295 8.4227 0.058069
+    69 6.3875 14.276 0 7.0273 0.01227
+    70 8.0042 17.558 0.8157 8.0002 0.038006
+    71 8.082 18.651 0.69349 8.144 0.035048
+    72 7.694 17.984 0.49536 7.9104 0.03005
+    73 7.1927 16.793 0.31211 7.5685 0.025069
+    74 6.6751 15.469 0.15931 7.197 0.020485
+    75 6.1623 14.143 0.029512 6.8184 0.016151
+    76 5.8335 13.149 0 6.5469 0.014631
+    77 5.5599 12.255 0 6.3056 0.014034
+    78 4.6551 9.2352 0 5.4844 0.011978
+    79 4.4327 8.6067 0 5.2832 0.011522
+    80 4.7601 9.746 0 5.5889 0.012375
+    81 5.2872 11.749 0 6.0919 0.013805
+    82 5.6084 13.281 0 6.434 0.014954
+    83 5.768 14.326 0 6.6426 0.015832
+    84 5.8041 14.92 0 6.7428 0.016467
+    85 5.7566 15.157 0 6.7636 0.016896
+    86 5.6541 15.131 0 6.7281 0.017166
+    87 6.3932 19.489 0 7.5729 0.019954
+    88 6.9313 23.649 0 8.2808 0.022497
+    89 7.0027 24.686 0 8.44 0.021942
+    90 6.8796 24.76 0 8.422 0.021965
+    91 6.4739 21.519 0 7.8662 0.020005
+    92 6.2405 20.099 0 7.5993 0.018927
+    93 6.0081 18.746 0 7.3353 0.018167
+    94 5.5708 15.943 0 6.7829 0.016314
+    95 5.368 14.88 0 6.552 0.015522
+    96 5.866 16.345 0 6.9181 0.013141
+    97 5.6375 15.283 0 6.6794 0.012578
+    98 5.1719 13.061 0 6.1735 0.012238
+    99 4.8989 11.553 0 5.8332 0.010427
+"""
+_FORM_FACTOR = {int(r.split()[0]): tuple(float(x) for x in r.split()[1:])
+                for r in _FORM_FACTOR_TABLE.strip().splitlines()}
 
 
 def form_factor_coefficients(Z):
