@@ -314,44 +314,3 @@ def test_output_files_of_a_gpu_run(small1, tmp_path):
     want = g.view("Out_nh")[:, :, vb[0], vb[1]].T / NMC * 1e24
     assert np.allclose(np.array([[float(x) for x in r[1:]] for r in rows]), want, rtol=1e-15, atol=0.0)
 
-
-@pytest.mark.gpu
-def test_edge_cases_match_oracle(gpu_lib):
-    """No iterations (every tally stays zero), a layer thinner than any SHI
-    flight (the ion may leave without a collision) and a single radial bin
-    that collects everything: FP64 runs equal the oracle's."""
-    w = configs.small(configs.cfg0, NMC=0)
-    t = api.Tables(w, lib=gpu_lib)
-    g, sg = api.mc_run(t, api.RunOptions(precision=1, seed=1))
-    assert sg.n_events == 0 and all(np.all(v == 0) for v in g.a.values())
-    for kw in (dict(NMC=3, layer=1e-6), dict(NMC=2, n_R=1)):
-        w = configs.small(configs.cfg0, **kw)
-        t = api.Tables(w, lib=gpu_lib)
-        o = _oracle_on(t, w)
-        opt = api.RunOptions(precision=1, seed=1)
-        g, sg = api.mc_run(t, opt)
-        r, sr = _oracle_run(o, w, opt)
-        assert sg.n_events == sr.n_events and sg.n_shi == sr.n_shi
-        _assert_tallies_equal(g, r, str(kw))
-        if "layer" in kw:
-            assert sg.n_shi <= kw["NMC"]
-        else:
-            assert np.allclose(g["Out_ne"] * np.pi * w.material.Layer * w.R_edges[0] ** 2, g["Out_tot_Ne"],
-                               rtol=1e-12)
-
-
-@pytest.mark.gpu
-def test_plasmon_limit_matches_oracle(gpu_lib):
-    """plasmon_Emax: valence-band transfers may reach the plasmon energy, in
-    the tables (Cross_sections.f90:930-936) and in the sampler's clamp
-    (CS:1833-1839); an FP64 run with mobile holes equals the oracle's."""
-    w = configs.small(configs.cfg1, NMC=4, Tim=20.0)
-    w.material.plasmon_Emax = 1
-    t = api.Tables(w, lib=gpu_lib)
-    o = _oracle_on(t, w)
-    opt = api.RunOptions(precision=1, seed=21)
-    g, sg = api.mc_run(t, opt)
-    r, sr = _oracle_run(o, w, opt)
-    assert sg.n_events == sr.n_events > 0 and sg.n_el_inelastic == sr.n_el_inelastic > 0
-    assert sg.n_hole_events == sr.n_hole_events > 0 and sg.error_bits == sr.error_bits
-    _assert_tallies_equal(g, r, "plasmon_Emax")
