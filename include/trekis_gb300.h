@@ -340,8 +340,16 @@ int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
  *     tallies of this (Nt, N_R, shells) shape; cfg->queue_capacity, when set,
  *     must not exceed it.  A tally shape that leaves too little room, or a
  *     requested capacity beyond it, returns TREKIS_EINVAL with the reason in
- *     trekis_last_error(); a single iteration that overflows the queues
- *     returns TREKIS_EOVERFLOW, as the allocating entry point does.
+ *     trekis_last_error() before any device work; a single iteration that
+ *     overflows the queues returns TREKIS_EOVERFLOW, as the allocating entry
+ *     point does.
+ *   - the side queues scale with the capacity: deep holes and SHI collision
+ *     records get half of it and photons an eighth, without the 65536-slot
+ *     floors of the allocating entry point, so a small caller-set capacity
+ *     can overflow (and retry with smaller batches, or return
+ *     TREKIS_EOVERFLOW) where the allocating entry point would not.
+ *   - sampler must be 0: the learned proposal is not run here
+ *     (TREKIS_EUNSUPPORTED otherwise).
  *   - status->device_ms and status->step_ms stay 0 (no timing events).
  *   - the spectra (Out_Ee_vs_E, Out_Eh_vs_E, Out_theta, Out_theta_h) must be
  *     NULL: their per-iteration histograms do not fit the fixed scratch
@@ -351,9 +359,12 @@ int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
  *     calls.
  * The first call on each device looks up the scratch address with that
  * device current, which may load this module; make that first call before
- * any stream capture begins on the device.  There is one scratch per device
- * and process: calls that overlap in time on the same device (from several
- * host threads) share it and race, so such callers must serialise them. */
+ * any stream capture begins on the device.  The address is kept for the
+ * life of the process: after cudaDeviceReset (or anything else that replaces
+ * the device's primary context) it is stale, and this entry point must not be
+ * called again in that process.  There is one scratch per device and
+ * process: calls that overlap in time on the same device (from several host
+ * threads) share it and race, so such callers must serialise them. */
 #define TREKIS_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int32_t trekis_mc_run_device_noalloc(const trekis_tables* t, const trekis_material* mat,
                                      const trekis_ion* ion, const trekis_run_cfg* cfg,

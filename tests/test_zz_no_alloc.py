@@ -20,18 +20,19 @@ from trekis import abi, api, configs
 RTOL = 1e-12
 
 
-def _device_tallies(torch, w):
-    tal = api.new_tallies(w)
+def _device_tallies(torch, w, spectra=False):
+    tal = api.new_tallies(w, spectra=spectra)
     dev = {k: torch.zeros(v.size, dtype=torch.float64, device="cuda") for k, v in tal.a.items()}
     ptr = lambda x: C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double))
-    ct = abi.Tallies(Nt=tal.Nt, N_R=tal.NR, Nat=tal.Nat, Nshl=tal.Nshl, **{k: ptr(v) for k, v in dev.items()})
+    ct = abi.Tallies(Nt=tal.Nt, N_R=tal.NR, Nat=tal.Nat, Nshl=tal.Nshl, N_dos=tal.N_dos,
+                     **{k: ptr(v) for k, v in dev.items()})
     return dev, ct
 
 
-def _run(lib, t, w, opt, noalloc):
+def _run(lib, t, w, opt, noalloc, NMC=None):
     import torch
     dev, ct = _device_tallies(torch, w)
-    cfg, _R = api.run_cfg(w, opt)
+    cfg, _R = api.run_cfg(w, opt, NMC)
     st = abi.Status.fresh()
     if noalloc:
         rc = lib.trekis_mc_run_device_noalloc(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(ct),
@@ -88,4 +89,76 @@ def test_noalloc_rejects_capacity_beyond_scratch(gpu_lib):
                                               C.byref(st), None)
     assert rc == -1 and b"exceeds" in gpu_lib.trekis_last_error()
     assert float(sum(v.abs().sum().item() for v in dev.values())) == 0.0
+    t.close()
+
+
+def _cfg1_small(**kw):
+    w = configs.small(configs.cfg1, NMC=6, Tim=30.0, **kw)
+    for atom in w.material.atoms:
+        for sh in atom.shells:
+            if sh.designator < 63:
+                sh.Radiat = sh.Auger * 2.0
+    return w
+
+
+@pytest.mark.gpu
+def test_noalloc_small_capacity_batches_and_retries(gpu_lib):
+    """A caller-set capacity of 2048 particles cannot hold a 12-iteration batch
+    (about 1,200 particles and 165 ion collisions per iteration): the batch
+    overflows and is retried as several smaller ones, and the sums still
+    match the allocating entry point's."""
+    pytest.importorskip("torch")
+    w = _cfg1_small()
+    t = api.Tables(w, lib=gpu_lib)
+    ref, sr = _run(gpu_lib, t, w, api.RunOptions(seed=29), noalloc=False, NMC=12)
+    got, sg = _run(gpu_lib, t, w, api.RunOptions(seed=29, queue_capacity=2048, iterations_per_batch=12),
+                   noalloc=True, NMC=12)
+    assert sg.n_events == sr.n_events > 0 and sg.n_particles == sr.n_particles
+    assert sg.batch_iterations < 12     # the first batch overflowed and was retried smaller
+    _close(got, ref, "small capacity")
+    t.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_logarithmic_time_grid(gpu_lib):
+    """dt_flag = 1 (time points 0.01 dt^k fs): the no-alloc entry point walks
+    the same time grid as the allocating one."""
+    pytest.importorskip("torch")
+    w = _cfg1_small()
+    w.dt_flag, w.dt = 1, 1.25
+    t = api.Tables(w, lib=gpu_lib)
+    opt = api.RunOptions(seed=31)
+    ref, sr = _run(gpu_lib, t, w, opt, noalloc=False)
+    got, sg = _run(gpu_lib, t, w, opt, noalloc=True)
+    assert sg.n_events == sr.n_events > 0
+    assert api.new_tallies(w).Nt == gpu_lib.trekis_time_points(w.Tim, w.dt, 1)
+    _close(got, ref, "log grid")
+    t.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_refusals(gpu_lib):
+    """Spectra, the learned proposal and a tally shape the scratch cannot hold
+    are refused before any device work, leaving the outputs untouched."""
+    pytest.importorskip("torch")
+    import torch
+    w = configs.small(configs.cfg0, NMC=1)
+    t = api.Tables(w, lib=gpu_lib)
+
+    def call(w_, opt, spectra=False):
+        dev, ct = _device_tallies(torch, w_, spectra=spectra)
+        cfg, _R = api.run_cfg(w_, opt)
+        st = abi.Status.fresh()
+        rc = gpu_lib.trekis_mc_run_device_noalloc(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(ct),
+                                                  C.byref(st), None)
+        assert float(sum(v.abs().sum().item() for v in dev.values())) == 0.0
+        return rc, gpu_lib.trekis_last_error()
+
+    rc, msg = call(w, api.RunOptions(), spectra=True)
+    assert rc == -7 and b"spectra" in msg
+    rc, msg = call(w, api.RunOptions(sampler=1))
+    assert rc == -7 and b"sampler" in msg
+    big = configs.small(configs.cfg0, NMC=1, Tim=20000.0)     # 20000 time rows x 100 radii x 4 shells
+    rc, msg = call(big, api.RunOptions())
+    assert rc == -1 and b"cannot hold" in msg
     t.close()

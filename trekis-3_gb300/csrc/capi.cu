@@ -275,23 +275,8 @@ static int upload_shi(trekis_tables* t, DevShi<T>& s) {
 
 // tallied grid times: min(t_i, Tim) while <= Tim - 1e-6 (Monte_Carlo.f90:572-580, 2118-2149)
 static std::vector<double> tallied_times(double Tim, double dt, int flag) {
-    std::vector<double> raw;
-    if (flag <= 0) {
-        int n = (int)std::ceil(Tim / dt) + 1;
-        raw.assign(n, 0.0); raw[0] = dt;
-        for (int i = 0; i < n - 2; ++i) raw[i + 1] = raw[i] + dt;
-        raw[n - 1] = Tim + dt;
-    } else {
-        int i = 0; double t = 0.01;
-        while (t <= Tim) { ++i; t *= dt; }
-        raw.assign(i + 1, 0.0); raw[0] = 0.01;
-        for (int k = 0; k < i - 1; ++k) raw[k + 1] = raw[k] * dt;
-        raw[i] = Tim + dt;
-    }
     std::vector<double> out;
-    double tim = 0.0;
-    size_t i = 0;
-    while (tim <= Tim - 1e-6 && i < raw.size()) { tim = std::min(raw[i], Tim); out.push_back(tim); ++i; }
+    walk_time_grid(Tim, dt, flag, [&](int, double t) { out.push_back(t); });
     return out;
 }
 

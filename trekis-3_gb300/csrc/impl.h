@@ -168,6 +168,28 @@ inline bool time_grid_ok(double Tim, double dt, int flag) {
     if (!(dt > 1.0)) return false;
     return Tim < 0.01 || std::log(Tim / 0.01) / std::log(dt) + 3.0 <= kMaxTimePoints;
 }
+// The tallied time points of a run, one at a time (set_time_grid,
+// Monte_Carlo.f90:2118-2149, and the loop condition of Monte_Carlo_modelling,
+// :572-580): the raw grid dt, 2dt, ..., Tim+dt (logarithmic: 0.01, 0.01 dt,
+// ..., Tim+dt) clipped at Tim, taken while the previous point lies below
+// Tim - 1e-6.  f(i, t) receives each point; returns how many there are.  The
+// caller checks the grid with time_grid_ok first.
+template <class F>
+inline int walk_time_grid(double Tim, double dt, int flag, F&& f) {
+    int n;
+    if (flag <= 0) n = (int)std::ceil(Tim / dt) + 1;
+    else { n = 0; for (double t = 0.01; t <= Tim; t *= dt) ++n; n += 1; }
+    double raw = flag <= 0 ? dt : 0.01, tim = 0.0;
+    int i = 0;
+    while (tim <= Tim - 1e-6 && i < n) {
+        const double r = (i == n - 1) ? Tim + dt : raw;
+        tim = r < Tim ? r : Tim;
+        f(i, tim);
+        ++i;
+        raw = flag <= 0 ? raw + dt : raw * dt;
+    }
+    return i;
+}
 void set_error(const std::string& s);
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st);
 std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax);

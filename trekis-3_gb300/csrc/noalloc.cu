@@ -63,27 +63,6 @@ bool sm103_current() {
     return ma == 10 && mi == 3;
 }
 
-// The tallied time points, one at a time: the raw grid dt, 2dt, ..., Tim+dt
-// (or 0.01, 0.01 dt, ..., Tim+dt on the logarithmic grid) clipped at Tim,
-// taken while the previous point lies below Tim - 1e-6 (the time grid of
-// Monte_Carlo.f90:120-160).  f(i, t) receives each point; returns the count.
-template <class F>
-int walk_times(double Tim, double dt, int flag, F&& f) {
-    int n;
-    if (flag <= 0) n = (int)std::ceil(Tim / dt) + 1;
-    else { n = 0; for (double t = 0.01; t <= Tim; t *= dt) ++n; n += 1; }
-    double raw = flag <= 0 ? dt : 0.01, tim = 0.0;
-    int i = 0;
-    while (tim <= Tim - 1e-6 && i < n) {
-        const double r = (i == n - 1) ? Tim + dt : raw;
-        tim = std::min(r, Tim);
-        f(i, tim);
-        ++i;
-        raw = flag <= 0 ? raw + dt : raw * dt;
-    }
-    return i;
-}
-
 // Bump allocator over the scratch; with base == nullptr it only measures.
 struct Carve {
     unsigned char* base;
@@ -217,24 +196,36 @@ int upload_chunked(U* dst, int n, G&& gen, cudaStream_t s) {
     return TREKIS_OK;
 }
 
+Shape shape_of(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const trekis_tallies& o) {
+    return Shape{Nt, cfg.N_R, t->nsh, o.Nat, o.Nshl, t->mat.hole_mass < 1e3, t->mat.include_photons != 0};
+}
+
+// The queue capacity of a call, or 0 with the reason set: host arithmetic
+// only, so a call the scratch cannot hold is refused before any device work.
 template <class T>
-int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const trekis_tallies& o,
-                trekis_status* st, cudaStream_t strm) {
-    const trekis_material& m = t->mat;
-    const Shape shp{Nt, cfg.N_R, t->nsh, o.Nat, o.Nshl, m.hole_mass < 1e3, m.include_photons != 0};
+int64_t capacity_of(const Shape& shp, const trekis_run_cfg& cfg) {
     const int64_t cap_max = max_capacity<T>(shp);
     if (cap_max == 0) {
         set_error("the no-alloc scratch (" + std::to_string(kScratchBytes >> 20) + " MiB) cannot hold the tallies of " +
-                  std::to_string(Nt) + " times x " + std::to_string(cfg.N_R) + " radii x " + std::to_string(t->nsh) +
-                  " shells plus a queue of " + std::to_string(kMinCap) + " particles");
-        return TREKIS_EINVAL;
+                  std::to_string(shp.Nt) + " times x " + std::to_string(shp.NR) + " radii x " +
+                  std::to_string(shp.nsh) + " shells plus a queue of " + std::to_string(kMinCap) + " particles");
+        return 0;
     }
     if (cfg.queue_capacity > cap_max) {
         set_error("queue_capacity " + std::to_string(cfg.queue_capacity) + " exceeds the " +
                   std::to_string(cap_max) + " particles the no-alloc scratch holds for this tally shape");
-        return TREKIS_EINVAL;
+        return 0;
     }
-    const int64_t cap = cfg.queue_capacity > 0 ? cfg.queue_capacity : cap_max;
+    return cfg.queue_capacity > 0 ? cfg.queue_capacity : cap_max;
+}
+
+template <class T>
+int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const trekis_tallies& o,
+                trekis_status* st, cudaStream_t strm) {
+    const trekis_material& m = t->mat;
+    const Shape shp = shape_of(t, cfg, Nt, o);
+    const int64_t cap = capacity_of<T>(shp, cfg);
+    if (cap == 0) return TREKIS_EINVAL;
     unsigned char* base = nullptr;
     int rc = scratch_of_current_device(&base);
     if (rc) return rc;
@@ -256,7 +247,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
                 ce = cudaMemcpyAsync(L.tg + at, buf, sizeof(T) * nbuf, cudaMemcpyHostToDevice, strm);
             at += nbuf; nbuf = 0;
         };
-        walk_times(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int, double x) { buf[nbuf++] = (T)x; if (nbuf == 256) flush(); });
+        walk_time_grid(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int, double x) { buf[nbuf++] = (T)x; if (nbuf == 256) flush(); });
         flush();
         NA_CK(ce);
     }
@@ -285,7 +276,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     C.elast_cdf = (t->mat.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
     {
         T first = T(0), last = T(0);
-        walk_times(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int i, double x) { if (i == 0) first = (T)x; last = (T)x; });
+        walk_time_grid(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int i, double x) { if (i == 0) first = (T)x; last = (T)x; });
         set_grid_hint_sizes<T>(C, first, last, (T)cfg.Out_R[0], (T)cfg.Out_R[NR - 1]);
     }
     C.tg_hint = L.th; C.rg_hint = C.rg_nb ? L.rh : nullptr;
@@ -364,11 +355,13 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     // holes: compact shells -> caller slices; per-call energies -> caller totals
     const size_t blk = (size_t)Nt * NR, nn = blk * nsh, n3 = (size_t)Nt * o.Nat * o.Nshl;
     const unsigned g = (unsigned)((nn + 255) / 256);
-    if (o.Out_nh) k_na_slices<<<g, 256, 0, strm>>>(o.Out_nh, L.hn, blk, nsh, L.hmap);
-    if (o.Out_Eh) k_na_slices<<<g, 256, 0, strm>>>(o.Out_Eh, L.hE, blk, nsh, L.hmap);
-    if (o.Out_Ehkin) k_na_slices<<<g, 256, 0, strm>>>(o.Out_Ehkin, L.hK, blk, nsh, L.hmap);
+    if (o.Out_nh && nn) k_na_slices<<<g, 256, 0, strm>>>(o.Out_nh, L.hn, blk, nsh, L.hmap);
+    if (o.Out_Eh && nn) k_na_slices<<<g, 256, 0, strm>>>(o.Out_Eh, L.hE, blk, nsh, L.hmap);
+    if (o.Out_Ehkin && nn) k_na_slices<<<g, 256, 0, strm>>>(o.Out_Ehkin, L.hK, blk, nsh, L.hmap);
     // the per-call hole energies go through the call buffer (slices of atom x shell)
-    k_na_slices<<<(unsigned)((Nt * nsh + 255) / 256), 256, 0, strm>>>(Eh_call, L.htE, (size_t)Nt, nsh, L.hmap);
+    if (nsh > 0)
+        k_na_slices<<<(unsigned)(((size_t)Nt * nsh + 255) / 256), 256, 0, strm>>>(Eh_call, L.htE, (size_t)Nt, nsh,
+                                                                                   L.hmap);
     const unsigned gt = (unsigned)((Nt + 127) / 128);
     if (o.Out_tot_E) k_na_total<<<gt, 128, 0, strm>>>(Nt, o.Nat * o.Nshl, m.include_photons, Ee_call, Eh_call, Ep_call,
                                                       Eat_call, o.Out_tot_E);
@@ -414,7 +407,7 @@ int check_args(const trekis_tables* t, const trekis_material* mat, const trekis_
     }
     for (int j = 1; j < cfg->N_R; ++j)
         if (!(cfg->Out_R[j] > cfg->Out_R[j - 1])) { set_error("radii must increase"); return TREKIS_EINVAL; }
-    *Nt = walk_times(cfg->Tim, cfg->dt, cfg->dt_flag, [](int, double) {});
+    *Nt = walk_time_grid(cfg->Tim, cfg->dt, cfg->dt_flag, [](int, double) {});
     if (o->Nt != *Nt || o->N_R != cfg->N_R || o->Nat != t->mat.N_atoms) {
         set_error("tally dimensions do not match"); return TREKIS_EINVAL;
     }
@@ -447,6 +440,11 @@ extern "C" int32_t trekis_mc_run_device_noalloc(const trekis_tables* t, const tr
     (void)ion;
     int Nt = 0;
     int rc = check_args(t, mat, cfg, o, &Nt);
+    if (!rc) {   // the scratch must hold this tally shape and queue capacity
+        const Shape shp = shape_of(t, *cfg, Nt, *o);
+        if ((cfg->precision == 1 ? capacity_of<double>(shp, *cfg) : capacity_of<float>(shp, *cfg)) == 0)
+            rc = TREKIS_EINVAL;
+    }
     if (!rc && !sm103_current()) { set_error("no usable sm_103a device"); rc = TREKIS_ENODEVICE; }
     if (!rc) {
         cudaStream_t s = (cudaStream_t)stream;
