@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TREKIS_ABI_VERSION 4
+#define TREKIS_ABI_VERSION 5
 
 #define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
 #define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
@@ -143,6 +143,17 @@ typedef struct {
     int32_t build_photon;       /* 1: photon absorption tables                */
     double  shi_E_window_lo;    /* [eV] SHI grid rows below this are skipped (<=0: all) */
     double  shi_E_window_hi;    /* [eV] SHI grid rows above this are skipped (<=0: all) */
+    /* 1: SHI energy-transfer rows at every SHI grid energy of the window, and
+     * the track loop draws each ion collision's transfer at the ion's current
+     * energy (the rows of the two grid energies around it, combined as
+     * interpolate_transferred_energy combines electron rows,
+     * Cross_sections.f90:1968-2045).  0: one row per shell at the ion's
+     * initial energy, which the track loop uses throughout, as the reference
+     * does (Universal_MC_for_SHI_MAIN.f90:231-238).  An extension with no
+     * counterpart in the reference; it matters when the ion loses a sizeable
+     * part of its energy inside the layer. */
+    int32_t shi_rows_by_energy;
+    int32_t pad_;
 } trekis_table_cfg;
 
 /* Opaque table set (device-resident FP64 + FP32 copies, host FP64 mirror). */
@@ -237,6 +248,9 @@ typedef struct {
     int32_t  pad_;
     uint64_t h2d_bytes;        /* host-to-device bytes copied by the call       */
     uint64_t d2h_bytes;        /* device-to-host bytes copied by the call       */
+    uint64_t n_fp64_redraws;   /* FP32 runs: transfer draws (ionising or phonon-CDF
+                                  elastic) whose bracket was too ill-conditioned for
+                                  FP32 and that were redone in FP64 on the FP64 rows */
 } trekis_status;
 
 /* ---- entry points ------------------------------------------------------ */
@@ -265,6 +279,23 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion,
 
 void trekis_tables_free(trekis_tables* t);
 
+/* Cost of the FP64 table build of a handle (CUDA events on the build's
+ * stream).  The omega-q integrals are the FP64 work: every point of the
+ * hbar-omega grids of every (shell, energy) job is one thread that runs the
+ * q Simpson loop of Diff_cross_section (Cross_sections.f90:2217-2282) or its
+ * SHI / phonon counterparts; each q step evaluates the loss function twice,
+ * one oscillator term per oscillator of the shell. */
+typedef struct {
+    double   build_ms;      /* whole build on the device: job sizing, abscissae, integrals, sums */
+    double   integral_ms;   /* the integral kernels alone (k_diff, k_diff_phonon)                */
+    uint64_t jobs;          /* (shell, energy) integrals                                         */
+    uint64_t points;        /* hbar-omega abscissae, each one q integral                        */
+    uint64_t q_steps;       /* Simpson steps over q, summed over the points                     */
+    uint64_t osc_terms;     /* oscillator terms of the loss function evaluated (2 per q step and
+                               oscillator; the screened phonon option adds its own terms)        */
+} trekis_build_stats;
+int32_t trekis_tables_stats(const trekis_tables* t, trekis_build_stats* s);
+
 /* Table kinds for the export functions. */
 #define TREKIS_TAB_EL_INEL   0  /* electron IMFP per shell   (Total_el_MFPs)    */
 #define TREKIS_TAB_EL_ELAST  1  /* electron EMFP             (Elastic_MFP%Total)*/
@@ -289,6 +320,9 @@ int32_t trekis_tables_export(const trekis_tables* t, int32_t kind, int32_t atom,
 #define TREKIS_ROW_H_INEL  1   /* aidCS%HIdCS (valence band)          */
 #define TREKIS_ROW_EL_ELAST 2  /* aidCS%EEdCS (phonon elastic)        */
 #define TREKIS_ROW_H_ELAST  3  /* aidCS%HEdCS (phonon elastic, holes) */
+#define TREKIS_ROW_SHI      4  /* SHI transfer row at SHI grid node iE (tables built with
+                                  shi_rows_by_energy; hw: energy, dsdhw: MFP column of
+                                  diff_SHI_MFP); TREKIS_EINVAL for a node outside the window */
 
 /* Release the device workspace (particle queues, int64 tallies) a table set
  * keeps between runs; the next run allocates it again.  For callers holding

@@ -1,0 +1,58 @@
+! trekis_pack.f90 -- packing shim between the reference program's objects and
+! the C ABI of include/trekis_gb300.h (the types of trekis_gb300.f90).
+!
+! Fortran derived types with allocatable components are not interoperable, so
+! once per run this copies
+!   Target_atoms(i) (type(Atom), Objects.f90:257-275)      -> cmat%atoms(i)
+!   Matter (type(Solid)), Mat_DOS, CDF_Phonon, NumPar flags -> cmat
+!   SHI (type(Ion), Objects.f90:44-53)                      -> cion
+! It needs the reference's module Objects in scope.  The DOS arrays are passed
+! by address (c_loc) and must stay allocated while the library runs; the
+! inverted DOS of metals is not carried.
+subroutine pack_inputs(Target_atoms, Matter, Mat_DOS, CDF_Phonon, NumPar, SHI, cmat, cion)
+  use iso_c_binding
+  use Objects
+  use trekis_gb300
+  type(Atom), dimension(:), intent(in) :: Target_atoms
+  type(Solid), intent(in) :: Matter
+  type(Density_of_states), intent(in), target :: Mat_DOS
+  type(CDF), intent(in) :: CDF_Phonon
+  type(Flag), intent(in) :: NumPar
+  type(Ion), intent(in) :: SHI
+  type(trekis_material), intent(out) :: cmat
+  type(trekis_ion), intent(out) :: cion
+  integer :: i, j, n
+  cmat%N_atoms = size(Target_atoms)
+  do i = 1, size(Target_atoms)
+     associate (a => Target_atoms(i), c => cmat%atoms(i))
+       c%Zat = a%Zat; c%N_shl = a%N_shl; c%Mass = a%Mass; c%Pers = a%Pers
+       do j = 1, a%N_shl
+          c%Shl_num(j) = a%Shl_num(j); c%KOCS(j) = a%KOCS(j); c%KOCS_SHI(j) = a%KOCS_SHI(j)
+          c%Nel(j) = a%Nel(j); c%Ip(j) = a%Ip(j); c%Auger(j) = a%Auger(j); c%Radiat(j) = a%Radiat(j)
+          n = size(a%Ritchi(j)%A); c%N_osc(j) = n
+          c%E0(1:n, j) = a%Ritchi(j)%E0; c%A(1:n, j) = a%Ritchi(j)%A; c%Gamma(1:n, j) = a%Ritchi(j)%Gamma
+       enddo
+       c%form_factor = 0.0d0
+       if (allocated(Matter%form_factor)) c%form_factor = Matter%form_factor(a%Zat, :)
+     end associate
+  enddo
+  cmat%Dens = Matter%Dens; cmat%At_Dens = Matter%At_Dens; cmat%Vsound = Matter%Vsound
+  cmat%E_F = Matter%E_F; cmat%Egap = Matter%Egap; cmat%Layer = Matter%Layer; cmat%N_VB_el = Matter%N_VB_el
+  cmat%work_function = Matter%work_function; cmat%bar_length = Matter%bar_length
+  cmat%bar_height = Matter%bar_height; cmat%hole_mass = Matter%hole_mass
+  cmat%El_eff_mass = Matter%El_eff_mass; cmat%cut_off = Matter%cut_off; cmat%temp = Matter%temp
+  cmat%v_f = Matter%v_f
+  n = 0
+  if (allocated(CDF_Phonon%A)) n = size(CDF_Phonon%A)
+  cmat%N_ph_osc = n
+  cmat%ph_E0(1:n) = CDF_Phonon%E0; cmat%ph_A(1:n) = CDF_Phonon%A; cmat%ph_Gamma(1:n) = CDF_Phonon%Gamma
+  cmat%N_dos = size(Mat_DOS%E)
+  cmat%dos_E = c_loc(Mat_DOS%E); cmat%dos_DOS = c_loc(Mat_DOS%DOS); cmat%dos_int = c_loc(Mat_DOS%int_DOS)
+  cmat%dos_k = c_loc(Mat_DOS%k); cmat%dos_Eff_m = c_loc(Mat_DOS%Eff_m)
+  cmat%kind_of_EMFP = NumPar%kind_of_EMFP; cmat%CDF_elast_Zeff = NumPar%CDF_elast_Zeff
+  cmat%kind_of_DR = NumPar%kind_of_DR
+  cmat%plasmon_Emax = merge(1, 0, NumPar%plasmon_Emax)
+  cmat%include_photons = merge(1, 0, NumPar%include_photons)
+  cion%Zat = SHI%Zat; cion%Kind_Zeff = SHI%Kind_Zeff; cion%Kind_ion = SHI%Kind_ion; cion%pad_ = 0
+  cion%Mass = SHI%Mass; cion%E = SHI%E; cion%fixed_Zeff = SHI%fixed_Zeff
+end subroutine pack_inputs

@@ -50,8 +50,26 @@ int oracle_tables_export(void* t, int kind, int a, int s, double* E, double* L, 
     return 0;
 }
 
+// SHI transfer row of grid node iE (tables built with shi_rows_by_energy), or null
+static MFPTab* shi_row_of(Tables* T, int a, int s, int iE) {
+    if (T->shi_row_nodes.empty()) return nullptr;
+    const int q = iE - T->shi_row_nodes.front();
+    std::vector<MFPTab>& v = T->shi_rows_E[a * TREKIS_MAX_SHELLS + s];
+    if (q < 0 || q >= (int)v.size()) return nullptr;
+    return &v[q];
+}
+
 int oracle_tables_row(void* t, int kind, int a, int s, int iE, double* hw, double* L, int64_t cap, int64_t* n) {
     Tables* T = (Tables*)t;
+    if (kind == TREKIS_ROW_SHI) {
+        const MFPTab* r = shi_row_of(T, a, s, iE);
+        if (!r) return TREKIS_EINVAL;
+        *n = (int64_t)r->E.size();
+        if (*n > cap) return TREKIS_EINVAL;
+        if (hw) std::memcpy(hw, r->E.data(), r->E.size() * 8);
+        if (L) std::memcpy(L, r->L.data(), r->L.size() * 8);
+        return 0;
+    }
     const RowSet* R = (kind == TREKIS_ROW_EL_INEL) ? &T->el_rows[a * TREKIS_MAX_SHELLS + s]
                       : (kind == TREKIS_ROW_H_INEL) ? &T->hole_rows
                       : (kind == TREKIS_ROW_EL_ELAST) ? &T->el_elast_rows
@@ -77,6 +95,14 @@ int oracle_tables_set(void* t, int kind, int a, int s, const double* E, const do
 }
 int oracle_tables_set_row(void* t, int kind, int a, int s, int iE, const double* hw, const double* L, int64_t n) {
     Tables* T = (Tables*)t;
+    if (kind == TREKIS_ROW_SHI) {
+        MFPTab* r = shi_row_of(T, a, s, iE);
+        if (!r) return TREKIS_EINVAL;
+        r->E.assign(hw, hw + n);
+        r->L.assign(L, L + n);
+        r->dEdx.assign(n, 0.0);
+        return 0;
+    }
     RowSet* R = (kind == TREKIS_ROW_EL_INEL) ? &T->el_rows[a * TREKIS_MAX_SHELLS + s]
                 : (kind == TREKIS_ROW_H_INEL) ? &T->hole_rows
                 : (kind == TREKIS_ROW_EL_ELAST) ? &T->el_elast_rows

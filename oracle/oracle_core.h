@@ -61,6 +61,10 @@ struct MFPTab { std::vector<double> E, L, dEdx; };                 // type(MFP)
 struct Tables {
     // per atom, per shell (flattened atom*MAX_SHELLS + shell)
     std::vector<MFPTab> el, hole, phot, shi, shi_dsde;
+    // shi_rows_by_energy: transfer rows at the SHI grid nodes shi_row_nodes
+    // (contiguous), shi_rows_E[atom*MAX_SHELLS + shell][q] at node shi_row_nodes[q]
+    std::vector<std::vector<MFPTab>> shi_rows_E;
+    std::vector<int> shi_row_nodes;
     MFPTab el_elast, hole_elast;
     std::vector<RowSet> el_rows;   // per atom,shell
     RowSet hole_rows;              // valence band only

@@ -380,6 +380,24 @@ void new_hole(Ctx& c, H& hh, double t0, double X, double Y, double Z, int a, int
     if (hh.Ehkin < -1.0e-9 || std::isnan(hh.Ehkin)) c.err |= TREKIS_ERR_NEG_ENERGY_H;
 }
 
+// SHI_energy_transfer's draw on one transfer row (Monte_Carlo.f90:1736-1780):
+// Tot = 1/L(Ip) + RN (1/L(end) - 1/L(Ip)) inverted in 1/L, log-log
+double shi_row_draw(const MFPTab& D, double Ip, double RN) {
+    const int N = (int)D.L.size();
+    if (N < 1) return Ip;   // shell beyond the SHI's maximum transfer
+    int Mt = find_monoton(D.E.data(), N, Ip);
+    double dL;
+    if (Mt > 1) dL = (D.L[Mt - 2] > 1.0e-10) ? interp(5, D.E[Mt - 2], D.E[Mt - 1], D.L[Mt - 2], D.L[Mt - 1], Ip)
+                                             : interp(1, D.E[Mt - 2], D.E[Mt - 1], D.L[Mt - 2], D.L[Mt - 1], Ip);
+    else dL = D.L[0];
+    double Tot = (dL > 0.0 && D.L[N - 1] > 0.0) ? 1.0 / dL + RN * (1.0 / D.L[N - 1] - 1.0 / dL) : 1.5e21;
+    int nt;
+    if (Tot < 1e20) { nt = 1; while (nt < N && 1.0 / D.L[nt - 1] < Tot) ++nt; }
+    else nt = Mt;
+    if (nt > Mt) return interp(5, 1.0 / D.L[nt - 2], 1.0 / D.L[nt - 1], D.E[nt - 2], D.E[nt - 1], Tot);
+    return Ip;
+}
+
 // ---- SHI_Monte_Carlo (Monte_Carlo.f90:2153-2249) --------------------------------
 void shi_event(Ctx& c, int i) {
     const trekis_material& m = *c.m;
@@ -390,26 +408,31 @@ void shi_event(Ctx& c, int i) {
     // SHI_energy_transfer (Monte_Carlo.f90:1719-1780), CDF branch
     double dE;
     {
-        const MFPTab& D = c.T->shi_dsde[sidx(A, S)];
-        const int N = (int)D.L.size();
         double RN = s.next();
-        double Ecur = m.atoms[A].Ip[S];
-        if (N < 1) { dE = Ecur; goto transferred; }  // shell beyond the SHI's maximum transfer
-        {
-        int Mt = find_monoton(D.E.data(), N, m.atoms[A].Ip[S]);
-        double dL;
-        if (Mt > 1) dL = (D.L[Mt - 2] > 1.0e-10) ? interp(5, D.E[Mt - 2], D.E[Mt - 1], D.L[Mt - 2], D.L[Mt - 1], Ecur)
-                                                 : interp(1, D.E[Mt - 2], D.E[Mt - 1], D.L[Mt - 2], D.L[Mt - 1], Ecur);
-        else dL = D.L[0];
-        double Tot = (dL > 0.0 && D.L[N - 1] > 0.0) ? 1.0 / dL + RN * (1.0 / D.L[N - 1] - 1.0 / dL) : 1.5e21;
-        int nt;
-        if (Tot < 1e20) { nt = 1; while (nt < N && 1.0 / D.L[nt - 1] < Tot) ++nt; }
-        else nt = Mt;
-        if (nt > Mt) dE = interp(5, 1.0 / D.L[nt - 2], 1.0 / D.L[nt - 1], D.E[nt - 2], D.E[nt - 1], Tot);
-        else dE = m.atoms[A].Ip[S];
+        const double Ip = m.atoms[A].Ip[S];
+        const Tables& T = *c.T;
+        if (T.shi_row_nodes.empty()) {   // the row at the initial energy (Universal_MC_for_SHI_MAIN.f90:231-238)
+            dE = shi_row_draw(T.shi_dsde[sidx(A, S)], Ip, RN);
+        } else {
+            // extension: the rows of the SHI grid energies around the ion's,
+            // combined as interpolate_transferred_energy does (Cross_sections.f90:1968-2045)
+            const std::vector<double>& gS = T.shi[sidx(A, S)].E;
+            const int w0 = T.shi_row_nodes.front(), nW = (int)T.shi_row_nodes.size();
+            int iE = find_monoton(gS.data(), (int)gS.size(), c.shi.E);
+            if (iE > 1 && std::fabs(gS[iE - 2] - c.shi.E) < 1.0e-6) iE -= 1;
+            auto row = [&](int node) {
+                const int q = node < w0 ? 0 : (node >= w0 + nW ? nW - 1 : node - w0);
+                return shi_row_draw(T.shi_rows_E[sidx(A, S)][q], Ip, RN);
+            };
+            const int up = iE - 1, lo = iE - 2;
+            const double d1 = row(up);
+            if (iE > 1 && lo >= w0 && up < w0 + nW) {
+                const double d2 = row(lo);
+                dE = (d1 < 1.0e-10 || d2 < 1.0e-10) ? interp(1, gS[lo], gS[up], d1, d2, c.shi.E)
+                                                    : interp(5, gS[lo], gS[up], d1, d2, c.shi.E);
+            } else dE = d1;
         }
     }
-transferred:
     double L_new = next_free_path_2d(c.T->SHI_path, c.shi.E);
     double RN = s.next();
     L_new = -L_new * std::log(RN);

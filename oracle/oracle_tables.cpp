@@ -717,13 +717,20 @@ int build_tables(const trekis_material& m, const trekis_ion& ion, const trekis_t
             if (cfg.shi_E_window_hi > 0 && i > 0 && gS[i - 1] > cfg.shi_E_window_hi) in = false;
             if (in) todo.push_back(i);
         }
+        // rows at every node of the window: an extension (trekis_table_cfg.shi_rows_by_energy)
+        T.shi_rows_E.assign(T.shi.size(), {});
+        if (cfg.shi_rows_by_energy)
+            for (int a = 0; a < m.N_atoms; ++a)
+                for (int s = 0; s < m.atoms[a].N_shl; ++s) T.shi_rows_E[sidx(a, s)].assign(todo.size(), {});
+        T.shi_row_nodes = cfg.shi_rows_by_energy ? todo : std::vector<int>();
 #pragma omp parallel for schedule(dynamic)
         for (int k = 0; k < (int)todo.size(); ++k) {
             int i = todo[k];
             for (int a = 0; a < m.N_atoms; ++a)
                 for (int s = 0; s < m.atoms[a].N_shl; ++s) {
                     double inv, dd;
-                    shi_totimfp(m, ion, a, s, gS[i], inv, dd, nullptr);
+                    shi_totimfp(m, ion, a, s, gS[i], inv, dd,
+                                cfg.shi_rows_by_energy ? &T.shi_rows_E[sidx(a, s)][k] : nullptr);
                     double L = (inv > 1.0e-10) ? 1.0 / inv : 1.0e28;
                     if (L > 1e30) L = 1e30;
                     T.shi[sidx(a, s)].L[i] = L;

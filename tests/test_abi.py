@@ -110,9 +110,12 @@ def test_delta_cdf_dispersion_refused(lib):
     assert rc == -7 and not out.value
 
 
+F90 = ROOT / "include" / "trekis_gb300.f90"
+
+
 def _fortran_types():
-    """The bind(C) derived types of INTEGRATION.md: name -> [(kind, count)]."""
-    txt = (ROOT / "INTEGRATION.md").read_text()
+    """The bind(C) derived types of the Fortran interface module: name -> [(kind, count)]."""
+    txt = F90.read_text()
     consts = {k: getattr(abi, k.replace("TREKIS_", "")) for k in
               ("TREKIS_MAX_ATOMS", "TREKIS_MAX_SHELLS", "TREKIS_MAX_OSC", "TREKIS_MAX_PH_OSC")}
     out = {}
@@ -152,17 +155,29 @@ def _c_layout(fields, types):
 
 
 def test_fortran_interface_types_match_c():
-    """Every bind(C) type INTEGRATION.md gives a Fortran maintainer has the size
-    of the C struct it mirrors, so the library never reads past a Fortran
-    argument."""
+    """Every bind(C) type of include/trekis_gb300.f90 has the size of the C
+    struct it mirrors, so the library never reads past a Fortran argument."""
     types = _fortran_types()
     mirrors = {"trekis_atom": abi.Atom, "trekis_material": abi.Material, "trekis_ion": abi.Ion,
                "trekis_table_cfg": abi.TableCfg, "trekis_run_cfg": abi.RunCfg, "trekis_tallies": abi.Tallies,
-               "trekis_status": abi.Status, "trekis_output_cfg": abi.OutputCfg, "trekis_batch_cfg": abi.BatchCfg}
-    assert set(types) <= set(mirrors), set(types) - set(mirrors)
-    assert {"trekis_material", "trekis_run_cfg", "trekis_tallies", "trekis_status"} <= set(types)
+               "trekis_status": abi.Status, "trekis_output_cfg": abi.OutputCfg, "trekis_batch_cfg": abi.BatchCfg,
+               "trekis_build_stats": abi.BuildStats, "trekis_tune": abi.Tune, "trekis_mlp_cfg": abi.MlpCfg,
+               "trekis_mlp_report": abi.MlpReport}
+    assert set(types) == set(mirrors), set(types) ^ set(mirrors)
     for name, fields in types.items():
         assert _c_layout(fields, types)[0] == C.sizeof(mirrors[name]), name
+
+
+def test_fortran_interface_covers_every_entry_point():
+    """The Fortran module binds every function the C header declares, under
+    the same name, and states the header's ABI version."""
+    txt = F90.read_text()
+    bound = set(re.findall(r"(?:function|subroutine)\s+(trekis_\w+)\s*\(", txt))
+    assert bound == set(abi.SIGNATURES), set(abi.SIGNATURES) ^ bound
+    m = re.search(r"TREKIS_ABI_VERSION\s*=\s*(\d+)", txt)
+    assert m and int(m.group(1)) == abi.ABI_VERSION
+    hdr = (ROOT / "include" / "trekis_gb300.h").read_text()
+    assert int(re.search(r"#define TREKIS_ABI_VERSION (\d+)", hdr).group(1)) == abi.ABI_VERSION
 
 
 def test_time_points(lib, oracle_lib):
@@ -183,14 +198,11 @@ def test_time_points(lib, oracle_lib):
 
 
 def test_c_caller_example(lib, tmp_path):
-    """The C caller of INTEGRATION.md compiles against the header alone, links
-    the library and runs: without a GB300 it stops at TREKIS_ENODEVICE."""
-    txt = (ROOT / "INTEGRATION.md").read_text()
-    src = txt.split("## 7. Calling from C", 1)[1].split("```c\n", 1)[1].split("```", 1)[0]
-    (tmp_path / "caller.c").write_text(src)
+    """examples/c_caller.c compiles against the header alone, links the
+    library and runs: without a GB300 it stops at TREKIS_ENODEVICE."""
     exe = tmp_path / "caller"
     subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", str(ROOT / "include"), "-o", str(exe),
-                    str(tmp_path / "caller.c"), "-L", str(build.LIB.parent), "-ltrekis_gb300",
+                    str(ROOT / "examples" / "c_caller.c"), "-L", str(build.LIB.parent), "-ltrekis_gb300",
                     f"-Wl,-rpath,{build.LIB.parent}"], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr

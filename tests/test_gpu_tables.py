@@ -215,3 +215,49 @@ def test_table_cache_files(gpu_lib, tmp_path, cfg_name):
     grid, rws = rows["el"][0]
     r0 = api.read_table_file(tmp_path / "lib" / "diff_CS" / [n for n in rdir if n.startswith(el_file[7:-4])][0])
     assert r0.shape[1] == 2
+
+
+@pytest.mark.gpu
+def test_shi_rows_by_energy(gpu_lib):
+    """shi_rows_by_energy: a transfer row at every SHI grid node of the window
+    (13 nodes per shell for a 2 MeV Xe ion), each equal to the oracle's
+    SHI_TotIMFP row at that energy (1e-6), and the FP64 track loop drawing at
+    the ion's current energy from the two rows around it equal to the
+    oracle's on the same tables; its draws differ from those of the row frozen
+    at the initial energy."""
+    import oracle_py
+    from conftest import copy_tables
+    w = configs.small(configs.cfg0, NMC=4, layer=100.0, Tim=20.0, ion_E=2.0e6)
+    t = api.Tables(w, lib=gpu_lib, shi_rows_by_energy=True)
+    tc = abi.TableCfg(build_shi=1, build_photon=0, shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01,
+                      shi_rows_by_energy=1)
+    o = oracle_py.OracleTables(t.mat, t.ion, tc)
+    nodes = 0
+    for a, atom in enumerate(w.material.atoms):
+        for s in range(len(atom.shells)):
+            E, _L, _D = t.export(abi.TAB_SHI, a, s)
+            for i in range(len(E)):
+                try:
+                    hw1, L1 = t.row(abi.ROW_SHI, a, s, i)
+                except RuntimeError:
+                    continue
+                hw2, L2 = o.row(abi.ROW_SHI, a, s, i)
+                assert _close(hw1, hw2, 1e-12) and _close(L1, L2), (a, s, i)
+                nodes += 1
+    assert nodes >= 40
+    # the track loop on identical tables, FP64: equal to the oracle's
+    copy_tables(t, o, w)
+    opt = api.RunOptions(precision=1, seed=3)
+    g, sg = api.mc_run(t, opt)
+    r = api.new_tallies(w)
+    cfg, _R = api.run_cfg(w, opt)
+    sr = abi.Status.fresh()
+    o.mc_run(cfg, r, sr)
+    assert sg.n_shi == sr.n_shi > 0 and sg.n_events == sr.n_events
+    for k in g.a:
+        tol = 1e-6 * np.abs(r[k]) + 1e-9 * (np.max(np.abs(r[k])) + 1e-300)
+        assert np.all(np.abs(g[k] - r[k]) <= tol), k
+    # and the draws differ from the frozen-row draws of the reference's method
+    t0 = api.Tables(w, lib=gpu_lib)
+    g0, s0 = api.mc_run(t0, opt)
+    assert not np.array_equal(g0["Out_tot_E"], g["Out_tot_E"])

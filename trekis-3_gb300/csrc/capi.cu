@@ -221,6 +221,22 @@ static double interp_h(int flag, double E1, double E2, double S1, double S2, dou
     return S1 + (S2 - S1) / (E2 - E1) * (Ex - E1);
 }
 
+// The constant part of SHI_energy_transfer (Monte_Carlo.f90:1736-1757) for
+// one transfer row: Mt, the index of Ip in the row, and 1/L at Ip and at the
+// row's end (0, 0 for a row that transfers nothing)
+static void shi_row_consts(const HTab& r, double Ip, int& Mt, double& ia, double& ib) {
+    const int N = (int)r.L.size();
+    ia = ib = 0.0; Mt = 1;
+    if (N < 1) return;
+    const int M = find_mono_d(r.E.data(), N, Ip);
+    double dL;
+    if (M > 1) dL = (r.L[M - 2] > 1.0e-10) ? interp_h(5, r.E[M - 2], r.E[M - 1], r.L[M - 2], r.L[M - 1], Ip)
+                                           : interp_h(1, r.E[M - 2], r.E[M - 1], r.L[M - 2], r.L[M - 1], Ip);
+    else dL = r.L[0];
+    Mt = M;
+    if (dL > 0.0 && r.L[N - 1] > 0.0) { ia = 1.0 / dL; ib = 1.0 / r.L[N - 1]; }
+}
+
 template <class T>
 static int upload_shi(trekis_tables* t, DevShi<T>& s) {
     Buffers& b = t->buf;
@@ -242,19 +258,7 @@ static int upload_shi(trekis_tables* t, DevShi<T>& s) {
         dE.insert(dE.end(), r.E.begin(), r.E.end());
         for (double x : r.L) dI.push_back(1.0 / x);
         off.push_back((int)dE.size());
-        const int N = (int)r.L.size();
-        ia[k] = ib[k] = 0.0; mt[k] = 1;
-        if (N > 0) {
-            // the constant part of SHI_energy_transfer (Monte_Carlo.f90:1736-1757)
-            const double Ip = t->mat.atoms[t->atom_of[k]].Ip[t->shell_of[k]];
-            const int M = find_mono_d(r.E.data(), N, Ip);
-            double dL;
-            if (M > 1) dL = (r.L[M - 2] > 1.0e-10) ? interp_h(5, r.E[M - 2], r.E[M - 1], r.L[M - 2], r.L[M - 1], Ip)
-                                                   : interp_h(1, r.E[M - 2], r.E[M - 1], r.L[M - 2], r.L[M - 1], Ip);
-            else dL = r.L[0];
-            mt[k] = M;
-            if (dL > 0.0 && r.L[N - 1] > 0.0) { ia[k] = 1.0 / dL; ib[k] = 1.0 / r.L[N - 1]; }
-        }
+        shi_row_consts(r, t->mat.atoms[t->atom_of[k]].Ip[t->shell_of[k]], mt[k], ia[k], ib[k]);
     }
     s.sL = upload<T>(b, L);
     s.lL = upload<T>(b, logs(L));
@@ -270,6 +274,30 @@ static int upload_shi(trekis_tables* t, DevShi<T>& s) {
     s.Mt = upload_i(b, mt);
     s.pow_zp = (T)std::pow((double)t->ion.Zat, 0.66666666);
     if (!s.sE || !s.sL || !s.pL || !s.d_off || !s.dE || !s.Mt) { set_error("SHI table upload failed"); return TREKIS_ENOMEM; }
+    // rows at every SHI grid energy of the window
+    s.nW = (int)t->shi_row_nodes.size();
+    s.w0 = s.nW ? t->shi_row_nodes[0] : 0;
+    s.wr_off = nullptr; s.wE = s.wlE = s.wI = s.wlI = s.w_ia = s.w_ib = nullptr; s.w_Mt = nullptr;
+    if (s.nW) {
+        std::vector<double> wE, wI, wa, wb;
+        std::vector<int> wo(1, 0), wm;
+        for (int k = 0; k < nsh; ++k)
+            for (int q = 0; q < s.nW; ++q) {
+                const HTab& r = t->dsde_E[k][q];
+                wE.insert(wE.end(), r.E.begin(), r.E.end());
+                for (double x : r.L) wI.push_back(1.0 / x);
+                wo.push_back((int)wE.size());
+                int M;
+                double a, c;
+                shi_row_consts(r, t->mat.atoms[t->atom_of[k]].Ip[t->shell_of[k]], M, a, c);
+                wm.push_back(M); wa.push_back(a); wb.push_back(c);
+            }
+        s.wr_off = upload_i(b, wo);
+        s.wE = upload<T>(b, wE); s.wlE = upload<T>(b, logs(wE));
+        s.wI = upload<T>(b, wI); s.wlI = upload<T>(b, logs(wI));
+        s.w_ia = upload<T>(b, wa); s.w_ib = upload<T>(b, wb); s.w_Mt = upload_i(b, wm);
+        if (!s.wr_off || !s.wE || !s.wI || !s.w_Mt) { set_error("SHI table upload failed"); return TREKIS_ENOMEM; }
+    }
     return TREKIS_OK;
 }
 
@@ -527,7 +555,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
           : (ws->per_it_peak > 0.0 ? (int)std::min<double>(0.5 * (double)cap / ws->per_it_peak, 1 << 30) : 256);
     B = std::max(1, std::min(std::min(B, B_max), cfg.NMC));
     CK(cudaEventRecord(ws->e0, strm));
-    uint64_t steps = 0, launches = 1, ev_tot[8] = {0}, peak_all = 0;   // the grid hints
+    uint64_t steps = 0, launches = 1, ev_tot[9] = {0}, peak_all = 0;   // the grid hints
     uint64_t h2d = sizeof(T) * (Nt + cfg.N_R) + 8 * cfg.N_R, d2h = 0;
     double step_ms = 0.0;
     Ctrs hc;
@@ -588,7 +616,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             continue;
         }
         steps += bsteps; launches += blaunch; step_ms += bms;
-        for (int q = 0; q < 8; ++q) ev_tot[q] += hc.ev[q];
+        for (int q = 0; q < 9; ++q) ev_tot[q] += hc.ev[q];
         ev_tot[7] += 2 * hc.ev[0];   // the pair of every SHI collision
         err_bits |= hc.err_bits;
         peak_all = std::max<uint64_t>(peak_all, (uint64_t)peak);
@@ -642,6 +670,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         st->batch_iterations = B;
         st->h2d_bytes += h2d;
         st->d2h_bytes += d2h;
+        st->n_fp64_redraws += ev_tot[8];
     }
     return TREKIS_OK;
 }
@@ -707,6 +736,13 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
     rc = build_tables_device(t, *cfg, st);
     if (!rc) rc = upload_mc<float>(t, t->d32);
     if (!rc) rc = upload_mc<double>(t, t->d64);
+    if (!rc) {   // the FP64 tables on the device, for FP32 draws redone in FP64
+        DevTabs<double>* a = (DevTabs<double>*)t->buf.alloc(sizeof(DevTabs<double>));
+        if (!a || cudaMemcpy(a, &t->d64, sizeof(DevTabs<double>), cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("table upload failed");
+            rc = TREKIS_ENOMEM;
+        } else t->d32.alt = a;
+    }
     if (!rc && t->has_shi) rc = upload_shi<float>(t, t->dshi32);
     if (!rc && t->has_shi) rc = upload_shi<double>(t, t->dshi64);
     if (rc) { delete t; if (st) st->code = rc; return rc; }
@@ -716,6 +752,13 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
 }
 
 void trekis_tables_free(trekis_tables* t) { delete t; }
+
+int32_t trekis_tables_stats(const trekis_tables* t, trekis_build_stats* s) {
+    if (!t || !s) { set_error("null argument"); return TREKIS_EINVAL; }
+    s->build_ms = t->build_ms; s->integral_ms = t->integral_ms; s->jobs = t->build_jobs;
+    s->points = t->build_points; s->q_steps = t->build_q_steps; s->osc_terms = t->build_osc_terms;
+    return TREKIS_OK;
+}
 
 void trekis_tables_trim(trekis_tables* t) {
     if (t) { t->ws.reset(); t->ws_key = 0; }
@@ -764,6 +807,18 @@ int32_t trekis_tables_row(const trekis_tables* t, int32_t kind, int32_t a, int32
     } else if (kind == TREKIS_ROW_H_INEL) R = &t->hole_rows;
     else if (kind == TREKIS_ROW_EL_ELAST) R = &t->el_elast_rows;
     else if (kind == TREKIS_ROW_H_ELAST) R = &t->hole_elast_rows;
+    else if (kind == TREKIS_ROW_SHI) {   // transfer row of an SHI grid node of the window
+        if (a < 0 || a >= t->mat.N_atoms || s < 0 || s >= t->mat.atoms[a].N_shl || t->shi_row_nodes.empty())
+            return TREKIS_EINVAL;
+        const int q = iE - t->shi_row_nodes[0];
+        if (q < 0 || q >= (int)t->shi_row_nodes.size()) return TREKIS_EINVAL;
+        const HTab& r = t->dsde_E[t->shell_index[a][s]][q];
+        *n = (int64_t)r.E.size();
+        if (*n > cap) return TREKIS_EINVAL;
+        if (hw) std::memcpy(hw, r.E.data(), 8 * r.E.size());
+        if (dsdhw) std::memcpy(dsdhw, r.L.data(), 8 * r.L.size());
+        return TREKIS_OK;
+    }
     if (!R || iE < 0 || iE >= (int)R->rows.size()) return TREKIS_EINVAL;
     const HRow& r = R->rows[iE];
     *n = (int64_t)r.hw.size();

@@ -172,6 +172,22 @@ __device__ __forceinline__ T interp(int flag, T E1, T E2, T S1, T S2, T Ex) {
     return S1 + (S2 - S1) / (E2 - E1) * (Ex - E1);
 }
 
+// Interpolate(5, ...) evaluated for accuracy in FP32.  FP64 keeps the
+// reference's expression.  FP32 evaluates the same log-log line through
+// ratios, S1 (S2/S1)^(log(Ex/E1) / log(E2/E1)): the logarithms are of numbers
+// near 1 and keep full FP32 relative precision, where the reference's form
+// subtracts logarithms of order 10 and loses about 1e-6 of relative accuracy.
+template <class T>
+__device__ __forceinline__ T interp5_acc(T E1, T E2, T S1, T S2, T Ex) {
+    if constexpr (sizeof(T) == 8) {
+        return interp<T>(5, E1, E2, S1, S2, Ex);
+    } else {
+        if (m_abs(E2 - E1) < T(1.0e-6)) return S1 > S2 ? S1 : S2;
+        if (Ex == E1) return S1;
+        return S1 * m_exp(m_log(S2 / S1) * (m_log(Ex / E1) / m_log(E2 / E1)));
+    }
+}
+
 // ---- a (E, L) mean-free-path table ---------------------------------------------
 template <class T>
 struct Tab {
@@ -190,7 +206,7 @@ __device__ __forceinline__ T nfp2(const Tab<T>& t, T E) {
     }
     T Ll = t.L[n - 2];
     if (Ll >= T(1.0e16)) return Ll;
-    return interp<T>(5, t.E[n - 2], t.E[n - 1], Ll, t.L[n - 1], E);
+    return interp5_acc<T>(t.E[n - 2], t.E[n - 1], Ll, t.L[n - 1], E);
 }
 // Next_free_path_1d (Monte_Carlo.f90:1835-1871): the floor compares with the energy array
 template <class T>
@@ -202,7 +218,7 @@ __device__ __forceinline__ T nfp1(const Tab<T>& t, T E) {
     }
     T Ll = t.L[n - 2];
     if (Ll >= T(1.0e16)) return Ll;
-    return interp<T>(5, t.E[n - 2], t.E[n - 1], Ll, t.L[n - 1], E);
+    return interp5_acc<T>(t.E[n - 2], t.E[n - 1], Ll, t.L[n - 1], E);
 }
 
 

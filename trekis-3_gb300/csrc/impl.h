@@ -99,6 +99,11 @@ struct DevTabs {
     const GHint<T>* dos_hint;   // uniform buckets over [dosE[0], dosE[nD-1]); null: bisection
     T dos_lo, dos_hi, dos_inv;
     int dos_nb;
+    // FP32 copy only: the FP64 copy of the same tables on the device.  An FP32
+    // draw whose bracket is ill-conditioned (the inversion would amplify the
+    // FP32 rounding of the row nodes and of L_need beyond 1e-5) is redone in
+    // FP64 on these rows.
+    const DevTabs<double>* alt = nullptr;
 };
 
 // SHI tables in the precision of the run, with host-precomputed logarithms so
@@ -115,6 +120,15 @@ struct DevShi {
     const T* invL_last;                // [nsh] 1/L at the end of the row
     const int* Mt;                     // [nsh] index of Ip in the row (Find_in_array_monoton)
     T pow_zp;                          // Z_ion^0.66666666
+    // transfer rows at the SHI grid energies w0 .. w0 + nW - 1 (trekis_table_cfg.
+    // shi_rows_by_energy; nW = 0: the rows above, at the initial energy, serve
+    // the whole track), row (k, q) of shell k and node w0 + q at wr_off[k nW + q]
+    int nW, w0;
+    const int* wr_off;                 // [nsh*nW + 1]
+    const T* wE; const T* wlE;         // the rows' lower edges and log
+    const T* wI; const T* wlI;         // 1/L and log
+    const T* w_ia; const T* w_ib;      // [nsh*nW] 1/L at the ionisation potential, at the row's end
+    const int* w_Mt;                   // [nsh*nW]
 };
 
 struct Buffers {          // device allocations owned by a table set
@@ -134,6 +148,10 @@ struct trekis_tables {
     int shell_index[TREKIS_MAX_ATOMS][TREKIS_MAX_SHELLS];
     // host FP64 mirror
     std::vector<tk::HTab> el, hole, phot, shi, dsde;  // per compact shell
+    // with shi_rows_by_energy: transfer rows at the SHI grid nodes shi_row_nodes
+    // (contiguous), dsde_E[k][q] for shell k and node shi_row_nodes[q]
+    std::vector<std::vector<tk::HTab>> dsde_E;
+    std::vector<int> shi_row_nodes;
     tk::HTab el_elast, hole_elast, El_IMFP, Hole_IMFP, Phot_IMFP, SHI_path;
     std::vector<tk::HRowSet> el_rows;   // per compact shell
     tk::HRowSet hole_rows;
@@ -146,8 +164,8 @@ struct trekis_tables {
     tk::DevTabs<double> d64;
     tk::DevShi<float> dshi32;
     tk::DevShi<double> dshi64;
-    double build_ms = 0.0;
-    uint64_t build_points = 0;
+    double build_ms = 0.0, integral_ms = 0.0;   // trekis_tables_stats
+    uint64_t build_points = 0, build_jobs = 0, build_q_steps = 0, build_osc_terms = 0;
     // reusable MC workspace (queues, int64 tallies, staging), rebuilt when the
     // precision, capacity or tally shape of a call changes
     std::shared_ptr<void> ws;

@@ -82,6 +82,13 @@ struct EvStream {
     }
     __device__ __forceinline__ T next() { return Uni<T>::of(word()); }
     __device__ __forceinline__ double next_d() { return Uni<double>::of(word()); }
+    // one word as the draw of the run's precision and as the FP64 draw (the
+    // latter feeds an FP32 draw that is redone in FP64)
+    __device__ __forceinline__ void next2(T& u, double& ud) {
+        const uint32_t w = word();
+        u = Uni<T>::of(w);
+        ud = Uni<double>::of(w);
+    }
     // FP32: u and 1 - u of one word, each rounded from all 32 bits, for
     // draws that depend on 1 - u near u = 1 (the FP64 draw is (w + 0.5) 2^-32)
     __device__ __forceinline__ void next_pair(float& u, float& omu) {
@@ -384,7 +391,7 @@ __device__ int which_shell(const McConst<T>& C, const T* Eg, const T* Lbase, int
         T M;
         if (nb == 1) M = T(1.0e20);
         else if (L[nb - 2] == L[nb - 1] || L[nb - 2] > T(1e20)) M = L[nb - 2];
-        else M = interp<T>(5, Eg[nb - 2], Eg[nb - 1], L[nb - 2], L[nb - 1], E);
+        else M = interp5_acc<T>(Eg[nb - 2], Eg[nb - 1], L[nb - 2], L[nb - 1], E);
         inv[k] = T(1) / M;
         tot += inv[k];
     }
@@ -618,14 +625,48 @@ __device__ void angles_lat(const McConst<T>& C, T E, T W, T M_eff, S& s, T& thet
 template <class T>
 __device__ __forceinline__ T elastic_uniform(T x, T inv_I, T Em) { return (x - inv_I) * Em; }
 
+// Conditioning of an FP32 draw.  A log-log bracket (x1, y1)-(x2, y2) maps a
+// relative error e of x onto |dlog y / dlog x| e in y.  In FP32, evaluated
+// through ratios (interp5_acc), e is a few 1e-7: the rounding of the row
+// nodes, of L_need (an FP32 interpolation of the shell MFP divided by an FP32
+// uniform) and of the ratios.  A bracket steeper than kIllRow in L, or than
+// kIllE between the two energy rows, could move the draw by more than about
+// 5e-6 relative to FP64, so the draw is redone in FP64.
+constexpr float kIllRow = 12.f;
+constexpr float kIllE = 12.f;
+
+// whether the log-log bracket (x1, y1)-(x2, y2) is steeper than thr
+template <class T>
+__device__ __forceinline__ bool steep(T x1, T x2, T y1, T y2, T thr) {
+    return !(m_abs(m_log(y2 / y1)) <= thr * m_abs(m_log(x2 / x1)));
+}
+
+// interp5_acc that also reports an ill-conditioned bracket (FP32 draws)
+template <class T>
+__device__ __forceinline__ T interp5_checked(T E1, T E2, T S1, T S2, T Ex, T thr, bool* ill) {
+    if (m_abs(E2 - E1) < T(1.0e-6)) { *ill = true; return S1 > S2 ? S1 : S2; }
+    if (Ex == E1) return S1;
+    const T ls = m_log(S2 / S1), le = m_log(E2 / E1);
+    if (!(m_abs(ls) <= thr * m_abs(le))) *ill = true;
+    return S1 * m_exp(ls * (m_log(Ex / E1) / le));
+}
+
 // interpolate_transferred_energy (CS:1968-2045) over one table of cumulative rows.
 // fg >= 0: a proposed bracket position (fraction of the row) from the learned
 // proposal; the search walks from it to the same bracket the bisection finds.
+// ill (FP32 only): set when a bracket is ill-conditioned (kIllRow, kIllE),
+// when a row transfers nothing (the ionisation threshold) or when Ele lies
+// outside the energy grid.  The rows are combined as the reference combines
+// them: the draw on the row above Ele is paired with the energy below it
+// (CS:2027-2040).
 template <class T>
 __device__ T interp_transfer(const T* Eg, int nE, const int* roff, const T* rhw, const T* rL, T Ele, T L_need,
-                             float fg = -1.f, const int* rmono = nullptr) {
+                             float fg = -1.f, const int* rmono = nullptr, bool* ill = nullptr) {
     int iE = find_monoton(Eg, nE, Ele);
     if (iE > 1 && m_abs(Eg[iE - 2] - Ele) < T(1.0e-6)) iE -= 1;
+    // beyond the grid the rows (and the caller's MFP) are extrapolated in log E,
+    // which multiplies the FP32 rounding of the logarithms
+    if (ill && !(Ele >= Eg[0] && Ele <= Eg[nE - 1])) *ill = true;
     auto one = [&](int ie) -> T {
         const int o = roff[ie - 1], len = roff[ie] - o;
         const T* hw = rhw + o;
@@ -633,56 +674,136 @@ __device__ T interp_transfer(const T* Eg, int nE, const int* roff, const T* rhw,
         const int ih = (fg >= 0.f && rmono && rmono[ie - 1])
                            ? find_decreasing_from(L, len, L_need, 1 + (int)(fg * (float)(len - 1)))
                            : find_decreasing(L, len, L_need);
-        if (ih == 1 || ih == len) return hw[ih - 1];
-        return interp<T>(5, L[ih - 1], L[ih], hw[ih - 1], hw[ih], L_need);
+        if (ih == 1 || ih == len) {
+            // beyond the row's first or last node: the FP64 search may land
+            // in the end interval instead, so that interval must be well conditioned
+            if (ill && len > 1) {
+                const int j = ih == 1 ? 1 : len - 1;
+                if (steep(L[j - 1], L[j], hw[j - 1], hw[j], T(kIllRow))) *ill = true;
+            }
+            return hw[ih - 1];
+        }
+        if (ill) return interp5_checked(L[ih - 1], L[ih], hw[ih - 1], hw[ih], L_need, T(kIllRow), ill);
+        return interp5_acc<T>(L[ih - 1], L[ih], hw[ih - 1], hw[ih], L_need);
     };
     T hw1 = one(iE);
     T out = hw1;
     if (iE > 1) {
         iE -= 1;
         T hw2 = one(iE);
-        if (hw1 < T(1.0e-10) || hw2 < T(1.0e-10)) out = interp<T>(1, Eg[iE - 1], Eg[iE], hw1, hw2, Ele);
-        else out = interp<T>(5, Eg[iE - 1], Eg[iE], hw1, hw2, Ele);
+        if (hw1 < T(1.0e-10) || hw2 < T(1.0e-10)) {
+            if (ill) *ill = true;
+            out = interp<T>(1, Eg[iE - 1], Eg[iE], hw1, hw2, Ele);
+        } else if (ill) out = interp5_checked(Eg[iE - 1], Eg[iE], hw1, hw2, Ele, T(kIllE), ill);
+        else out = interp5_acc<T>(Eg[iE - 1], Eg[iE], hw1, hw2, Ele);
     }
     return out;
 }
 
-// Electron_energy_transfer_inelastic (CS:1793-1871), tabulated rows (CS_method = 1)
-template <class T>
-__device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hole, int k, T Ele, T L_tot, T RN,
-                             unsigned& err, float fg = -1.f) {
-    T L_need = L_tot / RN;
-    T Emin = C.Ip[k];
-    if (Emin <= T(1.0e-3)) Emin = T(1.0e-3);
-    T Emax, Mass;
+// the constants of one ionising draw in the arithmetic type U
+template <class U>
+struct XConst {
+    U Ip, Egap, hole_mass, Eplasmon;
+    int plasmon;
+};
+
+// Electron_energy_transfer_inelastic (CS:1793-1871), tabulated rows (CS_method = 1),
+// given L_need = L_tot / RN
+template <class U>
+__device__ U transfer_rows(const XConst<U>& X, const DevTabs<U>& tb, bool hole, int k, U Ele, U L_need,
+                           unsigned& err, float fg, bool* ill) {
+    U Emin = X.Ip;
+    if (Emin <= U(1.0e-3)) Emin = U(1.0e-3);
+    U Emax, Mass;
     if (hole) {
-        Mass = (C.hole_mass >= T(0)) ? C.hole_mass : tb.dosM[dos_find(tb, Ele) - 1];
-        Emax = T(4) * Ele * Mass / ((Mass + T(1)) * (Mass + T(1)));
-    } else Emax = (Ele + Emin) / T(2);
-    if (C.plasmon && Emin == C.Egap) {   // the plasmon energy as upper limit (CS:1833-1839)
-        if (C.Eplasmon >= Emax) Emax = C.Eplasmon;
+        Mass = (X.hole_mass >= U(0)) ? X.hole_mass : tb.dosM[dos_find(tb, Ele) - 1];
+        Emax = U(4) * Ele * Mass / ((Mass + U(1)) * (Mass + U(1)));
+    } else Emax = (Ele + Emin) / U(2);
+    if (X.plasmon && Emin == X.Egap) {   // the plasmon energy as upper limit (CS:1833-1839)
+        if (X.Eplasmon >= Emax) Emax = X.Eplasmon;
         if (Ele < Emax) Emax = Ele;
     }
-    T E = hole ? interp_transfer(tb.hE, tb.nH, tb.hrow_off, tb.hrow_hw, tb.hrow_L, Ele, L_need, fg, tb.hrow_mono)
+    U E = hole ? interp_transfer(tb.hE, tb.nH, tb.hrow_off, tb.hrow_hw, tb.hrow_L, Ele, L_need, fg, tb.hrow_mono, ill)
                : interp_transfer(tb.elE, tb.nE, tb.row_off + (size_t)k * tb.nE, tb.row_hw, tb.row_L, Ele, L_need, fg,
-                                 tb.row_mono + (size_t)k * tb.nE);
+                                 tb.row_mono + (size_t)k * tb.nE, ill);
     if (E < Emin) E = Emin;
     if (E > Emax) E = Emax;
-    if (E < C.Egap) err |= TREKIS_ERR_NEG_TRANSFER;
+    if (E < X.Egap) err |= TREKIS_ERR_NEG_TRANSFER;
     if (m_isnan(E)) E = Emin;
     return E;
 }
 
+// An FP32 ionising draw redone in FP64 on the FP64 rows: the shell MFP, L_need
+// and the inversion, from the same energy and the same random word (RNd).
+// Out of line: it runs for a few per cent of the draws.
+__device__ __noinline__ float transfer_fp64(const McConst<float>& C, const DevTabs<double>& t64, bool hole, int k,
+                                            double Ele, double RNd, unsigned& err) {
+    const double Lt = hole ? nfp1(Tab<double>{t64.hE, t64.hL + (size_t)k * t64.nH, t64.nH}, Ele)
+                           : nfp1(Tab<double>{t64.elE, t64.elL + (size_t)k * t64.nE, t64.nE}, Ele);
+    const XConst<double> X{C.Ipd[k], C.Egap_d, C.hole_mass_d, C.Eplasmon_d, C.plasmon};
+    return (float)transfer_rows<double>(X, t64, hole, k, Ele, Lt / RNd, err, -1.f, nullptr);
+}
+
+// Electron_energy_transfer_inelastic for shell k at energy Ele with the shell's
+// MFP L_tot and the uniform RN (RNd: the same word as an FP64 draw); *nredo
+// (if given) counts the draws redone in FP64
+template <class T>
+__device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hole, int k, T Ele, T L_tot, T RN,
+                             double RNd, unsigned& err, float fg = -1.f, unsigned long long* nredo = nullptr) {
+    const XConst<T> X{C.Ip[k], C.Egap, C.hole_mass, C.Eplasmon, C.plasmon};
+    if constexpr (sizeof(T) == 4) {
+        bool ill = false;
+        unsigned e32 = 0;
+        const float E = transfer_rows<float>(X, tb, hole, k, Ele, L_tot / RN, e32, fg, &ill);
+        if (!ill || !tb.alt) { err |= e32; return E; }
+        if (nredo) ++*nredo;
+        return transfer_fp64(C, *tb.alt, hole, k, (double)Ele, RNd, err);
+    } else {
+        (void)RNd; (void)nredo;
+        return transfer_rows<T>(X, tb, hole, k, Ele, L_tot / RN, err, fg, nullptr);
+    }
+}
+
+// The phonon-CDF elastic draw of an FP32 run redone in FP64 (see transfer_fp64)
+__device__ __noinline__ float phonon_fp64(const DevTabs<double>& t64, bool hole, double Eel, double ud) {
+    const double EMFP = hole ? nfp1(Tab<double>{t64.hElastE, t64.hElastL, t64.nHel}, Eel)
+                             : nfp1(Tab<double>{t64.elastE, t64.elastL, t64.nEl}, Eel);
+    double hw = hole ? interp_transfer<double>(t64.hElastE, t64.nHel, t64.herow_off, t64.herow_hw, t64.herow_L, Eel,
+                                               EMFP / ud)
+                     : interp_transfer<double>(t64.elastE, t64.nEl, t64.erow_off, t64.erow_hw, t64.erow_L, Eel,
+                                               EMFP / ud);
+    if (hw >= Eel) hw = Eel;
+    return (float)hw;
+}
+
 // Electron_energy_transfer_elastic with tabulated rows (CS:2285-2428,
 // CS_method 1): L_need = EMFP / RN (EMFP by Next_free_path_1d) inverted on the
-// phonon-CDF cumulative rows, at most the particle's energy
+// phonon-CDF cumulative rows, at most the particle's energy.
+// defer (the hot kernel's FP32 elastic-only events): instead of redoing an
+// ill-conditioned draw in FP64 here, set *defer and return; the event is then
+// redone whole, from the same stream, by the rare-event kernel.
 template <class T, class S>
-__device__ T phonon_transfer(const DevTabs<T>& tb, bool hole, T Eel, S& s) {
+__device__ T phonon_transfer(const DevTabs<T>& tb, bool hole, T Eel, S& s, bool* defer = nullptr,
+                             unsigned long long* nredo = nullptr) {
     const T EMFP = hole ? nfp1(Tab<T>{tb.hElastE, tb.hElastL, tb.nHel}, Eel)
                         : nfp1(Tab<T>{tb.elastE, tb.elastL, tb.nEl}, Eel);
-    const T L_need = EMFP / s.next();
-    T hw = hole ? interp_transfer(tb.hElastE, tb.nHel, tb.herow_off, tb.herow_hw, tb.herow_L, Eel, L_need)
-                : interp_transfer(tb.elastE, tb.nEl, tb.erow_off, tb.erow_hw, tb.erow_L, Eel, L_need);
+    T u;
+    double ud;
+    s.next2(u, ud);
+    const T L_need = EMFP / u;
+    bool ill = false;
+    bool* pill = (sizeof(T) == 4) ? &ill : nullptr;
+    T hw = hole ? interp_transfer(tb.hElastE, tb.nHel, tb.herow_off, tb.herow_hw, tb.herow_L, Eel, L_need, -1.f,
+                                  (const int*)nullptr, pill)
+                : interp_transfer(tb.elastE, tb.nEl, tb.erow_off, tb.erow_hw, tb.erow_L, Eel, L_need, -1.f,
+                                  (const int*)nullptr, pill);
+    if constexpr (sizeof(T) == 4) {
+        if (ill && tb.alt) {
+            if (defer) { *defer = true; return T(0); }
+            if (nredo) ++*nredo;
+            return phonon_fp64(*tb.alt, hole, (double)Eel, ud);
+        }
+    }
     if (hw >= Eel) hw = Eel;
     return hw;
 }
@@ -752,6 +873,29 @@ __device__ __forceinline__ T shi_path(const DevShi<T>& sh, int nb, T E, T lx) {
     return interp5_pre(E1, E2, sh.lE[nb - 2], sh.lE[nb - 1], L1, sh.lpL[nb - 2], sh.lpL[nb - 1], E, lx);
 }
 
+// SHI_energy_transfer's draw on one transfer row (MC:1719-1780): DE[N] lower
+// edges, DI = 1/L (both with logs), Mt the index of Ip, a and b 1/L at Ip and
+// at the row's end; Tot = a + RN (b - a) is inverted in 1/L, log-log
+template <class T>
+__device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* lDI, int N, int Mt, T a, T b, T Ip,
+                               T RN) {
+    if (N < 1) return (double)Ip;
+    const T Tot = (a > T(0) && b > T(0)) ? a + RN * (b - a) : T(1.5e21);
+    int nt;
+    if (Tot < T(1e20)) {
+        int lo = 0, hi = N - 1;
+        while (lo < hi) { int mid = (lo + hi) >> 1; if (DI[mid] < Tot) lo = mid + 1; else hi = mid; }
+        nt = lo + 1;
+    } else nt = Mt;
+    if (nt <= Mt) return (double)Ip;
+    const T E1 = DI[nt - 2], E2 = DI[nt - 1];
+    T r;
+    if (m_abs(E2 - E1) < T(1.0e-6)) r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
+    else if (Tot == E1) r = DE[nt - 2];
+    else r = m_exp(lDE[nt - 2] + (lDE[nt - 1] - lDE[nt - 2]) / (lDI[nt - 1] - lDI[nt - 2]) * (m_log(Tot) - lDI[nt - 2]));
+    return (double)r;
+}
+
 struct ShiEv {  // one SHI collision: the ion state after it and the transfer
     double E, Zeff, t0, Z, dE;
     int k;
@@ -819,35 +963,33 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
             T sum = T(0);
             for (int q = 0; q < C.nsh; ++q) { sum += inv[q]; if (sum >= tot) { k = q; break; } }
         }
-        // SHI_energy_transfer (MC:1719-1780): inverse of the cumulative row at the initial energy
+        // SHI_energy_transfer (MC:1719-1780): inverse of a cumulative transfer row
         double dE;
         {
             const T RN = s.next();
-            const int o0 = sh.d_off[k], N = sh.d_off[k + 1] - o0;
             const T Ip = C.Ip[k];
-            if (N < 1) dE = (double)Ip;
-            else {
-                const int Mt = sh.Mt[k];
-                const T a = sh.invdL_ip[k], b = sh.invL_last[k];
-                const T Tot = (a > T(0) && b > T(0)) ? a + RN * (b - a) : T(1.5e21);
-                int nt;
-                if (Tot < T(1e20)) {
-                    const T* DI = sh.dI + o0;
-                    int lo = 0, hi = N - 1;
-                    while (lo < hi) { int mid = (lo + hi) >> 1; if (DI[mid] < Tot) lo = mid + 1; else hi = mid; }
-                    nt = lo + 1;
-                } else nt = Mt;
-                if (nt > Mt) {
-                    const T* DI = sh.dI + o0;
-                    const T* DE = sh.dE + o0;
-                    const T E1 = DI[nt - 2], E2 = DI[nt - 1];
-                    T r;
-                    if (m_abs(E2 - E1) < T(1.0e-6)) r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
-                    else if (Tot == E1) r = DE[nt - 2];
-                    else r = m_exp(sh.ldE[o0 + nt - 2] + (sh.ldE[o0 + nt - 1] - sh.ldE[o0 + nt - 2]) /
-                                   (sh.ldI[o0 + nt - 1] - sh.ldI[o0 + nt - 2]) * (m_log(Tot) - sh.ldI[o0 + nt - 2]));
-                    dE = (double)r;
-                } else dE = (double)Ip;
+            if (sh.nW == 0) {   // the row at the initial energy (Universal_MC_for_SHI_MAIN.f90:231-238)
+                const int o0 = sh.d_off[k];
+                dE = shi_row_draw(sh.dE + o0, sh.ldE + o0, sh.dI + o0, sh.ldI + o0, sh.d_off[k + 1] - o0, sh.Mt[k],
+                                  sh.invdL_ip[k], sh.invL_last[k], Ip, RN);
+            } else {
+                // the rows of the grid energies around the ion's, combined as
+                // interpolate_transferred_energy combines two rows (CS:1968-2045)
+                int iE = nb;
+                if (iE > 1 && m_abs(sh.sE[iE - 2] - Et) < T(1.0e-6)) iE -= 1;
+                auto row = [&](int node) -> double {
+                    const int q = node < sh.w0 ? 0 : (node >= sh.w0 + sh.nW ? sh.nW - 1 : node - sh.w0);
+                    const int r = k * sh.nW + q, o = sh.wr_off[r];
+                    return shi_row_draw(sh.wE + o, sh.wlE + o, sh.wI + o, sh.wlI + o, sh.wr_off[r + 1] - o, sh.w_Mt[r],
+                                        sh.w_ia[r], sh.w_ib[r], Ip, RN);
+                };
+                const int up = iE - 1, lo = iE - 2;   // 0-based nodes above and below the ion's energy
+                const T d1 = (T)row(up);
+                if (iE > 1 && lo >= sh.w0 && up < sh.w0 + sh.nW) {
+                    const T d2 = (T)row(lo);
+                    dE = (double)((d1 < T(1.0e-10) || d2 < T(1.0e-10)) ? interp<T>(1, sh.sE[lo], sh.sE[up], d1, d2, Et)
+                                                                        : interp5_acc<T>(sh.sE[lo], sh.sE[up], d1, d2, Et));
+                } else dE = (double)d1;
             }
         }
         // next flight with the energy before the loss
@@ -948,7 +1090,9 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ McConst<T
 // kernel): an ionising draw returns false with the particle untouched, and the
 // event is redone from the same stream by the FULL version.  DEFER leaves the
 // tally of the new segment to the caller (p.ti stays the event's grid index).
-template <class T, bool FULL, bool DEFER = false>
+// EL selects the elastic model at compile time (0: the run's, C.elast_cdf;
+// 1: Mott only; 2: phonon CDF only), so a hot kernel carries one model's code.
+template <class T, bool FULL, bool DEFER = false, int EL = 0>
 __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
                                P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc,
                                float fg = -1.f) {
@@ -972,7 +1116,10 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     if (FULL && ionise) {  // impact ionisation
         const int k = which_shell(C, tb.elE, tb.elL, tb.nE, Eel, s.next());
         const T Ish = nfp1(Tab<T>{tb.elE, tb.elL + (size_t)k * tb.nE, tb.nE}, Eel);
-        dE = sample_transfer(C, tb, false, k, Eel, Ish, s.next(), err, fg);
+        T RNt;
+        double RNd;
+        s.next2(RNt, RNd);
+        dE = sample_transfer(C, tb, false, k, Eel, Ish, RNt, RNd, err, fg, nev + 8);
         theta = m_acos((Eel - dE) / m_sqrt(Eel * (Eel - dE)));
         if (m_isnan(theta)) theta = s.next() * pi_<T>();
         phi = T(2) * pi_<T>() * s.next();
@@ -993,7 +1140,11 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
         nev[1]++; nev[7] += 2;
     } else {  // elastic: Mott, or the phonon CDF
-        dE = C.elast_cdf ? phonon_transfer(tb, false, Eel, s) : mott_transfer(C, Eel, T(1), s);
+        if (EL == 2 || (EL == 0 && C.elast_cdf)) {
+            bool defer = false;
+            dE = phonon_transfer(tb, false, Eel, s, FULL ? nullptr : &defer, nev + 8);
+            if (!FULL && defer) { p.ord = ord; return false; }   // redone by the rare kernel
+        } else dE = mott_transfer(C, Eel, T(1), s);
         angles_lat(C, Eel, dE, T(1), s, theta, phi, elastic_uniform(x, T(1) / I, Em));
         const int i = ti0;  // the interval t_{i-1} <= t < t_i
         const int j = rbin(C, m_sqrt(X * X + Y * Y));
@@ -1036,8 +1187,8 @@ __device__ T check_hole(const DevTabs<T>& tb, T Eel, T& dE, P<T>* el) {
 }
 
 // One hole event; FULL=false compiles only valence-hole elastic scattering;
-// DEFER as for electron_event.
-template <class T, bool FULL, bool DEFER = false>
+// DEFER and EL as for electron_event.
+template <class T, bool FULL, bool DEFER = false, int EL = 0>
 __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& h,
                            unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc, float fg = -1.f) {
     const uint32_t ord = h.ord;
@@ -1062,7 +1213,10 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         if (FULL && ionise) {
             const int k = which_shell(C, tb.hE, tb.hL, tb.nH, Eel, s.next());
             const T HIs = nfp1(Tab<T>{tb.hE, tb.hL + (size_t)k * tb.nH, tb.nH}, Eel);
-            dE = sample_transfer(C, tb, true, k, Eel, HIs, s.next(), err, fg);
+            T RNt;
+            double RNd;
+            s.next2(RNt, RNd);
+            dE = sample_transfer(C, tb, true, k, Eel, HIs, RNt, RNd, err, fg, nev + 8);
             // Update_holes_angles_el (MC:1142-1168)
             // masses in kg as the reference writes them (FP64); in electron
             // masses for FP32, where (Mh+me)^2 would underflow
@@ -1095,7 +1249,11 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
             nev[3]++; nev[7] += 2;
         } else {
-            dE = C.elast_cdf ? phonon_transfer(tb, true, Eel, s) : mott_transfer(C, Eel, hm, s);
+            if (EL == 2 || (EL == 0 && C.elast_cdf)) {
+                bool defer = false;
+                dE = phonon_transfer(tb, true, Eel, s, FULL ? nullptr : &defer, nev + 8);
+                if (!FULL && defer) { h.ord = ord; return false; }   // redone by the rare kernel
+            } else dE = mott_transfer(C, Eel, hm, s);
             // no ionisation channel (HI >= 1e15): RN chose nothing and is reused whole
             angles_lat(C, Eel, dE, hm, s, th1, ph1, HI < T(1e15) ? elastic_uniform(x, T(1) / HI, HE) : RN);
             Eh = check_hole(tb, Eel, dE, (P<T>*)nullptr);
@@ -1248,13 +1406,14 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
 }
 
 // Hot kernel of a wavefront step, one per particle kind (electrons, mobile
-// valence holes) so each carries only its own event code: every particle
+// valence holes) and elastic model (PHON: phonon-CDF rows, else Mott), so each
+// carries only its own event code: every particle
 // runs up to K elastic collisions.  A particle whose next event ionises goes
 // to a side queue; survivors go to the next generation's queue.  The warps
 // iterate together (a lane whose particle is done idles) so that segments
 // reaching a grid time can be parked in the warp's ring and tallied 32 at a
 // time; the tallies are integer sums, so the order does not matter.
-template <class T, bool IS_E>
+template <class T, bool IS_E, bool PHON>
 __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<T> C,
                                              const __grid_constant__ DevTabs<T> tb, const __grid_constant__ PQ<T> in,
                                              int n, const __grid_constant__ Out<T> o, const __grid_constant__ PQ<T> side,
@@ -1270,7 +1429,7 @@ __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<
         p.ti = tbin(C, p.tn);
     }
     unsigned err = 0;
-    unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long nev[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     LatAcc lat;
     MfpCache<T> mc;
     bool diverted = false;
@@ -1283,8 +1442,8 @@ __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<
         int ia = 0, ib = -1;
         if (act) {
             bool done;
-            if constexpr (IS_E) done = electron_event<T, false, true>(C, tb, tal, o, p, err, lat, nev, mc);
-            else done = hole_event<T, false, true>(C, tb, tal, o, p, err, lat, nev, mc);
+            if constexpr (IS_E) done = electron_event<T, false, true, PHON ? 2 : 1>(C, tb, tal, o, p, err, lat, nev, mc);
+            else done = hole_event<T, false, true, PHON ? 2 : 1>(C, tb, tal, o, p, err, lat, nev, mc);
             if (!done) { diverted = true; act = false; }
             else {
                 ia = p.ti;
@@ -1341,7 +1500,7 @@ __global__ void __launch_bounds__(128) k_rare(const __grid_constant__ McConst<T>
     const int n_e = o.ctr->n_out[Q_EINEL], n_h = o.ctr->n_out[Q_HINEL];
     const int total = n_e + n_h + n_deep + n_ph;
     unsigned err = 0;
-    unsigned long long nev[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    unsigned long long nev[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
         P<T> p;
         LatAcc lat;
@@ -1361,7 +1520,7 @@ __global__ void __launch_bounds__(128) k_rare(const __grid_constant__ McConst<T>
         lat.flush(tal);
         push(C, tal, o, kind, p);
     }
-    for (int q = 1; q < 8; ++q)
+    for (int q = 1; q < 9; ++q)
         if (nev[q]) atomicAdd(&o.ctr->ev[q], nev[q]);
     if (err) atomicOr(&o.ctr->err_bits, err);
 }
@@ -1503,11 +1662,18 @@ void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, c
         cudaEventRecord(fk->fork, s);
         cudaStreamWaitEvent(fk->s2, fk->fork, 0);
     }
-    if (n_in[Q_E] > 0)
-        k_hot<T, true><<<(n_in[Q_E] + bs - 1) / bs, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
-    if (n_in[Q_HVB] > 0)
-        k_hot<T, false><<<(n_in[Q_HVB] + bs - 1) / bs, bs, 0, two ? fk->s2 : s>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o,
-                                                                                h_inel, tal, K);
+    // one hot kernel per particle kind and elastic model
+    if (n_in[Q_E] > 0) {
+        const unsigned g = (n_in[Q_E] + bs - 1) / bs;
+        if (C.elast_cdf) k_hot<T, true, true><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+        else k_hot<T, true, false><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+    }
+    if (n_in[Q_HVB] > 0) {
+        const unsigned g = (n_in[Q_HVB] + bs - 1) / bs;
+        cudaStream_t sh = two ? fk->s2 : s;
+        if (C.elast_cdf) k_hot<T, false, true><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+        else k_hot<T, false, false><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+    }
     if (two) {
         cudaEventRecord(fk->join, fk->s2);
         cudaStreamWaitEvent(s, fk->join, 0);
@@ -1539,6 +1705,7 @@ struct FixedUniform {   // every draw returns u
     double u;
     __device__ __forceinline__ T next() { return (T)u; }
     __device__ __forceinline__ void next_pair(float& a, float& b) { a = (float)u; b = (float)(1.0 - u); }
+    __device__ __forceinline__ void next2(T& a, double& b) { a = (T)u; b = u; }
 };
 template <class T>
 __global__ void k_probe(const __grid_constant__ McConst<T> C, const __grid_constant__ DevTabs<T> tb, int kind,
@@ -1556,7 +1723,7 @@ __global__ void k_probe(const __grid_constant__ McConst<T> C, const __grid_const
         const int kk = hole ? C.vb : k;
         const T L = hole ? nfp1(Tab<T>{tb.hE, tb.hL + (size_t)kk * tb.nH, tb.nH}, E)
                          : nfp1(Tab<T>{tb.elE, tb.elL + (size_t)kk * tb.nE, tb.nE}, E);
-        r = sample_transfer(C, tb, hole, kk, E, L, u, err);
+        r = sample_transfer(C, tb, hole, kk, E, L, u, uin[i], err);
         break;
     }
     case 2: case 3: {   // total inelastic / elastic electron MFP as the track loop evaluates them

@@ -49,6 +49,8 @@ struct McConst {
     T mott_iM[TREKIS_MAX_ATOMS], mott_iM2[TREKIS_MAX_ATOMS], mott_wM[TREKIS_MAX_ATOMS];
     T inv_mec2;
     T Et_lat;           // Mtarget c^2 / e [eV]
+    // FP64 values of the transfer draw's constants, for FP32 draws redone in FP64
+    double Egap_d, hole_mass_d, Eplasmon_d;
     uint32_t rk[20];    // Philox round keys of seed
 };
 
@@ -117,7 +119,8 @@ struct Ctrs {
     int overflow;
     unsigned int err_bits;
     int first_bad_it;
-    unsigned long long ev[8];     // shi, el inel, el elastic, hole, auger, radiative, photon abs, particles
+    unsigned long long ev[9];     // shi, el inel, el elastic, hole, auger, radiative, photon abs, particles,
+                                  // FP32 transfer draws redone in FP64
     unsigned long long shi_slots; // SHI record slots handed out (some unused, marked it = -1)
 };
 
@@ -210,9 +213,11 @@ inline void fill_const(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt
     {
         const double Eg = m.atoms[0].Ip[m.atoms[0].N_shl - 1];
         C.plasmon = m.plasmon_Emax ? 1 : 0;
-        C.Eplasmon = (T)std::sqrt(m.N_VB_el * m.At_Dens * 1e6 * kH * kH / (kMe * kE0) + Eg * Eg);
+        C.Eplasmon_d = std::sqrt(m.N_VB_el * m.At_Dens * 1e6 * kH * kH / (kMe * kE0) + Eg * Eg);
+        C.Eplasmon = (T)C.Eplasmon_d;
+        C.Egap_d = Eg;
     }
-    C.cut_off = (T)m.cut_off; C.hole_mass = (T)m.hole_mass; C.Layer = m.Layer;
+    C.cut_off = (T)m.cut_off; C.hole_mass = (T)m.hole_mass; C.hole_mass_d = m.hole_mass; C.Layer = m.Layer;
     C.ion_Z = t->ion.Zat; C.ion_kind_zeff = t->ion.Kind_Zeff; C.ion_mass_p = t->ion.Mass; C.MSHI = kMp * t->ion.Mass;
     C.ion_E0 = t->ion.E; C.ion_fixed_zeff = t->ion.fixed_Zeff; C.Zt = zs / Psum;
     C.Tim = (T)cfg.Tim; C.Nt = Nt; C.NR = cfg.N_R; C.seed = cfg.seed;

@@ -287,7 +287,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     const int rare_blocks = 2 * 152;
     int B = cfg.iterations_per_batch > 0 ? cfg.iterations_per_batch : std::min(cfg.NMC, 256);
     const bool tune_batch = cfg.iterations_per_batch <= 0;
-    uint64_t steps = 0, launches = 1, ev_tot[8] = {0}, peak_all = 0;   // the grid hints
+    uint64_t steps = 0, launches = 1, ev_tot[9] = {0}, peak_all = 0;   // the grid hints
     uint64_t h2d = sizeof(T) * (Nt + NR) + 8 * NR + sizeof(int) * nsh, d2h = 0;
     unsigned err_bits = 0;
     Ctrs hc;
@@ -338,7 +338,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
             continue;
         }
         steps += bsteps;
-        for (int q = 0; q < 8; ++q) ev_tot[q] += hc.ev[q];
+        for (int q = 0; q < 9; ++q) ev_tot[q] += hc.ev[q];
         ev_tot[7] += 2 * hc.ev[0];
         err_bits |= hc.err_bits;
         peak_all = std::max<uint64_t>(peak_all, (uint64_t)peak);
@@ -387,6 +387,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
         st->batch_iterations = B;
         st->h2d_bytes += h2d;
         st->d2h_bytes += d2h;
+        st->n_fp64_redraws += ev_tot[8];
     }
     return TREKIS_OK;
 }

@@ -64,12 +64,13 @@ __device__ double d_imewq(const BuildMat* __restrict__ bm, int sh, double hw, do
 }
 
 // Diff_cross_section (Cross_sections.f90:2217-2282)
-__device__ double d_diff_cs(const BuildMat* __restrict__ bm, int sh, double Ele, double hw, double Mass) {
+__device__ double d_diff_cs(const BuildMat* __restrict__ bm, int sh, double Ele, double hw, double Mass, int& nq) {
     const double pre = sqrt(2.0 * Mass * kMe) / kH;
     double qmin, qmax;
     if (hw > Ele) { qmin = pre * sqrt(Ele); qmax = qmin; }
     else { qmin = pre * (sqrt(Ele) - sqrt(Ele - hw)); qmax = pre * (sqrt(Ele) + sqrt(Ele - hw)); }
     double dLs = 0.0, hq = qmin, dLs0 = 0.0;
+    nq = 0;
     while (hq < qmax) {
         double dq = hq / 100.0;
         double t1 = d_imewq(bm, sh, hw, hq + dq / 2.0);
@@ -77,6 +78,7 @@ __device__ double d_diff_cs(const BuildMat* __restrict__ bm, int sh, double Ele,
         dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) / hq;
         dLs0 = dL;
         hq = hq + dq;
+        ++nq;
     }
     double T = (bm->temp > 0.0) ? 1.0 / (1.0 - exp(-hw / bm->temp * kKb)) : 1.0;
     return 1.0 / (kPi * kA0 * Ele) * dLs * T;
@@ -185,8 +187,9 @@ __device__ double d_screening(const BuildMat* __restrict__ bm, double Ee, double
 // 1/q (CDF_elast_Zeff 0 or 1; the target charge enters as Zeff^2 in Tot_EMFP)
 // or (Z/eps)^2 / q (2, 3).  The q loop is bounded; qmin = 0 (hw below the
 // resolution of sqrt(Ele)) contributes nothing.
-__device__ double d_phonon_diff(const BuildMat* __restrict__ bm, double Ele, double hw, double Mass) {
+__device__ double d_phonon_diff(const BuildMat* __restrict__ bm, double Ele, double hw, double Mass, int& nq) {
     const double eps = 1.0e-12, pre = sqrt(2.0 * Mass * kMe) / kH;
+    nq = 0;
     if (fabs(hw) < eps) return 1.31e30;
     const double qmin = (hw > Ele - eps) ? pre * sqrt(Ele) : pre * (sqrt(Ele) - sqrt(fabs(Ele - hw)));
     const double qmax = pre * (sqrt(Ele) + sqrt(fabs(Ele - hw)));
@@ -200,13 +203,16 @@ __device__ double d_phonon_diff(const BuildMat* __restrict__ bm, double Ele, dou
         dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) * (scr / hq);
         dLs0 = dL;
         hq = hq + dq;
+        ++nq;
     }
     if (bm->temp > 1.0e-6) return 1.0 / (kPi * kA0 * Ele) * dLs / (1.0 - exp(-hw / bm->temp * kKb));
     return 1.0 / (kPi * kA0 * Ele) * dLs;
 }
 
 // SHI_Diff_cross_section (Cross_sections.f90:2683-2744)
-__device__ double d_shi_diff(const BuildMat* __restrict__ bm, int sh, double Ele, double MSHI, double Emax, double hw) {
+__device__ double d_shi_diff(const BuildMat* __restrict__ bm, int sh, double Ele, double MSHI, double Emax, double hw,
+                             int& nq) {
+    nq = 0;
     double qmin = (Ele > 0.0) ? hw / kH / sqrt(2.0 * Ele / MSHI) : 0.0;
     if (!(Emax > 0.0)) return 0.0;
     double qmax = sqrt(2.0 * kMe) / kH * sqrt(Emax);
@@ -218,6 +224,7 @@ __device__ double d_shi_diff(const BuildMat* __restrict__ bm, int sh, double Ele
         dLs = dLs + dq / 6.0 * (dLs0 + 4.0 * t1 + dL) / hq;
         dLs0 = dL;
         hq = hq + dq;
+        ++nq;
     }
     double T = (bm->temp > 0.0) ? 1.0 / (1.0 - exp(-hw / bm->temp * kKb)) : 1.0;
     return dLs * T;
@@ -251,25 +258,46 @@ __global__ void k_points(const Job* __restrict__ jobs, int nj, double* __restric
     }
 }
 
+// the q steps and oscillator terms of a warp's points, added to cnt[0], cnt[1]
+__device__ __forceinline__ void count_work(unsigned long long* cnt, int nq, int terms_per_step) {
+    const unsigned act = __activemask();
+    const unsigned q = __reduce_add_sync(act, (unsigned)nq);
+    const unsigned t = __reduce_add_sync(act, (unsigned)(nq * terms_per_step));
+    if ((int)(threadIdx.x & 31) == __ffs(act) - 1) {
+        atomicAdd(cnt, (unsigned long long)q);
+        atomicAdd(cnt + 1, (unsigned long long)t);
+    }
+}
+
 // electron/hole and SHI points [0, np)
 __global__ void k_diff(const BuildMat* __restrict__ bm, const Job* __restrict__ jobs, const double* __restrict__ pts,
-                       const int* __restrict__ pjob, double* __restrict__ val, int64_t np) {
+                       const int* __restrict__ pjob, double* __restrict__ val, int64_t np,
+                       unsigned long long* __restrict__ cnt) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     const Job& J = jobs[pjob[p]];
-    val[p] = (J.kind == 0) ? d_diff_cs(bm, J.sh, J.Ele, pts[p], J.Mass)
-                           : d_shi_diff(bm, J.sh, J.Ele, J.Mass, J.Emax, pts[p]);
+    int nq = 0;
+    val[p] = (J.kind == 0) ? d_diff_cs(bm, J.sh, J.Ele, pts[p], J.Mass, nq)
+                           : d_shi_diff(bm, J.sh, J.Ele, J.Mass, J.Emax, pts[p], nq);
+    count_work(cnt, nq, 2 * bm->nosc[J.sh]);
 }
 
 // phonon-CDF elastic points [p0, np), the last jobs of the build; a kernel of
 // their own keeps the screening's registers out of k_diff
 __global__ void k_diff_phonon(const BuildMat* __restrict__ bm, const Job* __restrict__ jobs,
                               const double* __restrict__ pts, const int* __restrict__ pjob,
-                              double* __restrict__ val, int64_t p0, int64_t np) {
+                              double* __restrict__ val, int64_t p0, int64_t np, unsigned long long* __restrict__ cnt) {
     int64_t p = p0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     const Job& J = jobs[pjob[p]];
-    val[p] = d_phonon_diff(bm, J.Ele, pts[p], J.Mass);
+    int nq = 0;
+    val[p] = d_phonon_diff(bm, J.Ele, pts[p], J.Mass, nq);
+    // the loss function twice per step, plus the CDFs the screening evaluates once per step
+    int scr = 0;
+    if (bm->elast_zeff == 2) scr = bm->nosc[bm->scr_vb];
+    else if (bm->elast_zeff == 3)
+        for (int i = 0; i < bm->scr_nat; ++i) scr += bm->nosc[bm->scr_k[i]];
+    count_work(cnt, nq, 2 * bm->n_ph + scr);
 }
 
 // Simpson accumulation in the reference's order; writes (Sigma, dEdx) and rows
@@ -486,10 +514,10 @@ static double mott_sigma(int Zi, double Ee) {
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st) {
     const trekis_material& m = T->mat;
     struct Events {   // released on every return
-        cudaEvent_t a = nullptr, b = nullptr;
-        ~Events() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); }
+        cudaEvent_t a = nullptr, b = nullptr, c = nullptr, d = nullptr;
+        ~Events() { for (cudaEvent_t e : {a, b, c, d}) if (e) cudaEventDestroy(e); }
     } ev;
-    CK(cudaEventCreate(&ev.a)); CK(cudaEventCreate(&ev.b));
+    CK(cudaEventCreate(&ev.a)); CK(cudaEventCreate(&ev.b)); CK(cudaEventCreate(&ev.c)); CK(cudaEventCreate(&ev.d));
     CK(cudaEventRecord(ev.a));
     // compact shells
     T->nsh = 0;
@@ -591,7 +619,12 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
             if (in) shi_nodes.push_back(i);
         }
         for (int k = 0; k < nsh; ++k)
-            for (int i : shi_nodes) { Job J{}; limits_shi(T, T->atom_of[k], T->shell_of[k], gS[i], J); J.sh = k; J.store = 0; jobs.push_back(J); }
+            for (int i : shi_nodes) {
+                Job J{};
+                limits_shi(T, T->atom_of[k], T->shell_of[k], gS[i], J);
+                J.sh = k; J.store = cfg.shi_rows_by_energy ? 2 : 0;   // the integral is the same; keep its row or not
+                jobs.push_back(J);
+            }
     }
     const size_t j_d0 = jobs.size();
     if (cfg.build_shi)
@@ -646,18 +679,23 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     double* d_rhw = (double*)scratch.alloc(8 * std::max<int64_t>(nr, 1));
     double* d_rL = (double*)scratch.alloc(8 * std::max<int64_t>(nr, 1));
     double* d_rX = (double*)scratch.alloc(8 * std::max<int64_t>(nr, 1));
-    if (!d_pts || !d_pj || !d_val || !d_sig || !d_ded || !d_rhw || !d_rL || !d_rX) return TREKIS_ENOMEM;
+    unsigned long long* d_cnt = (unsigned long long*)scratch.alloc(16);
+    if (!d_pts || !d_pj || !d_val || !d_sig || !d_ded || !d_rhw || !d_rL || !d_rX || !d_cnt) return TREKIS_ENOMEM;
+    CK(cudaMemset(d_cnt, 0, 16));
     k_points<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj, d_pts, d_pj);
     CK(cudaGetLastError());
     const int64_t np_el = (j_el0 < jobs.size()) ? jobs[j_el0].pt_off : np;   // phonon jobs come last
+    CK(cudaEventRecord(ev.c));
     if (np_el > 0) {
-        k_diff<<<(unsigned)((np_el + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np_el);
+        k_diff<<<(unsigned)((np_el + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np_el, d_cnt);
         CK(cudaGetLastError());
     }
     if (np > np_el) {
-        k_diff_phonon<<<(unsigned)((np - np_el + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np_el, np);
+        k_diff_phonon<<<(unsigned)((np - np_el + bs - 1) / bs), bs>>>(d_bm, d_jobs, d_pts, d_pj, d_val, np_el, np,
+                                                                      d_cnt);
         CK(cudaGetLastError());
     }
+    CK(cudaEventRecord(ev.d));
     k_accum<<<(nj + bs - 1) / bs, bs>>>(d_jobs, nj, d_val, d_sig, d_ded, d_rhw, d_rL, d_rX);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ev.b));
@@ -674,9 +712,17 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
     CK(cudaEventElapsedTime(&ms, ev.a, ev.b));
     T->build_ms = ms;
     T->build_points = (uint64_t)np;
+    CK(cudaEventElapsedTime(&ms, ev.c, ev.d));
+    T->integral_ms = ms;
+    T->build_jobs = (uint64_t)nj;
+    unsigned long long cnt[2];
+    CK(cudaMemcpy(cnt, d_cnt, 16, cudaMemcpyDeviceToHost));
+    T->build_q_steps = cnt[0];
+    T->build_osc_terms = cnt[1];
 
     // host mirror
     T->el.assign(nsh, {}); T->hole.assign(nsh, {}); T->shi.assign(nsh, {}); T->dsde.assign(nsh, {});
+    T->dsde_E.assign(nsh, {});
     T->phot.assign(nsh, {}); T->el_rows.assign(nsh, {});
     for (int k = 0; k < nsh; ++k) {
         HTab& t = T->el[k];
@@ -710,12 +756,18 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
                 t.L[shi_nodes[q]] = L > 1e30 ? 1e30 : L;
                 t.dEdx[shi_nodes[q]] = ded[j_s0 + (size_t)k * nn + q];
             }
-            const Job& J = jobs[j_d0 + k];
-            HTab& d = T->dsde[k];
-            d.E.assign(rhw.begin() + J.row_off, rhw.begin() + J.row_off + J.row_len);
-            d.L.assign(rL.begin() + J.row_off, rL.begin() + J.row_off + J.row_len);
-            d.dEdx.assign(rX.begin() + J.row_off, rX.begin() + J.row_off + J.row_len);
+            auto row_of = [&](const Job& J, HTab& d) {
+                d.E.assign(rhw.begin() + J.row_off, rhw.begin() + J.row_off + J.row_len);
+                d.L.assign(rL.begin() + J.row_off, rL.begin() + J.row_off + J.row_len);
+                d.dEdx.assign(rX.begin() + J.row_off, rX.begin() + J.row_off + J.row_len);
+            };
+            row_of(jobs[j_d0 + k], T->dsde[k]);
+            if (cfg.shi_rows_by_energy) {
+                T->dsde_E[k].assign(nn, {});
+                for (int q = 0; q < nn; ++q) row_of(jobs[j_s0 + (size_t)k * nn + q], T->dsde_E[k][q]);
+            }
         }
+        T->shi_row_nodes = cfg.shi_rows_by_energy ? shi_nodes : std::vector<int>();
         T->has_shi = true;
         T->shi_full = cfg.shi_E_window_lo <= 0 && cfg.shi_E_window_hi <= 0;
     }

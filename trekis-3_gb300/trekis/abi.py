@@ -14,7 +14,7 @@ MAX_OSC = 16
 MAX_PH_OSC = 8
 
 TAB_EL_INEL, TAB_EL_ELAST, TAB_H_INEL, TAB_H_ELAST, TAB_PHOT, TAB_SHI, TAB_SHI_DSDE = range(7)
-ROW_EL_INEL, ROW_H_INEL, ROW_EL_ELAST, ROW_H_ELAST = range(4)
+ROW_EL_INEL, ROW_H_INEL, ROW_EL_ELAST, ROW_H_ELAST, ROW_SHI = range(5)
 
 NOALLOC_SCRATCH_BYTES = 64 << 20   # TREKIS_NOALLOC_SCRATCH_BYTES
 
@@ -30,7 +30,7 @@ ERR_BITS = {
     1 << 6: "queue full", 1 << 7: "photon negative energy",
 }
 
-ABI_VERSION = 4   # TREKIS_ABI_VERSION of the header these structs mirror
+ABI_VERSION = 5   # TREKIS_ABI_VERSION of the header these structs mirror
 
 _S = MAX_SHELLS
 _O = MAX_OSC
@@ -70,10 +70,16 @@ class Ion(C.Structure):
     ]
 
 
+class BuildStats(C.Structure):
+    _fields_ = [("build_ms", C.c_double), ("integral_ms", C.c_double), ("jobs", C.c_uint64),
+                ("points", C.c_uint64), ("q_steps", C.c_uint64), ("osc_terms", C.c_uint64)]
+
+
 class TableCfg(C.Structure):
     _fields_ = [
         ("build_shi", C.c_int32), ("build_photon", C.c_int32),
         ("shi_E_window_lo", C.c_double), ("shi_E_window_hi", C.c_double),
+        ("shi_rows_by_energy", C.c_int32), ("pad_", C.c_int32),
     ]
 
 
@@ -142,7 +148,7 @@ class Status(C.Structure):
         ("n_steps", C.c_uint64), ("device_ms", C.c_double), ("n_kernel_launches", C.c_uint64),
         ("step_ms", C.c_double), ("step_events", C.c_uint64), ("step_launches", C.c_uint64),
         ("peak_queue", C.c_uint64), ("batch_iterations", C.c_int32), ("pad_", C.c_int32),
-        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+        ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64), ("n_fp64_redraws", C.c_uint64),
     ]
 
     @classmethod
@@ -163,6 +169,7 @@ SIGNATURES = {
     "trekis_tables_build": (C.c_int32, [C.POINTER(Material), C.POINTER(Ion), C.POINTER(TableCfg),
                                         C.POINTER(C.c_void_p), C.POINTER(Status)]),
     "trekis_tables_free": (None, [C.c_void_p]),
+    "trekis_tables_stats": (C.c_int32, [C.c_void_p, C.POINTER(BuildStats)]),
     "trekis_tables_trim": (None, [C.c_void_p]),
     "trekis_tables_size": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
     "trekis_tables_export": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _DP, _DP, _DP, C.c_int64]),

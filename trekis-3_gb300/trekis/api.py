@@ -127,14 +127,16 @@ def run_cfg(w, opt, NMC=None):
 class Tables:
     """GPU-built cross-section tables of one material and ion."""
 
-    def __init__(self, w, build_photon=None, shi_window=True, lib=None):
+    def __init__(self, w, build_photon=None, shi_window=True, lib=None, shi_rows_by_energy=False):
         self.lib = lib or abi.load()
         self.w = w
         self.mat = w.material.to_c()
         self.ion = ion_struct(w)
         bp = w.material.include_photons if build_photon is None else build_photon
         lo, hi = (w.ion_E * 0.5, w.ion_E * 1.01) if shi_window else (0.0, 0.0)
-        tc = abi.TableCfg(build_shi=1, build_photon=int(bp), shi_E_window_lo=lo, shi_E_window_hi=hi)
+        tc = abi.TableCfg(build_shi=1, build_photon=int(bp), shi_E_window_lo=lo, shi_E_window_hi=hi,
+                          shi_rows_by_energy=int(shi_rows_by_energy))
+        self.tcfg = tc
         self.h = C.c_void_p()
         self.status = abi.Status.fresh()
         rc = self.lib.trekis_tables_build(self.mat.ref(), C.byref(self.ion), C.byref(tc), C.byref(self.h),
