@@ -143,6 +143,113 @@ def profile_issue():
     return out
 
 
+def fixture(name):
+    """Committed batch statistics of the FP64 oracle on a workload (tests/golden)."""
+    p = ROOT / "tests" / "golden" / f"parity_{name}.npz"
+    return np.load(p) if p.exists() else None
+
+
+def three_sigma(mg, vg, nzg, Bg, mr, vr, nzr, Br):
+    """Fraction of live (time, radius) bins whose batch means agree within three
+    combined standard errors, chi^2 per live bin, live bins.  v*: variances of
+    the batch means; a bin is live when at least half of the batches of both
+    sides saw a particle in it."""
+    live = (nzg >= Bg / 2) & (nzr >= Br / 2)
+    se = np.sqrt(vg / Bg + vr / Br)
+    live &= se > 0
+    z = (mg[live] - mr[live]) / se[live]
+    return float(np.mean(np.abs(z) <= 3.0)), float(np.mean(z * z)), int(live.sum())
+
+
+def parity_of(snaps, iters, name="cfg1"):
+    """The timed job's radial electron density and energy density (one batch
+    per step, [step][t, R] per-iteration means) against the oracle fixture."""
+    fx = fixture(name)
+    if fx is None or len(snaps) < 2:
+        return None
+    out = {"reference": f"FP64 oracle, {int(fx['batches'])} batches x {int(fx['per_batch'])} iterations "
+                        f"(tests/golden/parity_{name}.npz)",
+           "gpu": f"{len(snaps)} timed steps x {iters} iterations, FP32",
+           "criterion": ">= 0.99 of live bins within 3 sigma"}
+    fr = []
+    for k in ("Out_ne", "Out_Ee"):
+        x = np.array([s_[k] for s_ in snaps])
+        f, c2, nl = three_sigma(x.mean(0), x.var(0, ddof=1), (x != 0).sum(0), len(snaps),
+                                fx[f"{k}_mean"].astype(np.float64), fx[f"{k}_var"].astype(np.float64),
+                                fx[f"{k}_nz"], int(fx["batches"]))
+        out[k] = {"frac_3sigma": f, "chi2_per_bin": c2, "live_bins": nl}
+        fr.append(f)
+    out["frac_3sigma"] = min(fr)
+    return out
+
+
+def fp64_peak(dev):
+    """Measured FP64 rate of this GPU: best of 5 float64 4096^3 matmuls (cuBLAS DGEMM)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best / 1e3) / 1e9       # GFLOP/s
+
+
+def profile_value(name, key):
+    """A machine-readable figure (key = value line) of a committed ncu summary."""
+    try:
+        for line in open(ROOT / "profiles" / name):
+            k, _, v = line.partition("=")
+            if v and k.strip() == key:
+                return float(v)
+    except Exception:
+        pass
+    return None
+
+
+def table_build(t, dev):
+    """FP64 table build of the bench's tables: the omega-q integral kernels'
+    time, their FP64 flops (oscillator terms counted by the kernels x the FP64
+    flops per term ncu measured) and the measured FP64 peak."""
+    from trekis import abi
+    s = abi.BuildStats()
+    abi.check(t.lib.trekis_tables_stats(t.h, C.byref(s)), t.lib)
+    fpt = profile_value("k_diff_cfg1_tables.md", "fp64_flops_per_osc_term")
+    pk = fp64_peak(dev)
+    out = {"build_ms": s.build_ms, "integral_ms": s.integral_ms, "jobs": s.jobs, "points": s.points,
+           "q_steps": s.q_steps, "osc_terms": s.osc_terms, "fp64_peak_gflops": pk,
+           "fp64_peak_source": "measured here: best of 5 float64 4096^3 torch.matmul (cuBLAS DGEMM)"}
+    if fpt:
+        gf = s.osc_terms * fpt / (s.integral_ms / 1e3) / 1e9
+        out.update({"fp64_flops_per_osc_term": fpt, "fp64_gflops": gf, "frac_of_fp64_peak": gf / pk,
+                    "flops_source": "profiles/k_diff_cfg1_tables.md (ncu DFMA/DADD/DMUL counts)"})
+    return out
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
+
+
 def alg_bytes_per_event(st, n_shells):
     """Algorithmic bytes per collision: 96 B particle state read+write, 64 B
     for two total-MFP lookups (2 nodes x (E,L) x 2 energies), and for events
@@ -208,11 +315,17 @@ def run_gpu(args):
     tot_ev = tot_ms = step_ms = step_ev = 0.0
     launches = 0
     sts = []
+    snaps = []          # per-step electron density and energy density (parity with the oracle)
+    prev = {k: dev_arrays[k].clone() for k in ("Out_ne", "Out_Ee")}
     with clk:
         torch.cuda.synchronize()
         for i in range(args.steps):
             st, _ = step(args.warmup + i)
             sts.append(st)
+            # outside the library's CUDA-event timing: this step's sums
+            cur = {k: dev_arrays[k].clone() for k in prev}
+            snaps.append({k: ((cur[k] - prev[k]) / iters).cpu().numpy().reshape(NR, Nt).T for k in cur})
+            prev = cur
             tot_ev += st.n_events
             tot_ms += st.device_ms
             step_ms += st.step_ms
@@ -272,28 +385,48 @@ def run_gpu(args):
             setattr(merged, f, getattr(merged, f) + getattr(st, f))
     bpe = alg_bytes_per_event(merged, n_sh)
     launches_step = sum(s.step_launches for s in sts)
-    achieved = bpe * step_ev / (step_ms / 1e3) / 1e9           # GB/s over the step kernels
+    ev_rate = step_ev / (step_ms / 1e3)                         # collisions/s inside the step kernels
+    achieved = bpe * ev_rate / 1e9                              # GB/s of algorithmic bytes
     dram_per_event = profile_traffic()
     traffic = dram_per_event * (step_ev / max(launches_step, 1)) if dram_per_event else None
-    roof = {"bound": "hbm", "kernel": "k_hot<float> + k_rare<float> (wavefront step)", "achieved": achieved,
-            "peak": hbm if hbm else 6800.0, "peak_source": "measured" if hbm else "fallback",
-            "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "traffic": traffic,
-            "bytes_per_event": bpe, "step_kernel_ms": step_ms, "step_kernel_launches": launches_step,
-            "events_per_step_kernel_s": step_ev / (step_ms / 1e3), "issue": profile_issue()}
+    hbm_roof = {"achieved": achieved, "peak": hbm if hbm else 6800.0, "peak_source": "measured" if hbm else "fallback",
+                "unit": "GB/s", "frac": achieved / (hbm if hbm else 6800.0), "bytes_per_event": bpe,
+                "note": "algorithmic bytes of an event-based design; measured DRAM bytes per collision are "
+                        f"{dram_per_event} (profiles/step_kernels_cfg1_traffic.txt): HBM is not the bound"}
+    clocks = clk.summary(local)
+    sm_mhz = (clocks or {}).get("sm_mhz") or pk.get("sm_max_mhz") or 2070.0
+    wipc = profile_value("k_hot_cfg1_mid.md", "warp_inst_per_collision")
+    roof = {"kernel": "k_hot<float> + k_rare<float> (wavefront step)", "traffic": traffic,
+            "step_kernel_ms": step_ms, "step_kernel_launches": launches_step, "events_per_step_kernel_s": ev_rate,
+            "issue_ncu": profile_issue(), "hbm": hbm_roof}
+    if wipc:
+        peak_issue = 152 * 4 * sm_mhz * 1e6       # one warp instruction per scheduler (4 per SM) per clock
+        roof.update({"bound": "issue", "achieved": wipc * ev_rate, "peak": peak_issue, "unit": "warp-inst/s",
+                     "frac": wipc * ev_rate / peak_issue, "warp_inst_per_collision": wipc,
+                     "peak_source": f"152 SMs x 4 schedulers x {sm_mhz:.0f} MHz (median SM clock of the timed region)",
+                     "inst_source": "profiles/k_hot_cfg1_mid.md (ncu smsp__inst_executed over a call / its collisions)"})
+    else:
+        roof.update({"bound": "hbm", "achieved": achieved, "peak": hbm_roof["peak"], "unit": "GB/s",
+                     "frac": hbm_roof["frac"]})
     cpu = None
     if world == 1 and not args.no_cpu:
         cpu = cpu_baseline(args)
+    tb = table_build(t, dev) if not args.no_table_build else None
+    c4 = cfg4_run(args, lib, dev, flush) if not args.no_cfg4 else None
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": tot_ms_all / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "iterations_per_s": world * args.steps * iters / (tot_ms_all / 1e3), "dtype": "f32", "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
-        "config": config_dict(w, iters, {"parallelism": f"iterations sharded over {world} GPU(s), no collective"}),
+        "iterations_per_s": world * args.steps * iters / (tot_ms_all / 1e3), "dtype": "f32",
+        "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
+        "config": config_dict(w, iters), "parallelism": f"iterations sharded over {world} GPU(s), no collective",
         "e2e": {"value": e2e_ev / e2e_s if e2e_s else None, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // max(args.e2e_steps, 1), "d2h_bytes_per_step": d2h // max(args.e2e_steps, 1)},
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "neural": neural,
-        "clocks": clk.summary(local),
+        "parity": parity_of(snaps, iters), "table_build": tb, "cfg4": c4,
+        "clocks": clocks,
         "events": {"total": tot_ev, "per_iteration": tot_ev / (args.steps * iters),
                    "elastic_frac": sum(s.n_el_elastic for s in sts) / max(tot_ev, 1),
+                   "fp64_redraws": sum(s.n_fp64_redraws for s in sts),
                    "by_kind_per_iteration": {f: sum(getattr(s, f) for s in sts) / (args.steps * iters) for f in (
                        "n_shi", "n_el_inelastic", "n_el_elastic", "n_hole_events", "n_auger", "n_radiative",
                        "n_photon_abs")},
@@ -306,16 +439,75 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def cfg4_run(args, lib, dev, flush):
+    """The large SiO2-like workload at its stated geometry (U 2.2 GeV, 100 nm,
+    0-1000 fs, 200 log radial bins over 0.5-5000 A, phonon-CDF elastic
+    scattering, mobile holes, radiative decay and photons), with the job's
+    10^6 iterations sub-sampled: --cfg4-steps timed calls of --cfg4-iters
+    iterations, table sampler and learned proposal."""
+    import torch
+    from trekis import abi, api, configs
+    w = configs.cfg4(NMC=args.cfg4_iters)
+    t = api.Tables(w, lib=lib)
+    tal_h = api.new_tallies(w)
+    dev_arrays = {k: torch.zeros(v.size, dtype=torch.float64, device=dev) for k, v in tal_h.a.items()}
+    dptr = lambda x: C.cast(C.c_void_p(x.data_ptr()), C.POINTER(C.c_double))
+    tal_d = abi.Tallies(Nt=tal_h.Nt, N_R=tal_h.NR, Nat=tal_h.Nat, Nshl=tal_h.Nshl,
+                        **{k: dptr(v) for k, v in dev_arrays.items()})
+
+    def run(i, sampler):
+        cfg, _R = api.run_cfg(w, api.RunOptions(seed=args.seed + 4, iteration_offset=i * args.cfg4_iters,
+                                                 queue_capacity=args.queue_cap, sampler=sampler),
+                              NMC=args.cfg4_iters)
+        st = abi.Status.fresh()
+        abi.check(lib.trekis_mc_run_device(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(tal_d),
+                                           C.byref(st)), lib)
+        flush.fill_(i & 0xFF)
+        return st
+
+    def timed(sampler):
+        run(0, sampler)        # warm-up: workspace and batch size
+        sts = [run(1 + i, sampler) for i in range(args.cfg4_steps)]
+        ev, ms = sum(s.n_events for s in sts), sum(s.device_ms for s in sts)
+        return sts, ev, ms
+
+    sts, ev, ms = timed(0)
+    out = {"workload": "cfg4: SiO2-like (rho 2.32, gap 9 eV, 8 shells, 6 VB oscillators, 3-oscillator phonon CDF), "
+                       "U 238u 2.2 GeV, 100 nm, 0-1000 fs dt 1 fs, 200 log radial bins 0.5-5000 A, mobile VB holes, "
+                       "radiative decay + photons, phonon-CDF elastic scattering",
+           "job_iterations": 1_000_000, "timed": f"{args.cfg4_steps} calls x {args.cfg4_iters} iterations (sub-sample)",
+           "table": {"value": ev / (ms / 1e3), "unit": UNIT,
+                     "iterations_per_s": args.cfg4_steps * args.cfg4_iters / (ms / 1e3),
+                     "events_per_iteration": ev / (args.cfg4_steps * args.cfg4_iters),
+                     "elastic_frac": sum(s.n_el_elastic for s in sts) / max(ev, 1),
+                     "fp64_redraws_frac": sum(s.n_fp64_redraws for s in sts) / max(ev, 1),
+                     "step_kernel_ms_frac": sum(s.step_ms for s in sts) / max(ms, 1e-9)}}
+    if not args.no_neural:
+        rep = api.train_proposal(t, n_samples=args.mlp_samples, epochs=3, batch=8192, E_lo=1.0, E_hi=1.0e5)
+        nsts, nev, nms = timed(1)
+        nv = nev / (nms / 1e3)
+        out["neural"] = {"value": nv, "unit": UNIT, "vs_table": nv / (ev / (ms / 1e3)),
+                         "same_collisions_as_table": bool(nev == ev), "training": rep}
+    t.close()
+    return out
+
+
 _ORACLE_TABLES = {}
 
 
 def cpu_baseline(args, n_it=None, nthreads=None):
     """The FP64 oracle (restatement of the reference's loop) on the host cores:
-    one cfg1 iteration per thread, heap-ordered earliest-event loop."""
+    one cfg1 iteration per thread, heap-ordered earliest-event loop; then one
+    cfg1 iteration on a single thread."""
     events, dt, nthreads, n_it = cpu_sample(args, n_it, nthreads)
-    return {"value": events / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{n_it} cfg1 iterations ({events} events) in {dt:.1f} s, FP64 oracle, "
-                      "OpenMP over iterations, heap event queue"}
+    out = {"value": events / dt, "unit": UNIT, "cores": nthreads, "kind": "port", "cpu_model": cpu_model(),
+           "sample": f"{n_it} cfg1 iterations ({events} events) in {dt:.1f} s, FP64 oracle, "
+                     "OpenMP over iterations, heap event queue"}
+    if not args.no_cpu_single:
+        e1, d1, _n, i1 = cpu_sample(args, 1, 1)
+        out["single_thread"] = {"value": e1 / d1, "unit": UNIT, "cores": 1,
+                                "sample": f"{i1} cfg1 iteration ({e1} events) in {d1:.1f} s on one thread"}
+    return out
 
 
 def cpu_sample(args, n_it=None, nthreads=None):
@@ -325,12 +517,12 @@ def cpu_sample(args, n_it=None, nthreads=None):
     w = workload()
     nthreads = nthreads or os.cpu_count() or 1
     n_it = n_it or args.cpu_iters or nthreads
-    if nthreads not in _ORACLE_TABLES:   # built once per thread count (the reference arm times several steps)
+    if "cfg1" not in _ORACLE_TABLES:   # built once, on every core (the reference arm times several steps)
         h = w.material.to_c()
         ion = api.ion_struct(w)
         tc = abi.TableCfg(build_shi=1, build_photon=1, shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
-        _ORACLE_TABLES[nthreads] = (h, oracle_py.OracleTables(h, ion, tc, nthreads=nthreads))
-    o = _ORACLE_TABLES[nthreads][1]
+        _ORACLE_TABLES["cfg1"] = (h, oracle_py.OracleTables(h, ion, tc, nthreads=os.cpu_count() or 1))
+    o = _ORACLE_TABLES["cfg1"][1]
     tal = api.new_tallies(w)
     cfg, R = api.run_cfg(w, api.RunOptions(precision=1, seed=args.seed, iteration_offset=900000), NMC=n_it)
     st = abi.Status.fresh()
@@ -368,7 +560,7 @@ def run_reference(args):
         tot_ev += ev
         tot_s += dt
     value = tot_ev / tot_s
-    cpu = {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+    cpu = {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "cpu_model": cpu_model(),
            "sample": f"{args.steps} x {n_it} cfg1 iterations ({int(tot_ev)} events) in {tot_s:.1f} s, FP64 oracle, "
                      "OpenMP over iterations, heap event queue"}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -376,8 +568,8 @@ def run_reference(args):
            "iterations_per_s": args.steps * n_it / tot_s,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
            "data": "synthetic (seeded Al2O3-like target, Xe ion; no dataset)",
-           "config": config_dict(w, args.iters, {"parallelism": "host threads",
-                                                 "reference_step": f"one FP64 iteration per host thread ({cpu['cores']})"}),
+           "config": config_dict(w, args.iters), "parallelism": "host threads",
+           "reference_step": f"one FP64 iteration per host thread ({cpu['cores']})",
            "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -401,6 +593,11 @@ def main():
                     help="particles per queue buffer (0: library default); 64 M holds about 2,400 cfg1 "
                          "iterations in flight, so a 2048-iteration step runs as two batches")
     ap.add_argument("--events-per-step", type=int, default=0, help="events per thread per wavefront step (0: tuned)")
+    ap.add_argument("--no-cpu-single", action="store_true", help="skip the one-thread CPU sample")
+    ap.add_argument("--no-table-build", action="store_true", help="skip the FP64 table-build figures")
+    ap.add_argument("--no-cfg4", action="store_true", help="skip the cfg4 sub-sample")
+    ap.add_argument("--cfg4-iters", type=int, default=1024, help="cfg4 iterations per timed call")
+    ap.add_argument("--cfg4-steps", type=int, default=3, help="cfg4 timed calls")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

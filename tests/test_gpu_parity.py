@@ -1,0 +1,105 @@
+"""The benchmark workloads at their stated size against the FP64 oracle.
+
+* cfg0 exactly as stated (Al2O3-like target, Xe 167 MeV, 10 nm, 0-100 fs,
+  100 log radial bins) and cfg1 at its full geometry and time grid (mobile
+  valence holes, radiative decay, photons, 0-1000 fs): FP32 GPU runs with
+  their own seeds against the oracle's committed batch statistics
+  (tests/golden/make_parity_fixtures.py): in >= 99 % of the live
+  (time, radius) bins the batch means agree within three combined standard
+  errors, at every time point for the electron density and energy density,
+  also for the lattice energy (cfg0: every time point; cfg1: every 10th) and
+  the valence holes' density and kinetic energy (cfg1, every 10th time
+  point).  A bin is live when at least half of the batches of both sides saw
+  a particle in it: the batch means of bins that are mostly empty are far
+  from normal, so a 3-sigma count says nothing there.  chi^2 per live bin is
+  printed and bounded.
+* Energy is conserved per iteration: single-iteration calls keep the total
+  energy (electrons, holes, photons, lattice) constant over the time grid to
+  1e-6 relative, in FP32.
+"""
+import pathlib
+
+import numpy as np
+import pytest
+
+from trekis import api, configs
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+
+# workload, GPU batches, iterations per GPU batch, GPU seed base
+PLANS = {
+    "cfg0": (lambda: configs.cfg0(), 32, 64, 100),
+    "cfg1": (lambda: configs.cfg1(NMC=32), 32, 32, 200),
+}
+
+
+def _vb(w):
+    return [(a, s) for a, at in enumerate(w.material.atoms) for s, sh in enumerate(at.shells)
+            if sh.designator >= 63][0]
+
+
+def _pick(tal, w, keys, coarse, stride, NMC):
+    a, s = _vb(w)
+    out = {}
+    for k in keys:
+        if k == "vb_nh":
+            v = tal.view("Out_nh")[:, :, a, s]
+        elif k == "vb_Ehkin":
+            v = tal.view("Out_Ehkin")[:, :, a, s]
+        else:
+            v = tal.view(k)
+        v = v / NMC
+        out[k] = v[stride - 1::stride] if k in coarse else v
+    return out
+
+
+def three_sigma(mg, vg, nzg, Bg, mr, vr, nzr, Br):
+    """Fraction of live bins within 3 combined standard errors, chi^2 per live
+    bin and the number of live bins.  v*: variances of the batch means, nz*:
+    batches with a non-zero value."""
+    live = (nzg >= Bg / 2) & (nzr >= Br / 2)
+    se = np.sqrt(vg / Bg + vr / Br)
+    live &= se > 0
+    z = (mg[live] - mr[live]) / se[live]
+    return float(np.mean(np.abs(z) <= 3.0)), float(np.mean(z * z)), int(live.sum())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cfg0", "cfg1"])
+def test_3sigma_full_size_against_oracle(gpu_lib, name):
+    fx = np.load(GOLDEN / f"parity_{name}.npz")
+    make, Bg, n, seed0 = PLANS[name]
+    w = make()
+    t = api.Tables(w, lib=gpu_lib)
+    full, coarse = list(fx["full_keys"]), list(fx["coarse_keys"])
+    keys = full + coarse
+    stride = int(fx["t_stride"])
+    acc = {k: [] for k in keys}
+    for b in range(Bg):
+        tal, _st = api.mc_run(t, api.RunOptions(seed=seed0 + b), NMC=n)
+        for k, v in _pick(tal, w, keys, coarse, stride, n).items():
+            acc[k].append(v)
+    Br = int(fx["batches"])
+    for k in keys:
+        x = np.array(acc[k])
+        frac, chi2, nlive = three_sigma(x.mean(0), x.var(0, ddof=1), (x != 0).sum(0), Bg,
+                                        fx[f"{k}_mean"].astype(np.float64), fx[f"{k}_var"].astype(np.float64),
+                                        fx[f"{k}_nz"], Br)
+        print(f"{name} {k}: {nlive} live bins, {100 * frac:.2f} % within 3 sigma, chi2/bin {chi2:.3f}")
+        assert nlive > 500, (k, nlive)
+        assert frac >= 0.99, (k, frac, chi2)
+        assert chi2 < 1.5, (k, chi2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["cfg0", "cfg1"])
+def test_energy_conserved_per_iteration(gpu_lib, name):
+    w = PLANS[name][0]()
+    t = api.Tables(w, lib=gpu_lib)
+    for i in range(6):
+        tal, st = api.mc_run(t, api.RunOptions(seed=31, iteration_offset=1000 + i), NMC=1)
+        tot = tal["Out_tot_E"]
+        assert tot[0] > 0 and st.n_events > 0
+        dev = float(np.max(np.abs(tot - tot[0])) / tot[0])
+        print(f"{name} iteration {1000 + i}: total {tot[0]:.6e} eV, largest relative change {dev:.2e}")
+        assert dev < 1e-6, (i, dev)
