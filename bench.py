@@ -287,12 +287,18 @@ def run_gpu(args):
     per_rank_steps = args.warmup + args.steps
     base_it = rank * per_rank_steps * iters
 
-    def step(i, host=False, sampler=0):
+    def step(i, host=False, sampler=0, words=None):
         opt = api.RunOptions(seed=args.seed, iteration_offset=base_it + i * iters, queue_capacity=args.queue_cap,
                              events_per_step=args.events_per_step, sampler=sampler)
         cfg, R = api.run_cfg(w, opt, NMC=iters)
         st = abi.Status.fresh()
-        if host:
+        if words is not None:   # the replicas' path: this step's exact sums are added to `words`
+            tl = api.new_tallies(w)
+            ct = tl.c()
+            rc = lib.trekis_mc_run_exact(t.h, t.mat.ref(), C.byref(t.ion), C.byref(cfg), C.byref(ct),
+                                         words.ctypes.data, len(words), C.byref(st))
+            dt = None
+        elif host:
             tl = api.new_tallies(w)
             ct = tl.c()
             t0 = time.perf_counter()
@@ -317,15 +323,27 @@ def run_gpu(args):
     sts = []
     snaps = []          # per-step electron density and energy density (parity with the oracle)
     prev = {k: dev_arrays[k].clone() for k in ("Out_ne", "Out_Ee")}
+    # with several ranks every step runs through the replicas' exact path
+    # (trekis_mc_run_exact); the job's sums are all-reduced as int64 after the
+    # timed region and made FP64 once
+    job_words = api.exact_words(t, iters) if world > 1 else None
+    fin_opt = api.RunOptions(queue_capacity=args.queue_cap, events_per_step=args.events_per_step)   # same workspace
     with clk:
         torch.cuda.synchronize()
         for i in range(args.steps):
-            st, _ = step(args.warmup + i)
+            if world > 1:
+                sw = np.zeros_like(job_words)
+                st, _ = step(args.warmup + i, words=sw)
+                job_words += sw
+                one = api.exact_finish(t, sw, opt=fin_opt)   # outside the library's timing: this step's tallies
+                snaps.append({k: (one[k] / iters).reshape(NR, Nt).T for k in prev})
+            else:
+                st, _ = step(args.warmup + i)
+                # outside the library's CUDA-event timing: this step's sums
+                cur = {k: dev_arrays[k].clone() for k in prev}
+                snaps.append({k: ((cur[k] - prev[k]) / iters).cpu().numpy().reshape(NR, Nt).T for k in cur})
+                prev = cur
             sts.append(st)
-            # outside the library's CUDA-event timing: this step's sums
-            cur = {k: dev_arrays[k].clone() for k in prev}
-            snaps.append({k: ((cur[k] - prev[k]) / iters).cpu().numpy().reshape(NR, Nt).T for k in cur})
-            prev = cur
             tot_ev += st.n_events
             tot_ms += st.device_ms
             step_ms += st.step_ms
@@ -339,8 +357,15 @@ def run_gpu(args):
         mx = v.clone(); dist.all_reduce(mx[:1], op=dist.ReduceOp.MAX)
         sm = v.clone(); dist.all_reduce(sm[1:], op=dist.ReduceOp.SUM)
         tot_ms_all, tot_ev_all = float(mx[0]), float(sm[1])
+        jw = torch.from_numpy(job_words).to(dev)
+        dist.all_reduce(jw, op=dist.ReduceOp.SUM)          # exact: int64 limbs of 128-bit sums
+        job = api.exact_finish(t, jw.cpu().numpy(), opt=fin_opt)
+        job_sum = {"iterations": world * args.steps * iters, "reduce": "int64 all-reduce of exact-sum words",
+                   "Out_tot_Ne_last_per_iteration": float(job["Out_tot_Ne"][-1]) / (world * args.steps * iters),
+                   "Out_tot_E_per_iteration": float(job["Out_tot_E"][0]) / (world * args.steps * iters)}
     else:
         tot_ms_all, tot_ev_all = tot_ms, tot_ev
+        job_sum = None
     # end-to-end through the drop-in call with host tally arrays
     e2e_ev = e2e_s = 0.0
     h2d = d2h = 0
@@ -422,7 +447,7 @@ def run_gpu(args):
         "e2e": {"value": e2e_ev / e2e_s if e2e_s else None, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // max(args.e2e_steps, 1), "d2h_bytes_per_step": d2h // max(args.e2e_steps, 1)},
         "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu, "neural": neural,
-        "parity": parity_of(snaps, iters), "table_build": tb, "cfg4": c4,
+        "parity": parity_of(snaps, iters), "table_build": tb, "cfg4": c4, "job_tallies": job_sum,
         "clocks": clocks,
         "events": {"total": tot_ev, "per_iteration": tot_ev / (args.steps * iters),
                    "elastic_frac": sum(s.n_el_elastic for s in sts) / max(tot_ev, 1),

@@ -13,7 +13,7 @@
 module trekis_gb300
   use iso_c_binding
   implicit none
-  integer, parameter :: TREKIS_ABI_VERSION = 5
+  integer, parameter :: TREKIS_ABI_VERSION = 6
   integer, parameter :: TREKIS_MAX_ATOMS = 8, TREKIS_MAX_SHELLS = 16, &
                         TREKIS_MAX_OSC = 16, TREKIS_MAX_PH_OSC = 8
   ! return codes
@@ -35,6 +35,11 @@ module trekis_gb300
      real(c_double)     :: form_factor(5)
   end type
 
+  type, bind(C) :: trekis_dsf
+     integer(c_int32_t) :: n_E, n_dE
+     type(c_ptr)        :: E, dE, dL, dL_emit, dL_absorb      ! C [n_E][n_dE]: Fortran (n_dE, n_E)
+  end type
+
   type, bind(C) :: trekis_material
      integer(c_int32_t) :: N_atoms
      type(trekis_atom)  :: atoms(TREKIS_MAX_ATOMS)
@@ -45,6 +50,7 @@ module trekis_gb300
      integer(c_int32_t) :: N_dos
      type(c_ptr)        :: dos_E, dos_DOS, dos_int, dos_k, dos_Eff_m
      integer(c_int32_t) :: kind_of_EMFP, CDF_elast_Zeff, kind_of_DR, plasmon_Emax, include_photons
+     type(c_ptr)        :: dsf_el, dsf_h                      ! c_loc of trekis_dsf, or c_null_ptr
   end type
 
   type, bind(C) :: trekis_ion
@@ -173,6 +179,21 @@ module trekis_gb300
        import; type(c_ptr), value :: tables; type(trekis_material), intent(in) :: mat
        type(trekis_ion), intent(in) :: ion; type(trekis_run_cfg), intent(in) :: cfg
        type(trekis_tallies), intent(inout) :: out; type(trekis_status), intent(inout) :: st
+     end function
+     integer(c_int64_t) function trekis_exact_words(tables, cfg) bind(C)
+       import; type(c_ptr), value :: tables; type(trekis_run_cfg), intent(in) :: cfg
+     end function
+     integer(c_int32_t) function trekis_mc_run_exact(tables, mat, ion, cfg, out, words, n_words, st) bind(C)
+       import; type(c_ptr), value :: tables; type(trekis_material), intent(in) :: mat
+       type(trekis_ion), intent(in) :: ion; type(trekis_run_cfg), intent(in) :: cfg
+       type(trekis_tallies), intent(inout) :: out; integer(c_int64_t), intent(inout) :: words(*)
+       integer(c_int64_t), value :: n_words; type(trekis_status), intent(inout) :: st
+     end function
+     integer(c_int32_t) function trekis_exact_finish(tables, mat, cfg, words, n_words, out, st) bind(C)
+       import; type(c_ptr), value :: tables; type(trekis_material), intent(in) :: mat
+       type(trekis_run_cfg), intent(in) :: cfg; integer(c_int64_t), intent(in) :: words(*)
+       integer(c_int64_t), value :: n_words; type(trekis_tallies), intent(inout) :: out
+       type(trekis_status), intent(inout) :: st
      end function
      integer(c_int32_t) function trekis_mc_run_device_noalloc(tables, mat, ion, cfg, out, st, stream) bind(C)
        import; type(c_ptr), value :: tables; type(trekis_material), intent(in) :: mat

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TREKIS_ABI_VERSION 5
+#define TREKIS_ABI_VERSION 6
 
 #define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
 #define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
@@ -81,6 +81,22 @@ typedef struct {
                                  analytical fit); read only with CDF_elast_Zeff 2 */
 } trekis_atom;
 
+/* Differential elastic mean free paths from a dynamic structure factor:
+ * mirrors `type(Differential_MFP)` (Objects.f90) as reading_DSF_cross_sections
+ * leaves it (Reading_files_and_parameters.f90:2516-2678).  Row-major
+ * [n_E][n_dE] arrays: for incident energy E[i] [eV] the transferred energies
+ * dE [eV] (increasing; > 0: emission, energy given to the lattice) and the
+ * cumulative MFPs [A] over all transfers (dL), the emissions (dL_emit) and
+ * the absorptions (dL_absorb). */
+typedef struct {
+    int32_t       n_E, n_dE;
+    const double* E;          /* [n_E]                                       */
+    const double* dE;         /* [n_E * n_dE]                                */
+    const double* dL;         /* [n_E * n_dE]                                */
+    const double* dL_emit;    /* [n_E * n_dE]                                */
+    const double* dL_absorb;  /* [n_E * n_dE]                                */
+} trekis_dsf;
+
 /* Target: mirrors `type(Solid)`, `type(Density_of_states)`, the phonon
  * `type(CDF)` and the flags of `type(Flag)` used on the path
  * (Source_files/Objects.f90:86-167). */
@@ -116,7 +132,8 @@ typedef struct {
     const double* dos_k;      /* [1/m]                                      */
     const double* dos_Eff_m;  /* [me]                                       */
     /* flags */
-    int32_t kind_of_EMFP;     /* 0 = Mott atomic elastic, 1 = phonon CDF      */
+    int32_t kind_of_EMFP;     /* 0 = Mott atomic elastic, 1 = phonon CDF,
+                                 2 = DSF tables (dsf_el, dsf_h)                */
     int32_t CDF_elast_Zeff;   /* target charge in the phonon CS: 0 Barkas-like, 1 one,
                                  2 nucleus screened by the valence CDF and core form
                                  factors, 3 screened by the shells' CDFs */
@@ -124,6 +141,10 @@ typedef struct {
                                  (4, the delta CDF: TREKIS_EUNSUPPORTED)     */
     int32_t plasmon_Emax;     /* 1: plasmon energy as upper limit            */
     int32_t include_photons;  /* 1: radiative decay and photon transport     */
+    /* DSF elastic scattering (kind_of_EMFP 2): DSF_DEMFP and DSF_DEMFP_H of
+     * the reference; read only when kind_of_EMFP is 2 */
+    const trekis_dsf* dsf_el;
+    const trekis_dsf* dsf_h;
 } trekis_material;
 
 /* The projectile: mirrors `type(Ion)` (Source_files/Objects.f90:44-53). */
@@ -348,6 +369,40 @@ int32_t trekis_mc_run(const trekis_tables* t, const trekis_material* mat,
 int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
                              const trekis_ion* ion, const trekis_run_cfg* cfg,
                              trekis_tallies* dev_out, trekis_status* st);
+
+/* ---- exact sums over replicas (the reduction of Monte_Carlo.f90:395-415) ----
+ * Every call keeps its radial tallies as exact integers (counts, energies in
+ * 2^-24 eV, lattice energy in 2^-40 eV, summed in 128 bits) and makes the
+ * FP64 tallies from them once, at its end; so the batch partition does not
+ * change a bit of Out_ne, Out_Ee, Out_nphot, Out_Ephot, Out_Elat, Out_nh,
+ * Out_Eh, Out_Ehkin, Out_tot_Ne, Out_tot_Nphot, Out_tot_E, Out_E_e,
+ * Out_E_phot, Out_E_at, Out_E_h.  To split NMC iterations over several GPUs
+ * or processes (disjoint iteration_offset ranges, the random streams being
+ * keyed by the global iteration) and get exactly what one call over all of
+ * them gives:
+ *   1. each replica calls trekis_mc_run_exact, which ADDS its exact sums to
+ *      words[trekis_exact_words(t, cfg)] (zero it first) instead of making
+ *      FP64 tallies; the spectra (Out_Ee_vs_E, Out_Eh_vs_E, Out_theta,
+ *      Out_theta_h) are added to `out` as trekis_mc_run does, and no other
+ *      member of `out` changes;
+ *   2. the words of all replicas are summed element by element as int64 (any
+ *      order, e.g. one integer all-reduce): each 128-bit sum is stored as four
+ *      32-bit limbs, low first, in int64 words, so the limb sums of up to
+ *      2^31 replicas cannot overflow;
+ *   3. one process calls trekis_exact_finish with the summed words and the
+ *      cfg of the runs (its NMC is not used), which adds the FP64 tallies of
+ *      those sums to `out` (host arrays) -- bit for bit what one
+ *      trekis_mc_run over all iterations adds.  The spectra are sums of
+ *      per-iteration fractions in FP64 and are summed in FP64.
+ * trekis_exact_words: the number of words for this tally shape, or -1. */
+int64_t trekis_exact_words(const trekis_tables* t, const trekis_run_cfg* cfg);
+int32_t trekis_mc_run_exact(const trekis_tables* t, const trekis_material* mat,
+                            const trekis_ion* ion, const trekis_run_cfg* cfg,
+                            trekis_tallies* out, int64_t* words, int64_t n_words,
+                            trekis_status* st);
+int32_t trekis_exact_finish(const trekis_tables* t, const trekis_material* mat,
+                            const trekis_run_cfg* cfg, const int64_t* words,
+                            int64_t n_words, trekis_tallies* out, trekis_status* st);
 
 /* Fixed-footprint variant of trekis_mc_run_device.  No counterpart in the
  * reference (its Fortran loop allocates and grows its particle arrays freely).

@@ -8,7 +8,10 @@
 !   SHI (type(Ion), Objects.f90:44-53)                      -> cion
 ! It needs the reference's module Objects in scope.  The DOS arrays are passed
 ! by address (c_loc) and must stay allocated while the library runs; the
-! inverted DOS of metals is not carried.
+! inverted DOS of metals is not carried.  pack_dsf flattens a DSF_DEMFP
+! array (type(Differential_MFP), read by reading_DSF_cross_sections) into
+! arrays the caller keeps until trekis_tables_build returns, for
+! cmat%dsf_el = c_loc(cdsf_el) and cmat%dsf_h = c_loc(cdsf_h).
 subroutine pack_inputs(Target_atoms, Matter, Mat_DOS, CDF_Phonon, NumPar, SHI, cmat, cion)
   use iso_c_binding
   use Objects
@@ -56,3 +59,27 @@ subroutine pack_inputs(Target_atoms, Matter, Mat_DOS, CDF_Phonon, NumPar, SHI, c
   cion%Zat = SHI%Zat; cion%Kind_Zeff = SHI%Kind_Zeff; cion%Kind_ion = SHI%Kind_ion; cion%pad_ = 0
   cion%Mass = SHI%Mass; cion%E = SHI%E; cion%fixed_Zeff = SHI%fixed_Zeff
 end subroutine pack_inputs
+
+subroutine pack_dsf(DSF_DEMFP, E, dE, dL, dL_emit, dL_absorb, cdsf)
+  use iso_c_binding
+  use Objects
+  use trekis_gb300
+  type(Differential_MFP), dimension(:), intent(in) :: DSF_DEMFP
+  real(c_double), dimension(:), allocatable, target, intent(inout) :: E
+  real(c_double), dimension(:,:), allocatable, target, intent(inout) :: dE, dL, dL_emit, dL_absorb
+  type(trekis_dsf), intent(out) :: cdsf
+  integer :: i, n, nE
+  nE = size(DSF_DEMFP)
+  n = size(DSF_DEMFP(1)%dE)
+  if (allocated(E)) deallocate(E, dE, dL, dL_emit, dL_absorb)
+  ! column i holds incident energy i: row-major [n_E][n_dE] as C reads it
+  allocate(E(nE), dE(n, nE), dL(n, nE), dL_emit(n, nE), dL_absorb(n, nE))
+  do i = 1, nE
+     E(i) = DSF_DEMFP(i)%E
+     dE(:, i) = DSF_DEMFP(i)%dE; dL(:, i) = DSF_DEMFP(i)%dL
+     dL_emit(:, i) = DSF_DEMFP(i)%dL_emit; dL_absorb(:, i) = DSF_DEMFP(i)%dL_absorb
+  enddo
+  cdsf%n_E = nE; cdsf%n_dE = n
+  cdsf%E = c_loc(E); cdsf%dE = c_loc(dE); cdsf%dL = c_loc(dL)
+  cdsf%dL_emit = c_loc(dL_emit); cdsf%dL_absorb = c_loc(dL_absorb)
+end subroutine pack_dsf

@@ -57,6 +57,8 @@ struct Stream {
 struct Row { std::vector<double> hw, L; };      // one cumulative row: hw, MFP
 struct RowSet { std::vector<double> E; std::vector<Row> rows; };  // type(diff_CS)
 struct MFPTab { std::vector<double> E, L, dEdx; };                 // type(MFP)
+// DSF_DEMFP (type(Differential_MFP)) of one particle kind, row-major [nE][n]
+struct DsfTab { int nE = 0, n = 0; std::vector<double> E, dE, dL, dLe, dLa; };
 
 struct Tables {
     // per atom, per shell (flattened atom*MAX_SHELLS + shell)
@@ -66,6 +68,7 @@ struct Tables {
     std::vector<std::vector<MFPTab>> shi_rows_E;
     std::vector<int> shi_row_nodes;
     MFPTab el_elast, hole_elast;
+    DsfTab dsf[2];                 // DSF elastic (kind_of_EMFP = 2): electrons, valence holes
     std::vector<RowSet> el_rows;   // per atom,shell
     RowSet hole_rows;              // valence band only
     RowSet el_elast_rows, hole_elast_rows;   // phonon-CDF elastic (aidCS%EEdCS, %HEdCS)
@@ -100,5 +103,6 @@ double sample_transfer_inelastic(const Tables& T, const trekis_material& m, int 
 double next_free_path_2d(const MFPTab& t, double E);
 double next_free_path_1d(const MFPTab& t, double E);
 double interp_transfer(const RowSet& R, double Ele, double L_need);
+double dsf_transfer(const DsfTab& D, double Eel, double RN1, double RN2);
 
 }  // namespace orc

@@ -134,6 +134,50 @@ double sample_transfer_inelastic(const Tables& T, const trekis_material& m, int 
     return E;
 }
 
+// NRG_transfer_elastic_DSF (Cross_sections.f90:3652-3795): emission or
+// absorption by the linearly interpolated MFPs, the cumulative MFP column of
+// that choice interpolated between the incident energies around Eel, then
+// Linear_approx_2x1d_DSF (Reading_files_and_parameters.f90:3718-3745)
+static double dsf_row_last(const DsfTab& D, const std::vector<double>& col, int i) { return col[(size_t)i * D.n + D.n - 1]; }
+
+double dsf_transfer(const DsfTab& D, double Eel, double RN1, double RN2) {
+    auto lin = [](double y1, double y2, double x1, double x2, double x) { return y1 + (y2 - y1) / (x2 - x1) * (x - x1); };
+    int NumE = find_monoton(D.E.data(), D.nE, Eel);
+    if (NumE > 1) NumE = NumE - 1;
+    const int i_MFP = NumE;            // Elastic_MFP%Total%E is the DSF energy grid
+    const int a = i_MFP - 1, b = i_MFP;   // 0-based
+    const double EMFP_tot = lin(dsf_row_last(D, D.dL, a), dsf_row_last(D, D.dL, b), D.E[a], D.E[b], Eel);
+    const double EMFP_emit = lin(dsf_row_last(D, D.dLe, a), dsf_row_last(D, D.dLe, b), D.E[a], D.E[b], Eel);
+    const double EMFP_absorb = lin(dsf_row_last(D, D.dLa, a), dsf_row_last(D, D.dLa, b), D.E[a], D.E[b], Eel);
+    const bool emission = RN1 < EMFP_tot / EMFP_emit;
+    const int n = D.n;
+    std::vector<double> dL(n), dEv(n);
+    const std::vector<double>& col = emission ? D.dLe : D.dLa;
+    const int r = NumE - 1;
+    if (NumE == D.nE) {
+        for (int j = 0; j < n; ++j) { dL[j] = col[(size_t)r * n + j]; dEv[j] = D.dE[(size_t)r * n + j]; }
+    } else {
+        const double Value1 = (Eel - D.E[r]) / (D.E[r + 1] - D.E[r]);
+        for (int j = 0; j < n; ++j) {
+            dL[j] = col[(size_t)r * n + j] + (col[(size_t)(r + 1) * n + j] - col[(size_t)r * n + j]) * Value1;
+            dEv[j] = D.dE[(size_t)r * n + j] + (D.dE[(size_t)(r + 1) * n + j] - D.dE[(size_t)r * n + j]) * Value1;
+        }
+    }
+    for (int j = 0; j < n; ++j) if (dL[j] < 0.0) dL[j] = 0.0;
+    const double L_need = (emission ? EMFP_emit : EMFP_absorb) / RN2;
+    // Linear_approx_2x1d_DSF: the bracket in the decreasing dL via the increasing -dL
+    std::vector<double> neg(n);
+    for (int j = 0; j < n; ++j) neg[j] = -dL[j];
+    const int Number = find_monoton(neg.data(), n, -L_need);
+    double dE;
+    if (Number == 1) dE = dEv[0] + (dEv[1] - dEv[0]) / (dL[1] - dL[0]) * (L_need - dL[0]);
+    else if (std::fabs(dL[Number - 1] - dL[Number - 2]) < 1.0e-9) dE = dEv[Number - 2];
+    else if (dL[Number - 2] > 1e20) dE = dEv[Number - 2];
+    else dE = dEv[Number - 2] + (dEv[Number - 1] - dEv[Number - 2]) / (dL[Number - 1] - dL[Number - 2]) * (L_need - dL[Number - 2]);
+    if (std::fabs(dE) > 1.0 && emission && dE > Eel) dE = Eel;
+    return dE;
+}
+
 namespace {
 
 struct P {            // Basic_particle (Objects.f90:31-41) + identity for the keyed RNG
@@ -511,8 +555,11 @@ void electron_event(Ctx& c, int NOP, int i) {
         c.el.push_back(ne);
         c.ho.push_back(hh);
         c.cnt[1]++;
-    } else {  // elastic: Mott (kind_of_EMFP = 0) or phonon CDF (1)
-        dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, false, Eel, s) : mott_transfer(c, Eel, 1.0, s);
+    } else {  // elastic: Mott (kind_of_EMFP = 0), phonon CDF (1) or DSF (2)
+        if (m.kind_of_EMFP == 2) {
+            const double u1 = s.next(), u2 = s.next();
+            dE = dsf_transfer(c.T->dsf[0], Eel, u1, u2);
+        } else dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, false, Eel, s) : mott_transfer(c, Eel, 1.0, s);
         angles_lat(c, Eel, dE, 1.0, s, theta, phi, elastic_uniform(x, 1.0 / I, Em));
         c.At_NRG += dE;
         add_elat(c, i, X, Y, dE);
@@ -604,7 +651,10 @@ void hole_event(Ctx& c, int NOP, int i, double t_cur) {
             c.ho.push_back(hh);
             c.cnt[3]++;
         } else {  // elastic, Mott with the hole mass, or phonon CDF
-            dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, true, Eel, s) : mott_transfer(c, Eel, hmass, s);
+            if (m.kind_of_EMFP == 2) {
+                const double u1 = s.next(), u2 = s.next();
+                dE = dsf_transfer(c.T->dsf[1], Eel, u1, u2);
+            } else dE = (m.kind_of_EMFP == 1) ? phonon_transfer(c, true, Eel, s) : mott_transfer(c, Eel, hmass, s);
             // no ionisation channel (HI >= 1e15): RN chose nothing and is reused whole
             angles_lat(c, Eel, dE, hmass, s, th1, ph1, HI < 1e15 ? elastic_uniform(x, 1.0 / HI, HE) : RN);
             Ehole = check_hole(c, Eel, dE, nullptr);
@@ -941,7 +991,8 @@ void one_iteration(Ctx& c, int64_t it_global, int sched) {
 int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, const trekis_run_cfg& cfg,
            trekis_tallies& out, trekis_status* st, int nthreads, int sched) {
     if (cfg.dt_flag != 0 && cfg.dt_flag != 1) return TREKIS_EINVAL;
-    if (m.work_function > 0.0 || m.kind_of_EMFP < 0 || m.kind_of_EMFP > 1 || ion.Kind_ion != 0) return TREKIS_EUNSUPPORTED;
+    if (m.work_function > 0.0 || m.kind_of_EMFP < 0 || m.kind_of_EMFP > 2 || ion.Kind_ion != 0) return TREKIS_EUNSUPPORTED;
+    if (m.kind_of_EMFP == 2 && (T.dsf[0].nE < 2 || T.dsf[1].nE < 2)) return TREKIS_EINVAL;
     if (m.kind_of_EMFP == 1 && T.el_elast_rows.rows.empty()) return TREKIS_EINVAL;
     if (!T.has_shi) return TREKIS_EINVAL;
     if (m.include_photons && !T.has_phot) return TREKIS_EINVAL;

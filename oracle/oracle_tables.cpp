@@ -686,6 +686,20 @@ int build_tables(const trekis_material& m, const trekis_ion& ion, const trekis_t
         if (m.hole_mass < 0)
             for (size_t i = 0; i < T.hole_elast.E.size(); ++i)
                 T.hole_elast.L[i] /= m.dos_Eff_m[find_monoton(m.dos_E, m.N_dos, T.hole_elast.E[i]) - 1];
+    } else if (m.kind_of_EMFP == 2) {   // DSF: Elastic_MFP%Total from the tables (Analytical_IMFPs.f90:907-914, 1181-1186)
+        for (int q = 0; q < 2; ++q) {
+            const trekis_dsf* d = q ? m.dsf_h : m.dsf_el;
+            if (!d || d->n_E < 2 || d->n_dE < 2) return TREKIS_EINVAL;
+            DsfTab& D = T.dsf[q];
+            const size_t nn = (size_t)d->n_E * d->n_dE;
+            D.nE = d->n_E; D.n = d->n_dE;
+            D.E.assign(d->E, d->E + d->n_E);
+            D.dE.assign(d->dE, d->dE + nn); D.dL.assign(d->dL, d->dL + nn);
+            D.dLe.assign(d->dL_emit, d->dL_emit + nn); D.dLa.assign(d->dL_absorb, d->dL_absorb + nn);
+            MFPTab& t = q ? T.hole_elast : T.el_elast;
+            t.E = D.E; t.L.resize(D.nE); t.dEdx.assign(D.nE, 0.0);
+            for (int i = 0; i < D.nE; ++i) t.L[i] = D.dL[(size_t)i * D.n + D.n - 1];
+        }
     } else return TREKIS_EUNSUPPORTED;
     // photons (AI:153, All_shells_Photon_MFP AI:2146)
     if (cfg.build_photon && m.include_photons) {

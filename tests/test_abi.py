@@ -45,7 +45,8 @@ def test_struct_layout_matches_c(tmp_path):
     names = {"trekis_atom": abi.Atom, "trekis_material": abi.Material, "trekis_ion": abi.Ion,
              "trekis_table_cfg": abi.TableCfg, "trekis_run_cfg": abi.RunCfg, "trekis_tallies": abi.Tallies,
              "trekis_status": abi.Status, "trekis_output_cfg": abi.OutputCfg, "trekis_batch_cfg": abi.BatchCfg,
-             "trekis_tune": abi.Tune, "trekis_mlp_cfg": abi.MlpCfg, "trekis_mlp_report": abi.MlpReport}
+             "trekis_tune": abi.Tune, "trekis_mlp_cfg": abi.MlpCfg, "trekis_mlp_report": abi.MlpReport,
+             "trekis_build_stats": abi.BuildStats, "trekis_dsf": abi.Dsf}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HDR}"', "int main(void){"]
     for cn in names:
         lines.append(f'printf("{cn} %zu\\n", sizeof({cn}));')
@@ -162,7 +163,7 @@ def test_fortran_interface_types_match_c():
                "trekis_table_cfg": abi.TableCfg, "trekis_run_cfg": abi.RunCfg, "trekis_tallies": abi.Tallies,
                "trekis_status": abi.Status, "trekis_output_cfg": abi.OutputCfg, "trekis_batch_cfg": abi.BatchCfg,
                "trekis_build_stats": abi.BuildStats, "trekis_tune": abi.Tune, "trekis_mlp_cfg": abi.MlpCfg,
-               "trekis_mlp_report": abi.MlpReport}
+               "trekis_mlp_report": abi.MlpReport, "trekis_dsf": abi.Dsf}
     assert set(types) == set(mirrors), set(types) ^ set(mirrors)
     for name, fields in types.items():
         assert _c_layout(fields, types)[0] == C.sizeof(mirrors[name]), name

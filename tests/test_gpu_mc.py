@@ -1,15 +1,18 @@
 """GPU track loop against the oracle.
 
-* FP64 mode on identical tables and identical Philox streams: every tally
-  equals the oracle's chronological loop to the fixed-point resolution
+* FP64 mode on identical tables and identical Philox streams (Mott,
+  phonon-CDF and DSF elastic scattering): every tally equals the oracle's
+  chronological loop to the fixed-point resolution
   (2^-24 eV per particle energy, 2^-40 eV per lattice deposit).
 * FP32 mode: radial electron density and energy density agree with the FP64
   oracle within 3 combined standard errors in >= 98 % of the populated
   (time, radius) bins (batch-means errors over independent seeds); with
   mobile holes and photons (cfg1) and phonon-CDF elastic scattering (cfg4)
   also the lattice energy and the valence holes' density and kinetic energy.
-* Scheduling knobs (events per step, block size) do not change a single bit;
-  batch sizes only change the order of the FP64 batch sums.
+* Scheduling knobs (events per step, block size, batch size) do not change
+  a single bit: every batch adds into exact integer sums, made FP64 once per
+  call; iterations split over replicas and summed as exact words give the
+  same bits as one call.
 """
 import ctypes as C
 
@@ -64,6 +67,14 @@ def small4(gpu_lib):
     return w, t, _oracle_on(t, w)
 
 
+@pytest.fixture(scope="module")
+def small_dsf(gpu_lib):
+    # DSF elastic scattering of electrons and valence holes (kind_of_EMFP = 2)
+    w = configs.small(configs.cfg1_dsf, NMC=4, Tim=30.0)
+    t = api.Tables(w, lib=gpu_lib)
+    return w, t, _oracle_on(t, w)
+
+
 def _assert_tallies_equal(g, r, what):
     for k in g.a:
         a, b = g[k], r[k]
@@ -73,7 +84,7 @@ def _assert_tallies_equal(g, r, what):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["small0", "small1", "small4"])
+@pytest.mark.parametrize("case", ["small0", "small1", "small4", "small_dsf"])
 def test_fp64_matches_oracle(case, request):
     w, t, o = request.getfixturevalue(case)
     opt = api.RunOptions(precision=1, seed=11)
@@ -86,6 +97,8 @@ def test_fp64_matches_oracle(case, request):
     _assert_tallies_equal(g, r, case)
     if case == "small1":
         assert sg.n_hole_events > 0 and sg.n_radiative > 0 and sg.n_photon_abs > 0
+    if case == "small_dsf":
+        assert sg.n_el_elastic > 0 and sg.n_hole_events > 0
 
 
 @pytest.mark.gpu
@@ -96,10 +109,10 @@ def test_scheduling_invariance_bit_exact(small1):
         g, st = api.mc_run(t, api.RunOptions(seed=5, iterations_per_batch=3, events_per_step=K, block_size=bs))
         for k in g.a:
             assert np.array_equal(g[k], ref[k]), (K, bs, k)
-    # another batching: same int64 sums, FP64 batch-sum order differs
+    # another batching: the batches add into the same exact sums
     g, _ = api.mc_run(t, api.RunOptions(seed=5, iterations_per_batch=1))
     for k in g.a:
-        assert np.allclose(g[k], ref[k], rtol=1e-12, atol=0), k
+        assert np.array_equal(g[k], ref[k]), k
 
 
 @pytest.mark.gpu
@@ -128,6 +141,40 @@ def test_shards_sum(small0):
     b, _ = api.mc_run(t, api.RunOptions(seed=4, iteration_offset=2), NMC=4)
     for k in full.a:
         assert np.allclose(full[k], a[k] + b[k], rtol=1e-12, atol=0), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("split", [(6,), (2, 4), (1, 1, 3, 1)])
+def test_exact_sums_over_replicas_bit_exact(small1, split):
+    """Iterations split over replicas (trekis_mc_run_exact on disjoint
+    iteration ranges), their words summed as int64 in any order and made FP64
+    once (trekis_exact_finish): every radial tally and total equals one
+    trekis_mc_run over all iterations bit for bit; the spectra agree to FP64
+    rounding."""
+    w, t, _o = small1
+    full, _ = api.mc_run(t, api.RunOptions(seed=6), NMC=6, tallies=api.new_tallies(w, spectra=True))
+    parts, off = [], 0
+    for n in split:
+        words = api.exact_words(t, 6)
+        spec = api.new_tallies(w, spectra=True)
+        _tal, st = api.mc_run_exact(t, words, api.RunOptions(seed=6, iteration_offset=off), NMC=n, tallies=spec)
+        assert st.n_events > 0
+        for k in spec.a:
+            if k not in api.SPECTRA:
+                assert not spec[k].any(), k        # only the spectra are touched
+        parts.append((words, spec))
+        off += n
+    total = np.zeros_like(parts[0][0])
+    for words, _spec in reversed(parts):
+        total += words
+    got = api.exact_finish(t, total, tallies=api.new_tallies(w, spectra=True))
+    for k in full.a:
+        if k in api.SPECTRA:
+            sp = sum(p[1][k] for p in parts)
+            assert np.allclose(sp, full[k], rtol=1e-12, atol=0), k
+        else:
+            assert np.array_equal(got[k], full[k]), k
+    assert full["Out_ne"].any() and full["Out_Elat"].any()
 
 
 @pytest.mark.gpu
@@ -182,8 +229,8 @@ def test_fp32_statistically_equal_to_oracle_mobile_holes(gpu_lib, case):
     energy, and the valence holes' density and kinetic energy agree with the
     FP64 oracle within 3 batch-means standard errors in >= 98 % of the live
     (time, radius) bins, independent seeds."""
-    if case == "cfg1":
-        w = configs.small(configs.cfg1, NMC=4, Tim=30.0)
+    if case in ("cfg1", "cfg1_dsf"):
+        w = configs.small(getattr(configs, case), NMC=4, Tim=30.0)
     else:
         w = configs.small(configs.cfg4, NMC=4, Tim=20.0, ion_E=50e6)
     t = api.Tables(w, lib=gpu_lib)
@@ -212,14 +259,14 @@ def test_fp32_statistically_equal_to_oracle_mobile_holes(gpu_lib, case):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["cfg1", "cfg4"])
+@pytest.mark.parametrize("case", ["cfg1", "cfg4", "cfg1_dsf"])
 def test_fp32_bias_against_fp64_same_streams(gpu_lib, case):
     """FP32 and FP64 runs of the same Philox streams differ only by rounding:
     over 64 seeds the mean relative difference of every total (electrons,
     electron energy, lattice energy, valence holes, collision counts) stays
     below 5e-4, against about 7e-2 seed-to-seed spread per run."""
-    if case == "cfg1":
-        w = configs.small(configs.cfg1, NMC=4, Tim=30.0)
+    if case in ("cfg1", "cfg1_dsf"):
+        w = configs.small(getattr(configs, case), NMC=4, Tim=30.0)
     else:
         w = configs.small(configs.cfg4, NMC=4, Tim=20.0, ion_E=50e6)
     t = api.Tables(w, lib=gpu_lib)

@@ -2,8 +2,8 @@
 FP64 samplers equal the oracle's restatement, and the FP32 track loop's
 samplers agree with them within 1e-5 relative: every draw of the transferred
 energy of ionising collisions (electrons of every shell, valence holes) and
-of the phonon-CDF elastic draw, and >= 99.9 % of the free paths and Mott
-transfers (fractions reported).
+of the phonon-CDF and DSF elastic draws, and >= 99.9 % of the free paths
+and Mott transfers (fractions reported).
 
 The FP32 transfer draws invert cumulative rows stored in FP32, with the
 log-log interpolations written through ratios (interp5_acc).  Where a bracket
@@ -29,11 +29,11 @@ def _probe(t, precision, kind, a, s, E, u):
     return out
 
 
-@pytest.fixture(scope="module", params=["cfg1", "cfg4"])
+@pytest.fixture(scope="module", params=["cfg1", "cfg4", "cfg1_dsf"])
 def tabs(request, gpu_lib):
     import oracle_py
-    if request.param == "cfg1":
-        w = configs.small(configs.cfg1, NMC=1)
+    if request.param in ("cfg1", "cfg1_dsf"):
+        w = configs.small(getattr(configs, request.param), NMC=1)
     else:
         w = configs.small(configs.cfg4, NMC=1, ion_E=50e6)
     t = api.Tables(w, lib=gpu_lib)
@@ -119,11 +119,32 @@ def test_free_paths_and_elastic(tabs):
         g64 = _probe(t, 1, 4, 0, 0, E, u)
         assert _report("Mott FP32 vs exact", g32, exact) >= 0.999
         assert _report("Mott FP64 (reference form) vs exact", g64, exact) >= 0.99
-    else:
+    elif w.material.kind_of_EMFP == 1:
         g64 = _probe(t, 1, 5, 0, 0, E, u)
         g32 = _probe(t, 0, 5, 0, 0, E, u)
         assert np.all(np.isfinite(g64)) and np.any(g64 > 0)
         assert _report("phonon-CDF elastic", g32, g64, E, u) == 1.0
+
+
+@pytest.mark.gpu
+def test_dsf_elastic(tabs):
+    """DSF elastic draws of electrons (probe kind 6) and valence holes (7),
+    both uniforms u: FP64 equals the oracle's NRG_transfer_elastic_DSF, FP32
+    agrees within 1e-5 relative or 1e-7 eV (transfers pass through 0 eV)."""
+    w, t, o = tabs
+    if w.material.kind_of_EMFP != 2:
+        pytest.skip("not a DSF material")
+    for kind, hole, lo, hi in ((6, 0, 1.0, 1.0e5), (7, 1, 0.005, 30.0)):
+        E, u = _inputs(lo, hi, 20000, 17 + kind)
+        g64 = _probe(t, 1, kind, 0, 0, E, u)
+        ref = np.array([o.lib.oracle_dsf_transfer(o.h, hole, e, x, x) for e, x in zip(E, u)])
+        assert np.allclose(g64, ref, rtol=1e-12, atol=1e-15), kind
+        assert np.any(g64 > 0) and np.any(g64 < 0) and np.all(np.abs(g64) <= 0.25)
+        g32 = _probe(t, 0, kind, 0, 0, E, u)
+        err = np.abs(g32 - g64)
+        ok = err <= np.maximum(1e-5 * np.abs(g64), 1e-7)
+        print(f"DSF kind {kind}: max abs err {err.max():.2e} eV, {100 * ok.mean():.3f} % within")
+        assert ok.all()
 
 
 @pytest.mark.gpu
@@ -134,7 +155,7 @@ def test_fp64_redraws_counted(tabs):
     w, t, o = tabs
     _tal, s32 = api.mc_run(t, api.RunOptions(seed=3), NMC=4)
     _tal, s64 = api.mc_run(t, api.RunOptions(seed=3, precision=1), NMC=4)
-    draws = s32.n_el_inelastic + s32.n_hole_events + (s32.n_el_elastic if w.material.kind_of_EMFP == 1 else 0)
+    draws = s32.n_el_inelastic + s32.n_hole_events + (s32.n_el_elastic if w.material.kind_of_EMFP in (1, 2) else 0)
     print(f"{s32.n_fp64_redraws} of about {draws} transfer draws redone in FP64")
     assert s32.n_fp64_redraws < 0.2 * draws
     if w.material.kind_of_EMFP == 1:

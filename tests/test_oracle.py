@@ -365,6 +365,70 @@ def test_screened_phonon_tables():
         oracle_py.OracleTables(w.material.to_c(), api.ion_struct(w), abi.TableCfg(build_shi=0, build_photon=0))
 
 
+def test_dsf_reader(tmp_path):
+    """reading_DSF_cross_sections as restated by the host (material.read_dsf):
+    a written file reads back to the same tables as its rows; the cumulative
+    MFPs decrease along the transfers and their last entries are the inverse
+    integrals of the DSF over -0.2..0.2 eV (all), 0..0.2 eV (emission) and
+    -0.2..0 eV (absorption) to the resampling's accuracy; the last data line
+    of the file is not read (its block starts from a zero point)."""
+    E_in = np.logspace(-1.0, 4.0, 6)
+    lam = lambda E: 4.0 + E ** 0.5
+    n, rows = configs.synthetic_dsf_rows(E_in, lam, n_dE=120)
+    material.write_dsf(tmp_path / "x.dsf", E_in, np.array([r[1] for r in rows[:n]]),
+                       np.array([r[2] for r in rows]).reshape(len(E_in), n))
+    a, b = material.read_dsf(tmp_path / "x.dsf"), material.prepare_dsf(n, rows)
+    for f in ("E", "dE", "dL", "dL_emit", "dL_absorb"):
+        assert np.allclose(getattr(a, f), getattr(b, f), rtol=1e-9, atol=0.0), f
+    assert np.allclose(a.E, E_in, rtol=1e-9)
+    x = np.array([r[1] for r in rows[:n]])[::-1]
+    for i, E in enumerate(E_in[:-1]):            # the last block lost its lowest point
+        S = np.array([r[2] for r in rows[i * n:(i + 1) * n]])[::-1]
+        S = np.where(S < 1e-10, 0.0, S)
+        m = (x >= -0.2) & (x <= 0.2)
+        tot = np.trapezoid(S[m], x[m])
+        emi = np.trapezoid(S[m & (x >= 0)], x[m & (x >= 0)])
+        assert np.all(np.diff(a.dL[i][a.dL[i] < 1e29]) <= 0.0)
+        assert abs(a.dL[i, -1] * tot - 1.0) < 0.05, (E, a.dL[i, -1], 1 / tot)
+        assert abs(a.dL_emit[i, -1] * emi - 1.0) < 0.1, (E, a.dL_emit[i, -1], 1 / emi)
+        assert abs(1.0 / a.dL[i, -1] - 1.0 / a.dL_emit[i, -1] - 1.0 / a.dL_absorb[i, -1]) < 1e-9 / a.dL[i, -1]
+        assert abs(a.dL[i, -1] - lam(E)) < 0.1 * lam(E)
+    assert np.all(np.diff(a.dE, axis=1) > 0) and np.isclose(a.dE[0, -1], 0.2) and a.dE[0, 0] > -0.2
+
+
+def test_dsf_draw_distribution(oracle_lib):
+    """The oracle's NRG_transfer_elastic_DSF (Cross_sections.f90:3652-3795) at
+    an incident energy of the table: emissions (positive transfers) chosen in
+    the proportion L_tot / L_emit, and the mean transfer of each branch equal to
+    the DSF's mean over that branch's side of -0.2..0.2 eV."""
+    import oracle_py
+    w = configs.small(configs.cfg1_dsf, NMC=1)
+    o = oracle_py.OracleTables(w.material.to_c(), api.ion_struct(w), abi.TableCfg(build_shi=0, build_photon=0),
+                               nthreads=4)
+    d = w.material.dsf_e
+    i = 25
+    rng = np.random.Generator(np.random.PCG64(4))
+    u1, u2 = rng.uniform(1e-9, 1.0, 40000), rng.uniform(1e-9, 1.0, 40000)
+    dE = np.array([oracle_lib.oracle_dsf_transfer(o.h, 0, d.E[i], a, b) for a, b in zip(u1, u2)])
+    p_emit = d.dL[i, -1] / d.dL_emit[i, -1]
+    emit = u1 < p_emit
+    x = d.dE[i]
+    # an emission lands on the emission side or, where L_need lies beyond the
+    # first finite emission MFP, on the last absorption point (the
+    # reference's L1 > 1e20 branch); an absorption never above 0 eV + one step
+    assert dE[emit].min() >= x[x < 0.0].max() - 1e-12
+    assert dE[~emit].max() <= x[x >= 0.0].min() + 1e-12 and dE[~emit].min() >= x[0] - 1e-12
+    assert 0.5 < emit.mean() < 1.0 and abs(emit.mean() - p_emit) < 4 * np.sqrt(p_emit * (1 - p_emit) / len(u1))
+    w_all = np.diff(np.concatenate([[0.0], 1.0 / d.dL[i]]))    # per-point weights of the cumulative sum
+    w_all[~np.isfinite(w_all)] = 0.0
+    for sel, side in ((emit, x >= 0.0), (~emit, x < 0.0)):
+        want = np.sum(x[side] * w_all[side]) / np.sum(w_all[side])
+        got = dE[sel].mean()
+        se = dE[sel].std() / np.sqrt(sel.sum())
+        assert abs(got - want) < 4 * se + 0.004, (got, want)
+    o.close()
+
+
 def test_phonon_normalisation_for_screening():
     """get_single_pole's renormalisation for CDF_elast_Zeff 2 and 3
     (Cross_sections.f90:637-653): the phonon k-sum counts the atoms of a

@@ -2,13 +2,12 @@
 memory; its scratch is a fixed static device array) against the allocating
 trekis_mc_run_device on the same tables, seed and tally shape.
 
-Two no-alloc calls in a row must each reproduce the allocating call: the
-second one checks that every call clears what its kernels accumulate into.
-The tallies are int64 fixed point per batch and the batches are summed in
-FP64, so a different batch partition (the no-alloc queue capacity differs)
-only reorders those sums: rtol 1e-12 of each value plus 1e-12 of the array
-maximum.  Event counts are exact.  The file is collected last so the test
-runs both alone and after every other GPU test.
+Two no-alloc calls in a row must each reproduce the allocating call bit for
+bit: the second one checks that every call clears what its kernels
+accumulate into.  The tallies are exact integer sums over the batches, made
+FP64 once per call, so a different batch partition (the no-alloc queue
+capacity differs) changes nothing.  Event counts are exact.  The file is
+collected last so the test runs both alone and after every other GPU test.
 """
 import ctypes as C
 
@@ -16,9 +15,6 @@ import numpy as np
 import pytest
 
 from trekis import abi, api, configs
-
-RTOL = 1e-12
-
 
 def _device_tallies(torch, w, spectra=False):
     tal = api.new_tallies(w, spectra=spectra)
@@ -47,8 +43,7 @@ def _run(lib, t, w, opt, noalloc, NMC=None):
 def _close(a, b, what):
     for k in b:
         x, y = a[k], b[k]
-        tol = RTOL * np.abs(y) + RTOL * (np.max(np.abs(y)) + 1e-300)
-        bad = np.abs(x - y) > tol
+        bad = x != y
         assert not np.any(bad), f"{what} {k}: {np.sum(bad)} cells differ, max {np.max(np.abs(x - y)):.3e}"
 
 

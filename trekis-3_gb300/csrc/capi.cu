@@ -166,6 +166,25 @@ static int upload_mc(trekis_tables* t, DevTabs<T>& d) {
     };
     rowset(t->el_elast_rows, d.erow_off, d.erow_hw, d.erow_L, d.erow_mono);
     rowset(t->hole_elast_rows, d.herow_off, d.herow_hw, d.herow_L, d.herow_mono);
+    // DSF elastic tables and their per-energy total, emission and absorption MFPs
+    for (int q = 0; q < 2; ++q) {
+        const HDsf& h = t->dsf[q];
+        DevDsf<T>& g = d.dsf[q];
+        g.nE = h.nE; g.n = h.n;
+        g.E = g.dE = g.dLe = g.dLa = g.Ltot = g.Lemit = g.Labs = nullptr;
+        if (!h.nE) continue;
+        std::vector<double> lt(h.nE), le(h.nE), la(h.nE);
+        for (int i = 0; i < h.nE; ++i) {
+            const size_t last = (size_t)i * h.n + h.n - 1;
+            lt[i] = h.dL[last]; le[i] = h.dLe[last]; la[i] = h.dLa[last];
+        }
+        g.E = upload<T>(b, h.E); g.dE = upload<T>(b, h.dE); g.dLe = upload<T>(b, h.dLe); g.dLa = upload<T>(b, h.dLa);
+        g.Ltot = upload<T>(b, lt); g.Lemit = upload<T>(b, le); g.Labs = upload<T>(b, la);
+        if (!g.E || !g.dE || !g.dLe || !g.dLa || !g.Ltot || !g.Lemit || !g.Labs) {
+            set_error("table upload failed");
+            return TREKIS_ENOMEM;
+        }
+    }
     if (t->has_phot) {
         d.nP = (int)t->phot[0].E.size();
         d.pE = upload<T>(b, t->phot[0].E);
@@ -386,7 +405,8 @@ struct Workspace {
     size_t out_n = 0;
     void* evs = nullptr;       // SHI collision records of a batch
     int64_t cap_ev = 0;
-    long long* lat_rows = nullptr;
+    unsigned long long* lat_rows = nullptr;   // 2*Nt words: 128-bit row sums of the lattice energy
+    Acc acc;                                  // the call's exact sums
     // spectra: per-iteration int32 histograms of up to spec_cap iterations
     int* spec = nullptr;
     int spec_cap = 0;
@@ -455,8 +475,12 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     w->out = (double*)b.alloc(8 * w->out_n);
     w->cap_ev = std::max<int64_t>(cap / 2, 1 << 16);
     w->evs = b.alloc(shi_event_bytes() * w->cap_ev);
-    w->lat_rows = (long long*)b.alloc(8 * Nt);
-    if (!w->evs || !w->lat_rows) return nullptr;
+    w->lat_rows = (unsigned long long*)b.alloc(16 * (size_t)Nt);
+    w->acc.n2 = (size_t)Nt * NR;
+    w->acc.nh = (size_t)Nt * NR * nsh;
+    w->acc.lo = (unsigned long long*)b.alloc(8 * w->acc.n());
+    w->acc.hi = (unsigned long long*)b.alloc(8 * w->acc.n());
+    if (!w->evs || !w->lat_rows || !w->acc.lo || !w->acc.hi) return nullptr;
     w->guess = (float*)b.alloc(4 * (size_t)(w->e_inel.cap + w->h_inel.cap));
     w->prop_err = (int*)b.alloc(16);
     if (!w->guess || !w->prop_err) return nullptr;
@@ -499,9 +523,46 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     return w;
 }
 
+// The exact sums of a call as host words: every 128-bit sum as four int64
+// limbs of 32 bits (low first; the top limb carries the sign), so that
+// summing the words of several calls limb by limb, in any order, is exact.
+struct ExactIO {
+    int64_t* add_to = nullptr;          // export: the call's sums are added here, no FP64 tallies made
+    const int64_t* load = nullptr;      // import: no iterations run; the FP64 tallies of these sums are made
+};
+
+static void words_from_acc(const std::vector<unsigned long long>& lo, const std::vector<unsigned long long>& hi,
+                           int64_t* w) {
+    for (size_t x = 0; x < lo.size(); ++x) {
+        w[4 * x] += (int64_t)(lo[x] & 0xffffffffull);
+        w[4 * x + 1] += (int64_t)(lo[x] >> 32);
+        w[4 * x + 2] += (int64_t)(hi[x] & 0xffffffffull);
+        w[4 * x + 3] += (int64_t)hi[x] >> 32;
+    }
+}
+// limbs of any size and sign -> the 128-bit value sum_k limb_k 2^(32k) mod 2^128
+static void acc_from_words(const int64_t* w, size_t n, std::vector<unsigned long long>& lo,
+                           std::vector<unsigned long long>& hi) {
+    lo.assign(n, 0); hi.assign(n, 0);
+    for (size_t x = 0; x < n; ++x) {
+        unsigned long long l = 0, h = 0;
+        auto add = [&](unsigned long long vl, unsigned long long vh) {
+            const unsigned long long b = l + vl;
+            h += vh + (b < l ? 1ull : 0ull);
+            l = b;
+        };
+        const int64_t l0 = w[4 * x], l1 = w[4 * x + 1], l2 = w[4 * x + 2], l3 = w[4 * x + 3];
+        add((unsigned long long)l0, l0 < 0 ? ~0ull : 0ull);                              // l0
+        add((unsigned long long)l1 << 32, (unsigned long long)(l1 >> 32));                // l1 * 2^32
+        add(0ull, (unsigned long long)l2);                                                 // l2 * 2^64
+        add(0ull, (unsigned long long)l3 << 32);                                           // l3 * 2^96
+        lo[x] = l; hi[x] = h;
+    }
+}
+
 template <class T>
 static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, DevOut out,
-                  trekis_status* st, cudaStream_t strm) {
+                  trekis_status* st, cudaStream_t strm, const ExactIO* xio) {
     const trekis_material& m = t->mat;
     const DevTabs<T>& tb = tabs_of<T>(t);
     int rc = 0;
@@ -511,7 +572,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     McConst<T> C;
     fill_const<T>(t, cfg, Nt, C);
     C.dosE = tb.dosE; C.nD = tb.nD;
-    C.elast_cdf = (m.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
+    C.elast_model = elastic_model_of(m, tb);
     std::vector<double> tg = tallied_times(cfg.Tim, cfg.dt, cfg.dt_flag);
     std::vector<T> tgT(tg.begin(), tg.end()), RgT(cfg.Out_R, cfg.Out_R + cfg.N_R);
     std::vector<double> V(cfg.N_R);
@@ -533,6 +594,17 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     Ctrs* dctr = ws->ctr;
     const double* dV = ws->V;
     CK(cudaMemsetAsync(ws->hstage, 0, 8 * ws->hstage_n, strm));
+    const Acc& acc = ws->acc;
+    if (xio && xio->load) {
+        std::vector<unsigned long long> lo, hi;
+        acc_from_words(xio->load, acc.n(), lo, hi);
+        CK(cudaMemcpyAsync(acc.lo, lo.data(), 8 * acc.n(), cudaMemcpyHostToDevice, strm));
+        CK(cudaMemcpyAsync(acc.hi, hi.data(), 8 * acc.n(), cudaMemcpyHostToDevice, strm));
+        CK(cudaStreamSynchronize(strm));   // the host vectors go out of scope
+    } else {
+        CK(cudaMemsetAsync(acc.lo, 0, 8 * acc.n(), strm));
+        CK(cudaMemsetAsync(acc.hi, 0, 8 * acc.n(), strm));
+    }
 
     // learned proposal of the energy-transfer draw (exact: it only steers the search)
     Proposer prop;
@@ -561,7 +633,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     Ctrs hc;
     std::memset(&hc, 0, sizeof hc);
     unsigned err_bits = 0;
-    int done = 0;
+    int done = (xio && xio->load) ? cfg.NMC : 0;
     while (done < cfg.NMC) {
         const int nb = std::min(B, cfg.NMC - done);
         C.it0 = cfg.iteration_offset + done;
@@ -620,12 +692,9 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         ev_tot[7] += 2 * hc.ev[0];   // the pair of every SHI collision
         err_bits |= hc.err_bits;
         peak_all = std::max<uint64_t>(peak_all, (uint64_t)peak);
-        // flush the batch into the FP64 accumulators
-        fin_block(tal.e_cnt, tal.e_E, nullptr, Nt, NR, 1, dV, out.ne, out.Ee, nullptr, out.totNe, out.E_e, strm);
-        fin_block(tal.p_cnt, tal.p_E, nullptr, Nt, NR, 1, dV, out.np, out.Ep, nullptr, out.totNp, out.E_p, strm);
-        fin_block(tal.h_cnt, tal.h_E, tal.h_Ek, Nt, NR, nsh, dV, ws->hn, ws->hE, ws->hK, ws->htn, ws->htE, strm);
-        fin_lat(tal.lat, Nt, NR, dV, out.lat, out.E_at, ws->lat_rows, strm);
-        launches += 8;
+        // add the batch into the call's exact sums
+        acc_batch(tal, Nt, NR, nsh, acc, strm);
+        launches += 4;
         if (tal.spec) {
             fin_spectra(tal, nb, Nt, ws->wE, ws->wD, out.sEe, out.sEh, out.sth, out.sthh, strm);
             launches += 2;
@@ -637,6 +706,19 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             ws->per_it_peak = per_it;
             B = std::max(1, std::min<int>((int)(0.5 * cap / per_it), B_max));
         }
+    }
+    if (xio && xio->add_to) {   // export the exact sums; the FP64 tallies are made where they are summed
+        std::vector<unsigned long long> lo(acc.n()), hi(acc.n());
+        CK(cudaMemcpyAsync(lo.data(), acc.lo, 8 * acc.n(), cudaMemcpyDeviceToHost, strm));
+        CK(cudaMemcpyAsync(hi.data(), acc.hi, 8 * acc.n(), cudaMemcpyDeviceToHost, strm));
+        CK(cudaStreamSynchronize(strm));
+        words_from_acc(lo, hi, xio->add_to);
+        d2h += 16 * acc.n();
+    } else {
+        FinOut fo{out.ne, out.Ee, out.totNe, out.E_e, out.np, out.Ep, out.totNp, out.E_p,
+                  ws->hn, ws->hE, ws->hK, ws->htn, ws->htE, out.lat, out.E_at};
+        acc_finish(acc, Nt, NR, nsh, dV, fo, ws->lat_rows, strm);
+        launches += 5;
     }
     // holes: compact shells -> caller slices
     {
@@ -713,6 +795,10 @@ static int validate_material(const trekis_material* m) {
         return TREKIS_EINVAL;
     // mobile valence holes and DOS-derived masses read the DOS arrays
     if (m->N_dos < 2 && (m->hole_mass < 1e3 || m->El_eff_mass == 0.0)) return TREKIS_EINVAL;
+    if (m->kind_of_EMFP == 2)   // DSF elastic scattering needs both tables
+        for (const trekis_dsf* d : {m->dsf_el, m->dsf_h})
+            if (!d || d->n_E < 2 || d->n_dE < 2 || !d->E || !d->dE || !d->dL || !d->dL_emit || !d->dL_absorb)
+                return TREKIS_EINVAL;
     return TREKIS_OK;
 }
 
@@ -733,6 +819,17 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
     t->dos_M.assign(mat->dos_Eff_m, mat->dos_Eff_m + nd);
     t->mat.dos_E = t->dos_E.data(); t->mat.dos_DOS = t->dos_D.data(); t->mat.dos_int = t->dos_I.data();
     t->mat.dos_k = t->dos_k.data(); t->mat.dos_Eff_m = t->dos_M.data();
+    t->mat.dsf_el = t->mat.dsf_h = nullptr;   // the caller's DSF arrays are copied, not kept
+    if (mat->kind_of_EMFP == 2)
+        for (int q = 0; q < 2; ++q) {
+            const trekis_dsf& d = *(q ? mat->dsf_h : mat->dsf_el);
+            HDsf& h = t->dsf[q];
+            const size_t nn = (size_t)d.n_E * d.n_dE;
+            h.nE = d.n_E; h.n = d.n_dE;
+            h.E.assign(d.E, d.E + d.n_E);
+            h.dE.assign(d.dE, d.dE + nn); h.dL.assign(d.dL, d.dL + nn);
+            h.dLe.assign(d.dL_emit, d.dL_emit + nn); h.dLa.assign(d.dL_absorb, d.dL_absorb + nn);
+        }
     rc = build_tables_device(t, *cfg, st);
     if (!rc) rc = upload_mc<float>(t, t->d32);
     if (!rc) rc = upload_mc<double>(t, t->d64);
@@ -851,15 +948,15 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
 }
 
 static int run_dispatch(const trekis_tables* tc, const trekis_run_cfg* cfg, int Nt, int Nat, int Nshl, DevOut d,
-                        trekis_status* st, cudaStream_t s) {
+                        trekis_status* st, cudaStream_t s, const ExactIO* x) {
     trekis_tables* t = const_cast<trekis_tables*>(tc);
-    return (cfg->precision == 1) ? run_mc<double>(t, *cfg, Nt, Nat, Nshl, d, st, s)
-                                 : run_mc<float>(t, *cfg, Nt, Nat, Nshl, d, st, s);
+    return (cfg->precision == 1) ? run_mc<double>(t, *cfg, Nt, Nat, Nshl, d, st, s, x)
+                                 : run_mc<float>(t, *cfg, Nt, Nat, Nshl, d, st, s, x);
 }
 
-// Accumulate into device tallies; `scratch` (n_scr doubles, zeroed) backs outputs the caller skipped.
+// Accumulate into device tallies (x: exact sums exported or imported instead).
 static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, int Nt, trekis_tallies* o,
-                           trekis_status* st, cudaStream_t s, double* scratch_host_path) {
+                           trekis_status* st, cudaStream_t s, const ExactIO* x) {
     trekis_tables* t = const_cast<trekis_tables*>(tc);
     const size_t n2 = (size_t)Nt * cfg->N_R, n4 = n2 * o->Nat * o->Nshl, n3 = (size_t)Nt * o->Nat * o->Nshl;
     // the workspace holds the per-call sums; create it first
@@ -868,7 +965,6 @@ static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, i
     const bool spec = o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h;
     if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) return rc; calls = calls_of<double>(t); }
     else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) return rc; calls = calls_of<float>(t); }
-    (void)scratch_host_path;
     CK(cudaMemsetAsync(calls, 0, 8 * (3 * (size_t)Nt + n3), s));
     double* Ee_call = calls;
     double* Ep_call = calls + Nt;
@@ -884,7 +980,7 @@ static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, i
         set_error("the device entry point needs every radial and count tally array");
         return TREKIS_EINVAL;
     }
-    rc = run_dispatch(t, cfg, Nt, o->Nat, o->Nshl, d, st, s);
+    rc = run_dispatch(t, cfg, Nt, o->Nat, o->Nshl, d, st, s, x);
     if (rc) return rc;
     const int phot = t->mat.include_photons;
     if (o->Out_tot_E) k_derive<<<(Nt + 127) / 128, 128, 0, s>>>(Nt, o->Nat * o->Nshl, phot, Ee_call, Eh_call, Ep_call, Eat_call, o->Out_tot_E);
@@ -914,9 +1010,8 @@ int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
     return rc;
 }
 
-int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const trekis_ion* ion,
-                      const trekis_run_cfg* cfg, trekis_tallies* o, trekis_status* st) {
-    (void)ion;
+static int mc_run_host(const trekis_tables* tc, const trekis_material* mat, const trekis_run_cfg* cfg,
+                       trekis_tallies* o, trekis_status* st, const ExactIO* x) {
     int Nt = 0;
     int rc = check_run(tc, mat, cfg, o, &Nt);
     if (!rc && !device_ok()) rc = TREKIS_ENODEVICE;
@@ -946,7 +1041,7 @@ int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const
     d.Out_theta_h = o->Out_theta_h ? p : nullptr; p += nth2;
     if (!spec) nout = (size_t)(d.Out_E_h - base) + n3;   // stage and copy back only the main tallies
     rc = (cudaMemsetAsync(base, 0, 8 * nout, s) == cudaSuccess) ? 0 : TREKIS_ECUDA;
-    if (!rc) rc = run_device_core(t, cfg, Nt, &d, st, s, base);
+    if (!rc) rc = run_device_core(t, cfg, Nt, &d, st, s, x);
     std::vector<double> h(nout);
     if (!rc && cudaMemcpyAsync(h.data(), base, 8 * nout, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = TREKIS_ECUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = TREKIS_ECUDA;
@@ -964,6 +1059,47 @@ int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const
     return TREKIS_OK;
 }
 
+int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const trekis_ion* ion,
+                      const trekis_run_cfg* cfg, trekis_tallies* o, trekis_status* st) {
+    (void)ion;
+    return mc_run_host(tc, mat, cfg, o, st, nullptr);
+}
+
+int64_t trekis_exact_words(const trekis_tables* t, const trekis_run_cfg* cfg) {
+    if (!t || !cfg || cfg->N_R < 1) return -1;
+    const int64_t Nt = trekis_time_points(cfg->Tim, cfg->dt, cfg->dt_flag);
+    if (Nt < 1) return -1;
+    return 4 * (5 * Nt * cfg->N_R + 3 * Nt * cfg->N_R * (int64_t)t->nsh);
+}
+
+int32_t trekis_mc_run_exact(const trekis_tables* t, const trekis_material* mat, const trekis_ion* ion,
+                            const trekis_run_cfg* cfg, trekis_tallies* o, int64_t* words, int64_t n_words,
+                            trekis_status* st) {
+    (void)ion;
+    const int64_t need = trekis_exact_words(t, cfg);
+    if (!words || need < 0 || n_words != need) {
+        set_error("exact sums: words missing or of the wrong size (trekis_exact_words)");
+        if (st) st->code = TREKIS_EINVAL;
+        return TREKIS_EINVAL;
+    }
+    ExactIO x;
+    x.add_to = words;
+    return mc_run_host(t, mat, cfg, o, st, &x);
+}
+
+int32_t trekis_exact_finish(const trekis_tables* t, const trekis_material* mat, const trekis_run_cfg* cfg,
+                            const int64_t* words, int64_t n_words, trekis_tallies* o, trekis_status* st) {
+    const int64_t need = trekis_exact_words(t, cfg);
+    if (!words || need < 0 || n_words != need) {
+        set_error("exact sums: words missing or of the wrong size (trekis_exact_words)");
+        if (st) st->code = TREKIS_EINVAL;
+        return TREKIS_EINVAL;
+    }
+    ExactIO x;
+    x.load = words;
+    return mc_run_host(t, mat, cfg, o, st, &x);
+}
+
 }  // extern "C"
 
 // ---- sampler probe ------------------------------------------------------------------------
@@ -977,7 +1113,7 @@ int probe(const trekis_tables* t, const DevTabs<T>& tb, int kind, int k, int64_t
     McConst<T> C;
     fill_const<T>(t, cfg, 1, C);
     C.dosE = tb.dosE; C.nD = tb.nD;
-    C.elast_cdf = (t->mat.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
+    C.elast_model = elastic_model_of(t->mat, tb);
     double* d = nullptr;
     if (cudaMalloc(&d, 24 * (size_t)n) != cudaSuccess) { set_error("device allocation failed"); return TREKIS_ENOMEM; }
     int rc = TREKIS_OK;
@@ -996,7 +1132,7 @@ int probe(const trekis_tables* t, const DevTabs<T>& tb, int kind, int k, int64_t
 
 int32_t trekis_probe_samplers(const trekis_tables* t, int32_t precision, int32_t kind, int32_t atom, int32_t shell,
                               int64_t n, const double* E, const double* u, double* out) {
-    if (!t || n < 0 || n > (1 << 26) || (n > 0 && (!E || !u || !out)) || kind < 0 || kind > 5 || atom < 0 ||
+    if (!t || n < 0 || n > (1 << 26) || (n > 0 && (!E || !u || !out)) || kind < 0 || kind > 7 || atom < 0 ||
         atom >= t->mat.N_atoms || shell < 0 || shell >= t->mat.atoms[atom].N_shl) {
         set_error("invalid probe arguments");
         return TREKIS_EINVAL;

@@ -67,6 +67,17 @@ struct FastTab {
     int n, nb;
 };
 
+// DSF elastic tables of one particle kind on the device (kind_of_EMFP 2):
+// row-major [nE][n] transferred energies and cumulative emission / absorption
+// MFPs, and per incident energy the three total MFPs (the rows' last values).
+template <class T>
+struct DevDsf {
+    const T* E;
+    const T* dE; const T* dLe; const T* dLa;
+    const T* Ltot; const T* Lemit; const T* Labs;
+    int nE, n;
+};
+
 // Device copies of a table set, one per precision.
 template <class T>
 struct DevTabs {
@@ -99,6 +110,8 @@ struct DevTabs {
     const GHint<T>* dos_hint;   // uniform buckets over [dosE[0], dosE[nD-1]); null: bisection
     T dos_lo, dos_hi, dos_inv;
     int dos_nb;
+    // DSF elastic tables: [0] electrons, [1] valence holes (nE = 0: none)
+    DevDsf<T> dsf[2];
     // FP32 copy only: the FP64 copy of the same tables on the device.  An FP32
     // draw whose bracket is ill-conditioned (the inversion would amplify the
     // FP32 rounding of the row nodes and of L_need beyond 1e-5) is redone in
@@ -139,8 +152,17 @@ struct Buffers {          // device allocations owned by a table set
 
 }  // namespace tk
 
+namespace tk {
+// A DSF table as the caller passed it (owned copies), row-major [nE][n]
+struct HDsf {
+    int nE = 0, n = 0;
+    std::vector<double> E, dE, dL, dLe, dLa;
+};
+}  // namespace tk
+
 struct trekis_tables {
     trekis_material mat;                 // copy (DOS pointers refer to owned copies below)
+    tk::HDsf dsf[2];                     // DSF elastic tables: electrons, valence holes (kind_of_EMFP 2)
     trekis_ion ion;
     std::vector<double> dos_E, dos_D, dos_I, dos_k, dos_M;
     int nsh = 0;

@@ -808,6 +808,96 @@ __device__ T phonon_transfer(const DevTabs<T>& tb, bool hole, T Eel, S& s, bool*
     return hw;
 }
 
+// NRG_transfer_elastic_DSF (CS:3652-3795) on the DSF tables of one particle
+// kind: the emission / absorption choice by the linearly interpolated MFPs,
+// the cumulative MFP column of that choice interpolated linearly between the
+// two incident energies around Eel (negative values clamped to 0), L_need =
+// MFP / RN inverted by Linear_approx_2x1d_DSF (RF:3718-3745).  A positive
+// transfer heats the lattice, a negative one cools it.  u1, u2: the two
+// uniforms; ill (FP32): set when the draw is ill-conditioned in FP32 (the
+// choice within rounding of its threshold, the inversion steep in L, a
+// degenerate bracket, or Eel outside the table).
+template <class T>
+__device__ T dsf_transfer(const DevDsf<T>& d, T Eel, T u1, T u2, bool* ill) {
+    int NumE = find_monoton(d.E, d.nE, Eel);
+    if (NumE > 1) NumE -= 1;
+    const int i = NumE - 1;                        // rows i and i + 1 (0-based)
+    const T E1 = d.E[i], E2 = d.E[i + 1];
+    if (ill && !(Eel >= d.E[0] && Eel <= d.E[d.nE - 1])) *ill = true;
+    const T Lt = d.Ltot[i] + (d.Ltot[i + 1] - d.Ltot[i]) / (E2 - E1) * (Eel - E1);
+    const T Le = d.Lemit[i] + (d.Lemit[i + 1] - d.Lemit[i]) / (E2 - E1) * (Eel - E1);
+    const T La = d.Labs[i] + (d.Labs[i + 1] - d.Labs[i]) / (E2 - E1) * (Eel - E1);
+    const T ratio = Lt / Le;
+    const bool emit = u1 < ratio;
+    if (ill && m_abs(u1 - ratio) < T(1.0e-6)) *ill = true;
+    const T v = (Eel - E1) / (E2 - E1);
+    const int n = d.n;
+    const T* a = (emit ? d.dLe : d.dLa) + (size_t)i * n;
+    const T* b = a + n;
+    const T* xa = d.dE + (size_t)i * n;
+    const T* xb = xa + n;
+    auto Lj = [&](int j) -> T { const T x = a[j] + (b[j] - a[j]) * v; return x < T(0) ? T(0) : x; };
+    auto Xj = [&](int j) -> T { return xa[j] + (xb[j] - xa[j]) * v; };
+    const T L_need = (emit ? Le : La) / u2;
+    // Find_in_array_monoton(-L, -L_need) (RF:3433-3493): -L increases
+    const T V = -L_need;
+    int num;
+    if (V < -Lj(0)) num = 1;
+    else if (V >= -Lj(n - 1)) num = n;
+    else {
+        int i1 = 1, i2 = n;
+        while (i1 != i2 - 1) {
+            const int ic = (i1 + i2) >> 1;
+            if (-Lj(ic - 1) <= V) i1 = ic; else i2 = ic;
+        }
+        num = i1 + 1;
+    }
+    T dE;
+    if (num == 1) {
+        if (ill) *ill = true;
+        dE = Xj(0) + (Xj(1) - Xj(0)) / (Lj(1) - Lj(0)) * (L_need - Lj(0));
+    } else {
+        const T L1 = Lj(num - 2), L2 = Lj(num - 1);
+        if (m_abs(L2 - L1) < T(1.0e-9)) { if (ill) *ill = true; dE = Xj(num - 2); }
+        else if (L1 > T(1e20)) dE = Xj(num - 2);
+        else {
+            const T slope = (Xj(num - 1) - Xj(num - 2)) / (L2 - L1);
+            // FP32 L_need and nodes carry a few 1e-7 of relative error: keep the
+            // draw's error below about 1e-7 eV
+            if (ill && m_abs(slope * L_need) > T(0.25)) *ill = true;
+            dE = Xj(num - 2) + slope * (L_need - L1);
+        }
+    }
+    if (m_abs(dE) > T(1) && emit && dE > Eel) dE = Eel;   // cannot give more than it has (CS:3765-3770)
+    return dE;
+}
+
+// an FP32 DSF draw redone in FP64 on the FP64 tables (see transfer_fp64)
+__device__ __noinline__ float dsf_fp64(const DevDsf<double>& d, double Eel, double u1, double u2) {
+    return (float)dsf_transfer<double>(d, Eel, u1, u2, nullptr);
+}
+
+// The DSF elastic draw of a particle kind (hole: valence holes); defer and
+// nredo as for phonon_transfer
+template <class T, class S>
+__device__ T dsf_draw(const DevTabs<T>& tb, bool hole, T Eel, S& s, bool* defer = nullptr,
+                      unsigned long long* nredo = nullptr) {
+    T u1, u2;
+    double u1d, u2d;
+    s.next2(u1, u1d);
+    s.next2(u2, u2d);
+    bool ill = false;
+    const T dE = dsf_transfer(tb.dsf[hole ? 1 : 0], Eel, u1, u2, (sizeof(T) == 4) ? &ill : nullptr);
+    if constexpr (sizeof(T) == 4) {
+        if (ill && tb.alt) {
+            if (defer) { *defer = true; return T(0); }
+            if (nredo) ++*nredo;
+            return dsf_fp64(tb.alt->dsf[hole ? 1 : 0], (double)Eel, u1d, u2d);
+        }
+    }
+    return dE;
+}
+
 // a hole created at (X,Y,Z) with random angles (Update_holes_angles_SHI, MC:1132-1140)
 template <class T, class S>
 __device__ void make_hole(const McConst<T>& C, const DevTabs<T>& tb, P<T>& hh, T t0, T X, T Y, T Z, int k, T Eh,
@@ -1090,8 +1180,9 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ McConst<T
 // kernel): an ionising draw returns false with the particle untouched, and the
 // event is redone from the same stream by the FULL version.  DEFER leaves the
 // tally of the new segment to the caller (p.ti stays the event's grid index).
-// EL selects the elastic model at compile time (0: the run's, C.elast_cdf;
-// 1: Mott only; 2: phonon CDF only), so a hot kernel carries one model's code.
+// EL selects the elastic model at compile time (0: the run's, C.elast_model;
+// 1: Mott only; 2: phonon CDF only; 3: DSF only), so a hot kernel carries one
+// model's code.
 template <class T, bool FULL, bool DEFER = false, int EL = 0>
 __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
                                P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc,
@@ -1140,10 +1231,15 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
         nev[1]++; nev[7] += 2;
     } else {  // elastic: Mott, or the phonon CDF
-        if (EL == 2 || (EL == 0 && C.elast_cdf)) {
+        const int model = EL ? EL - 1 : C.elast_model;
+        if (model == 1) {
             bool defer = false;
             dE = phonon_transfer(tb, false, Eel, s, FULL ? nullptr : &defer, nev + 8);
             if (!FULL && defer) { p.ord = ord; return false; }   // redone by the rare kernel
+        } else if (model == 2) {
+            bool defer = false;
+            dE = dsf_draw(tb, false, Eel, s, FULL ? nullptr : &defer, nev + 8);
+            if (!FULL && defer) { p.ord = ord; return false; }
         } else dE = mott_transfer(C, Eel, T(1), s);
         angles_lat(C, Eel, dE, T(1), s, theta, phi, elastic_uniform(x, T(1) / I, Em));
         const int i = ti0;  // the interval t_{i-1} <= t < t_i
@@ -1249,10 +1345,15 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             emit_hole(C, tal, hh, ti0); push(C, tal, o, 1, hh);
             nev[3]++; nev[7] += 2;
         } else {
-            if (EL == 2 || (EL == 0 && C.elast_cdf)) {
+            const int model = EL ? EL - 1 : C.elast_model;
+            if (model == 1) {
                 bool defer = false;
                 dE = phonon_transfer(tb, true, Eel, s, FULL ? nullptr : &defer, nev + 8);
                 if (!FULL && defer) { h.ord = ord; return false; }   // redone by the rare kernel
+            } else if (model == 2) {
+                bool defer = false;
+                dE = dsf_draw(tb, true, Eel, s, FULL ? nullptr : &defer, nev + 8);
+                if (!FULL && defer) { h.ord = ord; return false; }
             } else dE = mott_transfer(C, Eel, hm, s);
             // no ionisation channel (HI >= 1e15): RN chose nothing and is reused whole
             angles_lat(C, Eel, dE, hm, s, th1, ph1, HI < T(1e15) ? elastic_uniform(x, T(1) / HI, HE) : RN);
@@ -1406,14 +1507,14 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
 }
 
 // Hot kernel of a wavefront step, one per particle kind (electrons, mobile
-// valence holes) and elastic model (PHON: phonon-CDF rows, else Mott), so each
+// valence holes) and elastic model (ELM: 0 Mott, 1 phonon-CDF rows, 2 DSF), so each
 // carries only its own event code: every particle
 // runs up to K elastic collisions.  A particle whose next event ionises goes
 // to a side queue; survivors go to the next generation's queue.  The warps
 // iterate together (a lane whose particle is done idles) so that segments
 // reaching a grid time can be parked in the warp's ring and tallied 32 at a
 // time; the tallies are integer sums, so the order does not matter.
-template <class T, bool IS_E, bool PHON>
+template <class T, bool IS_E, int ELM>
 __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<T> C,
                                              const __grid_constant__ DevTabs<T> tb, const __grid_constant__ PQ<T> in,
                                              int n, const __grid_constant__ Out<T> o, const __grid_constant__ PQ<T> side,
@@ -1442,8 +1543,8 @@ __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<
         int ia = 0, ib = -1;
         if (act) {
             bool done;
-            if constexpr (IS_E) done = electron_event<T, false, true, PHON ? 2 : 1>(C, tb, tal, o, p, err, lat, nev, mc);
-            else done = hole_event<T, false, true, PHON ? 2 : 1>(C, tb, tal, o, p, err, lat, nev, mc);
+            if constexpr (IS_E) done = electron_event<T, false, true, ELM + 1>(C, tb, tal, o, p, err, lat, nev, mc);
+            else done = hole_event<T, false, true, ELM + 1>(C, tb, tal, o, p, err, lat, nev, mc);
             if (!done) { diverted = true; act = false; }
             else {
                 ia = p.ti;
@@ -1665,14 +1766,18 @@ void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, c
     // one hot kernel per particle kind and elastic model
     if (n_in[Q_E] > 0) {
         const unsigned g = (n_in[Q_E] + bs - 1) / bs;
-        if (C.elast_cdf) k_hot<T, true, true><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
-        else k_hot<T, true, false><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+        if (C.elast_model == 1) k_hot<T, true, 1><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+        else if (C.elast_model == 2) k_hot<T, true, 2><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+        else k_hot<T, true, 0><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
     }
     if (n_in[Q_HVB] > 0) {
         const unsigned g = (n_in[Q_HVB] + bs - 1) / bs;
         cudaStream_t sh = two ? fk->s2 : s;
-        if (C.elast_cdf) k_hot<T, false, true><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
-        else k_hot<T, false, false><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+        if (C.elast_model == 1)
+            k_hot<T, false, 1><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+        else if (C.elast_model == 2)
+            k_hot<T, false, 2><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+        else k_hot<T, false, 0><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
     }
     if (two) {
         cudaEventRecord(fk->join, fk->s2);
@@ -1733,7 +1838,8 @@ __global__ void k_probe(const __grid_constant__ McConst<T> C, const __grid_const
         break;
     }
     case 4: r = mott_transfer(C, E, T(1), s); break;   // every species draws u
-    case 5: r = C.elast_cdf ? phonon_transfer(tb, false, E, s) : T(0); break;
+    case 5: r = C.elast_model == 1 ? phonon_transfer(tb, false, E, s) : T(0); break;
+    case 6: case 7: r = C.elast_model == 2 ? dsf_draw(tb, kind == 7, E, s) : T(0); break;   // DSF, both uniforms u
     default: break;
     }
     out[i] = (double)r;
@@ -1783,64 +1889,137 @@ template void launch_grid_hints<double>(const McConst<double>&, GHint<double>*, 
 
 // ---- finalize: difference arrays -> FP64 tallies -----------------------------------------
 // One thread per (slice, bin): prefix over time rows, in place (exact int64).
-__global__ void k_prefix(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR,
-                         int ns) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+// ---- exact call sums ------------------------------------------------------------------
+__device__ __forceinline__ void add128(unsigned long long* lo, unsigned long long* hi, long long v) {
+    const unsigned long long a = *lo, b = a + (unsigned long long)v;
+    *lo = b;
+    *hi += (v < 0 ? ~0ull : 0ull) + (b < a ? 1ull : 0ull);
+}
+__device__ __forceinline__ void add128(unsigned long long& lo, unsigned long long& hi, unsigned long long vlo,
+                                       unsigned long long vhi) {
+    const unsigned long long b = lo + vlo;
+    hi += vhi + (b < lo ? 1ull : 0ull);
+    lo = b;
+}
+// the 128-bit two's-complement integer (lo, hi) as a double: exactly rounded
+// where it fits in int64, else magnitude hi * 2^64 + lo with two roundings
+__device__ __forceinline__ double i128_to_double(unsigned long long lo, unsigned long long hi) {
+    const long long h = (long long)hi, l = (long long)lo;
+    if ((h == 0 && l >= 0) || (h == -1 && l < 0)) return (double)l;
+    const bool neg = h < 0;
+    if (neg) { lo = ~lo + 1ull; hi = ~hi + (lo == 0 ? 1ull : 0ull); }
+    const double m = (double)hi * 18446744073709551616.0 + (double)lo;
+    return neg ? -m : m;
+}
+
+// One thread per (slice, radius): the running sums over the difference rows
+// (plus the single-row block) give the batch's value at each time, added
+// into the exact sums at the output's index i + Nt (j + NR s).
+__global__ void k_prefix_acc(const unsigned long long* cnt, const unsigned long long* en,
+                             const unsigned long long* ek, int Nt, int NR, int ns, unsigned long long* lo,
+                             unsigned long long* hi, size_t oc, size_t oe, size_t ok) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns * NR) return;
     const int s = t / NR, j = t % NR;
     const size_t blk = (size_t)(Nt + 2) * ns * NR;   // the single-row block follows the difference block
     long long c = 0, e = 0, k = 0;
     for (int r = 1; r <= Nt; ++r) {
-        size_t a = ((size_t)r * ns + s) * NR + j;
-        c += (long long)cnt[a]; cnt[a] = (unsigned long long)(c + (long long)cnt[a + blk]);
-        e += (long long)en[a]; en[a] = (unsigned long long)(e + (long long)en[a + blk]);
-        if (ek) { k += (long long)ek[a]; ek[a] = (unsigned long long)(k + (long long)ek[a + blk]); }
+        const size_t a = ((size_t)r * ns + s) * NR + j;
+        const size_t o = (size_t)(r - 1) + (size_t)Nt * (j + (size_t)NR * s);
+        c += (long long)cnt[a];
+        e += (long long)en[a];
+        const long long vc = c + (long long)cnt[a + blk], ve = e + (long long)en[a + blk];
+        if (vc) add128(lo + oc + o, hi + oc + o, vc);
+        if (ve) add128(lo + oe + o, hi + oe + o, ve);
+        if (ek) {
+            k += (long long)ek[a];
+            const long long vk = k + (long long)ek[a + blk];
+            if (vk) add128(lo + ok + o, hi + ok + o, vk);
+        }
     }
 }
-// One thread per (slice, row): weighted bins and per-time totals.
-__global__ void k_fin(const unsigned long long* cnt, const unsigned long long* en, const unsigned long long* ek,
-                      int Nt, int NR, int ns, const double* V, double* on, double* oE, double* oK, double* tn_,
-                      double* tE) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ns * Nt) return;
-    const int s = t / Nt, i = t % Nt;
-    long long sc = 0, se = 0;
-    for (int j = 0; j < NR; ++j) {
-        size_t a = ((size_t)(i + 1) * ns + s) * NR + j;
-        long long c = (long long)cnt[a], e = (long long)en[a];
-        size_t o = (size_t)i + (size_t)Nt * (j + (size_t)NR * s);
-        on[o] += (double)c * V[j];
-        oE[o] += (double)e / kEScale * V[j];
-        sc += c; se += e;
-        if (ek) { long long k = (long long)ek[a]; oK[o] += (double)k / kEScale * V[j]; se += k; }
-    }
-    if (tn_) tn_[i + (size_t)Nt * s] += (double)sc;
-    if (tE) tE[i + (size_t)Nt * s] += (double)se / kEScale;
-}
-__global__ void k_fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL,
-                          long long* rows) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= Nt) return;
-    long long sum = 0;
-    for (int j = 0; j < NR; ++j) {
-        long long v = (long long)lat[(size_t)t * NR + j];
-        oL[(size_t)t + (size_t)Nt * j] += (double)v / kLatScale * V[j];
-        sum += v;
-    }
-    rows[t] = sum;
-}
-__global__ void k_fin_lat_scan(const long long* rows, int Nt, double* Eat) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    long long cum = 0;
-    for (int i = 0; i < Nt; ++i) { cum += rows[i]; Eat[i] += (double)cum / kLatScale; }
+__global__ void k_lat_acc(const unsigned long long* lat, int Nt, int NR, unsigned long long* lo,
+                          unsigned long long* hi) {
+    const size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= (size_t)Nt * NR) return;
+    const int i = (int)(x % Nt), j = (int)(x / Nt);
+    const long long v = (long long)lat[(size_t)i * NR + j];
+    if (v) add128(lo + x, hi + x, v);
 }
 
-void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
-               const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s) {
-    int n1 = ns * NR;
-    k_prefix<<<(n1 + 127) / 128, 128, 0, s>>>(cnt, en, ek, Nt, NR, ns);
-    int n2 = ns * Nt;
-    k_fin<<<(n2 + 127) / 128, 128, 0, s>>>(cnt, en, ek, Nt, NR, ns, V, on, oE, oK, tn_, tE);
+void acc_batch(const Tal& tal, int Nt, int NR, int nsh, const Acc& a, cudaStream_t s) {
+    k_prefix_acc<<<(NR + 127) / 128, 128, 0, s>>>(tal.e_cnt, tal.e_E, nullptr, Nt, NR, 1, a.lo, a.hi,
+                                                  a.off(ACC_ECNT), a.off(ACC_EE), 0);
+    k_prefix_acc<<<(NR + 127) / 128, 128, 0, s>>>(tal.p_cnt, tal.p_E, nullptr, Nt, NR, 1, a.lo, a.hi,
+                                                  a.off(ACC_PCNT), a.off(ACC_PE), 0);
+    if (nsh > 0)
+        k_prefix_acc<<<(nsh * NR + 127) / 128, 128, 0, s>>>(tal.h_cnt, tal.h_E, tal.h_Ek, Nt, NR, nsh, a.lo, a.hi,
+                                                            a.off(ACC_HCNT), a.off(ACC_HE), a.off(ACC_HEK));
+    const size_t n = (size_t)Nt * NR;
+    k_lat_acc<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(tal.lat, Nt, NR, a.lo + a.off(ACC_LAT),
+                                                          a.hi + a.off(ACC_LAT));
+}
+
+// One thread per (slice, time): weighted bins and per-time totals of the
+// exact sums (counts x V, energies / 2^24 x V; the totals summed exactly).
+__global__ void k_fin_acc(const unsigned long long* lo, const unsigned long long* hi, size_t oc, size_t oe,
+                          size_t ok, bool has_k, int Nt, int NR, int ns, const double* V, double* on, double* oE,
+                          double* oK, double* tn_, double* tE) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns * Nt) return;
+    const int s = t / Nt, i = t % Nt;
+    unsigned long long cl = 0, ch = 0, el = 0, eh = 0;
+    for (int j = 0; j < NR; ++j) {
+        const size_t o = (size_t)i + (size_t)Nt * (j + (size_t)NR * s);
+        const unsigned long long c0 = lo[oc + o], c1 = hi[oc + o], e0 = lo[oe + o], e1 = hi[oe + o];
+        if (c0 | c1) on[o] += i128_to_double(c0, c1) * V[j];
+        if (e0 | e1) oE[o] += i128_to_double(e0, e1) / kEScale * V[j];
+        add128(cl, ch, c0, c1);
+        add128(el, eh, e0, e1);
+        if (has_k) {
+            const unsigned long long k0 = lo[ok + o], k1 = hi[ok + o];
+            if (k0 | k1) oK[o] += i128_to_double(k0, k1) / kEScale * V[j];
+            add128(el, eh, k0, k1);
+        }
+    }
+    if (tn_) tn_[i + (size_t)Nt * s] += i128_to_double(cl, ch);
+    if (tE) tE[i + (size_t)Nt * s] += i128_to_double(el, eh) / kEScale;
+}
+__global__ void k_fin_lat_acc(const unsigned long long* lo, const unsigned long long* hi, int Nt, int NR,
+                              const double* V, double* oL, unsigned long long* rows) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= Nt) return;
+    unsigned long long sl = 0, sh = 0;
+    for (int j = 0; j < NR; ++j) {
+        const size_t o = (size_t)t + (size_t)Nt * j;
+        const unsigned long long v0 = lo[o], v1 = hi[o];
+        if (v0 | v1) oL[o] += i128_to_double(v0, v1) / kLatScale * V[j];
+        add128(sl, sh, v0, v1);
+    }
+    rows[2 * (size_t)t] = sl;
+    rows[2 * (size_t)t + 1] = sh;
+}
+__global__ void k_fin_lat_scan(const unsigned long long* rows, int Nt, double* Eat) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned long long cl = 0, ch = 0;
+    for (int i = 0; i < Nt; ++i) {
+        add128(cl, ch, rows[2 * (size_t)i], rows[2 * (size_t)i + 1]);
+        Eat[i] += i128_to_double(cl, ch) / kLatScale;
+    }
+}
+
+void acc_finish(const Acc& a, int Nt, int NR, int nsh, const double* V, const FinOut& o, unsigned long long* rows,
+                cudaStream_t s) {
+    k_fin_acc<<<(Nt + 127) / 128, 128, 0, s>>>(a.lo, a.hi, a.off(ACC_ECNT), a.off(ACC_EE), 0, false, Nt, NR, 1, V,
+                                               o.ne, o.Ee, nullptr, o.totNe, o.E_e);
+    k_fin_acc<<<(Nt + 127) / 128, 128, 0, s>>>(a.lo, a.hi, a.off(ACC_PCNT), a.off(ACC_PE), 0, false, Nt, NR, 1, V,
+                                               o.np, o.Ep, nullptr, o.totNp, o.E_p);
+    if (nsh > 0)
+        k_fin_acc<<<(nsh * Nt + 127) / 128, 128, 0, s>>>(a.lo, a.hi, a.off(ACC_HCNT), a.off(ACC_HE), a.off(ACC_HEK),
+                                                         true, Nt, NR, nsh, V, o.hn, o.hE, o.hK, o.htn, o.htE);
+    k_fin_lat_acc<<<(Nt + 127) / 128, 128, 0, s>>>(a.lo + a.off(ACC_LAT), a.hi + a.off(ACC_LAT), Nt, NR, V, o.lat,
+                                                   rows);
+    k_fin_lat_scan<<<1, 32, 0, s>>>(rows, Nt, o.E_at);
 }
 // Spectra: one thread per (iteration, column) turns the difference rows into
 // per-time counts in place; then one thread per (time, bin) adds, over the
@@ -1888,9 +2067,4 @@ void fin_spectra(const Tal& tal, int nit, int Nt, const double* wE, const double
                                                            tal.sp_it, wE, wD, oEe, oEh, oth, othh);
 }
 
-void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,
-             long long* rows, cudaStream_t s) {
-    k_fin_lat<<<(Nt + 127) / 128, 128, 0, s>>>(lat, Nt, NR, V, oL, rows);
-    k_fin_lat_scan<<<1, 32, 0, s>>>(rows, Nt, Eat);
-}
 }  // namespace tk

@@ -39,7 +39,7 @@ struct McConst {
     T mec2, alpha;      // electron rest energy [eV], fine-structure constant
     const T* dosE;      // DOS energies (the valence-hole spectrum's bins)
     int nD;
-    int elast_cdf;      // 1: phonon-CDF elastic transfers from the rows, 0: Mott
+    int elast_model;    // elastic transfers: 0 Mott, 1 phonon-CDF rows, 2 DSF tables
     int plasmon;        // plasmon_Emax: valence-band transfers may reach the plasmon energy
     T Eplasmon;         // sqrt(N_VB_el At_Dens hbar^2 / (me e0) + Egap^2) [eV]
     // derived per species for the FP32 Mott transfer (finish_const): with
@@ -227,6 +227,14 @@ inline void fill_const(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt
     finish_const(C);
 }
 
+// the elastic model of a run: 0 Mott, 1 phonon-CDF rows, 2 DSF tables
+template <class T>
+inline int elastic_model_of(const trekis_material& m, const DevTabs<T>& tb) {
+    if (m.kind_of_EMFP == 1 && tb.erow_off) return 1;
+    if (m.kind_of_EMFP == 2 && tb.dsf[0].nE > 0) return 2;
+    return 0;
+}
+
 template <class T>
 void launch_probe(const McConst<T>& C, const DevTabs<T>& tb, int kind, int k, int n, const double* E, const double* u,
                   double* out, cudaStream_t s);
@@ -246,10 +254,31 @@ inline void set_grid_hint_sizes(McConst<T>& C, T tg_first, T tg_last, T rg_first
 template <class T>
 void launch_grid_hints(const McConst<T>& C, GHint<T>* th, GHint<T>* rh, cudaStream_t s);
 
-void fin_block(unsigned long long* cnt, unsigned long long* en, unsigned long long* ek, int Nt, int NR, int ns,
-               const double* V, double* on, double* oE, double* oK, double* tn_, double* tE, cudaStream_t s);
-void fin_lat(const unsigned long long* lat, int Nt, int NR, const double* V, double* oL, double* Eat,
-             long long* rows, cudaStream_t s);
+// Exact sums of a call.  A batch's per-(slice, time, radius) sums are int64;
+// the call adds them into 128-bit two's-complement accumulators (low and high
+// words in separate arrays), and the FP64 tallies are made from those once,
+// at the end of the call.  So neither the batch partition nor a split of the
+// iterations over several calls or GPUs (whose exact sums add) changes a bit
+// of the result.  Blocks, each in the FP64 output's layout (time fastest,
+// then radius, then slice): electron counts and energies, photon counts and
+// energies [Nt*NR each], hole counts, energies and kinetic energies of the
+// compact shells [Nt*NR*nsh each], lattice energy [Nt*NR].
+struct Acc {
+    unsigned long long *lo = nullptr, *hi = nullptr;
+    size_t n2 = 0, nh = 0;   // values of a species block and of a hole block
+    size_t n() const { return 5 * n2 + 3 * nh; }
+    size_t off(int b) const { return b < 4 ? (size_t)b * n2 : (b < 7 ? 4 * n2 + (size_t)(b - 4) * nh : 4 * n2 + 3 * nh); }
+};
+enum { ACC_ECNT = 0, ACC_EE, ACC_PCNT, ACC_PE, ACC_HCNT, ACC_HE, ACC_HEK, ACC_LAT };
+// FP64 destinations of the exact sums (+=); the hole ones are the compact-shell staging
+struct FinOut {
+    double *ne, *Ee, *totNe, *E_e, *np, *Ep, *totNp, *E_p, *hn, *hE, *hK, *htn, *htE, *lat, *E_at;
+};
+// adds one batch's tallies into the call's exact sums (4 launches)
+void acc_batch(const Tal& tal, int Nt, int NR, int nsh, const Acc& a, cudaStream_t s);
+// the FP64 tallies of the exact sums, added into o (5 launches); rows: 2*Nt words of scratch
+void acc_finish(const Acc& a, int Nt, int NR, int nsh, const double* V, const FinOut& o, unsigned long long* rows,
+                cudaStream_t s);
 // spectra of one batch of nit iterations -> FP64 outputs (any may be null);
 // wE[nE], wD[nD]: bin widths in eV
 void fin_spectra(const Tal& tal, int nit, int Nt, const double* wE, const double* wD, double* oEe, double* oEh,

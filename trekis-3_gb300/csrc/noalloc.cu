@@ -13,9 +13,9 @@
 // from small host buffers on the stack.
 //
 // The kernels are the ones of the allocating path (launch_shi, launch_pairs,
-// launch_step, fin_block, fin_lat), so the tallies are the same; only the
-// batch partition can differ (it follows the queue capacity), which changes
-// the order of the FP64 batch sums and nothing else.
+// launch_step, acc_batch, acc_finish), so the tallies are the same bit for
+// bit: the batch partition can differ (it follows the queue capacity), but
+// the batches add into exact integer sums.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -95,7 +95,8 @@ struct Layout {
     unsigned long long* tall; size_t n_all; Tal tal;
     double *hstage, *hn, *hE, *hK, *htn, *htE; size_t hstage_n;
     double* calls; size_t calls_n;
-    long long* lat_rows;
+    unsigned long long* lat_rows;   // 2*Nt words
+    Acc acc;                        // the call's exact sums
     QSet<T> qa, qb;
     PQ<T> e_inel, h_inel;
     void* evs; int64_t cap_ev;
@@ -130,7 +131,11 @@ size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
     }
     L.calls_n = 3 * (size_t)s.Nt + (size_t)s.Nt * s.Nat * s.Nshl;
     L.calls = c.take<double>(L.calls_n);
-    L.lat_rows = c.take<long long>((size_t)s.Nt);
+    L.lat_rows = c.take<unsigned long long>(2 * (size_t)s.Nt);
+    L.acc.n2 = (size_t)s.Nt * s.NR;
+    L.acc.nh = (size_t)s.Nt * s.NR * s.nsh;
+    L.acc.lo = c.take<unsigned long long>(L.acc.n());
+    L.acc.hi = c.take<unsigned long long>(L.acc.n());
     for (QSet<T>* q : {&L.qa, &L.qb}) {
         take_queue(c, q->q[Q_E], cap, false);
         take_queue(c, q->q[Q_HVB], s.mobile ? cap : 1, true);
@@ -264,6 +269,8 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     // everything the kernels accumulate into starts at zero
     NA_CK(cudaMemsetAsync(L.hstage, 0, 8 * L.hstage_n, strm));
     NA_CK(cudaMemsetAsync(L.calls, 0, 8 * L.calls_n, strm));
+    NA_CK(cudaMemsetAsync(L.acc.lo, 0, 8 * L.acc.n(), strm));
+    NA_CK(cudaMemsetAsync(L.acc.hi, 0, 8 * L.acc.n(), strm));
     double* Ee_call = L.calls;
     double* Ep_call = L.calls + Nt;
     double* Eat_call = L.calls + 2 * (size_t)Nt;
@@ -273,7 +280,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     fill_const<T>(t, cfg, Nt, C);
     C.tg = L.tg; C.Rg = L.Rg;
     C.dosE = tb.dosE; C.nD = tb.nD;
-    C.elast_cdf = (t->mat.kind_of_EMFP == 1 && tb.erow_off) ? 1 : 0;
+    C.elast_model = elastic_model_of(t->mat, tb);
     {
         T first = T(0), last = T(0);
         walk_time_grid(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int i, double x) { if (i == 0) first = (T)x; last = (T)x; });
@@ -342,15 +349,18 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
         ev_tot[7] += 2 * hc.ev[0];
         err_bits |= hc.err_bits;
         peak_all = std::max<uint64_t>(peak_all, (uint64_t)peak);
-        fin_block(L.tal.e_cnt, L.tal.e_E, nullptr, Nt, NR, 1, L.V, o.Out_ne, o.Out_Ee, nullptr, o.Out_tot_Ne, Ee_call, strm);
-        fin_block(L.tal.p_cnt, L.tal.p_E, nullptr, Nt, NR, 1, L.V, o.Out_nphot, o.Out_Ephot, nullptr, o.Out_tot_Nphot,
-                  Ep_call, strm);
-        fin_block(L.tal.h_cnt, L.tal.h_E, L.tal.h_Ek, Nt, NR, nsh, L.V, L.hn, L.hE, L.hK, L.htn, L.htE, strm);
-        fin_lat(L.tal.lat, Nt, NR, L.V, o.Out_Elat, Eat_call, L.lat_rows, strm);
-        launches += 8;
+        acc_batch(L.tal, Nt, NR, nsh, L.acc, strm);
+        launches += 4;
         NA_CK(cudaGetLastError());
         done += nb;
         if (tune_batch && peak > 0) B = std::max(1, std::min<int>((int)(0.5 * cap / ((double)peak / nb)), 1 << 16));
+    }
+    // the FP64 tallies of the call's exact sums
+    {
+        const FinOut fo{o.Out_ne, o.Out_Ee, o.Out_tot_Ne, Ee_call, o.Out_nphot, o.Out_Ephot, o.Out_tot_Nphot, Ep_call,
+                        L.hn, L.hE, L.hK, L.htn, L.htE, o.Out_Elat, Eat_call};
+        acc_finish(L.acc, Nt, NR, nsh, L.V, fo, L.lat_rows, strm);
+        launches += 5;
     }
     // holes: compact shells -> caller slices; per-call energies -> caller totals
     const size_t blk = (size_t)Nt * NR, nn = blk * nsh, n3 = (size_t)Nt * o.Nat * o.Nshl;

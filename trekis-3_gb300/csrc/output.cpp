@@ -243,7 +243,8 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
         else
             o.put(std::string(" Ion equilibrium charge is used with ") + zn[(ion->Kind_Zeff >= 0 && ion->Kind_Zeff < 4) ? ion->Kind_Zeff : 0] +
                   " formula, point-like charge model for SHI.\n");
-        o.put(std::string(" Elastic scattering: ") + (m->kind_of_EMFP == 1 ? "phonon CDF" : "Mott atomic cross sections") + "\n");
+        o.put(std::string(" Elastic scattering: ") +
+              (m->kind_of_EMFP == 1 ? "phonon CDF" : m->kind_of_EMFP == 2 ? "DSF" : "Mott atomic cross sections") + "\n");
         o.put(" Number of MC iterations: " + std::to_string(oc->NMC) + "\n");
         if (oc->ion_Zeff >= 0) o.put(" Ion equilibrium charge:         " + trim(f_fmt(oc->ion_Zeff, 6, 3)) + " [electron charge]\n");
         o.put(" MC calculated energy loss (Se): " + trim(f_fmt(t->Out_tot_E[N - 1] * inv / m->Layer, 9, 2)) + " [eV/A]\n");
@@ -552,13 +553,25 @@ extern "C" int32_t trekis_save_mfp_tables(const trekis_tables* t, const trekis_o
                        : m.CDF_elast_Zeff == 3 ? "Z_CDFe_" : "Zeff_";
         ee_name = std::string("Electron_EMFPs_CDF_") + zt + temp_tag(m.temp, 7) + "_K";
         he_name = "Hole_CDF_EMFPs_" + temp_tag(m.temp, 7) + "_K";
+    } else if (m.kind_of_EMFP == 2) {   // DSF: total, emission and absorption MFPs (Analytical_IMFPs.f90:808-830, 1393-1401)
+        ee_name = "Electron_DSF_EMFPs_" + temp_tag(m.temp, 7) + "_K";
+        he_name = "Hole_DSF_EMFPs_" + temp_tag(m.temp, 7) + "_K";
     } else {
         ee_name = "Electron_EMFPs_Mott";
         he_name = "Hole_Mott_EMFPs_" + temp_tag(m.temp, 7) + "_K";
     }
-    for (auto [name, tab] : {std::make_pair(ee_name, &t->el_elast), std::make_pair(he_name, &t->hole_elast)}) {
+    for (int q = 0; q < 2; ++q) {
+        const std::string& name = q ? he_name : ee_name;
+        const tk::HTab* tab = q ? &t->hole_elast : &t->el_elast;
         Out o(D + "/OUTPUT_" + name + ".dat");
-        for (size_t i = 0; i < tab->E.size(); ++i) o.put(f_def(tab->E[i]) + e_fmt(tab->L[i]) + "\n");
+        if (m.kind_of_EMFP == 2) {
+            const tk::HDsf& h = t->dsf[q];
+            for (int i = 0; i < h.nE; ++i) {
+                const size_t last = (size_t)i * h.n + h.n - 1;
+                o.put(f_def(h.E[i]) + es_fmt(h.dL[last]) + es_fmt(h.dLe[last]) + es_fmt(h.dLa[last]) + "\n");
+            }
+        } else
+            for (size_t i = 0; i < tab->E.size(); ++i) o.put(f_def(tab->E[i]) + e_fmt(tab->L[i]) + "\n");
         ok = ok && o.ok;
     }
     if (with_rows) {

@@ -648,7 +648,7 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
         gHel = grid_4CS(m, 0.01, dosmax + 1.0);
         for (double E : gEl) { Job J{}; limits_phonon(T, E, false, J); jobs.push_back(J); }
         for (double E : gHel) { Job J{}; limits_phonon(T, E, true, J); jobs.push_back(J); }
-    } else if (m.kind_of_EMFP != 0) {
+    } else if (m.kind_of_EMFP != 0 && m.kind_of_EMFP != 2) {
         set_error("elastic kind not supported");
         return TREKIS_EUNSUPPORTED;
     }
@@ -805,6 +805,15 @@ int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_st
         mott(grid_4CS(m, 0.01, Emax_e), false, T->el_elast);
         mott(grid_4CS(m, 0.01, dosmax + 1.0), true, T->hole_elast);
     }
+    // DSF: the elastic MFPs are the tables' totals, Elastic_MFP%Total at the
+    // DSF energies (Analytical_IMFPs.f90:907-914, 1181-1186)
+    if (m.kind_of_EMFP == 2)
+        for (int q = 0; q < 2; ++q) {
+            const HDsf& h = T->dsf[q];
+            HTab& t = q ? T->hole_elast : T->el_elast;
+            t.E = h.E; t.L.resize(h.nE); t.dEdx.assign(h.nE, 0.0);
+            for (int i = 0; i < h.nE; ++i) t.L[i] = h.dL[(size_t)i * h.n + h.n - 1];
+        }
     // photons (Tot_Phot_IMFP, Cross_sections.f90:833-878): Im(-1/eps) at q = 0
     if (cfg.build_photon && m.include_photons) {
         std::vector<double> gP = grid_4CS(m, 0.1, Emax_e);

@@ -30,7 +30,7 @@ ERR_BITS = {
     1 << 6: "queue full", 1 << 7: "photon negative energy",
 }
 
-ABI_VERSION = 5   # TREKIS_ABI_VERSION of the header these structs mirror
+ABI_VERSION = 6   # TREKIS_ABI_VERSION of the header these structs mirror
 
 _S = MAX_SHELLS
 _O = MAX_OSC
@@ -47,6 +47,12 @@ class Atom(C.Structure):
     ]
 
 
+class Dsf(C.Structure):
+    _fields_ = [("n_E", C.c_int32), ("n_dE", C.c_int32), ("E", C.POINTER(C.c_double)),
+                ("dE", C.POINTER(C.c_double)), ("dL", C.POINTER(C.c_double)), ("dL_emit", C.POINTER(C.c_double)),
+                ("dL_absorb", C.POINTER(C.c_double))]
+
+
 class Material(C.Structure):
     _fields_ = [
         ("N_atoms", C.c_int32), ("atoms", Atom * MAX_ATOMS),
@@ -60,6 +66,7 @@ class Material(C.Structure):
         ("dos_int", C.POINTER(C.c_double)), ("dos_k", C.POINTER(C.c_double)), ("dos_Eff_m", C.POINTER(C.c_double)),
         ("kind_of_EMFP", C.c_int32), ("CDF_elast_Zeff", C.c_int32), ("kind_of_DR", C.c_int32),
         ("plasmon_Emax", C.c_int32), ("include_photons", C.c_int32),
+        ("dsf_el", C.POINTER(Dsf)), ("dsf_h", C.POINTER(Dsf)),
     ]
 
 
@@ -179,6 +186,11 @@ SIGNATURES = {
                                   C.POINTER(Tallies), C.POINTER(Status)]),
     "trekis_mc_run_device": (C.c_int32, [C.c_void_p, C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
                                          C.POINTER(Tallies), C.POINTER(Status)]),
+    "trekis_exact_words": (C.c_int64, [C.c_void_p, C.POINTER(RunCfg)]),
+    "trekis_mc_run_exact": (C.c_int32, [C.c_void_p, C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
+                                        C.POINTER(Tallies), C.c_void_p, C.c_int64, C.POINTER(Status)]),
+    "trekis_exact_finish": (C.c_int32, [C.c_void_p, C.POINTER(Material), C.POINTER(RunCfg), C.c_void_p, C.c_int64,
+                                        C.POINTER(Tallies), C.POINTER(Status)]),
     "trekis_mc_run_device_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(Material), C.POINTER(Ion), C.POINTER(RunCfg),
                                                  C.POINTER(Tallies), C.POINTER(Status), C.c_void_p]),
     "trekis_tc_gemm_bf16": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64, C.c_int64,

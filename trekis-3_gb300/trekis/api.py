@@ -215,6 +215,43 @@ def mc_run(tables, opt=None, NMC=None, tallies=None):
     return tal, st
 
 
+def exact_words(tables, NMC=None, opt=None):
+    """Zeroed int64 words for the exact sums of runs on these tables (trekis_exact_words)."""
+    cfg, _R = run_cfg(tables.w, opt or RunOptions(), NMC)
+    n = tables.lib.trekis_exact_words(tables.h, C.byref(cfg))
+    if n < 0:
+        raise ValueError("no exact sums for this tally shape")
+    return np.zeros(n, dtype=np.int64)
+
+
+def mc_run_exact(tables, words, opt=None, NMC=None, tallies=None):
+    """Run NMC iterations and ADD their exact tally sums to `words`
+    (trekis_mc_run_exact); the returned TallySet holds only the spectra."""
+    opt = opt or RunOptions()
+    tal = tallies or new_tallies(tables.w)
+    cfg, R = run_cfg(tables.w, opt, NMC)
+    st = abi.Status.fresh()
+    ct = tal.c()
+    assert words.dtype == np.int64 and words.flags.c_contiguous
+    rc = tables.lib.trekis_mc_run_exact(tables.h, tables.mat.ref(), C.byref(tables.ion), C.byref(cfg), C.byref(ct),
+                                        words.ctypes.data, len(words), C.byref(st))
+    abi.check(rc, tables.lib)
+    return tal, st
+
+
+def exact_finish(tables, words, tallies=None, opt=None):
+    """Add the FP64 tallies of summed exact words to `tallies` (trekis_exact_finish)."""
+    tal = tallies or new_tallies(tables.w)
+    cfg, R = run_cfg(tables.w, opt or RunOptions(), None)
+    ct = tal.c()
+    st = abi.Status.fresh()
+    words = np.ascontiguousarray(words, dtype=np.int64)
+    rc = tables.lib.trekis_exact_finish(tables.h, tables.mat.ref(), C.byref(cfg), words.ctypes.data, len(words),
+                                        C.byref(ct), C.byref(st))
+    abi.check(rc, tables.lib)
+    return tal
+
+
 # element symbols by Z (Target_atoms(i)%Name)
 ELEMENTS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga Ge As Se Br Kr "
             "Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb "

@@ -196,6 +196,41 @@ def cfg4_screened(elast_zeff=3, **kw):
     return w
 
 
+def synthetic_dsf_rows(E_in, lam, omega=0.06, kT=0.025, n_dE=100, dE_max=0.25, qe_width=0.004, qe_weight=0.3):
+    """Data lines (E, dE, S) of a seeded-shape DSF file in the reference's
+    layout (blocks of ``n_dE`` transferred energies, decreasing, per incident
+    energy): a quasi-elastic peak at 0, an emission peak at +omega and an
+    absorption peak at -omega weighted by the Bose factors at kT, scaled per
+    incident energy so that the integral over dE is 1/lam(E) [1/A]."""
+    dE = np.linspace(dE_max, -dE_max, n_dE)
+    nb = 1.0 / math.expm1(omega / kT)
+    sig = omega / 4.0
+    shape = (qe_weight * np.exp(-0.5 * (dE / qe_width) ** 2) / qe_width
+             + (nb + 1.0) * np.exp(-0.5 * ((dE - omega) / sig) ** 2) / sig
+             + nb * np.exp(-0.5 * ((dE + omega) / sig) ** 2) / sig)
+    norm = np.trapezoid(shape[::-1], dE[::-1])
+    rows = []
+    for E in E_in:
+        S = shape / (norm * lam(E))
+        rows.extend((float(E), float(d), float(v)) for d, v in zip(dE, S))
+    return n_dE, rows
+
+
+def cfg1_dsf(Tim=1000.0, NMC=10000, layer=100.0, ion_E=167e6, n_R=100):
+    """cfg1 with DSF elastic scattering (kind_of_EMFP = 2) of electrons and
+    valence holes: synthetic DSF tables on 40 incident energies 0.01 eV -
+    100 keV (elastic MFP 5 (1 + E/100 eV)^0.7 A for electrons, 3 A x the same
+    for holes), a 60 meV optical mode at room temperature."""
+    from .material import prepare_dsf
+    w = cfg1(Tim=Tim, NMC=NMC, layer=layer, ion_E=ion_E, n_R=n_R)
+    E_in = np.logspace(-2.0, 5.0, 40)
+    w.material.kind_of_EMFP = 2
+    w.material.dsf_e = prepare_dsf(*synthetic_dsf_rows(E_in, lambda E: 5.0 * (1.0 + E / 100.0) ** 0.7))
+    w.material.dsf_h = prepare_dsf(*synthetic_dsf_rows(E_in, lambda E: 3.0 * (1.0 + E / 100.0) ** 0.7))
+    w.name = "cfg1-al2o3-xe167-holes-photons-dsf"
+    return w
+
+
 def small(cfg_fn=cfg0, **kw):
     """A few-second case of a configuration for parity tests."""
     args = dict(layer=5.0, Tim=20.0, NMC=8, ion_E=20e6)

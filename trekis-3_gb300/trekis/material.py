@@ -10,6 +10,7 @@ rounded to single precision as the Fortran literals are) are restated in
 plain float64 arithmetic in the reference's order of operations.
 """
 from dataclasses import dataclass, field
+import ctypes
 import math
 import re
 
@@ -222,6 +223,23 @@ class DOS:
 
 
 @dataclass
+class DSF:
+    """Differential elastic mean free paths from a dynamic structure factor
+    (type(Differential_MFP), Objects.f90), as reading_DSF_cross_sections
+    leaves them (Reading_files_and_parameters.f90:2516-2678): for every
+    incident energy E[i] [eV] the transferred energies dE[i, :] [eV]
+    (increasing; positive = energy given to the lattice, emission) and the
+    cumulative mean free paths [A] on them: dL over all transfers, dL_emit
+    over the emissions only, dL_absorb over the absorptions only (1e30 where
+    nothing has accumulated yet)."""
+    E: np.ndarray
+    dE: np.ndarray
+    dL: np.ndarray
+    dL_emit: np.ndarray
+    dL_absorb: np.ndarray
+
+
+@dataclass
 class MaterialModel:
     name: str
     atoms: list
@@ -245,6 +263,8 @@ class MaterialModel:
     ph_osc: list = field(default_factory=list)   # [(E0, A, Gamma)]
     ph_single_pole: bool = False   # ph_osc built by get_single_pole (the file had none)
     dos: DOS = None
+    dsf_e: DSF = None    # DSF elastic scattering of electrons (kind_of_EMFP = 2)
+    dsf_h: DSF = None    # ... and of valence holes
 
     # derived (Reading_files_and_parameters.f90:1352-1354)
     @property
@@ -309,6 +329,14 @@ class MaterialModel:
             m.dos_E, m.dos_DOS, m.dos_int, m.dos_k, m.dos_Eff_m = [abi.dptr(x) for x in arrs]
         m.kind_of_EMFP, m.CDF_elast_Zeff, m.kind_of_DR = self.kind_of_EMFP, self.CDF_elast_Zeff, self.kind_of_DR
         m.plasmon_Emax, m.include_photons = self.plasmon_Emax, self.include_photons
+        for name, d in (("dsf_el", self.dsf_e), ("dsf_h", self.dsf_h)):
+            if d is None:
+                continue
+            arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (d.E, d.dE, d.dL, d.dL_emit, d.dL_absorb)]
+            c = abi.Dsf(n_E=len(arrs[0]), n_dE=arrs[1].shape[1], E=abi.dptr(arrs[0]), dE=abi.dptr(arrs[1]),
+                        dL=abi.dptr(arrs[2]), dL_emit=abi.dptr(arrs[3]), dL_absorb=abi.dptr(arrs[4]))
+            keep.extend(arrs + [c])
+            setattr(m, name, ctypes.pointer(c))
         return CHolder(m, keep)
 
 
@@ -418,6 +446,81 @@ def _find_2d(x, V):
             ic = (i1 + i2) // 2
             tv = x[ic - 1]
     return ic + 1
+
+
+# ---- DSF elastic scattering: Reading_files_and_parameters.f90:2516-2678 ------------------
+
+def _linear_approx_2d(x, y, V, El1, El2):
+    """Linear_approx_2d (RF:3272-3307) with both starting points given."""
+    n = _find_2d(x, V)
+    if n == 1:
+        return El2 + (y[0] - El2) / (x[0] - El1) * (V - El1)
+    if y[n - 2] > 1e20:
+        return y[n - 2]
+    return y[n - 2] + (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]) * (V - x[n - 2])
+
+
+def prepare_dsf(NTEPo, rows):
+    """reading_DSF_cross_sections (RF:2516-2678) from the data lines of a DSF
+    file, rows = [(E, dE, DSF)] in file order (blocks of NTEPo lines per
+    incident energy, transferred energy decreasing).  As the reference reads
+    it: the last data line of the file is not read (its loop stops one line
+    short) and counts as zeros; DSF values below 1e-10 become 0; each block is
+    reversed to increasing dE and resampled on NTEPo points from -0.2 eV up to
+    min(its largest dE, 0.2 eV) by Linear_approx_2d, the cumulative MFPs
+    summed in that order."""
+    rows = [tuple(r) for r in rows]
+    M = len(rows)
+    raw = np.zeros((M, 3))
+    for i in range(M - 1):                 # the reference reads lines 2..M of an M+1-line file
+        E, d, S = rows[i]
+        raw[i] = (E, d, 0.0 if S < 1.0e-10 else S)
+    NEPo = M // NTEPo
+    E_out, dE_out = np.zeros(NEPo), np.zeros((NEPo, NTEPo))
+    dL, dLe, dLa = np.zeros((NEPo, NTEPo)), np.zeros((NEPo, NTEPo)), np.zeros((NEPo, NTEPo))
+    for i in range(NEPo):
+        blk = raw[i * NTEPo:(i + 1) * NTEPo]
+        E_out[i] = blk[0, 0]
+        x, y = blk[::-1, 1].copy(), blk[::-1, 2].copy()     # increasing transferred energy
+        Emin = -0.2
+        Emax = min(x[NTEPo - 1], 0.2)
+        step = (Emax - Emin) / NTEPo
+        E = Emin
+        s_all = s_emit = 0.0
+        for j in range(NTEPo):
+            E = E + step
+            loc = _linear_approx_2d(x, y, E, Emin - step, 0.0)
+            s_all = s_all + loc * step
+            dE_out[i, j] = E
+            dL[i, j] = 1.0 / s_all if abs(s_all) > 1.0e-10 else 1.0e30
+            if E >= 0.0:
+                s_emit = s_emit + loc * step
+                dLe[i, j] = 1.0 / s_emit if abs(s_emit) > 1.0e-10 else 1.0e30
+                dLa[i, j] = 1.0e30 if j == 0 else dLa[i, j - 1]
+            else:
+                dLa[i, j] = 1.0 / s_all if abs(s_all) > 1.0e-10 else 1.0e30
+                dLe[i, j] = 1.0e30 if j == 0 else dLe[i, j - 1]
+    return DSF(E_out, dE_out, dL, dLe, dLa)
+
+
+def read_dsf(path):
+    """A DSF file of the reference's format (first line: transferred-energy
+    points per incident energy; then lines 'E dE DSF', dE decreasing within
+    each block) prepared as reading_DSF_cross_sections prepares it."""
+    lines = [ln for ln in open(path).read().splitlines() if ln.strip()]
+    NTEPo = int(float(lines[0].split()[0]))
+    rows = [[float(t.replace("d", "e").replace("D", "e")) for t in ln.split()[:3]] for ln in lines[1:]]
+    return prepare_dsf(NTEPo, rows)
+
+
+def write_dsf(path, E, dE, S):
+    """Write a DSF table in the reference's file format: E [nE] incident
+    energies, dE [n] transferred energies (decreasing), S [nE, n] in 1/(A eV)."""
+    with open(path, "w") as f:
+        f.write(f"{len(dE)}\n")
+        for i, e in enumerate(E):
+            for j, d in enumerate(dE):
+                f.write(f"{e:.10e} {d:.10e} {S[i, j]:.10e}\n")
 
 
 def resample_dos(e_file, dos_file, N_VB_el, At_Dens, Pers_sum):
