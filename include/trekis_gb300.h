@@ -269,9 +269,9 @@ typedef struct {
     int32_t  pad_;
     uint64_t h2d_bytes;        /* host-to-device bytes copied by the call       */
     uint64_t d2h_bytes;        /* device-to-host bytes copied by the call       */
-    uint64_t n_fp64_redraws;   /* FP32 runs: transfer draws (ionising or phonon-CDF
-                                  elastic) whose bracket was too ill-conditioned for
-                                  FP32 and that were redone in FP64 on the FP64 rows */
+    uint64_t n_fp64_redraws;   /* FP32 runs: transfer draws (ionising, ion, phonon-CDF
+                                  or DSF elastic) whose bracket was too ill-conditioned
+                                  for FP32 and that were redone in FP64 on the FP64 rows */
 } trekis_status;
 
 /* ---- entry points ------------------------------------------------------ */
@@ -610,7 +610,14 @@ int32_t trekis_save_mfp_tables(const trekis_tables* t, const trekis_output_cfg* 
  *      1: the same for a valence hole;
  *      2, 3: total inelastic / elastic electron MFP [A] (Next_free_path_2d);
  *      4: Mott elastic transfer with every species drawing u (MC:2394-2407);
- *      5: phonon-CDF elastic transfer (0 without phonon tables).
+ *      5: phonon-CDF elastic transfer (0 without phonon tables);
+ *      6, 7: DSF elastic transfer of an electron / valence hole, both
+ *         uniforms u (NRG_transfer_elastic_DSF, Cross_sections.f90:3652-3795;
+ *         0 without DSF tables);
+ *      8: the ion's transferred energy on shell (atom, shell) at ion energy
+ *         E (SHI_energy_transfer, Monte_Carlo.f90:1719-1780; 0 without SHI
+ *         tables).
+ * FP32 draws that the track loop redoes in FP64 are redone here too.
  * Needs the GPU; copies through a temporary device buffer. */
 int32_t trekis_probe_samplers(const trekis_tables* t, int32_t precision, int32_t kind, int32_t atom, int32_t shell,
                               int64_t n, const double* E, const double* u, double* out);

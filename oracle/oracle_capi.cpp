@@ -123,6 +123,9 @@ int oracle_mc_run(void* t, const trekis_material* m, const trekis_ion* ion, cons
 }
 
 // ---- pieces for known-answer and per-draw tests -----------------------------------
+double oracle_shi_transfer(void* t, const trekis_material* m, int a, int s, double E, double u) {
+    return shi_transfer_probe(*(Tables*)t, *m, a, s, E, u);
+}
 double oracle_dsf_transfer(void* t, int hole, double Eel, double u1, double u2) {
     return dsf_transfer(((Tables*)t)->dsf[hole ? 1 : 0], Eel, u1, u2);
 }

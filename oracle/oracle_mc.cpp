@@ -442,6 +442,30 @@ double shi_row_draw(const MFPTab& D, double Ip, double RN) {
     return Ip;
 }
 
+// the transfer of an SHI collision on shell (A, S) at ion energy E
+double shi_transfer(const Tables& T, double Ip, int A, int S, double E, double RN) {
+    if (T.shi_row_nodes.empty())   // the row at the initial energy (Universal_MC_for_SHI_MAIN.f90:231-238)
+        return shi_row_draw(T.shi_dsde[sidx(A, S)], Ip, RN);
+    // extension: the rows of the SHI grid energies around the ion's,
+    // combined as interpolate_transferred_energy does (Cross_sections.f90:1968-2045)
+    const std::vector<double>& gS = T.shi[sidx(A, S)].E;
+    const int w0 = T.shi_row_nodes.front(), nW = (int)T.shi_row_nodes.size();
+    int iE = find_monoton(gS.data(), (int)gS.size(), E);
+    if (iE > 1 && std::fabs(gS[iE - 2] - E) < 1.0e-6) iE -= 1;
+    auto row = [&](int node) {
+        const int q = node < w0 ? 0 : (node >= w0 + nW ? nW - 1 : node - w0);
+        return shi_row_draw(T.shi_rows_E[sidx(A, S)][q], Ip, RN);
+    };
+    const int up = iE - 1, lo = iE - 2;
+    const double d1 = row(up);
+    if (iE > 1 && lo >= w0 && up < w0 + nW) {
+        const double d2 = row(lo);
+        return (d1 < 1.0e-10 || d2 < 1.0e-10) ? interp(1, gS[lo], gS[up], d1, d2, E)
+                                              : interp(5, gS[lo], gS[up], d1, d2, E);
+    }
+    return d1;
+}
+
 // ---- SHI_Monte_Carlo (Monte_Carlo.f90:2153-2249) --------------------------------
 void shi_event(Ctx& c, int i) {
     const trekis_material& m = *c.m;
@@ -450,33 +474,7 @@ void shi_event(Ctx& c, int i) {
     int A, S;
     which_shell(c, c.T->shi, c.shi.E, s, A, S);
     // SHI_energy_transfer (Monte_Carlo.f90:1719-1780), CDF branch
-    double dE;
-    {
-        double RN = s.next();
-        const double Ip = m.atoms[A].Ip[S];
-        const Tables& T = *c.T;
-        if (T.shi_row_nodes.empty()) {   // the row at the initial energy (Universal_MC_for_SHI_MAIN.f90:231-238)
-            dE = shi_row_draw(T.shi_dsde[sidx(A, S)], Ip, RN);
-        } else {
-            // extension: the rows of the SHI grid energies around the ion's,
-            // combined as interpolate_transferred_energy does (Cross_sections.f90:1968-2045)
-            const std::vector<double>& gS = T.shi[sidx(A, S)].E;
-            const int w0 = T.shi_row_nodes.front(), nW = (int)T.shi_row_nodes.size();
-            int iE = find_monoton(gS.data(), (int)gS.size(), c.shi.E);
-            if (iE > 1 && std::fabs(gS[iE - 2] - c.shi.E) < 1.0e-6) iE -= 1;
-            auto row = [&](int node) {
-                const int q = node < w0 ? 0 : (node >= w0 + nW ? nW - 1 : node - w0);
-                return shi_row_draw(T.shi_rows_E[sidx(A, S)][q], Ip, RN);
-            };
-            const int up = iE - 1, lo = iE - 2;
-            const double d1 = row(up);
-            if (iE > 1 && lo >= w0 && up < w0 + nW) {
-                const double d2 = row(lo);
-                dE = (d1 < 1.0e-10 || d2 < 1.0e-10) ? interp(1, gS[lo], gS[up], d1, d2, c.shi.E)
-                                                    : interp(5, gS[lo], gS[up], d1, d2, c.shi.E);
-            } else dE = d1;
-        }
-    }
+    const double dE = shi_transfer(*c.T, m.atoms[A].Ip[S], A, S, c.shi.E, s.next());
     double L_new = next_free_path_2d(c.T->SHI_path, c.shi.E);
     double RN = s.next();
     L_new = -L_new * std::log(RN);
@@ -986,6 +984,10 @@ void one_iteration(Ctx& c, int64_t it_global, int sched) {
 }
 
 }  // namespace
+
+double shi_transfer_probe(const Tables& T, const trekis_material& m, int A, int S, double E, double RN) {
+    return shi_transfer(T, m.atoms[A].Ip[S], A, S, E, RN);
+}
 
 
 int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, const trekis_run_cfg& cfg,

@@ -1,8 +1,9 @@
 """Many instances at once (trekis_mc_run_batch, the cfg2 workload): every
 instance of a batch gives the tallies and counts of its own trekis_mc_run.
-Autotuning changes the compaction interval (no effect on any result) and the
-queue capacity (only the order of the FP64 batch sums), hence rtol 1e-12.
-Two instances share a table handle, which the batch must run in order."""
+Autotuning changes the compaction interval and the block size, and the batch
+driver the queue capacity: none changes a bit (the tallies are exact integer
+sums per call).  Two instances share a table handle, which the batch must run
+in order."""
 import numpy as np
 import pytest
 
@@ -17,7 +18,8 @@ def test_batch_matches_single_runs(gpu_lib):
     opts = [api.RunOptions(precision=0, seed=41) for _ in ws]
     opts.append(api.RunOptions(precision=0, seed=41, iteration_offset=1000))
     tb, sb, tune = api.mc_run_batch(tables, opts, autotune=True, max_concurrent=3)
-    assert all(t_["events_per_step"] in (32, 64, 128) and t_["queue_capacity"] >= 1 << 16 for t_ in tune)
+    assert all(t_["events_per_step"] in (32, 64, 128) and t_["block_size"] in (128, 256)
+               and t_["queue_capacity"] >= 1 << 16 for t_ in tune)
     total = 0
     for t, opt, got, st in zip(tables, opts, tb, sb):
         ref, sr = api.mc_run(t, opt)
@@ -25,7 +27,6 @@ def test_batch_matches_single_runs(gpu_lib):
         for f in ("n_shi", "n_el_inelastic", "n_el_elastic", "n_hole_events", "n_particles"):
             assert getattr(st, f) == getattr(sr, f), f
         for k in ref.a:
-            a, b = got[k], ref[k]
-            assert np.allclose(a, b, rtol=1e-12, atol=1e-12 * (np.max(np.abs(b)) + 1e-300)), k
+            assert np.array_equal(got[k], ref[k]), k
         total += st.n_events
     assert total > 0

@@ -29,11 +29,13 @@ def _probe(t, precision, kind, a, s, E, u):
     return out
 
 
-@pytest.fixture(scope="module", params=["cfg1", "cfg4", "cfg1_dsf"])
+@pytest.fixture(scope="module", params=["cfg1", "cfg4", "cfg1_dsf", "cfg1_167MeV"])
 def tabs(request, gpu_lib):
     import oracle_py
     if request.param in ("cfg1", "cfg1_dsf"):
         w = configs.small(getattr(configs, request.param), NMC=1)
+    elif request.param == "cfg1_167MeV":     # the stated ion energy: delta electrons up to 2.8 keV
+        w = configs.cfg1(NMC=1)
     else:
         w = configs.small(configs.cfg4, NMC=1, ion_E=50e6)
     t = api.Tables(w, lib=gpu_lib)
@@ -124,6 +126,28 @@ def test_free_paths_and_elastic(tabs):
         g32 = _probe(t, 0, 5, 0, 0, E, u)
         assert np.all(np.isfinite(g64)) and np.any(g64 > 0)
         assert _report("phonon-CDF elastic", g32, g64, E, u) == 1.0
+
+
+@pytest.mark.gpu
+def test_shi_transfer(tabs):
+    """The ion's transferred energy (probe kind 8, SHI_energy_transfer): FP64
+    equals the oracle on every shell, FP32 agrees with it within 1e-5 on every
+    draw, uniforms near 0 and 1 included (the flat ends of the cumulative
+    rows, where FP32 once gave non-finite transfers)."""
+    w, t, o = tabs
+    rng = np.random.Generator(np.random.PCG64(23))
+    n = 6000
+    E = np.exp(rng.uniform(np.log(0.5 * w.ion_E), np.log(1.01 * w.ion_E), n)).astype(np.float32).astype(np.float64)
+    u = np.concatenate([rng.uniform(1e-7, 1.0 - 1e-7, n - 400), np.logspace(-7, -1, 200), 1.0 - np.logspace(-7, -1, 200)])
+    u = u.astype(np.float32).astype(np.float64)
+    for a, atom in enumerate(w.material.atoms):
+        for sh in range(len(atom.shells)):
+            g64 = _probe(t, 1, 8, a, sh, E, u)
+            ref = np.array([o.lib.oracle_shi_transfer(o.h, C.addressof(t.mat.struct), a, sh, e, x) for e, x in zip(E, u)])
+            assert np.allclose(g64, ref, rtol=1e-12, atol=0.0), (a, sh)
+            g32 = _probe(t, 0, 8, a, sh, E, u)
+            assert np.all(np.isfinite(g32)), (a, sh)
+            assert _report(f"SHI transfer atom {a} shell {sh}", g32, g64, E, u) == 1.0, (a, sh)
 
 
 @pytest.mark.gpu

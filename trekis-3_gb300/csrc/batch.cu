@@ -15,8 +15,9 @@
 //
 // Autotuning (optional): per material, the largest instance runs one probe
 // iteration per candidate compaction interval (events a particle runs before
-// it is re-queued: 32, 64, 128) on its own workspace before the batch starts;
-// every instance of that material runs with the fastest.  A probe call costs
+// it is re-queued: 32, 64, 128) and block size (128, 256 threads) on its own
+// workspace before the batch starts; every instance of that material runs
+// with the fastest pair.  A probe call costs
 // about as much as a whole small instance (host-side tally staging), so
 // probing per instance would not pay.  The probes also report the live-
 // particle peak of an iteration and the queue capacity a 256-iteration batch
@@ -35,6 +36,7 @@ namespace tk {
 namespace {
 
 constexpr int kProbeK[3] = {32, 64, 128};
+constexpr int kProbeBS[2] = {128, 256};
 constexpr double kBytesPerSlot = 480.0;   // device bytes per particle slot of a workspace (queues, side queues, SHI records)
 
 // host tallies of a run's shape, for probes whose results are dropped
@@ -63,21 +65,24 @@ int tune_instance(trekis_tables* t, const trekis_material* m, const trekis_ion* 
     double best = -1.0;
     uint64_t peak = 0;
     const auto t0 = std::chrono::steady_clock::now();
-    for (int k : kProbeK) {
-        trekis_run_cfg p = cfg;                  // same queue capacity: the workspace is reused
-        p.NMC = 1;
-        p.iteration_offset = cfg.iteration_offset + cfg.NMC + (1ll << 40);   // iterations the instance never runs
-        p.events_per_step = k;
-        p.iterations_per_batch = 1;
-        trekis_status st;
-        std::memset(&st, 0, sizeof st);
-        st.first_offender = -1;
-        const int rc = trekis_mc_run(t, m, ion, &p, &sc.t, &st);
-        if (rc) return rc;
-        const double rate = st.step_ms > 0 ? (double)st.step_events / st.step_ms : 0.0;
-        peak = std::max<uint64_t>(peak, st.peak_queue);
-        if (rate > best) { best = rate; out->events_per_step = k; }
-    }
+    for (int k : kProbeK)
+        for (int bs : kProbeBS) {
+            if (cfg.block_size > 0 && bs != cfg.block_size) continue;   // a caller's block size stays
+            trekis_run_cfg p = cfg;                  // same queue capacity: the workspace is reused
+            p.NMC = 1;
+            p.iteration_offset = cfg.iteration_offset + cfg.NMC + (1ll << 40);   // iterations the instance never runs
+            p.events_per_step = k;
+            p.block_size = bs;
+            p.iterations_per_batch = 1;
+            trekis_status st;
+            std::memset(&st, 0, sizeof st);
+            st.first_offender = -1;
+            const int rc = trekis_mc_run(t, m, ion, &p, &sc.t, &st);
+            if (rc) return rc;
+            const double rate = st.step_ms > 0 ? (double)st.step_events / st.step_ms : 0.0;
+            peak = std::max<uint64_t>(peak, st.peak_queue);
+            if (rate > best) { best = rate; out->events_per_step = k; out->block_size = bs; }
+        }
     if (rep) {
         rep->events_per_step = out->events_per_step;
         rep->block_size = out->block_size > 0 ? out->block_size : 256;
@@ -143,7 +148,7 @@ extern "C" int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables, 
         }
     }
     // autotune: one probe set per material, on the largest instance of it
-    std::vector<int> K_of(n, 0);
+    std::vector<int> K_of(n, 0), BS_of(n, 0);
     std::vector<trekis_tune> probe_rep(n);
     if (autotune) {
         auto same_material = [](const trekis_material* a, const trekis_material* b) {
@@ -172,7 +177,7 @@ extern "C" int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables, 
                 return rc;
             }
             for (int j = i; j < n; ++j)
-                if (rep_of[j] == i) { K_of[j] = tuned.events_per_step; probe_rep[j] = tr; }
+                if (rep_of[j] == i) { K_of[j] = tuned.events_per_step; BS_of[j] = tuned.block_size; probe_rep[j] = tr; }
         }
     }
     // larger instances first, so the long ones do not start last
@@ -207,8 +212,10 @@ extern "C" int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables, 
                 int rc = TREKIS_OK;
                 if (K_of[i] > 0) {
                     c.events_per_step = K_of[i];
+                    if (BS_of[i] > 0) c.block_size = BS_of[i];
                     if (tr) {
                         tr->events_per_step = K_of[i];
+                        tr->block_size = c.block_size > 0 ? c.block_size : 256;
                         tr->needed_capacity = probe_rep[i].needed_capacity;
                         tr->probe_ms = probe_rep[i].probe_ms;
                     }

@@ -523,6 +523,11 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     return w;
 }
 
+__attribute__((noinline)) double radial_volume(const double* R, int j, double Layer) {
+    const double R0 = j ? R[j - 1] : 0.0;
+    return 1.0 / ((R[j] * R[j] - R0 * R0) * kPi * Layer);
+}
+
 // The exact sums of a call as host words: every 128-bit sum as four int64
 // limbs of 32 bits (low first; the top limb carries the sign), so that
 // summing the words of several calls limb by limb, in any order, is exact.
@@ -576,8 +581,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     std::vector<double> tg = tallied_times(cfg.Tim, cfg.dt, cfg.dt_flag);
     std::vector<T> tgT(tg.begin(), tg.end()), RgT(cfg.Out_R, cfg.Out_R + cfg.N_R);
     std::vector<double> V(cfg.N_R);
-    double R0 = 0.0;
-    for (int j = 0; j < cfg.N_R; ++j) { V[j] = 1.0 / ((cfg.Out_R[j] * cfg.Out_R[j] - R0 * R0) * kPi * m.Layer); R0 = cfg.Out_R[j]; }
+    for (int j = 0; j < cfg.N_R; ++j) V[j] = radial_volume(cfg.Out_R, j, m.Layer);
     CK(cudaMemcpyAsync(ws->tg, tgT.data(), sizeof(T) * Nt, cudaMemcpyHostToDevice, strm));
     CK(cudaMemcpyAsync(ws->Rg, RgT.data(), sizeof(T) * cfg.N_R, cudaMemcpyHostToDevice, strm));
     CK(cudaMemcpyAsync(ws->V, V.data(), 8 * cfg.N_R, cudaMemcpyHostToDevice, strm));
@@ -842,6 +846,13 @@ int32_t trekis_tables_build(const trekis_material* mat, const trekis_ion* ion, c
     }
     if (!rc && t->has_shi) rc = upload_shi<float>(t, t->dshi32);
     if (!rc && t->has_shi) rc = upload_shi<double>(t, t->dshi64);
+    if (!rc && t->has_shi) {   // the FP64 SHI rows on the device, for FP32 draws redone in FP64
+        DevShi<double>* a = (DevShi<double>*)t->buf.alloc(sizeof(DevShi<double>));
+        if (!a || cudaMemcpy(a, &t->dshi64, sizeof(DevShi<double>), cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("table upload failed");
+            rc = TREKIS_ENOMEM;
+        } else t->dshi32.alt = a;
+    }
     if (rc) { delete t; if (st) st->code = rc; return rc; }
     *out = t;
     if (st) st->code = TREKIS_OK;
@@ -1120,7 +1131,7 @@ int probe(const trekis_tables* t, const DevTabs<T>& tb, int kind, int k, int64_t
     if (cudaMemcpy(d, E, 8 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(d + n, u, 8 * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) rc = TREKIS_ECUDA;
     if (!rc) {
-        launch_probe<T>(C, tb, kind, k, (int)n, d, d + n, d + 2 * n, 0);
+        launch_probe<T>(C, tb, shi_of<T>(t), kind, k, (int)n, d, d + n, d + 2 * n, 0);
         if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
             cudaMemcpy(out, d + 2 * n, 8 * (size_t)n, cudaMemcpyDeviceToHost) != cudaSuccess) rc = TREKIS_ECUDA;
     }
@@ -1132,7 +1143,7 @@ int probe(const trekis_tables* t, const DevTabs<T>& tb, int kind, int k, int64_t
 
 int32_t trekis_probe_samplers(const trekis_tables* t, int32_t precision, int32_t kind, int32_t atom, int32_t shell,
                               int64_t n, const double* E, const double* u, double* out) {
-    if (!t || n < 0 || n > (1 << 26) || (n > 0 && (!E || !u || !out)) || kind < 0 || kind > 7 || atom < 0 ||
+    if (!t || n < 0 || n > (1 << 26) || (n > 0 && (!E || !u || !out)) || kind < 0 || kind > 8 || atom < 0 ||
         atom >= t->mat.N_atoms || shell < 0 || shell >= t->mat.atoms[atom].N_shl) {
         set_error("invalid probe arguments");
         return TREKIS_EINVAL;

@@ -142,6 +142,9 @@ struct DevShi {
     const T* wI; const T* wlI;         // 1/L and log
     const T* w_ia; const T* w_ib;      // [nsh*nW] 1/L at the ionisation potential, at the row's end
     const int* w_Mt;                   // [nsh*nW]
+    // the FP64 rows on the device (FP32 tables only): ill-conditioned FP32
+    // transfer draws are redone there
+    const DevShi<double>* alt = nullptr;
 };
 
 struct Buffers {          // device allocations owned by a table set
@@ -231,6 +234,10 @@ inline int walk_time_grid(double Tim, double dt, int flag, F&& f) {
     return i;
 }
 void set_error(const std::string& s);
+// Out_V of radial bin j (Sorting_output_data.f90:1432): 1 / (pi Layer (R_j^2 -
+// R_(j-1)^2)), R_(-1) = 0.  One out-of-line definition, so that every entry
+// point weights its tallies with the same bits.
+double radial_volume(const double* R, int j, double Layer);
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st);
 std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax);
 double zeff_of(const trekis_ion& ion, const trekis_material& m, double E);   // Equilibrium_charge_SHI

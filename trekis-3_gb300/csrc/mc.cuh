@@ -236,8 +236,8 @@ inline int elastic_model_of(const trekis_material& m, const DevTabs<T>& tb) {
 }
 
 template <class T>
-void launch_probe(const McConst<T>& C, const DevTabs<T>& tb, int kind, int k, int n, const double* E, const double* u,
-                  double* out, cudaStream_t s);
+void launch_probe(const McConst<T>& C, const DevTabs<T>& tb, const DevShi<T>& sh, int kind, int k, int n,
+                  const double* E, const double* u, double* out, cudaStream_t s);
 
 // the hint sizes and end values from the first and last grid points (host)
 template <class T>

@@ -258,10 +258,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     }
     rc = upload_chunked<T>(L.Rg, NR, [&](int j) { return (T)cfg.Out_R[j]; }, strm);
     if (rc) return rc;
-    rc = upload_chunked<double>(L.V, NR, [&](int j) {
-        const double R0 = j ? cfg.Out_R[j - 1] : 0.0;
-        return 1.0 / ((cfg.Out_R[j] * cfg.Out_R[j] - R0 * R0) * kPi * m.Layer);
-    }, strm);
+    rc = upload_chunked<double>(L.V, NR, [&](int j) { return radial_volume(cfg.Out_R, j, m.Layer); }, strm);
     if (rc) return rc;
     rc = upload_chunked<int>(L.hmap, nsh, [&](int k) { return t->atom_of[k] + o.Nat * t->shell_of[k]; }, strm);
     if (rc) return rc;
