@@ -446,13 +446,21 @@ __device__ T electron_receives(const McConst<T>& C, const DevTabs<T>& tb, T dE, 
 }
 
 // Hole_parameters + Assign_holes_mass (MC:724-792); p.sh, p.t0 set by the caller.
-// A cache, when given, receives the MFPs at the new kinetic energy.
+// A cache, when given, receives the MFPs at the new kinetic energy.  The
+// reference skips elastic scattering when the kinetic energy came out equal
+// to the old one (MC:746), which in FP64 happens only for a collision that
+// transferred nothing; in FP32 an elastic transfer below the rounding of the
+// energy would also leave it equal, and the hole would then fly on without
+// elastic collisions.  So `same` (>= 0) gives the caller's FP64-equivalent
+// answer -- whether the collision transferred exactly nothing -- and -1
+// compares the energies as the reference does.
 template <class T, class S>
 __device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>& h, T Eh, S& s,
-                                MfpCache<T>* cache = nullptr) {
+                                MfpCache<T>* cache = nullptr, int same = -1) {
     if (h.sh == C.vb) {
         T Etemp = h.Ek;
         h.Ek = Eh - C.Egap;
+        const bool unchanged = same >= 0 ? same != 0 : Etemp == h.Ek;
         h.E = C.Egap;
         if (C.hole_mass > T(0)) h.M = C.hole_mass;
         else h.M = tb.dosM[dos_find(tb, h.Ek) - 1];
@@ -460,7 +468,7 @@ __device__ void hole_parameters(const McConst<T>& C, const DevTabs<T>& tb, P<T>&
             const T lx = f_log(h.Ek);
             const T HI = nfp2_fast(tb.fHIMFP, h.Ek, lx);
             T HE;
-            if (Etemp == Eh - C.Egap) HE = T(1.0e30);   // the reference skips elastic scattering here (MC:746)
+            if (unchanged) HE = T(1.0e30);   // the reference skips elastic scattering here (MC:746)
             else {
                 HE = nfp2_fast(tb.fHEMFP, h.Ek, lx);
                 if (cache) { cache->E = h.Ek; cache->I = HI; cache->Em = HE; }
@@ -969,7 +977,8 @@ __device__ __forceinline__ T shi_path(const DevShi<T>& sh, int nb, T E, T lx) {
 // ill (FP32): set where the FP32 evaluation is ill-conditioned -- the
 // bracket's log-log slope steeper than kIllRow (or its two 1/L nodes equal
 // in log), a result that is not finite, or Tot within FP32 rounding of one of
-// the draw's two discontinuities
+// the draw's discontinuities (the node of Ip; a bracket whose 1/L nodes
+// differ by about 1e-6; either node of a bracket that takes its upper node)
 template <class T>
 __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* lDI, int N, int Mt, T a, T b, T Ip,
                                T RN, bool* ill = nullptr) {
@@ -988,8 +997,12 @@ __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* 
     const T E1 = DI[nt - 2], E2 = DI[nt - 1];
     if (ill && m_abs(m_abs(E2 - E1) - T(1.0e-6)) <= T(4.0e-7) * (m_abs(E1) + m_abs(E2))) *ill = true;
     T r;
-    if (m_abs(E2 - E1) < T(1.0e-6)) r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
-    else if (Tot == E1) r = DE[nt - 2];
+    if (m_abs(E2 - E1) < T(1.0e-6)) {
+        // the reference takes the upper node (Interpolate, CS:4051-4086): the
+        // bracket alone decides the draw, so Tot near either node is ill
+        if (ill && (m_abs(Tot - E1) <= T(4.0e-7) * Tot || m_abs(E2 - Tot) <= T(4.0e-7) * Tot)) *ill = true;
+        r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
+    } else if (Tot == E1) r = DE[nt - 2];
     else {
         const T dl = lDI[nt - 1] - lDI[nt - 2], de = lDE[nt - 1] - lDE[nt - 2];
         if (ill && !(m_abs(de) <= T(kIllRow) * m_abs(dl))) *ill = true;
@@ -1399,7 +1412,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
         new_angles(ph0, th0, th1, ph1, hp2, ht2);
         h.t0 = tev; h.X = X; h.Y = Y; h.Z = Z; h.th = ht2; h.ph = hp2;
         mc.E = T(-1);
-        hole_parameters(C, tb, h, Eh + C.Egap, s, &mc);
+        hole_parameters(C, tb, h, Eh + C.Egap, s, &mc, sizeof(T) == 4 ? (dE == T(0) ? 1 : 0) : -1);
         cut_h(C, h);
         if (h.Ek < T(-1.0e-9) || m_isnan(h.Ek)) err |= TREKIS_ERR_NEG_ENERGY_H;
         if constexpr (!DEFER) h.ti = emit_hole(C, tal, h, ti0);
