@@ -269,9 +269,10 @@ typedef struct {
     int32_t  pad_;
     uint64_t h2d_bytes;        /* host-to-device bytes copied by the call       */
     uint64_t d2h_bytes;        /* device-to-host bytes copied by the call       */
-    uint64_t n_fp64_redraws;   /* FP32 runs: transfer draws (ionising, ion, phonon-CDF
-                                  or DSF elastic) whose bracket was too ill-conditioned
-                                  for FP32 and that were redone in FP64 on the FP64 rows */
+    uint64_t n_fp64_redraws;   /* FP32 runs: transfer draws (ionising, phonon-CDF or
+                                  DSF elastic) whose bracket was too ill-conditioned for
+                                  FP32 and that were redone in FP64 on the FP64 rows
+                                  (the ion's own draws are FP64 throughout) */
 } trekis_status;
 
 /* ---- entry points ------------------------------------------------------ */
@@ -616,7 +617,7 @@ int32_t trekis_save_mfp_tables(const trekis_tables* t, const trekis_output_cfg* 
  *         0 without DSF tables);
  *      8: the ion's transferred energy on shell (atom, shell) at ion energy
  *         E (SHI_energy_transfer, Monte_Carlo.f90:1719-1780; 0 without SHI
- *         tables).
+ *         tables; FP64 arithmetic in both precisions, as the track draws it).
  * FP32 draws that the track loop redoes in FP64 are redone here too.
  * Needs the GPU; copies through a temporary device buffer. */
 int32_t trekis_probe_samplers(const trekis_tables* t, int32_t precision, int32_t kind, int32_t atom, int32_t shell,

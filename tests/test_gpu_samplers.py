@@ -131,9 +131,9 @@ def test_free_paths_and_elastic(tabs):
 @pytest.mark.gpu
 def test_shi_transfer(tabs):
     """The ion's transferred energy (probe kind 8, SHI_energy_transfer): FP64
-    equals the oracle on every shell, FP32 agrees with it within 1e-5 on every
-    draw, uniforms near 0 and 1 included (the flat ends of the cumulative
-    rows, where FP32 once gave non-finite transfers)."""
+    equals the oracle on every shell, uniforms near 0 and 1 included (the flat
+    ends of the cumulative rows); FP32 runs draw it in FP64 on the FP64 rows,
+    so their draws are the same bits."""
     w, t, o = tabs
     rng = np.random.Generator(np.random.PCG64(23))
     n = 6000
@@ -146,8 +146,7 @@ def test_shi_transfer(tabs):
             ref = np.array([o.lib.oracle_shi_transfer(o.h, C.addressof(t.mat.struct), a, sh, e, x) for e, x in zip(E, u)])
             assert np.allclose(g64, ref, rtol=1e-12, atol=0.0), (a, sh)
             g32 = _probe(t, 0, 8, a, sh, E, u)
-            assert np.all(np.isfinite(g32)), (a, sh)
-            assert _report(f"SHI transfer atom {a} shell {sh}", g32, g64, E, u) == 1.0, (a, sh)
+            assert np.array_equal(g32, g64), (a, sh)
 
 
 @pytest.mark.gpu

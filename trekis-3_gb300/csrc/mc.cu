@@ -974,14 +974,9 @@ __device__ __forceinline__ T shi_path(const DevShi<T>& sh, int nb, T E, T lx) {
 // SHI_energy_transfer's draw on one transfer row (MC:1719-1780): DE[N] lower
 // edges, DI = 1/L (both with logs), Mt the index of Ip, a and b 1/L at Ip and
 // at the row's end; Tot = a + RN (b - a) is inverted in 1/L, log-log
-// ill (FP32): set where the FP32 evaluation is ill-conditioned -- the
-// bracket's log-log slope steeper than kIllRow (or its two 1/L nodes equal
-// in log), a result that is not finite, or Tot within FP32 rounding of one of
-// the draw's discontinuities (the node of Ip; a bracket whose 1/L nodes
-// differ by about 1e-6; either node of a bracket that takes its upper node)
 template <class T>
 __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* lDI, int N, int Mt, T a, T b, T Ip,
-                               T RN, bool* ill = nullptr) {
+                               T RN) {
     if (N < 1) return (double)Ip;
     const T Tot = (a > T(0) && b > T(0)) ? a + RN * (b - a) : T(1.5e21);
     int nt;
@@ -990,57 +985,58 @@ __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* 
         while (lo < hi) { int mid = (lo + hi) >> 1; if (DI[mid] < Tot) lo = mid + 1; else hi = mid; }
         nt = lo + 1;
     } else nt = Mt;
-    // the two discontinuities of the draw: Tot at the node of Ip (below it
-    // the transfer is Ip) and a bracket whose 1/L nodes differ by about 1e-6
-    if (ill && Mt >= 1 && Mt <= N && m_abs(Tot - DI[Mt - 1]) <= T(4.0e-7) * Tot) *ill = true;
     if (nt <= Mt) return (double)Ip;
     const T E1 = DI[nt - 2], E2 = DI[nt - 1];
-    if (ill && m_abs(m_abs(E2 - E1) - T(1.0e-6)) <= T(4.0e-7) * (m_abs(E1) + m_abs(E2))) *ill = true;
     T r;
-    if (m_abs(E2 - E1) < T(1.0e-6)) {
-        // the reference takes the upper node (Interpolate, CS:4051-4086): the
-        // bracket alone decides the draw, so Tot near either node is ill
-        if (ill && (m_abs(Tot - E1) <= T(4.0e-7) * Tot || m_abs(E2 - Tot) <= T(4.0e-7) * Tot)) *ill = true;
-        r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
-    } else if (Tot == E1) r = DE[nt - 2];
-    else {
-        const T dl = lDI[nt - 1] - lDI[nt - 2], de = lDE[nt - 1] - lDE[nt - 2];
-        if (ill && !(m_abs(de) <= T(kIllRow) * m_abs(dl))) *ill = true;
-        r = m_exp(lDE[nt - 2] + de / dl * (m_log(Tot) - lDI[nt - 2]));
-    }
-    if (ill && !(m_abs(r) < T(1e30))) *ill = true;
+    if (m_abs(E2 - E1) < T(1.0e-6)) r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
+    else if (Tot == E1) r = DE[nt - 2];
+    else r = m_exp(lDE[nt - 2] + (lDE[nt - 1] - lDE[nt - 2]) / (lDI[nt - 1] - lDI[nt - 2]) * (m_log(Tot) - lDI[nt - 2]));
     return (double)r;
 }
 
-// The transfer of an SHI collision on shell k at ion energy Et (grid bin nb
-// of Et): the row at the initial energy, or with rows by energy the two rows
-// around Et combined as interpolate_transferred_energy combines two rows
-// (CS:1968-2045); ill as for shi_row_draw, also set where the two rows'
-// combination is steep in energy.
+// The transfer of an SHI collision on shell k at ion energy E: the row at the
+// initial energy, or with rows by energy the two rows around E combined as
+// interpolate_transferred_energy combines two rows (CS:1968-2045).
 template <class T>
-__device__ double shi_transfer(const DevShi<T>& sh, int k, T Ip, T Et, int nb, T RN, bool* ill) {
+__device__ double shi_transfer(const DevShi<T>& sh, int k, T Ip, T E, T RN) {
     if (sh.nW == 0) {   // the row at the initial energy (Universal_MC_for_SHI_MAIN.f90:231-238)
         const int o0 = sh.d_off[k];
         return shi_row_draw(sh.dE + o0, sh.ldE + o0, sh.dI + o0, sh.ldI + o0, sh.d_off[k + 1] - o0, sh.Mt[k],
-                            sh.invdL_ip[k], sh.invL_last[k], Ip, RN, ill);
+                            sh.invdL_ip[k], sh.invL_last[k], Ip, RN);
     }
-    int iE = nb;
-    if (iE > 1 && m_abs(sh.sE[iE - 2] - Et) < T(1.0e-6)) iE -= 1;
+    int iE = find_monoton(sh.sE, sh.nS, E);
+    if (iE > 1 && m_abs(sh.sE[iE - 2] - E) < T(1.0e-6)) iE -= 1;
     auto row = [&](int node) -> double {
         const int q = node < sh.w0 ? 0 : (node >= sh.w0 + sh.nW ? sh.nW - 1 : node - sh.w0);
         const int r = k * sh.nW + q, o = sh.wr_off[r];
         return shi_row_draw(sh.wE + o, sh.wlE + o, sh.wI + o, sh.wlI + o, sh.wr_off[r + 1] - o, sh.w_Mt[r],
-                            sh.w_ia[r], sh.w_ib[r], Ip, RN, ill);
+                            sh.w_ia[r], sh.w_ib[r], Ip, RN);
     };
     const int up = iE - 1, lo = iE - 2;   // 0-based nodes above and below the ion's energy
     const T d1 = (T)row(up);
     if (iE > 1 && lo >= sh.w0 && up < sh.w0 + sh.nW) {
         const T d2 = (T)row(lo);
-        if (d1 < T(1.0e-10) || d2 < T(1.0e-10)) return (double)interp<T>(1, sh.sE[lo], sh.sE[up], d1, d2, Et);
-        if (ill && steep(sh.sE[lo], sh.sE[up], d1, d2, T(kIllE))) *ill = true;
-        return (double)interp5_acc<T>(sh.sE[lo], sh.sE[up], d1, d2, Et);
+        return (double)((d1 < T(1.0e-10) || d2 < T(1.0e-10)) ? interp<T>(1, sh.sE[lo], sh.sE[up], d1, d2, E)
+                                                            : interp5_acc<T>(sh.sE[lo], sh.sE[up], d1, d2, E));
     }
     return (double)d1;
+}
+
+// The ion's transfer as the track draws it in precision T.  FP32 runs draw it
+// in FP64 on the FP64 rows: the ion's energy is FP64 already, the rows are
+// short, and in FP32 the reference's jumps of the draw (to the upper node of
+// a bracket whose 1/L nodes differ by less than 1e-6, to Ip below the node of
+// Ip) fall on other brackets often enough to move whole draws by a node.
+template <class T>
+__device__ __forceinline__ double shi_draw(const McConst<T>& C, const DevShi<T>& sh, int k, double E, T RN,
+                                           double RNd) {
+    if constexpr (sizeof(T) == 4) {
+        if (sh.alt) return shi_transfer<double>(*sh.alt, k, C.Ipd[k], E, RNd);
+        return shi_transfer<T>(sh, k, C.Ip[k], (T)E, RN);
+    } else {
+        (void)RNd;
+        return shi_transfer<T>(sh, k, C.Ip[k], (T)E, RN);
+    }
 }
 
 struct ShiEv {  // one SHI collision: the ion state after it and the transfer
@@ -1066,7 +1062,7 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
     const int it = blockIdx.x * blockDim.x + threadIdx.x;
     if (it >= nit) return;
     unsigned err = 0;
-    unsigned long long nev = 0, nredo = 0;
+    unsigned long long nev = 0;
     const uint64_t pid = shi_pid(C.it0 + it);
     constexpr bool F32 = sizeof(T) == 4;
     const double vfac = 2.0 * kE / (C.ion_mass_p * kMp);   // v^2 = vfac E
@@ -1116,15 +1112,7 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
             T RN;
             double RNd;
             s.next2(RN, RNd);
-            bool ill = false;
-            dE = shi_transfer(sh, k, C.Ip[k], Et, nb, RN, F32 ? &ill : nullptr);
-            if constexpr (F32) {
-                if (ill && sh.alt) {   // redo it in FP64 on the FP64 rows, from the same random word
-                    const DevShi<double>& a = *sh.alt;
-                    dE = shi_transfer<double>(a, k, C.Ipd[k], E, find_monoton(a.sE, a.nS, E), RNd, nullptr);
-                    ++nredo;
-                }
-            }
+            dE = shi_draw(C, sh, k, E, RN, RNd);
         }
         // next flight with the energy before the loss
         double Lnew = (double)shi_path(sh, nb, Et, lx);
@@ -1173,7 +1161,6 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
     for (; slot < slot_end; ++slot)   // mark the rest of the last chunk unused
         if (slot < cap_ev) evs[slot].it = -1;
     if (nev) atomicAdd(&ctr->ev[0], nev);
-    if (nredo) atomicAdd(&ctr->ev[8], nredo);
     if (err) atomicOr(&ctr->err_bits, err);
 }
 
@@ -1885,17 +1872,9 @@ __global__ void k_probe(const __grid_constant__ McConst<T> C, const __grid_const
     case 4: r = mott_transfer(C, E, T(1), s); break;   // every species draws u
     case 5: r = C.elast_model == 1 ? phonon_transfer(tb, false, E, s) : T(0); break;
     case 6: case 7: r = C.elast_model == 2 ? dsf_draw(tb, kind == 7, E, s) : T(0); break;   // DSF, both uniforms u
-    case 8: {   // the ion's transfer on shell k at ion energy E, as k_shi_track draws it
-        if (sh.nS < 2) break;
-        bool ill = false;
-        double d = shi_transfer(sh, k, C.Ip[k], E, find_monoton(sh.sE, sh.nS, E), u, sizeof(T) == 4 ? &ill : nullptr);
-        if constexpr (sizeof(T) == 4)
-            if (ill && sh.alt)
-                d = shi_transfer<double>(*sh.alt, k, C.Ipd[k], Ein[i], find_monoton(sh.alt->sE, sh.alt->nS, Ein[i]),
-                                         uin[i], nullptr);
-        out[i] = d;
+    case 8:   // the ion's transfer on shell k at ion energy E, as k_shi_track draws it
+        out[i] = sh.nS < 2 ? 0.0 : shi_draw(C, sh, k, Ein[i], u, uin[i]);
         return;
-    }
     default: break;
     }
     out[i] = (double)r;
