@@ -13,7 +13,7 @@
 module trekis_gb300
   use iso_c_binding
   implicit none
-  integer, parameter :: TREKIS_ABI_VERSION = 6
+  integer, parameter :: TREKIS_ABI_VERSION = 7
   integer, parameter :: TREKIS_MAX_ATOMS = 8, TREKIS_MAX_SHELLS = 16, &
                         TREKIS_MAX_OSC = 16, TREKIS_MAX_PH_OSC = 8
   ! return codes
@@ -110,8 +110,9 @@ module trekis_gb300
   end type
 
   type, bind(C) :: trekis_batch_cfg
-     integer(c_int32_t) :: max_concurrent, autotune    ! 0: 16 in flight; 1: probe 32/64/128 collisions per visit
+     integer(c_int32_t) :: max_concurrent, autotune    ! 0: 16 in flight; 1: probe collisions per visit, block size
      integer(c_int64_t) :: device_budget               ! bytes for all workspaces (0: 3/4 of the free memory)
+     integer(c_int32_t) :: separate, pad_              ! 1: one wavefront per instance (never merged)
   end type
 
   type, bind(C) :: trekis_tune

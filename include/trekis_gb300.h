@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TREKIS_ABI_VERSION 6
+#define TREKIS_ABI_VERSION 7
 
 #define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
 #define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
@@ -463,21 +463,36 @@ int32_t trekis_mc_run_device_noalloc(const trekis_tables* t, const trekis_materi
 
 /* ---- many instances on one GPU (no counterpart in the reference) ----------
  * Runs n independent track-loop calls (each one what trekis_mc_run does with
- * tables[i], mats[i], ions[i], cfgs[i] into the host tallies[i]) with up to
- * max_concurrent of them in flight on their own CUDA streams, so instances
- * of very different cascade size share the GPU.  Instances that share a
- * table handle run one after the other.  Every table set's workspace is
- * allocated before the runs with an even share of device_budget (<= 0: three
- * quarters of the free device memory) unless its cfg sets queue_capacity,
- * and released at the end (trekis_tables_trim).  With autotune, the largest
- * instance of each material (among those without their own events_per_step)
- * first runs one probe iteration per candidate events_per_step (32, 64, 128)
- * and all instances of that material take the fastest; the choices land in
- * tune[i] (may be NULL).  Returns the first instance's error, if any. */
+ * tables[i], mats[i], ions[i], cfgs[i] into the host tallies[i]), so
+ * instances of very different cascade size share the GPU:
+ *   - merged (the default when every instance has its own table handle):
+ *     instances of one material -- equal trekis_material (DOS arrays by
+ *     content), time grid, radii, precision, seed and scheduling knobs, no
+ *     spectra, sampler 0 -- run as one wavefront, their iterations side by
+ *     side in the same batches and each particle's tallies and counts kept
+ *     per instance; each ion track runs on its instance's own tables.  One
+ *     workspace per material, on the tables of its largest instance.  The
+ *     tallies and event counts are bit for bit those of the instance's own
+ *     trekis_mc_run; the wavefront's figures in the status (n_steps,
+ *     device_ms, step_ms, launches, copies, peak queue) are the material's.
+ *   - separate (bcfg->separate, a shared table handle, or no two instances
+ *     mergeable): up to max_concurrent instances in flight on their own
+ *     CUDA streams; instances that share a table handle run one after the
+ *     other.
+ * Every workspace is allocated before the runs with an even share of
+ * device_budget (<= 0: three quarters of the free device memory) unless the
+ * cfg sets queue_capacity, and released at the end (trekis_tables_trim).
+ * With autotune, the largest instance of each material (among those without
+ * their own events_per_step) first runs one probe iteration per candidate
+ * events_per_step (32, 64, 128) and block size (128, 256), and all instances
+ * of that material take the fastest pair; the choices land in tune[i] (may
+ * be NULL).  Returns the first instance's error, if any. */
 typedef struct {
     int32_t max_concurrent;   /* 0: 16 */
     int32_t autotune;
     int64_t device_budget;    /* bytes */
+    int32_t separate;         /* 1: one wavefront per instance, never merged */
+    int32_t pad_;
 } trekis_batch_cfg;
 
 typedef struct {

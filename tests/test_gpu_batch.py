@@ -30,3 +30,34 @@ def test_batch_matches_single_runs(gpu_lib):
             assert np.array_equal(got[k], ref[k]), k
         total += st.n_events
     assert total > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1])
+def test_merged_batch_matches_single_runs(gpu_lib, precision):
+    """Instances of one material share a wavefront (every instance with its
+    own tables): each instance's tallies and event counts are bit for bit
+    those of its own trekis_mc_run, the instances of a material report the
+    same wavefront figures, and bcfg.separate gives the same tallies."""
+    ws = configs.cfg2(n_inst=7, layer=5.0, Tim=10.0, nmc_scale=0.002)
+    tables = [api.Tables(w, lib=gpu_lib) for w in ws]
+    opts = [api.RunOptions(precision=precision, seed=43, iteration_offset=100 * i) for i in range(len(ws))]
+    tm, sm, tune = api.mc_run_batch(tables, opts, autotune=True)
+    ts, ss, _ = api.mc_run_batch(tables, opts, autotune=False, separate=True)
+    mats = [w.notes["material"] for w in ws]
+    assert len(set(mats)) < len(mats)              # some material has several instances
+    for i, (t, opt) in enumerate(zip(tables, opts)):
+        ref, sr = api.mc_run(t, opt)
+        for st in (sm[i], ss[i]):
+            assert st.code == 0 and st.n_events == sr.n_events > 0, (i, st.n_events, sr.n_events)
+            for f in ("n_shi", "n_el_inelastic", "n_el_elastic", "n_hole_events", "n_particles", "n_photon_abs"):
+                assert getattr(st, f) == getattr(sr, f), (i, f)
+        for k in ref.a:
+            assert np.array_equal(tm[i][k], ref[k]), (i, k)
+            assert np.array_equal(ts[i][k], ref[k]), (i, k)
+    for m in set(mats):
+        group = [i for i in range(len(ws)) if mats[i] == m]
+        assert len({sm[i].n_steps for i in group}) == 1    # one wavefront per material
+        assert len({(tune[i]["events_per_step"], tune[i]["block_size"]) for i in group}) == 1
+    for t in tables:
+        t.close()

@@ -13,6 +13,14 @@
 // release synchronise the whole device, which would serialise the streams);
 // they are released when all instances are done.
 //
+// Instances of one material share one wavefront when every instance has its
+// own table set (mc_run_group: their iterations side by side in the same
+// batches, each particle's tallies and counts kept per instance, each ion
+// track on its own tables), so small instances stop costing a host round
+// trip per wavefront step each.  Their tallies are the same bits as their own
+// runs (exact integer sums).  trekis_batch_cfg.separate keeps one wavefront
+// per instance.
+//
 // Autotuning (optional): per material, the largest instance runs one probe
 // iteration per candidate compaction interval (events a particle runs before
 // it is re-queued: 32, 64, 128) and block size (128, 256 threads) on its own
@@ -93,10 +101,128 @@ int tune_instance(trekis_tables* t, const trekis_material* m, const trekis_ion* 
     return TREKIS_OK;
 }
 
+bool same_material(const trekis_material* a, const trekis_material* b) {
+    trekis_material x = *a, y = *b;   // the DOS arrays compared by content below
+    x.dos_E = x.dos_DOS = x.dos_int = x.dos_k = x.dos_Eff_m = nullptr;
+    y.dos_E = y.dos_DOS = y.dos_int = y.dos_k = y.dos_Eff_m = nullptr;
+    if (std::memcmp(&x, &y, sizeof x) != 0) return false;
+    const size_t nd = (size_t)(a->N_dos > 0 ? a->N_dos : 0);
+    auto eq = [&](const double* u, const double* v) {
+        return u == v || (u && v && std::memcmp(u, v, 8 * nd) == 0);
+    };
+    return eq(a->dos_E, b->dos_E) && eq(a->dos_DOS, b->dos_DOS) && eq(a->dos_int, b->dos_int) &&
+           eq(a->dos_k, b->dos_k) && eq(a->dos_Eff_m, b->dos_Eff_m);
+}
+
+// Whether instances i and j may share one wavefront: the same material (so
+// the same electron, hole, photon and elastic tables; the tables do not
+// depend on the ion), tally shape, time grid, precision, seed and knobs; no
+// spectra, table sampler.
+bool mergeable(const trekis_material* mi, const trekis_material* mj, const trekis_run_cfg& a, const trekis_run_cfg& b,
+               const trekis_tallies& ta, const trekis_tallies& tb) {
+    if (!same_material(mi, mj)) return false;
+    if (a.precision != b.precision || a.seed != b.seed || a.sampler != 0 || b.sampler != 0 || a.Tim != b.Tim ||
+        a.dt != b.dt || a.dt_flag != b.dt_flag || a.N_R != b.N_R || a.events_per_step != b.events_per_step ||
+        a.block_size != b.block_size || a.queue_capacity != b.queue_capacity || a.use_graph != b.use_graph)
+        return false;
+    if (a.N_R > 0 && std::memcmp(a.Out_R, b.Out_R, 8 * (size_t)a.N_R) != 0) return false;
+    if (ta.Nat != tb.Nat || ta.Nshl != tb.Nshl) return false;
+    for (const trekis_tallies* t : {&ta, &tb})
+        if (t->Out_Ee_vs_E || t->Out_Eh_vs_E || t->Out_theta || t->Out_theta_h) return false;
+    return true;
+}
+
 }  // namespace
 }  // namespace tk
 
 using namespace tk;
+
+// The merged path of trekis_mc_run_batch: instances of one material share a
+// wavefront (mc_run_group), one worker and one workspace per material.
+static int32_t run_batch_merged(int32_t n, trekis_tables* const* tables, const trekis_material* const* mats,
+                                const trekis_ion* const* ions, const trekis_run_cfg* cfgs, trekis_tallies* tallies,
+                                trekis_status* status, int conc, bool autotune, int64_t budget, trekis_tune* tune,
+                                const std::vector<std::vector<int>>& units) {
+    bool fp64 = false;
+    for (int i = 0; i < n; ++i) fp64 |= cfgs[i].precision == 1;
+    const double per_slot = fp64 ? 2.0 * kBytesPerSlot : kBytesPerSlot;
+    const int64_t cap_share = std::max<int64_t>(1 << 16, std::min<int64_t>((int64_t)64 << 20,
+        (int64_t)((double)budget / (double)units.size() / per_slot)));
+    auto trim_all = [&]() { for (const std::vector<int>& u : units) trekis_tables_trim(tables[u.front()]); };
+    // a workspace per unit, on its first instance's tables (the largest, which also probes)
+    std::vector<trekis_run_cfg> cf(cfgs, cfgs + n);
+    std::vector<trekis_tune> rep(n);
+    for (const std::vector<int>& u : units) {
+        const int f = u.front();
+        const int64_t cap = cfgs[f].queue_capacity > 0 ? cfgs[f].queue_capacity : cap_share;
+        for (int i : u) cf[i].queue_capacity = cap;
+        trekis_run_cfg c0 = cf[f];
+        c0.NMC = 0;
+        trekis_status st0;
+        std::memset(&st0, 0, sizeof st0);
+        int rc = trekis_mc_run(tables[f], mats[f], ions[f], &c0, &tallies[f], &st0);
+        if (!rc && autotune && cfgs[f].events_per_step <= 0) {
+            trekis_run_cfg tuned;
+            trekis_tune tr;
+            std::memset(&tr, 0, sizeof tr);
+            rc = tune_instance(tables[f], mats[f], ions[f], cf[f], tallies[f], &tuned, &tr);
+            for (int i : u) {
+                cf[i].events_per_step = tuned.events_per_step;
+                cf[i].block_size = tuned.block_size;
+                rep[i] = tr;
+            }
+        }
+        if (rc) { trim_all(); return rc; }
+    }
+    std::vector<int> rcs(units.size(), TREKIS_OK);
+    std::vector<std::string> errs(units.size());
+    std::atomic<size_t> next{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto worker = [&]() {
+        cudaSetDevice(dev);
+        while (true) {
+            const size_t k = next.fetch_add(1);
+            if (k >= units.size()) break;
+            const std::vector<int>& u = units[k];
+            std::vector<trekis_tables*> tb;
+            std::vector<const trekis_material*> ms;
+            std::vector<trekis_run_cfg> cs;
+            std::vector<trekis_tallies*> os;
+            std::vector<trekis_status*> ss;
+            for (int i : u) {
+                tb.push_back(tables[i]); ms.push_back(mats[i]); cs.push_back(cf[i]); os.push_back(&tallies[i]);
+                ss.push_back(status ? &status[i] : nullptr);
+            }
+            const auto t0 = std::chrono::steady_clock::now();
+            rcs[k] = mc_run_group(tb, ms, cs, os, ss);
+            const double ms_run = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (rcs[k]) errs[k] = trekis_last_error();
+            if (tune)
+                for (int i : u) {
+                    trekis_tune& tr = tune[i];
+                    std::memset(&tr, 0, sizeof tr);
+                    tr.events_per_step = cf[i].events_per_step > 0 ? cf[i].events_per_step : 64;
+                    tr.block_size = cf[i].block_size > 0 ? cf[i].block_size : 256;
+                    tr.queue_capacity = cf[i].queue_capacity;
+                    tr.needed_capacity = rep[i].needed_capacity;
+                    tr.probe_ms = rep[i].probe_ms;
+                    tr.run_ms = ms_run;
+                }
+        }
+    };
+    std::vector<std::thread> pool;
+    const int nw = std::min<int>(conc, (int)units.size());
+    for (int w = 0; w < nw; ++w) pool.emplace_back(worker);
+    for (std::thread& th : pool) th.join();
+    trim_all();
+    for (size_t k = 0; k < units.size(); ++k)
+        if (rcs[k]) {
+            set_error("instance " + std::to_string(units[k].front()) + ": " + errs[k]);
+            return rcs[k];
+        }
+    return TREKIS_OK;
+}
 
 extern "C" int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables, const trekis_material* const* mats,
                                        const trekis_ion* const* ions, const trekis_run_cfg* cfgs,
@@ -114,6 +240,40 @@ extern "C" int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables, 
         size_t fr = 0, tot = 0;
         if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { set_error("cudaMemGetInfo failed"); return TREKIS_ECUDA; }
         budget = (int64_t)(0.75 * (double)fr);
+    }
+    // instances of one material share a wavefront when every instance has its
+    // own table set (a shared set's workspace would serve two units) and the
+    // caller did not ask for separate runs
+    if (!(bcfg && bcfg->separate)) {
+        bool distinct = true;
+        for (int i = 0; i < n && distinct; ++i)
+            for (int j = 0; j < i; ++j) if (tables[i] == tables[j]) { distinct = false; break; }
+        if (distinct) {
+            std::vector<std::vector<int>> units;
+            std::vector<int> unit_of(n, -1);
+            for (int i = 0; i < n; ++i) {
+                if (unit_of[i] >= 0) continue;
+                unit_of[i] = (int)units.size();
+                units.push_back({i});
+                for (int j = i + 1; j < n; ++j)
+                    if (unit_of[j] < 0 && mergeable(mats[i], mats[j], cfgs[i], cfgs[j], tallies[i], tallies[j])) {
+                        unit_of[j] = unit_of[i];
+                        units.back().push_back(j);
+                    }
+            }
+            if (units.size() < (size_t)n) {
+                for (std::vector<int>& u : units)   // the largest instance first: it owns the workspace and probes
+                    std::stable_sort(u.begin(), u.end(), [&](int a, int b) { return cfgs[a].NMC > cfgs[b].NMC; });
+                std::stable_sort(units.begin(), units.end(), [&](const std::vector<int>& a, const std::vector<int>& b) {
+                    long long wa = 0, wb = 0;
+                    for (int i : a) wa += cfgs[i].NMC;
+                    for (int i : b) wb += cfgs[i].NMC;
+                    return wa > wb;
+                });
+                return run_batch_merged(n, tables, mats, ions, cfgs, tallies, status, conc, autotune, budget, tune,
+                                        units);
+            }
+        }
     }
     // instances that share a table handle share its workspace: one worker runs them in order
     std::vector<std::vector<int>> groups;
@@ -151,12 +311,6 @@ extern "C" int32_t trekis_mc_run_batch(int32_t n, trekis_tables* const* tables, 
     std::vector<int> K_of(n, 0), BS_of(n, 0);
     std::vector<trekis_tune> probe_rep(n);
     if (autotune) {
-        auto same_material = [](const trekis_material* a, const trekis_material* b) {
-            trekis_material x = *a, y = *b;
-            x.dos_E = x.dos_DOS = x.dos_int = x.dos_k = x.dos_Eff_m = nullptr;
-            y.dos_E = y.dos_DOS = y.dos_int = y.dos_k = y.dos_Eff_m = nullptr;
-            return std::memcmp(&x, &y, sizeof x) == 0;
-        };
         std::vector<int> rep_of(n, -1);
         for (int i = 0; i < n; ++i) {
             if (rep_of[i] >= 0 || cfgs[i].events_per_step > 0) continue;

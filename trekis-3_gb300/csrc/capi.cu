@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI (include/trekis_gb300.h): table handles and the
 // do_Monte_Carlo replacement (batched wavefront driver).
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -565,9 +566,23 @@ static void acc_from_words(const int64_t* w, size_t n, std::vector<unsigned long
     }
 }
 
+// Several instances of one material in one wavefront (trekis_mc_run_batch):
+// their iterations are concatenated into the batches, every particle finds
+// its instance through its iteration, and each instance keeps its own
+// tallies, exact sums and counters.  The tables of the first instance serve
+// all (the material's tables are equal); each instance's own tables give its
+// ion track (ion, SHI rows).  Shape, seed and precision are the first
+// instance's; NMC and iteration_offset are each instance's.
+struct Group {
+    std::vector<trekis_tables*> tabs;
+    std::vector<trekis_run_cfg> cfgs;
+    std::vector<std::vector<int64_t>> words;              // out: each instance's exact sums
+    std::vector<std::array<unsigned long long, 9>> ev;    // out: each instance's counters
+};
+
 template <class T>
 static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, DevOut out,
-                  trekis_status* st, cudaStream_t strm, const ExactIO* xio) {
+                  trekis_status* st, cudaStream_t strm, const ExactIO* xio, Group* grp = nullptr) {
     const trekis_material& m = t->mat;
     const DevTabs<T>& tb = tabs_of<T>(t);
     int rc = 0;
@@ -598,7 +613,41 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     Ctrs* dctr = ws->ctr;
     const double* dV = ws->V;
     CK(cudaMemsetAsync(ws->hstage, 0, 8 * ws->hstage_n, strm));
-    const Acc& acc = ws->acc;
+    Acc acc = ws->acc;
+    // several instances: their tallies, exact sums and counters side by side
+    const int n_inst = grp ? (int)grp->tabs.size() : 1;
+    Buffers gb;
+    uint16_t* d_inst = nullptr;
+    InstInfo* d_info = nullptr;
+    std::vector<McConst<T>> Ci;
+    std::vector<int64_t> nmc_of(1, cfg.NMC);
+    if (grp) {
+        if (out.spectra() || cfg.sampler != 0) { set_error("merged instances take neither spectra nor sampler 1"); return TREKIS_EINVAL; }
+        nmc_of.assign(n_inst, 0);
+        for (int i = 0; i < n_inst; ++i) nmc_of[i] = grp->cfgs[i].NMC;
+        unsigned long long* tall = (unsigned long long*)gb.alloc(8 * ws->n_all * n_inst);
+        acc.lo = (unsigned long long*)gb.alloc(8 * acc.n() * n_inst);
+        acc.hi = (unsigned long long*)gb.alloc(8 * acc.n() * n_inst);
+        d_inst = (uint16_t*)gb.alloc(2 * (size_t)(1 << 16));
+        d_info = (InstInfo*)gb.alloc(sizeof(InstInfo) * n_inst);
+        tal.ev_inst = (unsigned long long*)gb.alloc(8 * 9 * (size_t)n_inst);
+        if (!tall || !acc.lo || !acc.hi || !d_inst || !d_info || !tal.ev_inst) {
+            set_error("device allocation for merged instances failed");
+            return TREKIS_ENOMEM;
+        }
+        const ptrdiff_t shift = tall - ws->tall;   // the same layout, from another base
+        for (unsigned long long** f : {&tal.e_cnt, &tal.e_E, &tal.p_cnt, &tal.p_E, &tal.h_cnt, &tal.h_E, &tal.h_Ek, &tal.lat})
+            *f += shift;
+        tal.inst_of = d_inst;
+        tal.st_e = tal.st_h = tal.st_lat = ws->n_all;   // whole blocks per instance
+        Ci.resize(n_inst);
+        for (int i = 0; i < n_inst; ++i) {   // each instance's ion and iterations (its own table set)
+            fill_const<T>(grp->tabs[i], grp->cfgs[i], Nt, Ci[i]);
+            Ci[i].tg = C.tg; Ci[i].Rg = C.Rg;
+        }
+    }
+    int64_t NMC_all = 0;
+    for (int64_t x : nmc_of) NMC_all += x;
     if (xio && xio->load) {
         std::vector<unsigned long long> lo, hi;
         acc_from_words(xio->load, acc.n(), lo, hi);
@@ -606,8 +655,8 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         CK(cudaMemcpyAsync(acc.hi, hi.data(), 8 * acc.n(), cudaMemcpyHostToDevice, strm));
         CK(cudaStreamSynchronize(strm));   // the host vectors go out of scope
     } else {
-        CK(cudaMemsetAsync(acc.lo, 0, 8 * acc.n(), strm));
-        CK(cudaMemsetAsync(acc.hi, 0, 8 * acc.n(), strm));
+        CK(cudaMemsetAsync(acc.lo, 0, 8 * acc.n() * n_inst, strm));
+        CK(cudaMemsetAsync(acc.hi, 0, 8 * acc.n() * n_inst, strm));
     }
 
     // learned proposal of the energy-transfer draw (exact: it only steers the search)
@@ -629,7 +678,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     // queues, else 256 iterations; later batches follow the measured peak
     int B = !tune_batch ? cfg.iterations_per_batch
           : (ws->per_it_peak > 0.0 ? (int)std::min<double>(0.5 * (double)cap / ws->per_it_peak, 1 << 30) : 256);
-    B = std::max(1, std::min(std::min(B, B_max), cfg.NMC));
+    B = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(B, B_max), std::max<int64_t>(NMC_all, 1)));
     CK(cudaEventRecord(ws->e0, strm));
     uint64_t steps = 0, launches = 1, ev_tot[9] = {0}, peak_all = 0;   // the grid hints
     uint64_t h2d = sizeof(T) * (Nt + cfg.N_R) + 8 * cfg.N_R, d2h = 0;
@@ -637,23 +686,65 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     Ctrs hc;
     std::memset(&hc, 0, sizeof hc);
     unsigned err_bits = 0;
-    int done = (xio && xio->load) ? cfg.NMC : 0;
-    while (done < cfg.NMC) {
-        const int nb = std::min(B, cfg.NMC - done);
-        C.it0 = cfg.iteration_offset + done;
-        CK(cudaMemsetAsync(ws->tall, 0, 8 * ws->n_all, strm));
+    int64_t done = (xio && xio->load) ? NMC_all : 0;
+    // the instance slices of a batch: instance, first batch iteration, count
+    struct Slice { int inst, base, n; };
+    std::vector<Slice> slices;
+    std::vector<uint16_t> h_inst;
+    std::vector<InstInfo> h_info(n_inst);
+    std::vector<unsigned long long> ev_inst_tot(9 * (size_t)n_inst, 0);
+    while (done < NMC_all) {
+        const int nb = (int)std::min<int64_t>(B, NMC_all - done);
+        slices.clear();
+        {   // concatenated iterations done .. done+nb-1
+            int64_t first = 0;
+            for (int i = 0; i < n_inst; ++i) {
+                const int64_t a = std::max(done, first), b = std::min(done + nb, first + nmc_of[i]);
+                if (b > a) slices.push_back(Slice{i, (int)(a - done), (int)(b - a)});
+                first += nmc_of[i];
+            }
+        }
+        if (grp) {
+            h_inst.assign(nb, 0);
+            int64_t first = 0;
+            std::vector<int64_t> first_of(n_inst);
+            for (int i = 0; i < n_inst; ++i) { first_of[i] = first; first += nmc_of[i]; }
+            for (const Slice& sl : slices) {
+                for (int k = 0; k < sl.n; ++k) h_inst[sl.base + k] = (uint16_t)sl.inst;
+                // global iteration of batch iteration it: offset + (done + it - first) = it0 + it
+                Ci[sl.inst].it0 = grp->cfgs[sl.inst].iteration_offset + (done - first_of[sl.inst]);
+                h_info[sl.inst] = InstInfo{Ci[sl.inst].it0, Ci[sl.inst].MSHI};
+            }
+            CK(cudaMemcpyAsync(d_inst, h_inst.data(), 2 * (size_t)nb, cudaMemcpyHostToDevice, strm));
+            CK(cudaMemcpyAsync(d_info, h_info.data(), sizeof(InstInfo) * n_inst, cudaMemcpyHostToDevice, strm));
+            CK(cudaMemsetAsync(tal.e_cnt, 0, 8 * ws->n_all * n_inst, strm));
+            CK(cudaMemsetAsync(tal.ev_inst, 0, 8 * 9 * (size_t)n_inst, strm));   // this batch's counts
+            h2d += 2 * (size_t)nb + sizeof(InstInfo) * n_inst;
+        } else {
+            C.it0 = cfg.iteration_offset + done;
+            CK(cudaMemsetAsync(ws->tall, 0, 8 * ws->n_all, strm));
+        }
         if (tal.spec) CK(cudaMemsetAsync(tal.spec, 0, 4 * ws->spec_it * nb, strm));
         CK(cudaMemsetAsync(dctr, 0, sizeof(Ctrs), strm));
         QSet<T>* in = &ws->qa;
         QSet<T>* ot = &ws->qb;
-        launch_shi<T>(C, shi_of<T>(t), ws->evs, ws->cap_ev, dctr, nb, strm);
-        ++launches;
+        if (grp) {
+            for (const Slice& sl : slices) {
+                launch_shi<T>(Ci[sl.inst], shi_of<T>(grp->tabs[sl.inst]), ws->evs, ws->cap_ev, dctr, sl.n, strm, sl.base,
+                              tal.ev_inst + 9 * (size_t)sl.inst);
+                ++launches;
+            }
+        } else {
+            launch_shi<T>(C, shi_of<T>(t), ws->evs, ws->cap_ev, dctr, nb, strm);
+            ++launches;
+        }
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
         d2h += sizeof hc;
         CK(cudaStreamSynchronize(strm));
         if (!hc.overflow) {
-            launch_pairs<T>(C, tb, ws->evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)ws->cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], tal, dctr, strm);
+            launch_pairs<T>(C, tb, ws->evs, (int64_t)std::min<unsigned long long>(hc.shi_slots, (unsigned long long)ws->cap_ev), ot->q[Q_E], ot->q[Q_HVB], ot->q[Q_HDEEP], tal, dctr, strm,
+                            grp ? d_info : nullptr);
             ++launches;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(&hc, dctr, sizeof hc, cudaMemcpyDeviceToHost, strm));
@@ -692,13 +783,33 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             continue;
         }
         steps += bsteps; launches += blaunch; step_ms += bms;
+        if (grp) {   // the batch's counts of each instance
+            std::vector<unsigned long long> evb(9 * (size_t)n_inst);
+            CK(cudaMemcpyAsync(evb.data(), tal.ev_inst, 8 * evb.size(), cudaMemcpyDeviceToHost, strm));
+            CK(cudaStreamSynchronize(strm));
+            d2h += 8 * evb.size();
+            for (size_t x = 0; x < evb.size(); ++x) { ev_inst_tot[x] += evb[x]; hc.ev[x % 9] += evb[x]; }
+        }
         for (int q = 0; q < 9; ++q) ev_tot[q] += hc.ev[q];
         ev_tot[7] += 2 * hc.ev[0];   // the pair of every SHI collision
         err_bits |= hc.err_bits;
         peak_all = std::max<uint64_t>(peak_all, (uint64_t)peak);
-        // add the batch into the call's exact sums
-        acc_batch(tal, Nt, NR, nsh, acc, strm);
-        launches += 4;
+        // add the batch into the call's exact sums (each instance's into its own)
+        if (grp) {
+            for (const Slice& sl : slices) {
+                Tal ti = tal;
+                const size_t o = (size_t)sl.inst * ws->n_all;
+                for (unsigned long long** f : {&ti.e_cnt, &ti.e_E, &ti.p_cnt, &ti.p_E, &ti.h_cnt, &ti.h_E, &ti.h_Ek, &ti.lat})
+                    *f += o;
+                Acc ai = acc;
+                ai.lo += (size_t)sl.inst * acc.n(); ai.hi += (size_t)sl.inst * acc.n();
+                acc_batch(ti, Nt, NR, nsh, ai, strm);
+                launches += 4;
+            }
+        } else {
+            acc_batch(tal, Nt, NR, nsh, acc, strm);
+            launches += 4;
+        }
         if (tal.spec) {
             fin_spectra(tal, nb, Nt, ws->wE, ws->wD, out.sEe, out.sEh, out.sth, out.sthh, strm);
             launches += 2;
@@ -711,7 +822,20 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             B = std::max(1, std::min<int>((int)(0.5 * cap / per_it), B_max));
         }
     }
-    if (xio && xio->add_to) {   // export the exact sums; the FP64 tallies are made where they are summed
+    if (grp) {   // each instance's exact sums and counters; its FP64 tallies are made by the caller
+        grp->words.assign(n_inst, std::vector<int64_t>(4 * acc.n(), 0));
+        grp->ev.assign(n_inst, std::array<unsigned long long, 9>{});
+        std::vector<unsigned long long> lo(acc.n()), hi(acc.n());
+        for (int i = 0; i < n_inst; ++i) {
+            CK(cudaMemcpyAsync(lo.data(), acc.lo + (size_t)i * acc.n(), 8 * acc.n(), cudaMemcpyDeviceToHost, strm));
+            CK(cudaMemcpyAsync(hi.data(), acc.hi + (size_t)i * acc.n(), 8 * acc.n(), cudaMemcpyDeviceToHost, strm));
+            CK(cudaStreamSynchronize(strm));
+            words_from_acc(lo, hi, grp->words[i].data());
+            for (int q = 0; q < 9; ++q) grp->ev[i][q] = ev_inst_tot[9 * (size_t)i + q];
+            grp->ev[i][7] += 2 * grp->ev[i][0];   // the pair of every SHI collision
+        }
+        d2h += 16 * acc.n() * n_inst;
+    } else if (xio && xio->add_to) {   // export the exact sums; the FP64 tallies are made where they are summed
         std::vector<unsigned long long> lo(acc.n()), hi(acc.n());
         CK(cudaMemcpyAsync(lo.data(), acc.lo, 8 * acc.n(), cudaMemcpyDeviceToHost, strm));
         CK(cudaMemcpyAsync(hi.data(), acc.hi, 8 * acc.n(), cudaMemcpyDeviceToHost, strm));
@@ -1075,6 +1199,73 @@ int32_t trekis_mc_run(const trekis_tables* tc, const trekis_material* mat, const
     (void)ion;
     return mc_run_host(tc, mat, cfg, o, st, nullptr);
 }
+
+}  // extern "C"
+
+namespace tk {
+// Several instances of one material in one wavefront, each instance's
+// tallies added into its host arrays as its own trekis_mc_run would add them
+// (bit for bit: the exact sums are finished by the same code).  The caller
+// has checked that the instances may share a wavefront (equal material,
+// tally shape, precision, seed and scheduling knobs; no spectra; sampler 0).
+int mc_run_group(const std::vector<trekis_tables*>& tabs, const std::vector<const trekis_material*>& mats,
+                 std::vector<trekis_run_cfg> cfgs, const std::vector<trekis_tallies*>& outs,
+                 const std::vector<trekis_status*>& sts) {
+    const size_t n = tabs.size();
+    if (n == 0 || mats.size() != n || cfgs.size() != n || outs.size() != n || sts.size() != n) return TREKIS_EINVAL;
+    int Nt = 0;
+    for (size_t i = 0; i < n; ++i) {
+        int nt = 0;
+        const int rc = check_run(tabs[i], mats[i], &cfgs[i], outs[i], &nt);
+        if (rc) return rc;
+        if (i && nt != Nt) { set_error("merged instances need one time grid"); return TREKIS_EINVAL; }
+        Nt = nt;
+        cfgs[i].queue_capacity = cfgs[0].queue_capacity;   // one workspace: the first table set's
+    }
+    if (!device_ok()) return TREKIS_ENODEVICE;
+    Group grp;
+    grp.tabs = tabs;
+    grp.cfgs = cfgs;
+    trekis_status gst;
+    std::memset(&gst, 0, sizeof gst);
+    gst.first_offender = -1;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return TREKIS_ECUDA;
+    DevOut none{};
+    int rc = (cfgs[0].precision == 1)
+        ? run_mc<double>(tabs[0], cfgs[0], Nt, outs[0]->Nat, outs[0]->Nshl, none, &gst, s, nullptr, &grp)
+        : run_mc<float>(tabs[0], cfgs[0], Nt, outs[0]->Nat, outs[0]->Nshl, none, &gst, s, nullptr, &grp);
+    if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = TREKIS_ECUDA;
+    cudaStreamDestroy(s);
+    if (rc) return rc;
+    for (size_t i = 0; i < n; ++i) {
+        ExactIO x;
+        x.load = grp.words[i].data();
+        rc = mc_run_host(tabs[0], mats[i], &cfgs[i], outs[i], nullptr, &x);
+        if (rc) return rc;
+        trekis_status* st = sts[i];
+        if (!st) continue;
+        const std::array<unsigned long long, 9>& e = grp.ev[i];
+        st->n_shi += e[0]; st->n_el_inelastic += e[1]; st->n_el_elastic += e[2]; st->n_hole_events += e[3];
+        st->n_auger += e[4]; st->n_radiative += e[5]; st->n_photon_abs += e[6]; st->n_particles += e[7];
+        const uint64_t step_ev = e[1] + e[2] + e[3] + e[4] + e[5] + e[6];
+        st->n_events += e[0] + step_ev;
+        st->step_events += step_ev;
+        st->n_fp64_redraws += e[8];
+        st->error_bits |= gst.error_bits;
+        // the wavefront's figures are the group's
+        st->n_steps += gst.n_steps; st->device_ms += gst.device_ms; st->step_ms += gst.step_ms;
+        st->n_kernel_launches += gst.n_kernel_launches; st->step_launches += gst.step_launches;
+        st->peak_queue = std::max<uint64_t>(st->peak_queue, gst.peak_queue);
+        st->batch_iterations = gst.batch_iterations;
+        st->h2d_bytes += gst.h2d_bytes; st->d2h_bytes += gst.d2h_bytes;
+        st->code = TREKIS_OK;
+    }
+    return TREKIS_OK;
+}
+}  // namespace tk
+
+extern "C" {
 
 int64_t trekis_exact_words(const trekis_tables* t, const trekis_run_cfg* cfg) {
     if (!t || !cfg || cfg->N_R < 1) return -1;

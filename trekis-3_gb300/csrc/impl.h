@@ -238,6 +238,10 @@ void set_error(const std::string& s);
 // R_(j-1)^2)), R_(-1) = 0.  One out-of-line definition, so that every entry
 // point weights its tallies with the same bits.
 double radial_volume(const double* R, int j, double Layer);
+// several instances of one material in one wavefront (capi.cu; used by trekis_mc_run_batch)
+int mc_run_group(const std::vector<trekis_tables*>& tabs, const std::vector<const trekis_material*>& mats,
+                 std::vector<trekis_run_cfg> cfgs, const std::vector<trekis_tallies*>& outs,
+                 const std::vector<trekis_status*>& sts);
 int build_tables_device(trekis_tables* T, const trekis_table_cfg& cfg, trekis_status* st);
 std::vector<double> grid_4CS(const trekis_material& m, double Emin, double Emax);
 double zeff_of(const trekis_ion& ion, const trekis_material& m, double E);   // Equilibrium_charge_SHI

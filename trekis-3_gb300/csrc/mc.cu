@@ -142,16 +142,17 @@ __device__ __forceinline__ int tbin(const McConst<T>& C, T t) {
 }
 
 // one run of equal radial bin over rows [r0, r1] (1-based)
-template <class T>
-__device__ void flush_run(const McConst<T>& C, const Tal& tal, int kind, int sh, int j, int r0, int r1,
-                          long long qE, long long qK) {
+template <class T, class TL>
+__device__ void flush_run(const McConst<T>& C, const TL& tal, int kind, int sh, int j, int r0, int r1,
+                          long long qE, long long qK, int it) {
     const int NR = C.NR;
+    const size_t io = inst_index(tal, it);
     // A run of a single grid time goes to the single-row block that follows
     // each difference block (one entry instead of a start and an end entry);
     // the finalize adds it after the prefix sum.
     if (kind == 0 || kind == 2) {
-        unsigned long long* cnt = kind == 0 ? tal.e_cnt : tal.p_cnt;
-        unsigned long long* en = kind == 0 ? tal.e_E : tal.p_E;
+        unsigned long long* cnt = (kind == 0 ? tal.e_cnt : tal.p_cnt) + io * tal.st_e;
+        unsigned long long* en = (kind == 0 ? tal.e_E : tal.p_E) + io * tal.st_e;
         if (r0 == r1) {
             const size_t a = (size_t)(C.Nt + 2 + r0) * NR + (j - 1);
             add64(cnt + a, 1);
@@ -165,15 +166,16 @@ __device__ void flush_run(const McConst<T>& C, const Tal& tal, int kind, int sh,
             add64(en + (size_t)(r1 + 1) * NR + (j - 1), -qE);
         }
     } else {
+        const size_t oh = io * tal.st_h;   // the instance's hole arrays
         if (r0 == r1) {
-            const size_t a = ((size_t)(C.Nt + 2 + r0) * C.nsh + sh) * NR + (j - 1);
+            const size_t a = ((size_t)(C.Nt + 2 + r0) * C.nsh + sh) * NR + (j - 1) + oh;
             add64(tal.h_cnt + a, 1); add64(tal.h_E + a, qE); add64(tal.h_Ek + a, qK);
             return;
         }
-        const size_t a = ((size_t)r0 * C.nsh + sh) * NR + (j - 1);
+        const size_t a = ((size_t)r0 * C.nsh + sh) * NR + (j - 1) + oh;
         add64(tal.h_cnt + a, 1); add64(tal.h_E + a, qE); add64(tal.h_Ek + a, qK);
         if (r1 < C.Nt) {
-            const size_t b = ((size_t)(r1 + 1) * C.nsh + sh) * NR + (j - 1);
+            const size_t b = ((size_t)(r1 + 1) * C.nsh + sh) * NR + (j - 1) + oh;
             add64(tal.h_cnt + b, -1); add64(tal.h_E + b, -qE); add64(tal.h_Ek + b, -qK);
         }
     }
@@ -207,8 +209,8 @@ __device__ __forceinline__ int theta_bin(T th) {
 // Spectra of one segment over rows [ia, ib] of its iteration
 // (Calculated_statistics, Monte_Carlo.f90:1019-1081): the particle count,
 // its energy bin and, when the angle counts, its angle bin.
-template <class T>
-__device__ void emit_spec(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T th, bool ang, int it,
+template <class T, class TL>
+__device__ void emit_spec(const McConst<T>& C, const TL& tal, int kind, int sh, T E, T Ek, T th, bool ang, int it,
                           int ia, int ib) {
     int* base = tal.spec + (size_t)it * tal.sp_it;
     const size_t r0 = (size_t)ia * tal.sp_row, r1 = (size_t)(ib + 1) * tal.sp_row;
@@ -241,13 +243,13 @@ __device__ __forceinline__ int seg_span(const McConst<T>& C, T t0, T tn, int& ib
 }
 
 // Tally rows ia..ib (ia <= ib) of one segment.
-template <class T>
-__device__ void seg_body(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T X, T Y,
+template <class T, class TL>
+__device__ void seg_body(const McConst<T>& C, const TL& tal, int kind, int sh, T E, T Ek, T t0, T X, T Y,
                          T th, T ph, T V, int it, bool ang, int ia, int ib) {
     if (tal.spec && kind != 2) emit_spec(C, tal, kind, sh, E, Ek, th, ang, it, ia, ib);
     const long long qE = fixE(E), qK = fixE(Ek);
     if (V == T(0)) {
-        flush_run(C, tal, kind, sh, rbin(C, m_sqrt(X * X + Y * Y)), ia, ib, qE, qK);
+        flush_run(C, tal, kind, sh, rbin(C, m_sqrt(X * X + Y * Y)), ia, ib, qE, qK, it);
         return;
     }
     const T s_t = f_sin(th), s_p = f_sin(ph), c_p = f_cos(ph);
@@ -259,11 +261,11 @@ __device__ void seg_body(const McConst<T>& C, const Tal& tal, int kind, int sh, 
         T y = Y + L0 * s_t * c_p;
         int j = rbin(C, m_sqrt(x * x + y * y));
         if (j != cur) {
-            if (cur > 0) flush_run(C, tal, kind, sh, cur, start, i - 1, qE, qK);
+            if (cur > 0) flush_run(C, tal, kind, sh, cur, start, i - 1, qE, qK, it);
             cur = j; start = i;
         }
     }
-    flush_run(C, tal, kind, sh, cur, start, ib, qE, qK);
+    flush_run(C, tal, kind, sh, cur, start, ib, qE, qK, it);
 }
 
 // Tally the free-flight segment [t0, tn) at every grid time t_i with
@@ -273,8 +275,8 @@ __device__ void seg_body(const McConst<T>& C, const Tal& tal, int kind, int sh, 
 // event that started the segment); returns the index of min(tn, Tim), which is
 // the next segment's ia.  Consecutive segments of a particle tile the time
 // axis, so one search per segment suffices.
-template <class T>
-__device__ __forceinline__ int emit_seg(const McConst<T>& C, const Tal& tal, int kind, int sh, T E, T Ek, T t0, T tn,
+template <class T, class TL>
+__device__ __forceinline__ int emit_seg(const McConst<T>& C, const TL& tal, int kind, int sh, T E, T Ek, T t0, T tn,
                                         T X, T Y, T th, T ph, T V /* m/s, 0: static */, int it, bool ang, int ia) {
     int ib;
     const int tnext = seg_span(C, t0, tn, ib);
@@ -296,22 +298,22 @@ template <class T> __device__ __forceinline__ T tn_of(T t0, T L, T V) {
     return (V > T(1.0e-10)) ? t0 + L / V * T(1e5) : T(1.0e25);
 }
 
-template <class T>
-__device__ __forceinline__ int emit_electron(const McConst<T>& C, const Tal& tal, const P<T>& p, int ia) {
+template <class T, class TL>
+__device__ __forceinline__ int emit_electron(const McConst<T>& C, const TL& tal, const P<T>& p, int ia) {
     const T co = C.cut_off > T(0) ? C.cut_off : T(0);
     const bool mv = p.E > co;
     return emit_seg(C, tal, 0, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0),
                     mv ? v_el(p.E) : T(0), p.it, true, ia);
 }
-template <class T>
-__device__ __forceinline__ int emit_hole(const McConst<T>& C, const Tal& tal, const P<T>& p, int ia) {
+template <class T, class TL>
+__device__ __forceinline__ int emit_hole(const McConst<T>& C, const TL& tal, const P<T>& p, int ia) {
     const T co = C.cut_off > T(0) ? C.cut_off : T(0);
     const bool mv = (p.M < T(1.0e3)) && (p.Ek > co);
     return emit_seg(C, tal, 1, p.sh, p.E, p.Ek, p.t0, p.tn, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0), p.it,
                     mv, ia);
 }
-template <class T>
-__device__ __forceinline__ void emit_photon(const McConst<T>& C, const Tal& tal, const P<T>& p, int ia) {
+template <class T, class TL>
+__device__ __forceinline__ void emit_photon(const McConst<T>& C, const TL& tal, const P<T>& p, int ia) {
     if (p.E > T(0)) emit_seg(C, tal, 2, 0, p.E, T(0), p.t0, p.tn, p.X, p.Y, p.th, p.ph, T(kC), p.it, false, ia);
 }
 
@@ -341,8 +343,8 @@ __device__ __forceinline__ void park_seg(SegRing<T>& R, int w, int slot, T E, T 
 }
 
 // lanes 0..cnt-1 of the warp tally the segments at ring slots head..head+cnt-1
-template <class T>
-__device__ __forceinline__ void drain_segs(const McConst<T>& C, const Tal& tal, const SegRing<T>& R, int kind, int w,
+template <class T, class TL>
+__device__ __forceinline__ void drain_segs(const McConst<T>& C, const TL& tal, const SegRing<T>& R, int kind, int w,
                                            int lane, int head, int cnt) {
     if (lane < cnt) {
         const int q = (head + lane) & (kSegQ - 1);
@@ -356,16 +358,18 @@ __device__ __forceinline__ void drain_segs(const McConst<T>& C, const Tal& tal, 
 // per-thread accumulator of the lattice energy (one atomic per change of
 // cell); each deposit is rounded to fixed point on its own, so the sum does
 // not depend on how events are grouped into threads and launches
+// (cells of the particle's instance: `it` is its batch iteration)
 struct LatAcc {
     int cell = -1;
     long long sum = 0;
-    template <class T>
-    __device__ __forceinline__ void add(const Tal& tal, int c, T v) {
-        if (c != cell) { flush(tal); cell = c; }
+    template <class T, class TL>
+    __device__ __forceinline__ void add(const TL& tal, int c, T v, int it) {
+        if (c != cell) { flush(tal, it); cell = c; }
         sum += fixLat(v);
     }
-    __device__ __forceinline__ void flush(const Tal& tal) {
-        if (cell >= 0 && sum != 0) add64(tal.lat + cell, sum);
+    template <class TL>
+    __device__ __forceinline__ void flush(const TL& tal, int it) {
+        if (cell >= 0 && sum != 0) add64(tal.lat + inst_index(tal, it) * tal.st_lat + cell, sum);
         sum = 0;
     }
 };
@@ -931,8 +935,8 @@ __device__ __forceinline__ void append(const PQ<T>& q, int* n, int* overflow, co
 }
 
 // kind 0 electron, 1 hole, 2 photon; holes go to the mobile-valence or the deep queue
-template <class T>
-__device__ __forceinline__ void push(const McConst<T>& C, const Tal& tal, const Out<T>& o, int kind, const P<T>& p) {
+template <class T, class TL>
+__device__ __forceinline__ void push(const McConst<T>& C, const TL& tal, const Out<T>& o, int kind, const P<T>& p) {
     if (!(p.tn < C.Tim)) return;           // no event left inside the run
     const int qi = kind == 0 ? Q_E : kind == 2 ? Q_P : (p.sh == C.vb ? Q_HVB : Q_HDEEP);
     append(o.q[qi], &o.ctr->n_out[qi], &o.ctr->overflow, p);
@@ -1058,9 +1062,11 @@ constexpr int kSlotChunk = 32;
 
 template <class T>
 __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McConst<T> C, const __grid_constant__ DevShi<T> sh,
-                                                  ShiEv* __restrict__ evs, int64_t cap_ev, Ctrs* ctr, int nit) {
-    const int it = blockIdx.x * blockDim.x + threadIdx.x;
-    if (it >= nit) return;
+                                                  ShiEv* __restrict__ evs, int64_t cap_ev, Ctrs* ctr, int nit,
+                                                  int it_base, unsigned long long* ev_inst) {
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local >= nit) return;
+    const int it = it_base + local;   // the iteration's index in the batch
     unsigned err = 0;
     unsigned long long nev = 0;
     const uint64_t pid = shi_pid(C.it0 + it);
@@ -1160,26 +1166,28 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
     }
     for (; slot < slot_end; ++slot)   // mark the rest of the last chunk unused
         if (slot < cap_ev) evs[slot].it = -1;
-    if (nev) atomicAdd(&ctr->ev[0], nev);
+    if (nev) atomicAdd(ev_inst ? ev_inst : &ctr->ev[0], nev);
     if (err) atomicOr(&ctr->err_bits, err);
 }
 
 // The electron-hole pair of each SHI collision, one thread each (MC:2198-2247);
 // draws continue in the collision's stream after the ion's three.
-template <class T>
+template <class T, class TL>
 __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ McConst<T> C, const __grid_constant__ DevTabs<T> tb,
                                                const ShiEv* __restrict__ evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
-                                               PQ<T> qhdeep, const __grid_constant__ Tal tal, Ctrs* ctr) {
+                                               PQ<T> qhdeep, const __grid_constant__ TL tal, Ctrs* ctr,
+                                               const InstInfo* __restrict__ inst) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_ev) return;
     const ShiEv ev = evs[i];
     if (ev.it < 0) return;   // an unused slot of a reserved chunk
-    const uint64_t pid = shi_pid(C.it0 + ev.it);
+    const InstInfo ii = inst ? inst[inst_index(tal, ev.it)] : InstInfo{C.it0, C.MSHI};
+    const uint64_t pid = shi_pid(ii.it0 + ev.it);
     EvStream<T> s(C.rk, pid, ev.ord);
     s.word(); s.word(); s.word();
     unsigned err = 0;
     const int k = ev.k;
-    const double E = ev.E, dE = ev.dE, MSHI = C.MSHI;
+    const double E = ev.E, dE = ev.dE, MSHI = ii.MSHI;
     Out<T> o{{qe, qhvb, qhdeep, qe}, ctr};
     P<T> el;
     el.pid = child_pid(pid, ev.ord, 0); el.ord = 0; el.sh = 0; el.Ek = T(0); el.M = T(0); el.it = ev.it;
@@ -1215,8 +1223,8 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ McConst<T
 // EL selects the elastic model at compile time (0: the run's, C.elast_model;
 // 1: Mott only; 2: phonon CDF only; 3: DSF only), so a hot kernel carries one
 // model's code.
-template <class T, bool FULL, bool DEFER = false, int EL = 0>
-__device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o,
+template <class T, bool FULL, bool DEFER = false, int EL = 0, class TL>
+__device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const TL& tal, const Out<T>& o,
                                P<T>& p, unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc,
                                float fg = -1.f) {
     const uint32_t ord = p.ord;
@@ -1276,7 +1284,7 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
         angles_lat(C, Eel, dE, T(1), s, theta, phi, elastic_uniform(x, T(1) / I, Em));
         const int i = ti0;  // the interval t_{i-1} <= t < t_i
         const int j = rbin(C, m_sqrt(X * X + Y * Y));
-        lat.add(tal, (i - 1) * C.NR + (j - 1), dE);
+        lat.add(tal, (i - 1) * C.NR + (j - 1), dE, p.it);
         nev[2]++;
     }
     p.E = Eel - dE;
@@ -1316,8 +1324,8 @@ __device__ T check_hole(const DevTabs<T>& tb, T Eel, T& dE, P<T>* el) {
 
 // One hole event; FULL=false compiles only valence-hole elastic scattering;
 // DEFER and EL as for electron_event.
-template <class T, bool FULL, bool DEFER = false, int EL = 0>
-__device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& h,
+template <class T, bool FULL, bool DEFER = false, int EL = 0, class TL>
+__device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const TL& tal, const Out<T>& o, P<T>& h,
                            unsigned& err, LatAcc& lat, unsigned long long* nev, MfpCache<T>& mc, float fg = -1.f) {
     const uint32_t ord = h.ord;
     EvStream<T> s(C.rk, h.pid, ord);
@@ -1392,7 +1400,7 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
             Eh = check_hole(tb, Eel, dE, (P<T>*)nullptr);
             const int i = ti0;
             const int j = rbin(C, m_sqrt(X * X + Y * Y));
-            lat.add(tal, (i - 1) * C.NR + (j - 1), dE);
+            lat.add(tal, (i - 1) * C.NR + (j - 1), dE, h.it);
             nev[3]++;
         }
         T hp2, ht2;
@@ -1506,8 +1514,8 @@ __device__ bool hole_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal&
     return true;
 }
 
-template <class T>
-__device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Tal& tal, const Out<T>& o, P<T>& p,
+template <class T, class TL>
+__device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const TL& tal, const Out<T>& o, P<T>& p,
                              unsigned& err, unsigned long long* nev) {
     const uint32_t ord = p.ord++;
     EvStream<T> s(C.rk, p.pid, ord);
@@ -1546,11 +1554,11 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const Ta
 // iterate together (a lane whose particle is done idles) so that segments
 // reaching a grid time can be parked in the warp's ring and tallied 32 at a
 // time; the tallies are integer sums, so the order does not matter.
-template <class T, bool IS_E, int ELM>
+template <class T, bool IS_E, int ELM, class TL>
 __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<T> C,
                                              const __grid_constant__ DevTabs<T> tb, const __grid_constant__ PQ<T> in,
                                              int n, const __grid_constant__ Out<T> o, const __grid_constant__ PQ<T> side,
-                                             const __grid_constant__ Tal tal, int K) {
+                                             const __grid_constant__ TL tal, int K) {
     __shared__ SegRing<T> ring;
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1612,23 +1620,27 @@ __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<
     __syncwarp();
     drain_segs(C, tal, ring, IS_E ? 0 : 1, w, lane, head, cnt);
     if (!valid) return;
-    lat.flush(tal);
+    lat.flush(tal, p.it);
     if (diverted) append(side, &o.ctr->n_out[IS_E ? Q_EINEL : Q_HINEL], &o.ctr->overflow, p);
     else push(C, tal, o, IS_E ? 0 : 1, p);
     const unsigned long long ne = IS_E ? nev[2] : nev[3];
-    if (ne) atomicAdd(&o.ctr->ev[IS_E ? 2 : 3], ne);
+    if constexpr (std::is_same<TL, TalMulti>::value) {
+        if (ne) atomicAdd(tal.ev_inst + 9 * inst_index(tal, p.it) + (IS_E ? 2 : 3), ne);
+    } else {
+        if (ne) atomicAdd(&o.ctr->ev[IS_E ? 2 : 3], ne);
+    }
     if (err) atomicOr(&o.ctr->err_bits, err);
 }
 
 // Rare kernel of a wavefront step (grid-stride; counts read on the device):
 // one full event for each particle of the ionisation side queues, each deep
 // hole (Auger or radiative decay) and each photon (absorption).
-template <class T>
+template <class T, class TL>
 __global__ void __launch_bounds__(128) k_rare(const __grid_constant__ McConst<T> C,
                                               const __grid_constant__ DevTabs<T> tb, const __grid_constant__ PQ<T> e_inel,
                                               const __grid_constant__ PQ<T> h_inel, const __grid_constant__ PQ<T> hdeep,
                                               int n_deep, const __grid_constant__ PQ<T> ph, int n_ph,
-                                              const __grid_constant__ Out<T> o, const __grid_constant__ Tal tal,
+                                              const __grid_constant__ Out<T> o, const __grid_constant__ TL tal,
                                               const float* __restrict__ guess) {
     const int n_e = o.ctr->n_out[Q_EINEL], n_h = o.ctr->n_out[Q_HINEL];
     const int total = n_e + n_h + n_deep + n_ph;
@@ -1650,7 +1662,12 @@ __global__ void __launch_bounds__(128) k_rare(const __grid_constant__ McConst<T>
         }
         else if (g < n_e + n_h + n_deep) { load(hdeep, g - n_e - n_h, p); p.ti = tbin(C, p.tn); hole_event<T, true>(C, tb, tal, o, p, err, lat, nev, mc); kind = 1; }
         else { load(ph, g - n_e - n_h - n_deep, p); p.ti = tbin(C, p.tn); photon_event(C, tb, tal, o, p, err, nev); kind = 2; }
-        lat.flush(tal);
+        lat.flush(tal, p.it);
+        if constexpr (std::is_same<TL, TalMulti>::value) {   // this particle's counts go to its instance
+            unsigned long long* c = tal.ev_inst + 9 * inst_index(tal, p.it);
+            for (int q = 1; q < 9; ++q)
+                if (nev[q]) { atomicAdd(c + q, nev[q]); nev[q] = 0; }
+        }
         push(C, tal, o, kind, p);
     }
     for (int q = 1; q < 9; ++q)
@@ -1773,21 +1790,25 @@ template void launch_propose<double>(const Proposer&, const McConst<double>&, co
 
 template <class T>
 void launch_shi(const McConst<T>& C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
-                cudaStream_t s) {
-    k_shi_track<T><<<(nit + 63) / 64, 64, 0, s>>>(C, sh, (ShiEv*)evs, cap_ev, ctr, nit);
+                cudaStream_t s, int it_base, unsigned long long* ev_inst) {
+    if (nit <= 0) return;
+    k_shi_track<T><<<(nit + 63) / 64, 64, 0, s>>>(C, sh, (ShiEv*)evs, cap_ev, ctr, nit, it_base, ev_inst);
 }
 template <class T>
 void launch_pairs(const McConst<T>& C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
-                  PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s) {
+                  PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s, const InstInfo* inst) {
     if (n_ev <= 0) return;
-    k_pairs<T><<<(unsigned)((n_ev + 127) / 128), 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qhvb, qhdeep, tal, ctr);
+    const unsigned g = (unsigned)((n_ev + 127) / 128);
+    if (tal.inst_of)
+        k_pairs<T, TalMulti><<<g, 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qhvb, qhdeep, as_multi(tal), ctr, inst);
+    else k_pairs<T, Tal><<<g, 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qhvb, qhdeep, tal, ctr, inst);
 }
 size_t shi_event_bytes() { return sizeof(ShiEv); }
 
-template <class T>
-void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
-                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
-                 const float* guess, const Proposer* prop, const Fork* fk) {
+template <class T, class TL>
+static void launch_step_tl(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in,
+                           const QSet<T>& out, PQ<T> e_inel, PQ<T> h_inel, const TL& tal, Ctrs* ctr, int K, int bs,
+                           int rare_blocks, cudaStream_t s, const float* guess, const Proposer* prop, const Fork* fk) {
     Out<T> o{{out.q[0], out.q[1], out.q[2], out.q[3]}, ctr};
     // the two hot kernels touch disjoint queues; counters and tallies are atomics
     const bool two = fk && fk->s2 && fk->fork && fk->join && n_in[Q_E] > 0 && n_in[Q_HVB] > 0;
@@ -1798,34 +1819,45 @@ void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, c
     // one hot kernel per particle kind and elastic model
     if (n_in[Q_E] > 0) {
         const unsigned g = (n_in[Q_E] + bs - 1) / bs;
-        if (C.elast_model == 1) k_hot<T, true, 1><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
-        else if (C.elast_model == 2) k_hot<T, true, 2><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
-        else k_hot<T, true, 0><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+        if (C.elast_model == 1) k_hot<T, true, 1, TL><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+        else if (C.elast_model == 2) k_hot<T, true, 2, TL><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
+        else k_hot<T, true, 0, TL><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
     }
     if (n_in[Q_HVB] > 0) {
         const unsigned g = (n_in[Q_HVB] + bs - 1) / bs;
         cudaStream_t sh = two ? fk->s2 : s;
         if (C.elast_model == 1)
-            k_hot<T, false, 1><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+            k_hot<T, false, 1, TL><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
         else if (C.elast_model == 2)
-            k_hot<T, false, 2><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
-        else k_hot<T, false, 0><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+            k_hot<T, false, 2, TL><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+        else k_hot<T, false, 0, TL><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
     }
     if (two) {
         cudaEventRecord(fk->join, fk->s2);
         cudaStreamWaitEvent(s, fk->join, 0);
     }
     if (prop) launch_propose<T>(*prop, C, tb, e_inel, h_inel, ctr, s);
-    k_rare<T><<<rare_blocks, 128, 0, s>>>(C, tb, e_inel, h_inel, in.q[Q_HDEEP], n_in[Q_HDEEP], in.q[Q_P],
-                                          n_in[Q_P], o, tal, prop ? guess : nullptr);
+    k_rare<T, TL><<<rare_blocks, 128, 0, s>>>(C, tb, e_inel, h_inel, in.q[Q_HDEEP], n_in[Q_HDEEP], in.q[Q_P],
+                                              n_in[Q_P], o, tal, prop ? guess : nullptr);
+}
+template <class T>
+void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
+                 PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
+                 const float* guess, const Proposer* prop, const Fork* fk) {
+    if (tal.inst_of)
+        launch_step_tl<T, TalMulti>(C, tb, in, n_in, out, e_inel, h_inel, as_multi(tal), ctr, K, bs, rare_blocks, s,
+                                    guess, prop, fk);
+    else launch_step_tl<T, Tal>(C, tb, in, n_in, out, e_inel, h_inel, tal, ctr, K, bs, rare_blocks, s, guess, prop, fk);
 }
 
-template void launch_shi<float>(const McConst<float>&, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t);
-template void launch_shi<double>(const McConst<double>&, const DevShi<double>&, void*, int64_t, Ctrs*, int, cudaStream_t);
+template void launch_shi<float>(const McConst<float>&, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t,
+                                int, unsigned long long*);
+template void launch_shi<double>(const McConst<double>&, const DevShi<double>&, void*, int64_t, Ctrs*, int, cudaStream_t,
+                                 int, unsigned long long*);
 template void launch_pairs<float>(const McConst<float>&, const DevTabs<float>&, const void*, int64_t, PQ<float>,
-                                  PQ<float>, PQ<float>, Tal, Ctrs*, cudaStream_t);
+                                  PQ<float>, PQ<float>, Tal, Ctrs*, cudaStream_t, const InstInfo*);
 template void launch_pairs<double>(const McConst<double>&, const DevTabs<double>&, const void*, int64_t, PQ<double>,
-                                   PQ<double>, PQ<double>, Tal, Ctrs*, cudaStream_t);
+                                   PQ<double>, PQ<double>, Tal, Ctrs*, cudaStream_t, const InstInfo*);
 template void launch_step<float>(const McConst<float>&, const DevTabs<float>&, const QSet<float>&, const int*,
                                  const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t,
                                  const float*, const Proposer*, const Fork*);

@@ -2,6 +2,7 @@
 #pragma once
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include "common.cuh"
 #include "impl.h"
 
@@ -95,6 +96,31 @@ struct Tal {
     int sp_nE, sp_nD;   // energy bins of electrons (N_R) and of valence holes (N_dos)
     size_t sp_row;      // ints per row: 1 + nE + 180 + 1 + nD + 180
     size_t sp_it;       // ints per iteration: (Nt + 2) * sp_row
+    // Several instances in one wavefront (trekis_mc_run_batch): the instance
+    // of each iteration of the batch, the words between two instances' arrays
+    // (electrons and photons, holes, lattice) and per-instance event counters
+    // [instance][9].  inst_of = null: one instance, offsets 0.
+    const uint16_t* inst_of = nullptr;
+    size_t st_e = 0, st_h = 0, st_lat = 0;
+    unsigned long long* ev_inst = nullptr;
+};
+// The same tallies, known at compile time to hold several instances: the
+// kernels are instantiated for Tal (one instance, no per-deposit instance
+// lookup) and for TalMulti.
+struct TalMulti : Tal {};
+// the instance of batch iteration it
+__device__ __forceinline__ size_t inst_index(const Tal&, int) { return 0; }
+__device__ __forceinline__ size_t inst_index(const TalMulti& tal, int it) { return (size_t)tal.inst_of[it]; }
+inline TalMulti as_multi(const Tal& t) {
+    TalMulti m;
+    static_cast<Tal&>(m) = t;
+    return m;
+}
+// an SHI track's instance constants for the pair kernel: the global index of
+// batch iteration 0 of the instance (iteration it is it0 + it) and the ion mass
+struct InstInfo {
+    int64_t it0;
+    double MSHI;
 };
 constexpr int kNTheta = 180;
 // offsets inside one spectra row
@@ -124,12 +150,17 @@ struct Ctrs {
     unsigned long long shi_slots; // SHI record slots handed out (some unused, marked it = -1)
 };
 
+// the ion tracks of nit iterations, batch iterations it_base .. it_base+nit-1
+// (C.it0 + it is the global index of batch iteration it); ev_inst: the
+// instance's counters (null: ctr->ev)
 template <class T>
 void launch_shi(const McConst<T>& C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
-                cudaStream_t s);
+                cudaStream_t s, int it_base = 0, unsigned long long* ev_inst = nullptr);
+// the pairs of n_ev SHI records; inst (device, per instance; null: one
+// instance, C.it0 and C.MSHI)
 template <class T>
 void launch_pairs(const McConst<T>& C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
-                  PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s);
+                  PQ<T> qhdeep, Tal tal, Ctrs* ctr, cudaStream_t s, const InstInfo* inst = nullptr);
 size_t shi_event_bytes();
 template <class T>
 struct QSet {   // the four particle queues of one generation

@@ -30,7 +30,7 @@ ERR_BITS = {
     1 << 6: "queue full", 1 << 7: "photon negative energy",
 }
 
-ABI_VERSION = 6   # TREKIS_ABI_VERSION of the header these structs mirror
+ABI_VERSION = 7   # TREKIS_ABI_VERSION of the header these structs mirror
 
 _S = MAX_SHELLS
 _O = MAX_OSC
@@ -101,7 +101,8 @@ class RunCfg(C.Structure):
 
 
 class BatchCfg(C.Structure):
-    _fields_ = [("max_concurrent", C.c_int32), ("autotune", C.c_int32), ("device_budget", C.c_int64)]
+    _fields_ = [("max_concurrent", C.c_int32), ("autotune", C.c_int32), ("device_budget", C.c_int64),
+                ("separate", C.c_int32), ("pad_", C.c_int32)]
 
 
 class Tune(C.Structure):

@@ -338,7 +338,8 @@ def train_proposal(tables, n_samples=1_000_000, epochs=3, batch=8192, lr=2e-3, E
     return rep.as_dict()
 
 
-def mc_run_batch(tables_list, opts, tallies_list=None, autotune=True, max_concurrent=0, device_budget=0):
+def mc_run_batch(tables_list, opts, tallies_list=None, autotune=True, max_concurrent=0, device_budget=0,
+                 separate=False):
     """Run many instances at once (trekis_mc_run_batch); returns
     (tallies list, status list, tune list as dicts)."""
     n = len(tables_list)
@@ -358,7 +359,8 @@ def mc_run_batch(tables_list, opts, tallies_list=None, autotune=True, max_concur
     for s_ in sts:
         s_.first_offender = -1
     tunes = (abi.Tune * n)()
-    bc = abi.BatchCfg(max_concurrent=max_concurrent, autotune=int(autotune), device_budget=device_budget)
+    bc = abi.BatchCfg(max_concurrent=max_concurrent, autotune=int(autotune), device_budget=device_budget,
+                      separate=int(separate))
     rc = lib.trekis_mc_run_batch(n, tabs, mats, ions, cfgs, cts, sts, C.byref(bc), tunes)
     abi.check(rc, lib)
     tune = [{f: getattr(tu, f) for f, _ in abi.Tune._fields_} for tu in tunes]
