@@ -321,8 +321,10 @@ def run_gpu(args):
         abi.check(rc, lib)
         return st, dt
 
+    warm_step_ev = 0          # collisions of the warm-up steps' step kernels (for whole-process ncu counts)
     for i in range(args.warmup):
-        step(i)
+        st_w, _ = step(i)
+        warm_step_ev += st_w.step_events
         flush.fill_(i & 0xFF)
     torch.cuda.synchronize()
     if world > 1:
@@ -461,6 +463,7 @@ def run_gpu(args):
         "parity": parity_of(snaps, iters), "table_build": tb, "cfg4": c4, "job_tallies": job_sum, "cfg2": c2,
         "clocks": clocks,
         "events": {"total": tot_ev, "per_iteration": tot_ev / (args.steps * iters),
+                   "step_kernel_events": step_ev, "warmup_step_kernel_events": warm_step_ev,
                    "elastic_frac": sum(s.n_el_elastic for s in sts) / max(tot_ev, 1),
                    "fp64_redraws": sum(s.n_fp64_redraws for s in sts),
                    "by_kind_per_iteration": {f: sum(getattr(s, f) for s in sts) / (args.steps * iters) for f in (

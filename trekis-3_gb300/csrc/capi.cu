@@ -292,8 +292,24 @@ static int upload_shi(trekis_tables* t, DevShi<T>& s) {
     s.invdL_ip = upload<T>(b, ia);
     s.invL_last = upload<T>(b, ib);
     s.Mt = upload_i(b, mt);
+    {   // search hints: per row, the lower bound of 1/L at kShiBuckets+1 equally spaced Tot values
+        std::vector<int> h((size_t)nsh * (kShiBuckets + 1), -1);
+        for (int k = 0; k < nsh; ++k) {
+            const double* D = dI.data() + off[k];
+            const int N = off[k + 1] - off[k];
+            bool mono = N > 1 && ia[k] > 0.0 && ib[k] > ia[k];
+            for (int i = 1; i < N && mono; ++i) mono = D[i] >= D[i - 1];
+            if (!mono) continue;
+            for (int q = 0; q <= kShiBuckets; ++q) {
+                const double Tq = ia[k] + (ib[k] - ia[k]) * q / kShiBuckets;
+                const int lb = (int)(std::lower_bound(D, D + N, Tq) - D);
+                h[(size_t)k * (kShiBuckets + 1) + q] = std::min(lb, N - 1);
+            }
+        }
+        s.bkt = upload_i(b, h);
+    }
     s.pow_zp = (T)std::pow((double)t->ion.Zat, 0.66666666);
-    if (!s.sE || !s.sL || !s.pL || !s.d_off || !s.dE || !s.Mt) { set_error("SHI table upload failed"); return TREKIS_ENOMEM; }
+    if (!s.sE || !s.sL || !s.pL || !s.d_off || !s.dE || !s.Mt || !s.bkt) { set_error("SHI table upload failed"); return TREKIS_ENOMEM; }
     // rows at every SHI grid energy of the window
     s.nW = (int)t->shi_row_nodes.size();
     s.w0 = s.nW ? t->shi_row_nodes[0] : 0;

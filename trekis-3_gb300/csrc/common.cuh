@@ -138,6 +138,19 @@ __device__ __forceinline__ int find_monoton(const T* __restrict__ A, int N, T V)
     }
     return i1 + 1;
 }
+// find_monoton from the result j0 of a nearby value: the same index (for a
+// non-decreasing A, j = min(N, 1 + #{k: A[k] <= V})), walked to from j0 in
+// as many steps as the two values are nodes apart; NaN goes to find_monoton
+template <class T>
+__device__ __forceinline__ int walk_monoton(const T* __restrict__ A, int N, T V, int j0) {
+    if (!(V == V)) return find_monoton(A, N, V);
+    int c = j0 - 1;   // a guess of #{k: A[k] <= V}
+    if (c < 0) c = 0;
+    if (c > N) c = N;
+    while (c > 0 && A[c - 1] > V) --c;
+    while (c < N && A[c] <= V) ++c;
+    return c + 1 < N ? c + 1 : N;
+}
 // decreasing array: 1-based i with A[i-1] > V >= A[i] (N below the last, 1 above the first)
 template <class T>
 __device__ __forceinline__ int find_decreasing(const T* __restrict__ A, int N, T V) {

@@ -121,6 +121,7 @@ struct DevTabs {
 
 // SHI tables in the precision of the run, with host-precomputed logarithms so
 // the serial ion track evaluates each log-log interpolation with one exp.
+constexpr int kShiBuckets = 1024;   // search hints per SHI transfer row
 template <class T>
 struct DevShi {
     const T* sE; const T* lE; int nS;  // SHI energy grid and log(E)
@@ -132,6 +133,10 @@ struct DevShi {
     const T* invdL_ip;                 // [nsh] 1/L at the ionisation potential (0: none)
     const T* invL_last;                // [nsh] 1/L at the end of the row
     const int* Mt;                     // [nsh] index of Ip in the row (Find_in_array_monoton)
+    // [nsh][kShiBuckets+1] search hints of the rows: the row's first index
+    // with 1/L >= a + (b - a) q / kShiBuckets (-1 for a row that is not
+    // monotone, which is bisected)
+    const int* bkt;
     T pow_zp;                          // Z_ion^0.66666666
     // transfer rows at the SHI grid energies w0 .. w0 + nW - 1 (trekis_table_cfg.
     // shi_rows_by_energy; nW = 0: the rows above, at the initial energy, serve

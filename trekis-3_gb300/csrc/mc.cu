@@ -978,14 +978,25 @@ __device__ __forceinline__ T shi_path(const DevShi<T>& sh, int nb, T E, T lx) {
 // SHI_energy_transfer's draw on one transfer row (MC:1719-1780): DE[N] lower
 // edges, DI = 1/L (both with logs), Mt the index of Ip, a and b 1/L at Ip and
 // at the row's end; Tot = a + RN (b - a) is inverted in 1/L, log-log
+// (bkt: the row's search hints, or null / -1: bisection; either gives the
+// first node with 1/L >= Tot)
 template <class T>
 __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* lDI, int N, int Mt, T a, T b, T Ip,
-                               T RN) {
+                               T RN, const int* bkt = nullptr) {
     if (N < 1) return (double)Ip;
     const T Tot = (a > T(0) && b > T(0)) ? a + RN * (b - a) : T(1.5e21);
     int nt;
     if (Tot < T(1e20)) {
         int lo = 0, hi = N - 1;
+        if (bkt && bkt[0] >= 0 && Tot == Tot) {
+            // the bound lies in [bkt[q], bkt[q+1]] for Tot in bucket q (both
+            // ends checked, for the rounding of Tot): bisect that range only,
+            // so no lane of a warp walks far
+            const T u = (Tot - a) / (b - a) * T(kShiBuckets);
+            const int q = !(u >= T(0)) ? 0 : (u >= T(kShiBuckets) ? kShiBuckets - 1 : (int)u);
+            const int l = bkt[q], h = bkt[q + 1];
+            if ((l == 0 || DI[l - 1] < Tot) && (h == N - 1 || DI[h] >= Tot)) { lo = l; hi = h; }
+        }
         while (lo < hi) { int mid = (lo + hi) >> 1; if (DI[mid] < Tot) lo = mid + 1; else hi = mid; }
         nt = lo + 1;
     } else nt = Mt;
@@ -1006,7 +1017,8 @@ __device__ double shi_transfer(const DevShi<T>& sh, int k, T Ip, T E, T RN) {
     if (sh.nW == 0) {   // the row at the initial energy (Universal_MC_for_SHI_MAIN.f90:231-238)
         const int o0 = sh.d_off[k];
         return shi_row_draw(sh.dE + o0, sh.ldE + o0, sh.dI + o0, sh.ldI + o0, sh.d_off[k + 1] - o0, sh.Mt[k],
-                            sh.invdL_ip[k], sh.invL_last[k], Ip, RN);
+                            sh.invdL_ip[k], sh.invL_last[k], Ip, RN,
+                            sh.bkt ? sh.bkt + (size_t)k * (kShiBuckets + 1) : nullptr);
     }
     int iE = find_monoton(sh.sE, sh.nS, E);
     if (iE > 1 && m_abs(sh.sE[iE - 2] - E) < T(1.0e-6)) iE -= 1;
@@ -1084,10 +1096,12 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
         }
     };
     double E = C.ion_E0, t0 = 0.0, tn, Z = 0.0, L;
+    int nb_last;   // the grid bin of the ion's last energy: the next search walks from it
     {
         EvStream<T> s(C.rk, pid, 0xFFFFFFFFu);
         const T Et = (T)E, lx = m_log(Et);
         const int nb = find_monoton(sh.sE, sh.nS, Et);
+        nb_last = nb;
         L = (double)shi_path(sh, nb, Et, lx);
         L = -L * (double)m_log(s.next());
         const double dt = flight_time(E, L);
@@ -1099,7 +1113,8 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
         if (ord >= (1u << 26)) { err |= TREKIS_ERR_NAN; break; }   // no SHI track has this many collisions
         EvStream<T> s(C.rk, pid, ord);
         const T Et = (T)E, lx = m_log(Et);
-        const int nb = find_monoton(sh.sE, sh.nS, Et);
+        const int nb = walk_monoton(sh.sE, sh.nS, Et, nb_last);   // the ion slows by little per collision
+        nb_last = nb;
         // Which_shell
         int k = C.nsh - 1;
         {
