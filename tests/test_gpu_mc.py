@@ -361,3 +361,26 @@ def test_output_files_of_a_gpu_run(small1, tmp_path):
     want = g.view("Out_nh")[:, :, vb[0], vb[1]].T / NMC * 1e24
     assert np.allclose(np.array([[float(x) for x in r[1:]] for r in rows]), want, rtol=1e-15, atol=0.0)
 
+
+
+@pytest.mark.gpu
+def test_run_sharded_exact_single_rank(small1):
+    """shard.run_sharded_exact on a one-rank gloo group (the multi-rank
+    exchange itself runs on the CPU in tests/test_shard_gloo.py): the radial
+    tallies equal one trekis_mc_run bit for bit."""
+    import socket
+    import torch.distributed as dist
+    from trekis import shard
+    w, t, _o = small1
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=0, world_size=1)
+    try:
+        got = shard.run_sharded_exact(t, api.RunOptions(seed=12), 0, 1, 6)
+    finally:
+        dist.destroy_process_group()
+    ref, _ = api.mc_run(t, api.RunOptions(seed=12), NMC=6)
+    for k in ref.a:
+        assert np.array_equal(got[k], ref[k]), k
