@@ -235,6 +235,31 @@ __device__ __forceinline__ T nfp1(const Tab<T>& t, T E) {
 }
 
 
+// find_monoton over a FastTab's energies (the same index), from the bucket
+// hint and a short forward walk; lx = log(E) only picks the bucket
+template <class T>
+__device__ __forceinline__ int fast_index(const FastTab<T>& t, T E, T lx) {
+    if (!(E > T(0))) return find_monoton(t.E, t.n, E);
+    int b = (int)m_floor((lx - t.lo) * t.inv) - 1;
+    b = b < 0 ? 0 : (b >= t.nb ? t.nb - 1 : b);
+    int n = t.hint[b];
+    while (n < t.n && t.node[n - 1].E <= E) ++n;
+    return n;
+}
+
+// Next_free_path_1d (nfp1) at the bracket n that find_monoton gives for E
+template <class T>
+__device__ __forceinline__ T nfp1_at(const FastTab<T>& t, int n, T E) {
+    if (n == 1) {
+        const FNode<T> a = t.node[0], c = t.node[1];
+        T M = interp<T>(1, a.E, c.E, a.L, c.L, E);
+        return M < a.E ? a.E : M;
+    }
+    const FNode<T> lo = t.node[n - 2], hi = t.node[n - 1];
+    if (lo.L >= T(1.0e16)) return lo.L;
+    return interp5_acc<T>(lo.E, hi.E, lo.L, hi.L, E);
+}
+
 // Next_free_path_2d on a FastTab: same result as nfp2 (same comparisons,
 // same log-log formula with precomputed logs); lx = log(E) is shared.
 // The walk carries the nodes it passes, so the bracketing interval

@@ -679,8 +679,8 @@ __device__ __forceinline__ T interp5_checked(T E1, T E2, T S1, T S2, T Ex, T thr
 // (CS:2027-2040).
 template <class T>
 __device__ T interp_transfer(const T* Eg, int nE, const int* roff, const T* rhw, const T* rL, T Ele, T L_need,
-                             float fg = -1.f, const int* rmono = nullptr, bool* ill = nullptr) {
-    int iE = find_monoton(Eg, nE, Ele);
+                             float fg = -1.f, const int* rmono = nullptr, bool* ill = nullptr, int iE0 = 0) {
+    int iE = iE0 > 0 ? iE0 : find_monoton(Eg, nE, Ele);   // iE0: the caller's find_monoton(Eg, nE, Ele)
     if (iE > 1 && m_abs(Eg[iE - 2] - Ele) < T(1.0e-6)) iE -= 1;
     // beyond the grid the rows (and the caller's MFP) are extrapolated in log E,
     // which multiplies the FP32 rounding of the logarithms
@@ -803,8 +803,11 @@ __device__ __noinline__ float phonon_fp64(const DevTabs<double>& t64, bool hole,
 template <class T, class S>
 __device__ T phonon_transfer(const DevTabs<T>& tb, bool hole, T Eel, S& s, bool* defer = nullptr,
                              unsigned long long* nredo = nullptr) {
-    const T EMFP = hole ? nfp1(Tab<T>{tb.hElastE, tb.hElastL, tb.nHel}, Eel)
-                        : nfp1(Tab<T>{tb.elastE, tb.elastL, tb.nEl}, Eel);
+    // the elastic MFP table and the rows share one energy grid: one search
+    // (by the table's bucket hint) serves both
+    const FastTab<T>& ft = hole ? tb.fHEMFP : tb.fEMFP;
+    const int n = fast_index(ft, Eel, f_log(Eel));
+    const T EMFP = nfp1_at(ft, n, Eel);
     T u;
     double ud;
     s.next2(u, ud);
@@ -812,9 +815,9 @@ __device__ T phonon_transfer(const DevTabs<T>& tb, bool hole, T Eel, S& s, bool*
     bool ill = false;
     bool* pill = (sizeof(T) == 4) ? &ill : nullptr;
     T hw = hole ? interp_transfer(tb.hElastE, tb.nHel, tb.herow_off, tb.herow_hw, tb.herow_L, Eel, L_need, -1.f,
-                                  (const int*)nullptr, pill)
+                                  (const int*)nullptr, pill, n)
                 : interp_transfer(tb.elastE, tb.nEl, tb.erow_off, tb.erow_hw, tb.erow_L, Eel, L_need, -1.f,
-                                  (const int*)nullptr, pill);
+                                  (const int*)nullptr, pill, n);
     if constexpr (sizeof(T) == 4) {
         if (ill && tb.alt) {
             if (defer) { *defer = true; return T(0); }
