@@ -13,7 +13,7 @@
 module trekis_gb300
   use iso_c_binding
   implicit none
-  integer, parameter :: TREKIS_ABI_VERSION = 7
+  integer, parameter :: TREKIS_ABI_VERSION = 8
   integer, parameter :: TREKIS_MAX_ATOMS = 8, TREKIS_MAX_SHELLS = 16, &
                         TREKIS_MAX_OSC = 16, TREKIS_MAX_PH_OSC = 8
   ! return codes
@@ -86,6 +86,7 @@ module trekis_gb300
                     Out_tot_Ne, Out_tot_Nphot, Out_tot_E, Out_E_e, Out_E_phot, Out_E_at, Out_E_h
      integer(c_int32_t) :: N_dos, pad_
      type(c_ptr) :: Out_Ee_vs_E, Out_Eh_vs_E, Out_theta, Out_theta_h
+     type(c_ptr) :: Out_Ne_Em, Out_E_Em, Out_Ee_vs_E_Em
   end type
 
   type, bind(C) :: trekis_status

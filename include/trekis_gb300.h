@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define TREKIS_ABI_VERSION 7
+#define TREKIS_ABI_VERSION 8
 
 #define TREKIS_MAX_ATOMS   8   /* kinds of atoms in a compound                 */
 #define TREKIS_MAX_SHELLS  16  /* shells per kind of atom                      */
@@ -110,9 +110,9 @@ typedef struct {
     double Egap;          /* [eV]                                         */
     double Layer;         /* [A] thickness of the analysed layer          */
     double N_VB_el;       /* valence electrons per formula unit           */
-    double work_function; /* [eV] (<=0: no emission)                      */
-    double bar_length;    /* [A]                                          */
-    double bar_height;    /* [eV]                                         */
+    double work_function; /* [eV] surface emission when > 0               */
+    double bar_length;    /* [A] width of the surface barrier             */
+    double bar_height;    /* [eV] height of the surface barrier           */
     double hole_mass;     /* [me] valence-hole mass (>=1e3: immobile; <0: from DOS) */
     double El_eff_mass;   /* [me] electron mass in the dispersion (0: from DOS) */
     double cut_off;       /* [eV] electron/VB-hole cut-off                */
@@ -242,6 +242,19 @@ typedef struct {
     double* Out_theta;     /* [(Nt+1)*180] electron polar angle of flight,
                               1-degree bins (row Nt+1 stays zero)          */
     double* Out_theta_h;   /* [(Nt+1)*180] the same for mobile valence holes */
+    /* Surface emission (material work_function > 0; calculate_emission,
+     * Monte_Carlo.f90:2477-2513, tallied at :958-959 and :1100-1109).  An
+     * electron whose collision point lies in front of the surface (Z < 0)
+     * leaves the target, keeping its energy and flight in the tallies above
+     * but colliding no more.  Out_Ne_Em: electrons emitted up to each grid
+     * time; Out_E_Em: their energies outside, E - work_function.
+     * Out_Ee_vs_E_Em is a spectrum like Out_Ee_vs_E: emitted electrons per eV
+     * of E - work_function on bins whose edges are the Out_R values divided
+     * by 10, each iteration normalised by its own emitted count at that time.
+     * All three stay zero without emission. */
+    double* Out_Ne_Em;      /* [Nt]                                     */
+    double* Out_E_Em;       /* [Nt]                                     */
+    double* Out_Ee_vs_E_Em; /* [Nt*N_R]                                 */
 } trekis_tallies;
 
 /* Counters and error record. */
@@ -384,8 +397,8 @@ int32_t trekis_mc_run_device(const trekis_tables* t, const trekis_material* mat,
  *   1. each replica calls trekis_mc_run_exact, which ADDS its exact sums to
  *      words[trekis_exact_words(t, cfg)] (zero it first) instead of making
  *      FP64 tallies; the spectra (Out_Ee_vs_E, Out_Eh_vs_E, Out_theta,
- *      Out_theta_h) are added to `out` as trekis_mc_run does, and no other
- *      member of `out` changes;
+ *      Out_theta_h, Out_Ee_vs_E_Em) are added to `out` as trekis_mc_run
+ *      does, and no other member of `out` changes;
  *   2. the words of all replicas are summed element by element as int64 (any
  *      order, e.g. one integer all-reduce): each 128-bit sum is stored as four
  *      32-bit limbs, low first, in int64 words, so the limb sums of up to
@@ -441,9 +454,10 @@ int32_t trekis_exact_finish(const trekis_tables* t, const trekis_material* mat,
  *   - sampler must be 0: the learned proposal is not run here
  *     (TREKIS_EUNSUPPORTED otherwise).
  *   - status->device_ms and status->step_ms stay 0 (no timing events).
- *   - the spectra (Out_Ee_vs_E, Out_Eh_vs_E, Out_theta, Out_theta_h) must be
- *     NULL: their per-iteration histograms do not fit the fixed scratch
- *     (TREKIS_EUNSUPPORTED otherwise).
+ *   - the spectra (Out_Ee_vs_E, Out_Eh_vs_E, Out_theta, Out_theta_h,
+ *     Out_Ee_vs_E_Em) must be NULL: their per-iteration histograms do not
+ *     fit the fixed scratch (TREKIS_EUNSUPPORTED otherwise).  Out_Ne_Em and
+ *     Out_E_Em are tallied as by the allocating entry point.
  *   - the scratch is zeroed by each call where the kernels need zeros
  *     (tallies, counters, staging), so nothing has to be cleared between
  *     calls.

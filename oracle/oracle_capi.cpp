@@ -129,6 +129,7 @@ double oracle_shi_transfer(void* t, const trekis_material* m, int a, int s, doub
 double oracle_dsf_transfer(void* t, int hole, double Eel, double u1, double u2) {
     return dsf_transfer(((Tables*)t)->dsf[hole ? 1 : 0], Eel, u1, u2);
 }
+void oracle_barrier(const trekis_material* m, double* E1, double* gamma) { barrier_parameters(*m, *E1, *gamma); }
 void oracle_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) { philox4x32(ctr, key, out); }
 uint64_t oracle_child_pid(uint64_t parent, uint32_t ordinal, uint32_t slot) { return child_pid(parent, ordinal, slot); }
 uint64_t oracle_shi_pid(int64_t it) { return shi_pid(it); }

@@ -104,6 +104,8 @@ double next_free_path_2d(const MFPTab& t, double E);
 double next_free_path_1d(const MFPTab& t, double E);
 double interp_transfer(const RowSet& R, double Ele, double L_need);
 double dsf_transfer(const DsfTab& D, double Eel, double RN1, double RN2);
+// barrier_parameters (Monte_Carlo.f90:2094-2115) of the material's surface
+void barrier_parameters(const trekis_material& m, double& E1, double& gamma);
 double shi_transfer_probe(const Tables& T, const trekis_material& m, int A, int S, double E, double RN);
 
 }  // namespace orc

@@ -211,6 +211,14 @@ struct Ctx {
     double *sEe = nullptr, *sEh = nullptr, *sth = nullptr, *sthh = nullptr;
     int N_dos = 0;
     uint64_t cnt[8];
+    // surface emission (work_function > 0): barrier_parameters' E1 and gamma,
+    // the energies E - W of this iteration's emitted electrons in the order
+    // of emission (Em_electrons, Em_Nel), their tallies and spectrum bins
+    bool emit = false;
+    double em_E1 = 0, em_gamma = 0;
+    std::vector<double> em;
+    double *emN = nullptr, *emE = nullptr, *sEm = nullptr;
+    std::vector<double> Eg;   // Out_E = Out_R / 10
 };
 
 inline bool is_vb(const Ctx& c, int a, int s) { return a == c.a_vb && s == c.s_vb; }
@@ -228,6 +236,35 @@ double tn_of(double t0, double L, double V) { return (V > 1.0e-10) ? t0 + L / V 
 
 void cut_e(Ctx& c, P& p) { if (p.E < c.m->cut_off) p.tn = 1.0e20; }
 void cut_h(Ctx& c, H& p) { if (p.Mass < 1e15 && p.Ehkin < c.m->cut_off) p.tn = 1.0e20; }
+
+// calculate_emission (Monte_Carlo.f90:2477-2513), after the collision that
+// left the electron at Z < 0: it escapes when E >= 1.5 bar_height, else with
+// the penetrability 1/(1 + exp(gamma (E1 - E))) of the barrier when
+// E - work_function > 0 (one uniform drawn); an escaped electron collides no
+// more (tn = L = 1e30) but keeps its energy and flight.  Otherwise a flight
+// away from the target (cos theta < 0) is turned back.
+void emission(Ctx& c, P& p, Stream& s) {
+    const trekis_material& m = *c.m;
+    if (!(p.Z < 0.0)) return;
+    bool out;
+    double Ek;
+    if (p.E >= 1.5 * m.bar_height) {
+        out = true;
+        Ek = p.E - m.work_function;
+    } else {
+        const double RN = s.next();
+        const double pen = 1.0 / (1.0 + std::exp(c.em_gamma * (c.em_E1 - p.E)));
+        Ek = p.E - m.work_function;
+        out = (Ek > 0.0) && (RN < pen);
+    }
+    if (out) {
+        p.tn = 1.0e30;
+        p.L = 1.0e30;
+        c.em.push_back(Ek);
+    } else if (std::cos(p.theta) < 0.0) {
+        p.theta = Pi - p.theta;
+    }
+}
 
 // New_Angles_both (Monte_Carlo.f90:1328-1360)
 void new_angles(double phi0, double theta0, double theta, double psi, double& phi1, double& theta1) {
@@ -572,6 +609,7 @@ void electron_event(Ctx& c, int NOP, int i) {
     p.E = Eel - dE; p.t0 = tev; p.X = X; p.Y = Y; p.Z = Z; p.L = Mt; p.theta = th1; p.phi = ph1;
     p.tn = tn_of(p.t0, Mt, v_electron(p.E));
     cut_e(c, p);
+    if (c.emit) emission(c, p, s);
     if (p.E < -1.0e-9 || std::isnan(p.E)) c.err |= TREKIS_ERR_NEG_ENERGY_E;
 }
 
@@ -894,6 +932,20 @@ void statistics(Ctx& c, int i, double tim) {
         sumH += hh.E + hh.Ehkin;
     }
     if (c.sEe) spectra(c, i, co);
+    if (c.emit) {   // Monte_Carlo.f90:958-959, 1100-1109
+        double sum = 0.0;
+        for (double x : c.em) sum += x;
+        c.emN[i - 1] += (double)c.em.size();
+        c.emE[i - 1] += sum;
+        if (c.sEm) {
+            const double n = (double)c.em.size();
+            for (double x : c.em) {
+                const int j = find_monoton(c.Eg.data(), NR, x);
+                const double w = (j > 1) ? c.Eg[j - 1] - c.Eg[j - 2] : c.Eg[0];
+                c.sEm[(i - 1) + (size_t)Nt * (j - 1)] += 1.0 / w / n;
+            }
+        }
+    }
     c.totNe[i - 1] += (double)c.el.size();
     if (c.m->include_photons) {
         c.totNph[i - 1] += (double)nph;
@@ -909,7 +961,7 @@ void statistics(Ctx& c, int i, double tim) {
 // ---- Monte_Carlo_modelling (Monte_Carlo.f90:427-679) --------------------------------
 void one_iteration(Ctx& c, int64_t it_global, int sched) {
     const trekis_material& m = *c.m;
-    c.el.clear(); c.ho.clear(); c.ph.clear();
+    c.el.clear(); c.ho.clear(); c.ph.clear(); c.em.clear();
     c.At_NRG = 0.0;
     c.shi = P();
     c.shi.E = c.ion->E;
@@ -985,6 +1037,22 @@ void one_iteration(Ctx& c, int64_t it_global, int sched) {
 
 }  // namespace
 
+// barrier_parameters (Monte_Carlo.f90:2094-2115): the surface barrier's E1
+// and gamma of the penetrability 1/(1 + exp(gamma (E1 - E))), from the work
+// function W, the barrier height U and its length [A]
+void barrier_parameters(const trekis_material& m, double& E1, double& gamma) {
+    const double W = m.work_function, U = m.bar_height, L = m.bar_length * 1.0e-10;
+    const double B = 2.0 * U - W + 2.0 * std::sqrt(U * U - U * W);
+    const double h2 = (2.0 * Pi * h) * (2.0 * Pi * h);
+    const double ksi = 0.5 * std::sqrt(8.0 * me * L * L * B * e / h2 - 1.0);
+    const double bb = std::cosh(2.0 * Pi * ksi);
+    const double delta = 2.0 * Pi * L * std::sqrt(2.0 * me * e) / (2.0 * Pi * h);
+    E1 = U + 2.0 * std::sqrt(U * (U - W)) * (std::acosh(bb) / (delta * (std::sqrt(U) + std::sqrt(U - W))) - 1.0);
+    const double g1 = delta * (std::sqrt(E1) + std::sqrt(E1 - W));
+    const double g2 = delta * (std::sqrt(E1) - std::sqrt(E1 - W));
+    gamma = (g1 * std::sinh(g1) + 2.0 * g2 * std::sinh(g2)) / (std::sqrt(E1 * (E1 - W)) * (bb + std::cosh(g1)));
+}
+
 double shi_transfer_probe(const Tables& T, const trekis_material& m, int A, int S, double E, double RN) {
     return shi_transfer(T, m.atoms[A].Ip[S], A, S, E, RN);
 }
@@ -993,7 +1061,7 @@ double shi_transfer_probe(const Tables& T, const trekis_material& m, int A, int 
 int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, const trekis_run_cfg& cfg,
            trekis_tallies& out, trekis_status* st, int nthreads, int sched) {
     if (cfg.dt_flag != 0 && cfg.dt_flag != 1) return TREKIS_EINVAL;
-    if (m.work_function > 0.0 || m.kind_of_EMFP < 0 || m.kind_of_EMFP > 2 || ion.Kind_ion != 0) return TREKIS_EUNSUPPORTED;
+    if (m.kind_of_EMFP < 0 || m.kind_of_EMFP > 2 || ion.Kind_ion != 0) return TREKIS_EUNSUPPORTED;
     if (m.kind_of_EMFP == 2 && (T.dsf[0].nE < 2 || T.dsf[1].nE < 2)) return TREKIS_EINVAL;
     if (m.kind_of_EMFP == 1 && T.el_elast_rows.rows.empty()) return TREKIS_EINVAL;
     if (!T.has_shi) return TREKIS_EINVAL;
@@ -1021,10 +1089,15 @@ int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, con
     double R0 = 0.0;
     for (int j = 0; j < NR; ++j) { Vg[j] = 1.0 / ((Rg[j] * Rg[j] - R0 * R0) * Pi * m.Layer); R0 = Rg[j]; }
     const size_t n2 = (size_t)Nt * NR, n4 = n2 * m.N_atoms * Nshl, n1 = Nt, n3 = (size_t)Nt * m.N_atoms * Nshl;
-    const bool spec = out.Out_Ee_vs_E || out.Out_Eh_vs_E || out.Out_theta || out.Out_theta_h;
+    const bool emit = m.work_function > 0.0;
+    const bool spec = out.Out_Ee_vs_E || out.Out_Eh_vs_E || out.Out_theta || out.Out_theta_h ||
+                      (emit && out.Out_Ee_vs_E_Em);
     if (spec && out.N_dos != m.N_dos) return TREKIS_EINVAL;
     const size_t nth2 = (size_t)(Nt + 1) * 180, nd2 = (size_t)Nt * std::max(m.N_dos, 0);
-    const size_t per = 5 * n2 + 3 * n4 + 6 * n1 + n3 + (spec ? n2 + nd2 + 2 * nth2 : 0);
+    const size_t nem = emit ? 2 * n1 + (spec ? n2 : 0) : 0;
+    const size_t per = 5 * n2 + 3 * n4 + 6 * n1 + n3 + (spec ? n2 + nd2 + 2 * nth2 : 0) + nem;
+    double em_E1 = 0.0, em_gamma = 0.0;
+    if (emit) barrier_parameters(m, em_E1, em_gamma);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
     int nth = omp_get_max_threads();
@@ -1061,6 +1134,13 @@ int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, con
         if (spec) {
             c.sEe = c.Eh_t + n3; c.sEh = c.sEe + n2; c.sth = c.sEh + nd2; c.sthh = c.sth + nth2;
             c.N_dos = m.N_dos;
+        }
+        if (emit) {
+            c.emit = true; c.em_E1 = em_E1; c.em_gamma = em_gamma;
+            c.emN = c.Eh_t + n3 + (spec ? n2 + nd2 + 2 * nth2 : 0); c.emE = c.emN + n1;
+            if (spec) c.sEm = c.emE + n1;
+            c.Eg.resize(NR);
+            for (int j = 0; j < NR; ++j) c.Eg[j] = Rg[j] / 10.0;   // Out_E (Monte_Carlo.f90:953)
         }
         std::memset(c.cnt, 0, sizeof c.cnt);
 #pragma omp for schedule(dynamic)
@@ -1101,6 +1181,11 @@ int mc_run(const Tables& T, const trekis_material& m, const trekis_ion& ion, con
         addto(out.Out_Eh_vs_E, off, nd2); off += nd2;
         addto(out.Out_theta, off, nth2); off += nth2;
         addto(out.Out_theta_h, off, nth2); off += nth2;
+    }
+    if (emit) {
+        addto(out.Out_Ne_Em, off, n1); off += n1;
+        addto(out.Out_E_Em, off, n1); off += n1;
+        if (spec) { addto(out.Out_Ee_vs_E_Em, off, n2); off += n2; }
     }
     if (st) {
         uint32_t eb = 0;

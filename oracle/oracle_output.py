@@ -83,13 +83,15 @@ def vb_numbers(atoms):
 def write(out_dir, run, T, NMC):
     """run: dict with ion (name, Z, Mass, E, Kind_Zeff, fixed_Zeff), material
     (name, Dens, At_Dens, Layer, temp, hole_mass, kind_of_EMFP,
-    include_photons, dos_E, atoms=[{name, shells=[{name, designator, Ip}]}]),
+    include_photons, work_function, bar_length, bar_height, dos_E,
+    atoms=[{name, shells=[{name, designator, Ip}]}]),
     Tim, dt, dt_flag, R, ion_Zeff, duration_s.  T: dict of the tally arrays
     (Fortran order, un-normalised) and Nt, NR, Nat.  Returns the folder."""
     ion, mat = run["ion"], run["material"]
     N, NR, Nat = T["Nt"], T["NR"], T["Nat"]
-    inv = 1.0 / NMC
+    nmc = float(NMC)   # every sum divided by NMC (Universal_MC_for_SHI_MAIN.f90:281-304)
     photons = bool(mat["include_photons"])
+    emission = mat.get("work_function", 0.0) > 0.0
     base = os.path.join(out_dir, f"{ion['name']}_E_{ff(ion['E'] / 1e6, 8, 2).strip()}_MeV_"
                                  f"{ff(run['Tim'], 10, 2).strip()}_fs")
     d, i = base, 0
@@ -101,10 +103,10 @@ def write(out_dir, run, T, NMC):
     R = run["R"]
 
     def a2(name, k, i):
-        return T[name][k + N * i] * inv
+        return T[name][k + N * i] / nmc
 
     def a4(name, k, i, at, s):
-        return T[name][k + N * (i + NR * (at + Nat * s))] * inv
+        return T[name][k + N * (i + NR * (at + Nat * s))] / nmc
 
     def header(first):
         return first + "".join(ff(t, 10, 2) + "[fs]   " for t in tg) + " \n"
@@ -148,11 +150,19 @@ def write(out_dir, run, T, NMC):
             names = ["Barkas", "Bohr", "Nikolaev-Dmitriev", "Schiwietz-Grande"]
             kz = ion["Kind_Zeff"] if 0 <= ion["Kind_Zeff"] < 4 else 0
             f.write(f" Ion equilibrium charge is used with {names[kz]} formula, point-like charge model for SHI.\n")
-        f.write(" Elastic scattering: " + ("phonon CDF" if mat["kind_of_EMFP"] == 1 else "Mott atomic cross sections") + "\n")
+        ke = mat["kind_of_EMFP"]
+        f.write(" Elastic scattering: " + ("phonon CDF" if ke == 1 else "DSF" if ke == 2 else "Mott atomic cross sections")
+                + "\n")
+        if emission:   # print_parameters, Sorting_output_data.f90:235-244
+            f.write(f" Electron emission included. Work function = {ff(mat['work_function'], 12, 3).strip()} [eV]\n")
+            f.write(f" Potential barrier length = {ff(mat['bar_length'], 12, 3).strip()} [A] Barrier height = "
+                    f"{ff(mat['bar_height'], 12, 3).strip()} [eV]\n")
+        else:
+            f.write(" Electron emission is excluded\n")
         f.write(f" Number of MC iterations: {NMC}\n")
         if run["ion_Zeff"] >= 0:
             f.write(f" Ion equilibrium charge:         {ff(run['ion_Zeff'], 6, 3).strip()} [electron charge]\n")
-        f.write(f" MC calculated energy loss (Se): {ff(T['Out_tot_E'][N - 1] * inv / mat['Layer'], 9, 2).strip()} [eV/A]\n")
+        f.write(f" MC calculated energy loss (Se): {ff(T['Out_tot_E'][N - 1] / nmc / mat['Layer'], 9, 2).strip()} [eV/A]\n")
         if run["duration_s"] >= 0:
             f.write(f" Duration of calculation:        {ff(run['duration_s'], 12, 3).strip()} [sec]\n")
 
@@ -160,7 +170,7 @@ def write(out_dir, run, T, NMC):
         with open(os.path.join(d, fname), "w") as f:
             f.write(header(first))
             for i in range(180):
-                vals = "".join(fe(arr[k + (N + 1) * i] * inv if arr is not None else 0.0) for k in range(N))
+                vals = "".join(fe(arr[k + (N + 1) * i] / nmc if arr is not None else 0.0) for k in range(N))
                 f.write(fe(float(i + 1)) + vals + " \n")
 
     theta("Electrons_theta_distribution.txt", "#Angle[deg] ", T.get("Out_theta"))
@@ -169,9 +179,11 @@ def write(out_dir, run, T, NMC):
     with open(os.path.join(d, "Total_numbers.txt"), "w") as f:
         f.write("#Time[fs]    Ne    Ne_Emitted    Energy[eV]     Energy_Emitted[eV]" + (" N_photons" if photons else "") + "\n")
         for k in range(N):
-            row = [tg[k], T["Out_tot_Ne"][k] * inv, 0.0, T["Out_tot_E"][k] * inv, 0.0]
+            nem = T["Out_Ne_Em"][k] / nmc if emission and "Out_Ne_Em" in T else 0.0
+            eem = T["Out_E_Em"][k] / nmc if emission and "Out_E_Em" in T else 0.0
+            row = [tg[k], T["Out_tot_Ne"][k] / nmc, nem, T["Out_tot_E"][k] / nmc, eem]
             if photons:
-                row.append(T["Out_tot_Nphot"][k] * inv)
+                row.append(T["Out_tot_Nphot"][k] / nmc)
             f.write("".join(fe(v) for v in row) + "\n")
 
     with open(os.path.join(d, "Total_energies.txt"), "w") as f:
@@ -181,12 +193,12 @@ def write(out_dir, run, T, NMC):
                 f.write(label(a, s) + "[eV]    ")
         f.write(" \n")
         for k in range(N):
-            row = [tg[k], T["Out_E_e"][k] * inv, T["Out_E_at"][k] * inv, 0.0]
+            row = [tg[k], T["Out_E_e"][k] / nmc, T["Out_E_at"][k] / nmc, 0.0]
             if photons:
-                row.append(T["Out_E_phot"][k] * inv)
+                row.append(T["Out_E_phot"][k] / nmc)
             for a, at in enumerate(atoms):
                 for s in range(len(at["shells"])):
-                    row.append(T["Out_E_h"][k + N * (a + Nat * s)] * inv)
+                    row.append(T["Out_E_h"][k + N * (a + Nat * s)] / nmc)
             f.write("".join(fe(v) for v in row) + " \n")
 
     radial("Radial_electron_density[1_cm^-3].txt", lambda k, i: a2("Out_ne", k, i) * 1.0e24)
@@ -208,6 +220,13 @@ def write(out_dir, run, T, NMC):
         for i, e in enumerate(mat["dos_E"]):
             f.write(ff(e, 9, 1) + "".join(fe(a2("Out_Eh_vs_E", k, i) if "Out_Eh_vs_E" in T else 0.0)
                                           for k in range(N)) + " \n")
+
+    if emission:   # Sorting_output_data.f90:591-615
+        with open(os.path.join(d, "Emitted_electron_distribution_vs_E[1_eV].txt"), "w") as f:
+            f.write(header("#Energy[eV] "))
+            for i in range(NR):
+                f.write(ff(R[i] / 10.0, 9, 1) + "".join(fe(a2("Out_Ee_vs_E_Em", k, i) if "Out_Ee_vs_E_Em" in T else 0.0)
+                                                    for k in range(N)) + " \n")
 
     lat = [[0.0] * NR for _ in range(N)]
     for i in range(NR):

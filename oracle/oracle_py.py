@@ -60,6 +60,8 @@ def load():
     lib.oracle_shi_transfer.argtypes = [vp, vp, C.c_int, C.c_int, C.c_double, C.c_double]
     lib.oracle_dsf_transfer.restype = C.c_double
     lib.oracle_dsf_transfer.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double]
+    lib.oracle_barrier.restype = None
+    lib.oracle_barrier.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.oracle_free_path.restype = C.c_double
     lib.oracle_free_path.argtypes = [vp, C.c_int, C.c_double]
     _lib = lib

@@ -157,6 +157,75 @@ def test_counts_match_tallies(small_runs):
     assert np.allclose(counts, a["Out_tot_Ne"], rtol=1e-9)
 
 
+def _barrier_restated(W, U, Lb):
+    """barrier_parameters (Monte_Carlo.f90:2094-2115) in numpy: E1 and gamma
+    of the surface barrier's penetrability 1/(1 + exp(gamma (E1 - E)))."""
+    me, e, hb = 9.1093821545e-31, 1.602176487e-19, 1.05457162853e-34
+    L = Lb * 1e-10
+    B = 2 * U - W + 2 * np.sqrt(U * U - U * W)
+    ksi = 0.5 * np.sqrt(8 * me * L * L * B * e / (2 * np.pi * hb) ** 2 - 1)
+    bb = np.cosh(2 * np.pi * ksi)
+    d = 2 * np.pi * L * np.sqrt(2 * me * e) / (2 * np.pi * hb)
+    E1 = U + 2 * np.sqrt(U * (U - W)) * (np.arccosh(bb) / (d * (np.sqrt(U) + np.sqrt(U - W))) - 1)
+    g1, g2 = d * (np.sqrt(E1) + np.sqrt(E1 - W)), d * (np.sqrt(E1) - np.sqrt(E1 - W))
+    gamma = (g1 * np.sinh(g1) + 2 * g2 * np.sinh(g2)) / (np.sqrt(E1 * (E1 - W)) * (bb + np.cosh(g1)))
+    return E1, gamma
+
+
+def test_barrier_parameters(oracle_lib):
+    """The oracle's barrier parameters against a numpy restatement; the
+    penetrability rises through 1/2 near E1, just under the barrier height."""
+    import ctypes as C
+    w = configs.small(configs.cfg1)
+    for W, U, Lb in ((4.0, 6.18, 10.0), (1.0, 6.18, 10.0), (5.5, 8.0, 5.0)):
+        m = w.material
+        m.work_function, m.bar_height, m.bar_length = W, U, Lb
+        h = m.to_c()
+        E1, g = C.c_double(), C.c_double()
+        oracle_lib.oracle_barrier(C.addressof(h.struct), C.byref(E1), C.byref(g))
+        e1, gg = _barrier_restated(W, U, Lb)
+        assert abs(E1.value - e1) < 1e-12 * e1 and abs(g.value - gg) < 1e-12 * gg, (W, U, Lb)
+        assert W < E1.value < U and g.value > 0
+
+
+def test_emission_oracle():
+    """Surface emission in the oracle (calculate_emission, Monte_Carlo.f90:
+    2477-2513): emitted counts never fall in time, each iteration's
+    spectrum is normalised to one electron, the event order does not change a
+    bit, energy is still conserved (an emitted electron keeps its energy in
+    the tallies), and a work function above every electron's reach emits only
+    what clears 1.5 barrier heights."""
+    import oracle_py
+    w = configs.small(configs.cfg1, NMC=4, Tim=20.0)
+    w.material.work_function = 4.0
+
+    def run(sched, nthreads):
+        h = w.material.to_c()
+        tc = abi.TableCfg(build_shi=1, build_photon=w.material.include_photons,
+                          shi_E_window_lo=w.ion_E * 0.5, shi_E_window_hi=w.ion_E * 1.01)
+        o = oracle_py.OracleTables(h, api.ion_struct(w), tc, nthreads=nthreads)
+        tal = api.new_tallies(w, spectra=True)
+        cfg, _R = api.run_cfg(w, api.RunOptions(seed=9))
+        st = abi.Status.fresh()
+        o.mc_run(cfg, tal, st, nthreads=nthreads, sched=sched)
+        return tal, st
+
+    a, sa = run(0, 1)
+    b, sb = run(1, 3)
+    assert sa.n_events == sb.n_events > 0
+    for k in a.a:
+        assert np.allclose(a[k], b[k], rtol=1e-12, atol=1e-12 * (np.max(np.abs(a[k])) + 1e-300)), k
+    ne, ee = a["Out_Ne_Em"], a["Out_E_Em"]
+    assert ne[-1] > 0 and np.all(np.diff(ne) >= 0) and np.all(ee >= 0)
+    width = np.diff(np.concatenate(([0.0], np.asarray(w.R_edges) / 10.0)))
+    per_t = a.view("Out_Ee_vs_E_Em") @ width
+    assert np.all(per_t <= w.NMC + 1e-9) and abs(per_t[-1] - round(per_t[-1])) < 1e-9 and per_t[-1] >= 1
+    tot = a["Out_tot_E"]
+    assert tot[0] > 0 and np.max(np.abs(tot - tot[0])) / tot[0] < 1e-12
+    parts = a["Out_E_e"] + a["Out_E_h"].reshape(-1, a.Nt).sum(0) + a["Out_E_at"] + a["Out_E_phot"]
+    assert np.allclose(parts, tot, rtol=1e-12)
+
+
 def test_seed_changes_result():
     w = configs.small(configs.cfg0, NMC=2)
     a, _ = _oracle_run(w, api.RunOptions(seed=1))

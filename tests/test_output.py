@@ -35,7 +35,8 @@ def run_dict(w, ion_Zeff, duration_s):
                 "fixed_Zeff": float(w.ion_Z)},
         "material": {"name": m.name, "Dens": m.Dens, "At_Dens": m.At_Dens, "Layer": m.Layer, "temp": m.temp,
                      "hole_mass": m.hole_mass, "kind_of_EMFP": m.kind_of_EMFP,
-                     "include_photons": m.include_photons, "dos_E": list(m.dos.E) if m.dos is not None else [],
+                     "include_photons": m.include_photons, "work_function": m.work_function,
+                     "bar_length": m.bar_length, "bar_height": m.bar_height, "dos_E": list(m.dos.E) if m.dos is not None else [],
                      "atoms": [{"name": api.ELEMENTS[a.Z - 1],
                                 "shells": [{"name": api.shell_name(s.designator), "designator": s.designator,
                                             "Ip": s.Ip} for s in a.shells]} for a in m.atoms]},
@@ -44,10 +45,13 @@ def run_dict(w, ion_Zeff, duration_s):
     }
 
 
-@pytest.mark.parametrize("cfg_fn,photons", [(configs.cfg1, 1), (configs.cfg0, 0)])
-def test_files_match_the_oracle(lib, tmp_path, cfg_fn, photons):
+@pytest.mark.parametrize("cfg_fn,photons,emission", [(configs.cfg1, 1, False), (configs.cfg0, 0, False),
+                                                     (configs.cfg1, 1, True)])
+def test_files_match_the_oracle(lib, tmp_path, cfg_fn, photons, emission):
     w = configs.small(cfg_fn, Tim=12.0, n_R=7)
     assert w.material.include_photons == photons
+    if emission:   # surface emission: its spectrum file and the emission columns
+        w.material.work_function = 4.25
     tal = seeded_tallies(w, 11 + photons)
     before = {k: v.copy() for k, v in tal.a.items()}
     NMC = 7
@@ -60,6 +64,7 @@ def test_files_match_the_oracle(lib, tmp_path, cfg_fn, photons):
     names = sorted(os.listdir(got))
     assert names == sorted(os.listdir(ref))
     assert ("Radial_photon_density[1_cm^-3].txt" in names) == bool(photons)
+    assert ("Emitted_electron_distribution_vs_E[1_eV].txt" in names) == emission
     for n in names:
         a = open(os.path.join(got, n), "rb").read()
         b = open(os.path.join(ref, n), "rb").read()

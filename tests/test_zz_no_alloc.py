@@ -48,14 +48,16 @@ def _close(a, b, what):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [0, 1])
-def test_noalloc_matches_allocating_entry_point(gpu_lib, precision):
+@pytest.mark.parametrize("precision,emission", [(0, False), (1, False), (0, True), (1, True)])
+def test_noalloc_matches_allocating_entry_point(gpu_lib, precision, emission):
     pytest.importorskip("torch")
     w = configs.small(configs.cfg1, NMC=6, Tim=30.0)   # mobile valence holes, radiative decay, photons
     for atom in w.material.atoms:
         for sh in atom.shells:
             if sh.designator < 63:
                 sh.Radiat = sh.Auger * 2.0
+    if emission:
+        w.material.work_function = 4.0   # surface emission: Out_Ne_Em and Out_E_Em tallied too
     t = api.Tables(w, lib=gpu_lib)
     opt = api.RunOptions(precision=precision, seed=23)
     ref, sr = _run(gpu_lib, t, w, opt, noalloc=False)
@@ -68,6 +70,8 @@ def test_noalloc_matches_allocating_entry_point(gpu_lib, precision):
             assert getattr(sg, f) == getattr(sr, f), (call, f)
         assert sg.error_bits == sr.error_bits
         _close(got, ref, f"call {call}")
+    if emission:
+        assert ref["Out_Ne_Em"][-1] > 0
     t.close()
 
 

@@ -117,7 +117,7 @@ bool same_material(const trekis_material* a, const trekis_material* b) {
 // Whether instances i and j may share one wavefront: the same material (so
 // the same electron, hole, photon and elastic tables; the tables do not
 // depend on the ion), tally shape, time grid, precision, seed and knobs; no
-// spectra, table sampler.
+// spectra, table sampler, no surface emission.
 bool mergeable(const trekis_material* mi, const trekis_material* mj, const trekis_run_cfg& a, const trekis_run_cfg& b,
                const trekis_tallies& ta, const trekis_tallies& tb) {
     if (!same_material(mi, mj)) return false;
@@ -127,6 +127,7 @@ bool mergeable(const trekis_material* mi, const trekis_material* mj, const treki
         return false;
     if (a.N_R > 0 && std::memcmp(a.Out_R, b.Out_R, 8 * (size_t)a.N_R) != 0) return false;
     if (ta.Nat != tb.Nat || ta.Nshl != tb.Nshl) return false;
+    if (mi->work_function > 0.0) return false;   // surface emission runs on the single-instance kernels
     for (const trekis_tallies* t : {&ta, &tb})
         if (t->Out_Ee_vs_E || t->Out_Eh_vs_E || t->Out_theta || t->Out_theta_h) return false;
     return true;

@@ -387,7 +387,8 @@ __global__ void k_add(double* dst, const double* src, size_t n) {
 struct DevOut {
     double *ne, *Ee, *np, *Ep, *lat, *nh, *Eh, *Ek, *totNe, *totNp, *totE, *E_e, *E_p, *E_at, *E_h;
     double *sEe = nullptr, *sEh = nullptr, *sth = nullptr, *sthh = nullptr;   // spectra
-    bool spectra() const { return sEe || sEh || sth || sthh; }
+    double *emN = nullptr, *emE = nullptr, *sEm = nullptr;                    // surface emission
+    bool spectra() const { return sEe || sEh || sth || sthh || sEm; }
 };
 
 template <class T> static const DevTabs<T>& tabs_of(const trekis_tables* t);
@@ -429,6 +430,8 @@ struct Workspace {
     int spec_cap = 0;
     size_t spec_it = 0, spec_row = 0;
     double *wE = nullptr, *wD = nullptr;   // bin widths [eV]
+    double* wEm = nullptr;                 // emitted electrons' bin widths [eV] (runs with emission)
+    T* em_Eg = nullptr;                    // their bin edges Out_R / 10 [eV]
     double per_it_peak = 0.0;   // live particles per iteration at the peak of the last batch (batch sizing)
     cudaEvent_t e0 = nullptr, e1 = nullptr, s0 = nullptr, s1 = nullptr;
     Fork fk;   // second stream for the hole kernel of a step
@@ -438,8 +441,8 @@ struct Workspace {
     }
 };
 
-static uint64_t ws_key(int prec, int64_t cap, int Nt, int NR, int Nat, int Nshl, bool spec) {
-    uint64_t k = (uint64_t)prec * 2 + (spec ? 1 : 0);
+static uint64_t ws_key(int prec, int64_t cap, int Nt, int NR, int Nat, int Nshl, bool spec, bool em) {
+    uint64_t k = (uint64_t)prec * 4 + (spec ? 2 : 0) + (em ? 1 : 0);
     k = k * 1000003ull + (uint64_t)cap;
     k = k * 1000003ull + (uint64_t)Nt;
     k = k * 1000003ull + (uint64_t)NR;
@@ -451,7 +454,8 @@ template <class T>
 static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, int Nshl, bool spec,
                             int* rc) {
     const int64_t cap = cfg.queue_capacity > 0 ? cfg.queue_capacity : (int64_t)(sizeof(T) == 4 ? 8 : 4) << 20;
-    const uint64_t key = ws_key(sizeof(T), cap, Nt, cfg.N_R, Nat, Nshl, spec);
+    const bool em = t->mat.work_function > 0.0;
+    const uint64_t key = ws_key(sizeof(T), cap, Nt, cfg.N_R, Nat, Nshl, spec, em);
     if (t->ws && t->ws_key == key) { *rc = 0; return (Workspace<T>*)t->ws.get(); }
     t->ws.reset();
     auto* w = new Workspace<T>();
@@ -472,7 +476,7 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     const int NR = cfg.N_R, nsh = t->nsh;
     const size_t rows = (size_t)Nt + 2;
     const size_t n_e = rows * NR, n_h = rows * nsh * NR, n_l = (size_t)Nt * NR;
-    w->n_all = 2 * (4 * n_e + 3 * n_h) + n_l;   // difference + single-row blocks, lattice
+    w->n_all = 2 * (4 * n_e + 3 * n_h) + n_l + 2 * rows;   // difference + single-row blocks, lattice, emission
     w->tall = (unsigned long long*)b.alloc(8 * w->n_all);
     w->ctr = (Ctrs*)b.alloc(sizeof(Ctrs));
     w->tg = (T*)b.alloc(sizeof(T) * Nt);
@@ -488,13 +492,14 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     w->calls = (double*)b.alloc(8 * (3 * (size_t)Nt + n3));
     const size_t n2 = (size_t)Nt * NR, n4 = n2 * Nat * Nshl;
     const size_t nsp = n2 + (size_t)Nt * t->dos_E.size() + 2 * (size_t)(Nt + 1) * kNTheta;
-    w->out_n = 5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3 + nsp;
+    w->out_n = 5 * n2 + 3 * n4 + 6 * (size_t)Nt + n3 + 2 * (size_t)Nt + nsp + n2;   // ... emission, spectra
     w->out = (double*)b.alloc(8 * w->out_n);
     w->cap_ev = std::max<int64_t>(cap / 2, 1 << 16);
     w->evs = b.alloc(shi_event_bytes() * w->cap_ev);
     w->lat_rows = (unsigned long long*)b.alloc(16 * (size_t)Nt);
     w->acc.n2 = (size_t)Nt * NR;
     w->acc.nh = (size_t)Nt * NR * nsh;
+    w->acc.nt = (size_t)Nt;
     w->acc.lo = (unsigned long long*)b.alloc(8 * w->acc.n());
     w->acc.hi = (unsigned long long*)b.alloc(8 * w->acc.n());
     if (!w->evs || !w->lat_rows || !w->acc.lo || !w->acc.hi) return nullptr;
@@ -504,13 +509,18 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     if (cudaMemset(w->prop_err, 0, 16) != cudaSuccess) { *rc = TREKIS_ECUDA; return nullptr; }
     if (spec) {   // histograms of up to 1 GiB worth of iterations per batch
         const int nD = (int)t->dos_E.size();
-        w->spec_row = sp_row_ints(NR, nD);
+        w->spec_row = sp_row_ints(NR, nD, em);
         w->spec_it = (size_t)(Nt + 2) * w->spec_row;
         w->spec_cap = (int)std::max<size_t>(1, std::min<size_t>((1ull << 30) / (4 * w->spec_it), 65535));
         w->spec = (int*)b.alloc(4 * w->spec_it * w->spec_cap);
         w->wE = (double*)b.alloc(8 * NR);
         w->wD = (double*)b.alloc(8 * std::max(nD, 1));
         if (!w->spec || !w->wE || !w->wD) return nullptr;
+        if (em) {
+            w->wEm = (double*)b.alloc(8 * NR);
+            w->em_Eg = (T*)b.alloc(sizeof(T) * NR);
+            if (!w->wEm || !w->em_Eg) return nullptr;
+        }
         std::vector<double> wd(std::max(nD, 1), 1.0);
         for (int j = 0; j < nD; ++j)   // Monte_Carlo.f90:1034-1039
             wd[j] = j > 0 ? t->dos_E[j] - t->dos_E[j - 1] : (nD > 1 ? t->dos_E[1] - t->dos_E[0] : 1.0);
@@ -522,6 +532,7 @@ static Workspace<T>* get_ws(trekis_tables* t, const trekis_run_cfg& cfg, int Nt,
     tal.e_cnt = w->tall; tal.e_E = w->tall + 2 * n_e; tal.p_cnt = w->tall + 4 * n_e; tal.p_E = w->tall + 6 * n_e;
     tal.h_cnt = w->tall + 8 * n_e; tal.h_E = tal.h_cnt + 2 * n_h; tal.h_Ek = tal.h_E + 2 * n_h;
     tal.lat = tal.h_Ek + 2 * n_h;
+    tal.em = tal.lat + n_l;
     tal.spec = w->spec; tal.sp_nE = NR; tal.sp_nD = (int)t->dos_E.size(); tal.sp_row = w->spec_row;
     tal.sp_it = w->spec_it;
     w->hn = w->hstage; w->hE = w->hn + (size_t)Nt * NR * nsh; w->hK = w->hE + (size_t)Nt * NR * nsh;
@@ -619,6 +630,14 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     std::vector<double> wE(cfg.N_R);   // electron energy bins are the radius values (Monte_Carlo.f90:1024-1029)
     for (int j = 0; j < cfg.N_R; ++j) wE[j] = j > 0 ? cfg.Out_R[j] - cfg.Out_R[j - 1] : cfg.Out_R[0];
     if (ws->wE) CK(cudaMemcpyAsync(ws->wE, wE.data(), 8 * cfg.N_R, cudaMemcpyHostToDevice, strm));
+    // emitted electrons' energy bins: Out_E = Out_R / 10 (Monte_Carlo.f90:953, 1100-1109)
+    std::vector<double> emE(cfg.N_R), wEm(cfg.N_R);
+    for (int j = 0; j < cfg.N_R; ++j) emE[j] = cfg.Out_R[j] / 10.0;
+    for (int j = 0; j < cfg.N_R; ++j) wEm[j] = j > 0 ? emE[j] - emE[j - 1] : emE[0];
+    std::vector<T> emET(emE.begin(), emE.end());
+    if (ws->wEm) CK(cudaMemcpyAsync(ws->wEm, wEm.data(), 8 * cfg.N_R, cudaMemcpyHostToDevice, strm));
+    if (ws->em_Eg) CK(cudaMemcpyAsync(ws->em_Eg, emET.data(), sizeof(T) * cfg.N_R, cudaMemcpyHostToDevice, strm));
+    C.em_Eg = ws->em_Eg;
     C.tg = ws->tg; C.Rg = ws->Rg;
     set_grid_hint_sizes<T>(C, tgT[0], tgT[Nt - 1], RgT[0], RgT[cfg.N_R - 1]);
     C.tg_hint = ws->th; C.rg_hint = C.rg_nb ? ws->rh : nullptr;
@@ -626,6 +645,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     const int NR = cfg.N_R, nsh = t->nsh;
     Tal tal = ws->tal;
     if (!out.spectra()) tal.spec = nullptr;
+    if (!C.emit) tal.em = nullptr;   // no emission tallies to make
     Ctrs* dctr = ws->ctr;
     const double* dV = ws->V;
     CK(cudaMemsetAsync(ws->hstage, 0, 8 * ws->hstage_n, strm));
@@ -638,7 +658,10 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
     std::vector<McConst<T>> Ci;
     std::vector<int64_t> nmc_of(1, cfg.NMC);
     if (grp) {
-        if (out.spectra() || cfg.sampler != 0) { set_error("merged instances take neither spectra nor sampler 1"); return TREKIS_EINVAL; }
+        if (out.spectra() || cfg.sampler != 0 || C.emit) {
+            set_error("merged instances take neither spectra, sampler 1 nor surface emission");
+            return TREKIS_EINVAL;
+        }
         nmc_of.assign(n_inst, 0);
         for (int i = 0; i < n_inst; ++i) nmc_of[i] = grp->cfgs[i].NMC;
         unsigned long long* tall = (unsigned long long*)gb.alloc(8 * ws->n_all * n_inst);
@@ -652,14 +675,14 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             return TREKIS_ENOMEM;
         }
         const ptrdiff_t shift = tall - ws->tall;   // the same layout, from another base
-        for (unsigned long long** f : {&tal.e_cnt, &tal.e_E, &tal.p_cnt, &tal.p_E, &tal.h_cnt, &tal.h_E, &tal.h_Ek, &tal.lat})
-            *f += shift;
+        for (unsigned long long** f : {&tal.e_cnt, &tal.e_E, &tal.p_cnt, &tal.p_E, &tal.h_cnt, &tal.h_E, &tal.h_Ek, &tal.lat, &tal.em})
+            if (*f) *f += shift;   // em is null without emission
         tal.inst_of = d_inst;
         tal.st_e = tal.st_h = tal.st_lat = ws->n_all;   // whole blocks per instance
         Ci.resize(n_inst);
         for (int i = 0; i < n_inst; ++i) {   // each instance's ion and iterations (its own table set)
             fill_const<T>(grp->tabs[i], grp->cfgs[i], Nt, Ci[i]);
-            Ci[i].tg = C.tg; Ci[i].Rg = C.Rg;
+            Ci[i].tg = C.tg; Ci[i].Rg = C.Rg; Ci[i].em_Eg = C.em_Eg;
         }
     }
     int64_t NMC_all = 0;
@@ -815,19 +838,20 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             for (const Slice& sl : slices) {
                 Tal ti = tal;
                 const size_t o = (size_t)sl.inst * ws->n_all;
-                for (unsigned long long** f : {&ti.e_cnt, &ti.e_E, &ti.p_cnt, &ti.p_E, &ti.h_cnt, &ti.h_E, &ti.h_Ek, &ti.lat})
-                    *f += o;
+                for (unsigned long long** f : {&ti.e_cnt, &ti.e_E, &ti.p_cnt, &ti.p_E, &ti.h_cnt, &ti.h_E, &ti.h_Ek, &ti.lat, &ti.em})
+                    if (*f) *f += o;
                 Acc ai = acc;
                 ai.lo += (size_t)sl.inst * acc.n(); ai.hi += (size_t)sl.inst * acc.n();
                 acc_batch(ti, Nt, NR, nsh, ai, strm);
-                launches += 4;
+                launches += tal.em ? 5 : 4;
             }
         } else {
             acc_batch(tal, Nt, NR, nsh, acc, strm);
-            launches += 4;
+            launches += tal.em ? 5 : 4;
         }
         if (tal.spec) {
-            fin_spectra(tal, nb, Nt, ws->wE, ws->wD, out.sEe, out.sEh, out.sth, out.sthh, strm);
+            fin_spectra(tal, nb, Nt, C.emit != 0, ws->wE, ws->wD, ws->wEm, out.sEe, out.sEh, out.sth, out.sthh,
+                        out.sEm, strm);
             launches += 2;
         }
         CK(cudaGetLastError());
@@ -860,9 +884,9 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
         d2h += 16 * acc.n();
     } else {
         FinOut fo{out.ne, out.Ee, out.totNe, out.E_e, out.np, out.Ep, out.totNp, out.E_p,
-                  ws->hn, ws->hE, ws->hK, ws->htn, ws->htE, out.lat, out.E_at};
+                  ws->hn, ws->hE, ws->hK, ws->htn, ws->htE, out.lat, out.E_at, out.emN, out.emE};
         acc_finish(acc, Nt, NR, nsh, dV, fo, ws->lat_rows, strm);
-        launches += 5;
+        launches += (out.emN || out.emE) ? 6 : 5;
     }
     // holes: compact shells -> caller slices
     {
@@ -1081,7 +1105,6 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
     if (!t || !cfg || !o || !mat) return TREKIS_EINVAL;
     if (!t->has_shi) { set_error("tables were built without the SHI part"); return TREKIS_EINVAL; }
     if (t->mat.include_photons && !t->has_phot) { set_error("photon tables missing"); return TREKIS_EINVAL; }
-    if (t->mat.work_function > 0.0) { set_error("surface emission is not supported"); return TREKIS_EUNSUPPORTED; }
     if (t->ion.Kind_ion != 0) { set_error("Brandt-Kitagawa ions are not supported"); return TREKIS_EUNSUPPORTED; }
     if (cfg->NMC < 0 || cfg->N_R < 1 || !cfg->Out_R || !(cfg->Tim > 0) || !(cfg->dt > 0)) return TREKIS_EINVAL;
     if (!time_grid_ok(cfg->Tim, cfg->dt, cfg->dt_flag)) {
@@ -1096,6 +1119,12 @@ static int check_run(const trekis_tables* t, const trekis_material* mat, const t
     for (int a = 0; a < t->mat.N_atoms; ++a) if (t->mat.atoms[a].N_shl > o->Nshl) return TREKIS_EINVAL;
     if (o->Out_Eh_vs_E && o->N_dos != (int)t->dos_E.size()) { set_error("N_dos of the tallies differs from the material's"); return TREKIS_EINVAL; }
     return TREKIS_OK;
+}
+
+// the spectra a call tallies (the emitted electrons' only with emission on)
+static bool wants_spectra(const trekis_tables* t, const trekis_tallies* o) {
+    return o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h ||
+           (t->mat.work_function > 0.0 && o->Out_Ee_vs_E_Em);
 }
 
 static int run_dispatch(const trekis_tables* tc, const trekis_run_cfg* cfg, int Nt, int Nat, int Nshl, DevOut d,
@@ -1113,7 +1142,7 @@ static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, i
     // the workspace holds the per-call sums; create it first
     int rc = 0;
     double* calls;
-    const bool spec = o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h;
+    const bool spec = wants_spectra(t, o);
     if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) return rc; calls = calls_of<double>(t); }
     else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) return rc; calls = calls_of<float>(t); }
     CK(cudaMemsetAsync(calls, 0, 8 * (3 * (size_t)Nt + n3), s));
@@ -1127,6 +1156,7 @@ static int run_device_core(const trekis_tables* tc, const trekis_run_cfg* cfg, i
     d.totNe = o->Out_tot_Ne; d.totNp = o->Out_tot_Nphot; d.totE = o->Out_tot_E;
     d.E_e = Ee_call; d.E_p = Ep_call; d.E_at = Eat_call; d.E_h = Eh_call;
     d.sEe = o->Out_Ee_vs_E; d.sEh = o->Out_Eh_vs_E; d.sth = o->Out_theta; d.sthh = o->Out_theta_h;
+    if (t->mat.work_function > 0.0) { d.emN = o->Out_Ne_Em; d.emE = o->Out_E_Em; d.sEm = o->Out_Ee_vs_E_Em; }
     if (!d.ne || !d.Ee || !d.np || !d.Ep || !d.lat || !d.totNe || !d.totNp) {
         set_error("the device entry point needs every radial and count tally array");
         return TREKIS_EINVAL;
@@ -1169,7 +1199,8 @@ static int mc_run_host(const trekis_tables* tc, const trekis_material* mat, cons
     if (rc) { if (st) st->code = rc; return rc; }
     trekis_tables* t = const_cast<trekis_tables*>(tc);
     const size_t n2 = (size_t)Nt * cfg->N_R, n4 = n2 * o->Nat * o->Nshl, n3 = (size_t)Nt * o->Nat * o->Nshl;
-    const bool spec = o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h;
+    const bool spec = wants_spectra(t, o);
+    const bool em = t->mat.work_function > 0.0;
     const size_t nD2 = (size_t)Nt * t->dos_E.size(), nth2 = (size_t)(Nt + 1) * kNTheta;
     if (cfg->precision == 1) { if (!get_ws<double>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) { if (st) st->code = rc; return rc; } }
     else { if (!get_ws<float>(t, *cfg, Nt, o->Nat, o->Nshl, spec, &rc)) { if (st) st->code = rc; return rc; } }
@@ -1185,12 +1216,15 @@ static int mc_run_host(const trekis_tables* tc, const trekis_material* mat, cons
     double** f1[] = {&d.Out_tot_Ne, &d.Out_tot_Nphot, &d.Out_tot_E, &d.Out_E_e, &d.Out_E_phot, &d.Out_E_at};
     for (double** f : f1) { *f = p; p += Nt; }
     d.Out_E_h = p; p += n3;
+    d.Out_Ne_Em = em ? p : nullptr; p += Nt;
+    d.Out_E_Em = em ? p : nullptr; p += Nt;
     // spectra go through the same staging, only those the caller asked for
     d.Out_Ee_vs_E = o->Out_Ee_vs_E ? p : nullptr; p += n2;
     d.Out_Eh_vs_E = o->Out_Eh_vs_E ? p : nullptr; p += nD2;
     d.Out_theta = o->Out_theta ? p : nullptr; p += nth2;
     d.Out_theta_h = o->Out_theta_h ? p : nullptr; p += nth2;
-    if (!spec) nout = (size_t)(d.Out_E_h - base) + n3;   // stage and copy back only the main tallies
+    d.Out_Ee_vs_E_Em = (em && o->Out_Ee_vs_E_Em) ? p : nullptr; p += n2;
+    if (!spec) nout = (size_t)(d.Out_E_h - base) + n3 + 2 * (size_t)Nt;   // stage and copy back only the main tallies
     rc = (cudaMemsetAsync(base, 0, 8 * nout, s) == cudaSuccess) ? 0 : TREKIS_ECUDA;
     if (!rc) rc = run_device_core(t, cfg, Nt, &d, st, s, x);
     std::vector<double> h(nout);
@@ -1205,7 +1239,11 @@ static int mc_run_host(const trekis_tables* tc, const trekis_material* mat, cons
     add(o->Out_nh, n4); add(o->Out_Eh, n4); add(o->Out_Ehkin, n4);
     add(o->Out_tot_Ne, Nt); add(o->Out_tot_Nphot, Nt); add(o->Out_tot_E, Nt); add(o->Out_E_e, Nt);
     add(o->Out_E_phot, Nt); add(o->Out_E_at, Nt); add(o->Out_E_h, n3);
-    if (spec) { add(o->Out_Ee_vs_E, n2); add(o->Out_Eh_vs_E, nD2); add(o->Out_theta, nth2); add(o->Out_theta_h, nth2); }
+    add(em ? o->Out_Ne_Em : nullptr, Nt); add(em ? o->Out_E_Em : nullptr, Nt);
+    if (spec) {
+        add(o->Out_Ee_vs_E, n2); add(o->Out_Eh_vs_E, nD2); add(o->Out_theta, nth2); add(o->Out_theta_h, nth2);
+        add(em ? o->Out_Ee_vs_E_Em : nullptr, n2);
+    }
     if (st) st->code = TREKIS_OK;
     return TREKIS_OK;
 }
@@ -1287,7 +1325,7 @@ int64_t trekis_exact_words(const trekis_tables* t, const trekis_run_cfg* cfg) {
     if (!t || !cfg || cfg->N_R < 1) return -1;
     const int64_t Nt = trekis_time_points(cfg->Tim, cfg->dt, cfg->dt_flag);
     if (Nt < 1) return -1;
-    return 4 * (5 * Nt * cfg->N_R + 3 * Nt * cfg->N_R * (int64_t)t->nsh);
+    return 4 * (5 * Nt * cfg->N_R + 3 * Nt * cfg->N_R * (int64_t)t->nsh + 2 * Nt);
 }
 
 int32_t trekis_mc_run_exact(const trekis_tables* t, const trekis_material* mat, const trekis_ion* ion,

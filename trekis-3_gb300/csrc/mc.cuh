@@ -1,4 +1,4 @@
-// mc.cuh -- data layout of the event-based wavefront (shared by mc.cu and capi.cu).
+// mc.cuh -- data layout of the event-based wavefront (shared by the track-loop units and capi.cu).
 #pragma once
 #include <cstdint>
 #include <cstring>
@@ -52,6 +52,12 @@ struct McConst {
     T Et_lat;           // Mtarget c^2 / e [eV]
     // FP64 values of the transfer draw's constants, for FP32 draws redone in FP64
     double Egap_d, hole_mass_d, Eplasmon_d;
+    // surface emission (work_function > 0): the work function, 1.5 x the
+    // barrier height, barrier_parameters' E1 and gamma, and the emitted
+    // electrons' energy bins Out_R / 10 (device, spectra only)
+    int emit;
+    T em_W, em_bar15, em_E1, em_gamma;
+    const T* em_Eg;
     uint32_t rk[20];    // Philox round keys of seed
 };
 
@@ -103,16 +109,29 @@ struct Tal {
     const uint16_t* inst_of = nullptr;
     size_t st_e = 0, st_h = 0, st_lat = 0;
     unsigned long long* ev_inst = nullptr;
+    // surface emission: difference arrays over the time index (rows
+    // 0..Nt+1) of emitted electrons and of their fixed-point energies outside,
+    // em[0 .. Nt+1] and em[Nt+2 .. 2Nt+3] (an instance's at + st_e)
+    unsigned long long* em = nullptr;
 };
 // The same tallies, known at compile time to hold several instances: the
 // kernels are instantiated for Tal (one instance, no per-deposit instance
 // lookup) and for TalMulti.
 struct TalMulti : Tal {};
+// One instance with surface emission (em set): the electron kernels of runs
+// with a work function are instantiated for TalEmit, so the kernels of every
+// other run carry no emission code at all.
+struct TalEmit : Tal {};
 // the instance of batch iteration it
 __device__ __forceinline__ size_t inst_index(const Tal&, int) { return 0; }
 __device__ __forceinline__ size_t inst_index(const TalMulti& tal, int it) { return (size_t)tal.inst_of[it]; }
 inline TalMulti as_multi(const Tal& t) {
     TalMulti m;
+    static_cast<Tal&>(m) = t;
+    return m;
+}
+inline TalEmit as_emit(const Tal& t) {
+    TalEmit m;
     static_cast<Tal&>(m) = t;
     return m;
 }
@@ -130,7 +149,12 @@ __host__ __device__ inline int sp_eth(int nE) { return 1 + nE; }
 __host__ __device__ inline int sp_nh(int nE) { return 1 + nE + kNTheta; }
 __host__ __device__ inline int sp_hE(int nE) { return 2 + nE + kNTheta; }
 __host__ __device__ inline int sp_hth(int nE, int nD) { return 2 + nE + kNTheta + nD; }
-__host__ __device__ inline size_t sp_row_ints(int nE, int nD) { return (size_t)(2 + nE + 2 * kNTheta + nD); }
+// emitted electrons (runs with surface emission): count, then nE energy bins
+__host__ __device__ inline int sp_emn(int nE, int nD) { return 2 + nE + 2 * kNTheta + nD; }
+__host__ __device__ inline int sp_emE(int nE, int nD) { return 3 + nE + 2 * kNTheta + nD; }
+__host__ __device__ inline size_t sp_row_ints(int nE, int nD, bool em) {
+    return (size_t)(2 + nE + 2 * kNTheta + nD) + (em ? (size_t)(1 + nE) : 0);
+}
 
 constexpr double kEScale = 16777216.0;      // 2^24 per eV for particle energies
 constexpr double kLatScale = 1099511627776.0;  // 2^40 per eV for lattice energy
@@ -218,6 +242,23 @@ constexpr int kRgHintMax = 4096;
 __host__ __device__ inline uint32_t radius_key(float x) { uint32_t u; memcpy(&u, &x, 4); return u >> 19; }
 __host__ __device__ inline uint32_t radius_key(double x) { uint64_t u; memcpy(&u, &x, 8); return (uint32_t)(u >> 48); }
 
+// barrier_parameters (Monte_Carlo.f90:2094-2115): E1 and gamma of the
+// surface barrier's penetrability 1/(1 + exp(gamma (E1 - E))) for an electron
+// of energy E, from the work function W, the barrier height U [eV] and its
+// length [A] (host, FP64)
+inline void barrier_parameters(const trekis_material& m, double& E1, double& gamma) {
+    const double W = m.work_function, U = m.bar_height, L = m.bar_length * 1.0e-10;
+    const double B = 2.0 * U - W + 2.0 * std::sqrt(U * U - U * W);
+    const double h2 = (2.0 * kPi * kH) * (2.0 * kPi * kH);
+    const double ksi = 0.5 * std::sqrt(8.0 * kMe * L * L * B * kE / h2 - 1.0);
+    const double bb = std::cosh(2.0 * kPi * ksi);
+    const double delta = 2.0 * kPi * L * std::sqrt(2.0 * kMe * kE) / (2.0 * kPi * kH);
+    E1 = U + 2.0 * std::sqrt(U * (U - W)) * (std::acosh(bb) / (delta * (std::sqrt(U) + std::sqrt(U - W))) - 1.0);
+    const double g1 = delta * (std::sqrt(E1) + std::sqrt(E1 - W));
+    const double g2 = delta * (std::sqrt(E1) - std::sqrt(E1 - W));
+    gamma = (g1 * std::sinh(g1) + 2.0 * g2 * std::sinh(g2)) / (std::sqrt(E1 * (E1 - W)) * (bb + std::cosh(g1)));
+}
+
 // Run constants of a table set and run configuration (host); the grids,
 // hints and DOS pointers are set by the caller.
 template <class T>
@@ -255,6 +296,13 @@ inline void fill_const(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt
     C.mobile_holes = m.hole_mass < 1e3;
     C.mec2 = (T)(kMe * kC * kC / kE);
     C.alpha = (T)(kE * kE / (kH * kC * 4.0 * kPi * kE0));
+    if (m.work_function > 0.0) {
+        double E1, gamma;
+        barrier_parameters(m, E1, gamma);
+        C.emit = 1;
+        C.em_W = (T)m.work_function; C.em_bar15 = (T)(1.5 * m.bar_height);
+        C.em_E1 = (T)E1; C.em_gamma = (T)gamma;
+    }
     finish_const(C);
 }
 
@@ -297,22 +345,31 @@ void launch_grid_hints(const McConst<T>& C, GHint<T>* th, GHint<T>* rh, cudaStre
 struct Acc {
     unsigned long long *lo = nullptr, *hi = nullptr;
     size_t n2 = 0, nh = 0;   // values of a species block and of a hole block
-    size_t n() const { return 5 * n2 + 3 * nh; }
-    size_t off(int b) const { return b < 4 ? (size_t)b * n2 : (b < 7 ? 4 * n2 + (size_t)(b - 4) * nh : 4 * n2 + 3 * nh); }
+    size_t nt = 0;           // time points (the emission blocks)
+    size_t n() const { return 5 * n2 + 3 * nh + 2 * nt; }
+    size_t off(int b) const {
+        return b < 4 ? (size_t)b * n2
+             : (b < 7 ? 4 * n2 + (size_t)(b - 4) * nh
+             : (b == 7 ? 4 * n2 + 3 * nh : 5 * n2 + 3 * nh + (size_t)(b - 8) * nt));
+    }
 };
-enum { ACC_ECNT = 0, ACC_EE, ACC_PCNT, ACC_PE, ACC_HCNT, ACC_HE, ACC_HEK, ACC_LAT };
+// ... followed by the emitted electrons and their energies outside [Nt each]
+enum { ACC_ECNT = 0, ACC_EE, ACC_PCNT, ACC_PE, ACC_HCNT, ACC_HE, ACC_HEK, ACC_LAT, ACC_EMN, ACC_EME };
 // FP64 destinations of the exact sums (+=); the hole ones are the compact-shell staging
 struct FinOut {
     double *ne, *Ee, *totNe, *E_e, *np, *Ep, *totNp, *E_p, *hn, *hE, *hK, *htn, *htE, *lat, *E_at;
+    double *emN = nullptr, *emE = nullptr;
 };
-// adds one batch's tallies into the call's exact sums (4 launches)
+// adds one batch's tallies into the call's exact sums (4 launches, 5 with emission)
 void acc_batch(const Tal& tal, int Nt, int NR, int nsh, const Acc& a, cudaStream_t s);
-// the FP64 tallies of the exact sums, added into o (5 launches); rows: 2*Nt words of scratch
+// the FP64 tallies of the exact sums, added into o (5 launches, 6 with emission
+// outputs); rows: 2*Nt words of scratch
 void acc_finish(const Acc& a, int Nt, int NR, int nsh, const double* V, const FinOut& o, unsigned long long* rows,
                 cudaStream_t s);
 // spectra of one batch of nit iterations -> FP64 outputs (any may be null);
-// wE[nE], wD[nD]: bin widths in eV
-void fin_spectra(const Tal& tal, int nit, int Nt, const double* wE, const double* wD, double* oEe, double* oEh,
-                 double* oth, double* othh, cudaStream_t s);
+// wE[nE], wD[nD], wEm[nE]: bin widths in eV; em: the rows hold the emitted
+// electrons' columns
+void fin_spectra(const Tal& tal, int nit, int Nt, bool em, const double* wE, const double* wD, const double* wEm,
+                 double* oEe, double* oEh, double* oth, double* othh, double* oEm, cudaStream_t s);
 
 }  // namespace tk

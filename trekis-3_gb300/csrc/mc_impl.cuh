@@ -1,4 +1,4 @@
-// mc.cu -- the Monte Carlo track loop as an event-based wavefront on sm_103a.
+// mc_impl.cuh -- the Monte Carlo track loop as an event-based wavefront on sm_103a.
 //
 // The reference advances one global clock and always processes the earliest
 // event of all particles (Find_min_time_particle, Monte_Carlo.f90:2060-2092),
@@ -21,6 +21,9 @@
 // The event bodies follow, draw for draw, SHI_Monte_Carlo (MC:2153-2249),
 // Electron_Monte_Carlo (MC:2253-2474), Hole_Monte_Carlo (MC:2517-2869) and
 // Photon_Monte_Carlo (MC:2873-2965).
+// The kernels are templates over the precision T; mc_f32.cu and mc_f64.cu
+// instantiate them (two translation units, compiled in parallel).
+#pragma once
 #include "mc.cuh"
 #include "tc.cuh"
 
@@ -754,7 +757,7 @@ __device__ U transfer_rows(const XConst<U>& X, const DevTabs<U>& tb, bool hole, 
 // An FP32 ionising draw redone in FP64 on the FP64 rows: the shell MFP, L_need
 // and the inversion, from the same energy and the same random word (RNd).
 // Out of line: it runs for a few per cent of the draws.
-__device__ __noinline__ float transfer_fp64(const McConst<float>& C, const DevTabs<double>& t64, bool hole, int k,
+static __device__ __noinline__ float transfer_fp64(const McConst<float>& C, const DevTabs<double>& t64, bool hole, int k,
                                             double Ele, double RNd, unsigned& err) {
     const double Lt = hole ? nfp1(Tab<double>{t64.hE, t64.hL + (size_t)k * t64.nH, t64.nH}, Ele)
                            : nfp1(Tab<double>{t64.elE, t64.elL + (size_t)k * t64.nE, t64.nE}, Ele);
@@ -783,7 +786,7 @@ __device__ T sample_transfer(const McConst<T>& C, const DevTabs<T>& tb, bool hol
 }
 
 // The phonon-CDF elastic draw of an FP32 run redone in FP64 (see transfer_fp64)
-__device__ __noinline__ float phonon_fp64(const DevTabs<double>& t64, bool hole, double Eel, double ud) {
+static __device__ __noinline__ float phonon_fp64(const DevTabs<double>& t64, bool hole, double Eel, double ud) {
     const double EMFP = hole ? nfp1(Tab<double>{t64.hElastE, t64.hElastL, t64.nHel}, Eel)
                              : nfp1(Tab<double>{t64.elastE, t64.elastL, t64.nEl}, Eel);
     double hw = hole ? interp_transfer<double>(t64.hElastE, t64.nHel, t64.herow_off, t64.herow_hw, t64.herow_L, Eel,
@@ -894,7 +897,7 @@ __device__ T dsf_transfer(const DevDsf<T>& d, T Eel, T u1, T u2, bool* ill) {
 }
 
 // an FP32 DSF draw redone in FP64 on the FP64 tables (see transfer_fp64)
-__device__ __noinline__ float dsf_fp64(const DevDsf<double>& d, double Eel, double u1, double u2) {
+static __device__ __noinline__ float dsf_fp64(const DevDsf<double>& d, double Eel, double u1, double u2) {
     return (float)dsf_transfer<double>(d, Eel, u1, u2, nullptr);
 }
 
@@ -1240,6 +1243,41 @@ __global__ void __launch_bounds__(128) k_pairs(const __grid_constant__ McConst<T
 }
 
 // ---- cascade events ------------------------------------------------------------------------
+// calculate_emission (MC:2477-2513), after the collision that left an
+// electron of energy E at Z < 0 (in front of the surface): it escapes when E
+// reaches 1.5 times the barrier height, else with the barrier's penetrability
+// 1/(1 + exp(gamma (E1 - E))) when E - W > 0.  The uniform of that case is
+// the first word of block 2^32 - 1 of the event's stream (c0, c1, c2): a
+// block the event's sequential draws never reach, so the draw does not
+// depend on how many numbers the collision took.  Returns whether the
+// electron escapes, after tallying its energy outside, E - W, from the
+// event's grid time ti on (and binning it on Out_R / 10 for the spectrum).
+// Values in, so that the caller's particle and stream stay in registers.
+template <class T, class TL>
+__device__ __noinline__ bool surface_emission(const McConst<T>& C, const TL& tal, T E, uint32_t c0, uint32_t c1,
+                                              uint32_t c2, int it, int ti) {
+    const T Ek = E - C.em_W;
+    if (!(E >= C.em_bar15)) {
+        uint32_t w[4];
+        philox4x32_rk(c0, c1, c2, 0xFFFFFFFFu, C.rk, w);
+        const T RN = Uni<T>::of(w[0]);
+        const T pen = T(1) / (T(1) + m_exp(C.em_gamma * (C.em_E1 - E)));
+        if (!(Ek > T(0) && RN < pen)) return false;
+    }
+    if (tal.em) {
+        unsigned long long* em = tal.em + inst_index(tal, it) * tal.st_e;
+        atomicAdd(em + ti, 1ull);
+        atomicAdd(em + (C.Nt + 2) + ti, (unsigned long long)fixE(Ek));
+    }
+    if (tal.spec) {   // no end row: an emitted electron counts at every later time
+        int* row = tal.spec + (size_t)it * tal.sp_it + (size_t)ti * tal.sp_row;
+        const int nE = tal.sp_nE, nD = tal.sp_nD;
+        atomicAdd(row + sp_emn(nE, nD), 1);
+        atomicAdd(row + sp_emE(nE, nD) + find_monoton(C.em_Eg, C.NR, Ek) - 1, 1);
+    }
+    return true;
+}
+
 // One electron event.  FULL=false compiles only the elastic branch (the hot
 // kernel): an ionising draw returns false with the particle untouched, and the
 // event is redone from the same stream by the FULL version.  DEFER leaves the
@@ -1320,6 +1358,12 @@ __device__ bool electron_event(const McConst<T>& C, const DevTabs<T>& tb, const 
     new_angles(ph0, th0, theta, phi, ph1, th1);
     p.X = X; p.Y = Y; p.Z = Z; p.th = th1; p.ph = ph1;
     cut_e(C, p);
+    if constexpr (std::is_same<TL, TalEmit>::value) {   // runs with surface emission
+        if (Z < T(0)) {   // an escaped electron collides no more; else a flight outwards turns back
+            if (surface_emission(C, tal, p.E, s.c0, s.c1, s.c2, (int)p.it, ti0)) { p.tn = T(1.0e30); p.L = T(1.0e30); }
+            else if (m_cos(p.th) < T(0)) p.th = pi_<T>() - p.th;
+        }
+    }
     if (p.E < T(-1.0e-9) || m_isnan(p.E)) err |= TREKIS_ERR_NEG_ENERGY_E;
     if constexpr (!DEFER) p.ti = emit_electron(C, tal, p, ti0);
     return true;
@@ -1807,10 +1851,6 @@ void launch_propose(const Proposer& p, const McConst<T>& C, const DevTabs<T>& tb
     // 24 KB used; asking for 48 KB keeps at most four CTAs (256 TMEM columns) per SM
     k_propose<T><<<p.blocks, 128, 48 * 1024, s>>>(C, tb, e_inel, h_inel, ctr, p.net, p.guess, p.err);
 }
-template void launch_propose<float>(const Proposer&, const McConst<float>&, const DevTabs<float>&, PQ<float>,
-                                    PQ<float>, const Ctrs*, cudaStream_t);
-template void launch_propose<double>(const Proposer&, const McConst<double>&, const DevTabs<double>&, PQ<double>,
-                                     PQ<double>, const Ctrs*, cudaStream_t);
 
 template <class T>
 void launch_shi(const McConst<T>& C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
@@ -1827,13 +1867,15 @@ void launch_pairs(const McConst<T>& C, const DevTabs<T>& tb, const void* evs, in
         k_pairs<T, TalMulti><<<g, 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qhvb, qhdeep, as_multi(tal), ctr, inst);
     else k_pairs<T, Tal><<<g, 128, 0, s>>>(C, tb, (const ShiEv*)evs, n_ev, qe, qhvb, qhdeep, tal, ctr, inst);
 }
-size_t shi_event_bytes() { return sizeof(ShiEv); }
 
 template <class T, class TL>
 static void launch_step_tl(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in,
                            const QSet<T>& out, PQ<T> e_inel, PQ<T> h_inel, const TL& tal, Ctrs* ctr, int K, int bs,
                            int rare_blocks, cudaStream_t s, const float* guess, const Proposer* prop, const Fork* fk) {
     Out<T> o{{out.q[0], out.q[1], out.q[2], out.q[3]}, ctr};
+    // holes do not emit: their kernels take the tallies without emission
+    using TH = typename std::conditional<std::is_same<TL, TalEmit>::value, Tal, TL>::type;
+    const TH& th = tal;
     // the two hot kernels touch disjoint queues; counters and tallies are atomics
     const bool two = fk && fk->s2 && fk->fork && fk->join && n_in[Q_E] > 0 && n_in[Q_HVB] > 0;
     if (two) {
@@ -1851,10 +1893,10 @@ static void launch_step_tl(const McConst<T>& C, const DevTabs<T>& tb, const QSet
         const unsigned g = (n_in[Q_HVB] + bs - 1) / bs;
         cudaStream_t sh = two ? fk->s2 : s;
         if (C.elast_model == 1)
-            k_hot<T, false, 1, TL><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+            k_hot<T, false, 1, TH><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, th, K);
         else if (C.elast_model == 2)
-            k_hot<T, false, 2, TL><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
-        else k_hot<T, false, 0, TL><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, tal, K);
+            k_hot<T, false, 2, TH><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, th, K);
+        else k_hot<T, false, 0, TH><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, th, K);
     }
     if (two) {
         cudaEventRecord(fk->join, fk->s2);
@@ -1868,26 +1910,15 @@ template <class T>
 void launch_step(const McConst<T>& C, const DevTabs<T>& tb, const QSet<T>& in, const int* n_in, const QSet<T>& out,
                  PQ<T> e_inel, PQ<T> h_inel, Tal tal, Ctrs* ctr, int K, int bs, int rare_blocks, cudaStream_t s,
                  const float* guess, const Proposer* prop, const Fork* fk) {
-    if (tal.inst_of)
+    if (tal.inst_of)   // several instances (never with surface emission)
         launch_step_tl<T, TalMulti>(C, tb, in, n_in, out, e_inel, h_inel, as_multi(tal), ctr, K, bs, rare_blocks, s,
                                     guess, prop, fk);
+    else if (tal.em)   // surface emission
+        launch_step_tl<T, TalEmit>(C, tb, in, n_in, out, e_inel, h_inel, as_emit(tal), ctr, K, bs, rare_blocks, s,
+                                   guess, prop, fk);
     else launch_step_tl<T, Tal>(C, tb, in, n_in, out, e_inel, h_inel, tal, ctr, K, bs, rare_blocks, s, guess, prop, fk);
 }
 
-template void launch_shi<float>(const McConst<float>&, const DevShi<float>&, void*, int64_t, Ctrs*, int, cudaStream_t,
-                                int, unsigned long long*);
-template void launch_shi<double>(const McConst<double>&, const DevShi<double>&, void*, int64_t, Ctrs*, int, cudaStream_t,
-                                 int, unsigned long long*);
-template void launch_pairs<float>(const McConst<float>&, const DevTabs<float>&, const void*, int64_t, PQ<float>,
-                                  PQ<float>, PQ<float>, Tal, Ctrs*, cudaStream_t, const InstInfo*);
-template void launch_pairs<double>(const McConst<double>&, const DevTabs<double>&, const void*, int64_t, PQ<double>,
-                                   PQ<double>, PQ<double>, Tal, Ctrs*, cudaStream_t, const InstInfo*);
-template void launch_step<float>(const McConst<float>&, const DevTabs<float>&, const QSet<float>&, const int*,
-                                 const QSet<float>&, PQ<float>, PQ<float>, Tal, Ctrs*, int, int, int, cudaStream_t,
-                                 const float*, const Proposer*, const Fork*);
-template void launch_step<double>(const McConst<double>&, const DevTabs<double>&, const QSet<double>&, const int*,
-                                  const QSet<double>&, PQ<double>, PQ<double>, Tal, Ctrs*, int, int, int, cudaStream_t,
-                                  const float*, const Proposer*, const Fork*);
 
 // ---- sampler probe --------------------------------------------------------------------------
 // One call of a per-collision sampler per element, on given energies and
@@ -1940,10 +1971,6 @@ void launch_probe(const McConst<T>& C, const DevTabs<T>& tb, const DevShi<T>& sh
                   const double* E, const double* u, double* out, cudaStream_t s) {
     if (n > 0) k_probe<T><<<(n + 127) / 128, 128, 0, s>>>(C, tb, sh, kind, k, n, E, u, out);
 }
-template void launch_probe<float>(const McConst<float>&, const DevTabs<float>&, const DevShi<float>&, int, int, int,
-                                  const double*, const double*, double*, cudaStream_t);
-template void launch_probe<double>(const McConst<double>&, const DevTabs<double>&, const DevShi<double>&, int, int,
-                                   int, const double*, const double*, double*, cudaStream_t);
 
 // ---- grid hints ----------------------------------------------------------------------------
 // hint of a bucket = the search result at the bucket's lowest value, which
@@ -1974,188 +2001,6 @@ void launch_grid_hints(const McConst<T>& C, GHint<T>* th, GHint<T>* rh, cudaStre
     const int n = C.tg_nb > C.rg_nb ? C.tg_nb : C.rg_nb;
     k_grid_hints<T><<<(n + 127) / 128, 128, 0, s>>>(C.tg, C.Nt, C.tg_inv, th, C.tg_nb, C.Rg, C.NR, C.rg_key0,
                                                     C.rg_nb ? rh : nullptr, C.rg_nb);
-}
-template void launch_grid_hints<float>(const McConst<float>&, GHint<float>*, GHint<float>*, cudaStream_t);
-template void launch_grid_hints<double>(const McConst<double>&, GHint<double>*, GHint<double>*, cudaStream_t);
-
-// ---- finalize: difference arrays -> FP64 tallies -----------------------------------------
-// One thread per (slice, bin): prefix over time rows, in place (exact int64).
-// ---- exact call sums ------------------------------------------------------------------
-__device__ __forceinline__ void add128(unsigned long long* lo, unsigned long long* hi, long long v) {
-    const unsigned long long a = *lo, b = a + (unsigned long long)v;
-    *lo = b;
-    *hi += (v < 0 ? ~0ull : 0ull) + (b < a ? 1ull : 0ull);
-}
-__device__ __forceinline__ void add128(unsigned long long& lo, unsigned long long& hi, unsigned long long vlo,
-                                       unsigned long long vhi) {
-    const unsigned long long b = lo + vlo;
-    hi += vhi + (b < lo ? 1ull : 0ull);
-    lo = b;
-}
-// the 128-bit two's-complement integer (lo, hi) as a double: exactly rounded
-// where it fits in int64, else magnitude hi * 2^64 + lo with two roundings
-__device__ __forceinline__ double i128_to_double(unsigned long long lo, unsigned long long hi) {
-    const long long h = (long long)hi, l = (long long)lo;
-    if ((h == 0 && l >= 0) || (h == -1 && l < 0)) return (double)l;
-    const bool neg = h < 0;
-    if (neg) { lo = ~lo + 1ull; hi = ~hi + (lo == 0 ? 1ull : 0ull); }
-    const double m = (double)hi * 18446744073709551616.0 + (double)lo;
-    return neg ? -m : m;
-}
-
-// One thread per (slice, radius): the running sums over the difference rows
-// (plus the single-row block) give the batch's value at each time, added
-// into the exact sums at the output's index i + Nt (j + NR s).
-__global__ void k_prefix_acc(const unsigned long long* cnt, const unsigned long long* en,
-                             const unsigned long long* ek, int Nt, int NR, int ns, unsigned long long* lo,
-                             unsigned long long* hi, size_t oc, size_t oe, size_t ok) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ns * NR) return;
-    const int s = t / NR, j = t % NR;
-    const size_t blk = (size_t)(Nt + 2) * ns * NR;   // the single-row block follows the difference block
-    long long c = 0, e = 0, k = 0;
-    for (int r = 1; r <= Nt; ++r) {
-        const size_t a = ((size_t)r * ns + s) * NR + j;
-        const size_t o = (size_t)(r - 1) + (size_t)Nt * (j + (size_t)NR * s);
-        c += (long long)cnt[a];
-        e += (long long)en[a];
-        const long long vc = c + (long long)cnt[a + blk], ve = e + (long long)en[a + blk];
-        if (vc) add128(lo + oc + o, hi + oc + o, vc);
-        if (ve) add128(lo + oe + o, hi + oe + o, ve);
-        if (ek) {
-            k += (long long)ek[a];
-            const long long vk = k + (long long)ek[a + blk];
-            if (vk) add128(lo + ok + o, hi + ok + o, vk);
-        }
-    }
-}
-__global__ void k_lat_acc(const unsigned long long* lat, int Nt, int NR, unsigned long long* lo,
-                          unsigned long long* hi) {
-    const size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= (size_t)Nt * NR) return;
-    const int i = (int)(x % Nt), j = (int)(x / Nt);
-    const long long v = (long long)lat[(size_t)i * NR + j];
-    if (v) add128(lo + x, hi + x, v);
-}
-
-void acc_batch(const Tal& tal, int Nt, int NR, int nsh, const Acc& a, cudaStream_t s) {
-    k_prefix_acc<<<(NR + 127) / 128, 128, 0, s>>>(tal.e_cnt, tal.e_E, nullptr, Nt, NR, 1, a.lo, a.hi,
-                                                  a.off(ACC_ECNT), a.off(ACC_EE), 0);
-    k_prefix_acc<<<(NR + 127) / 128, 128, 0, s>>>(tal.p_cnt, tal.p_E, nullptr, Nt, NR, 1, a.lo, a.hi,
-                                                  a.off(ACC_PCNT), a.off(ACC_PE), 0);
-    if (nsh > 0)
-        k_prefix_acc<<<(nsh * NR + 127) / 128, 128, 0, s>>>(tal.h_cnt, tal.h_E, tal.h_Ek, Nt, NR, nsh, a.lo, a.hi,
-                                                            a.off(ACC_HCNT), a.off(ACC_HE), a.off(ACC_HEK));
-    const size_t n = (size_t)Nt * NR;
-    k_lat_acc<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(tal.lat, Nt, NR, a.lo + a.off(ACC_LAT),
-                                                          a.hi + a.off(ACC_LAT));
-}
-
-// One thread per (slice, time): weighted bins and per-time totals of the
-// exact sums (counts x V, energies / 2^24 x V; the totals summed exactly).
-__global__ void k_fin_acc(const unsigned long long* lo, const unsigned long long* hi, size_t oc, size_t oe,
-                          size_t ok, bool has_k, int Nt, int NR, int ns, const double* V, double* on, double* oE,
-                          double* oK, double* tn_, double* tE) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ns * Nt) return;
-    const int s = t / Nt, i = t % Nt;
-    unsigned long long cl = 0, ch = 0, el = 0, eh = 0;
-    for (int j = 0; j < NR; ++j) {
-        const size_t o = (size_t)i + (size_t)Nt * (j + (size_t)NR * s);
-        const unsigned long long c0 = lo[oc + o], c1 = hi[oc + o], e0 = lo[oe + o], e1 = hi[oe + o];
-        if (c0 | c1) on[o] += i128_to_double(c0, c1) * V[j];
-        if (e0 | e1) oE[o] += i128_to_double(e0, e1) / kEScale * V[j];
-        add128(cl, ch, c0, c1);
-        add128(el, eh, e0, e1);
-        if (has_k) {
-            const unsigned long long k0 = lo[ok + o], k1 = hi[ok + o];
-            if (k0 | k1) oK[o] += i128_to_double(k0, k1) / kEScale * V[j];
-            add128(el, eh, k0, k1);
-        }
-    }
-    if (tn_) tn_[i + (size_t)Nt * s] += i128_to_double(cl, ch);
-    if (tE) tE[i + (size_t)Nt * s] += i128_to_double(el, eh) / kEScale;
-}
-__global__ void k_fin_lat_acc(const unsigned long long* lo, const unsigned long long* hi, int Nt, int NR,
-                              const double* V, double* oL, unsigned long long* rows) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= Nt) return;
-    unsigned long long sl = 0, sh = 0;
-    for (int j = 0; j < NR; ++j) {
-        const size_t o = (size_t)t + (size_t)Nt * j;
-        const unsigned long long v0 = lo[o], v1 = hi[o];
-        if (v0 | v1) oL[o] += i128_to_double(v0, v1) / kLatScale * V[j];
-        add128(sl, sh, v0, v1);
-    }
-    rows[2 * (size_t)t] = sl;
-    rows[2 * (size_t)t + 1] = sh;
-}
-__global__ void k_fin_lat_scan(const unsigned long long* rows, int Nt, double* Eat) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    unsigned long long cl = 0, ch = 0;
-    for (int i = 0; i < Nt; ++i) {
-        add128(cl, ch, rows[2 * (size_t)i], rows[2 * (size_t)i + 1]);
-        Eat[i] += i128_to_double(cl, ch) / kLatScale;
-    }
-}
-
-void acc_finish(const Acc& a, int Nt, int NR, int nsh, const double* V, const FinOut& o, unsigned long long* rows,
-                cudaStream_t s) {
-    k_fin_acc<<<(Nt + 127) / 128, 128, 0, s>>>(a.lo, a.hi, a.off(ACC_ECNT), a.off(ACC_EE), 0, false, Nt, NR, 1, V,
-                                               o.ne, o.Ee, nullptr, o.totNe, o.E_e);
-    k_fin_acc<<<(Nt + 127) / 128, 128, 0, s>>>(a.lo, a.hi, a.off(ACC_PCNT), a.off(ACC_PE), 0, false, Nt, NR, 1, V,
-                                               o.np, o.Ep, nullptr, o.totNp, o.E_p);
-    if (nsh > 0)
-        k_fin_acc<<<(nsh * Nt + 127) / 128, 128, 0, s>>>(a.lo, a.hi, a.off(ACC_HCNT), a.off(ACC_HE), a.off(ACC_HEK),
-                                                         true, Nt, NR, nsh, V, o.hn, o.hE, o.hK, o.htn, o.htE);
-    k_fin_lat_acc<<<(Nt + 127) / 128, 128, 0, s>>>(a.lo + a.off(ACC_LAT), a.hi + a.off(ACC_LAT), Nt, NR, V, o.lat,
-                                                   rows);
-    k_fin_lat_scan<<<1, 32, 0, s>>>(rows, Nt, o.E_at);
-}
-// Spectra: one thread per (iteration, column) turns the difference rows into
-// per-time counts in place; then one thread per (time, bin) adds, over the
-// iterations in order, count / (particles of that iteration at that time).
-__global__ void k_spec_prefix(int* sp, int nit, int Nt, size_t row, size_t per_it) {
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (size_t)nit * row) return;
-    int* b = sp + (t / row) * per_it + t % row;
-    int c = 0;
-    for (int r = 1; r <= Nt; ++r) { c += b[(size_t)r * row]; b[(size_t)r * row] = c; }
-}
-__global__ void k_spec_fin(const int* sp, int nit, int Nt, int nE, int nD, size_t row, size_t per_it,
-                           const double* wE, const double* wD, double* oEe, double* oEh, double* oth, double* othh) {
-    const int nb = nE + nD + 2 * kNTheta;
-    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (size_t)Nt * nb) return;
-    const int i = (int)(t / nb), b = (int)(t % nb);   // time row i+1, column b
-    int col, ncol;
-    double* out;
-    size_t o;
-    double w = 1.0;
-    if (b < nE) { col = sp_eE() + b; ncol = sp_ne(); out = oEe; o = i + (size_t)Nt * b; }
-    else if (b < nE + kNTheta) { const int k = b - nE; col = sp_eth(nE) + k; ncol = sp_ne(); out = oth; o = i + (size_t)(Nt + 1) * k; }
-    else if (b < nE + kNTheta + nD) { const int k = b - nE - kNTheta; col = sp_hE(nE) + k; ncol = sp_nh(nE); out = oEh; o = i + (size_t)Nt * k; }
-    else { const int k = b - nE - kNTheta - nD; col = sp_hth(nE, nD) + k; ncol = sp_nh(nE); out = othh; o = i + (size_t)(Nt + 1) * k; }
-    if (!out) return;
-    if (b < nE) w = wE[b];
-    else if (b >= nE + kNTheta && b < nE + kNTheta + nD) w = wD[b - nE - kNTheta];
-    const size_t r = (size_t)(i + 1) * row;
-    double acc = 0.0;
-    for (int it = 0; it < nit; ++it) {
-        const int* p = sp + (size_t)it * per_it + r;
-        const int n = p[ncol], c = p[col];
-        if (n > 0 && c != 0) acc += (double)c / (double)n;
-    }
-    if (acc != 0.0) out[o] += acc / w;
-}
-
-void fin_spectra(const Tal& tal, int nit, int Nt, const double* wE, const double* wD, double* oEe, double* oEh,
-                 double* oth, double* othh, cudaStream_t s) {
-    const size_t n1 = (size_t)nit * tal.sp_row;
-    k_spec_prefix<<<(unsigned)((n1 + 127) / 128), 128, 0, s>>>(tal.spec, nit, Nt, tal.sp_row, tal.sp_it);
-    const size_t n2 = (size_t)Nt * (tal.sp_nE + tal.sp_nD + 2 * kNTheta);
-    k_spec_fin<<<(unsigned)((n2 + 127) / 128), 128, 0, s>>>(tal.spec, nit, Nt, tal.sp_nE, tal.sp_nD, tal.sp_row,
-                                                           tal.sp_it, wE, wD, oEe, oEh, oth, othh);
 }
 
 }  // namespace tk

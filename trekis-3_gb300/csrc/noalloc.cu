@@ -114,12 +114,13 @@ size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
     L.hmap = c.take<int>((size_t)s.nsh);
     const size_t rows = (size_t)s.Nt + 2;
     const size_t n_e = rows * s.NR, n_h = rows * s.nsh * s.NR, n_l = (size_t)s.Nt * s.NR;
-    L.n_all = 2 * (4 * n_e + 3 * n_h) + n_l;   // difference + single-row blocks, lattice
+    L.n_all = 2 * (4 * n_e + 3 * n_h) + n_l + 2 * rows;   // difference + single-row blocks, lattice, emission
     L.tall = c.take<unsigned long long>(L.n_all);
     if (L.tall) {
         Tal& t = L.tal;
         t.e_cnt = L.tall; t.e_E = L.tall + 2 * n_e; t.p_cnt = L.tall + 4 * n_e; t.p_E = L.tall + 6 * n_e;
         t.h_cnt = L.tall + 8 * n_e; t.h_E = t.h_cnt + 2 * n_h; t.h_Ek = t.h_E + 2 * n_h; t.lat = t.h_Ek + 2 * n_h;
+        t.em = t.lat + n_l;
         t.spec = nullptr; t.sp_nE = 0; t.sp_nD = 0; t.sp_row = 0; t.sp_it = 0;   // no spectra on this path
     }
     const size_t blk = (size_t)s.Nt * s.NR * s.nsh;
@@ -134,6 +135,7 @@ size_t lay_out(Carve& c, const Shape& s, int64_t cap, Layout<T>& L) {
     L.lat_rows = c.take<unsigned long long>(2 * (size_t)s.Nt);
     L.acc.n2 = (size_t)s.Nt * s.NR;
     L.acc.nh = (size_t)s.Nt * s.NR * s.nsh;
+    L.acc.nt = (size_t)s.Nt;
     L.acc.lo = c.take<unsigned long long>(L.acc.n());
     L.acc.hi = c.take<unsigned long long>(L.acc.n());
     for (QSet<T>* q : {&L.qa, &L.qb}) {
@@ -278,6 +280,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     C.tg = L.tg; C.Rg = L.Rg;
     C.dosE = tb.dosE; C.nD = tb.nD;
     C.elast_model = elastic_model_of(t->mat, tb);
+    if (!C.emit) L.tal.em = nullptr;   // no emission tallies to make
     {
         T first = T(0), last = T(0);
         walk_time_grid(cfg.Tim, cfg.dt, cfg.dt_flag, [&](int i, double x) { if (i == 0) first = (T)x; last = (T)x; });
@@ -347,7 +350,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
         err_bits |= hc.err_bits;
         peak_all = std::max<uint64_t>(peak_all, (uint64_t)peak);
         acc_batch(L.tal, Nt, NR, nsh, L.acc, strm);
-        launches += 4;
+        launches += L.tal.em ? 5 : 4;
         NA_CK(cudaGetLastError());
         done += nb;
         if (tune_batch && peak > 0) B = std::max(1, std::min<int>((int)(0.5 * cap / ((double)peak / nb)), 1 << 16));
@@ -355,9 +358,10 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
     // the FP64 tallies of the call's exact sums
     {
         const FinOut fo{o.Out_ne, o.Out_Ee, o.Out_tot_Ne, Ee_call, o.Out_nphot, o.Out_Ephot, o.Out_tot_Nphot, Ep_call,
-                        L.hn, L.hE, L.hK, L.htn, L.htE, o.Out_Elat, Eat_call};
+                        L.hn, L.hE, L.hK, L.htn, L.htE, o.Out_Elat, Eat_call,
+                        C.emit ? o.Out_Ne_Em : nullptr, C.emit ? o.Out_E_Em : nullptr};
         acc_finish(L.acc, Nt, NR, nsh, L.V, fo, L.lat_rows, strm);
-        launches += 5;
+        launches += (fo.emN || fo.emE) ? 6 : 5;
     }
     // holes: compact shells -> caller slices; per-call energies -> caller totals
     const size_t blk = (size_t)Nt * NR, nn = blk * nsh, n3 = (size_t)Nt * o.Nat * o.Nshl;
@@ -404,7 +408,6 @@ int check_args(const trekis_tables* t, const trekis_material* mat, const trekis_
     if (!t || !cfg || !o || !mat) { set_error("null argument"); return TREKIS_EINVAL; }
     if (!t->has_shi) { set_error("tables were built without the SHI part"); return TREKIS_EINVAL; }
     if (t->mat.include_photons && !t->has_phot) { set_error("photon tables missing"); return TREKIS_EINVAL; }
-    if (t->mat.work_function > 0.0) { set_error("surface emission is not supported"); return TREKIS_EUNSUPPORTED; }
     if (t->ion.Kind_ion != 0) { set_error("Brandt-Kitagawa ions are not supported"); return TREKIS_EUNSUPPORTED; }
     if (cfg->NMC < 0 || cfg->N_R < 1 || !cfg->Out_R || !(cfg->Tim > 0) || !(cfg->dt > 0)) {
         set_error("invalid run configuration"); return TREKIS_EINVAL;
@@ -426,7 +429,8 @@ int check_args(const trekis_tables* t, const trekis_material* mat, const trekis_
         return TREKIS_EUNSUPPORTED;
     }
     if (cfg->use_graph != 0) { set_error("graph capture of the wavefront loop is not built (use_graph must be 0)"); return TREKIS_EUNSUPPORTED; }
-    if (o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h) {
+    if (o->Out_Ee_vs_E || o->Out_Eh_vs_E || o->Out_theta || o->Out_theta_h ||
+        (t->mat.work_function > 0.0 && o->Out_Ee_vs_E_Em)) {
         set_error("spectra are not tallied by the no-alloc entry point (their per-iteration histograms would not fit)");
         return TREKIS_EUNSUPPORTED;
     }

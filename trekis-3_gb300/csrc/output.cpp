@@ -21,10 +21,12 @@
 // VB_holes_distribution_vs_E, Radial_Lattice_energy, Radial_Track_energy,
 // Radial_Lattice_temperature, and per shell the holes' density, energy
 // (valence band: potential and kinetic) and the valence holes' temperature.
+// With surface emission also Emitted_electron_distribution_vs_E and the
+// emission columns of Total_numbers.txt.
 // Not written: the copy of the input file (there is none at this boundary),
-// the electric-field and emission files (no fields, no emission on this
-// path) and Hole_mean_diffusion_coefficient.txt (not computed: the
-// reference's value depends on its OpenMP schedule).
+// the electric-field files (no fields on this path) and
+// Hole_mean_diffusion_coefficient.txt (not computed: the reference's value
+// depends on its OpenMP schedule).
 //
 // Also here: the SHI table files of Analytical_ion_dEdx (IMFP and dE/dx per
 // shell, the ion's effective charge, its stopping power and range) written
@@ -157,8 +159,9 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
         for (int s = 0; s < m->atoms[a].N_shl; ++s)
             if (!oc->shell_names[a][s]) { tk::set_error("missing shell name"); return TREKIS_EINVAL; }
     }
-    const double inv = 1.0 / (double)oc->NMC;
+    const double nmc = (double)oc->NMC;   // every sum is divided by NMC (Universal_MC_for_SHI_MAIN.f90:281-304)
     const bool photons = m->include_photons != 0;
+    const bool emission = m->work_function > 0.0;
     auto need = [&](const double* p, const char* what) {
         if (!p) tk::set_error(std::string("tally array missing: ") + what);
         return p != nullptr;
@@ -188,9 +191,9 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
 
     const std::vector<double> tg = out_times(cfg->Tim, cfg->dt, cfg->dt_flag, N);
     const double* R = cfg->Out_R;
-    auto at2 = [&](const double* a, int k, int i) { return a[(size_t)k + (size_t)N * i] * inv; };
+    auto at2 = [&](const double* a, int k, int i) { return a[(size_t)k + (size_t)N * i] / nmc; };
     auto at4 = [&](const double* a, int k, int i, int at, int s) {
-        return a[(size_t)k + (size_t)N * ((size_t)i + (size_t)NR * ((size_t)at + (size_t)Nat * s))] * inv;
+        return a[(size_t)k + (size_t)N * ((size_t)i + (size_t)NR * ((size_t)at + (size_t)Nat * s))] / nmc;
     };
     auto time_header = [&](Out& o, const char* first) {
         o.put(first);
@@ -245,9 +248,16 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
                   " formula, point-like charge model for SHI.\n");
         o.put(std::string(" Elastic scattering: ") +
               (m->kind_of_EMFP == 1 ? "phonon CDF" : m->kind_of_EMFP == 2 ? "DSF" : "Mott atomic cross sections") + "\n");
+        if (emission) {   // :235-244
+            o.put(" Electron emission included. Work function = " + trim(f_fmt(m->work_function, 12, 3)) + " [eV]\n");
+            o.put(" Potential barrier length = " + trim(f_fmt(m->bar_length, 12, 3)) + " [A] Barrier height = " +
+                  trim(f_fmt(m->bar_height, 12, 3)) + " [eV]\n");
+        } else {
+            o.put(" Electron emission is excluded\n");
+        }
         o.put(" Number of MC iterations: " + std::to_string(oc->NMC) + "\n");
         if (oc->ion_Zeff >= 0) o.put(" Ion equilibrium charge:         " + trim(f_fmt(oc->ion_Zeff, 6, 3)) + " [electron charge]\n");
-        o.put(" MC calculated energy loss (Se): " + trim(f_fmt(t->Out_tot_E[N - 1] * inv / m->Layer, 9, 2)) + " [eV/A]\n");
+        o.put(" MC calculated energy loss (Se): " + trim(f_fmt(t->Out_tot_E[N - 1] / nmc / m->Layer, 9, 2)) + " [eV/A]\n");
         if (oc->duration_s >= 0) o.put(" Duration of calculation:        " + trim(f_fmt(oc->duration_s, 12, 3)) + " [sec]\n");
         ok = ok && o.ok;
     }
@@ -258,7 +268,7 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
         time_header(o, first);
         for (int i = 0; i < 180; ++i) {
             o.put(e_fmt((double)(i + 1)));
-            for (int k = 0; k < N; ++k) o.put(e_fmt(a ? a[(size_t)k + (size_t)(N + 1) * i] * inv : 0.0));
+            for (int k = 0; k < N; ++k) o.put(e_fmt(a ? a[(size_t)k + (size_t)(N + 1) * i] / nmc : 0.0));
             o.put(" \n");
         }
         ok = ok && o.ok;
@@ -266,14 +276,17 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
     theta("Electrons_theta_distribution.txt", "#Angle[deg] ", t->Out_theta);
     theta("VB_holes_theta_distribution.txt", "Angle[deg] ", t->Out_theta_h);
 
-    // Total_numbers.txt (:625-647): no emission on this path, so Ne_Emitted and Energy_Emitted are 0
+    // Total_numbers.txt (:625-647); the emission columns are 0 without emission
     {
         Out o(dir + "/Total_numbers.txt");
         o.put(photons ? "#Time[fs]    Ne    Ne_Emitted    Energy[eV]     Energy_Emitted[eV] N_photons\n"
                       : "#Time[fs]    Ne    Ne_Emitted    Energy[eV]     Energy_Emitted[eV]\n");
+        const double* nem = emission ? t->Out_Ne_Em : nullptr;
+        const double* eem = emission ? t->Out_E_Em : nullptr;
         for (int k = 0; k < N; ++k) {
-            o.put(e_fmt(tg[k]) + e_fmt(t->Out_tot_Ne[k] * inv) + e_fmt(0.0) + e_fmt(t->Out_tot_E[k] * inv) + e_fmt(0.0));
-            if (photons) o.put(e_fmt(t->Out_tot_Nphot[k] * inv));
+            o.put(e_fmt(tg[k]) + e_fmt(t->Out_tot_Ne[k] / nmc) + e_fmt(nem ? nem[k] / nmc : 0.0) +
+                  e_fmt(t->Out_tot_E[k] / nmc) + e_fmt(eem ? eem[k] / nmc : 0.0));
+            if (photons) o.put(e_fmt(t->Out_tot_Nphot[k] / nmc));
             o.put("\n");
         }
         ok = ok && o.ok;
@@ -288,11 +301,11 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
             for (int s = 0; s < m->atoms[a].N_shl; ++s) o.put(shell_label(a, s) + "[eV]    ");
         o.put(" \n");
         for (int k = 0; k < N; ++k) {
-            o.put(e_fmt(tg[k]) + e_fmt(t->Out_E_e[k] * inv) + e_fmt(t->Out_E_at[k] * inv) + e_fmt(0.0));
-            if (photons) o.put(e_fmt(t->Out_E_phot[k] * inv));
+            o.put(e_fmt(tg[k]) + e_fmt(t->Out_E_e[k] / nmc) + e_fmt(t->Out_E_at[k] / nmc) + e_fmt(0.0));
+            if (photons) o.put(e_fmt(t->Out_E_phot[k] / nmc));
             for (int a = 0; a < Nat; ++a)
                 for (int s = 0; s < m->atoms[a].N_shl; ++s)
-                    o.put(e_fmt(t->Out_E_h[(size_t)k + (size_t)N * ((size_t)a + (size_t)Nat * s)] * inv));
+                    o.put(e_fmt(t->Out_E_h[(size_t)k + (size_t)N * ((size_t)a + (size_t)Nat * s)] / nmc));
             o.put(" \n");
         }
         ok = ok && o.ok;
@@ -331,6 +344,18 @@ extern "C" int32_t trekis_save_output(const trekis_output_cfg* oc, const trekis_
             o.put(f_fmt(m->dos_E[i], 9, 1));
             for (int k = 0; k < N; ++k)
                 o.put(e_fmt(t->Out_Eh_vs_E && t->N_dos == m->N_dos ? at2(t->Out_Eh_vs_E, k, i) : 0.0));
+            o.put(" \n");
+        }
+        ok = ok && o.ok;
+    }
+    // emitted electrons' spectrum (:591-615), with emission only: energies
+    // Out_R / 10 in the first column
+    if (emission) {
+        Out o(dir + "/Emitted_electron_distribution_vs_E[1_eV].txt");
+        time_header(o, "#Energy[eV] ");
+        for (int i = 0; i < NR; ++i) {
+            o.put(f_fmt(R[i] / 10.0, 9, 1));
+            for (int k = 0; k < N; ++k) o.put(e_fmt(t->Out_Ee_vs_E_Em ? at2(t->Out_Ee_vs_E_Em, k, i) : 0.0));
             o.put(" \n");
         }
         ok = ok && o.ok;

@@ -30,7 +30,7 @@ ERR_BITS = {
     1 << 6: "queue full", 1 << 7: "photon negative energy",
 }
 
-ABI_VERSION = 7   # TREKIS_ABI_VERSION of the header these structs mirror
+ABI_VERSION = 8   # TREKIS_ABI_VERSION of the header these structs mirror
 
 _S = MAX_SHELLS
 _O = MAX_OSC
@@ -143,7 +143,8 @@ class Tallies(C.Structure):
             "Out_ne", "Out_Ee", "Out_nphot", "Out_Ephot", "Out_Elat", "Out_nh", "Out_Eh", "Out_Ehkin",
             "Out_tot_Ne", "Out_tot_Nphot", "Out_tot_E", "Out_E_e", "Out_E_phot", "Out_E_at", "Out_E_h")
     ] + [("N_dos", C.c_int32), ("pad_", C.c_int32)] + [
-        (n, _DP) for n in ("Out_Ee_vs_E", "Out_Eh_vs_E", "Out_theta", "Out_theta_h")
+        (n, _DP) for n in ("Out_Ee_vs_E", "Out_Eh_vs_E", "Out_theta", "Out_theta_h",
+                           "Out_Ne_Em", "Out_E_Em", "Out_Ee_vs_E_Em")
     ]
 
 

@@ -48,15 +48,18 @@ def n_time_points(Tim, dt, dt_flag=0):
     return out
 
 
-SPECTRA = ("Out_Ee_vs_E", "Out_Eh_vs_E", "Out_theta", "Out_theta_h")
+SPECTRA = ("Out_Ee_vs_E", "Out_Eh_vs_E", "Out_theta", "Out_theta_h", "Out_Ee_vs_E_Em")
+EMISSION = ("Out_Ne_Em", "Out_E_Em")   # emitted electrons and their energy outside, per time
 N_THETA = 180   # 1-degree bins of Out_theta (Sorting_output_data.f90:1191-1196)
 
 
 class TallySet:
     """Caller-owned tally arrays (numpy, float64), Fortran layout.  With
-    ``spectra`` the four spectra of Calculated_statistics are tallied too."""
+    ``spectra`` the spectra of Calculated_statistics are tallied too; with
+    ``emission`` the surface-emission tallies (and, with ``spectra``, the
+    emitted electrons' spectrum)."""
 
-    def __init__(self, Nt, NR, Nat, Nshl, N_dos=0, spectra=False):
+    def __init__(self, Nt, NR, Nat, Nshl, N_dos=0, spectra=False, emission=False):
         self.Nt, self.NR, self.Nat, self.Nshl, self.N_dos = Nt, NR, Nat, Nshl, N_dos
         self.a = {}
         for k in TALLY_2D:
@@ -71,6 +74,11 @@ class TallySet:
             self.a["Out_Eh_vs_E"] = np.zeros(Nt * N_dos)
             self.a["Out_theta"] = np.zeros((Nt + 1) * N_THETA)
             self.a["Out_theta_h"] = np.zeros((Nt + 1) * N_THETA)
+        if emission:
+            for k in EMISSION:
+                self.a[k] = np.zeros(Nt)
+            if spectra:
+                self.a["Out_Ee_vs_E_Em"] = np.zeros(Nt * NR)
 
     def c(self):
         return abi.Tallies(Nt=self.Nt, N_R=self.NR, Nat=self.Nat, Nshl=self.Nshl, N_dos=self.N_dos,
@@ -78,7 +86,7 @@ class TallySet:
 
     def view(self, name):
         v = self.a[name]
-        if name in TALLY_2D or name == "Out_Ee_vs_E":
+        if name in TALLY_2D or name in ("Out_Ee_vs_E", "Out_Ee_vs_E_Em"):
             return v.reshape(self.NR, self.Nt).T          # [t, R]
         if name in TALLY_4D:
             return v.reshape(self.Nshl, self.Nat, self.NR, self.Nt).transpose(3, 2, 1, 0)  # [t, R, atom, shell]
@@ -198,7 +206,8 @@ def new_tallies(w, spectra=False):
     Nt = len(n_time_points(w.Tim, w.dt, w.dt_flag))
     m = w.material
     nd = len(m.dos.E) if m.dos is not None else 0
-    return TallySet(Nt, len(w.R_edges), len(m.atoms), m.n_shells_max, N_dos=nd, spectra=spectra)
+    return TallySet(Nt, len(w.R_edges), len(m.atoms), m.n_shells_max, N_dos=nd, spectra=spectra,
+                    emission=m.work_function > 0.0)
 
 
 def mc_run(tables, opt=None, NMC=None, tallies=None):

@@ -22,7 +22,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-r
 # The track-loop kernels: single-precision division and square root to about
 # one ulp and FP32 denormals flushed.  These flags touch only FP32 arithmetic,
 # so FP64 runs keep IEEE division and square root (and their oracle parity).
-PER_FILE_FLAGS = {"mc": ["--prec-div=false", "--prec-sqrt=false", "--ftz=true"],
+_FAST32 = ["--prec-div=false", "--prec-sqrt=false", "--ftz=true"]
+PER_FILE_FLAGS = {"mc_f32": _FAST32, "mc_f64": _FAST32, "mc_tally": _FAST32,
                   # host-only output code: no fused multiply-add, so sums print the same on every host
                   "output": ["-Xcompiler", "-ffp-contract=off"]}
 
