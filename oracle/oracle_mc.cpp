@@ -240,10 +240,12 @@ void cut_h(Ctx& c, H& p) { if (p.Mass < 1e15 && p.Ehkin < c.m->cut_off) p.tn = 1
 // calculate_emission (Monte_Carlo.f90:2477-2513), after the collision that
 // left the electron at Z < 0: it escapes when E >= 1.5 bar_height, else with
 // the penetrability 1/(1 + exp(gamma (E1 - E))) of the barrier when
-// E - work_function > 0 (one uniform drawn); an escaped electron collides no
-// more (tn = L = 1e30) but keeps its energy and flight.  Otherwise a flight
-// away from the target (cos theta < 0) is turned back.
-void emission(Ctx& c, P& p, Stream& s) {
+// E - work_function > 0; an escaped electron collides no more (tn = L =
+// 1e30) but keeps its energy and flight.  Otherwise a flight away from the
+// target (cos theta < 0) is turned back.  The uniform is the first word of
+// block 2^32 - 1 of the event's stream (pid, ord), which its sequential
+// draws never reach.
+void emission(Ctx& c, P& p, uint64_t pid, uint32_t ord) {
     const trekis_material& m = *c.m;
     if (!(p.Z < 0.0)) return;
     bool out;
@@ -252,7 +254,9 @@ void emission(Ctx& c, P& p, Stream& s) {
         out = true;
         Ek = p.E - m.work_function;
     } else {
-        const double RN = s.next();
+        Stream es(c.seed, pid, ord);
+        es.ctr[3] = 0xFFFFFFFFu;
+        const double RN = es.next();
         const double pen = 1.0 / (1.0 + std::exp(c.em_gamma * (c.em_E1 - p.E)));
         Ek = p.E - m.work_function;
         out = (Ek > 0.0) && (RN < pen);
@@ -609,7 +613,7 @@ void electron_event(Ctx& c, int NOP, int i) {
     p.E = Eel - dE; p.t0 = tev; p.X = X; p.Y = Y; p.Z = Z; p.L = Mt; p.theta = th1; p.phi = ph1;
     p.tn = tn_of(p.t0, Mt, v_electron(p.E));
     cut_e(c, p);
-    if (c.emit) emission(c, p, s);
+    if (c.emit) emission(c, p, pid, ord);
     if (p.E < -1.0e-9 || std::isnan(p.E)) c.err |= TREKIS_ERR_NEG_ENERGY_E;
 }
 
