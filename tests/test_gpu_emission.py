@@ -8,7 +8,8 @@ are tallied per grid time (Out_Ne_Em, Out_E_Em, :958-959) and as a spectrum
 normalised per iteration (Out_Ee_vs_E_Em, :1100-1109).
 
 * FP64 mode on identical tables and Philox streams: every tally, the
-  emission tallies and the spectra included, equals the oracle's.
+  emission tallies and the spectra included, equals the oracle's (to the
+  2^-24 eV fixed-point resolution of the energy sums).
 * Emission tallies go through the exact integer sums: a split of the
   iterations into exact words and the scheduling knobs change no bit.
 * FP32 mode: the emitted electrons per iteration and their energy agree
@@ -68,7 +69,10 @@ def test_fp64_emission_matches_oracle(small_em):
     assert set(g.a) == set(r.a) and "Out_Ee_vs_E_Em" in g.a
     for k in g.a:
         a, b = g[k], r[k]
-        tol = 1e-9 * np.abs(b) + 1e-12 * (np.max(np.abs(b)) + 1e-300)
+        if k in api.SPECTRA:   # FP64 sums of per-iteration fractions
+            tol = 1e-9 * np.abs(b) + 1e-12 * (np.max(np.abs(b)) + 1e-300)
+        else:                  # integer sums of 2^-24 eV fixed-point energies
+            tol = 1e-6 * np.abs(b) + 1e-9 * (np.max(np.abs(b)) + 1e-300)
         bad = np.abs(a - b) > tol
         assert not np.any(bad), f"{k}: {np.sum(bad)} cells differ, max {np.max(np.abs(a - b)):.3e}"
     ne = g["Out_Ne_Em"]
