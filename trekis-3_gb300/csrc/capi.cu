@@ -307,9 +307,24 @@ static int upload_shi(trekis_tables* t, DevShi<T>& s) {
             }
         }
         s.bkt = upload_i(b, h);
+        std::vector<double> sc(nsh, 0.0);   // 0: the draw divides (a row without hints)
+        for (int k = 0; k < nsh; ++k)
+            if (ib[k] > ia[k] && ia[k] > 0.0) sc[k] = (double)kShiBuckets / (ib[k] - ia[k]);
+        s.bkt_scale = upload<T>(b, sc);
+    }
+    {   // log-log slopes of the brackets, in T, as the draw would form them
+        std::vector<T> lE(dE.size()), lI(dI.size());
+        for (size_t i = 0; i < dE.size(); ++i) { lE[i] = (T)std::log(dE[i]); lI[i] = (T)std::log(dI[i]); }
+        std::vector<double> sl(dE.size(), 0.0);
+        for (int k = 0; k < nsh; ++k)
+            for (int i = off[k] + 1; i < off[k + 1]; ++i) sl[i] = (double)((lE[i] - lE[i - 1]) / (lI[i] - lI[i - 1]));
+        s.dS = upload<T>(b, sl);
     }
     s.pow_zp = (T)std::pow((double)t->ion.Zat, 0.66666666);
-    if (!s.sE || !s.sL || !s.pL || !s.d_off || !s.dE || !s.Mt || !s.bkt) { set_error("SHI table upload failed"); return TREKIS_ENOMEM; }
+    if (!s.sE || !s.sL || !s.pL || !s.d_off || !s.dE || !s.Mt || !s.bkt || !s.bkt_scale || !s.dS) {
+        set_error("SHI table upload failed");
+        return TREKIS_ENOMEM;
+    }
     // rows at every SHI grid energy of the window
     s.nW = (int)t->shi_row_nodes.size();
     s.w0 = s.nW ? t->shi_row_nodes[0] : 0;

@@ -137,6 +137,9 @@ struct DevShi {
     // with 1/L >= a + (b - a) q / kShiBuckets (-1 for a row that is not
     // monotone, which is bisected)
     const int* bkt;
+    const T* bkt_scale;                // [nsh] kShiBuckets / (b - a): a row's bucket of Tot is (Tot - a) x this
+    const T* dS;                       // log-log slope of each bracket of the rows, at its upper node
+                                       // ((ldE[i] - ldE[i-1]) / (ldI[i] - ldI[i-1]), made once)
     T pow_zp;                          // Z_ion^0.66666666
     // transfer rows at the SHI grid energies w0 .. w0 + nW - 1 (trekis_table_cfg.
     // shi_rows_by_energy; nW = 0: the rows above, at the initial energy, serve

@@ -994,7 +994,7 @@ __device__ __forceinline__ T shi_path(const DevShi<T>& sh, int nb, T E, T lx) {
 // first node with 1/L >= Tot)
 template <class T>
 __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* lDI, int N, int Mt, T a, T b, T Ip,
-                               T RN, const int* bkt = nullptr) {
+                               T RN, const int* bkt = nullptr, T scale = T(0), const T* S = nullptr) {
     if (N < 1) return (double)Ip;
     const T Tot = (a > T(0) && b > T(0)) ? a + RN * (b - a) : T(1.5e21);
     int nt;
@@ -1004,7 +1004,7 @@ __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* 
             // the bound lies in [bkt[q], bkt[q+1]] for Tot in bucket q (both
             // ends checked, for the rounding of Tot): bisect that range only,
             // so no lane of a warp walks far
-            const T u = (Tot - a) / (b - a) * T(kShiBuckets);
+            const T u = scale > T(0) ? (Tot - a) * scale : (Tot - a) / (b - a) * T(kShiBuckets);
             const int q = !(u >= T(0)) ? 0 : (u >= T(kShiBuckets) ? kShiBuckets - 1 : (int)u);
             const int l = bkt[q], h = bkt[q + 1];
             if ((l == 0 || DI[l - 1] < Tot) && (h == N - 1 || DI[h] >= Tot)) { lo = l; hi = h; }
@@ -1017,7 +1017,10 @@ __device__ double shi_row_draw(const T* DE, const T* lDE, const T* DI, const T* 
     T r;
     if (m_abs(E2 - E1) < T(1.0e-6)) r = DE[nt - 2] > DE[nt - 1] ? DE[nt - 2] : DE[nt - 1];
     else if (Tot == E1) r = DE[nt - 2];
-    else r = m_exp(lDE[nt - 2] + (lDE[nt - 1] - lDE[nt - 2]) / (lDI[nt - 1] - lDI[nt - 2]) * (m_log(Tot) - lDI[nt - 2]));
+    else {   // the slope made once per bracket (S) equals the one formed here, bit for bit
+        const T sl = S ? S[nt - 1] : (lDE[nt - 1] - lDE[nt - 2]) / (lDI[nt - 1] - lDI[nt - 2]);
+        r = m_exp(lDE[nt - 2] + sl * (m_log(Tot) - lDI[nt - 2]));
+    }
     return (double)r;
 }
 
@@ -1030,7 +1033,8 @@ __device__ double shi_transfer(const DevShi<T>& sh, int k, T Ip, T E, T RN) {
         const int o0 = sh.d_off[k];
         return shi_row_draw(sh.dE + o0, sh.ldE + o0, sh.dI + o0, sh.ldI + o0, sh.d_off[k + 1] - o0, sh.Mt[k],
                             sh.invdL_ip[k], sh.invL_last[k], Ip, RN,
-                            sh.bkt ? sh.bkt + (size_t)k * (kShiBuckets + 1) : nullptr);
+                            sh.bkt ? sh.bkt + (size_t)k * (kShiBuckets + 1) : nullptr,
+                            sh.bkt_scale ? sh.bkt_scale[k] : T(0), sh.dS ? sh.dS + o0 : nullptr);
     }
     int iE = find_monoton(sh.sE, sh.nS, E);
     if (iE > 1 && m_abs(sh.sE[iE - 2] - E) < T(1.0e-6)) iE -= 1;
@@ -1075,22 +1079,44 @@ struct ShiEv {  // one SHI collision: the ion state after it and the transfer
     int pad;
 };
 
-// The ion of each iteration, one thread each: Which_shell, SHI_energy_transfer,
-// next free path and the charge update (SHI_Monte_Carlo, MC:2153-2196).  The
+// The ion of each iteration: Which_shell, SHI_energy_transfer, next free
+// path and the charge update (SHI_Monte_Carlo, MC:2153-2196), one group of G
+// lanes per track (G a power of two, 32 / G tracks per warp).  A track's
+// collisions form one dependent chain; the group shortens it: lane j computes
+// the 1/MFP of shells j, j + G, ... (the sums over shells are then taken in
+// shell order, as one thread takes them) and holds the Philox block of
+// collision ord + j, G collisions ahead.  The leader (lane 0 of the group)
+// alone does the rest -- the FP64 transfer draw, the flight, the charge, the
+// record -- and hands the ion's energy and next time to its group, so the
+// narrow FP64 pipe sees one lane per track.  shi_group_lanes sizes G.  The
 // energy, depth and time accumulate in FP64; the table arithmetic is in T.
 // In FP32 mode the velocity, flight time and Bohr charge are FP32 too (a
 // serial FP64 chain is slow on this part); FP64 mode keeps the reference's
-// expressions.  Record slots are reserved kSlotChunk at a time; slots a
-// thread leaves unused are marked it = -1 and skipped by the pair kernel.
+// expressions.  Record slots are reserved kSlotChunk at a time; slots a track
+// leaves unused are marked it = -1 and skipped by the pair kernel.
 constexpr int kSlotChunk = 32;
+constexpr int kShiPerLane = 8;            // shells per lane at most
+constexpr unsigned kFullWarp = 0xffffffffu;
+
+// G: enough lanes for kShiPerLane shells each, more while the tracks' warps
+// stay within about two per SM (the leaders' FP64 draws then stay below the
+// chain's latency), never more lanes than shells or 32
+inline int shi_group_lanes(int n_tracks, int nsh) {
+    int g = 1;
+    while (g * kShiPerLane < nsh) g *= 2;
+    while (g < 32 && g < nsh && (int64_t)n_tracks * (2 * g) <= 2 * 32 * 152) g *= 2;
+    return g;
+}
 
 template <class T>
-__global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McConst<T> C, const __grid_constant__ DevShi<T> sh,
-                                                  ShiEv* __restrict__ evs, int64_t cap_ev, Ctrs* ctr, int nit,
-                                                  int it_base, unsigned long long* ev_inst) {
-    const int local = blockIdx.x * blockDim.x + threadIdx.x;
-    if (local >= nit) return;
-    const int it = it_base + local;   // the iteration's index in the batch
+__global__ void __launch_bounds__(128)
+    k_shi_track(const __grid_constant__ McConst<T> C, const __grid_constant__ DevShi<T> sh, ShiEv* __restrict__ evs,
+                int64_t cap_ev, Ctrs* ctr, int nit, int it_base, unsigned long long* ev_inst, int G) {
+    const int lane = (int)(threadIdx.x & 31), j = lane & (G - 1);
+    const int local = (int)(((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * (32 / G)) + lane / G;
+    const bool valid = local < nit;
+    const bool leader = valid && j == 0;
+    const int it = it_base + (valid ? local : 0);   // the iteration's index in the batch
     unsigned err = 0;
     unsigned long long nev = 0;
     const uint64_t pid = shi_pid(C.it0 + it);
@@ -1119,78 +1145,114 @@ __global__ void __launch_bounds__(64) k_shi_track(const __grid_constant__ McCons
         const double dt = flight_time(E, L);
         tn = dt >= 0.0 ? t0 + dt : 1.0e25;
     }
+    // lane j's Philox block of collision base + j (words 0-2: the shell, the
+    // transfer and the free path of that collision, as EvStream draws them)
+    const uint32_t c0 = (uint32_t)pid, c1 = (uint32_t)(pid >> 32);
+    uint32_t pw0 = 0, pw1 = 0, pw2 = 0, base = 0;
+    bool have = false;
     uint32_t ord = 0;
     int64_t slot = 0, slot_end = 0;
-    while (tn < (double)C.Tim) {
-        if (ord >= (1u << 26)) { err |= TREKIS_ERR_NAN; break; }   // no SHI track has this many collisions
-        EvStream<T> s(C.rk, pid, ord);
+    const int nsh = C.nsh;
+    bool run = valid && tn < (double)C.Tim;   // the same on every lane of a group
+    while (__any_sync(kFullWarp, run)) {
+        if (run && ord >= (1u << 26)) { err |= TREKIS_ERR_NAN; run = false; }   // no SHI track has this many collisions
+        if (run && (!have || ord - base >= (uint32_t)G)) {
+            base = ord;
+            have = true;
+            uint32_t w[4];
+            philox4x32_rk(c0, c1, base + (uint32_t)j, 0u, C.rk, w);
+            pw0 = w[0]; pw1 = w[1]; pw2 = w[2];
+        }
+        const int src = (int)((ord - base) & (uint32_t)(G - 1));
+        const uint32_t w0 = __shfl_sync(kFullWarp, pw0, src, G), w1 = __shfl_sync(kFullWarp, pw1, src, G),
+                       w2 = __shfl_sync(kFullWarp, pw2, src, G);
         const T Et = (T)E, lx = m_log(Et);
         const int nb = walk_monoton(sh.sE, sh.nS, Et, nb_last);   // the ion slows by little per collision
         nb_last = nb;
-        // Which_shell
-        int k = C.nsh - 1;
-        {
-            T inv[MAXSH], tot = T(0);
-            for (int q = 0; q < C.nsh; ++q) {
-                inv[q] = T(1) / shi_mfp_shell(sh, sh.sL + (size_t)q * sh.nS, sh.lL + (size_t)q * sh.nS, nb, Et, lx);
-                tot += inv[q];
+        // Which_shell: lane j has shells j, j + G, ...; sums in shell order
+        T mine[kShiPerLane];
+#pragma unroll
+        for (int r = 0; r < kShiPerLane; ++r) {
+            mine[r] = T(0);
+            if (r * G >= nsh) break;   // the same on every lane
+            const int q = r * G + j;
+            if (q < nsh) mine[r] = T(1) / shi_mfp_shell(sh, sh.sL + (size_t)q * sh.nS, sh.lL + (size_t)q * sh.nS, nb, Et, lx);
+        }
+        T tot = T(0);
+#pragma unroll
+        for (int r = 0; r < kShiPerLane; ++r) {
+            if (r * G >= nsh) break;
+            const int m = nsh - r * G < G ? nsh - r * G : G;
+            for (int jj = 0; jj < m; ++jj) tot += __shfl_sync(kFullWarp, mine[r], jj, G);
+        }
+        tot = Uni<T>::of(w0) * tot;
+        int k = -1;
+        T sum = T(0);
+#pragma unroll
+        for (int r = 0; r < kShiPerLane; ++r) {
+            if (r * G >= nsh) break;
+            const int m = nsh - r * G < G ? nsh - r * G : G;
+            for (int jj = 0; jj < m; ++jj) {
+                sum += __shfl_sync(kFullWarp, mine[r], jj, G);
+                if (k < 0 && sum >= tot) k = r * G + jj;
             }
-            tot = s.next() * tot;
-            T sum = T(0);
-            for (int q = 0; q < C.nsh; ++q) { sum += inv[q]; if (sum >= tot) { k = q; break; } }
         }
-        // SHI_energy_transfer (MC:1719-1780): inverse of a cumulative transfer row
-        double dE;
-        {
-            T RN;
-            double RNd;
-            s.next2(RN, RNd);
-            dE = shi_draw(C, sh, k, E, RN, RNd);
-        }
-        // next flight with the energy before the loss
-        double Lnew = (double)shi_path(sh, nb, Et, lx);
-        Lnew = -Lnew * (double)m_log(s.next());
-        Z = Z + L;
-        E -= dE; t0 = tn; L = Lnew;
-        const double dt = flight_time(E, L);
-        tn = dt >= 0.0 ? t0 + dt : 1.0e25;
-        // Equilibrium_charge_SHI (CS:2641-2680)
-        double Zeff;
-        if (F32 && C.ion_kind_zeff == 0) {
-            const T vp = E > 0.0 ? m_sqrt((T)E * vfac_t) : T(0);
-            Zeff = (double)(T(C.ion_Z) * (T(1) - m_exp(-(vp * zfac))));
-        } else {
-            const double vp = E > 0.0 ? sqrt(2.0 * E * kE / (C.ion_mass_p * kMp)) : 0.0;
-            const double Zp = C.ion_Z;
-            if (C.ion_kind_zeff == 0) Zeff = Zp * (1.0 - exp(-(vp * 125.0 / kC / (double)sh.pow_zp)));
-            else {
-                const double v0 = sqrt(2.0 * kRy * kE / kMe);
-                switch (C.ion_kind_zeff) {
-                case 1: Zeff = Zp * (1.0 - exp(-(vp / v0 / (double)sh.pow_zp))); break;
-                case 2: Zeff = Zp * pow(1.0 + pow(vp / (pow(Zp, 0.45) * v0 * 4.0 / 3.0), -1.0 / 0.6), -0.6); break;
-                case 3: {
-                    double Zt = C.Zt, c1 = 1.0 - 0.26 * exp(-Zt / 11.0 - (Zt - Zp) * (Zt - Zp) / 9.0);
-                    double vpvo = pow(Zp, -0.543) * vp / v0, c2 = 1.0 + 0.03 * vpvo * log(Zt);
-                    double x = c1 * pow(vpvo / c2 / 1.54, 1.0 + 1.83 / Zp), x2 = x * x, x4 = x2 * x2;
-                    Zeff = Zp * (8.29 * x + x4) / (0.06 / x + 4.0 + 7.4 * x + x4);
-                } break;
-                default: Zeff = C.ion_fixed_zeff;
+        if (k < 0) k = nsh - 1;
+        // record slots: the leader reserves, the group learns the first
+        const bool need = run && slot == slot_end;
+        long long first = 0;
+        if (need && leader) first = (long long)atomicAdd(&ctr->shi_slots, (unsigned long long)kSlotChunk);
+        first = __shfl_sync(kFullWarp, first, 0, G);
+        if (need) { slot = (int64_t)first; slot_end = slot + kSlotChunk; }
+        if (run && leader) {
+            // SHI_energy_transfer (MC:1719-1780): inverse of a cumulative transfer row
+            const double dE = shi_draw(C, sh, k, E, Uni<T>::of(w1), Uni<double>::of(w1));
+            // next flight with the energy before the loss
+            double Lnew = (double)shi_path(sh, nb, Et, lx);
+            Lnew = -Lnew * (double)m_log(Uni<T>::of(w2));
+            Z = Z + L;
+            E -= dE; t0 = tn; L = Lnew;
+            const double dt = flight_time(E, L);
+            tn = dt >= 0.0 ? t0 + dt : 1.0e25;
+            // Equilibrium_charge_SHI (CS:2641-2680)
+            double Zeff;
+            if (F32 && C.ion_kind_zeff == 0) {
+                const T vp = E > 0.0 ? m_sqrt((T)E * vfac_t) : T(0);
+                Zeff = (double)(T(C.ion_Z) * (T(1) - m_exp(-(vp * zfac))));
+            } else {
+                const double vp = E > 0.0 ? sqrt(2.0 * E * kE / (C.ion_mass_p * kMp)) : 0.0;
+                const double Zp = C.ion_Z;
+                if (C.ion_kind_zeff == 0) Zeff = Zp * (1.0 - exp(-(vp * 125.0 / kC / (double)sh.pow_zp)));
+                else {
+                    const double v0 = sqrt(2.0 * kRy * kE / kMe);
+                    switch (C.ion_kind_zeff) {
+                    case 1: Zeff = Zp * (1.0 - exp(-(vp / v0 / (double)sh.pow_zp))); break;
+                    case 2: Zeff = Zp * pow(1.0 + pow(vp / (pow(Zp, 0.45) * v0 * 4.0 / 3.0), -1.0 / 0.6), -0.6); break;
+                    case 3: {
+                        double Zt = C.Zt, c1z = 1.0 - 0.26 * exp(-Zt / 11.0 - (Zt - Zp) * (Zt - Zp) / 9.0);
+                        double vpvo = pow(Zp, -0.543) * vp / v0, c2z = 1.0 + 0.03 * vpvo * log(Zt);
+                        double x = c1z * pow(vpvo / c2z / 1.54, 1.0 + 1.83 / Zp), x2 = x * x, x4 = x2 * x2;
+                        Zeff = Zp * (8.29 * x + x4) / (0.06 / x + 4.0 + 7.4 * x + x4);
+                    } break;
+                    default: Zeff = C.ion_fixed_zeff;
+                    }
                 }
             }
+            if (slot < cap_ev) {
+                ShiEv ev;
+                ev.E = E; ev.Zeff = Zeff; ev.t0 = t0; ev.Z = Z; ev.dE = dE; ev.k = k; ev.ord = ord; ev.it = it; ev.pad = 0;
+                evs[slot] = ev;
+            } else atomicExch(&ctr->overflow, 1);
+            ++nev;
+            if (Z >= C.Layer) tn = 1.0e16;
         }
-        if (slot == slot_end) {
-            slot = (int64_t)atomicAdd(&ctr->shi_slots, (unsigned long long)kSlotChunk);
-            slot_end = slot + kSlotChunk;
-        }
-        if (slot < cap_ev) {
-            ShiEv ev;
-            ev.E = E; ev.Zeff = Zeff; ev.t0 = t0; ev.Z = Z; ev.dE = dE; ev.k = k; ev.ord = ord; ev.it = it; ev.pad = 0;
-            evs[slot] = ev;
-        } else atomicExch(&ctr->overflow, 1);
-        ++slot;
-        ++ord; ++nev;
-        if (Z >= C.Layer) tn = 1.0e16;
+        // the leader's new energy and next time for its group
+        E = __shfl_sync(kFullWarp, E, 0, G);
+        tn = __shfl_sync(kFullWarp, tn, 0, G);
+        if (run) { ++slot; ++ord; }
+        run = run && tn < (double)C.Tim;
     }
+    if (!leader) return;
     for (; slot < slot_end; ++slot)   // mark the rest of the last chunk unused
         if (slot < cap_ev) evs[slot].it = -1;
     if (nev) atomicAdd(ev_inst ? ev_inst : &ctr->ev[0], nev);
@@ -1856,7 +1918,10 @@ template <class T>
 void launch_shi(const McConst<T>& C, const DevShi<T>& sh, void* evs, int64_t cap_ev, Ctrs* ctr, int nit,
                 cudaStream_t s, int it_base, unsigned long long* ev_inst) {
     if (nit <= 0) return;
-    k_shi_track<T><<<(nit + 63) / 64, 64, 0, s>>>(C, sh, (ShiEv*)evs, cap_ev, ctr, nit, it_base, ev_inst);
+    const int G = shi_group_lanes(nit, C.nsh);
+    const int64_t warps = ((int64_t)nit * G + 31) / 32;
+    k_shi_track<T><<<(unsigned)((warps + 3) / 4), 128, 0, s>>>(C, sh, (ShiEv*)evs, cap_ev, ctr, nit, it_base,
+                                                               ev_inst, G);
 }
 template <class T>
 void launch_pairs(const McConst<T>& C, const DevTabs<T>& tb, const void* evs, int64_t n_ev, PQ<T> qe, PQ<T> qhvb,
