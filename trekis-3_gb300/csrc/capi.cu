@@ -815,7 +815,7 @@ static int run_mc(trekis_tables* t, const trekis_run_cfg& cfg, int Nt, int Nat, 
             if (steps + bsteps > (1ull << 24)) { set_error("wavefront did not drain"); return TREKIS_ETIMEOUT; }
             std::swap(in, ot);
             int n_in[4] = {hc.n_out[Q_E], hc.n_out[Q_HVB], hc.n_out[Q_HDEEP], hc.n_out[Q_P]};
-            CK(cudaMemsetAsync(dctr, 0, NQ * sizeof(int), strm));
+            CK(cudaMemsetAsync(dctr, 0, (NQ + 2) * sizeof(int), strm));   // queue counts and hot-kernel cursors
             CK(cudaEventRecord(ws->s0, strm));
             launch_step<T>(C, tb, *in, n_in, *ot, ws->e_inel, ws->h_inel, tal, dctr, K, bs, rare_blocks, strm,
                            ws->guess, pp, &ws->fk);

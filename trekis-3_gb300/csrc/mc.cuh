@@ -166,6 +166,7 @@ enum { Q_E = 0, Q_HVB = 1, Q_HDEEP = 2, Q_P = 3, Q_EINEL = 4, Q_HINEL = 5, NQ = 
 
 struct Ctrs {
     int n_out[NQ];                // appended particles per queue
+    int hot_next[2];              // next input particle of the refilling hot kernels (electrons, holes)
     int overflow;
     unsigned int err_bits;
     int first_bad_it;

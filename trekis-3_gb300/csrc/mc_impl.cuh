@@ -1684,12 +1684,119 @@ __device__ void photon_event(const McConst<T>& C, const DevTabs<T>& tb, const TL
 // iterate together (a lane whose particle is done idles) so that segments
 // reaching a grid time can be parked in the warp's ring and tallied 32 at a
 // time; the tallies are integer sums, so the order does not matter.
+// The hot kernel's loop for the phonon-CDF and DSF elastic models.  There a
+// particle's next event ionises far more often than with Mott scattering, so
+// particles leave the loop after a few collisions and their lanes would idle
+// until the warp's last particle is done.  Here a lane whose particle is done
+// takes the next particle of the input queue (one cursor per kind, one atomic
+// per warp and refill), so the lanes stay busy.  Every particle still gets at
+// most K collisions in this step, and the tallies are integer sums, so the
+// results do not change; only the order of the output queues does.
+template <class T, bool IS_E, int ELM, class TL>
+__device__ __forceinline__ void hot_refill(const McConst<T>& C, const DevTabs<T>& tb, const PQ<T>& in, int n,
+                                           const Out<T>& o, const PQ<T>& side, const TL& tal, int K,
+                                           SegRing<T>& ring) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int* cursor = &o.ctr->hot_next[IS_E ? 0 : 1];
+    P<T> p;
+    bool has = false, diverted = false, drained = false;
+    int evp = 0;
+    unsigned err = 0;
+    unsigned long long nev[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    LatAcc lat;
+    MfpCache<T> mc;
+    const T co = C.cut_off > T(0) ? C.cut_off : T(0);
+    int head = 0, cnt = 0;   // the warp's ring: parked segments at head..head+cnt-1
+    for (;;) {
+        const unsigned need = __ballot_sync(0xffffffffu, !has);
+        if (need && !drained) {   // the lanes without a particle take the next ones
+            const int leader = __ffs(need) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(cursor, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!has) {
+                const int i = base + __popc(need & ((1u << lane) - 1u));
+                if (i < n) {
+                    load(in, i, p);
+                    p.ti = tbin(C, p.tn);
+                    has = true; diverted = false; evp = 0;
+                }
+            }
+            if (base + __popc(need) >= n) drained = true;   // the same on every lane
+        }
+        if (!__any_sync(0xffffffffu, has)) break;
+        bool pend = false, fin = false;
+        int ia = 0, ib = -1;
+        if (has) {
+            if (evp < K && p.tn < C.Tim) {
+                bool done;
+                if constexpr (IS_E) done = electron_event<T, false, true, ELM + 1>(C, tb, tal, o, p, err, lat, nev, mc);
+                else done = hole_event<T, false, true, ELM + 1>(C, tb, tal, o, p, err, lat, nev, mc);
+                ++evp;
+                if (!done) { diverted = true; fin = true; }
+                else {
+                    ia = p.ti;
+                    p.ti = seg_span(C, p.t0, p.tn, ib);
+                    pend = ib >= ia;
+                    fin = !(p.tn < C.Tim) || evp >= K;
+                }
+            } else fin = true;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, pend);
+        if (m) {
+            if (pend) {
+                const int slot = (head + cnt + __popc(m & ((1u << lane) - 1u))) & (kSegQ - 1);
+                if constexpr (IS_E) {
+                    const bool mv = p.E > co;
+                    park_seg(ring, w, slot, p.E, T(0), p.t0, p.X, p.Y, mv ? p.th : T(0), mv ? p.ph : T(0),
+                             mv ? v_el(p.E) : T(0), ia, ib, p.it, 0, true);
+                } else {
+                    const bool mv = (p.M < T(1.0e3)) && (p.Ek > co);
+                    park_seg(ring, w, slot, p.E, p.Ek, p.t0, p.X, p.Y, p.th, p.ph, mv ? v_hole(p.Ek, p.M) : T(0),
+                             ia, ib, p.it, p.sh, mv);
+                }
+            }
+            cnt += __popc(m);
+            if (cnt >= 32) {
+                __syncwarp();
+                drain_segs(C, tal, ring, IS_E ? 0 : 1, w, lane, head, 32);
+                __syncwarp();
+                head = (head + 32) & (kSegQ - 1);
+                cnt -= 32;
+            }
+        }
+        if (fin) {   // the particle leaves this step: its deposits, its queue and (several instances) its counts
+            lat.flush(tal, p.it);
+            lat.cell = -1;
+            if (diverted) append(side, &o.ctr->n_out[IS_E ? Q_EINEL : Q_HINEL], &o.ctr->overflow, p);
+            else push(C, tal, o, IS_E ? 0 : 1, p);
+            if constexpr (std::is_same<TL, TalMulti>::value) {
+                unsigned long long& ne = nev[IS_E ? 2 : 3];
+                if (ne) atomicAdd(tal.ev_inst + 9 * inst_index(tal, p.it) + (IS_E ? 2 : 3), ne);
+                ne = 0;
+            }
+            has = false;
+        }
+    }
+    __syncwarp();
+    drain_segs(C, tal, ring, IS_E ? 0 : 1, w, lane, head, cnt);
+    if constexpr (!std::is_same<TL, TalMulti>::value) {
+        const unsigned long long ne = IS_E ? nev[2] : nev[3];
+        if (ne) atomicAdd(&o.ctr->ev[IS_E ? 2 : 3], ne);
+    }
+    if (err) atomicOr(&o.ctr->err_bits, err);
+}
+
 template <class T, bool IS_E, int ELM, class TL>
 __global__ void __launch_bounds__(256, 4) k_hot(const __grid_constant__ McConst<T> C,
                                              const __grid_constant__ DevTabs<T> tb, const __grid_constant__ PQ<T> in,
                                              int n, const __grid_constant__ Out<T> o, const __grid_constant__ PQ<T> side,
                                              const __grid_constant__ TL tal, int K) {
     __shared__ SegRing<T> ring;
+    if constexpr (ELM != 0) {   // phonon-CDF and DSF elastic models: lanes refill from the queue
+        hot_refill<T, IS_E, ELM, TL>(C, tb, in, n, o, side, tal, K, ring);
+        return;
+    }
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (blockIdx.x * blockDim.x + (threadIdx.x & ~31) >= n) return;   // whole warp past the end
@@ -1948,14 +2055,18 @@ static void launch_step_tl(const McConst<T>& C, const DevTabs<T>& tb, const QSet
         cudaStreamWaitEvent(fk->s2, fk->fork, 0);
     }
     // one hot kernel per particle kind and elastic model
+    // the refilling kernels (elastic models 1, 2) need no more blocks than fit at once
+    const unsigned g_cap = 152u * 4u * 256u / (unsigned)bs;
     if (n_in[Q_E] > 0) {
-        const unsigned g = (n_in[Q_E] + bs - 1) / bs;
+        unsigned g = (n_in[Q_E] + bs - 1) / bs;
+        if (C.elast_model != 0 && g > g_cap) g = g_cap;
         if (C.elast_model == 1) k_hot<T, true, 1, TL><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
         else if (C.elast_model == 2) k_hot<T, true, 2, TL><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
         else k_hot<T, true, 0, TL><<<g, bs, 0, s>>>(C, tb, in.q[Q_E], n_in[Q_E], o, e_inel, tal, K);
     }
     if (n_in[Q_HVB] > 0) {
-        const unsigned g = (n_in[Q_HVB] + bs - 1) / bs;
+        unsigned g = (n_in[Q_HVB] + bs - 1) / bs;
+        if (C.elast_model != 0 && g > g_cap) g = g_cap;
         cudaStream_t sh = two ? fk->s2 : s;
         if (C.elast_model == 1)
             k_hot<T, false, 1, TH><<<g, bs, 0, sh>>>(C, tb, in.q[Q_HVB], n_in[Q_HVB], o, h_inel, th, K);

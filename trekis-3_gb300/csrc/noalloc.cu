@@ -328,7 +328,7 @@ int run_noalloc(const trekis_tables* t, const trekis_run_cfg& cfg, int Nt, const
             if (steps + bsteps > (1ull << 24)) { set_error("wavefront did not drain"); return TREKIS_ETIMEOUT; }
             std::swap(in, ot);
             const int n_in[4] = {hc.n_out[Q_E], hc.n_out[Q_HVB], hc.n_out[Q_HDEEP], hc.n_out[Q_P]};
-            NA_CK(cudaMemsetAsync(L.ctr, 0, NQ * sizeof(int), strm));
+            NA_CK(cudaMemsetAsync(L.ctr, 0, (NQ + 2) * sizeof(int), strm));   // queue counts and hot-kernel cursors
             launch_step<T>(C, tb, *in, n_in, *ot, L.e_inel, L.h_inel, L.tal, L.ctr, K, bs, rare_blocks, strm);
             bl += 1 + (n_in[Q_E] > 0) + (n_in[Q_HVB] > 0); ++bsteps;
             NA_CK(cudaGetLastError());
