@@ -288,7 +288,7 @@ def test_fp32_bias_against_fp64_same_streams(gpu_lib, case):
 def test_queue_overflow_recovers(small0):
     w, t, _o = small0
     ref, _ = api.mc_run(t, api.RunOptions(seed=6, iterations_per_batch=1))
-    # capacity below one batch: the driver shrinks the batch and retries
+    # capacity below one batch: the host loop shrinks the batch and retries
     g, st = api.mc_run(t, api.RunOptions(seed=6, iterations_per_batch=6, queue_capacity=4000))
     for k in g.a:
         assert np.allclose(g[k], ref[k], rtol=1e-12, atol=0), k
