@@ -671,3 +671,42 @@ def test_run_from_reference_input_files(tmp_path):
     o.mc_run(cfg, tal, st, nthreads=2)
     assert st.n_shi > 0 and st.n_events > st.n_shi and st.error_bits == 0
     assert api.ion_struct(w).Kind_Zeff == 4 and api.ion_struct(w).fixed_Zeff == 54.0
+
+
+def test_emission_from_reference_input_files(tmp_path):
+    """The work-function line of INPUT_PARAMETERS.txt turns surface emission
+    on (Read_input_file keeps a positive work function only with a positive
+    barrier length and height), and the oracle then tallies the emitted
+    electrons of the run."""
+    import oracle_py
+    (tmp_path / "cdf").mkdir()
+    (tmp_path / "dos").mkdir()
+    (tmp_path / "cdf" / "oxide.cdf").write_text(_CDF_NUMERIC)
+    e, d = material.parabolic_dos_file(12.0)
+    (tmp_path / "dos" / "Oxide.dos").write_text("".join(f"{x:.6f} {y:.6f}\n" for x, y in zip(e, d)))
+    read = lambda text: configs.workload_from_input(_write(tmp_path, text), tmp_path / "cdf", tmp_path / "dos")
+    off = read(_INPUT.replace("-1.0 10.0d0  6.18d0", "4.5 -10.0d0  6.18d0"))
+    assert off.material.work_function == 0.0          # no barrier length: no emission
+    w = read(_INPUT.replace("-1.0 10.0d0  6.18d0", "4.5 10.0d0  6.18d0"))
+    m = w.material
+    assert (m.work_function, m.bar_length, m.bar_height) == (4.5, 10.0, 6.18)
+    m.atoms[1].shells[0].KOCS = m.atoms[1].shells[0].KOCS_SHI = 1   # the file's BEB shell, made CDF for the oracle
+    m.atoms[1].shells[0].E0, m.atoms[1].shells[0].A, m.atoms[1].shells[0].Gamma = [548.0], [300.0], [548.0]
+    w.dt = 1.0
+    o = oracle_py.OracleTables(m.to_c(), api.ion_struct(w),
+                               abi.TableCfg(build_shi=1, build_photon=0, shi_E_window_lo=w.ion_E * 0.5,
+                                            shi_E_window_hi=w.ion_E * 1.01), nthreads=4)
+    tal = api.new_tallies(w, spectra=True)
+    cfg, _R = api.run_cfg(w, api.RunOptions(precision=1, seed=2))
+    st = abi.Status.fresh()
+    o.mc_run(cfg, tal, st, nthreads=2)
+    assert st.error_bits == 0
+    ne = tal["Out_Ne_Em"]
+    assert ne[-1] > 0 and np.all(np.diff(ne) >= 0) and np.all(tal["Out_E_Em"] >= 0)
+    assert tal["Out_Ee_vs_E_Em"].any()
+
+
+def _write(d, text):
+    p = d / "INPUT_PARAMETERS.txt"
+    p.write_text(text)
+    return p
