@@ -9,7 +9,8 @@ normalised per iteration (Out_Ee_vs_E_Em, :1100-1109).
 
 * FP64 mode on identical tables and Philox streams: every tally, the
   emission tallies and the spectra included, equals the oracle's (to the
-  2^-24 eV fixed-point resolution of the energy sums).
+  2^-24 eV fixed-point resolution of the energy sums), with Mott and with
+  phonon-CDF elastic scattering.
 * Emission tallies go through the exact integer sums: a split of the
   iterations into exact words and the scheduling knobs change no bit.
 * FP32 mode: the emitted electrons per iteration and their energy agree
@@ -55,9 +56,19 @@ def small_em(gpu_lib):
     return w, t, _oracle_on(t, w)
 
 
+@pytest.fixture(scope="module")
+def small_em4(gpu_lib):
+    # SiO2-like target with phonon-CDF elastic scattering (its hot kernels refill idle lanes)
+    w = configs.small(configs.cfg4, NMC=4, Tim=20.0, ion_E=50e6)
+    w.material.work_function = WORK_FUNCTION
+    t = api.Tables(w, lib=gpu_lib)
+    return w, t, _oracle_on(t, w)
+
+
 @pytest.mark.gpu
-def test_fp64_emission_matches_oracle(small_em):
-    w, t, o = small_em
+@pytest.mark.parametrize("case", ["small_em", "small_em4"])
+def test_fp64_emission_matches_oracle(case, request):
+    w, t, o = request.getfixturevalue(case)
     opt = api.RunOptions(precision=1, seed=17)
     g, sg = api.mc_run(t, opt, tallies=api.new_tallies(w, spectra=True))
     r, sr = _oracle_run(o, w, opt, spectra=True)
